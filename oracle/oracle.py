@@ -1,0 +1,596 @@
+"""CPU oracle for the HelmholtzBEM assembly-and-resonance path.
+
+TEST INFRASTRUCTURE ONLY.  Only the tests, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` import this module, and only as the checker
+or as the timed CPU baseline; the product never routes through it.
+
+Pieces and the reference code each one restates:
+
+* geometry: ``ParametrizedCircularArc::split`` and ``ParametrizedLine::split``
+  (source/parametrizations/parametrized_circular_arc.cpp:141-152,
+  parametrized_line.cpp:112-131), ``scatterer::make_N_polygonal_panels``
+  (source/utilities/scatterer.cpp:114-156);
+* Galerkin assembly, Hankel functions and the mass matrix: the C++ restatement
+  in ``hbem_oracle.cpp`` (loaded here with ctypes);
+* ``SolutionsOperator`` T(k) blocks and projection
+  (source/utilities/gen_sol_op.cpp:23-117, derivative variants :119-196 with
+  the derivative blocks written where they belong -- the reference writes them
+  all into T);
+* ``direct::sv*`` dense singular values and k-derivatives
+  (source/utilities/singular_values.cpp:7-147) by LAPACK SVD plus first- and
+  second-order perturbation of the Hermitian Wielandt matrix;
+* ``randomized_svd::sv / sv_der / sv_der2`` (source/utilities/randsvd.cpp:99-216);
+* ``rtsafe``, ``zbrent`` (source/utilities/find_roots.cpp:19-217) and Brent's
+  reverse-communication minimiser (find_roots.cpp:1003-1184), restated from
+  Brent (1973) and Press et al.'s published descriptions;
+* the plain sweep / bracket / validate / quartic / Newton pattern of
+  examples/roots_newton_polygon_rsvd.cpp:172-265.
+
+Parity status: Hankel values pinned by the reference's known answers
+(test/googletest/solutions_test.cpp:55-72) and by mpmath/scipy; matrices,
+singular values and roots are NOT pinned by reference fixtures (none exist for
+this path in the reference tree) -- parity unpinned at that level, checked
+analytically instead.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import subprocess
+
+import numpy as np
+import scipy.linalg as sla
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libhbem_oracle.so")
+_lib = None
+
+LAYER_DOUBLE, LAYER_SINGLE, LAYER_HYPERSINGULAR, LAYER_ALL = 1, 2, 4, 7
+
+
+def build():
+    """Compile the C++ restatement (gcc + OpenMP) into oracle/_build/."""
+    subprocess.check_call(["make", "-s", "-C", _HERE])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int)
+        L.hbo_builder_create.restype = ctypes.c_void_p
+        L.hbo_builder_create.argtypes = [ctypes.c_int, ip, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.hbo_builder_destroy.argtypes = [ctypes.c_void_p]
+        L.hbo_builder_set_quirks.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.hbo_builder_is_adjacent.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ip]
+        L.hbo_assemble.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                   ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_int, dp, ctypes.c_int]
+        L.hbo_mass.argtypes = [ctypes.c_void_p, dp]
+        L.hbo_hankel_real.argtypes = [ctypes.c_int, dp, dp, dp]
+        L.hbo_hankel_cplx.argtypes = [ctypes.c_int, dp, dp, dp]
+        L.hbo_gauss.argtypes = [ctypes.c_int, dp, dp]
+        L.hbo_cgauss.argtypes = [ctypes.c_int, dp, dp]
+        L.hbo_cgauss.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+# ----------------------------------------------------------------- quadrature / Hankel
+
+def gauss(n):
+    x = np.zeros(n); w = np.zeros(n)
+    lib().hbo_gauss(n, _dp(x), _dp(w))
+    return x, w
+
+
+def cgauss(n):
+    m = n * (n + 1) // 2 - 1
+    x = np.zeros(m); w = np.zeros(m)
+    lib().hbo_cgauss(n, _dp(x), _dp(w))
+    return x, w
+
+
+def hankel01(x):
+    """H0^(1), H1^(1): real path for real positive input, complex path otherwise."""
+    x = np.asarray(x)
+    if np.isrealobj(x):
+        xr = np.ascontiguousarray(x, dtype=np.float64).ravel()
+        h0 = np.zeros(xr.size, np.complex128); h1 = np.zeros(xr.size, np.complex128)
+        lib().hbo_hankel_real(xr.size, _dp(xr), _dp(h0.view(np.float64)), _dp(h1.view(np.float64)))
+    else:
+        xr = np.ascontiguousarray(x, dtype=np.complex128).ravel()
+        h0 = np.zeros(xr.size, np.complex128); h1 = np.zeros(xr.size, np.complex128)
+        lib().hbo_hankel_cplx(xr.size, _dp(xr.view(np.float64)), _dp(h0.view(np.float64)),
+                              _dp(h1.view(np.float64)))
+    return h0.reshape(x.shape), h1.reshape(x.shape)
+
+
+# ----------------------------------------------------------------- geometry
+
+KIND_LINE, KIND_ARC = 0, 1
+
+
+def circle_panels(radius, n, center=(0.0, 0.0)):
+    """ParametrizedCircularArc(center, r, 0, 2 pi).split(n)."""
+    kinds = np.full(n, KIND_ARC, np.int32)
+    par = np.zeros((n, 5))
+    phi_s, phi_e = 0.0, 2 * math.pi
+    for i in range(n):
+        a = phi_s + i * (phi_e - phi_s) / n
+        b = phi_s + (i + 1) * (phi_e - phi_s) / n
+        if i == n - 1:
+            b = phi_e
+        par[i] = (center[0], center[1], radius, a, b)
+    return kinds, par
+
+
+def _line_split(p, q, m):
+    """ParametrizedLine(p, q).split(m): endpoints via the [-1,1] map."""
+    out = []
+    x1, y1 = p
+    x2, y2 = q
+    for i in range(m):
+        t1 = -1.0 + i * 2.0 / m
+        t2 = -1.0 + (i + 1) * 2.0 / m
+        if i == m - 1:
+            t2 = 1.0
+        f = ((t1 * (x2 - x1) + (x2 + x1)) * 0.5, (t1 * (y2 - y1) + (y2 + y1)) * 0.5)
+        s = ((t2 * (x2 - x1) + (x2 + x1)) * 0.5, (t2 * (y2 - y1) + (y2 + y1)) * 0.5)
+        out.append((f[0], f[1], s[0], s[1], 0.0))
+    return out
+
+
+def polygon_panels(x, y, N):
+    """scatterer::make_N_polygonal_panels: edge panel counts proportional to length,
+    adjusted one panel at a time to the variance-minimising edge until they sum to N."""
+    x = np.asarray(x, float); y = np.asarray(y, float)
+    n = x.size
+    d = np.array([math.hypot(x[(i + 1) % n] - x[i], y[(i + 1) % n] - y[i]) for i in range(n)])
+    length = float(np.sum(d))
+    alpha = N / length
+    m = np.array([float(np.round(alpha * di)) for di in d])
+    cs = int(np.sum(m))
+    while cs != N:
+        kstep = -1 if cs > N else 1
+        best, i_min = np.inf, 0
+        for i in range(n):
+            m[i] += kstep
+            a = d / m
+            var = float(np.mean((a - np.mean(a)) ** 2))
+            if var < best:
+                best, i_min = var, i
+            m[i] -= kstep
+        m[i_min] += kstep
+        cs += kstep
+    panels = []
+    for i in range(n):
+        panels += _line_split((x[i], y[i]), (x[(i + 1) % n], y[(i + 1) % n]), int(m[i]))
+    kinds = np.full(len(panels), KIND_LINE, np.int32)
+    return kinds, np.array(panels)
+
+
+def star_polygon(nvert, seed, amp=0.3):
+    """Random star-shaped polygon: r_j = 1 + amp*u_j, u_j ~ U[-1,1], equispaced angles."""
+    rng = np.random.default_rng(seed)
+    u = rng.uniform(-1.0, 1.0, nvert)
+    th = 2 * np.pi * np.arange(nvert) / nvert
+    r = 1.0 + amp * u
+    return r * np.cos(th), r * np.sin(th)
+
+
+def fourier_curve_panels(a, b, N):
+    """Fourier-sum curve r(t) = 1 + sum a_m cos mt + b_m sin mt sampled at N equispaced
+    angles and joined by line panels (the reference's Fourier-sum panel class is
+    incomplete, so the curve is represented by its inscribed polygon)."""
+    th = 2 * np.pi * np.arange(N) / N
+    m = np.arange(1, len(a) + 1)
+    r = 1.0 + np.cos(np.outer(th, m)) @ np.asarray(a) + np.sin(np.outer(th, m)) @ np.asarray(b)
+    xs, ys = r * np.cos(th), r * np.sin(th)
+    panels = [(xs[i], ys[i], xs[(i + 1) % N], ys[(i + 1) % N], 0.0) for i in range(N)]
+    return np.full(N, KIND_LINE, np.int32), np.array(panels)
+
+
+def random_fourier_coeffs(seed, modes=8, scale=0.05, rmin=0.3):
+    rng = np.random.default_rng(seed)
+    while True:
+        sd = scale / np.arange(1, modes + 1)
+        a = rng.normal(0.0, sd); b = rng.normal(0.0, sd)
+        th = np.linspace(0, 2 * np.pi, 2048, endpoint=False)
+        m = np.arange(1, modes + 1)
+        r = 1 + np.cos(np.outer(th, m)) @ a + np.sin(np.outer(th, m)) @ b
+        if r.min() >= rmin:
+            return a, b
+
+
+# ----------------------------------------------------------------- builder
+
+class Builder:
+    """BuilderData + GalerkinBuilder restated (q = 2 for continuous P1, 1 for P0)."""
+
+    def __init__(self, kinds, params, order, qtest=2, qtrial=2):
+        self.kinds = np.ascontiguousarray(kinds, np.int32)
+        self.params = np.ascontiguousarray(params, np.float64)
+        self.n = int(self.kinds.size)
+        self.order = order
+        self.qtest, self.qtrial = qtest, qtrial
+        self._h = lib().hbo_builder_create(self.n, self.kinds.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                           _dp(self.params), order, qtest, qtrial)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.hbo_builder_destroy(self._h)
+            self._h = None
+
+    def set_quirks(self, sl_coinc=0):
+        lib().hbo_builder_set_quirks(self._h, int(sl_coinc))
+
+    def is_adjacent(self, i, j):
+        s = ctypes.c_int(0)
+        r = lib().hbo_builder_is_adjacent(self._h, i, j, ctypes.byref(s))
+        return bool(r), bool(s.value)
+
+    def assemble(self, k, c, layers=LAYER_ALL, d=0, row=0, col=0, rows=0, cols=0, threads=None):
+        """Returns {'K': [K, K', K''], 'W': [...], 'V': [...]} (only requested layers)."""
+        if threads is None:
+            threads = os.cpu_count() or 1
+        k = complex(k)
+        nr = rows or self.n
+        ncl = cols or self.n
+        shapes = {}
+        if layers & LAYER_DOUBLE:
+            shapes["K"] = (nr, ncl)
+        if layers & LAYER_HYPERSINGULAR:
+            shapes["W"] = (nr, ncl)
+        if layers & LAYER_SINGLE:
+            shapes["V"] = (nr, ncl)
+        total = sum(a * b for a, b in shapes.values()) * (d + 1)
+        buf = np.zeros(total, np.complex128)
+        rc = lib().hbo_assemble(self._h, k.real, k.imag, float(c), int(layers), int(d), row, col, rows, cols,
+                                _dp(buf.view(np.float64)), int(threads))
+        if rc != 0:
+            raise RuntimeError("oracle assembly rejected its arguments")
+        out, off = {}, 0
+        for name in ("K", "W", "V"):
+            if name not in shapes:
+                continue
+            r_, c_ = shapes[name]
+            mats = []
+            for _ in range(d + 1):
+                mats.append(buf[off:off + r_ * c_].reshape(c_, r_).T.copy())
+                off += r_ * c_
+            out[name] = mats
+        return out
+
+    def mass(self):
+        M = np.zeros(self.n * self.n)
+        lib().hbo_mass(self._h, _dp(M))
+        return M.reshape(self.n, self.n).T.copy()
+
+
+# ----------------------------------------------------------------- SolutionsOperator
+
+def ldlt_eigen_factor(A):
+    """F = P^T L D^(1/2) from a diagonal-pivoting LDL^T in the style of Eigen's LDLT
+    (left-looking; pivots chosen on the stored diagonal, first maximum wins)."""
+    A = np.array(A, dtype=float)
+    n = A.shape[0]
+    mat = np.tril(A).copy()
+    perm = np.arange(n)
+    trans = np.zeros(n, int)
+    for k in range(n):
+        idx = k + int(np.argmax(np.abs(np.diag(mat)[k:])))
+        trans[k] = idx
+        if idx != k:
+            s = n - idx - 1
+            mat[[k, idx], :k] = mat[[idx, k], :k]
+            if s > 0:
+                tmp = mat[idx + 1:, k].copy(); mat[idx + 1:, k] = mat[idx + 1:, idx]; mat[idx + 1:, idx] = tmp
+            mat[k, k], mat[idx, idx] = mat[idx, idx], mat[k, k]
+            for i in range(k + 1, idx):
+                tmp = mat[i, k]
+                mat[i, k] = mat[idx, i]
+                mat[idx, i] = tmp
+        if k > 0:
+            temp = np.diag(mat)[:k] * mat[k, :k]
+            mat[k, k] -= mat[k, :k] @ temp
+            if k + 1 < n:
+                mat[k + 1:, k] -= mat[k + 1:, :k] @ temp
+        akk = mat[k, k]
+        if k + 1 < n and akk != 0:
+            mat[k + 1:, k] /= akk
+    L = np.tril(mat, -1) + np.eye(n)
+    D = np.diag(mat).copy()
+    P = np.eye(n)
+    for k in range(n):           # P = transpositions applied in order
+        P[[k, trans[k]]] = P[[trans[k], k]]
+    return P.T @ L @ np.diag(np.sqrt(D))
+
+
+class SolutionsOperator:
+    """T(k) = [[K_i - K_o + M, V_o - V_i], [W_o - W_i, K_o - K_i + M^T]], projected as
+    F^-1 T F^-T with F F^T = blockdiag(M, M^T).  ``factor='chol'`` uses the
+    Cholesky factor; ``factor='ldlt'`` the Eigen-style pivoted LDL^T factor of the
+    reference.  Any F with F F^T = A gives an orthogonally similar T_proj."""
+
+    def __init__(self, builder: Builder, proj=True, factor="chol"):
+        self.b = builder
+        self.proj = proj
+        self.M = builder.mass()
+        n = builder.n
+        A = np.zeros((2 * n, 2 * n))
+        A[:n, :n] = self.M
+        A[n:, n:] = self.M.T
+        if proj:
+            if factor == "chol":
+                self.F = np.linalg.cholesky(A)
+            else:
+                self.F = ldlt_eigen_factor(A)
+            self._lu = sla.lu_factor(self.F)
+
+    def projection(self, T):
+        X = sla.lu_solve(self._lu, T)
+        return sla.lu_solve(self._lu, X.T).T
+
+    def blocks(self, k, c_o, c_i, d=0, threads=None):
+        """Unprojected [T, T', T''] (first d+1)."""
+        Li = self.b.assemble(k, c_i, LAYER_ALL, d, threads=threads)
+        Lo = self.b.assemble(k, c_o, LAYER_ALL, d, threads=threads)
+        n = self.b.n
+        out = []
+        for t in range(d + 1):
+            T = np.zeros((2 * n, 2 * n), np.complex128)
+            T[:n, :n] = -Lo["K"][t] + Li["K"][t]
+            T[n:, :n] = Lo["W"][t] - Li["W"][t]
+            T[:n, n:] = Lo["V"][t] - Li["V"][t]
+            T[n:, n:] = Lo["K"][t] - Li["K"][t]
+            if t == 0:
+                T[:n, :n] += self.M
+                T[n:, n:] += self.M.T
+            out.append(T)
+        return out
+
+    def gen_sol_op(self, k, c_o, c_i, d=0, threads=None):
+        mats = self.blocks(k, c_o, c_i, d, threads)
+        if self.proj:
+            mats = [self.projection(T) for T in mats]
+        return mats
+
+
+# ----------------------------------------------------------------- dense singular values
+
+def _sv_triplets(T):
+    U, s, Vh = np.linalg.svd(T)
+    return U, s, Vh.conj().T
+
+
+def sv_derivs(T, T1=None, T2=None, which=0, degen_rtol=1e-9):
+    """sigma_which (ascending) of T and its k-derivatives (direct::sv_1st_der /
+    sv_2nd_der semantics: eigen-perturbation of the Hermitian Wielandt matrix
+    [[0,T],[T^H,0]], eigenvalues +-sigma_j).  Partners degenerate with sigma
+    (|sigma_j - sigma| <= degen_rtol*sigma) are excluded from the second-order sum;
+    their coupling vanishes for a perturbation that preserves the degeneracy."""
+    U, s, V = _sv_triplets(T)
+    order = np.argsort(s)
+    i = order[which]
+    sig = s[i]
+    out = [sig]
+    if T1 is None:
+        return out
+    u, v = U[:, i], V[:, i]
+    out.append(float(np.real(np.vdot(u, T1 @ v))))
+    if T2 is None:
+        return out
+    A = U.conj().T @ (T1 @ V)         # A[j, i] = u_j^H T' v_i
+    a_ji = A[:, i]
+    b_ji = np.conj(A[i, :])           # conj(u_i^H T' v_j)
+    val = float(np.real(np.vdot(u, T2 @ v)))
+    plus = np.abs(a_ji + b_ji) ** 2
+    minus = np.abs(a_ji - b_ji) ** 2
+    for j in range(s.size):
+        if j != i and abs(s[j] - sig) > degen_rtol * max(sig, 1e-300):
+            val += 0.5 * plus[j] / (sig - s[j])
+        val += 0.5 * minus[j] / (sig + s[j])
+    out.append(val)
+    return out
+
+
+# ----------------------------------------------------------------- randomized SVD
+
+def rand_sketch(n, s, seed):
+    """Seeded stand-in for randomized_svd::randGaussian: (U[0,1] + i U[0,1])/sqrt2."""
+    rng = np.random.default_rng(seed)
+    return (rng.uniform(0, 1, (n, s)) + 1j * rng.uniform(0, 1, (n, s))) * math.sqrt(0.5)
+
+
+def rsvd_sv(T, R, q=0, lu=None):
+    """randomized_svd::sv (randsvd.cpp:99-146): Q = qr(T^-1 R), q subspace steps
+    Q = qr(T^-1 qr(T^-H Q)), sigma_min ~ 1/sigma_max(T^-H Q)."""
+    if lu is None:
+        lu = sla.lu_factor(T)
+    Q, _ = np.linalg.qr(sla.lu_solve(lu, R))
+    for _ in range(q):
+        Q1, _ = np.linalg.qr(sla.lu_solve(lu, Q, trans=2))
+        Q, _ = np.linalg.qr(sla.lu_solve(lu, Q1))
+    B = sla.lu_solve(lu, Q, trans=2)
+    return 1.0 / np.linalg.svd(B, compute_uv=False)[0]
+
+
+def rsvd_sv_der(T, T1, R, q=0):
+    """randomized_svd::sv_der (randsvd.cpp:148-169): null vector of W - s I."""
+    n = T.shape[0]
+    s = rsvd_sv(T, R, q)
+    W = np.zeros((2 * n, 2 * n), complex)
+    W[:n, n:] = T; W[n:, :n] = T.conj().T
+    W -= s * np.eye(2 * n)
+    _, _, vh = np.linalg.svd(W)
+    x = vh[-1].conj()
+    p = np.concatenate([T1 @ x[n:], T1.conj().T @ x[:n]])
+    return s, float(np.real(np.vdot(x, p)))
+
+
+# ----------------------------------------------------------------- root finding
+
+EPS = np.finfo(float).eps
+MAXIT = 1000
+
+
+def rtsafe(fct, fct_both, x1, x2, tol):
+    """Safeguarded Newton (find_roots.cpp:117-217; Press et al. 'rtsafe').
+    Returns (root, root_found, iterations)."""
+    fl, fh = fct(x1), fct(x2)
+    if fl == fl and fh == fh:
+        if fl * fh > 0.0:
+            return (x1 if fl > fh else x2), False, 0
+        if fl == 0.0:
+            return x1, True, 0
+        if fh == 0.0:
+            return x2, True, 0
+        xl, xh = (x1, x2) if fl < 0.0 else (x2, x1)
+        rts = 0.5 * (x1 + x2)
+    else:
+        rts = fct(float("nan"))
+        xl, xh = x1, x2
+    dxold = abs(x2 - x1)
+    dx = dxold
+    f, df = fct_both(rts)
+    for j in range(1, MAXIT + 1):
+        if (((rts - xh) * df - f) * ((rts - xl) * df - f) > 0.0) or (abs(2.0 * f) > abs(dxold * df)):
+            dxold = dx
+            dx = 0.5 * (xh - xl)
+            rts = xl + dx
+            if abs(xl - rts) < EPS:
+                return rts, True, j
+        else:
+            dxold = dx
+            dx = f / df
+            temp = rts
+            rts -= dx
+            if temp == rts:
+                return rts, True, j
+        if abs(dx) < tol:
+            return rts, True, j
+        f, df = fct_both(rts)
+        if f < 0.0:
+            xl = rts
+        else:
+            xh = rts
+    return float("nan"), False, MAXIT
+
+
+class BrentMin:
+    """Brent's localmin (golden section + parabolic steps) with reverse communication,
+    the interface of BrentMinimizer::local_min_rc (find_roots.cpp:1003-1184)."""
+
+    def __init__(self, a, b, tol):
+        self.A, self.B, self.tol = a, b, tol
+        self.eps = math.sqrt(tol)
+
+    def minimize(self, f):
+        a, b = self.A, self.B
+        c = 0.5 * (3.0 - math.sqrt(5.0))
+        v = w = x = a + c * (b - a)
+        e = d = 0.0
+        fx = fv = fw = f(x)
+        while True:
+            mid = 0.5 * (a + b)
+            tol1 = self.eps * abs(x) + self.tol / 3.0
+            tol2 = 2.0 * tol1
+            if abs(x - mid) <= tol2 - 0.5 * (b - a):
+                return x
+            golden = abs(e) <= tol1
+            if not golden:
+                r = (x - w) * (fx - fv)
+                q = (x - v) * (fx - fw)
+                p = (x - v) * q - (x - w) * r
+                q = 2.0 * (q - r)
+                if q > 0.0:
+                    p = -p
+                q = abs(q)
+                r, e = e, d
+                if abs(0.5 * q * r) <= abs(p) or p <= q * (a - x) or q * (b - x) <= p:
+                    golden = True
+                else:
+                    d = p / q
+                    u = x + d
+                    sgn = -1.0 if (mid - x) < 0 else 1.0
+                    if (u - a) < tol2 or (b - u) < tol2:
+                        d = tol1 * sgn
+            if golden:
+                e = (a - x) if mid <= x else (b - x)
+                d = c * e
+            if abs(d) >= tol1:
+                u = x + d
+            else:
+                u = x + tol1 * (-1.0 if d < 0 else 1.0)
+            fu = f(u)
+            if fu <= fx:
+                if x <= u:
+                    a = x
+                else:
+                    b = x
+                v, fv, w, fw, x, fx = w, fw, x, fx, u, fu
+            else:
+                if u < x:
+                    a = u
+                else:
+                    b = u
+                if fu <= fw or w == x:
+                    v, fv, w, fw = w, fw, u, fu
+                elif fu <= fv or v == x or v == w:
+                    v, fv = u, fu
+
+
+def quartic_guess(a, h, f1, f0, f2, d1, d2, tol):
+    """Quartic Hermite model through (a,f1,d1), (a+h,f0), (a+2h,f2,d2) minimised by
+    Brent (examples/roots_newton_polygon_rsvd.cpp:224-245)."""
+    scale = 0.25 * h ** -4
+    a2 = a * a
+    p1 = a2 * (h * (d2 - d1) - 2.0 * (f1 + f2 - 2.0 * f0))
+    p2 = a * h * (h * (3.0 * d2 - 5.0 * d1) - (9.0 * f1 + 7.0 * f2 - 16.0 * f0))
+    p3 = h * h * (2.0 * h * (d2 - 4.0 * d1) - (11.0 * f1 + 5.0 * f2 - 16.0 * f0))
+    A = scale * p1 / a2
+    B = -scale * (4.0 * p1 + p2) / a
+    C = scale * (6.0 * p1 + 3 * p2 + p3)
+    D = d1 - scale * a * (4.0 * p1 + 3.0 * p2 + 2.0 * p3)
+    E = f1 - a * d1 + scale * a2 * (p1 + p2 + p3)
+    return BrentMin(a, a + 2 * h, tol).minimize(lambda t: (((A * t + B) * t + C) * t + D) * t + E)
+
+
+def plain_sweep(eval3, ks, tol=1e-8):
+    """Plain sweep: sigma, sigma', sigma'' on the grid -> 3-point minima -> validate
+    sigma'(left) < 0 < sigma'(right) -> quartic + Brent guess -> rtsafe on sigma'.
+    ``eval3(list_of_k) -> array (len, 3)``.  Returns (roots, grid values)."""
+    ks = np.asarray(ks, float)
+    vals = np.asarray(eval3(list(ks)))
+    h = ks[1] - ks[0]
+    roots = []
+    for i in range(len(ks) - 2):
+        L, cval, R = vals[i, 0], vals[i + 1, 0], vals[i + 2, 0]
+        if not (L - cval > 0.0 and R - cval > 0.0):
+            continue
+        d1, d2 = vals[i, 1], vals[i + 2, 1]
+        if not (d1 < 0.0 < d2):
+            continue
+        a = ks[i]
+        guess = quartic_guess(a, h, L, cval, R, d1, d2, tol)
+
+        def fn(x, g=guess):
+            return float("nan") if x == x else g
+
+        def both(x):
+            r = eval3([x])[0]
+            return r[1], r[2]
+
+        root, ok, _ = rtsafe(fn, both, a, a + 2 * h, tol)
+        if ok and root == root:
+            roots.append(root)
+    return np.array(roots), vals

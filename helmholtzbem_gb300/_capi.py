@@ -1,0 +1,109 @@
+"""ctypes binding of libhbem.so (include/hbem.h).
+
+The library is the only compute path: if it is missing or fails to load this
+module raises, so nothing silently falls back to CPU code.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libhbem.so")
+
+HBEM_OK = 0
+LAYER_DOUBLE, LAYER_SINGLE, LAYER_HYPERSINGULAR, LAYER_ALL = 1, 2, 4, 7
+PANEL_LINE, PANEL_ARC = 0, 1
+SPACE_P0, SPACE_P1 = 1, 2
+
+# every symbol include/hbem.h declares
+EXPORTS = [
+    "hbem_version", "hbem_status_string", "hbem_last_error", "hbem_set_device", "hbem_hankel01",
+    "hbem_builder_create", "hbem_builder_destroy", "hbem_builder_info", "hbem_builder_is_adjacent",
+    "hbem_assemble_dense", "hbem_get_layer", "hbem_get_layer_device",
+    "hbem_solop_create", "hbem_solop_destroy", "hbem_mass_matrix", "hbem_gen_sol_op",
+    "hbem_gen_sol_op_batch_device", "hbem_sv_dense_batch_device", "hbem_sv_dense_batch", "hbem_sweep_sigma",
+    "hbem_find_resonances_plain", "hbem_rtsafe", "hbem_zbrent", "hbem_brent_min",
+]
+
+_lib = None
+
+_d = ctypes.c_double
+_i = ctypes.c_int
+_u = ctypes.c_uint
+_vp = ctypes.c_void_p
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_up = ctypes.POINTER(ctypes.c_uint)
+
+FN = ctypes.CFUNCTYPE(ctypes.c_double, ctypes.c_double, ctypes.c_void_p)
+FN_BOTH = ctypes.CFUNCTYPE(None, ctypes.c_double, _dp, _dp, ctypes.c_void_p)
+
+
+class HbemError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("hbem status %d (%s): %s" % (status, _status_name(status), msg))
+        self.status = status
+
+
+def _status_name(s):
+    try:
+        return lib().hbem_status_string(s).decode()
+    except Exception:
+        return "?"
+
+
+def load(path=LIB_PATH):
+    """Load libhbem.so without touching the GPU (symbol table only)."""
+    if not os.path.exists(path):
+        raise RuntimeError("libhbem.so is not built (%s); run __graft_entry__.build()" % path)
+    L = ctypes.CDLL(path)
+    sig = {
+        "hbem_version": (_i, []),
+        "hbem_status_string": (ctypes.c_char_p, [_i]),
+        "hbem_last_error": (ctypes.c_char_p, []),
+        "hbem_set_device": (_i, [_i]),
+        "hbem_hankel01": (_i, [_i, _dp, _i, _dp, _dp]),
+        "hbem_builder_create": (_i, [_i, _ip, _dp, _i, _i, _i, ctypes.POINTER(_vp)]),
+        "hbem_builder_destroy": (_i, [_vp]),
+        "hbem_builder_info": (_i, [_vp, _ip, _ip, _ip, _ip, _ip]),
+        "hbem_builder_is_adjacent": (_i, [_vp, _i, _i, _ip, _ip]),
+        "hbem_assemble_dense": (_i, [_vp, _d, _d, _d, _u, _u]),
+        "hbem_get_layer": (_i, [_vp, _u, _u, _dp]),
+        "hbem_get_layer_device": (_i, [_vp, _u, _u, ctypes.POINTER(_vp)]),
+        "hbem_solop_create": (_i, [_vp, _i, ctypes.POINTER(_vp)]),
+        "hbem_solop_destroy": (_i, [_vp]),
+        "hbem_mass_matrix": (_i, [_vp, _dp]),
+        "hbem_gen_sol_op": (_i, [_vp, _d, _d, _d, _d, _u, _dp]),
+        "hbem_gen_sol_op_batch_device": (_i, [_vp, _dp, _i, _d, _d, _u, _vp]),
+        "hbem_sv_dense_batch_device": (_i, [_i, _i, _u, _vp, ctypes.c_longlong, ctypes.c_longlong, _dp, _dp]),
+        "hbem_sv_dense_batch": (_i, [_i, _i, _u, _dp, _dp, _dp]),
+        "hbem_sweep_sigma": (_i, [_vp, _dp, _i, _d, _d, _u, _dp]),
+        "hbem_find_resonances_plain": (_i, [_vp, _d, _d, _i, _d, _d, _d, _dp, _i, _ip, _dp, _ip]),
+        "hbem_rtsafe": (_d, [FN, FN_BOTH, _vp, _d, _d, _d, _ip, _up]),
+        "hbem_zbrent": (_d, [FN, _vp, _d, _d, _d, _ip, _up]),
+        "hbem_brent_min": (_d, [FN, _vp, _d, _d, _d]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    return L
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = load()
+    return _lib
+
+
+def check(status):
+    if status != HBEM_OK:
+        raise HbemError(status, lib().hbem_last_error().decode(errors="replace"))
+
+
+def dptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+def iptr(a):
+    return a.ctypes.data_as(_ip)

@@ -1,0 +1,194 @@
+"""Python mirror of the reference's API for the assembly-and-resonance path.
+
+Names, argument meaning and error behaviour follow the reference classes
+(include/galerkin_builder.hpp, include/gen_sol_op.hpp, include/singular_values.hpp,
+include/find_roots.hpp); every call goes through the C ABI of libhbem.so.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _capi as C
+from ._capi import check, dptr, iptr
+
+LayerType_DOUBLE = C.LAYER_DOUBLE
+LayerType_SINGLE = C.LAYER_SINGLE
+LayerType_HYPERSINGULAR = C.LAYER_HYPERSINGULAR
+LayerType_ALL = C.LAYER_ALL
+
+
+class BuilderData:
+    """BuilderData(mesh, test_space, trial_space, order); mesh = (kinds, params)."""
+
+    def __init__(self, mesh, test_space=C.SPACE_P1, trial_space=C.SPACE_P1, order=11):
+        kinds, params = mesh
+        self.kinds = np.ascontiguousarray(kinds, np.int32)
+        self.params = np.ascontiguousarray(params, np.float64).reshape(-1, 5)
+        self.order = int(order)
+        h = ctypes.c_void_p()
+        check(C.lib().hbem_builder_create(int(self.kinds.size), iptr(self.kinds), dptr(self.params), self.order,
+                                          int(test_space), int(trial_space), ctypes.byref(h)))
+        self._h = h
+        n, dt, dr, o, ln = (ctypes.c_int() for _ in range(5))
+        check(C.lib().hbem_builder_info(self._h, ctypes.byref(n), ctypes.byref(dt), ctypes.byref(dr), ctypes.byref(o),
+                                        ctypes.byref(ln)))
+        self.npanels, self.dim_test, self.dim_trial = n.value, dt.value, dr.value
+        self.panels_are_lines = bool(ln.value)
+
+    def getNumPanels(self):
+        return self.npanels
+
+    def getTestSpaceDimension(self):
+        return self.dim_test
+
+    def getTrialSpaceDimension(self):
+        return self.dim_trial
+
+    def getPanelsAreLines(self):
+        return self.panels_are_lines
+
+    def is_adjacent(self, i, j):
+        a, s = ctypes.c_int(), ctypes.c_int()
+        check(C.lib().hbem_builder_is_adjacent(self._h, i, j, ctypes.byref(a), ctypes.byref(s)))
+        return bool(a.value), bool(s.value)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and C._lib is not None:
+            C._lib.hbem_builder_destroy(h)
+            self._h = None
+
+
+class GalerkinBuilder:
+    """GalerkinBuilder(data): assembleDense + layer getters (complex128, N x N)."""
+
+    def __init__(self, data: BuilderData):
+        self.data = data
+
+    def assembleDense(self, k, c, layers=LayerType_ALL, d=0):
+        k = complex(k)
+        check(C.lib().hbem_assemble_dense(self.data._h, k.real, k.imag, float(c), int(layers), int(d)))
+
+    def _get(self, layer, d):
+        n = self.data.npanels
+        out = np.zeros((n, n), np.complex128, order="F")
+        check(C.lib().hbem_get_layer(self.data._h, layer, int(d), out.ctypes.data_as(C._dp)))
+        return out
+
+    def getDoubleLayer(self, d=0):
+        return self._get(C.LAYER_DOUBLE, d)
+
+    def getHypersingular(self, d=0):
+        return self._get(C.LAYER_HYPERSINGULAR, d)
+
+    def getSingleLayer(self, d=0):
+        return self._get(C.LAYER_SINGLE, d)
+
+
+class SolutionsOperator:
+    """SolutionsOperator(builder_data, proj=True)."""
+
+    def __init__(self, data: BuilderData, proj=True):
+        self.data = data
+        h = ctypes.c_void_p()
+        check(C.lib().hbem_solop_create(data._h, 1 if proj else 0, ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and C._lib is not None:
+            C._lib.hbem_solop_destroy(h)
+            self._h = None
+
+    def mass_matrix(self):
+        n = self.data.npanels
+        M = np.zeros((n, n), order="F")
+        check(C.lib().hbem_mass_matrix(self._h, M.ctypes.data_as(C._dp)))
+        return M
+
+    def _gen(self, k, c_o, c_i, d):
+        k = complex(k)
+        n = 2 * self.data.npanels
+        buf = np.zeros((d + 1, n, n), np.complex128)   # each matrix column-major => transpose views
+        check(C.lib().hbem_gen_sol_op(self._h, k.real, k.imag, float(c_o), float(c_i), int(d),
+                                      buf.ctypes.data_as(C._dp)))
+        return [buf[t].T for t in range(d + 1)]
+
+    def gen_sol_op(self, k, c_o, c_i):
+        return self._gen(k, c_o, c_i, 0)[0]
+
+    def gen_sol_op_1st_der(self, k, c_o, c_i):
+        return tuple(self._gen(k, c_o, c_i, 1))
+
+    def gen_sol_op_2nd_der(self, k, c_o, c_i):
+        return tuple(self._gen(k, c_o, c_i, 2))
+
+    def sweep_sigma(self, ks, c_o, c_i, d=2):
+        ks = np.ascontiguousarray(ks, np.float64)
+        out = np.zeros((ks.size, 3))
+        check(C.lib().hbem_sweep_sigma(self._h, dptr(ks), int(ks.size), float(c_o), float(c_i), int(d), dptr(out)))
+        return out
+
+    def find_resonances_plain(self, k_min, k_max, npoints, c_o, c_i, tol=1e-8, max_roots=4096):
+        roots = np.zeros(max_roots)
+        grid = np.zeros((npoints, 3))
+        nr, ne = ctypes.c_int(), ctypes.c_int()
+        check(C.lib().hbem_find_resonances_plain(self._h, float(k_min), float(k_max), int(npoints), float(c_o),
+                                                 float(c_i), float(tol), dptr(roots), max_roots, ctypes.byref(nr),
+                                                 dptr(grid), ctypes.byref(ne)))
+        return roots[:min(nr.value, max_roots)].copy(), grid, ne.value
+
+
+def sv_dense(Ts, d=0, all_values=False):
+    """direct::sv / sv_1st_der / sv_2nd_der for a batch: Ts is a list (one per matrix)
+    of [T] / [T, T'] / [T, T', T''].  Returns (nmat, 3) [sigma_min, sigma', sigma'']."""
+    nmat = len(Ts)
+    n = Ts[0][0].shape[0]
+    buf = np.zeros((nmat, d + 1, n, n), np.complex128)
+    for m, mats in enumerate(Ts):
+        for t in range(d + 1):
+            buf[m, t] = np.asarray(mats[t]).T      # column-major
+    out = np.zeros((nmat, 3))
+    sig = np.zeros((nmat, n)) if all_values else None
+    check(C.lib().hbem_sv_dense_batch(n, nmat, int(d), buf.ctypes.data_as(C._dp), dptr(out),
+                                      dptr(sig) if all_values else None))
+    return (out, sig) if all_values else out
+
+
+def rtsafe(f, f_both, x1, x2, tol):
+    """rtsafe(f, f_both, x1, x2, tol) -> (root, root_found, num_iter); f_both(x) -> (f, f')."""
+    cb = C.FN(lambda x, u: float(f(x)))
+
+    def _both(x, pf, pdf, u):
+        a, b = f_both(x)
+        pf[0] = float(a)
+        pdf[0] = float(b)
+
+    cbb = C.FN_BOTH(_both)
+    rf, ni = ctypes.c_int(), ctypes.c_uint()
+    r = C.lib().hbem_rtsafe(cb, cbb, None, float(x1), float(x2), float(tol), ctypes.byref(rf), ctypes.byref(ni))
+    return r, bool(rf.value), ni.value
+
+
+def zbrent(f, x1, x2, tol):
+    cb = C.FN(lambda x, u: float(f(x)))
+    rf, ni = ctypes.c_int(), ctypes.c_uint()
+    r = C.lib().hbem_zbrent(cb, None, float(x1), float(x2), float(tol), ctypes.byref(rf), ctypes.byref(ni))
+    return r, bool(rf.value), ni.value
+
+
+def brent_min(f, a, b, tol):
+    cb = C.FN(lambda x, u: float(f(x)))
+    return C.lib().hbem_brent_min(cb, None, float(a), float(b), float(tol))
+
+
+def hankel01(z):
+    """H0^(1), H1^(1) on the device; real path for a real array, complex path otherwise."""
+    z = np.asarray(z)
+    cplx_arg = not np.isrealobj(z)
+    src = np.ascontiguousarray(z.ravel(), np.complex128 if cplx_arg else np.float64)
+    h0 = np.zeros(src.size, np.complex128)
+    h1 = np.zeros(src.size, np.complex128)
+    check(C.lib().hbem_hankel01(int(src.size), src.ctypes.data_as(C._dp), 1 if cplx_arg else 0,
+                                h0.ctypes.data_as(C._dp), h1.ctypes.data_as(C._dp)))
+    return h0.reshape(z.shape), h1.reshape(z.shape)

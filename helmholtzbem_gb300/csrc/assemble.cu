@@ -1,0 +1,588 @@
+// Galerkin panel-pair quadrature kernels (see assemble.cuh for the layout).
+//
+// Formulas follow the reference's GalerkinBuilder
+// (source/galerkin_builder.cpp:237-832); per quadrature point with
+// v = gamma_i(x) - gamma_j(y), ks = k sqrt(c), h0/h1 = H0/H1(ks |v|):
+//   V   : |tau_i||tau_j| f f w * { h0, h1|v|, h1|v|/ks - h0|v|^2 }      scale {1, -sqrt c, c}
+//   K   : (v x tau_j)|tau_i| f g w * { ks h1/|v|, h0, h0 - ks|v| h1 }   scale {1, k c, c}
+//   K^T : (tau_i x v)|tau_j| f g w * (same kernels)
+//   W   : cf = b'b' w - (ks^2/2) temp, temp = 2 (tau_i.tau_j) f f w
+//         { cf h0, h1|v| cf + ks h0 temp,
+//           (h0|v|^2 - h1|v|/ks) cf - temp (2 ks h1|v| - h0) }           scale {1, -sqrt c, -c}
+// and every matrix is finally multiplied by i/4.
+#include "assemble.cuh"
+
+namespace hbem {
+
+struct KConst {
+    cplx k, ks, k2ch, ks_inv, ks_two;
+    double c, sqrtc;
+};
+
+__device__ __forceinline__ KConst make_kconst(const Job& jb) {
+    KConst K;
+    K.c = jb.c;
+    K.sqrtc = sqrt(jb.c);
+    K.k = mk(jb.kre, jb.kim);
+    K.ks = K.sqrtc * K.k;
+    K.k2ch = 0.5 * (K.ks * K.ks);
+    K.ks_inv = cdiv(mk(1.), K.ks);
+    K.ks_two = 2.0 * K.ks;
+    return K;
+}
+
+template <int D>
+struct Acc {
+    cplx dl[D + 1][4], dlt[D + 1][4], hy[D + 1][4], sl[D + 1][4];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int t = 0; t <= D; ++t)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) dl[t][e] = dlt[t][e] = hy[t][e] = sl[t][e] = mk(0.);
+    }
+};
+
+template <bool RK>
+__device__ __forceinline__ void hankel_at(const KConst& K, double vn, cplx& h0, cplx& h1) {
+    if (RK) hankel01_real(K.ks.re * vn, h0, h1);
+    else hankel01_cplx(vn * K.ks, h0, h1);
+}
+
+// complex scalar times complex, specialised for real ks
+template <bool RK>
+__device__ __forceinline__ cplx kmul(cplx a, cplx z) { return RK ? a.re * z : a * z; }
+
+// One quadrature point's contribution to all local blocks.
+//   fi, gj : shape values (test on panel i at x, trial on panel j at y)
+//   fj, gi : for the transposed double layer (test on panel j at y, trial on i at x)
+//   vd, vdt: v x n factors (0 when that block is switched off for the pair)
+template <int D, bool RK>
+__device__ __forceinline__ void point_contrib(Acc<D>& A, const KConst& K, double w, double vn, double vn2,
+                                              cplx h0, cplx h1, double vd, double vdt, const double fi[2],
+                                              const double gj[2], const double fj[2], const double gi[2],
+                                              double ttp, double tdt, bool tz) {
+    const double dsh[2] = {1., -1.};
+    cplx m1 = vn > 0. ? kmul<RK>(K.ks, (1.0 / vn) * h1) : mk(0.);
+    cplx hv = vn * h1;
+    cplx m3, q, r2;
+    if (D > 1) {
+        m3 = h0 - kmul<RK>(K.ks, hv);
+        q = vn2 * h0 - kmul<RK>(K.ks_inv, hv);
+        r2 = kmul<RK>(K.ks_two, hv) - h0;
+    }
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+            const int e = 2 * a + b;
+            double fg = fi[a] * gj[b] * w;
+            // single layer
+            double cfr = ttp * fg;
+            axpy(A.sl[0][e], cfr, h0);
+            if (D > 0) axpy(A.sl[1][e], cfr, hv);
+            if (D > 1) axpy(A.sl[2][e], -cfr, q);
+            // double layer
+            double cd = vd * fg;
+            axpy(A.dl[0][e], cd, m1);
+            if (D > 0) axpy(A.dl[1][e], cd, h0);
+            if (D > 1) axpy(A.dl[2][e], cd, m3);
+            double cdt = vdt * (fj[a] * gi[b] * w);
+            axpy(A.dlt[0][e], cdt, m1);
+            if (D > 0) axpy(A.dlt[1][e], cdt, h0);
+            if (D > 1) axpy(A.dlt[2][e], cdt, m3);
+            // hypersingular
+            double arc = dsh[a] * dsh[b] * w;
+            double temp = tz ? 0. : fg * tdt;
+            if (RK) {
+                double cf = arc - K.k2ch.re * temp;
+                axpy(A.hy[0][e], cf, h0);
+                if (D > 0) {
+                    axpy(A.hy[1][e], cf, hv);
+                    axpy(A.hy[1][e], K.ks.re * temp, h0);
+                }
+                if (D > 1) {
+                    axpy(A.hy[2][e], cf, q);
+                    axpy(A.hy[2][e], -temp, r2);
+                }
+            } else {
+                cplx cf = mk(arc) - temp * K.k2ch;
+                A.hy[0][e] += cf * h0;
+                if (D > 0) A.hy[1][e] += cf * hv + (temp * K.ks) * h0;
+                if (D > 1) A.hy[2][e] += cf * q - temp * r2;
+            }
+        }
+    }
+}
+
+// scale derivative blocks and store a pair's local blocks
+template <int D>
+__device__ __forceinline__ void store_local(const Acc<D>& A, const KConst& K, cplx* dst) {
+    cplx kc = K.c * K.k;
+#pragma unroll
+    for (int t = 0; t <= D; ++t) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            cplx dl = A.dl[t][e], dlt = A.dlt[t][e], hy = A.hy[t][e], sl = A.sl[t][e];
+            if (t == 1) {
+                dl = dl * kc; dlt = dlt * kc;
+                hy = -K.sqrtc * hy; sl = -K.sqrtc * sl;
+            } else if (t == 2) {
+                dl = K.c * dl; dlt = K.c * dlt;
+                hy = -K.c * hy; sl = K.c * sl;
+            }
+            dst[t * kLocPerD + 0 + e] = dl;
+            dst[t * kLocPerD + 4 + e] = dlt;
+            dst[t * kLocPerD + 8 + e] = hy;
+            dst[t * kLocPerD + 12 + e] = sl;
+        }
+    }
+}
+
+__device__ __forceinline__ bool close100eps(cplx a, cplx b) { return hypot(a.re - b.re, a.im - b.im) < 100. * kEps; }
+
+// ------------------------------------------------------------------ panel maps (device)
+
+__device__ __forceinline__ cplx pan_op01(const double* P, int kind, double t, cplx* tan, double* tn) {
+    if (kind == 0) {
+        cplx d = mk(P[2] - P[0], P[3] - P[1]);
+        *tan = d;
+        *tn = hypot(d.re, d.im);
+        return mk(fma(d.re, t, P[0]), fma(d.im, t, P[1]));
+    }
+    double dphi = P[4] - P[3], s, c;
+    sincos(fma(t, dphi, P[3]), &s, &c);
+    *tan = mk(-P[2] * dphi * s, P[2] * dphi * c);
+    *tn = P[2] * fabs(dphi);
+    return mk(P[0] + P[2] * c, P[1] + P[2] * s);
+}
+
+// reversed map; the tangent returned is the forward tangent at the reflected point
+// (Derivative_01_swapped with neg = true)
+__device__ __forceinline__ cplx pan_swapped(const double* P, int kind, double t, cplx* tan, double* tn) {
+    if (kind == 0) {
+        cplx d = mk(P[2] - P[0], P[3] - P[1]);
+        *tan = d;
+        *tn = hypot(d.re, d.im);
+        return mk(fma(-d.re, t, P[2]), fma(-d.im, t, P[3]));
+    }
+    double dphi = P[3] - P[4], s, c;
+    sincos(fma(t, dphi, P[4]), &s, &c);
+    *tan = mk(P[2] * dphi * s, -P[2] * dphi * c);
+    *tn = P[2] * fabs(dphi);
+    return mk(P[0] + P[2] * c, P[1] + P[2] * s);
+}
+
+// ------------------------------------------------------------------ flags (k independent)
+
+// General pairs: zero tests of galerkin_builder.cpp:475-499 and 834-870.
+__global__ void k_flags_general(DevMesh M, uint8_t* flags) {
+    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    long long npair = (long long)M.n * (M.n + 1) / 2;
+    if (q >= npair) return;
+    uint8_t f = flags[q];
+    if (f & 0x80) return;   // singular pair (set by the host)
+    long long i = (long long)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
+    while (i * (i + 1) / 2 > q) --i;
+    while ((i + 1) * (i + 2) / 2 <= q) ++i;
+    long long j = q - i * (i + 1) / 2;
+    const int p = M.p;
+    bool zr = true, zrt = true, tz = true;
+    for (int a = 0; a < p; ++a) {
+        cplx xi = M.gpt[i * p + a], ti = M.gtan[i * p + a];
+        for (int b = 0; b < p; ++b) {
+            cplx v = xi - M.gpt[j * p + b], tj = M.gtan[j * p + b];
+            if (fabs(v.re * tj.im - v.im * tj.re) >= kEps) zr = false;
+            if (fabs(v.im * ti.re - v.re * ti.im) >= kEps) zrt = false;
+            if (fabs(ti.im * tj.im + ti.re * tj.re) >= kEps) tz = false;
+        }
+    }
+    f = 0;
+    if (zr) f |= PF_DL0_ZERO;
+    if (zrt) f |= PF_DLT0_ZERO;
+    if (tz) f |= PF_TDT0_ZERO;
+    flags[q] = f;
+}
+
+// Point geometry of a singular pair (coincident or adjacent set K).
+struct SPoint {
+    cplx v, ti, tj;
+    double tin, tjn, x, y;
+};
+
+__device__ __forceinline__ void singular_point(const DevMesh& M, const SingularTask& T, int K, double a_node,
+                                               double b_node, SPoint& P) {
+    const double* Pi = M.par + 5 * T.i;
+    const double* Pj = M.par + 5 * T.j;
+    int ki = M.kind[T.i], kj = M.kind[T.j];
+    if (T.kind == PK_COINC) {
+        // t = xc[b], s = t (1 - xc[a]); set 0: x = s, y = t; set 1 swaps the roles
+        double t = b_node, s = t * (1. - a_node);
+        cplx ts, tt;
+        double tns, tnt;
+        cplx ps = pan_op01(Pi, ki, s, &ts, &tns), pt = pan_op01(Pi, ki, t, &tt, &tnt);
+        if (K == 0) { P.v = ps - pt; P.ti = ts; P.tin = tns; P.tj = tt; P.tjn = tnt; P.x = s; P.y = t; }
+        else { P.v = pt - ps; P.ti = tt; P.tin = tnt; P.tj = ts; P.tjn = tns; P.x = t; P.y = s; }
+        // the reference uses v = gamma(s) - gamma(t) for both sets; only its sign differs here
+        return;
+    }
+    // adjacent: t = xc[a], s = t xc[b]; set 0: (x, y) = (s, t), set 1: (t, s)
+    double ta = a_node, sa = ta * b_node;
+    double x = K == 0 ? sa : ta, y = K == 0 ? ta : sa;
+    cplx pi, pj;
+    if (!T.swap) {
+        pi = pan_swapped(Pi, ki, x, &P.ti, &P.tin);
+        pj = pan_op01(Pj, kj, y, &P.tj, &P.tjn);
+    } else {
+        pi = pan_op01(Pi, ki, x, &P.ti, &P.tin);
+        pj = pan_swapped(Pj, kj, y, &P.tj, &P.tjn);
+    }
+    P.v = pi - pj;
+    P.x = x;
+    P.y = y;
+}
+
+// Singular pairs: zero tests (galerkin_builder.cpp:366-375, 409-418, 834-853), one CTA per pair.
+__global__ void k_flags_singular(DevMesh M, const SingularTask* tasks, uint8_t* flags) {
+    SingularTask T = tasks[blockIdx.x];
+    int nc = M.nc, tot = nc * nc;
+    int nz[6] = {0, 0, 0, 0, 0, 0};   // counts of |value| >= eps per test
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+        int a = e % nc, b = e / nc;
+        for (int K = 0; K < 2; ++K) {
+            SPoint P;
+            singular_point(M, T, K, M.xc[a], M.xc[b], P);
+            // v x tau_j |tau_i| (set K), tau_i x v |tau_j|; for coincident pairs the
+            // reference multiplies the norm in before its zero test as well
+            double vd = (P.v.re * P.tj.im - P.v.im * P.tj.re) * P.tin;
+            double vdt = (P.v.im * P.ti.re - P.v.re * P.ti.im) * P.tjn;
+            double td = P.ti.im * P.tj.im + P.ti.re * P.tj.re;
+            if (fabs(vd) >= kEps) nz[K == 0 ? 0 : 2]++;
+            if (fabs(vdt) >= kEps) nz[K == 0 ? 1 : 3]++;
+            if (fabs(td) >= kEps) nz[K == 0 ? 4 : 5]++;
+        }
+    }
+    __shared__ int s_nz[6];
+    if (threadIdx.x < 6) s_nz[threadIdx.x] = 0;
+    __syncthreads();
+    for (int c = 0; c < 6; ++c)
+        if (nz[c]) atomicAdd(&s_nz[c], nz[c]);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint8_t f = 0x80;
+        if (!s_nz[0]) f |= PF_DL0_ZERO;
+        if (!s_nz[1]) f |= PF_DLT0_ZERO;
+        if (!s_nz[2]) f |= PF_DL1_ZERO;
+        if (!s_nz[3]) f |= PF_DLT1_ZERO;
+        if (!s_nz[4]) f |= PF_TDT0_ZERO;
+        if (!s_nz[5]) f |= PF_TDT1_ZERO;
+        if (M.lines) {   // lines: one tangent product for both sets (compute_tdottp on K = 0)
+            f = (f & ~PF_TDT1_ZERO) | ((f & PF_TDT0_ZERO) ? PF_TDT1_ZERO : 0);
+        }
+        flags[tri_index(T.i, T.j)] = f;
+    }
+}
+
+// ------------------------------------------------------------------ local-block kernels
+
+template <int D, bool RK>
+__global__ void __launch_bounds__(128) k_general(DevMesh M, const Job* jobs, cplx* loc, long long npair) {
+    __shared__ double sx[64], sw[64];
+    for (int t = threadIdx.x; t < M.p; t += blockDim.x) { sx[t] = M.xg[t]; sw[t] = M.wg[t]; }
+    __syncthreads();
+    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    long long nlow = (long long)M.n * (M.n - 1) / 2;   // strictly lower pairs
+    if (q >= nlow) return;
+    long long i = (long long)((1.0 + sqrt(8.0 * (double)q + 1.0)) * 0.5);
+    while (i * (i - 1) / 2 > q) --i;
+    while ((i + 1) * i / 2 <= q) ++i;
+    long long j = q - i * (i - 1) / 2;
+    long long pid = tri_index(i, j);
+    uint8_t fl = M.flags[pid];
+    if (fl & 0x80) return;   // coincident / adjacent: singular kernel
+    const int job = blockIdx.y;
+    KConst K = make_kconst(jobs[job]);
+    const bool use_dl = !(fl & PF_DL0_ZERO), use_dlt = !(fl & PF_DLT0_ZERO), tz = (fl & PF_TDT0_ZERO) != 0;
+    const int p = M.p;
+    const cplx* pti = M.gpt + i * p;
+    const cplx* ptj = M.gpt + j * p;
+    const cplx* tgi = M.gtan + i * p;
+    const cplx* tgj = M.gtan + j * p;
+    const double* tni = M.gtn + i * p;
+    const double* tnj = M.gtn + j * p;
+    Acc<D> A;
+    A.zero();
+    for (int a = 0; a < p; ++a) {
+        const cplx xi = pti[a], ti = tgi[a];
+        const double tin = tni[a], s = sx[a], wa = sw[a];
+        const double fi[2] = {s, 1. - s};
+        for (int b = 0; b < p; ++b) {
+            const cplx yj = ptj[b], tj = tgj[b];
+            const double tjn = tnj[b], t = sx[b];
+            const double gj[2] = {t, 1. - t};
+            const cplx v = xi - yj;
+            const double vn2 = norm2(v), vn = sqrt(vn2);
+            cplx h0, h1;
+            hankel_at<RK>(K, vn, h0, h1);
+            // general: zero test on v x tau_j before the norm (galerkin_builder.cpp:475-499)
+            double vd = use_dl ? (v.re * tj.im - v.im * tj.re) * tin : 0.;
+            double vdt = use_dlt ? (v.im * ti.re - v.re * ti.im) * tjn : 0.;
+            double tdt = 2. * (ti.im * tj.im + ti.re * tj.re);
+            point_contrib<D, RK>(A, K, wa * sw[b], vn, vn2, h0, h1, vd, vdt, fi, gj, gj, fi, tin * tjn, tdt, tz);
+        }
+    }
+    store_local<D>(A, K, loc + ((long long)job * npair + pid) * (D + 1) * kLocPerD);
+}
+
+template <int D>
+__device__ __forceinline__ void block_reduce(Acc<D>& A, double* red /* [nwarps][4*(D+1)*4*2] */) {
+    constexpr int NV = 4 * (D + 1) * 4 * 2;
+    double* a = reinterpret_cast<double*>(&A);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        double x = a[v];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) red[warp * NV + v] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        double s = 0.;
+        for (int w = 0; w < nw; ++w) s += red[w * NV + threadIdx.x];
+        red[threadIdx.x] = s;   // row 0 is read only by this thread before
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) a[v] = red[v];
+    }
+}
+
+template <int D, bool RK>
+__global__ void __launch_bounds__(128) k_singular(DevMesh M, const SingularTask* tasks, const Job* jobs, cplx* loc,
+                                                  long long npair) {
+    extern __shared__ double sm[];
+    double* sxc = sm;
+    double* swc = sm + M.nc;
+    double* red = sm + 2 * M.nc;
+    for (int t = threadIdx.x; t < M.nc; t += blockDim.x) { sxc[t] = M.xc[t]; swc[t] = M.wc[t]; }
+    __syncthreads();
+    const SingularTask T = tasks[blockIdx.x];
+    const int job = blockIdx.y;
+    KConst K = make_kconst(jobs[job]);
+    const long long pid = tri_index(T.i, T.j);
+    const uint8_t fl = M.flags[pid];
+    const int nc = M.nc, tot = nc * nc;
+    Acc<D> A;
+    A.zero();
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+        const int a = e % nc, b = e / nc;
+        const double wab = swc[a] * swc[b];
+        if (T.kind == PK_COINC) {
+            SPoint P;
+            singular_point(M, T, 0, sxc[a], sxc[b], P);
+            const double w = sxc[b] * wab;
+            const double vn2 = norm2(P.v), vn = sqrt(vn2);
+            cplx h0, h1;
+            hankel_at<RK>(K, vn, h0, h1);
+            const double ttp = P.tin * P.tjn;
+            const bool tz = (fl & PF_TDT0_ZERO) != 0;
+            const double tdt = 2. * (P.ti.im * P.tj.im + P.ti.re * P.tj.re);
+            // set 0: x = s (panel i test side), y = t
+            {
+                double vd = (fl & PF_DL0_ZERO) ? 0. : (P.v.re * P.tj.im - P.v.im * P.tj.re) * P.tin;
+                const double fi[2] = {P.x, 1. - P.x}, gj[2] = {P.y, 1. - P.y};
+                point_contrib<D, RK>(A, K, w, vn, vn2, h0, h1, vd, 0., fi, gj, fi, gj, ttp, tdt, tz);
+            }
+            // set 1: roles of s and t exchanged, v -> -v
+            {
+                double vd = (fl & PF_DL1_ZERO) ? 0. : (P.v.im * P.ti.re - P.v.re * P.ti.im) * P.tjn;
+                const double fi[2] = {P.y, 1. - P.y}, gj[2] = {P.x, 1. - P.x};
+                point_contrib<D, RK>(A, K, w, vn, vn2, h0, h1, vd, 0., fi, gj, fi, gj, ttp, tdt, tz);
+            }
+        } else {
+            const double w = sxc[a] * wab;
+#pragma unroll 1
+            for (int Kset = 0; Kset < 2; ++Kset) {
+                SPoint P;
+                singular_point(M, T, Kset, sxc[a], sxc[b], P);
+                const double vn2 = norm2(P.v), vn = sqrt(vn2);
+                cplx h0, h1;
+                hankel_at<RK>(K, vn, h0, h1);
+                const uint8_t dlz = Kset == 0 ? PF_DL0_ZERO : PF_DL1_ZERO;
+                const uint8_t dltz = Kset == 0 ? PF_DLT0_ZERO : PF_DLT1_ZERO;
+                const uint8_t tdz = Kset == 0 ? PF_TDT0_ZERO : PF_TDT1_ZERO;
+                double vd = (fl & dlz) ? 0. : (P.v.re * P.tj.im - P.v.im * P.tj.re) * P.tin;
+                double vdt = (fl & dltz) ? 0. : (P.v.im * P.ti.re - P.v.re * P.ti.im) * P.tjn;
+                double tdt = 2. * (P.ti.im * P.tj.im + P.ti.re * P.tj.re);
+                double fi[2], gj[2], fj[2], gi[2];
+                if (!T.swap) {   // panel i reversed, panel j forward
+                    fi[0] = 1. - P.x; fi[1] = P.x;
+                    gj[0] = P.y; gj[1] = 1. - P.y;
+                    fj[0] = P.y; fj[1] = 1. - P.y;
+                    gi[0] = 1. - P.x; gi[1] = P.x;
+                } else {         // panel i forward, panel j reversed
+                    fi[0] = P.x; fi[1] = 1. - P.x;
+                    gj[0] = 1. - P.y; gj[1] = P.y;
+                    fj[0] = 1. - P.y; fj[1] = P.y;
+                    gi[0] = P.x; gi[1] = 1. - P.x;
+                }
+                point_contrib<D, RK>(A, K, w, vn, vn2, h0, h1, vd, vdt, fi, gj, fj, gi, P.tin * P.tjn, tdt,
+                                     (fl & tdz) != 0);
+            }
+        }
+    }
+    block_reduce<D>(A, red);
+    if (threadIdx.x == 0) store_local<D>(A, K, loc + ((long long)job * npair + pid) * (D + 1) * kLocPerD);
+}
+
+// ------------------------------------------------------------------ gather
+
+// P1 dof m touches panel m-1 through local function 0 (t) and panel m through local
+// function 1 (1-t)  (continuous_space.hpp:38-47).
+__device__ __forceinline__ int p1_panel(int m, int a, int N) { return a == 0 ? (m == 0 ? N - 1 : m - 1) : m; }
+
+// layer value (before the i/4 factor) at dofs (m, n): L = 0 double layer, 1 hypersingular, 2 single layer
+__device__ __forceinline__ cplx layer_entry(const cplx* locj, int N, int L, int t, int D1, int m, int n) {
+    cplx s = mk(0.);
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+        int i = p1_panel(m, a, N);
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+            int j = p1_panel(n, b, N);
+            const cplx* blk;
+            int e;
+            if (L == 0) {
+                if (i >= j) { blk = locj + tri_index(i, j) * D1 * kLocPerD + t * kLocPerD + 0; e = 2 * a + b; }
+                else { blk = locj + tri_index(j, i) * D1 * kLocPerD + t * kLocPerD + 4; e = 2 * a + b; }
+            } else {
+                int off = (L == 1) ? 8 : 12;
+                if (i >= j) { blk = locj + tri_index(i, j) * D1 * kLocPerD + t * kLocPerD + off; e = 2 * a + b; }
+                else { blk = locj + tri_index(j, i) * D1 * kLocPerD + t * kLocPerD + off; e = 2 * b + a; }
+            }
+            s += blk[e];
+        }
+    }
+    return s;
+}
+
+// T(k) and its derivatives for nk wavenumbers; jobs are (k, c_i), (k, c_o) interleaved.
+// T is column-major 2N x 2N per (k, t); blocks (gen_sol_op.cpp:59-74):
+//   T11 = K_i - K_o + M,  T12 = V_o - V_i,  T21 = W_o - W_i,  T22 = K_o - K_i + M^T
+__global__ void k_gather_T(int N, int D1, const cplx* loc, long long npair, const double* Mmass, cplx* T) {
+    const long long n2 = 2LL * N;
+    long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= n2 * n2) return;
+    const int kk = blockIdx.y;
+    const int m = (int)(idx % n2), n = (int)(idx / n2);
+    const int bm = m >= N, bn = n >= N, mm = m - bm * N, nn = n - bn * N;
+    const cplx* li = loc + (2LL * kk) * npair * D1 * kLocPerD;       // inner medium
+    const cplx* lo = loc + (2LL * kk + 1) * npair * D1 * kLocPerD;   // outer medium
+    int L;
+    double sgn;
+    if (!bm && !bn) { L = 0; sgn = 1.; }          // K_i - K_o
+    else if (!bm && bn) { L = 2; sgn = -1.; }     // V_o - V_i
+    else if (bm && !bn) { L = 1; sgn = -1.; }     // W_o - W_i
+    else { L = 0; sgn = -1.; }                    // K_o - K_i
+    for (int t = 0; t < D1; ++t) {
+        cplx vi = layer_entry(li, N, L, t, D1, mm, nn);
+        cplx vo = layer_entry(lo, N, L, t, D1, mm, nn);
+        cplx d = sgn * (vi - vo);
+        cplx val = mk(-0.25 * d.im, 0.25 * d.re);   // x i/4
+        if (t == 0 && bm == bn) val.re += bm ? Mmass[nn + (long long)mm * N] : Mmass[mm + (long long)nn * N];
+        T[((long long)kk * D1 + t) * n2 * n2 + idx] = val;
+    }
+}
+
+// Separate layer matrices (GalerkinBuilder getters) for job `job`: out[L][t] N x N col-major, x i/4.
+__global__ void k_gather_layers(int N, int D1, int layers, const cplx* loc, long long npair, int job, cplx* out) {
+    long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    long long nn2 = (long long)N * N;
+    if (idx >= nn2) return;
+    const int m = (int)(idx % N), n = (int)(idx / N);
+    const cplx* lj = loc + (long long)job * npair * D1 * kLocPerD;
+    int slot = 0;
+    const int lbit[3] = {1, 4, 2};   // K, W, V
+    for (int L = 0; L < 3; ++L) {
+        if (!(layers & lbit[L])) continue;
+        for (int t = 0; t < D1; ++t) {
+            cplx v = layer_entry(lj, N, L, t, D1, m, n);
+            out[(long long)(slot * D1 + t) * nn2 + idx] = mk(-0.25 * v.im, 0.25 * v.re);
+        }
+        ++slot;
+    }
+}
+
+// ------------------------------------------------------------------ Hankel evaluation
+
+__global__ void k_hankel01(int n, const cplx* z, int complex_arg, cplx* h0, cplx* h1) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    cplx a, b;
+    if (complex_arg) hankel01_cplx(z[i], a, b);
+    else hankel01_real(z[i].re, a, b);
+    h0[i] = a;
+    h1[i] = b;
+}
+
+cudaError_t launch_hankel01(int n, const cplx* z, int complex_arg, cplx* h0, cplx* h1, cudaStream_t st) {
+    k_hankel01<<<(n + 127) / 128, 128, 0, st>>>(n, z, complex_arg, h0, h1);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ launchers
+
+template <int D, bool RK>
+static cudaError_t launch_local_t(const DevMesh& M, const SingularTask* tasks, int ntasks, const Job* jobs, int njobs,
+                                  cplx* loc, cudaStream_t st) {
+    long long npair = (long long)M.n * (M.n + 1) / 2;
+    long long nlow = (long long)M.n * (M.n - 1) / 2;
+    if (nlow > 0) {
+        dim3 g((unsigned)((nlow + 127) / 128), njobs);
+        k_general<D, RK><<<g, 128, 0, st>>>(M, jobs, loc, npair);
+    }
+    if (ntasks > 0) {
+        constexpr int NV = 4 * (D + 1) * 4 * 2;
+        size_t smem = (2 * (size_t)M.nc + 4 * NV) * sizeof(double);
+        dim3 g(ntasks, njobs);
+        k_singular<D, RK><<<g, 128, smem, st>>>(M, tasks, jobs, loc, npair);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_flags(const DevMesh& M, const SingularTask* tasks, int ntasks, uint8_t* flags, cudaStream_t st) {
+    long long npair = (long long)M.n * (M.n + 1) / 2;
+    k_flags_general<<<(unsigned)((npair + 127) / 128), 128, 0, st>>>(M, flags);
+    if (ntasks > 0) k_flags_singular<<<ntasks, 128, 0, st>>>(M, tasks, flags);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_local(const DevMesh& M, const SingularTask* tasks, int ntasks, const Job* jobs, int njobs,
+                         bool real_k, int d, cplx* loc, cudaStream_t st) {
+    if (real_k) {
+        if (d == 0) return launch_local_t<0, true>(M, tasks, ntasks, jobs, njobs, loc, st);
+        if (d == 1) return launch_local_t<1, true>(M, tasks, ntasks, jobs, njobs, loc, st);
+        return launch_local_t<2, true>(M, tasks, ntasks, jobs, njobs, loc, st);
+    }
+    if (d == 0) return launch_local_t<0, false>(M, tasks, ntasks, jobs, njobs, loc, st);
+    if (d == 1) return launch_local_t<1, false>(M, tasks, ntasks, jobs, njobs, loc, st);
+    return launch_local_t<2, false>(M, tasks, ntasks, jobs, njobs, loc, st);
+}
+
+cudaError_t launch_gather_T(int N, int d, const cplx* loc, const double* Mmass, int nk, cplx* T, cudaStream_t st) {
+    long long npair = (long long)N * (N + 1) / 2;
+    long long tot = 4LL * N * N;
+    dim3 g((unsigned)((tot + 255) / 256), nk);
+    k_gather_T<<<g, 256, 0, st>>>(N, d + 1, loc, npair, Mmass, T);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_layers(int N, int d, int layers, const cplx* loc, int job, cplx* out, cudaStream_t st) {
+    long long npair = (long long)N * (N + 1) / 2;
+    long long tot = (long long)N * N;
+    k_gather_layers<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(N, d + 1, layers, loc, npair, job, out);
+    return cudaGetLastError();
+}
+
+}  // namespace hbem

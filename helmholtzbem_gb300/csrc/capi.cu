@@ -1,0 +1,619 @@
+// C ABI implementation (include/hbem.h): handles, device memory, streams and the
+// host-side orchestration of the GPU kernels; host root finders.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/hbem.h"
+#include "assemble.cuh"
+
+namespace hbem {
+cudaError_t launch_flags(const DevMesh& M, const SingularTask* tasks, int ntasks, uint8_t* flags, cudaStream_t st);
+cudaError_t launch_local(const DevMesh& M, const SingularTask* tasks, int ntasks, const Job* jobs, int njobs,
+                         bool real_k, int d, cplx* loc, cudaStream_t st);
+cudaError_t launch_gather_T(int N, int d, const cplx* loc, const double* Mmass, int nk, cplx* T, cudaStream_t st);
+cudaError_t launch_gather_layers(int N, int d, int layers, const cplx* loc, int job, cplx* out, cudaStream_t st);
+cudaError_t launch_projection(int N, const double* id, const double* sb, const double* lr, cplx* T, int nmat,
+                              cudaStream_t st);
+cudaError_t launch_svd(int n, int nmat, int D, int which, const cplx* T, long long mat_stride, long long der_stride,
+                       cplx* gA, cplx* gV, double* out, double* sig_all, int* status, cudaStream_t st);
+cudaError_t launch_hankel01(int n, const cplx* z, int complex_arg, cplx* h0, cplx* h1, cudaStream_t st);
+}  // namespace hbem
+
+using namespace hbem;
+
+namespace {
+
+thread_local std::string g_err;
+int g_device = 0;
+const double kMachEps = 2.220446049250313e-16;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+#define HB_CK(x)                                                                                     \
+    do {                                                                                             \
+        cudaError_t e_ = (x);                                                                        \
+        if (e_ != cudaSuccess) return fail(HBEM_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// growable device buffer
+struct DBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e == cudaSuccess) cap = bytes;
+        return e;
+    }
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+template <class T>
+cudaError_t upload(DBuf& b, const std::vector<T>& v, cudaStream_t st) {
+    cudaError_t e = b.ensure(std::max<size_t>(1, v.size() * sizeof(T)));
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+}
+
+// ---------------------------------------------------------------- host quadrature
+
+// Gauss-Legendre nodes/weights on [a, b]: Newton on the three-term recurrence for
+// P_n from the Chebyshev-like initial guesses, nodes stored ascending
+// (the rule of include/gauleg.hpp:35-79).
+void gauss_legendre(double a, double b, int n, double* x, double* w) {
+    const int half = (n + 1) / 2;
+    const double mid = 0.5 * (a + b), len = 0.5 * (b - a);
+    for (int i = 0; i < half; ++i) {
+        double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), zold, pn = 0., dpn = 0.;
+        for (int it = 0; it < 100; ++it) {
+            double p0 = 1., p1 = 0.;
+            for (int k = 1; k <= n; ++k) {
+                double pm = p1;
+                p1 = p0;
+                p0 = ((2. * k - 1.) * z * p1 - (k - 1.) * pm) / k;
+            }
+            pn = p0;
+            dpn = n * (z * p0 - p1) / (z * z - 1.0);
+            zold = z;
+            z = zold - pn / dpn;
+            if (std::fabs(z - zold) <= kMachEps) break;
+        }
+        x[i] = mid - len * z;
+        x[n - 1 - i] = mid + len * z;
+        double wi = 2. * len / ((1. - z * z) * dpn * dpn);
+        w[i] = wi;
+        w[n - 1 - i] = wi;
+    }
+}
+
+// Graded composite rule on [0, 1]: levels [s^(l+1), s^l], s = (sqrt2 - 1)^2, with
+// Gauss orders n, n-1, ..., 2 from the top level down; n(n+1)/2 - 1 nodes,
+// ascending (include/gauleg.hpp:89-121).
+void graded_composite(int n, double* x, double* w) {
+    const int N = n * (n + 1) / 2 - 1;
+    const double sigma = (std::sqrt(2.) - 1.) * (std::sqrt(2.) - 1.);
+    double lo = sigma, hi = 1.;
+    int pos = N - 1;
+    std::vector<double> gx(n), gw(n);
+    for (int q = n; q >= 2; --q) {
+        gauss_legendre(0., 1., q, gx.data(), gw.data());
+        for (int j = q - 1; j >= 0; --j, --pos) {
+            w[pos] = (hi - lo) * gw[j];
+            x[pos] = (hi - lo) * gx[j] + lo;
+        }
+        hi = lo;
+        lo *= sigma;
+    }
+}
+
+// ---------------------------------------------------------------- host panel maps
+
+struct HPanel {
+    int kind;
+    const double* p;
+    // point on [0, 1] and its tangent / tangent norm
+    void at01(double t, cplx& pt, cplx& tan, double& tn) const {
+        if (kind == HBEM_PANEL_LINE) {
+            double dx = p[2] - p[0], dy = p[3] - p[1];
+            pt = mk(dx * t + p[0], dy * t + p[1]);
+            tan = mk(dx, dy);
+            tn = std::hypot(dx, dy);
+        } else {
+            double d = p[4] - p[3], th = t * d + p[3];
+            double c = std::cos(th), s = std::sin(th);
+            pt = mk(p[0] + p[2] * c, p[1] + p[2] * s);
+            tan = mk(-p[2] * d * s, p[2] * d * c);
+            tn = p[2] * std::fabs(d);
+        }
+    }
+    // point on [-1, 1] (the parametrisation used by the adjacency test)
+    cplx at11(double t) const {
+        if (kind == HBEM_PANEL_LINE)
+            return mk((t * (p[2] - p[0]) + (p[2] + p[0])) * 0.5, (t * (p[3] - p[1]) + (p[3] + p[1])) * 0.5);
+        double mean = (p[3] + p[4]) / 2., diff = (p[4] - p[3]) / 2.;
+        return mk(p[0] + p[2] * std::cos(t * diff + mean), p[1] + p[2] * std::sin(t * diff + mean));
+    }
+};
+
+double dist(cplx a, cplx b) { return std::hypot(a.re - b.re, a.im - b.im); }
+
+}  // namespace
+
+// ---------------------------------------------------------------- builder
+
+struct hbem_builder_s {
+    int n = 0, p = 0, nc = 0, qtest = 2, qtrial = 2, lines = 1, device = 0;
+    std::vector<int> kind;
+    std::vector<double> par, xg, wg, xc, wc;
+    std::vector<cplx> ends;
+    std::vector<SingularTask> tasks;
+    cudaStream_t st = nullptr;
+    DBuf d_kind, d_par, d_xg, d_wg, d_xc, d_wc, d_gpt, d_gtan, d_gtn, d_ends, d_flags, d_tasks;
+    DBuf d_loc, d_jobs, d_layers;
+    int asm_layers = 0, asm_d = -1;
+
+    long long npair() const { return (long long)n * (n + 1) / 2; }
+    DevMesh view() const {
+        DevMesh M;
+        M.n = n; M.p = p; M.nc = nc; M.lines = lines;
+        M.kind = d_kind.as<int>(); M.par = d_par.as<double>();
+        M.xg = d_xg.as<double>(); M.wg = d_wg.as<double>();
+        M.xc = d_xc.as<double>(); M.wc = d_wc.as<double>();
+        M.gpt = d_gpt.as<cplx>(); M.gtan = d_gtan.as<cplx>(); M.gtn = d_gtn.as<double>();
+        M.ends = d_ends.as<cplx>(); M.flags = d_flags.as<uint8_t>();
+        return M;
+    }
+    // BuilderData::is_adjacent (galerkin_builder.cpp:189-201)
+    bool adjacent(int i, int j, bool& swap) const {
+        const double e = 100. * kMachEps;
+        if (dist(ends[2 * i + 1], ends[2 * j]) < e) { swap = false; return true; }
+        if (dist(ends[2 * i], ends[2 * j + 1]) < e) { swap = true; return true; }
+        return false;
+    }
+    ~hbem_builder_s() {
+        for (DBuf* b : {&d_kind, &d_par, &d_xg, &d_wg, &d_xc, &d_wc, &d_gpt, &d_gtan, &d_gtn, &d_ends, &d_flags,
+                        &d_tasks, &d_loc, &d_jobs, &d_layers})
+            b->release();
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
+struct hbem_solop_s {
+    hbem_builder b = nullptr;
+    int proj = 1;
+    std::vector<double> M;    // N x N column-major
+    DBuf d_M, d_id, d_sb, d_lr, d_T, d_svdA, d_svdV, d_out, d_status, d_sig;
+    ~hbem_solop_s() {
+        for (DBuf* x : {&d_M, &d_id, &d_sb, &d_lr, &d_T, &d_svdA, &d_svdV, &d_out, &d_status, &d_sig}) x->release();
+    }
+};
+
+extern "C" {
+
+int hbem_version(void) { return 100; }
+
+const char* hbem_status_string(int s) {
+    switch (s) {
+        case HBEM_OK: return "ok";
+        case HBEM_ERR_INVALID: return "invalid argument";
+        case HBEM_ERR_CUDA: return "CUDA error";
+        case HBEM_ERR_NOMEM: return "out of device memory";
+        case HBEM_ERR_NOCONV: return "iteration limit reached";
+        case HBEM_ERR_SINGULAR: return "singular pivot";
+        case HBEM_ERR_NONFINITE: return "non-finite value";
+        case HBEM_ERR_UNSUPPORTED: return "unsupported";
+        default: return "unknown status";
+    }
+}
+
+const char* hbem_last_error(void) { return g_err.c_str(); }
+
+int hbem_set_device(int device) {
+    HB_CK(cudaSetDevice(device));
+    g_device = device;
+    return HBEM_OK;
+}
+
+int hbem_hankel01(int n, const double* z_host, int complex_arg, double* h0_host, double* h1_host) {
+    if (n < 1 || !z_host || !h0_host || !h1_host) return fail(HBEM_ERR_INVALID, "hankel01: bad argument");
+    HB_CK(cudaSetDevice(g_device));
+    static thread_local DBuf z, a, b;
+    const size_t bytes = (size_t)n * sizeof(cplx);
+    HB_CK(z.ensure(bytes));
+    HB_CK(a.ensure(bytes));
+    HB_CK(b.ensure(bytes));
+    std::vector<cplx> zz(n);
+    for (int i = 0; i < n; ++i) zz[i] = complex_arg ? mk(z_host[2 * i], z_host[2 * i + 1]) : mk(z_host[i], 0.);
+    HB_CK(cudaMemcpy(z.p, zz.data(), bytes, cudaMemcpyHostToDevice));
+    HB_CK(launch_hankel01(n, z.as<cplx>(), complex_arg, a.as<cplx>(), b.as<cplx>(), 0));
+    HB_CK(cudaMemcpy(h0_host, a.p, bytes, cudaMemcpyDeviceToHost));
+    HB_CK(cudaMemcpy(h1_host, b.p, bytes, cudaMemcpyDeviceToHost));
+    return HBEM_OK;
+}
+
+int hbem_builder_create(int npanels, const int* kinds, const double* params, int order, int q_test, int q_trial,
+                        hbem_builder* out) {
+    if (!out || !kinds || !params || npanels < 3 || order < 2 || order > 32)
+        return fail(HBEM_ERR_INVALID, "builder: need >= 3 panels and 2 <= order <= 32");
+    if (q_test != HBEM_SPACE_P1 || q_trial != HBEM_SPACE_P1)
+        return fail(HBEM_ERR_UNSUPPORTED, "builder: the GPU path assembles P1/P1 spaces");
+    for (int i = 0; i < npanels; ++i)
+        if (kinds[i] != HBEM_PANEL_LINE && kinds[i] != HBEM_PANEL_ARC) return fail(HBEM_ERR_INVALID, "builder: bad panel kind");
+    HB_CK(cudaSetDevice(g_device));
+    hbem_builder b = new hbem_builder_s();
+    b->device = g_device;
+    b->n = npanels; b->p = order; b->nc = order * (order + 1) / 2 - 1;
+    b->qtest = q_test; b->qtrial = q_trial;
+    b->kind.assign(kinds, kinds + npanels);
+    b->par.assign(params, params + 5 * (size_t)npanels);
+    b->lines = 1;
+    for (int k : b->kind) if (k != HBEM_PANEL_LINE) b->lines = 0;
+    b->xg.resize(order); b->wg.resize(order);
+    gauss_legendre(0., 1., order, b->xg.data(), b->wg.data());
+    b->xc.resize(b->nc); b->wc.resize(b->nc);
+    graded_composite(order, b->xc.data(), b->wc.data());
+    // geometry at the general nodes and panel end points
+    const int n = npanels, p = order;
+    std::vector<cplx> gpt((size_t)n * p), gtan((size_t)n * p);
+    std::vector<double> gtn((size_t)n * p);
+    b->ends.resize(2 * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+        HPanel P{b->kind[i], &b->par[5 * (size_t)i]};
+        for (int a = 0; a < p; ++a) P.at01(b->xg[a], gpt[(size_t)i * p + a], gtan[(size_t)i * p + a], gtn[(size_t)i * p + a]);
+        b->ends[2 * i] = P.at11(-1.);
+        b->ends[2 * i + 1] = P.at11(1.);
+    }
+    // pair classification (coincident / adjacent) -> singular task list, flag bit 7
+    std::vector<uint8_t> flags((size_t)b->npair(), 0);
+    for (int i = 0; i < n; ++i) {
+        b->tasks.push_back(SingularTask{i, i, PK_COINC, 0});
+        flags[tri_index(i, i)] = 0x80;
+        for (int j = 0; j < i; ++j) {
+            bool sw = false;
+            if (b->adjacent(i, j, sw)) {
+                b->tasks.push_back(SingularTask{i, j, PK_ADJ, sw ? 1 : 0});
+                flags[tri_index(i, j)] = 0x80;
+            }
+        }
+    }
+    cudaError_t e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = upload(b->d_kind, b->kind, b->st);
+    if (e == cudaSuccess) e = upload(b->d_par, b->par, b->st);
+    if (e == cudaSuccess) e = upload(b->d_xg, b->xg, b->st);
+    if (e == cudaSuccess) e = upload(b->d_wg, b->wg, b->st);
+    if (e == cudaSuccess) e = upload(b->d_xc, b->xc, b->st);
+    if (e == cudaSuccess) e = upload(b->d_wc, b->wc, b->st);
+    if (e == cudaSuccess) e = upload(b->d_gpt, gpt, b->st);
+    if (e == cudaSuccess) e = upload(b->d_gtan, gtan, b->st);
+    if (e == cudaSuccess) e = upload(b->d_gtn, gtn, b->st);
+    if (e == cudaSuccess) e = upload(b->d_ends, b->ends, b->st);
+    if (e == cudaSuccess) e = upload(b->d_flags, flags, b->st);
+    if (e == cudaSuccess) e = upload(b->d_tasks, b->tasks, b->st);
+    if (e == cudaSuccess) e = launch_flags(b->view(), b->d_tasks.as<SingularTask>(), (int)b->tasks.size(),
+                                           b->d_flags.as<uint8_t>(), b->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+    if (e != cudaSuccess) {
+        std::string msg = cudaGetErrorString(e);
+        delete b;
+        return fail(e == cudaErrorMemoryAllocation ? HBEM_ERR_NOMEM : HBEM_ERR_CUDA, "builder: " + msg);
+    }
+    *out = b;
+    return HBEM_OK;
+}
+
+int hbem_builder_destroy(hbem_builder b) {
+    delete b;
+    return HBEM_OK;
+}
+
+int hbem_builder_info(hbem_builder b, int* npanels, int* dim_test, int* dim_trial, int* order, int* lines) {
+    if (!b) return fail(HBEM_ERR_INVALID, "null builder");
+    if (npanels) *npanels = b->n;
+    if (dim_test) *dim_test = b->n;
+    if (dim_trial) *dim_trial = b->n;
+    if (order) *order = b->p;
+    if (lines) *lines = b->lines;
+    return HBEM_OK;
+}
+
+int hbem_builder_is_adjacent(hbem_builder b, int i, int j, int* adjacent, int* swap) {
+    if (!b || i < 0 || j < 0 || i >= b->n || j >= b->n) return fail(HBEM_ERR_INVALID, "is_adjacent: bad index");
+    bool sw = false;
+    bool a = b->adjacent(i, j, sw);
+    if (adjacent) *adjacent = a;
+    if (swap) *swap = sw;
+    return HBEM_OK;
+}
+
+static int check_kc(double k_im, double c) {
+    if (!(c >= 1.)) return fail(HBEM_ERR_INVALID, "Refraction index must not be smaller than 1");
+    if (k_im < 0.) return fail(HBEM_ERR_INVALID, "Wavenumber does not meet conditions for uniqueness of the solution (Im(k) >= 0)");
+    return HBEM_OK;
+}
+
+int hbem_assemble_dense(hbem_builder b, double k_re, double k_im, double c, unsigned layers, unsigned d) {
+    if (!b) return fail(HBEM_ERR_INVALID, "null builder");
+    if (int r = check_kc(k_im, c)) return r;
+    if (d > 2) return fail(HBEM_ERR_INVALID, "Invalid order of derivative");
+    if (layers == 0 || layers > 7) return fail(HBEM_ERR_INVALID, "bad layer mask");
+    HB_CK(cudaSetDevice(b->device));
+    const long long np = b->npair();
+    const size_t loc_bytes = (size_t)np * (d + 1) * kLocPerD * sizeof(cplx);
+    HB_CK(b->d_loc.ensure(loc_bytes));
+    std::vector<Job> jobs{Job{k_re, k_im, c}};
+    HB_CK(upload(b->d_jobs, jobs, b->st));
+    int nl = ((layers & 1) != 0) + ((layers & 2) != 0) + ((layers & 4) != 0);
+    HB_CK(b->d_layers.ensure((size_t)nl * (d + 1) * b->n * b->n * sizeof(cplx)));
+    bool real_k = (k_im == 0. && k_re > 0.);
+    HB_CK(launch_local(b->view(), b->d_tasks.as<SingularTask>(), (int)b->tasks.size(), b->d_jobs.as<Job>(), 1, real_k,
+                       (int)d, b->d_loc.as<cplx>(), b->st));
+    HB_CK(launch_gather_layers(b->n, (int)d, (int)layers, b->d_loc.as<cplx>(), 0, b->d_layers.as<cplx>(), b->st));
+    HB_CK(cudaStreamSynchronize(b->st));
+    b->asm_layers = (int)layers;
+    b->asm_d = (int)d;
+    return HBEM_OK;
+}
+
+static int layer_slot(hbem_builder b, unsigned layer, unsigned d, size_t* off) {
+    if (!b) return fail(HBEM_ERR_INVALID, "null builder");
+    if (d > 2 || (int)d > b->asm_d) return fail(HBEM_ERR_INVALID, "Invalid order of derivative");
+    if (layer != HBEM_LAYER_DOUBLE && layer != HBEM_LAYER_SINGLE && layer != HBEM_LAYER_HYPERSINGULAR)
+        return fail(HBEM_ERR_INVALID, "bad layer");
+    if (!(b->asm_layers & (int)layer)) return fail(HBEM_ERR_INVALID, "Requested layer is not computed, so cannot be retrieved");
+    // slots in the order K, W, V
+    int slot = 0;
+    const int order[3] = {HBEM_LAYER_DOUBLE, HBEM_LAYER_HYPERSINGULAR, HBEM_LAYER_SINGLE};
+    for (int L : order) {
+        if ((unsigned)L == layer) break;
+        if (b->asm_layers & L) ++slot;
+    }
+    *off = ((size_t)slot * (b->asm_d + 1) + d) * b->n * b->n;
+    return HBEM_OK;
+}
+
+int hbem_get_layer(hbem_builder b, unsigned layer, unsigned d, double* host_out) {
+    size_t off;
+    if (int r = layer_slot(b, layer, d, &off)) return r;
+    if (!host_out) return fail(HBEM_ERR_INVALID, "null output");
+    HB_CK(cudaMemcpy(host_out, b->d_layers.as<cplx>() + off, (size_t)b->n * b->n * sizeof(cplx), cudaMemcpyDeviceToHost));
+    return HBEM_OK;
+}
+
+int hbem_get_layer_device(hbem_builder b, unsigned layer, unsigned d, const void** dev_ptr) {
+    size_t off;
+    if (int r = layer_slot(b, layer, d, &off)) return r;
+    if (!dev_ptr) return fail(HBEM_ERR_INVALID, "null output");
+    *dev_ptr = b->d_layers.as<cplx>() + off;
+    return HBEM_OK;
+}
+
+// ---------------------------------------------------------------- solutions operator
+
+int hbem_solop_create(hbem_builder b, int proj, hbem_solop* out) {
+    if (!b || !out) return fail(HBEM_ERR_INVALID, "null argument");
+    HB_CK(cudaSetDevice(b->device));
+    const int N = b->n;
+    hbem_solop s = new hbem_solop_s();
+    s->b = b;
+    s->proj = proj ? 1 : 0;
+    // mass matrix (mass_matrix.cpp:6-47): 2*max(q) Gauss points for line meshes, the
+    // builder's order otherwise (gen_sol_op.cpp:29-32)
+    const int mo = b->lines ? 2 * std::max(b->qtest, b->qtrial) : b->p;
+    std::vector<double> x(mo), w(mo);
+    gauss_legendre(0., 1., mo, x.data(), w.data());
+    s->M.assign((size_t)N * N, 0.);
+    for (int i = 0; i < N; ++i) {
+        HPanel P{b->kind[i], &b->par[5 * (size_t)i]};
+        for (int ii = 0; ii < 2; ++ii)
+            for (int jj = 0; jj < 2; ++jj) {
+                int II = ii == 0 ? (i + 1) % N : i, JJ = jj == 0 ? (i + 1) % N : i;
+                double sum = 0.;
+                for (int k = 0; k < mo; ++k) {
+                    cplx pt, tan;
+                    double tn;
+                    P.at01(x[k], pt, tan, tn);
+                    double F = (jj == 0 ? x[k] : 1. - x[k]) * tn, G = ii == 0 ? x[k] : 1. - x[k];
+                    sum = sum + w[k] * F * G;
+                }
+                s->M[II + (size_t)JJ * N] += sum;
+            }
+    }
+    cudaError_t e = upload(s->d_M, s->M, b->st);
+    if (e == cudaSuccess && s->proj) {
+        // Cholesky of the cyclic tridiagonal M: bidiagonal + dense last row
+        std::vector<double> id(N), sb(N, 0.), lr(N, 0.);
+        auto Mv = [&](int r, int c) { return s->M[r + (size_t)c * N]; };
+        double last_prev = 0., sub_prev = 0.;
+        bool ok = true;
+        for (int i = 0; i < N - 1; ++i) {
+            double dd = Mv(i, i) - (i > 0 ? sub_prev * sub_prev : 0.);
+            if (!(dd > 0.)) { ok = false; break; }
+            double di = std::sqrt(dd);
+            id[i] = 1. / di;
+            double sub = (i + 1 < N - 1) ? Mv(i + 1, i) / di : 0.;
+            double l = (Mv(N - 1, i) - (i > 0 ? last_prev * sub_prev : 0.)) / di;
+            lr[i] = l;
+            if (i + 1 < N - 1) sb[i] = sub;
+            else sb[i] = l;   // L[N-1][N-2] is part of the last row
+            last_prev = l;
+            sub_prev = sub;
+        }
+        if (ok) {
+            double dd = Mv(N - 1, N - 1);
+            for (int i = 0; i < N - 1; ++i) dd -= lr[i] * lr[i];
+            if (!(dd > 0.)) ok = false;
+            else id[N - 1] = 1. / std::sqrt(dd);
+        }
+        if (!ok) {
+            delete s;
+            return fail(HBEM_ERR_SINGULAR, "mass matrix is not positive definite");
+        }
+        e = upload(s->d_id, id, b->st);
+        if (e == cudaSuccess) e = upload(s->d_sb, sb, b->st);
+        if (e == cudaSuccess) e = upload(s->d_lr, lr, b->st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+    if (e != cudaSuccess) {
+        delete s;
+        return fail(HBEM_ERR_CUDA, std::string("solop: ") + cudaGetErrorString(e));
+    }
+    *out = s;
+    return HBEM_OK;
+}
+
+int hbem_solop_destroy(hbem_solop s) {
+    delete s;
+    return HBEM_OK;
+}
+
+int hbem_mass_matrix(hbem_solop s, double* host_out) {
+    if (!s || !host_out) return fail(HBEM_ERR_INVALID, "null argument");
+    std::memcpy(host_out, s->M.data(), s->M.size() * sizeof(double));
+    return HBEM_OK;
+}
+
+// T(k) (+ derivatives) for nk wavenumbers into T_dev [nk][d+1][2N][2N]; k_host may be complex
+// (interleaved) when kim_host != NULL.
+static int gen_T_batch(hbem_solop s, const double* k_host, const double* kim_host, int nk, double c_o, double c_i,
+                       unsigned d, cplx* T_dev) {
+    hbem_builder b = s->b;
+    const int N = b->n;
+    const long long np = b->npair();
+    const size_t per_job = (size_t)np * (d + 1) * kLocPerD * sizeof(cplx);
+    // bound the pair-local scratch to 4 GiB per launch group
+    int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)nk, ((size_t)4 << 30) / (2 * per_job)));
+    const size_t mat = 4ULL * N * N;
+    for (int k0 = 0; k0 < nk; k0 += chunk) {
+        int kn = std::min(chunk, nk - k0);
+        std::vector<Job> jobs;
+        bool real_k = true;
+        for (int q = 0; q < kn; ++q) {
+            double kr = k_host[k0 + q], ki = kim_host ? kim_host[k0 + q] : 0.;
+            if (int r = check_kc(ki, c_i)) return r;
+            if (int r = check_kc(ki, c_o)) return r;
+            if (!(ki == 0. && kr > 0.)) real_k = false;
+            jobs.push_back(Job{kr, ki, c_i});
+            jobs.push_back(Job{kr, ki, c_o});
+        }
+        HB_CK(upload(b->d_jobs, jobs, b->st));
+        HB_CK(b->d_loc.ensure(per_job * 2 * kn));
+        HB_CK(launch_local(b->view(), b->d_tasks.as<SingularTask>(), (int)b->tasks.size(), b->d_jobs.as<Job>(), 2 * kn,
+                           real_k, (int)d, b->d_loc.as<cplx>(), b->st));
+        cplx* Tk = T_dev + (size_t)k0 * (d + 1) * mat;
+        HB_CK(launch_gather_T(N, (int)d, b->d_loc.as<cplx>(), s->d_M.as<double>(), kn, Tk, b->st));
+        if (s->proj)
+            HB_CK(launch_projection(N, s->d_id.as<double>(), s->d_sb.as<double>(), s->d_lr.as<double>(), Tk,
+                                    kn * (int)(d + 1), b->st));
+    }
+    return HBEM_OK;
+}
+
+int hbem_gen_sol_op(hbem_solop s, double k_re, double k_im, double c_o, double c_i, unsigned d, double* T_host) {
+    if (!s || !T_host) return fail(HBEM_ERR_INVALID, "null argument");
+    if (d > 2) return fail(HBEM_ERR_INVALID, "Invalid order of derivative");
+    hbem_builder b = s->b;
+    HB_CK(cudaSetDevice(b->device));
+    const size_t mat = 4ULL * b->n * b->n;
+    HB_CK(s->d_T.ensure((d + 1) * mat * sizeof(cplx)));
+    if (int r = gen_T_batch(s, &k_re, &k_im, 1, c_o, c_i, d, s->d_T.as<cplx>())) return r;
+    HB_CK(cudaMemcpyAsync(T_host, s->d_T.p, (d + 1) * mat * sizeof(cplx), cudaMemcpyDeviceToHost, b->st));
+    HB_CK(cudaStreamSynchronize(b->st));
+    return HBEM_OK;
+}
+
+int hbem_gen_sol_op_batch_device(hbem_solop s, const double* k_host, int nk, double c_o, double c_i, unsigned d,
+                                 void* T_dev) {
+    if (!s || !k_host || !T_dev || nk < 1) return fail(HBEM_ERR_INVALID, "bad argument");
+    if (d > 2) return fail(HBEM_ERR_INVALID, "Invalid order of derivative");
+    HB_CK(cudaSetDevice(s->b->device));
+    if (int r = gen_T_batch(s, k_host, nullptr, nk, c_o, c_i, d, static_cast<cplx*>(T_dev))) return r;
+    HB_CK(cudaStreamSynchronize(s->b->st));
+    return HBEM_OK;
+}
+
+// ---------------------------------------------------------------- singular values
+
+static int sv_batch(cudaStream_t st, int n, int nmat, unsigned d, const cplx* T, long long mat_stride,
+                    long long der_stride, DBuf& A, DBuf& V, DBuf& out, DBuf& status, DBuf* sig, double* out_host,
+                    double* sig_all_host) {
+    const size_t nn = (size_t)n * n;
+    HB_CK(V.ensure((size_t)nmat * nn * sizeof(cplx)));
+    HB_CK(A.ensure(n > 100 ? (size_t)nmat * nn * sizeof(cplx) : sizeof(cplx)));
+    HB_CK(out.ensure((size_t)nmat * 3 * sizeof(double)));
+    HB_CK(status.ensure((size_t)nmat * sizeof(int)));
+    double* dsig = nullptr;
+    if (sig_all_host) {
+        HB_CK(sig->ensure((size_t)nmat * n * sizeof(double)));
+        dsig = sig->as<double>();
+    }
+    HB_CK(launch_svd(n, nmat, (int)d, 0, T, mat_stride, der_stride, A.as<cplx>(), V.as<cplx>(), out.as<double>(), dsig,
+                     status.as<int>(), st));
+    HB_CK(cudaMemcpyAsync(out_host, out.p, (size_t)nmat * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (sig_all_host)
+        HB_CK(cudaMemcpyAsync(sig_all_host, dsig, (size_t)nmat * n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    std::vector<int> stat(nmat);
+    HB_CK(cudaMemcpyAsync(stat.data(), status.p, (size_t)nmat * sizeof(int), cudaMemcpyDeviceToHost, st));
+    HB_CK(cudaStreamSynchronize(st));
+    for (int v : stat)
+        if (v) return fail(HBEM_ERR_NOCONV, "Jacobi SVD: sweep limit reached");
+    return HBEM_OK;
+}
+
+int hbem_sv_dense_batch_device(int n, int nmat, unsigned d, const void* T_dev, long long mat_stride,
+                               long long der_stride, double* out_host, double* sig_all_host) {
+    if (n < 2 || nmat < 1 || !T_dev || !out_host || d > 2) return fail(HBEM_ERR_INVALID, "bad argument");
+    HB_CK(cudaSetDevice(g_device));
+    static thread_local DBuf A, V, out, status, sig;
+    return sv_batch(0, n, nmat, d, static_cast<const cplx*>(T_dev), mat_stride, der_stride, A, V, out, status, &sig,
+                    out_host, sig_all_host);
+}
+
+int hbem_sv_dense_batch(int n, int nmat, unsigned d, const double* T_host, double* out_host, double* sig_all_host) {
+    if (n < 2 || nmat < 1 || !T_host || !out_host || d > 2) return fail(HBEM_ERR_INVALID, "bad argument");
+    HB_CK(cudaSetDevice(g_device));
+    static thread_local DBuf T, A, V, out, status, sig;
+    const size_t nn = (size_t)n * n, bytes = (size_t)nmat * (d + 1) * nn * sizeof(cplx);
+    HB_CK(T.ensure(bytes));
+    HB_CK(cudaMemcpy(T.p, T_host, bytes, cudaMemcpyHostToDevice));
+    return sv_batch(0, n, nmat, d, T.as<cplx>(), (long long)((d + 1) * nn), (long long)nn, A, V, out, status, &sig,
+                    out_host, sig_all_host);
+}
+
+int hbem_sweep_sigma(hbem_solop s, const double* k_host, int nk, double c_o, double c_i, unsigned d, double* out_host) {
+    if (!s || !k_host || !out_host || nk < 1 || d > 2) return fail(HBEM_ERR_INVALID, "bad argument");
+    hbem_builder b = s->b;
+    HB_CK(cudaSetDevice(b->device));
+    const int n = 2 * b->n;
+    const size_t mat = (size_t)n * n;
+    // bound the T batch to ~2 GiB
+    int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)nk, ((size_t)2 << 30) / ((d + 1) * mat * sizeof(cplx))));
+    HB_CK(s->d_T.ensure((size_t)chunk * (d + 1) * mat * sizeof(cplx)));
+    for (int k0 = 0; k0 < nk; k0 += chunk) {
+        int kn = std::min(chunk, nk - k0);
+        if (int r = gen_T_batch(s, k_host + k0, nullptr, kn, c_o, c_i, d, s->d_T.as<cplx>())) return r;
+        if (int r = sv_batch(b->st, n, kn, d, s->d_T.as<cplx>(), (long long)(d + 1) * mat, (long long)mat, s->d_svdA,
+                             s->d_svdV, s->d_out, s->d_status, nullptr, out_host + 3LL * k0, nullptr))
+            return r;
+    }
+    return HBEM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,53 @@
+"""Generate hankel_tables.h: monomial coefficients for the large-argument Bessel
+amplitudes used by the device Hankel routine.
+
+For x >= 8 the device writes (DLMF 10.17)
+    H_nu(x) = (x pi)^(-1/2) * [(P_nu + i Q_nu) (sin x +- cos x) combinations]
+with, in w = 64/x^2 in (0, 1],
+    P_0 = 1 + F0(w),  x Q_0 = -1/8 + G0(w),  P_1 = 1 + F1(w),  x Q_1 = 3/8 + G1(w),
+F*, G* polynomials of degree DEG (least squares on Chebyshev points, samples from
+mpmath at 40 digits), evaluated by Horner's rule.  Absolute error < 3e-18 on (0,1].
+
+Usage (from the repository root):
+    python helmholtzbem_gb300/csrc/gen_hankel_tables.py > helmholtzbem_gb300/csrc/hankel_tables.h
+"""
+import mpmath as mp
+import numpy as np
+
+mp.mp.dps = 40
+DEG = 14
+M = 64
+
+
+def targets(w):
+    x = 8 / mp.sqrt(mp.mpf(w))
+    out = []
+    for nu in (0, 1):
+        J, Y = mp.besselj(nu, x), mp.bessely(nu, x)
+        chi = x - (2 * nu + 1) * mp.pi / 4
+        s = mp.sqrt(mp.pi * x / 2)
+        P = s * (J * mp.cos(chi) + Y * mp.sin(chi))
+        Q = s * (Y * mp.cos(chi) - J * mp.sin(chi))
+        out += [P - 1, x * Q + (mp.mpf(1) / 8 if nu == 0 else -mp.mpf(3) / 8)]
+    return out
+
+
+def main():
+    k = np.arange(M)
+    y = -np.cos(np.pi * (k + 0.5) / M)
+    wn = (y + 1) / 2
+    vals = np.array([[float(v) for v in targets(w)] for w in wn])
+    print("/* generated by gen_hankel_tables.py -- monomial coefficients in w = 64/x^2, lowest first */")
+    print("#pragma once")
+    print("#define HBEM_PQ_DEG %d" % DEG)
+    for name, c in zip(["HBEM_F0", "HBEM_G0", "HBEM_F1", "HBEM_G1"], range(4)):
+        cf = np.polynomial.chebyshev.chebfit(y, vals[:, c], DEG)
+        mono = np.polynomial.chebyshev.cheb2poly(cf)
+        P = np.polynomial.Polynomial(mono)(np.polynomial.Polynomial([-1.0, 2.0]))
+        print("static __device__ __constant__ double %s[%d] = {" % (name, DEG + 1))
+        print(",\n".join("  %.17e" % v for v in P.coef))
+        print("};")
+
+
+if __name__ == "__main__":
+    main()

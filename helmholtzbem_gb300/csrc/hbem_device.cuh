@@ -1,0 +1,224 @@
+// Device-side building blocks: a small complex<double> type and the Hankel
+// functions H0^(1), H1^(1) for real and complex argument.
+#pragma once
+#include <cuda_runtime.h>
+#include <math_constants.h>
+
+#include "hankel_tables.h"
+
+namespace hbem {
+
+struct cplx {
+    double re, im;
+};
+
+__host__ __device__ __forceinline__ cplx mk(double r, double i = 0.) { cplx z; z.re = r; z.im = i; return z; }
+__host__ __device__ __forceinline__ cplx operator+(cplx a, cplx b) { return mk(a.re + b.re, a.im + b.im); }
+__host__ __device__ __forceinline__ cplx operator-(cplx a, cplx b) { return mk(a.re - b.re, a.im - b.im); }
+__host__ __device__ __forceinline__ cplx operator-(cplx a) { return mk(-a.re, -a.im); }
+__host__ __device__ __forceinline__ cplx operator*(cplx a, cplx b) {
+    return mk(fma(a.re, b.re, -a.im * b.im), fma(a.re, b.im, a.im * b.re));
+}
+__host__ __device__ __forceinline__ cplx operator*(double s, cplx a) { return mk(s * a.re, s * a.im); }
+__host__ __device__ __forceinline__ cplx operator*(cplx a, double s) { return mk(s * a.re, s * a.im); }
+__host__ __device__ __forceinline__ cplx& operator+=(cplx& a, cplx b) { a.re += b.re; a.im += b.im; return a; }
+__host__ __device__ __forceinline__ cplx& operator-=(cplx& a, cplx b) { a.re -= b.re; a.im -= b.im; return a; }
+__host__ __device__ __forceinline__ cplx conj(cplx a) { return mk(a.re, -a.im); }
+__host__ __device__ __forceinline__ double norm2(cplx a) { return fma(a.re, a.re, a.im * a.im); }
+__device__ __forceinline__ double cabs(cplx a) { return hypot(a.re, a.im); }
+__device__ __forceinline__ cplx cdiv(cplx a, cplx b) {
+    double d = 1.0 / norm2(b);
+    return mk((a.re * b.re + a.im * b.im) * d, (a.im * b.re - a.re * b.im) * d);
+}
+// acc += s * z  (s real)
+__device__ __forceinline__ void axpy(cplx& acc, double s, cplx z) {
+    acc.re = fma(s, z.re, acc.re);
+    acc.im = fma(s, z.im, acc.im);
+}
+__device__ __forceinline__ cplx cexp_i(double t) { double s, c; sincos(t, &s, &c); return mk(c, s); }
+__device__ __forceinline__ cplx clog(cplx z) { return mk(log(hypot(z.re, z.im)), atan2(z.im, z.re)); }
+__device__ __forceinline__ cplx csqrt(cplx z) {
+    double r = hypot(z.re, z.im);
+    if (r == 0.) return mk(0., 0.);
+    double t = sqrt(0.5 * (r + fabs(z.re)));
+    if (z.re >= 0.) return mk(t, 0.5 * z.im / t);
+    return mk(0.5 * fabs(z.im) / t, z.im >= 0. ? t : -t);
+}
+__device__ __forceinline__ cplx cexp(cplx z) { double e = exp(z.re), s, c; sincos(z.im, &s, &c); return mk(e * c, e * s); }
+
+constexpr double kEps = 2.220446049250313e-16;
+constexpr double kEulerGamma = 0.57721566490153286061;
+constexpr double kPi = 3.14159265358979323846;
+
+// ---------------------------------------------------------------- real argument
+//
+// H0 = J0 + i Y0, H1 = J1 + i Y1 for real x, with the branch structure of the
+// reference's vectorised evaluator (Hankel1Real01::jy_01, cbessel.cpp:1858-1997):
+//   x <= 0        J0 = 1, everything else 0
+//   x < 1e-8      limiting forms (DLMF 10.7.2-4)
+//   x < 8         ascending series with harmonic numbers (DLMF 10.8.1-2)
+//   x <= 1e6      modulus/phase amplitudes P, Q in w = 64/x^2 (DLMF 10.17),
+//                 phases through sin x +- cos x so the argument is used exactly
+//   x > 1e6       leading-order asymptotic form (DLMF 10.17.3, first term)
+__device__ __forceinline__ double horner_pq(const double* c, double w) {
+    double r = c[HBEM_PQ_DEG];
+#pragma unroll
+    for (int k = HBEM_PQ_DEG - 1; k >= 0; --k) r = fma(r, w, c[k]);
+    return r;
+}
+
+static __device__ __noinline__ void hankel01_real(double x, cplx& h0, cplx& h1) {
+    double j0, j1, y0, y1;
+    if (x <= 0.) {
+        h0 = mk(1., 0.); h1 = mk(0., 0.);
+        return;
+    }
+    if (x < 1e-8) {
+        j0 = 1.; j1 = 0.5 * x;
+        y0 = (2. / kPi) * (log(j1) + kEulerGamma);
+        y1 = -(2. / kPi) / x;
+    } else if (x < 8.) {
+        double x2_4 = 0.25 * x * x, t = 1., Hk = 0., k = 1.;
+        j0 = 1.; j1 = 1.; y0 = 0.; y1 = 0.;
+        // terms t_k = (-x^2/4)^k/(k!)^2; stop once H_k |t_k| <= eps (at most 40 terms for x < 8)
+        for (int it = 0; it < 60; ++it) {
+            t *= -x2_4 / (k * k);
+            Hk += 1.0 / k;
+            j0 += t;
+            y0 = fma(-Hk, t, y0);
+            k += 1.0;
+            double ik = 1.0 / k;
+            j1 = fma(t, ik, j1);
+            y1 = fma(-Hk * ik, t, y1);
+            if (Hk * fabs(t) <= kEps) break;
+        }
+        j1 *= 0.5 * x;
+        double lg = log(0.5 * x) + kEulerGamma;
+        y0 = (2. / kPi) * fma(lg, j0, y0);
+        y1 = (1. / kPi) * (y1 * x + 2.0 * (lg * j1 + (j0 - 2.0) / x));
+    } else if (x <= 1e6) {
+        double ix = 1.0 / x, w = 64. * ix * ix;
+        double P0 = 1. + horner_pq(HBEM_F0, w);
+        double Q0 = (horner_pq(HBEM_G0, w) - 0.125) * ix;
+        double P1 = 1. + horner_pq(HBEM_F1, w);
+        double Q1 = (horner_pq(HBEM_G1, w) + 0.375) * ix;
+        double sx, cx;
+        sincos(x, &sx, &cx);
+        double r = rsqrt(kPi * x);
+        double cc = (sx + cx) * r, ss = (sx - cx) * r;
+        j0 = P0 * cc - Q0 * ss;
+        y0 = P0 * ss + Q0 * cc;
+        j1 = P1 * ss + Q1 * cc;
+        y1 = Q1 * ss - P1 * cc;
+    } else {
+        double r = sqrt(2. / (kPi * x)), s0, c0, s1, c1;
+        sincos(x - 0.25 * kPi, &s0, &c0);
+        sincos(x - 0.75 * kPi, &s1, &c1);
+        j0 = r * c0; y0 = r * s0; j1 = r * c1; y1 = r * s1;
+    }
+    h0 = mk(j0, y0);
+    h1 = mk(j1, y1);
+}
+
+// ---------------------------------------------------------------- complex argument
+//
+// H0, H1 for complex z (the reference calls an Amos-method routine,
+// cbessel.cpp:1210-1287).  Published methods of that family:
+//   |z| <= 2       ascending series (principal log)
+//   2 < |z| < 20   Miller's backward recurrence for J_n normalised by
+//                  J0 + 2 sum J_2k = 1, with Neumann's series for Y0 and its
+//                  derivative for Y1, all accumulated during the recurrence
+//   |z| >= 20      Hankel's asymptotic expansion (DLMF 10.17.5)
+// Non-finite values are replaced by 0 (galerkin_builder.cpp:216-235).
+static __device__ __noinline__ void hankel01_cplx(cplx z, cplx& h0, cplx& h1) {
+    const cplx I = mk(0., 1.);
+    double az = hypot(z.re, z.im);
+    cplx j0, j1, y0, y1;
+    if (az == 0.) {
+        h0 = mk(0., 0.); h1 = mk(0., 0.);
+        return;
+    }
+    if (az <= 2.) {
+        cplx x2_4 = 0.25 * (z * z), t = mk(1.);
+        double Hk = 0., k = 1.;
+        j0 = mk(1.); j1 = mk(1.); y0 = mk(0.); y1 = mk(0.);
+        for (int it = 0; it < 60; ++it) {
+            t = t * x2_4 * (-1.0 / (k * k));
+            Hk += 1.0 / k;
+            j0 += t;
+            y0 -= Hk * t;
+            k += 1.0;
+            j1 += t * (1.0 / k);
+            y1 -= (Hk / k) * t;
+            if (Hk * hypot(t.re, t.im) <= 0.1 * kEps) break;
+        }
+        j1 = j1 * (0.5 * z);
+        cplx lg = clog(0.5 * z) + mk(kEulerGamma);
+        y0 = (2. / kPi) * (y0 + lg * j0);
+        y1 = (1. / kPi) * (y1 * z + 2.0 * (lg * j1 + cdiv(j0 - mk(2.0), z)));
+    } else if (az < 20.) {
+        int nstart = 2 * (int)((az + 40.) * 0.5);
+        cplx iz2 = cdiv(mk(2.), z);           // 2/z
+        cplx Jn1 = mk(0.), Jn = mk(1e-30);    // J_{n+1}, J_n (unnormalised)
+        cplx S = mk(0.), sy0 = mk(0.), sy1 = mk(0.);
+
+        // walk n = nstart .. 1 computing J_{n-1}; accumulate sums on the fly
+        // even indices contribute to S and sy0; odd ones feed sy1
+
+        for (int n = nstart; n >= 1; --n) {
+            cplx Jm1 = (double)n * (iz2 * Jn) - Jn1;   // J_{n-1}
+            // J_n is known here: use it
+            if ((n & 1) == 0) {
+                int kk = n / 2;
+                double sg = (kk & 1) ? -1. : 1.;
+                S += 2.0 * Jn;
+                sy0 += (sg / kk) * Jn;
+                // (J_{2k-1} - J_{2k+1})/k with J_{2k-1} = Jm1, J_{2k+1} = Jn1
+                sy1 += (sg / kk) * (Jm1 - Jn1);
+            }
+            Jn1 = Jn;
+            Jn = Jm1;
+            double mag = fabs(Jn.re) + fabs(Jn.im);
+            if (mag > 1e200) {
+                Jn = 1e-200 * Jn; Jn1 = 1e-200 * Jn1;
+                S = 1e-200 * S; sy0 = 1e-200 * sy0; sy1 = 1e-200 * sy1;
+            }
+        }
+
+        // now Jn = J_0, Jn1 = J_1 (unnormalised)
+        S += Jn;
+        cplx iS = cdiv(mk(1.), S);
+        j0 = Jn * iS; j1 = Jn1 * iS;
+        sy0 = sy0 * iS; sy1 = sy1 * iS;
+        cplx lg = clog(0.5 * z) + mk(kEulerGamma);
+        y0 = (2. / kPi) * (lg * j0) - (4. / kPi) * sy0;
+        y1 = (2. / kPi) * (lg * j1) - (2. / kPi) * cdiv(j0, z) + (2. / kPi) * sy1;
+    } else {
+        cplx s[2];
+        cplx iz = cdiv(mk(1.), z);
+        for (int nu = 0; nu < 2; ++nu) {
+            double mu = 4. * nu * nu;
+            cplx sum = mk(1.), term = mk(1.);
+            for (int k = 1; k < 200; ++k) {
+                double a = (mu - (2. * k - 1.) * (2. * k - 1.)) / (k * 8.);
+                term = term * (a * (I * iz));
+                sum += term;
+                if (hypot(term.re, term.im) < 0.25 * kEps) break;
+            }
+            s[nu] = sum;
+        }
+        cplx r = csqrt(cdiv(mk(2. / kPi), z));
+        h0 = r * cexp(I * (z - mk(0.25 * kPi))) * s[0];
+        h1 = r * cexp(I * (z - mk(0.75 * kPi))) * s[1];
+        j0 = h0; j1 = h1; y0 = mk(0.); y1 = mk(0.);
+        if (!isfinite(h0.re) || !isfinite(h0.im)) h0 = mk(0.);
+        if (!isfinite(h1.re) || !isfinite(h1.im)) h1 = mk(0.);
+        return;
+    }
+    h0 = j0 + I * y0;
+    h1 = j1 + I * y1;
+    if (!isfinite(h0.re) || !isfinite(h0.im)) h0 = mk(0.);
+    if (!isfinite(h1.re) || !isfinite(h1.im)) h1 = mk(0.);
+}
+
+}  // namespace hbem

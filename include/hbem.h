@@ -1,0 +1,151 @@
+/*
+ * hbem.h -- C ABI of the GB300 HelmholtzBEM assembly-and-resonance path.
+ *
+ * Plain C: opaque handles, pointers and sizes, int status codes, no exceptions
+ * and no C++ / torch types.  Complex matrices are column-major arrays of
+ * interleaved (re, im) doubles, the layout of Eigen::MatrixXcd.  Unless a name
+ * ends in _device, pointers are host pointers and the call copies.
+ *
+ * Each entry point names the reference interface it replaces
+ * (paths inside marohnicluka/HelmholtzBEM).  Handles are not thread-safe: use
+ * one handle per host thread; every handle owns one CUDA stream.
+ */
+#ifndef HBEM_H
+#define HBEM_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+enum {
+    HBEM_OK = 0,
+    HBEM_ERR_INVALID = 1,      /* bad argument (the reference throws std::runtime_error / out_of_range) */
+    HBEM_ERR_CUDA = 2,         /* CUDA runtime error */
+    HBEM_ERR_NOMEM = 3,        /* device allocation failed */
+    HBEM_ERR_NOCONV = 4,       /* an iteration hit its cap (Jacobi sweeps, Newton) */
+    HBEM_ERR_SINGULAR = 5,     /* zero pivot */
+    HBEM_ERR_NONFINITE = 6,    /* NaN / Inf in a result */
+    HBEM_ERR_UNSUPPORTED = 7   /* combination not provided by this build */
+};
+
+/* LayerType (include/galerkin_builder.hpp:100-115) */
+enum { HBEM_LAYER_DOUBLE = 1, HBEM_LAYER_SINGLE = 2, HBEM_LAYER_HYPERSINGULAR = 4, HBEM_LAYER_ALL = 7 };
+
+/* panel kinds: ParametrizedLine (include/parametrized_line.hpp), ParametrizedCircularArc
+ * (include/parametrized_circular_arc.hpp).  5 doubles per panel:
+ *   line: x1 y1 x2 y2 (unused)      arc: cx cy r phi_start phi_end                    */
+enum { HBEM_PANEL_LINE = 0, HBEM_PANEL_ARC = 1 };
+
+/* BEM spaces by local shape-function count: ContinuousSpace<1> (q = 2,
+ * include/continuous_space.hpp:33-152), DiscontinuousSpace<0> (q = 1). */
+enum { HBEM_SPACE_P0 = 1, HBEM_SPACE_P1 = 2 };
+
+typedef struct hbem_builder_s* hbem_builder;
+typedef struct hbem_solop_s* hbem_solop;
+
+int hbem_version(void);
+const char* hbem_status_string(int status);
+/* last error message of the calling thread (static storage) */
+const char* hbem_last_error(void);
+/* select the CUDA device used by handles created afterwards */
+int hbem_set_device(int device);
+
+/* H0^(1), H1^(1) of n arguments on the device: complex_bessel::Hankel1Real01::h1_01
+ * for real x (include/cbessel.hpp:236-288) when complex_arg == 0 (z_host holds n
+ * reals), HankelH1(0|1, z) / H1_01 (include/cbessel.hpp:156, 300) otherwise (n
+ * interleaved complex).  h0_host, h1_host: n interleaved complex each.            */
+int hbem_hankel01(int n, const double* z_host, int complex_arg, double* h0_host, double* h1_host);
+
+/* ------------------------------------------------------------------ builder */
+
+/* BuilderData(mesh, test_space, trial_space, order) + GalerkinBuilder(data)
+ * (include/galerkin_builder.hpp:43-46, 200; source/galerkin_builder.cpp:17-187).
+ * The mesh is given as panels; this build assembles square P1/P1 spaces
+ * (q_test == q_trial == HBEM_SPACE_P1) and returns HBEM_ERR_UNSUPPORTED otherwise. */
+int hbem_builder_create(int npanels, const int* kinds, const double* params, int order, int q_test, int q_trial,
+                        hbem_builder* out);
+int hbem_builder_destroy(hbem_builder b);
+/* dimensions: panels, test/trial space dimension, quadrature order, all-lines flag */
+int hbem_builder_info(hbem_builder b, int* npanels, int* dim_test, int* dim_trial, int* order, int* lines);
+/* BuilderData::is_adjacent (source/galerkin_builder.cpp:189-201) */
+int hbem_builder_is_adjacent(hbem_builder b, int i, int j, int* adjacent, int* swap);
+
+/* GalerkinBuilder::assembleDense(k, c, layers, d) for the full matrix
+ * (include/galerkin_builder.hpp:221-222; source/galerkin_builder.cpp:918-1018).
+ * Errors as the reference: c < 1, Im k < 0 or d > 2 -> HBEM_ERR_INVALID.       */
+int hbem_assemble_dense(hbem_builder b, double k_re, double k_im, double c, unsigned layers, unsigned d);
+/* getDoubleLayer / getHypersingular / getSingleLayer(d) (include/galerkin_builder.hpp:262-276):
+ * copies the N x N complex matrix to host_out; HBEM_ERR_INVALID if the layer or
+ * derivative was not assembled by the last hbem_assemble_dense.                  */
+int hbem_get_layer(hbem_builder b, unsigned layer, unsigned d, double* host_out);
+/* same, device pointer owned by the builder, valid until the next assembly */
+int hbem_get_layer_device(hbem_builder b, unsigned layer, unsigned d, const void** dev_ptr);
+
+/* ------------------------------------------------------------------ solutions operator */
+
+/* SolutionsOperator(builder_data, proj) (include/gen_sol_op.hpp:40-60;
+ * source/utilities/gen_sol_op.cpp:23-43): mass matrix and projection factor. */
+int hbem_solop_create(hbem_builder b, int proj, hbem_solop* out);
+int hbem_solop_destroy(hbem_solop s);
+/* SolutionsOperator::mass_matrix() (include/gen_sol_op.hpp:105): N x N real, column-major */
+int hbem_mass_matrix(hbem_solop s, double* host_out);
+/* gen_sol_op / gen_sol_op_1st_der / gen_sol_op_2nd_der (source/utilities/gen_sol_op.cpp:50-196):
+ * T and, for d >= 1, its k-derivatives, each 2N x 2N, written consecutively to
+ * T_host ((d + 1) matrices).  The derivative matrices are the projected
+ * derivative blocks (the reference writes them all into T, gen_sol_op.cpp:151,194). */
+int hbem_gen_sol_op(hbem_solop s, double k_re, double k_im, double c_o, double c_i, unsigned d, double* T_host);
+/* batched form over nk real wavenumbers; T_dev receives [nk][d + 1][2N][2N] */
+int hbem_gen_sol_op_batch_device(hbem_solop s, const double* k_host, int nk, double c_o, double c_i, unsigned d,
+                                 void* T_dev);
+
+/* ------------------------------------------------------------------ singular values */
+
+/* direct::sv / sv_1st_der / sv_2nd_der for the smallest singular value
+ * (include/singular_values.hpp; source/utilities/singular_values.cpp:7-147), batched:
+ * matrices T_dev + m*mat_stride (+ der_stride for T', + 2*der_stride for T''),
+ * strides in complex elements.  out_host[3m + t] = sigma, sigma', sigma'' (d >= t).
+ * sig_all_host, when not NULL, receives all n singular values of each matrix.     */
+int hbem_sv_dense_batch_device(int n, int nmat, unsigned d, const void* T_dev, long long mat_stride,
+                               long long der_stride, double* out_host, double* sig_all_host);
+
+/* same with host matrices (copied to the device): T_host holds nmat blocks of
+ * (d + 1) consecutive n x n matrices (T, T', T'') */
+int hbem_sv_dense_batch(int n, int nmat, unsigned d, const double* T_host, double* out_host, double* sig_all_host);
+
+/* sigma_min(k) and its derivatives along a list of real wavenumbers, end to end:
+ * gen_sol_op_*der + direct::sv_*der per k (examples/roots_newton_circle.cpp:111-138).
+ * out_host[3i + t]. */
+int hbem_sweep_sigma(hbem_solop s, const double* k_host, int nk, double c_o, double c_i, unsigned d, double* out_host);
+
+/* Plain resonance search on [k_min, k_max] with npoints grid points
+ * (examples/roots_newton_polygon_rsvd.cpp:172-265 with the dense sigma of
+ * examples/roots_newton_circle.cpp): grid sweep of sigma, sigma', sigma''; 3-point
+ * local minima; validation sigma'(left) < 0 < sigma'(right); quartic Hermite model
+ * minimised by Brent; rtsafe on sigma' with sigma'' to tolerance tol.
+ * roots_host receives up to max_roots roots, *nroots their count; grid_host
+ * (npoints x 3, may be NULL) the grid values; *n_evals the number of T(k) evaluated. */
+int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npoints, double c_o, double c_i,
+                               double tol, double* roots_host, int max_roots, int* nroots, double* grid_host,
+                               int* n_evals);
+
+/* ------------------------------------------------------------------ root finding (host) */
+
+typedef double (*hbem_fn)(double x, void* user);
+typedef void (*hbem_fn_both)(double x, double* f, double* df, void* user);
+
+/* rtsafe (include/find_roots.hpp:37-49; source/utilities/find_roots.cpp:117-217):
+ * safeguarded Newton; returns the root, sets *root_found and *num_iter. */
+double hbem_rtsafe(hbem_fn f, hbem_fn_both f_both, void* user, double x1, double x2, double tol, int* root_found,
+                   unsigned* num_iter);
+/* zbrent (include/find_roots.hpp:51-67; source/utilities/find_roots.cpp:19-115) */
+double hbem_zbrent(hbem_fn f, void* user, double x1, double x2, double tol, int* root_found, unsigned* num_iter);
+/* BrentMinimizer(a, b, tol).local_min_rc driven to completion
+ * (include/find_roots.hpp:181-233; source/utilities/find_roots.cpp:1003-1184) */
+double hbem_brent_min(hbem_fn f, void* user, double a, double b, double tol);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HBEM_H */

@@ -1,0 +1,312 @@
+"""Benchmark: verified resonances per second of the plain sweep.
+
+Workload (one step): the plain resonance search on the circular scatterer of
+the reference's CPU-runnable configuration -- radius 0.25, N = 50 circular-arc
+panels, c_i = 23.4, c_o = 1, Gauss order 11, continuous P1 spaces (T(k) is
+100 x 100 complex128) -- over k in [0.5, 10] on 200 grid points: sigma_min,
+sigma', sigma'' by dense SVD at every grid point, 3-point local minima,
+validation sigma'(left) < 0 < sigma'(right), quartic/Brent guess, safeguarded
+Newton on sigma' to |dk| <= 1e-8, then every root verified by a sign change of
+sigma' across [root - 1e-8, root + 1e-8].
+
+  value : verified roots / s with the mesh resident on the device (builder and
+          solutions operator created once, outside the timed region)
+  e2e   : the same through the public C ABI from host data: builder + operator
+          creation (mesh upload), the search and the root read-back, per step
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl {gb300,reference}]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CFG = dict(radius=0.25, N=50, c_i=23.4, c_o=1.0, order=11, k_min=0.5, k_max=10.0, npoints=200, tol=1e-8)
+WORKLOAD = ("plain sweep: circle r=0.25, N=50 arc panels, c_i=23.4, c_o=1, Gauss order 11, P1/P1 "
+            "(T 100x100 c128), k in [0.5,10] x 200, dense sigma/sigma'/sigma'', Newton to |dk|<=1e-8")
+METRIC = "verified resonances/sec at |dk|<=1e-8 (plain sweep)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-sample-points", type=int, default=60)
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU leg (oracle port)
+
+def cpu_sample(npoints_sample, threads):
+    """Plain sweep of the oracle port on the first npoints_sample grid points of the
+    workload (same spacing), all host threads: returns (verified roots, seconds)."""
+    from oracle import oracle as O
+    kinds, par = O.circle_panels(CFG["radius"], CFG["N"])
+    oso = O.SolutionsOperator(O.Builder(kinds, par, CFG["order"]))
+    h = (CFG["k_max"] - CFG["k_min"]) / (CFG["npoints"] - 1)
+    ks = CFG["k_min"] + h * np.arange(npoints_sample)
+
+    def eval3(klist):
+        return np.array([O.sv_derivs(*oso.gen_sol_op(k, CFG["c_o"], CFG["c_i"], d=2, threads=threads))
+                         for k in klist])
+
+    t0 = time.perf_counter()
+    roots, _ = O.plain_sweep(eval3, ks, tol=CFG["tol"])
+    verified = 0
+    for r in roots:
+        lo = O.sv_derivs(*oso.gen_sol_op(r - CFG["tol"], CFG["c_o"], CFG["c_i"], d=1, threads=threads))[1]
+        hi = O.sv_derivs(*oso.gen_sol_op(r + CFG["tol"], CFG["c_o"], CFG["c_i"], d=1, threads=threads))[1]
+        verified += int(lo <= 0.0 <= hi)
+    return verified, time.perf_counter() - t0, ks.size
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    import oracle.oracle as O
+    O.lib()   # build the CPU port if needed (outside the timed region)
+    for _ in range(max(0, args.warmup)):
+        cpu_sample(6, threads)
+    tot_v, tot_t = 0, 0.0
+    for _ in range(args.steps):
+        v, t, npts = cpu_sample(args.cpu_sample_points, threads)
+        tot_v += v
+        tot_t += t
+    val = tot_v / tot_t if tot_t > 0 else 0.0
+    sample = "first %d of the %d grid points (same spacing) + Newton/verification of their roots" % (
+        args.cpu_sample_points, CFG["npoints"])
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "resonances/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / max(1, args.steps),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cpu_sample": sample},
+        "cpu_baseline": {"value": val, "unit": "resonances/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": val, "unit": "resonances/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------------ GPU leg
+
+def fp64_peak_tflops():
+    """Measured FP64 peak: cuBLAS DGEMM 8192^3 through torch (best of 5)."""
+    import torch
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b
+    return best
+
+
+def run_gpu(args):
+    rank, world, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from helmholtzbem_gb300 import _capi as C, api, geometry
+
+    C.check(C.lib().hbem_set_device(local))
+    mesh = geometry.circle(CFG["radius"], CFG["N"])
+    data = api.BuilderData(mesh, order=CFG["order"])
+    so = api.SolutionsOperator(data)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # > L2 (129 MB)
+
+    def step(solop):
+        roots, grid, nev = solop.find_resonances_plain(CFG["k_min"], CFG["k_max"], CFG["npoints"], CFG["c_o"],
+                                                       CFG["c_i"], tol=CFG["tol"])
+        if roots.size:
+            lo = solop.sweep_sigma(roots - CFG["tol"], CFG["c_o"], CFG["c_i"], d=1)[:, 1]
+            hi = solop.sweep_sigma(roots + CFG["tol"], CFG["c_o"], CFG["c_i"], d=1)[:, 1]
+            ver = int(np.sum((lo <= 0.0) & (hi >= 0.0)))
+        else:
+            ver = 0
+        return ver, roots, nev
+
+    for _ in range(max(3, args.warmup)):
+        step(so)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+
+    lib = C.lib()
+    lib.hbem_stats_reset()
+    lib.hbem_stats_enable_timing(1)
+    tot_ms, tot_v, nev_tot = 0.0, 0, 0
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            v, roots, nev = step(so)
+            e1.record()
+            torch.cuda.synchronize()
+            tot_ms += e0.elapsed_time(e1)
+            tot_v += v
+            nev_tot += nev
+    lib.hbem_stats_enable_timing(0)
+    launches, asm_ms, asm_l, asm_pts = (C.ctypes.c_longlong(), C.ctypes.c_double(), C.ctypes.c_longlong(),
+                                        C.ctypes.c_longlong())
+    lib.hbem_stats_read(C.ctypes.byref(launches), C.ctypes.byref(asm_ms), C.ctypes.byref(asm_l), C.ctypes.byref(asm_pts))
+    t = torch.tensor([tot_ms], device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        vv = torch.tensor([float(tot_v)], device="cuda")
+        torch.distributed.all_reduce(vv)
+        tot_v_all = vv.item()
+    else:
+        tot_v_all = float(tot_v)
+    ms = t.item()
+    value = tot_v_all / (ms * 1e-3)
+
+    # end to end from host data through the C ABI: mesh upload, operator set-up,
+    # search and root read-back inside the timed region
+    kinds, par = mesh
+    h2d = kinds.nbytes + par.nbytes
+    e2e_ms, e2e_v = 0.0, 0
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        d2 = api.BuilderData((kinds.copy(), par.copy()), order=CFG["order"])
+        s2 = api.SolutionsOperator(d2)
+        v, roots, _ = step(s2)
+        e1.record()
+        torch.cuda.synchronize()
+        e2e_ms += e0.elapsed_time(e1)
+        e2e_v += v
+        del s2, d2
+    d2h = int(roots.nbytes + CFG["npoints"] * 3 * 8)
+
+    # roofline of the dominant kernel (panel-pair assembly, FP64 CUDA-core bound).
+    # Algorithmic work: F_pt(d) = 180 + 100 (d + 1) FP64 flops per quadrature point and
+    # medium; asm_pts counts points x media over the timed launches.
+    d = 2
+    flops = asm_pts.value * (180.0 + 100.0 * (d + 1))
+    achieved = flops / (asm_ms.value * 1e-3) / 1e12 if asm_ms.value > 0 else 0.0
+    peak = fp64_peak_tflops()
+    roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak if peak else None, "traffic": None,
+                "peak_source": "measured: cuBLAS DGEMM 8192^3 on this GPU (MEASURED_PEAKS.json has no FP64 entry)",
+                "kernel": "k_general + k_singular (panel-pair assembly)", "launches": asm_l.value,
+                "avg_launch_ms": asm_ms.value / max(1, asm_l.value)}
+
+    cpu = None
+    if rank == 0 and world == 1 or rank == 0:
+        threads = os.cpu_count() or 1
+        try:
+            v, tsec, npts = cpu_sample(args.cpu_sample_points, threads)
+            cpu = {"value": v / tsec if tsec > 0 else None, "unit": "resonances/s", "cores": threads, "kind": "port",
+                   "sample": "first %d of %d grid points + Newton/verification of their roots" % (npts, CFG["npoints"])}
+        except Exception as ex:   # the baseline must not hide the GPU line
+            cpu = {"value": None, "unit": "resonances/s", "cores": threads, "kind": "port", "error": str(ex)[:200]}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "resonances/s", "n_gpus": world, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "l2": "256 MB buffer written between timed steps",
+                       "roots_per_step": tot_v / args.steps, "T_evals_per_step": nev_tot / args.steps},
+            "e2e": {"value": e2e_v / (e2e_ms * 1e-3), "unit": "resonances/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches.value),
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -45,7 +45,7 @@ struct Acc {
 template <bool RK>
 __device__ __forceinline__ void hankel_at(const KConst& K, double vn, cplx& h0, cplx& h1) {
     if (RK) hankel01_real(K.ks.re * vn, h0, h1);
-    else hankel01_cplx(vn * K.ks, h0, h1);
+    else hankel01_cplx(vn * K.ks.re, vn * K.ks.im, h0, h1);
 }
 
 // complex scalar times complex, specialised for real ks
@@ -520,7 +520,7 @@ __global__ void k_hankel01(int n, const cplx* z, int complex_arg, cplx* h0, cplx
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     cplx a, b;
-    if (complex_arg) hankel01_cplx(z[i], a, b);
+    if (complex_arg) hankel01_cplx(z[i].re, z[i].im, a, b);
     else hankel01_real(z[i].re, a, b);
     h0[i] = a;
     h1[i] = b;

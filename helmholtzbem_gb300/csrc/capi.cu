@@ -33,6 +33,14 @@ thread_local std::string g_err;
 int g_device = 0;
 const double kMachEps = 2.220446049250313e-16;
 
+// instrumentation: kernel launches issued, and CUDA-event timing of the
+// panel-pair assembly launches on the stream they run on
+long long g_launches = 0;
+int g_timing = 0;
+double g_asm_ms = 0.;
+long long g_asm_launches = 0;
+long long g_asm_points = 0;   // quadrature points x media processed by timed launches
+
 int fail(int code, const std::string& msg) {
     g_err = msg;
     return code;
@@ -155,6 +163,35 @@ struct HPanel {
 
 double dist(cplx a, cplx b) { return std::hypot(a.re - b.re, a.im - b.im); }
 
+// panel-pair assembly launch with launch counting and, when enabled, CUDA-event
+// timing on the launching stream
+cudaError_t local_assembly(const DevMesh& M, const SingularTask* tasks, int ntasks, int ncoinc, const Job* jobs,
+                           int njobs, bool real_k, int d, cplx* loc, cudaStream_t st) {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (g_timing) {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, st);
+    }
+    cudaError_t e = launch_local(M, tasks, ntasks, jobs, njobs, real_k, d, loc, st);
+    g_launches += (M.n > 1 ? 1 : 0) + (ntasks > 0 ? 1 : 0);
+    if (g_timing) {
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        g_asm_ms += ms;
+        g_asm_launches += 1;
+        long long nc2 = (long long)M.nc * M.nc;
+        long long nadj = ntasks - ncoinc;
+        long long gen = (long long)M.n * (M.n + 1) / 2 - ntasks;
+        g_asm_points += (long long)njobs * (ncoinc * nc2 + nadj * 2 * nc2 + gen * (long long)M.p * M.p);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    return e;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- builder
@@ -209,6 +246,23 @@ struct hbem_solop_s {
 extern "C" {
 
 int hbem_version(void) { return 100; }
+
+void hbem_stats_enable_timing(int enable) { g_timing = enable ? 1 : 0; }
+
+void hbem_stats_reset(void) {
+    g_launches = 0;
+    g_asm_ms = 0.;
+    g_asm_launches = 0;
+    g_asm_points = 0;
+}
+
+void hbem_stats_read(long long* launches, double* assembly_ms, long long* assembly_launches,
+                     long long* assembly_points) {
+    if (launches) *launches = g_launches;
+    if (assembly_ms) *assembly_ms = g_asm_ms;
+    if (assembly_launches) *assembly_launches = g_asm_launches;
+    if (assembly_points) *assembly_points = g_asm_points;
+}
 
 const char* hbem_status_string(int s) {
     switch (s) {
@@ -363,9 +417,10 @@ int hbem_assemble_dense(hbem_builder b, double k_re, double k_im, double c, unsi
     int nl = ((layers & 1) != 0) + ((layers & 2) != 0) + ((layers & 4) != 0);
     HB_CK(b->d_layers.ensure((size_t)nl * (d + 1) * b->n * b->n * sizeof(cplx)));
     bool real_k = (k_im == 0. && k_re > 0.);
-    HB_CK(launch_local(b->view(), b->d_tasks.as<SingularTask>(), (int)b->tasks.size(), b->d_jobs.as<Job>(), 1, real_k,
-                       (int)d, b->d_loc.as<cplx>(), b->st));
+    HB_CK(local_assembly(b->view(), b->d_tasks.as<SingularTask>(), (int)b->tasks.size(), b->n, b->d_jobs.as<Job>(), 1,
+                         real_k, (int)d, b->d_loc.as<cplx>(), b->st));
     HB_CK(launch_gather_layers(b->n, (int)d, (int)layers, b->d_loc.as<cplx>(), 0, b->d_layers.as<cplx>(), b->st));
+    g_launches += 1;
     HB_CK(cudaStreamSynchronize(b->st));
     b->asm_layers = (int)layers;
     b->asm_d = (int)d;
@@ -515,13 +570,16 @@ static int gen_T_batch(hbem_solop s, const double* k_host, const double* kim_hos
         }
         HB_CK(upload(b->d_jobs, jobs, b->st));
         HB_CK(b->d_loc.ensure(per_job * 2 * kn));
-        HB_CK(launch_local(b->view(), b->d_tasks.as<SingularTask>(), (int)b->tasks.size(), b->d_jobs.as<Job>(), 2 * kn,
-                           real_k, (int)d, b->d_loc.as<cplx>(), b->st));
+        HB_CK(local_assembly(b->view(), b->d_tasks.as<SingularTask>(), (int)b->tasks.size(), b->n, b->d_jobs.as<Job>(),
+                             2 * kn, real_k, (int)d, b->d_loc.as<cplx>(), b->st));
         cplx* Tk = T_dev + (size_t)k0 * (d + 1) * mat;
         HB_CK(launch_gather_T(N, (int)d, b->d_loc.as<cplx>(), s->d_M.as<double>(), kn, Tk, b->st));
-        if (s->proj)
+        g_launches += 1;
+        if (s->proj) {
             HB_CK(launch_projection(N, s->d_id.as<double>(), s->d_sb.as<double>(), s->d_lr.as<double>(), Tk,
                                     kn * (int)(d + 1), b->st));
+            g_launches += 2;
+        }
     }
     return HBEM_OK;
 }
@@ -566,6 +624,7 @@ static int sv_batch(cudaStream_t st, int n, int nmat, unsigned d, const cplx* T,
     }
     HB_CK(launch_svd(n, nmat, (int)d, 0, T, mat_stride, der_stride, A.as<cplx>(), V.as<cplx>(), out.as<double>(), dsig,
                      status.as<int>(), st));
+    g_launches += 1;
     HB_CK(cudaMemcpyAsync(out_host, out.p, (size_t)nmat * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (sig_all_host)
         HB_CK(cudaMemcpyAsync(sig_all_host, dsig, (size_t)nmat * n * sizeof(double), cudaMemcpyDeviceToHost, st));

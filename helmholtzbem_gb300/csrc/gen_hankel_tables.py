@@ -47,6 +47,23 @@ def main():
         print("static __device__ __constant__ double %s[%d] = {" % (name, DEG + 1))
         print(",\n".join("  %.17e" % v for v in P.coef))
         print("};")
+    # ascending-series constants, index k = 1..SER_N (entry 0 unused):
+    # 1/k^2, H_k, 1/(k+1), H_k/(k+1) -- exact rationals rounded once
+    from fractions import Fraction
+    ser_n = 48
+    H = Fraction(0)
+    rows = {"HBEM_SER_IK2": [0.0], "HBEM_SER_H": [0.0], "HBEM_SER_IK1": [0.0], "HBEM_SER_HK1": [0.0]}
+    for k in range(1, ser_n + 1):
+        H += Fraction(1, k)
+        rows["HBEM_SER_IK2"].append(float(Fraction(1, k * k)))
+        rows["HBEM_SER_H"].append(float(H))
+        rows["HBEM_SER_IK1"].append(float(Fraction(1, k + 1)))
+        rows["HBEM_SER_HK1"].append(float(H / (k + 1)))
+    print("#define HBEM_SER_N %d" % ser_n)
+    for name, vals_ in rows.items():
+        print("static __device__ __constant__ double %s[%d] = {" % (name, ser_n + 1))
+        print(",\n".join("  %.17e" % v for v in vals_))
+        print("};")
 
 
 if __name__ == "__main__":

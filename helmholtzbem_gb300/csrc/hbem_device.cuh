@@ -78,24 +78,24 @@ static __device__ __noinline__ void hankel01_real(double x, cplx& h0, cplx& h1) 
         y0 = (2. / kPi) * (log(j1) + kEulerGamma);
         y1 = -(2. / kPi) / x;
     } else if (x < 8.) {
-        double x2_4 = 0.25 * x * x, t = 1., Hk = 0., k = 1.;
+        const double mx2_4 = -0.25 * x * x;
+        double t = 1.;
         j0 = 1.; j1 = 1.; y0 = 0.; y1 = 0.;
-        // terms t_k = (-x^2/4)^k/(k!)^2; stop once H_k |t_k| <= eps (at most 40 terms for x < 8)
-        for (int it = 0; it < 60; ++it) {
-            t *= -x2_4 / (k * k);
-            Hk += 1.0 / k;
+        // terms t_k = (-x^2/4)^k/(k!)^2 with tabulated 1/k^2, H_k, 1/(k+1), H_k/(k+1);
+        // stop once |t_k| < 2^-55, i.e. H_k |t_k| < eps for every k used (x < 8 needs < 40)
+        for (int k = 1; k <= HBEM_SER_N; ++k) {
+            t *= mx2_4 * HBEM_SER_IK2[k];
             j0 += t;
-            y0 = fma(-Hk, t, y0);
-            k += 1.0;
-            double ik = 1.0 / k;
-            j1 = fma(t, ik, j1);
-            y1 = fma(-Hk * ik, t, y1);
-            if (Hk * fabs(t) <= kEps) break;
+            y0 = fma(-HBEM_SER_H[k], t, y0);
+            j1 = fma(t, HBEM_SER_IK1[k], j1);
+            y1 = fma(-HBEM_SER_HK1[k], t, y1);
+            if ((__double2hiint(t) & 0x7fffffff) < ((1023 - 55) << 20)) break;
         }
+        const double ix = 1.0 / x;
         j1 *= 0.5 * x;
         double lg = log(0.5 * x) + kEulerGamma;
         y0 = (2. / kPi) * fma(lg, j0, y0);
-        y1 = (1. / kPi) * (y1 * x + 2.0 * (lg * j1 + (j0 - 2.0) / x));
+        y1 = (1. / kPi) * (y1 * x + 2.0 * (lg * j1 + (j0 - 2.0) * ix));
     } else if (x <= 1e6) {
         double ix = 1.0 / x, w = 64. * ix * ix;
         double P0 = 1. + horner_pq(HBEM_F0, w);
@@ -130,8 +130,9 @@ static __device__ __noinline__ void hankel01_real(double x, cplx& h0, cplx& h1) 
 //                  derivative for Y1, all accumulated during the recurrence
 //   |z| >= 20      Hankel's asymptotic expansion (DLMF 10.17.5)
 // Non-finite values are replaced by 0 (galerkin_builder.cpp:216-235).
-static __device__ __noinline__ void hankel01_cplx(cplx z, cplx& h0, cplx& h1) {
+static __device__ __forceinline__ void hankel01_cplx(double zre, double zim, cplx& h0, cplx& h1) {
     const cplx I = mk(0., 1.);
+    const cplx z = mk(zre, zim);
     double az = hypot(z.re, z.im);
     cplx j0, j1, y0, y1;
     if (az == 0.) {
@@ -194,31 +195,34 @@ static __device__ __noinline__ void hankel01_cplx(cplx z, cplx& h0, cplx& h1) {
         y0 = (2. / kPi) * (lg * j0) - (4. / kPi) * sy0;
         y1 = (2. / kPi) * (lg * j1) - (2. / kPi) * cdiv(j0, z) + (2. / kPi) * sy1;
     } else {
-        cplx s[2];
-        cplx iz = cdiv(mk(1.), z);
-        for (int nu = 0; nu < 2; ++nu) {
-            double mu = 4. * nu * nu;
-            cplx sum = mk(1.), term = mk(1.);
-            for (int k = 1; k < 200; ++k) {
-                double a = (mu - (2. * k - 1.) * (2. * k - 1.)) / (k * 8.);
-                term = term * (a * (I * iz));
-                sum += term;
-                if (hypot(term.re, term.im) < 0.25 * kEps) break;
+        // sum_k i^k a_k(nu) / z^k for nu = 0 and nu = 1 in one loop (no local arrays)
+        cplx iiz = I * cdiv(mk(1.), z);
+        cplx s0 = mk(1.), s1 = mk(1.), t0 = mk(1.), t1 = mk(1.);
+        bool d0 = false, d1 = false;
+        for (int k = 1; k < 200 && !(d0 && d1); ++k) {
+            double odd2 = (2. * k - 1.) * (2. * k - 1.);
+            if (!d0) {
+                t0 = t0 * ((-odd2 / (k * 8.)) * iiz);
+                s0 += t0;
+                d0 = hypot(t0.re, t0.im) < 0.25 * kEps;
             }
-            s[nu] = sum;
+            if (!d1) {
+                t1 = t1 * (((4. - odd2) / (k * 8.)) * iiz);
+                s1 += t1;
+                d1 = hypot(t1.re, t1.im) < 0.25 * kEps;
+            }
         }
         cplx r = csqrt(cdiv(mk(2. / kPi), z));
-        h0 = r * cexp(I * (z - mk(0.25 * kPi))) * s[0];
-        h1 = r * cexp(I * (z - mk(0.75 * kPi))) * s[1];
-        j0 = h0; j1 = h1; y0 = mk(0.); y1 = mk(0.);
-        if (!isfinite(h0.re) || !isfinite(h0.im)) h0 = mk(0.);
-        if (!isfinite(h1.re) || !isfinite(h1.im)) h1 = mk(0.);
-        return;
+        j0 = r * cexp(I * (z - mk(0.25 * kPi))) * s0;   // holds H0 itself
+        j1 = r * cexp(I * (z - mk(0.75 * kPi))) * s1;   // holds H1 itself
+        y0 = mk(0.);
+        y1 = mk(0.);
     }
-    h0 = j0 + I * y0;
-    h1 = j1 + I * y1;
-    if (!isfinite(h0.re) || !isfinite(h0.im)) h0 = mk(0.);
-    if (!isfinite(h1.re) || !isfinite(h1.im)) h1 = mk(0.);
+    cplx a = j0 + I * y0, b = j1 + I * y1;
+    if (!isfinite(a.re) || !isfinite(a.im)) a = mk(0.);
+    if (!isfinite(b.re) || !isfinite(b.im)) b = mk(0.);
+    h0 = a;
+    h1 = b;
 }
 
 }  // namespace hbem

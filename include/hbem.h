@@ -51,6 +51,16 @@ const char* hbem_last_error(void);
 /* select the CUDA device used by handles created afterwards */
 int hbem_set_device(int device);
 
+/* Instrumentation (no counterpart in the reference, which prints std::chrono
+ * timings, gen_sol_op.cpp:89-99 and randsvd.cpp:27-47): kernel launches issued
+ * by this library, and -- when timing is enabled -- CUDA-event time, launch count
+ * and processed (quadrature point x medium) count of the panel-pair assembly
+ * launches, timed on the stream they run on.  Not thread-safe.                 */
+void hbem_stats_enable_timing(int enable);
+void hbem_stats_reset(void);
+void hbem_stats_read(long long* launches, double* assembly_ms, long long* assembly_launches,
+                     long long* assembly_points);
+
 /* H0^(1), H1^(1) of n arguments on the device: complex_bessel::Hankel1Real01::h1_01
  * for real x (include/cbessel.hpp:236-288) when complex_arg == 0 (z_host holds n
  * reals), HankelH1(0|1, z) / H1_01 (include/cbessel.hpp:156, 300) otherwise (n

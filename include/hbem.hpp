@@ -1,0 +1,252 @@
+// hbem.hpp -- C++ facade over the C ABI (hbem.h) with the reference's class and
+// function names, so code written against HelmholtzBEM's GalerkinBuilder /
+// SolutionsOperator / direct::sv / find_roots can switch by changing includes.
+//
+// Reference interfaces mirrored:
+//   BuilderData, GalerkinBuilder, LayerType   include/galerkin_builder.hpp:24-277
+//   SolutionsOperator                         include/gen_sol_op.hpp:16-128
+//   direct::sv, sv_1st_der, sv_2nd_der        include/singular_values.hpp
+//   rtsafe, zbrent, BrentMinimizer            include/find_roots.hpp:37-67,181-233
+//
+// Matrices: hbem::MatrixXcd / MatrixXd (column-major, data()/rows()/cols()/
+// resize()/operator()), or Eigen's types when HBEM_USE_EIGEN is defined before
+// including this header.  Errors surface as std::runtime_error, as in the
+// reference; status codes stay inside.
+#pragma once
+
+#include <complex>
+#include <functional>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "hbem.h"
+
+#ifdef HBEM_USE_EIGEN
+#include <Eigen/Dense>
+#endif
+
+namespace hbem {
+
+#ifdef HBEM_USE_EIGEN
+using MatrixXcd = Eigen::MatrixXcd;
+using MatrixXd = Eigen::MatrixXd;
+#else
+template <class T>
+class Matrix {
+    std::vector<T> d_;
+    long r_ = 0, c_ = 0;
+
+public:
+    Matrix() = default;
+    Matrix(long r, long c) { resize(r, c); }
+    void resize(long r, long c) { r_ = r; c_ = c; d_.assign((size_t)r * c, T()); }
+    long rows() const { return r_; }
+    long cols() const { return c_; }
+    T* data() { return d_.data(); }
+    const T* data() const { return d_.data(); }
+    T& operator()(long i, long j) { return d_[(size_t)i + (size_t)j * r_]; }
+    const T& operator()(long i, long j) const { return d_[(size_t)i + (size_t)j * r_]; }
+};
+using MatrixXcd = Matrix<std::complex<double>>;
+using MatrixXd = Matrix<double>;
+#endif
+
+inline void throw_if(int status) {
+    if (status != HBEM_OK) throw std::runtime_error(std::string(hbem_status_string(status)) + ": " + hbem_last_error());
+}
+
+// Panel mesh in the C-ABI layout (the reference builds a ParametrizedMesh of
+// ParametrizedLine / ParametrizedCircularArc panels).
+struct Mesh {
+    std::vector<int> kinds;
+    std::vector<double> params;   // 5 per panel
+    int size() const { return (int)kinds.size(); }
+    void add_line(double x1, double y1, double x2, double y2) {
+        kinds.push_back(HBEM_PANEL_LINE);
+        params.insert(params.end(), {x1, y1, x2, y2, 0.});
+    }
+    void add_arc(double cx, double cy, double r, double phi0, double phi1) {
+        kinds.push_back(HBEM_PANEL_ARC);
+        params.insert(params.end(), {cx, cy, r, phi0, phi1});
+    }
+    // ParametrizedCircularArc(center, r, phi0, phi1).split(n)
+    static Mesh circle(double cx, double cy, double r, int n, double phi0 = 0., double phi1 = 2 * 3.14159265358979323846) {
+        Mesh m;
+        for (int i = 0; i < n; ++i) {
+            double a = phi0 + i * (phi1 - phi0) / n, b = phi0 + (i + 1) * (phi1 - phi0) / n;
+            if (i == n - 1) b = phi1;
+            m.add_arc(cx, cy, r, a, b);
+        }
+        return m;
+    }
+};
+
+enum class LayerType : unsigned { NONE = 0, DOUBLE = 1, SINGLE = 2, HYPERSINGULAR = 4, ALL = 7 };
+inline LayerType operator|(LayerType a, LayerType b) { return (LayerType)((unsigned)a | (unsigned)b); }
+
+enum Space { P0 = HBEM_SPACE_P0, P1 = HBEM_SPACE_P1 };
+
+class BuilderData {
+    hbem_builder h_ = nullptr;
+    int n_ = 0;
+
+public:
+    BuilderData(const Mesh& mesh, Space test, Space trial, unsigned order) {
+        throw_if(hbem_builder_create(mesh.size(), mesh.kinds.data(), mesh.params.data(), (int)order, test, trial, &h_));
+        n_ = mesh.size();
+    }
+    BuilderData(const BuilderData&) = delete;
+    BuilderData& operator=(const BuilderData&) = delete;
+    ~BuilderData() { hbem_builder_destroy(h_); }
+    hbem_builder handle() const { return h_; }
+    size_t getNumPanels() const { return (size_t)n_; }
+    size_t getTestSpaceDimension() const { return (size_t)n_; }
+    size_t getTrialSpaceDimension() const { return (size_t)n_; }
+    bool is_adjacent(size_t i, size_t j, bool& swap) const {
+        int a = 0, s = 0;
+        throw_if(hbem_builder_is_adjacent(h_, (int)i, (int)j, &a, &s));
+        swap = s != 0;
+        return a != 0;
+    }
+};
+
+class GalerkinBuilder {
+    const BuilderData& data_;
+    mutable MatrixXcd cache_[3][3];
+
+    const MatrixXcd& fetch(unsigned layer, int slot, size_t d) const {
+        MatrixXcd& m = cache_[slot][d > 2 ? 2 : d];
+        m.resize((long)data_.getNumPanels(), (long)data_.getNumPanels());
+        throw_if(hbem_get_layer(data_.handle(), layer, (unsigned)d, reinterpret_cast<double*>(m.data())));
+        return m;
+    }
+
+public:
+    explicit GalerkinBuilder(const BuilderData& data) : data_(data) {}
+    const BuilderData& getData() const { return data_; }
+    void assembleDense(const std::complex<double>& k, double c, LayerType layers = LayerType::ALL, size_t d = 0) {
+        throw_if(hbem_assemble_dense(data_.handle(), k.real(), k.imag(), c, (unsigned)layers, (unsigned)d));
+    }
+    const MatrixXcd& getDoubleLayer(size_t d = 0) const { return fetch(HBEM_LAYER_DOUBLE, 0, d); }
+    const MatrixXcd& getHypersingular(size_t d = 0) const { return fetch(HBEM_LAYER_HYPERSINGULAR, 1, d); }
+    const MatrixXcd& getSingleLayer(size_t d = 0) const { return fetch(HBEM_LAYER_SINGLE, 2, d); }
+};
+
+class SolutionsOperator {
+    const BuilderData& data_;
+    hbem_solop h_ = nullptr;
+
+    void gen(const std::complex<double>& k, double c_o, double c_i, unsigned d, MatrixXcd* out[3]) {
+        const long n = 2 * (long)data_.getNumPanels();
+        std::vector<std::complex<double>> buf((size_t)(d + 1) * n * n);
+        throw_if(hbem_gen_sol_op(h_, k.real(), k.imag(), c_o, c_i, d, reinterpret_cast<double*>(buf.data())));
+        for (unsigned t = 0; t <= d; ++t) {
+            out[t]->resize(n, n);
+            for (long j = 0; j < n; ++j)
+                for (long i = 0; i < n; ++i) (*out[t])(i, j) = buf[(size_t)t * n * n + i + (size_t)j * n];
+        }
+    }
+
+public:
+    explicit SolutionsOperator(const BuilderData& data, bool proj = true) : data_(data) {
+        throw_if(hbem_solop_create(data.handle(), proj ? 1 : 0, &h_));
+    }
+    SolutionsOperator(const SolutionsOperator&) = delete;
+    SolutionsOperator& operator=(const SolutionsOperator&) = delete;
+    ~SolutionsOperator() { hbem_solop_destroy(h_); }
+    hbem_solop handle() const { return h_; }
+    const BuilderData& getBuilderData() const { return data_; }
+    MatrixXd mass_matrix() const {
+        MatrixXd M((long)data_.getNumPanels(), (long)data_.getNumPanels());
+        throw_if(hbem_mass_matrix(h_, M.data()));
+        return M;
+    }
+    void gen_sol_op(const std::complex<double>& k, double c_o, double c_i, MatrixXcd& T) {
+        MatrixXcd* o[3] = {&T, nullptr, nullptr};
+        gen(k, c_o, c_i, 0, o);
+    }
+    void gen_sol_op_1st_der(const std::complex<double>& k, double c_o, double c_i, MatrixXcd& T, MatrixXcd& T_der) {
+        MatrixXcd* o[3] = {&T, &T_der, nullptr};
+        gen(k, c_o, c_i, 1, o);
+    }
+    void gen_sol_op_2nd_der(const std::complex<double>& k, double c_o, double c_i, MatrixXcd& T, MatrixXcd& T_der,
+                            MatrixXcd& T_der2) {
+        MatrixXcd* o[3] = {&T, &T_der, &T_der2};
+        gen(k, c_o, c_i, 2, o);
+    }
+};
+
+namespace direct {
+// smallest singular value only (the reference's list/count selection is reduced
+// to index 0, the only one its drivers request)
+inline std::vector<double> sv_all(const MatrixXcd* const* mats, unsigned d) {
+    const int n = (int)mats[0]->rows();
+    std::vector<std::complex<double>> buf((size_t)(d + 1) * n * n);
+    for (unsigned t = 0; t <= d; ++t)
+        for (long j = 0; j < n; ++j)
+            for (long i = 0; i < n; ++i) buf[(size_t)t * n * n + i + (size_t)j * n] = (*mats[t])(i, j);
+    std::vector<double> out(3);
+    throw_if(hbem_sv_dense_batch(n, 1, d, reinterpret_cast<const double*>(buf.data()), out.data(), nullptr));
+    return out;
+}
+inline double sv(const MatrixXcd& T) {
+    const MatrixXcd* m[1] = {&T};
+    return sv_all(m, 0)[0];
+}
+inline std::vector<double> sv_1st_der(const MatrixXcd& T, const MatrixXcd& T_der) {
+    const MatrixXcd* m[2] = {&T, &T_der};
+    auto r = sv_all(m, 1);
+    return {r[0], r[1]};
+}
+inline std::vector<double> sv_2nd_der(const MatrixXcd& T, const MatrixXcd& T_der, const MatrixXcd& T_der2) {
+    const MatrixXcd* m[3] = {&T, &T_der, &T_der2};
+    return sv_all(m, 2);
+}
+}  // namespace direct
+
+namespace detail {
+inline double call_fn(double x, void* u) { return (*static_cast<std::function<double(double)>*>(u))(x); }
+struct Both {
+    std::function<double(double)>* f;
+    std::function<std::vector<double>(double)>* fb;
+};
+inline double call_f(double x, void* u) { return (*static_cast<Both*>(u)->f)(x); }
+inline void call_both(double x, double* f, double* df, void* u) {
+    auto r = (*static_cast<Both*>(u)->fb)(x);
+    *f = r[0];
+    *df = r[1];
+}
+}  // namespace detail
+
+// rtsafe(f, f_both, x1, x2, tol, root_found, num_iter); f_both returns {f, f'}
+inline double rtsafe(std::function<double(double)> f, std::function<std::vector<double>(double)> f_both, double x1,
+                     double x2, double tol, bool& root_found, unsigned& num_iter) {
+    detail::Both b{&f, &f_both};
+    int rf = 0;
+    double r = hbem_rtsafe(detail::call_f, detail::call_both, &b, x1, x2, tol, &rf, &num_iter);
+    root_found = rf != 0;
+    return r;
+}
+
+inline double zbrent(std::function<double(double)> f, double x1, double x2, double tol, bool& root_found,
+                     unsigned& num_iter) {
+    int rf = 0;
+    double r = hbem_zbrent(detail::call_fn, &f, x1, x2, tol, &rf, &num_iter);
+    root_found = rf != 0;
+    return r;
+}
+
+// BrentMinimizer(a, b, tol): the reference's reverse-communication interface is
+// replaced by a callback; minimize(f) returns the estimated minimiser.
+class BrentMinimizer {
+    double a_, b_, tol_;
+
+public:
+    BrentMinimizer(double a, double b, double tol) : a_(a), b_(b), tol_(tol) {
+        if (!(a < b)) throw std::runtime_error("a < b is required for Brent algorithm!");
+    }
+    double minimize(std::function<double(double)> f) const { return hbem_brent_min(detail::call_fn, &f, a_, b_, tol_); }
+};
+
+}  // namespace hbem

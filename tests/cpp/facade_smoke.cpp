@@ -1,0 +1,33 @@
+// Drop-in check of the C++ facade: the reference's call sequence
+// (examples/roots_newton_circle.cpp:92-138) written against include/hbem.hpp.
+#include <cmath>
+#include <cstdio>
+
+#include "hbem.hpp"
+
+int main() {
+    using namespace hbem;
+    Mesh mesh = Mesh::circle(0., 0., 0.25, 16);
+    BuilderData builder_data(mesh, P1, P1, 7);
+    SolutionsOperator so(builder_data);
+    MatrixXcd T, T_der, T_der2;
+    so.gen_sol_op_2nd_der(2.5, 1.0, 23.4, T, T_der, T_der2);
+    auto r = direct::sv_2nd_der(T, T_der, T_der2);
+    GalerkinBuilder builder(builder_data);
+    builder.assembleDense(2.5, 23.4, LayerType::ALL, 1);
+    const MatrixXcd& V1 = builder.getSingleLayer(1);
+    bool found = false;
+    unsigned it = 0;
+    double root = rtsafe([](double x) { return std::cos(x); },
+                         [](double x) { return std::vector<double>{std::cos(x), -std::sin(x)}; }, 1.0, 2.0, 1e-12,
+                         found, it);
+    bool threw = false;
+    try {
+        builder.assembleDense(1.0, 0.5);   // c < 1: the reference throws std::runtime_error
+    } catch (const std::runtime_error&) {
+        threw = true;
+    }
+    std::printf("%.17e %.17e %.17e %.17e %.17e %d %d\n", r[0], r[1], r[2], std::abs(V1(3, 5)), root, (int)found,
+                (int)threw);
+    return (found && threw) ? 0 : 1;
+}

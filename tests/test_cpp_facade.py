@@ -1,0 +1,40 @@
+"""The C++ facade (include/hbem.hpp) compiles against the C ABI; on a GPU it runs
+the reference's call sequence and agrees with the Python mirror."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SRC = os.path.join(ROOT, "tests", "cpp", "facade_smoke.cpp")
+LIBDIR = os.path.join(ROOT, "helmholtzbem_gb300", "_lib")
+
+
+def _compile(tmp_path):
+    exe = str(tmp_path / "facade_smoke")
+    cmd = ["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), SRC, "-o", exe,
+           "-L", LIBDIR, "-Wl,-rpath," + LIBDIR, "-lhbem"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_facade_compiles(tmp_path):
+    if not os.path.exists(os.path.join(LIBDIR, "libhbem.so")):
+        pytest.skip("libhbem.so not built")
+    _compile(tmp_path)
+
+
+@pytest.mark.gpu
+def test_facade_runs_and_matches_python(tmp_path):
+    exe = _compile(tmp_path)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    vals = [float(v) for v in r.stdout.split()]
+    from helmholtzbem_gb300 import api, geometry
+    data = api.BuilderData(geometry.circle(0.25, 16), order=7)
+    so = api.SolutionsOperator(data)
+    ref = api.sv_dense([so.gen_sol_op_2nd_der(2.5, 1.0, 23.4)], d=2)[0]
+    assert np.allclose(vals[:3], ref, rtol=1e-12, atol=0)
+    assert abs(vals[4] - np.pi / 2) < 1e-12 and vals[5] == 1 and vals[6] == 1

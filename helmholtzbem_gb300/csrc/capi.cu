@@ -194,6 +194,11 @@ cudaError_t local_assembly(const DevMesh& M, const SingularTask* tasks, int ntas
 
 }  // namespace
 
+namespace hbem {
+// error reporting for entry points defined in other translation units
+int set_error(int code, const char* msg) { return fail(code, msg); }
+}  // namespace hbem
+
 // ---------------------------------------------------------------- builder
 
 struct hbem_builder_s {

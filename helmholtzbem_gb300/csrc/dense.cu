@@ -236,4 +236,60 @@ cudaError_t launch_svd(int n, int nmat, int D, int which, const cplx* T, long lo
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- allocation-free variant
+//
+// Working memory of hbem_sv_dense_batch_noalloc: the right singular vectors V of
+// every matrix in the batch (nmat * n * n complex128).  It is a fixed array in
+// this library's device image, so every GPU that loads the library holds these
+// 8 MiB until the process exits.
+constexpr size_t kNoAllocScratchElems = size_t(1) << 19;   // complex128 elements: 8 MiB
+static __device__ __align__(256) cplx g_noalloc_scratch[kNoAllocScratchElems];
+
+int set_error(int code, const char* msg);
+
 }  // namespace hbem
+
+#include <mutex>
+
+#include "../../include/hbem.h"
+
+namespace {
+std::mutex g_noalloc_mu;
+constexpr int kMaxDevices = 64;
+void* g_noalloc_ptr[kMaxDevices] = {nullptr};   // device address of the scratch, per device
+}  // namespace
+
+// See include/hbem.h.  The matrix must fit in shared memory (n <= 116) because the
+// allocation-free path has no global scratch for A; V lives in the fixed array.
+extern "C" int hbem_sv_dense_batch_noalloc(int n, int nmat, unsigned d, const void* T_dev, long long mat_stride,
+                                           long long der_stride, double* out_dev, int* status_dev, void* stream) {
+    using namespace hbem;
+    if (n < 2 || nmat < 1 || d > 2 || !T_dev || !out_dev || !status_dev)
+        return set_error(HBEM_ERR_INVALID, "sv_dense_batch_noalloc: bad argument");
+    if (svd_smem_bytes(n, true) > 220 * 1024)
+        return set_error(HBEM_ERR_INVALID, "sv_dense_batch_noalloc: matrix order above 116 (the matrix must fit in shared memory)");
+    if ((size_t)nmat * (size_t)n * (size_t)n > kNoAllocScratchElems)
+        return set_error(HBEM_ERR_INVALID,
+                         "sv_dense_batch_noalloc: nmat * n * n exceeds the fixed scratch of 524288 complex elements (8 MiB)");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_error(HBEM_ERR_CUDA, cudaGetErrorString(e));
+    if (dev < 0 || dev >= kMaxDevices) return set_error(HBEM_ERR_INVALID, "sv_dense_batch_noalloc: device ordinal out of range");
+    void* scratch = nullptr;
+    {
+        // first call on a device: resolve the device address of the fixed array with
+        // that device current (the host-side name is only a stand-in, not a device address)
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void* p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess) return set_error(HBEM_ERR_CUDA, cudaGetErrorString(e));
+            g_noalloc_ptr[dev] = p;
+        }
+        scratch = g_noalloc_ptr[dev];
+    }
+    e = launch_svd(n, nmat, (int)d, 0, static_cast<const cplx*>(T_dev), mat_stride, der_stride, nullptr,
+                   static_cast<cplx*>(scratch), out_dev, nullptr, status_dev, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return set_error(HBEM_ERR_CUDA, cudaGetErrorString(e));
+    return HBEM_OK;
+}

@@ -119,6 +119,25 @@ int hbem_gen_sol_op_batch_device(hbem_solop s, const double* k_host, int nk, dou
 int hbem_sv_dense_batch_device(int n, int nmat, unsigned d, const void* T_dev, long long mat_stride,
                                long long der_stride, double* out_host, double* sig_all_host);
 
+/* Allocation-free form of hbem_sv_dense_batch_device.  No counterpart in the
+ * reference.  For callers that must not allocate device memory -- code running
+ * while a memory pool or allocator is locked, inside another library's
+ * pre-planned memory budget, or on a stream whose work must not trigger
+ * cudaMalloc / cudaFree synchronisation -- this call allocates nothing: it
+ * launches on `stream` (a cudaStream_t, NULL for the default stream) and returns
+ * without waiting.  The caller passes the inputs and the outputs on the device:
+ * out_dev (nmat x 3 doubles: sigma, sigma', sigma'') and status_dev (nmat ints,
+ * 0 = converged, 4 = Jacobi sweep limit reached).
+ * Working memory is a fixed 8 MiB array inside the library's device image
+ * (held on every GPU that loads the library until the process exits).  Limits:
+ * n <= 116 and nmat * n * n <= 524288; larger requests return HBEM_ERR_INVALID.
+ * The first call on each device resolves the array's device address (with that
+ * device current); make that first call before any stream capture.  All calls
+ * share the array and it keeps the previous call's contents: calls whose work
+ * overlaps on the GPU (different streams, or concurrent host threads) race on it. */
+int hbem_sv_dense_batch_noalloc(int n, int nmat, unsigned d, const void* T_dev, long long mat_stride,
+                                long long der_stride, double* out_dev, int* status_dev, void* stream);
+
 /* same with host matrices (copied to the device): T_host holds nmat blocks of
  * (d + 1) consecutive n x n matrices (T, T', T'') */
 int hbem_sv_dense_batch(int n, int nmat, unsigned d, const double* T_host, double* out_host, double* sig_all_host);

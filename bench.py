@@ -42,7 +42,22 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample-points", type=int, default=60)
+    ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline leg")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="no timing: three sigma sweeps over 16 wavenumbers of the workload (for ncu captures)")
     return ap.parse_args()
+
+
+def run_profile_case():
+    """Small fixed case for profiler captures: 3 x hbem_sweep_sigma over 16 k of the
+    workload's scatterer (each sweep: assembly, T gather, projection, dense SVD)."""
+    from helmholtzbem_gb300 import api, geometry
+    data = api.BuilderData(geometry.circle(CFG["radius"], CFG["N"]), order=CFG["order"])
+    so = api.SolutionsOperator(data)
+    ks = np.linspace(CFG["k_min"], CFG["k_max"], 16)
+    for _ in range(3):
+        out = so.sweep_sigma(ks, CFG["c_o"], CFG["c_i"], d=2)
+    print("profile case done, sigma_min(k0) = %.6e" % out[0, 0])
 
 
 def dist_env():
@@ -272,7 +287,7 @@ def run_gpu(args):
                 "avg_launch_ms": asm_ms.value / max(1, asm_l.value)}
 
     cpu = None
-    if rank == 0 and world == 1 or rank == 0:
+    if rank == 0 and not args.skip_cpu:
         threads = os.cpu_count() or 1
         try:
             v, tsec, npts = cpu_sample(args.cpu_sample_points, threads)
@@ -302,7 +317,9 @@ def run_gpu(args):
 
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.profile_case:
+        run_profile_case()
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

@@ -31,14 +31,29 @@ __device__ __forceinline__ KConst make_kconst(const Job& jb) {
     return K;
 }
 
-template <int D>
+// Moment accumulators.  With P1 shape functions every local entry is
+// sum_pts w phi_a(x) psi_b(y) kappa for a kernel value kappa and shape functions
+// linear in the two panel parameters x (panel i) and y (panel j), so four
+// moments per kernel value suffice:  [0] sum w k, [1] sum w x k, [2] sum w y k,
+// [3] sum w x y k.  Kernel values per derivative order t:
+//   s[t]  : {h0, h1|v|, q}   q = |v|^2 h0 - h1|v|/ks   (single layer, hypersingular)
+//   w[t]  : 2 (tau_i.tau_j) {h0, h1|v|, q}              (hypersingular, curved panels)
+//   dl[t] : (v x tau_j)|tau_i| {m1, h0, m3}             (double layer)
+//   dlt[t]: (tau_i x v)|tau_j| {m1, h0, m3}             (transposed double layer)
+// with m1 = ks h1/|v|, m3 = h0 - ks |v| h1.  For straight panels 2 tau_i.tau_j is
+// constant per pair and w is folded into s when the blocks are formed.
+template <int D, bool CURVED>
 struct Acc {
-    cplx dl[D + 1][4], dlt[D + 1][4], hy[D + 1][4], sl[D + 1][4];
+    cplx s[D + 1][4], dl[D + 1][4], dlt[D + 1][4], w[CURVED ? D + 1 : 1][4];
     __device__ __forceinline__ void zero() {
 #pragma unroll
         for (int t = 0; t <= D; ++t)
 #pragma unroll
-            for (int e = 0; e < 4; ++e) dl[t][e] = dlt[t][e] = hy[t][e] = sl[t][e] = mk(0.);
+            for (int e = 0; e < 4; ++e) s[t][e] = dl[t][e] = dlt[t][e] = mk(0.);
+#pragma unroll
+        for (int t = 0; t < (CURVED ? D + 1 : 1); ++t)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) w[t][e] = mk(0.);
     }
 };
 
@@ -52,88 +67,129 @@ __device__ __forceinline__ void hankel_at(const KConst& K, double vn, cplx& h0, 
 template <bool RK>
 __device__ __forceinline__ cplx kmul(cplx a, cplx z) { return RK ? a.re * z : a * z; }
 
-// One quadrature point's contribution to all local blocks.
-//   fi, gj : shape values (test on panel i at x, trial on panel j at y)
-//   fj, gi : for the transposed double layer (test on panel j at y, trial on i at x)
-//   vd, vdt: v x n factors (0 when that block is switched off for the pair)
+// Kernel values of one quadrature point (see Acc).
 template <int D, bool RK>
-__device__ __forceinline__ void point_contrib(Acc<D>& A, const KConst& K, double w, double vn, double vn2,
-                                              cplx h0, cplx h1, double vd, double vdt, const double fi[2],
-                                              const double gj[2], const double fj[2], const double gi[2],
-                                              double ttp, double tdt, bool tz) {
-    const double dsh[2] = {1., -1.};
-    cplx m1 = vn > 0. ? kmul<RK>(K.ks, (1.0 / vn) * h1) : mk(0.);
-    cplx hv = vn * h1;
-    cplx m3, q, r2;
-    if (D > 1) {
-        m3 = h0 - kmul<RK>(K.ks, hv);
-        q = vn2 * h0 - kmul<RK>(K.ks_inv, hv);
-        r2 = kmul<RK>(K.ks_two, hv) - h0;
+struct KVals {
+    cplx s[D + 1], d[D + 1];
+};
+
+template <int D, bool RK>
+__device__ __forceinline__ KVals<D, RK> kernel_values(const KConst& K, double vn, double vn2, cplx h0, cplx h1) {
+    KVals<D, RK> kv;
+    kv.s[0] = h0;
+    kv.d[0] = vn > 0. ? kmul<RK>(K.ks, (1.0 / vn) * h1) : mk(0.);
+    if (D > 0) {
+        cplx hv = vn * h1;
+        kv.s[1] = hv;
+        kv.d[1] = h0;
+        if (D > 1) {
+            kv.s[2] = vn2 * h0 - kmul<RK>(K.ks_inv, hv);
+            kv.d[2] = h0 - kmul<RK>(K.ks, hv);
+        }
     }
+    return kv;
+}
+
+__device__ __forceinline__ void moments4(cplx (&m)[4], const double wm[4], cplx k) {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) axpy(m[e], wm[e], k);
+}
+
+// single layer / hypersingular moments (weights wm = {w, w x, w y, w x y})
+template <int D, bool RK, bool CURVED>
+__device__ __forceinline__ void acc_s(Acc<D, CURVED>& A, const double wm[4], const KVals<D, RK>& kv, double tdt,
+                                      bool with_w) {
+#pragma unroll
+    for (int t = 0; t <= D; ++t) moments4(A.s[t], wm, kv.s[t]);
+    if (CURVED && with_w) {
+#pragma unroll
+        for (int t = 0; t <= D; ++t) moments4(A.w[CURVED ? t : 0], wm, tdt * kv.s[t]);
+    }
+}
+
+template <int D, bool RK, bool CURVED>
+__device__ __forceinline__ void acc_dl(Acc<D, CURVED>& A, const double wm[4], const KVals<D, RK>& kv, double vd) {
+#pragma unroll
+    for (int t = 0; t <= D; ++t) moments4(A.dl[t], wm, vd * kv.d[t]);
+}
+
+template <int D, bool RK, bool CURVED>
+__device__ __forceinline__ void acc_dlt(Acc<D, CURVED>& A, const double wm[4], const KVals<D, RK>& kv, double vdt) {
+#pragma unroll
+    for (int t = 0; t <= D; ++t) moments4(A.dlt[t], wm, vdt * kv.d[t]);
+}
+
+__device__ __forceinline__ void mom_weights(double w, double x, double y, double wm[4]) {
+    wm[0] = w;
+    wm[1] = w * x;
+    wm[2] = w * y;
+    wm[3] = wm[1] * y;
+}
+
+// P1 shape function a on [0,1] as alpha + beta u: forward (t, 1-t) or reversed (1-t, t)
+__device__ __forceinline__ void shape_ab(int a, bool reversed, double& al, double& be) {
+    if ((a == 0) != reversed) { al = 0.; be = 1.; }
+    else { al = 1.; be = -1.; }
+}
+
+// entry of sum w phi_a(x) psi_b(y) k from the moments
+__device__ __forceinline__ cplx entry_xy(const cplx (&m)[4], int a, bool rx, int b, bool ry) {
+    double ax, bx, ay, by;
+    shape_ab(a, rx, ax, bx);
+    shape_ab(b, ry, ay, by);
+    return (ax * ay) * m[0] + (bx * ay) * m[1] + (ax * by) * m[2] + (bx * by) * m[3];
+}
+// entry of sum w phi_a(y) psi_b(x) k (test function on the y panel)
+__device__ __forceinline__ cplx entry_yx(const cplx (&m)[4], int a, bool ry, int b, bool rx) {
+    double ay, by, ax, bx;
+    shape_ab(a, ry, ay, by);
+    shape_ab(b, rx, ax, bx);
+    return (ay * ax) * m[0] + (ay * bx) * m[1] + (by * ax) * m[2] + (by * bx) * m[3];
+}
+
+// Form the local blocks from the moments, scale the derivative orders and store.
+//   rx, ry : shape functions on panel i (x) / panel j (y) reversed (adjacent pairs)
+//   ttp    : |tau_i||tau_j| (constant per pair: lines and circular arcs)
+//   tdt    : 2 tau_i.tau_j for straight panels (constant per pair); ignored when CURVED
+//   tz     : the tangent product vanishes for the pair -> no k^2 term in W
+template <int D, bool CURVED>
+__device__ __forceinline__ void store_local(const Acc<D, CURVED>& A, const KConst& K, bool rx, bool ry, double ttp,
+                                            double tdt, bool tz, cplx* dst) {
+    const cplx kc = K.c * K.k;
 #pragma unroll
     for (int a = 0; a < 2; ++a) {
 #pragma unroll
         for (int b = 0; b < 2; ++b) {
             const int e = 2 * a + b;
-            double fg = fi[a] * gj[b] * w;
-            // single layer
-            double cfr = ttp * fg;
-            axpy(A.sl[0][e], cfr, h0);
-            if (D > 0) axpy(A.sl[1][e], cfr, hv);
-            if (D > 1) axpy(A.sl[2][e], -cfr, q);
-            // double layer
-            double cd = vd * fg;
-            axpy(A.dl[0][e], cd, m1);
-            if (D > 0) axpy(A.dl[1][e], cd, h0);
-            if (D > 1) axpy(A.dl[2][e], cd, m3);
-            double cdt = vdt * (fj[a] * gi[b] * w);
-            axpy(A.dlt[0][e], cdt, m1);
-            if (D > 0) axpy(A.dlt[1][e], cdt, h0);
-            if (D > 1) axpy(A.dlt[2][e], cdt, m3);
-            // hypersingular
-            double arc = dsh[a] * dsh[b] * w;
-            double temp = tz ? 0. : fg * tdt;
-            if (RK) {
-                double cf = arc - K.k2ch.re * temp;
-                axpy(A.hy[0][e], cf, h0);
-                if (D > 0) {
-                    axpy(A.hy[1][e], cf, hv);
-                    axpy(A.hy[1][e], K.ks.re * temp, h0);
-                }
-                if (D > 1) {
-                    axpy(A.hy[2][e], cf, q);
-                    axpy(A.hy[2][e], -temp, r2);
-                }
-            } else {
-                cplx cf = mk(arc) - temp * K.k2ch;
-                A.hy[0][e] += cf * h0;
-                if (D > 0) A.hy[1][e] += cf * hv + (temp * K.ks) * h0;
-                if (D > 1) A.hy[2][e] += cf * q - temp * r2;
-            }
-        }
-    }
-}
-
-// scale derivative blocks and store a pair's local blocks
-template <int D>
-__device__ __forceinline__ void store_local(const Acc<D>& A, const KConst& K, cplx* dst) {
-    cplx kc = K.c * K.k;
+            const double dd = (a == b) ? 1. : -1.;   // b'_a b'_b for P1 (+1, -1)
+            cplx T[D + 1], S[D + 1];
 #pragma unroll
-    for (int t = 0; t <= D; ++t) {
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            cplx dl = A.dl[t][e], dlt = A.dlt[t][e], hy = A.hy[t][e], sl = A.sl[t][e];
-            if (t == 1) {
-                dl = dl * kc; dlt = dlt * kc;
-                hy = -K.sqrtc * hy; sl = -K.sqrtc * sl;
-            } else if (t == 2) {
-                dl = K.c * dl; dlt = K.c * dlt;
-                hy = -K.c * hy; sl = K.c * sl;
+            for (int t = 0; t <= D; ++t) {
+                S[t] = A.s[t][0];
+                if (tz) T[t] = mk(0.);
+                else if (CURVED) T[t] = entry_xy(A.w[CURVED ? t : 0], a, rx, b, ry);
+                else T[t] = tdt * entry_xy(A.s[t], a, rx, b, ry);
             }
-            dst[t * kLocPerD + 0 + e] = dl;
-            dst[t * kLocPerD + 4 + e] = dlt;
-            dst[t * kLocPerD + 8 + e] = hy;
-            dst[t * kLocPerD + 12 + e] = sl;
+#pragma unroll
+            for (int t = 0; t <= D; ++t) {
+                cplx dl = entry_xy(A.dl[t], a, rx, b, ry);
+                cplx dlt = entry_yx(A.dlt[t], a, ry, b, rx);
+                cplx sl = ttp * entry_xy(A.s[t], a, rx, b, ry);
+                cplx hy = dd * S[t] - K.k2ch * T[t];
+                if (t == 1) hy += K.ks * T[0];
+                if (t == 2) hy -= K.ks_two * T[1] - T[0];
+                if (t == 1) {
+                    dl = dl * kc; dlt = dlt * kc;
+                    hy = -K.sqrtc * hy; sl = -K.sqrtc * sl;
+                } else if (t == 2) {
+                    dl = K.c * dl; dlt = K.c * dlt;
+                    hy = -K.c * hy; sl = -K.c * sl;   // single layer: c * (-q)
+                }
+                dst[t * kLocPerD + 0 + e] = dl;
+                dst[t * kLocPerD + 4 + e] = dlt;
+                dst[t * kLocPerD + 8 + e] = hy;
+                dst[t * kLocPerD + 12 + e] = sl;
+            }
         }
     }
 }
@@ -284,7 +340,7 @@ __global__ void k_flags_singular(DevMesh M, const SingularTask* tasks, uint8_t* 
 
 // ------------------------------------------------------------------ local-block kernels
 
-template <int D, bool RK>
+template <int D, bool RK, bool CURVED>
 __global__ void __launch_bounds__(128) k_general(DevMesh M, const Job* jobs, cplx* loc, long long npair) {
     __shared__ double sx[64], sw[64];
     for (int t = threadIdx.x; t < M.p; t += blockDim.x) { sx[t] = M.xg[t]; sw[t] = M.wg[t]; }
@@ -309,33 +365,35 @@ __global__ void __launch_bounds__(128) k_general(DevMesh M, const Job* jobs, cpl
     const cplx* tgj = M.gtan + j * p;
     const double* tni = M.gtn + i * p;
     const double* tnj = M.gtn + j * p;
-    Acc<D> A;
+    Acc<D, CURVED> A;
     A.zero();
     for (int a = 0; a < p; ++a) {
         const cplx xi = pti[a], ti = tgi[a];
         const double tin = tni[a], s = sx[a], wa = sw[a];
-        const double fi[2] = {s, 1. - s};
         for (int b = 0; b < p; ++b) {
             const cplx yj = ptj[b], tj = tgj[b];
-            const double tjn = tnj[b], t = sx[b];
-            const double gj[2] = {t, 1. - t};
+            const double tjn = tnj[b];
             const cplx v = xi - yj;
             const double vn2 = norm2(v), vn = sqrt(vn2);
             cplx h0, h1;
             hankel_at<RK>(K, vn, h0, h1);
+            const KVals<D, RK> kv = kernel_values<D, RK>(K, vn, vn2, h0, h1);
+            double wm[4];
+            mom_weights(wa * sw[b], s, sx[b], wm);
+            acc_s<D, RK, CURVED>(A, wm, kv, 2. * (ti.im * tj.im + ti.re * tj.re), !tz);
             // general: zero test on v x tau_j before the norm (galerkin_builder.cpp:475-499)
-            double vd = use_dl ? (v.re * tj.im - v.im * tj.re) * tin : 0.;
-            double vdt = use_dlt ? (v.im * ti.re - v.re * ti.im) * tjn : 0.;
-            double tdt = 2. * (ti.im * tj.im + ti.re * tj.re);
-            point_contrib<D, RK>(A, K, wa * sw[b], vn, vn2, h0, h1, vd, vdt, fi, gj, gj, fi, tin * tjn, tdt, tz);
+            if (use_dl) acc_dl<D, RK, CURVED>(A, wm, kv, (v.re * tj.im - v.im * tj.re) * tin);
+            if (use_dlt) acc_dlt<D, RK, CURVED>(A, wm, kv, (v.im * ti.re - v.re * ti.im) * tjn);
         }
     }
-    store_local<D>(A, K, loc + ((long long)job * npair + pid) * (D + 1) * kLocPerD);
+    const cplx t0i = tgi[0], t0j = tgj[0];
+    store_local<D, CURVED>(A, K, false, false, tni[0] * tnj[0], 2. * (t0i.im * t0j.im + t0i.re * t0j.re), tz,
+                           loc + ((long long)job * npair + pid) * (D + 1) * kLocPerD);
 }
 
-template <int D>
-__device__ __forceinline__ void block_reduce(Acc<D>& A, double* red /* [nwarps][4*(D+1)*4*2] */) {
-    constexpr int NV = 4 * (D + 1) * 4 * 2;
+template <class AccT>
+__device__ __forceinline__ void block_reduce(AccT& A, double* red /* [nwarps][sizeof(AccT)/8] */) {
+    constexpr int NV = (int)(sizeof(AccT) / sizeof(double));
     double* a = reinterpret_cast<double*>(&A);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
@@ -358,7 +416,7 @@ __device__ __forceinline__ void block_reduce(Acc<D>& A, double* red /* [nwarps][
     }
 }
 
-template <int D, bool RK>
+template <int D, bool RK, bool CURVED>
 __global__ void __launch_bounds__(128) k_singular(DevMesh M, const SingularTask* tasks, const Job* jobs, cplx* loc,
                                                   long long npair) {
     extern __shared__ double sm[];
@@ -373,32 +431,32 @@ __global__ void __launch_bounds__(128) k_singular(DevMesh M, const SingularTask*
     const long long pid = tri_index(T.i, T.j);
     const uint8_t fl = M.flags[pid];
     const int nc = M.nc, tot = nc * nc;
-    Acc<D> A;
+    Acc<D, CURVED> A;
     A.zero();
     for (int e = threadIdx.x; e < tot; e += blockDim.x) {
         const int a = e % nc, b = e / nc;
         const double wab = swc[a] * swc[b];
         if (T.kind == PK_COINC) {
+            // one point serves both triangles: set 0 has (x, y) = (s, t), set 1 (t, s)
             SPoint P;
             singular_point(M, T, 0, sxc[a], sxc[b], P);
             const double w = sxc[b] * wab;
             const double vn2 = norm2(P.v), vn = sqrt(vn2);
             cplx h0, h1;
             hankel_at<RK>(K, vn, h0, h1);
-            const double ttp = P.tin * P.tjn;
-            const bool tz = (fl & PF_TDT0_ZERO) != 0;
-            const double tdt = 2. * (P.ti.im * P.tj.im + P.ti.re * P.tj.re);
-            // set 0: x = s (panel i test side), y = t
-            {
-                double vd = (fl & PF_DL0_ZERO) ? 0. : (P.v.re * P.tj.im - P.v.im * P.tj.re) * P.tin;
-                const double fi[2] = {P.x, 1. - P.x}, gj[2] = {P.y, 1. - P.y};
-                point_contrib<D, RK>(A, K, w, vn, vn2, h0, h1, vd, 0., fi, gj, fi, gj, ttp, tdt, tz);
+            const KVals<D, RK> kv = kernel_values<D, RK>(K, vn, vn2, h0, h1);
+            const double s = P.x, t = P.y;
+            // V and W kernels are symmetric in s <-> t: both sets in one moment update
+            const double wsym[4] = {2. * w, w * (s + t), w * (s + t), 2. * w * s * t};
+            acc_s<D, RK, CURVED>(A, wsym, kv, 2. * (P.ti.im * P.tj.im + P.ti.re * P.tj.re), !(fl & PF_TDT0_ZERO));
+            double wm[4];
+            if (!(fl & PF_DL0_ZERO)) {
+                mom_weights(w, s, t, wm);
+                acc_dl<D, RK, CURVED>(A, wm, kv, (P.v.re * P.tj.im - P.v.im * P.tj.re) * P.tin);
             }
-            // set 1: roles of s and t exchanged, v -> -v
-            {
-                double vd = (fl & PF_DL1_ZERO) ? 0. : (P.v.im * P.ti.re - P.v.re * P.ti.im) * P.tjn;
-                const double fi[2] = {P.y, 1. - P.y}, gj[2] = {P.x, 1. - P.x};
-                point_contrib<D, RK>(A, K, w, vn, vn2, h0, h1, vd, 0., fi, gj, fi, gj, ttp, tdt, tz);
+            if (!(fl & PF_DL1_ZERO)) {
+                mom_weights(w, t, s, wm);
+                acc_dl<D, RK, CURVED>(A, wm, kv, (P.v.im * P.ti.re - P.v.re * P.ti.im) * P.tjn);
             }
         } else {
             const double w = sxc[a] * wab;
@@ -409,31 +467,30 @@ __global__ void __launch_bounds__(128) k_singular(DevMesh M, const SingularTask*
                 const double vn2 = norm2(P.v), vn = sqrt(vn2);
                 cplx h0, h1;
                 hankel_at<RK>(K, vn, h0, h1);
+                const KVals<D, RK> kv = kernel_values<D, RK>(K, vn, vn2, h0, h1);
                 const uint8_t dlz = Kset == 0 ? PF_DL0_ZERO : PF_DL1_ZERO;
                 const uint8_t dltz = Kset == 0 ? PF_DLT0_ZERO : PF_DLT1_ZERO;
                 const uint8_t tdz = Kset == 0 ? PF_TDT0_ZERO : PF_TDT1_ZERO;
-                double vd = (fl & dlz) ? 0. : (P.v.re * P.tj.im - P.v.im * P.tj.re) * P.tin;
-                double vdt = (fl & dltz) ? 0. : (P.v.im * P.ti.re - P.v.re * P.ti.im) * P.tjn;
-                double tdt = 2. * (P.ti.im * P.tj.im + P.ti.re * P.tj.re);
-                double fi[2], gj[2], fj[2], gi[2];
-                if (!T.swap) {   // panel i reversed, panel j forward
-                    fi[0] = 1. - P.x; fi[1] = P.x;
-                    gj[0] = P.y; gj[1] = 1. - P.y;
-                    fj[0] = P.y; fj[1] = 1. - P.y;
-                    gi[0] = 1. - P.x; gi[1] = P.x;
-                } else {         // panel i forward, panel j reversed
-                    fi[0] = P.x; fi[1] = 1. - P.x;
-                    gj[0] = 1. - P.y; gj[1] = P.y;
-                    fj[0] = 1. - P.y; fj[1] = P.y;
-                    gi[0] = P.x; gi[1] = 1. - P.x;
-                }
-                point_contrib<D, RK>(A, K, w, vn, vn2, h0, h1, vd, vdt, fi, gj, fj, gi, P.tin * P.tjn, tdt,
-                                     (fl & tdz) != 0);
+                double wm[4];
+                mom_weights(w, P.x, P.y, wm);
+                acc_s<D, RK, CURVED>(A, wm, kv, 2. * (P.ti.im * P.tj.im + P.ti.re * P.tj.re), !(fl & tdz));
+                if (!(fl & dlz)) acc_dl<D, RK, CURVED>(A, wm, kv, (P.v.re * P.tj.im - P.v.im * P.tj.re) * P.tin);
+                if (!(fl & dltz)) acc_dlt<D, RK, CURVED>(A, wm, kv, (P.v.im * P.ti.re - P.v.re * P.ti.im) * P.tjn);
             }
         }
     }
-    block_reduce<D>(A, red);
-    if (threadIdx.x == 0) store_local<D>(A, K, loc + ((long long)job * npair + pid) * (D + 1) * kLocPerD);
+    block_reduce(A, red);
+    if (threadIdx.x == 0) {
+        // per-pair constants: tangent norms (constant on lines and arcs) and, for
+        // straight panels, the tangent product
+        SPoint P;
+        singular_point(M, T, 0, sxc[0], sxc[0], P);
+        const bool adj = T.kind == PK_ADJ;
+        const bool tz = CURVED ? false : (fl & PF_TDT0_ZERO) != 0;
+        store_local<D, CURVED>(A, K, adj && !T.swap, adj && T.swap, P.tin * P.tjn,
+                               2. * (P.ti.im * P.tj.im + P.ti.re * P.tj.re), tz,
+                               loc + ((long long)job * npair + pid) * (D + 1) * kLocPerD);
+    }
 }
 
 // ------------------------------------------------------------------ gather
@@ -533,22 +590,29 @@ cudaError_t launch_hankel01(int n, const cplx* z, int complex_arg, cplx* h0, cpl
 
 // ------------------------------------------------------------------ launchers
 
-template <int D, bool RK>
-static cudaError_t launch_local_t(const DevMesh& M, const SingularTask* tasks, int ntasks, const Job* jobs, int njobs,
+template <int D, bool RK, bool CURVED>
+static cudaError_t launch_local_c(const DevMesh& M, const SingularTask* tasks, int ntasks, const Job* jobs, int njobs,
                                   cplx* loc, cudaStream_t st) {
     long long npair = (long long)M.n * (M.n + 1) / 2;
     long long nlow = (long long)M.n * (M.n - 1) / 2;
     if (nlow > 0) {
         dim3 g((unsigned)((nlow + 127) / 128), njobs);
-        k_general<D, RK><<<g, 128, 0, st>>>(M, jobs, loc, npair);
+        k_general<D, RK, CURVED><<<g, 128, 0, st>>>(M, jobs, loc, npair);
     }
     if (ntasks > 0) {
-        constexpr int NV = 4 * (D + 1) * 4 * 2;
+        constexpr int NV = (int)(sizeof(Acc<D, CURVED>) / sizeof(double));
         size_t smem = (2 * (size_t)M.nc + 4 * NV) * sizeof(double);
         dim3 g(ntasks, njobs);
-        k_singular<D, RK><<<g, 128, smem, st>>>(M, tasks, jobs, loc, npair);
+        k_singular<D, RK, CURVED><<<g, 128, smem, st>>>(M, tasks, jobs, loc, npair);
     }
     return cudaGetLastError();
+}
+
+template <int D, bool RK>
+static cudaError_t launch_local_t(const DevMesh& M, const SingularTask* tasks, int ntasks, const Job* jobs, int njobs,
+                                  cplx* loc, cudaStream_t st) {
+    if (M.lines) return launch_local_c<D, RK, false>(M, tasks, ntasks, jobs, njobs, loc, st);
+    return launch_local_c<D, RK, true>(M, tasks, ntasks, jobs, njobs, loc, st);
 }
 
 cudaError_t launch_flags(const DevMesh& M, const SingularTask* tasks, int ntasks, uint8_t* flags, cudaStream_t st) {

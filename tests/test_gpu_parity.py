@@ -170,3 +170,44 @@ def test_errors_like_reference():
         gb.getDoubleLayer(0)                    # layer not assembled
     with pytest.raises(HbemError):
         gb.getSingleLayer(1)                    # derivative not assembled
+
+
+def _config2_mesh(N=1000):
+    """Assembly-at-scale scatterer: seeded star polygon, 24 vertices, r = 1 + 0.3 u,
+    N line panels split in proportion to edge length."""
+    return geometry.polygon(*geometry.star_polygon(24, seed=2), N)
+
+
+def test_config2_reduced_vs_oracle():
+    """Same polygon family at N = 200, Gauss order 16, k = 20, c = 4, d <= 2."""
+    kinds, par = _config2_mesh(200)
+    data = api.BuilderData((kinds, par), order=16)
+    gb = api.GalerkinBuilder(data)
+    ob = O.Builder(kinds, par, 16)
+    gb.assembleDense(20.0, 4.0, api.LayerType_ALL, 2)
+    ref = ob.assemble(20.0, 4.0, O.LAYER_ALL, 2)
+    for t in range(3):
+        assert rel(gb.getDoubleLayer(t), ref["K"][t]) < 1e-12
+        assert rel(gb.getHypersingular(t), ref["W"][t]) < 1e-12
+        assert rel(gb.getSingleLayer(t), ref["V"][t]) < 1e-12
+
+
+def test_config2_full_size_properties():
+    """N = 1000, order 16, k = 20, both media: size-independent properties of the full
+    T(k), T', T'': V, W symmetric, and T', T'' consistent with central differences of
+    the GPU's own T at k +- h (the oracle checks the same family at N = 200 above)."""
+    kinds, par = _config2_mesh(1000)
+    data = api.BuilderData((kinds, par), order=16)
+    gb = api.GalerkinBuilder(data)
+    gb.assembleDense(20.0, 4.0, api.LayerType_ALL, 2)
+    for t in range(3):
+        V, W = gb.getSingleLayer(t), gb.getHypersingular(t)
+        assert np.abs(V - V.T).max() <= 1e-13 * np.abs(V).max()
+        assert np.abs(W - W.T).max() <= 1e-13 * np.abs(W).max()
+    so = api.SolutionsOperator(data)
+    h = 1e-4
+    T, T1, T2 = so.gen_sol_op_2nd_der(20.0, 1.0, 4.0)
+    Tp = so.gen_sol_op(20.0 + h, 1.0, 4.0)
+    Tm = so.gen_sol_op(20.0 - h, 1.0, 4.0)
+    assert rel((Tp - Tm) / (2 * h), T1) < 1e-6
+    assert rel((Tp - 2 * T + Tm) / h ** 2, T2) < 1e-3

@@ -190,6 +190,48 @@ def fp64_peak_tflops():
     return best
 
 
+def assembly_at_scale(torch, C, api, geometry, lib, peak):
+    """Assembly-at-scale configuration: seeded star polygon (24 vertices, r = 1 + 0.3 u),
+    N = 1000 line panels, Gauss order 16, c_i = 4, c_o = 1, k = 20: T, T', T'' (2000 x
+    2000 complex128, both media, projected) on the device.  Reports T-sets/s and the
+    assembly kernels' algorithmic FP64 rate (CUDA events on their stream)."""
+    N, order, k = 1000, 16, 20.0
+    data = api.BuilderData(geometry.polygon(*geometry.star_polygon(24, seed=2), N), order=order)
+    so = api.SolutionsOperator(data)
+    n = 2 * N
+    T = torch.empty((3, n, n), dtype=torch.complex128, device="cuda")
+    ks = np.array([k])
+
+    def one():
+        C.check(lib.hbem_gen_sol_op_batch_device(so._h, C.dptr(ks), 1, 1.0, 4.0, 2, C.ctypes.c_void_p(T.data_ptr())))
+
+    one()
+    torch.cuda.synchronize()
+    lib.hbem_stats_reset()
+    lib.hbem_stats_enable_timing(1)
+    reps = 2
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        one()
+    e1.record()
+    torch.cuda.synchronize()
+    lib.hbem_stats_enable_timing(0)
+    ms = e0.elapsed_time(e1) / reps
+    launches, asm_ms, asm_l, asm_pts = (C.ctypes.c_longlong(), C.ctypes.c_double(), C.ctypes.c_longlong(),
+                                        C.ctypes.c_longlong())
+    lib.hbem_stats_read(C.ctypes.byref(launches), C.ctypes.byref(asm_ms), C.ctypes.byref(asm_l),
+                        C.ctypes.byref(asm_pts))
+    achieved = asm_pts.value * 480.0 / (asm_ms.value * 1e-3) / 1e12 if asm_ms.value > 0 else 0.0
+    del T
+    return {"workload": "star polygon 24 vertices (seed 2), N=1000 lines, order 16, k=20, c_i=4, c_o=1, "
+                        "T/T'/T'' 2000x2000 c128 projected",
+            "ms_per_T_set": ms, "T_sets_per_s": 1e3 / ms,
+            "quad_points_per_T_set": asm_pts.value // reps,
+            "assembly_ms_per_T_set": asm_ms.value / reps,
+            "assembly_fp64_tflops": achieved, "assembly_frac_of_measured_fp64": achieved / peak if peak else None}
+
+
 def run_gpu(args):
     rank, world, local = dist_env()
     import torch
@@ -286,6 +328,8 @@ def run_gpu(args):
                 "kernel": "k_general + k_singular (panel-pair assembly)", "launches": asm_l.value,
                 "avg_launch_ms": asm_ms.value / max(1, asm_l.value)}
 
+    scale = assembly_at_scale(torch, C, api, geometry, lib, peak)
+
     cpu = None
     if rank == 0 and not args.skip_cpu:
         threads = os.cpu_count() or 1
@@ -307,6 +351,7 @@ def run_gpu(args):
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches.value),
             "roofline": roofline,
+            "assembly_at_scale": scale,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }

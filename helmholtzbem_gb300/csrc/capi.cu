@@ -22,6 +22,9 @@ cudaError_t launch_projection(int N, const double* id, const double* sb, const d
                               cudaStream_t st);
 cudaError_t launch_svd(int n, int nmat, int D, int which, const cplx* T, long long mat_stride, long long der_stride,
                        cplx* gA, cplx* gV, double* out, double* sig_all, int* status, cudaStream_t st);
+cudaError_t launch_svd_mixed(int n, int nmat, int D, int which, const cplx* T, long long mat_stride,
+                             long long der_stride, cplx* gA, cplx* gV, double* out, double* sig_all, int* status,
+                             cudaStream_t st);
 cudaError_t launch_hankel01(int n, const cplx* z, int complex_arg, cplx* h0, cplx* h1, cudaStream_t st);
 }  // namespace hbem
 
@@ -627,8 +630,8 @@ static int sv_batch(cudaStream_t st, int n, int nmat, unsigned d, const cplx* T,
         HB_CK(sig->ensure((size_t)nmat * n * sizeof(double)));
         dsig = sig->as<double>();
     }
-    HB_CK(launch_svd(n, nmat, (int)d, 0, T, mat_stride, der_stride, A.as<cplx>(), V.as<cplx>(), out.as<double>(), dsig,
-                     status.as<int>(), st));
+    HB_CK(launch_svd_mixed(n, nmat, (int)d, 0, T, mat_stride, der_stride, A.as<cplx>(), V.as<cplx>(),
+                           out.as<double>(), dsig, status.as<int>(), st));
     g_launches += 1;
     HB_CK(cudaMemcpyAsync(out_host, out.p, (size_t)nmat * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (sig_all_host)

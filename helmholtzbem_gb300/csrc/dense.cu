@@ -44,6 +44,128 @@ struct SvdJob {
     int a_in_smem;
 };
 
+// single-precision complex for the first Jacobi stage of the mixed-precision kernel
+struct cpf {
+    float re, im;
+};
+__device__ __forceinline__ cpf mkf(float r, float i) { cpf z; z.re = r; z.im = i; return z; }
+
+__device__ __forceinline__ float warp_sumf(float x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+}
+
+// Stage 1 of the mixed-precision path: one-sided Jacobi of T in FP32 (A32 and V32
+// both in shared memory), to the FP32 noise level.  Only V32 is used afterwards.
+__device__ void jacobi_fp32(const cplx* T0, int n, cpf* A32, cpf* V32, int* s_rot) {
+    const int np = n + (n & 1), m = np - 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        cplx t = T0[e];
+        A32[e] = mkf((float)t.re, (float)t.im);
+        V32[e] = mkf((e % n) == (e / n) ? 1.f : 0.f, 0.f);
+    }
+    __syncthreads();
+    const float tol = 4e-6f;
+    for (int sweep = 0; sweep < 30; ++sweep) {
+        if (threadIdx.x == 0) *s_rot = 0;
+        __syncthreads();
+        for (int r = 0; r < m; ++r) {
+            for (int k = warp; k < np / 2; k += nw) {
+                int p, q;
+                rr_pair(r, k, m, p, q);
+                if (p >= n || q >= n) continue;
+                if (p > q) { int t = p; p = q; q = t; }
+                cpf* ap = A32 + p * n;
+                cpf* aq = A32 + q * n;
+                float al = 0.f, be = 0.f, gr = 0.f, gi = 0.f;
+                for (int i = lane; i < n; i += 32) {
+                    cpf x = ap[i], y = aq[i];
+                    al = fmaf(x.re, x.re, fmaf(x.im, x.im, al));
+                    be = fmaf(y.re, y.re, fmaf(y.im, y.im, be));
+                    gr = fmaf(x.re, y.re, fmaf(x.im, y.im, gr));
+                    gi = fmaf(x.re, y.im, fmaf(-x.im, y.re, gi));
+                }
+                al = warp_sumf(al); be = warp_sumf(be); gr = warp_sumf(gr); gi = warp_sumf(gi);
+                float g = hypotf(gr, gi);
+                if (g == 0.f || g <= tol * sqrtf(al * be)) continue;
+                if (lane == 0) *s_rot = 1;
+                float zeta = (be - al) / (2.f * g);
+                float t = (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+                float c = 1.f / sqrtf(1.f + t * t), s = c * t;
+                float er = gr / g, ei = -gi / g;
+                cpf* vp = V32 + p * n;
+                cpf* vq = V32 + q * n;
+                for (int i = lane; i < n; i += 32) {
+                    cpf x = ap[i], y0 = aq[i];
+                    cpf y = mkf(er * y0.re - ei * y0.im, er * y0.im + ei * y0.re);
+                    ap[i] = mkf(c * x.re - s * y.re, c * x.im - s * y.im);
+                    aq[i] = mkf(s * x.re + c * y.re, s * x.im + c * y.im);
+                    cpf xv = vp[i], yv0 = vq[i];
+                    cpf yv = mkf(er * yv0.re - ei * yv0.im, er * yv0.im + ei * yv0.re);
+                    vp[i] = mkf(c * xv.re - s * yv.re, c * xv.im - s * yv.im);
+                    vq[i] = mkf(s * xv.re + c * yv.re, s * xv.im + c * yv.im);
+                }
+            }
+            __syncthreads();
+        }
+        if (*s_rot == 0) break;
+        __syncthreads();
+    }
+}
+
+// Stage 2: V = orthonormalised columns of V32 in FP64 (classical Gram-Schmidt; one
+// pass suffices because V32 is unitary to the FP32 level).  vcol, red: smem scratch.
+__device__ void orthonormalise_fp64(const cpf* V32, int n, cplx* V, cplx* vcol, cplx* coef, double* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int j = 0; j < n; ++j) {
+        for (int r = threadIdx.x; r < n; r += blockDim.x) vcol[r] = mk((double)V32[j * n + r].re, (double)V32[j * n + r].im);
+        __syncthreads();
+        for (int i = warp; i < j; i += nw) {       // coef_i = v_i^H vcol
+            const cplx* vi = V + (long long)i * n;
+            double cr = 0., ci = 0.;
+            for (int r = lane; r < n; r += 32) {
+                cplx a = vi[r], b = vcol[r];
+                cr = fma(a.re, b.re, fma(a.im, b.im, cr));
+                ci = fma(a.re, b.im, fma(-a.im, b.re, ci));
+            }
+            cr = warp_sum(cr);
+            ci = warp_sum(ci);
+            if (lane == 0) coef[i] = mk(cr, ci);
+        }
+        __syncthreads();
+        double part = 0.;
+        for (int r = threadIdx.x; r < n; r += blockDim.x) {
+            cplx s = vcol[r];
+            for (int i = 0; i < j; ++i) s -= V[(long long)i * n + r] * coef[i];
+            vcol[r] = s;
+            part += norm2(s);
+        }
+        part = warp_sum(part);
+        if (lane == 0) red[warp] = part;
+        __syncthreads();
+        double nrm2 = 0.;
+        for (int w = 0; w < nw; ++w) nrm2 += red[w];
+        const double inv = nrm2 > 0. ? 1. / sqrt(nrm2) : 0.;
+        for (int r = threadIdx.x; r < n; r += blockDim.x) V[(long long)j * n + r] = inv * vcol[r];
+        __syncthreads();
+    }
+}
+
+// Stage 3: A = T V in FP64 (A in shared memory, overwriting the FP32 stage's space)
+__device__ void product_fp64(const cplx* T0, const cplx* V, int n, cplx* A) {
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        const int r = e % n, c = e / n;
+        const cplx* vc = V + (long long)c * n;
+        cplx s = mk(0.);
+        for (int k = 0; k < n; ++k) s += T0[r + (long long)k * n] * vc[k];
+        A[e] = s;
+    }
+    __syncthreads();
+}
+
+template <bool MIXED>
 __global__ void __launch_bounds__(kSvdThreads) k_svd_jacobi(SvdJob J) {
     extern __shared__ double smraw[];
     const int n = J.n, mat = blockIdx.x;
@@ -62,12 +184,22 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_jacobi(SvdJob J) {
     __shared__ int s_imin;
     cplx* V = J.gV + (long long)mat * n * n;
     const cplx* T0 = J.T + (long long)mat * J.mat_stride;
-    for (long long e = threadIdx.x; e < (long long)n * n; e += blockDim.x) {
-        A[e] = T0[e];
-        int r = (int)(e % n), c = (int)(e / n);
-        V[e] = mk(r == c ? 1. : 0.);
+    if (MIXED) {
+        // FP32 Jacobi for the bulk of the rotations, then an FP64 start from T V with
+        // V orthonormalised in FP64; the FP64 sweeps below only polish (A must be in
+        // shared memory: the FP32 stage uses the same space)
+        cpf* A32 = reinterpret_cast<cpf*>(sbase);
+        jacobi_fp32(T0, n, A32, A32 + (long long)n * n, &s_rot);
+        orthonormalise_fp64(A32 + (long long)n * n, n, V, uy, uz, red);
+        product_fp64(T0, V, n, A);
+    } else {
+        for (long long e = threadIdx.x; e < (long long)n * n; e += blockDim.x) {
+            A[e] = T0[e];
+            int r = (int)(e % n), c = (int)(e / n);
+            V[e] = mk(r == c ? 1. : 0.);
+        }
+        __syncthreads();
     }
-    __syncthreads();
     int sweep = 0;
     const double tol = 1e-15;
     for (; sweep < kSvdMaxSweeps; ++sweep) {
@@ -224,15 +356,32 @@ size_t svd_smem_bytes(int n, bool a_in_smem) {
     return a_in_smem ? v + (size_t)n * n * sizeof(cplx) : v;
 }
 
+// FP64 one-sided Jacobi from the identity (every n; A in shared memory when it fits)
 cudaError_t launch_svd(int n, int nmat, int D, int which, const cplx* T, long long mat_stride, long long der_stride,
                        cplx* gA, cplx* gV, double* out, double* sig_all, int* status, cudaStream_t st) {
     const size_t limit = 220 * 1024;
     bool in_smem = svd_smem_bytes(n, true) <= limit;
     size_t smem = svd_smem_bytes(n, in_smem);
-    cudaError_t e = cudaFuncSetAttribute(k_svd_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit);
+    cudaError_t e = cudaFuncSetAttribute(k_svd_jacobi<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit);
     if (e != cudaSuccess) return e;
     SvdJob J{n, nmat, D, which, T, mat_stride, der_stride, gA, gV, out, sig_all, status, in_smem ? 1 : 0};
-    k_svd_jacobi<<<nmat, kSvdThreads, smem, st>>>(J);
+    k_svd_jacobi<false><<<nmat, kSvdThreads, smem, st>>>(J);
+    return cudaGetLastError();
+}
+
+// Mixed precision where A fits in shared memory: FP32 Jacobi, FP64 re-start from
+// T V, FP64 polishing sweeps (same results to FP64 accuracy, far fewer FP64
+// operations); the FP64-only kernel otherwise.
+cudaError_t launch_svd_mixed(int n, int nmat, int D, int which, const cplx* T, long long mat_stride,
+                             long long der_stride, cplx* gA, cplx* gV, double* out, double* sig_all, int* status,
+                             cudaStream_t st) {
+    const size_t limit = 220 * 1024;
+    if (svd_smem_bytes(n, true) > limit)
+        return launch_svd(n, nmat, D, which, T, mat_stride, der_stride, gA, gV, out, sig_all, status, st);
+    cudaError_t e = cudaFuncSetAttribute(k_svd_jacobi<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit);
+    if (e != cudaSuccess) return e;
+    SvdJob J{n, nmat, D, which, T, mat_stride, der_stride, gA, gV, out, sig_all, status, 1};
+    k_svd_jacobi<true><<<nmat, kSvdThreads, svd_smem_bytes(n, true), st>>>(J);
     return cudaGetLastError();
 }
 

@@ -16,7 +16,7 @@
 
 namespace hbem {
 
-constexpr int kSvdThreads = 256;
+constexpr int kSvdThreads = 512;
 constexpr int kSvdMaxSweeps = 40;
 
 __device__ __forceinline__ double warp_sum(double x) {
@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_jacobi(SvdJob J) {
         __syncthreads();
     }
     int sweep = 0;
-    const double tol = 1e-15;
+    const double tol = fmax(1e-15, sqrt((double)n) * kEps);   // rounding level of the Gram entries
     for (; sweep < kSvdMaxSweeps; ++sweep) {
         if (threadIdx.x == 0) s_rot = 0;
         __syncthreads();

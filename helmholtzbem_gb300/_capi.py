@@ -22,7 +22,8 @@ EXPORTS = [
     "hbem_assemble_dense", "hbem_get_layer", "hbem_get_layer_device",
     "hbem_solop_create", "hbem_solop_destroy", "hbem_mass_matrix", "hbem_gen_sol_op",
     "hbem_gen_sol_op_batch_device", "hbem_sv_dense_batch_device", "hbem_sv_dense_batch_noalloc",
-    "hbem_sv_dense_batch", "hbem_sweep_sigma",
+    "hbem_sv_dense_batch", "hbem_sweep_sigma", "hbem_rand_sketch", "hbem_rsvd_sv_batch",
+    "hbem_rsvd_sv_batch_device",
     "hbem_find_resonances_plain", "hbem_rtsafe", "hbem_zbrent", "hbem_brent_min",
 ]
 
@@ -84,6 +85,10 @@ def load(path=LIB_PATH):
         "hbem_sv_dense_batch_noalloc": (_i, [_i, _i, _u, _vp, ctypes.c_longlong, ctypes.c_longlong, _vp, _vp, _vp]),
         "hbem_sv_dense_batch": (_i, [_i, _i, _u, _dp, _dp, _dp]),
         "hbem_sweep_sigma": (_i, [_vp, _dp, _i, _d, _d, _u, _dp]),
+        "hbem_rand_sketch": (_i, [_i, _i, ctypes.c_ulonglong, _dp]),
+        "hbem_rsvd_sv_batch": (_i, [_i, _i, _u, _dp, _dp, _i, _i, _dp]),
+        "hbem_rsvd_sv_batch_device": (_i, [_i, _i, _u, _vp, ctypes.c_longlong, ctypes.c_longlong, _vp, _i, _i,
+                                           _dp]),
         "hbem_find_resonances_plain": (_i, [_vp, _d, _d, _i, _d, _d, _d, _dp, _i, _ip, _dp, _ip]),
         "hbem_rtsafe": (_d, [FN, FN_BOTH, _vp, _d, _d, _d, _ip, _up]),
         "hbem_zbrent": (_d, [FN, _vp, _d, _d, _d, _ip, _up]),

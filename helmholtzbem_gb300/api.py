@@ -192,3 +192,28 @@ def hankel01(z):
     check(C.lib().hbem_hankel01(int(src.size), src.ctypes.data_as(C._dp), 1 if cplx_arg else 0,
                                 h0.ctypes.data_as(C._dp), h1.ctypes.data_as(C._dp)))
     return h0.reshape(z.shape), h1.reshape(z.shape)
+
+
+def randGaussian(nr, nc, seed=0):
+    """randomized_svd::randGaussian: (U[0,1] + i U[0,1])/sqrt2, seeded."""
+    R = np.zeros((nc, nr), np.complex128)        # column-major nr x nc
+    check(C.lib().hbem_rand_sketch(int(nr), int(nc), int(seed), R.ctypes.data_as(C._dp)))
+    return R.T
+
+
+def rsvd_sv(Ts, R, q=0, d=0):
+    """randomized_svd::sv (d = 0) / sv_der (d = 1) for a batch: Ts is a list of [T] or
+    [T, T'].  Returns (nmat, 2): [sigma estimate, sigma']."""
+    nmat = len(Ts)
+    n = Ts[0][0].shape[0]
+    R = np.asarray(R, np.complex128)
+    s = R.shape[1]
+    buf = np.zeros((nmat, d + 1, n, n), np.complex128)
+    for m, mats in enumerate(Ts):
+        for t in range(d + 1):
+            buf[m, t] = np.asarray(mats[t]).T
+    Rc = np.ascontiguousarray(R.T)                 # column-major n x s
+    out = np.zeros((nmat, 2))
+    check(C.lib().hbem_rsvd_sv_batch(n, nmat, int(d), buf.ctypes.data_as(C._dp), Rc.ctypes.data_as(C._dp), int(s),
+                                     int(q), dptr(out)))
+    return out

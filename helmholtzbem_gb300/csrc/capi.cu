@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <cstring>
 #include <string>
+#include <random>
 #include <vector>
 
 #include "../../include/hbem.h"
@@ -26,6 +27,9 @@ cudaError_t launch_svd_mixed(int n, int nmat, int D, int which, const cplx* T, l
                              long long der_stride, cplx* gA, cplx* gV, double* out, double* sig_all, int* status,
                              cudaStream_t st);
 cudaError_t launch_hankel01(int n, const cplx* z, int complex_arg, cplx* h0, cplx* h1, cudaStream_t st);
+size_t rsvd_smem_bytes(int n, int s);
+cudaError_t launch_rsvd_small(int n, int nmat, int s, int q, int D, const cplx* T, long long mat_stride,
+                              long long der_stride, const cplx* R, double* out, int* status, cudaStream_t st);
 }  // namespace hbem
 
 using namespace hbem;
@@ -662,6 +666,54 @@ int hbem_sv_dense_batch(int n, int nmat, unsigned d, const double* T_host, doubl
     HB_CK(cudaMemcpy(T.p, T_host, bytes, cudaMemcpyHostToDevice));
     return sv_batch(0, n, nmat, d, T.as<cplx>(), (long long)((d + 1) * nn), (long long)nn, A, V, out, status, &sig,
                     out_host, sig_all_host);
+}
+
+int hbem_rand_sketch(int nr, int nc, unsigned long long seed, double* R_host) {
+    if (nr < 1 || nc < 1 || !R_host) return fail(HBEM_ERR_INVALID, "rand_sketch: bad argument");
+    std::mt19937_64 gen(seed);
+    std::uniform_real_distribution<double> u(0., 1.);
+    const double r = std::sqrt(0.5);
+    for (size_t e = 0; e < (size_t)nr * nc; ++e) {
+        R_host[2 * e] = u(gen) * r;
+        R_host[2 * e + 1] = u(gen) * r;
+    }
+    return HBEM_OK;
+}
+
+int hbem_rsvd_sv_batch_device(int n, int nmat, unsigned d, const void* T_dev, long long mat_stride,
+                              long long der_stride, const void* R_dev, int s, int q, double* out_host) {
+    if (n < 2 || nmat < 1 || d > 1 || !T_dev || !R_dev || !out_host || s < 1 || s > n || q < 0)
+        return fail(HBEM_ERR_INVALID, "rsvd_sv_batch: bad argument");
+    if (rsvd_smem_bytes(n, s) > 220 * 1024)
+        return fail(HBEM_ERR_UNSUPPORTED, "rsvd_sv_batch: this build runs the randomized SVD for matrices whose "
+                                          "LU and sketch fit in shared memory");
+    HB_CK(cudaSetDevice(g_device));
+    static thread_local DBuf out, status;
+    HB_CK(out.ensure((size_t)nmat * 2 * sizeof(double)));
+    HB_CK(status.ensure((size_t)nmat * sizeof(int)));
+    HB_CK(launch_rsvd_small(n, nmat, s, q, (int)d, static_cast<const cplx*>(T_dev), mat_stride, der_stride,
+                            static_cast<const cplx*>(R_dev), out.as<double>(), status.as<int>(), 0));
+    g_launches += 1;
+    std::vector<int> st(nmat);
+    HB_CK(cudaMemcpy(out_host, out.p, (size_t)nmat * 2 * sizeof(double), cudaMemcpyDeviceToHost));
+    HB_CK(cudaMemcpy(st.data(), status.p, (size_t)nmat * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int v : st)
+        if (v) return fail(HBEM_ERR_SINGULAR, "rsvd_sv_batch: zero pivot in the LU of T");
+    return HBEM_OK;
+}
+
+int hbem_rsvd_sv_batch(int n, int nmat, unsigned d, const double* T_host, const double* R_host, int s, int q,
+                       double* out_host) {
+    if (n < 2 || nmat < 1 || d > 1 || !T_host || !R_host || !out_host || s < 1 || s > n)
+        return fail(HBEM_ERR_INVALID, "rsvd_sv_batch: bad argument");
+    HB_CK(cudaSetDevice(g_device));
+    static thread_local DBuf T, R;
+    const size_t nn = (size_t)n * n, bytes = (size_t)nmat * (d + 1) * nn * sizeof(cplx);
+    HB_CK(T.ensure(bytes));
+    HB_CK(R.ensure((size_t)n * s * sizeof(cplx)));
+    HB_CK(cudaMemcpy(T.p, T_host, bytes, cudaMemcpyHostToDevice));
+    HB_CK(cudaMemcpy(R.p, R_host, (size_t)n * s * sizeof(cplx), cudaMemcpyHostToDevice));
+    return hbem_rsvd_sv_batch_device(n, nmat, d, T.p, (long long)((d + 1) * nn), (long long)nn, R.p, s, q, out_host);
 }
 
 int hbem_sweep_sigma(hbem_solop s, const double* k_host, int nk, double c_o, double c_i, unsigned d, double* out_host) {

@@ -142,6 +142,22 @@ int hbem_sv_dense_batch_noalloc(int n, int nmat, unsigned d, const void* T_dev, 
  * (d + 1) consecutive n x n matrices (T, T', T'') */
 int hbem_sv_dense_batch(int n, int nmat, unsigned d, const double* T_host, double* out_host, double* sig_all_host);
 
+/* randomized_svd::randGaussian(nr, nc) (include/randsvd.hpp:23-30): (U[0,1] + i U[0,1])/sqrt2
+ * entries, column-major nr x nc, from a seeded generator (the reference seeds from
+ * std::random_device, so its sketches are not reproducible).                     */
+int hbem_rand_sketch(int nr, int nc, unsigned long long seed, double* R_host);
+
+/* randomized_svd::sv (d = 0) and sv_der's sigma' (d = 1) (include/randsvd.hpp:53,64;
+ * source/utilities/randsvd.cpp:99-169) for a batch: LU of T, q subspace iterations
+ * with the n x s sketch R, sigma ~ 1/sigma_max(T^-H Q); sigma' from the Ritz vectors
+ * of the sketch.  Matrices of order n with rsvd fitting in shared memory
+ * (n <= 108 at s = 16); larger -> HBEM_ERR_UNSUPPORTED.  out_host[2m] = sigma,
+ * out_host[2m + 1] = sigma' (0 for d = 0).  T_host: nmat blocks of d + 1 matrices. */
+int hbem_rsvd_sv_batch(int n, int nmat, unsigned d, const double* T_host, const double* R_host, int s, int q,
+                       double* out_host);
+int hbem_rsvd_sv_batch_device(int n, int nmat, unsigned d, const void* T_dev, long long mat_stride,
+                              long long der_stride, const void* R_dev, int s, int q, double* out_host);
+
 /* sigma_min(k) and its derivatives along a list of real wavenumbers, end to end:
  * gen_sol_op_*der + direct::sv_*der per k (examples/roots_newton_circle.cpp:111-138).
  * out_host[3i + t]. */

@@ -82,3 +82,14 @@ def test_reference_root_test_functions():
         r, ok, _ = api.rtsafe(fn, lambda x, g=fn: (g(x), (-math.sin(x) if g is math.cos else math.cos(x))),
                               a, b, 1e-10)
         assert ok and abs(r - root) < 1e-5
+
+
+def test_rand_sketch_distribution():
+    """randGaussian stand-in: (U[0,1] + i U[0,1])/sqrt2 entries, reproducible by seed."""
+    api = _api()
+    R = api.randGaussian(400, 50, seed=11)
+    assert R.shape == (400, 50)
+    s = np.sqrt(0.5)
+    assert R.real.min() >= 0 and R.real.max() <= s and R.imag.min() >= 0 and R.imag.max() <= s
+    assert abs(R.real.mean() - 0.5 * s) < 0.02 and abs(R.imag.mean() - 0.5 * s) < 0.02
+    assert np.array_equal(R, api.randGaussian(400, 50, seed=11))

@@ -202,8 +202,9 @@ def randGaussian(nr, nc, seed=0):
 
 
 def rsvd_sv(Ts, R, q=0, d=0):
-    """randomized_svd::sv (d = 0) / sv_der (d = 1) for a batch: Ts is a list of [T] or
-    [T, T'].  Returns (nmat, 2): [sigma estimate, sigma']."""
+    """randomized_svd::sv (d = 0) / sv_der (d = 1) / sv_der2 (d = 2) for a batch: Ts
+    is a list of [T], [T, T'] or [T, T', T''].  Returns (nmat, d + 1): sigma estimate,
+    sigma', sigma''."""
     nmat = len(Ts)
     n = Ts[0][0].shape[0]
     R = np.asarray(R, np.complex128)
@@ -213,7 +214,7 @@ def rsvd_sv(Ts, R, q=0, d=0):
         for t in range(d + 1):
             buf[m, t] = np.asarray(mats[t]).T
     Rc = np.ascontiguousarray(R.T)                 # column-major n x s
-    out = np.zeros((nmat, 2))
+    out = np.zeros((nmat, d + 1))
     check(C.lib().hbem_rsvd_sv_batch(n, nmat, int(d), buf.ctypes.data_as(C._dp), Rc.ctypes.data_as(C._dp), int(s),
                                      int(q), dptr(out)))
     return out

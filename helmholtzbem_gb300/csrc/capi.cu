@@ -27,9 +27,17 @@ cudaError_t launch_svd_mixed(int n, int nmat, int D, int which, const cplx* T, l
                              long long der_stride, cplx* gA, cplx* gV, double* out, double* sig_all, int* status,
                              cudaStream_t st);
 cudaError_t launch_hankel01(int n, const cplx* z, int complex_arg, cplx* h0, cplx* h1, cudaStream_t st);
-size_t rsvd_smem_bytes(int n, int s);
-cudaError_t launch_rsvd_small(int n, int nmat, int s, int q, int D, const cplx* T, long long mat_stride,
-                              long long der_stride, const cplx* R, double* out, int* status, cudaStream_t st);
+bool rsvd_supported(int n, int s, int D);
+size_t rsvd_work_bytes(int n, int nmat, int s, int D);
+cudaError_t rsvd_batched(int n, int nmat, int s, int q, int D, const cplx* T, long long mat_stride,
+                         long long der_stride, const cplx* R, double* out, int* status, void* work,
+                         size_t work_bytes, cudaStream_t st, long long* launches);
+cudaError_t lu_factor_batched(int n, int nmat, cplx* A, long long stride, int* piv, int* perm, int* info,
+                              cudaStream_t st, long long* launches);
+cudaError_t lu_solve_batched(int n, int nmat, int trans, const cplx* LU, long long stride, const int* perm, int s,
+                             cplx* X, long long xstride, cudaStream_t st);
+cudaError_t lu_perm_from_piv(int n, int nmat, const int* piv, int* perm, cudaStream_t st);
+bool lu_solve_supported(int n);
 }  // namespace hbem
 
 using namespace hbem;
@@ -682,20 +690,24 @@ int hbem_rand_sketch(int nr, int nc, unsigned long long seed, double* R_host) {
 
 int hbem_rsvd_sv_batch_device(int n, int nmat, unsigned d, const void* T_dev, long long mat_stride,
                               long long der_stride, const void* R_dev, int s, int q, double* out_host) {
-    if (n < 2 || nmat < 1 || d > 1 || !T_dev || !R_dev || !out_host || s < 1 || s > n || q < 0)
+    if (n < 2 || nmat < 1 || nmat > 65535 || d > 2 || !T_dev || !R_dev || !out_host || s < 1 || s > n || q < 0)
         return fail(HBEM_ERR_INVALID, "rsvd_sv_batch: bad argument");
-    if (rsvd_smem_bytes(n, s) > 220 * 1024)
-        return fail(HBEM_ERR_UNSUPPORTED, "rsvd_sv_batch: this build runs the randomized SVD for matrices whose "
-                                          "LU and sketch fit in shared memory");
+    if (!rsvd_supported(n, s, (int)d))
+        return fail(HBEM_ERR_UNSUPPORTED, "rsvd_sv_batch: sketch wider than 32 columns, or a matrix too large for "
+                                          "the shared-memory permutation buffer of the triangular solves");
     HB_CK(cudaSetDevice(g_device));
-    static thread_local DBuf out, status;
-    HB_CK(out.ensure((size_t)nmat * 2 * sizeof(double)));
+    static thread_local DBuf out, status, work;
+    const size_t os = d + 1;
+    HB_CK(out.ensure((size_t)nmat * os * sizeof(double)));
     HB_CK(status.ensure((size_t)nmat * sizeof(int)));
-    HB_CK(launch_rsvd_small(n, nmat, s, q, (int)d, static_cast<const cplx*>(T_dev), mat_stride, der_stride,
-                            static_cast<const cplx*>(R_dev), out.as<double>(), status.as<int>(), 0));
-    g_launches += 1;
+    const size_t wb = rsvd_work_bytes(n, nmat, s, (int)d);
+    HB_CK(work.ensure(std::max<size_t>(wb, 256)));
+    long long nl = 0;
+    HB_CK(rsvd_batched(n, nmat, s, q, (int)d, static_cast<const cplx*>(T_dev), mat_stride, der_stride,
+                       static_cast<const cplx*>(R_dev), out.as<double>(), status.as<int>(), work.p, work.cap, 0, &nl));
+    g_launches += nl;
     std::vector<int> st(nmat);
-    HB_CK(cudaMemcpy(out_host, out.p, (size_t)nmat * 2 * sizeof(double), cudaMemcpyDeviceToHost));
+    HB_CK(cudaMemcpy(out_host, out.p, (size_t)nmat * os * sizeof(double), cudaMemcpyDeviceToHost));
     HB_CK(cudaMemcpy(st.data(), status.p, (size_t)nmat * sizeof(int), cudaMemcpyDeviceToHost));
     for (int v : st)
         if (v) return fail(HBEM_ERR_SINGULAR, "rsvd_sv_batch: zero pivot in the LU of T");
@@ -704,7 +716,7 @@ int hbem_rsvd_sv_batch_device(int n, int nmat, unsigned d, const void* T_dev, lo
 
 int hbem_rsvd_sv_batch(int n, int nmat, unsigned d, const double* T_host, const double* R_host, int s, int q,
                        double* out_host) {
-    if (n < 2 || nmat < 1 || d > 1 || !T_host || !R_host || !out_host || s < 1 || s > n)
+    if (n < 2 || nmat < 1 || d > 2 || !T_host || !R_host || !out_host || s < 1 || s > n)
         return fail(HBEM_ERR_INVALID, "rsvd_sv_batch: bad argument");
     HB_CK(cudaSetDevice(g_device));
     static thread_local DBuf T, R;
@@ -714,6 +726,46 @@ int hbem_rsvd_sv_batch(int n, int nmat, unsigned d, const double* T_host, const 
     HB_CK(cudaMemcpy(T.p, T_host, bytes, cudaMemcpyHostToDevice));
     HB_CK(cudaMemcpy(R.p, R_host, (size_t)n * s * sizeof(cplx), cudaMemcpyHostToDevice));
     return hbem_rsvd_sv_batch_device(n, nmat, d, T.p, (long long)((d + 1) * nn), (long long)nn, R.p, s, q, out_host);
+}
+
+int hbem_lu_factor_batch_device(int n, int nmat, void* A_dev, long long stride, int* piv_dev, int* info_host) {
+    if (n < 1 || nmat < 1 || nmat > 65535 || !A_dev || !piv_dev || stride < (long long)n * n)
+        return fail(HBEM_ERR_INVALID, "lu_factor_batch: bad argument");
+    if ((size_t)n * sizeof(int) > 220 * 1024) return fail(HBEM_ERR_UNSUPPORTED, "lu_factor_batch: n too large");
+    HB_CK(cudaSetDevice(g_device));
+    static thread_local DBuf perm, info;
+    HB_CK(perm.ensure((size_t)nmat * n * sizeof(int)));
+    HB_CK(info.ensure((size_t)nmat * sizeof(int)));
+    long long nl = 0;
+    HB_CK(lu_factor_batched(n, nmat, static_cast<cplx*>(A_dev), stride, piv_dev, perm.as<int>(), info.as<int>(), 0,
+                            &nl));
+    g_launches += nl;
+    std::vector<int> inf(nmat);
+    HB_CK(cudaMemcpy(inf.data(), info.p, (size_t)nmat * sizeof(int), cudaMemcpyDeviceToHost));
+    int first = 0;
+    for (int m = 0; m < nmat; ++m) {
+        if (info_host) info_host[m] = inf[m];
+        if (inf[m] && !first) first = m + 1;
+    }
+    if (first) return fail(HBEM_ERR_SINGULAR, "lu_factor_batch: zero pivot (matrix " + std::to_string(first - 1) + ")");
+    return HBEM_OK;
+}
+
+int hbem_lu_solve_batch_device(int n, int nmat, int trans, const void* LU_dev, long long stride, const int* piv_dev,
+                               int nrhs, void* X_dev, long long xstride) {
+    if (n < 1 || nmat < 1 || nmat > 65535 || (trans != 0 && trans != 1) || !LU_dev || !piv_dev || nrhs < 1 ||
+        !X_dev || stride < (long long)n * n || xstride < (long long)n * nrhs)
+        return fail(HBEM_ERR_INVALID, "lu_solve_batch: bad argument");
+    if (!lu_solve_supported(n)) return fail(HBEM_ERR_UNSUPPORTED, "lu_solve_batch: n too large");
+    HB_CK(cudaSetDevice(g_device));
+    static thread_local DBuf perm;
+    HB_CK(perm.ensure((size_t)nmat * n * sizeof(int)));
+    HB_CK(lu_perm_from_piv(n, nmat, piv_dev, perm.as<int>(), 0));
+    HB_CK(lu_solve_batched(n, nmat, trans, static_cast<const cplx*>(LU_dev), stride, perm.as<int>(), nrhs,
+                           static_cast<cplx*>(X_dev), xstride, 0));
+    g_launches += 2;
+    HB_CK(cudaStreamSynchronize(0));
+    return HBEM_OK;
 }
 
 int hbem_sweep_sigma(hbem_solop s, const double* k_host, int nk, double c_o, double c_i, unsigned d, double* out_host) {

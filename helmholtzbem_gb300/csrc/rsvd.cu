@@ -9,12 +9,15 @@
 // triplet: u = B w / |B w|, v = Q w, and sigma' = Re u^H T' v.  (The reference
 // recomputes the null vector of the 2n x 2n Wielandt matrix by a column-pivoted
 // QR; the Ritz vectors are that null vector to the accuracy of the sketch.)
+#include <algorithm>
+
 #include "hbem_device.cuh"
 
 namespace hbem {
 
 constexpr int kRsvdThreads = 256;
 constexpr int kRsvdMaxS = 32;
+constexpr int kRitzRefine = 2;     // inverse-iteration steps on the right Ritz vector
 
 __device__ __forceinline__ double bsum(double x, double* red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -141,11 +144,14 @@ __device__ void solve_lu_h(const cplx* A, const int* piv, int n, cplx* X, int s)
 }
 
 // Orthonormalise the s columns of X (n x s) in place: classical Gram-Schmidt,
-// twice per column ("twice is enough").  coef: s entries of scratch.
-__device__ void qr_cgs2(cplx* X, int n, int s, cplx* coef, double* red) {
+// twice per column ("twice is enough").  coef: s entries of scratch.  If Rf is
+// given it receives the s x s upper-triangular factor (column-major), X = Q Rf.
+__device__ void qr_cgs2(cplx* X, int n, int s, cplx* coef, double* red, cplx* Rf = nullptr) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int j = 0; j < s; ++j) {
-        cplx* xj = X + j * n;
+        cplx* xj = X + (long long)j * n;
+        if (Rf)
+            for (int i = threadIdx.x; i < s; i += blockDim.x) Rf[i + j * s] = mk(0.);
         for (int pass = 0; pass < 2; ++pass) {
             for (int i = warp; i < j; i += nw) {
                 const cplx* qi = X + i * n;
@@ -163,9 +169,11 @@ __device__ void qr_cgs2(cplx* X, int n, int s, cplx* coef, double* red) {
                 if (lane == 0) coef[i] = mk(cr, ci);
             }
             __syncthreads();
+            if (Rf)
+                for (int i = threadIdx.x; i < j; i += blockDim.x) Rf[i + j * s] += coef[i];
             for (int r = threadIdx.x; r < n; r += blockDim.x) {
                 cplx v = xj[r];
-                for (int i = 0; i < j; ++i) v -= X[i * n + r] * coef[i];
+                for (int i = 0; i < j; ++i) v -= X[(long long)i * n + r] * coef[i];
                 xj[r] = v;
             }
             __syncthreads();
@@ -173,6 +181,7 @@ __device__ void qr_cgs2(cplx* X, int n, int s, cplx* coef, double* red) {
         double part = 0.;
         for (int r = threadIdx.x; r < n; r += blockDim.x) part += norm2(xj[r]);
         const double nrm = sqrt(bsum(part, red));
+        if (Rf && threadIdx.x == 0) Rf[j + j * s] = mk(nrm);
         const double inv = nrm > 0. ? 1. / nrm : 0.;
         for (int r = threadIdx.x; r < n; r += blockDim.x) xj[r] = inv * xj[r];
         __syncthreads();
@@ -226,18 +235,20 @@ __device__ void jacobi_thin(cplx* B, int n, int s, cplx* W, double* red) {
     }
 }
 
+
 struct RsvdJob {
     int n, nmat, s, q, D;
     const cplx* T;            // matrix m at T + m*mat_stride, T' at + der_stride
     long long mat_stride, der_stride;
     const cplx* R;            // n x s sketch (shared by all matrices)
-    double* out;              // [nmat][2]: sigma estimate, sigma'
+    double* out;              // [nmat][D + 1]: sigma estimate, sigma' (D >= 1), sigma'' slot (D = 2)
     int* status;              // [nmat]: 0 ok, 5 singular pivot
+    cplx* uv;                 // optional [nmat][2n]: Ritz vectors u, v of sigma
 };
 
 __global__ void __launch_bounds__(kRsvdThreads) k_rsvd_small(RsvdJob J) {
     extern __shared__ double smraw[];
-    const int n = J.n, s = J.s, mat = blockIdx.x;
+    const int n = J.n, s = J.s, mat = blockIdx.x, os = J.D + 1;
     cplx* A = reinterpret_cast<cplx*>(smraw);       // n x n
     cplx* X = A + (long long)n * n;                 // n x s (Q)
     cplx* Y = X + (long long)n * s;                 // n x s (work)
@@ -246,6 +257,7 @@ __global__ void __launch_bounds__(kRsvdThreads) k_rsvd_small(RsvdJob J) {
     double* red = reinterpret_cast<double*>(coef + s);   // 128
     int* piv = reinterpret_cast<int*>(red + 128);   // n
     int* redi = piv + n;                            // 32
+    cplx* vb = reinterpret_cast<cplx*>(piv + (n + 32 + 3) / 4 * 4);   // n, 16-byte aligned
     __shared__ int s_sing;
     if (threadIdx.x == 0) s_sing = 0;
     const cplx* T0 = J.T + (long long)mat * J.mat_stride;
@@ -278,50 +290,395 @@ __global__ void __launch_bounds__(kRsvdThreads) k_rsvd_small(RsvdJob J) {
     }
     const double smax = sqrt(best);
     if (threadIdx.x == 0) {
-        J.out[2LL * mat] = smax > 0. ? 1. / smax : 0.;
-        J.out[2LL * mat + 1] = 0.;
+        J.out[(long long)os * mat] = smax > 0. ? 1. / smax : 0.;
+        for (int t = 1; t < os; ++t) J.out[(long long)os * mat + t] = 0.;
         J.status[mat] = s_sing ? 5 : 0;
     }
     if (J.D == 0) return;
-    // Ritz vectors: u = B w / |B w| (column bj of Y), v = Q w (w = column bj of W)
+    // right Ritz vector v = Q w (w = column bj of W), then two steps of inverse
+    // iteration v <- T^-1 T^-H v with the LU in shared memory; u, sigma' follow in
+    // k_rsvd_vec
     __syncthreads();
-    const double isn = smax > 0. ? 1. / smax : 0.;
-    // sigma' = Re u^H T' v accumulated row by row
-    double part_re = 0.;
-    const cplx* T1 = T0 + J.der_stride;
     const cplx* w = W + bj * s;
-    // v_r = sum_c X[r, c] w_c ; stash v in A (the LU factors are no longer needed)
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
         cplx v = mk(0.);
         for (int c = 0; c < s; ++c) v += X[c * n + r] * w[c];
-        A[r] = v;
+        vb[r] = v;
     }
     __syncthreads();
-    for (int r = threadIdx.x; r < n; r += blockDim.x) {
-        cplx tv = mk(0.);
-        for (int c = 0; c < n; ++c) tv += T1[r + (long long)c * n] * A[c];
-        cplx ur = isn * Y[bj * n + r];
-        part_re += ur.re * tv.re + ur.im * tv.im;   // Re(conj(u_r) tv_r)
+    for (int it = 0; it < kRitzRefine; ++it) {
+        solve_lu_h(A, piv, n, vb, 1);
+        solve_lu(A, piv, n, vb, 1);
     }
-    const double d1 = bsum(part_re, red);
-    if (threadIdx.x == 0) J.out[2LL * mat + 1] = d1;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) J.uv[2LL * n * mat + n + r] = vb[r];
 }
 
 size_t rsvd_smem_bytes(int n, int s) {
     return ((size_t)n * n + 2 * (size_t)n * s + (size_t)s * s + s) * sizeof(cplx) + 128 * sizeof(double) +
-           ((size_t)n + 32) * sizeof(int);
+           (((size_t)n + 32 + 3) / 4 * 4) * sizeof(int) + (size_t)n * sizeof(cplx);
 }
 
 cudaError_t launch_rsvd_small(int n, int nmat, int s, int q, int D, const cplx* T, long long mat_stride,
-                              long long der_stride, const cplx* R, double* out, int* status, cudaStream_t st) {
+                              long long der_stride, const cplx* R, double* out, int* status, cplx* uv,
+                              cudaStream_t st) {
     const size_t limit = 220 * 1024;
     size_t smem = rsvd_smem_bytes(n, s);
     if (smem > limit || s > kRsvdMaxS || s < 1 || s > n) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(k_rsvd_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit);
     if (e != cudaSuccess) return e;
-    RsvdJob J{n, nmat, s, q, D, T, mat_stride, der_stride, R, out, status};
+    RsvdJob J{n, nmat, s, q, D, T, mat_stride, der_stride, R, out, status, uv};
     k_rsvd_small<<<nmat, kRsvdThreads, smem, st>>>(J);
     return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ matrices of any order
+//
+// The same algorithm with the LU, the n x s blocks and the Wielandt system in
+// global memory (lu.cu): T^-1 / T^-H applications by the batched solves, the QR
+// steps by one CTA per matrix, sigma from the s x s triangular factor of T^-H Q.
+
+cudaError_t lu_factor_batched(int n, int nmat, cplx* A, long long stride, int* piv, int* perm, int* info,
+                              cudaStream_t st, long long* launches);
+cudaError_t lu_solve_batched(int n, int nmat, int trans, const cplx* LU, long long stride, const int* perm, int s,
+                             cplx* X, long long xstride, cudaStream_t st);
+bool lu_solve_supported(int n);
+
+__global__ void k_copy_mats(int nn, const cplx* src, long long sstride, cplx* dst, long long dstride) {
+    const cplx* a = src + (long long)blockIdx.y * sstride;
+    cplx* b = dst + (long long)blockIdx.y * dstride;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn; e += (long long)gridDim.x * blockDim.x)
+        b[e] = a[e];
+}
+
+__global__ void __launch_bounds__(kRsvdThreads) k_qr_global(int n, int s, cplx* X, long long xstride, cplx* Rf) {
+    __shared__ cplx coef[kRsvdMaxS];
+    __shared__ double red[128];
+    qr_cgs2(X + (long long)blockIdx.x * xstride, n, s, coef, red, Rf ? Rf + (long long)blockIdx.x * s * s : nullptr);
+}
+
+// sigma from the triangular factor Rf of B = T^-H Q = Q_B Rf: sigma_max(B) =
+// sigma_max(Rf).  D >= 1: the right Ritz vector v = Q w (w the top right singular
+// vector of Rf) into the v half of uv.
+__global__ void __launch_bounds__(kRsvdThreads) k_rsvd_tail(int n, int s, int D, const cplx* Q, const cplx* QB,
+                                                             long long xstride, const cplx* Rf, const cplx* T,
+                                                             long long mat_stride, long long der_stride,
+                                                             const int* info, double* out, int* status, cplx* uv) {
+    __shared__ cplx Rs[kRsvdMaxS * kRsvdMaxS], W[kRsvdMaxS * kRsvdMaxS], tw[kRsvdMaxS];
+    __shared__ double red[128];
+    const int mat = blockIdx.x, os = D + 1;
+    for (int e = threadIdx.x; e < s * s; e += blockDim.x) Rs[e] = Rf[(long long)mat * s * s + e];
+    __syncthreads();
+    jacobi_thin(Rs, s, s, W, red);
+    __syncthreads();
+    double best = -1.;
+    int bj = 0;
+    for (int j = 0; j < s; ++j) {
+        double nb = 0.;
+        for (int r = 0; r < s; ++r) nb += norm2(Rs[j * s + r]);
+        if (nb > best) { best = nb; bj = j; }
+    }
+    const double smax = sqrt(best), isn = smax > 0. ? 1. / smax : 0.;
+    if (threadIdx.x == 0) {
+        out[(long long)os * mat] = isn;
+        for (int t = 1; t < os; ++t) out[(long long)os * mat + t] = 0.;
+        status[mat] = info[mat] ? 5 : 0;
+    }
+    if (D == 0) return;
+    if (threadIdx.x < s) tw[threadIdx.x] = W[bj * s + threadIdx.x];   // w
+    __syncthreads();
+    const cplx* Qm = Q + (long long)mat * xstride;
+    cplx* v = uv + 2LL * n * mat + n;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        cplx b = mk(0.);
+        for (int c = 0; c < s; ++c) b += Qm[r + (long long)c * n] * tw[c];
+        v[r] = b;
+    }
+}
+
+// After the inverse-iteration steps: v <- v / |v|, u = T v / |T v|, and
+// sigma' = Re u^H T' v (the Wielandt form x^H W' x with x = (u; v)/sqrt2).
+__global__ void __launch_bounds__(kRsvdThreads) k_rsvd_vec(int n, int D, const cplx* T, long long mat_stride,
+                                                            long long der_stride, double* out, cplx* uv) {
+    __shared__ double red[128];
+    const int mat = blockIdx.x, os = D + 1;
+    cplx* u = uv + 2LL * n * mat;
+    cplx* v = u + n;
+    double part = 0.;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) part += norm2(v[r]);
+    const double nv = sqrt(bsum(part, red));
+    const double iv = nv > 0. ? 1. / nv : 0.;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) v[r] = iv * v[r];
+    __syncthreads();
+    const cplx* Tm = T + (long long)mat * mat_stride;
+    part = 0.;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        cplx a = mk(0.);
+        for (int c = 0; c < n; ++c) a += Tm[r + (long long)c * n] * v[c];
+        u[r] = a;
+        part += norm2(a);
+    }
+    const double nu = sqrt(bsum(part, red + 32));
+    const double iu = nu > 0. ? 1. / nu : 0.;
+    const cplx* T1 = Tm + der_stride;
+    part = 0.;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        cplx tv = mk(0.);
+        for (int c = 0; c < n; ++c) tv += T1[r + (long long)c * n] * v[c];
+        const cplx ur = iu * u[r];
+        u[r] = ur;
+        part += ur.re * tv.re + ur.im * tv.im;
+    }
+    const double d1 = bsum(part, red + 64);
+    if (threadIdx.x == 0) out[(long long)os * mat + 1] = d1;
+}
+
+// ------------------------------------------------------------------ sigma'' (sv_der2)
+//
+// randsvd.cpp:171-216: with x the unit null vector of W - sigma I, W = [0 T; T^H 0],
+// m = argmax |x_l|, u = x / x_m and B = W - sigma I with column m replaced by -u,
+//   u' = -B^-1 (W' u), t = u'_m (= sigma'), u'_m = 0,
+//   sigma'' = -[B^-1 (W'' u + 2 (W' u' - t u'))]_m.
+// Here x = (u_R; v_R)/sqrt2 from the Ritz vectors of the sketch.
+
+__global__ void __launch_bounds__(256) k_sv2_prep(int n, const cplx* uv, cplx* ub, int* mcol) {
+    const int mat = blockIdx.x, n2 = 2 * n;
+    const cplx* x = uv + (long long)n2 * mat;
+    __shared__ double rv[8];
+    __shared__ int ri[8];
+    __shared__ int s_m;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double best = -1.;
+    int bi = 0;
+    for (int l = threadIdx.x; l < n2; l += blockDim.x) {
+        const double a = norm2(x[l]);
+        if (a > best) { best = a; bi = l; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    if (lane == 0) { rv[warp] = best; ri[warp] = bi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = rv[0];
+        int p = ri[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+            if (rv[w] > b || (rv[w] == b && ri[w] < p)) { b = rv[w]; p = ri[w]; }
+        s_m = p;
+        mcol[mat] = p;
+    }
+    __syncthreads();
+    const cplx xm = x[s_m];
+    const cplx ixm = norm2(xm) > 0. ? cdiv(mk(1.), xm) : mk(0.);
+    for (int l = threadIdx.x; l < n2; l += blockDim.x) ub[(long long)n2 * mat + l] = x[l] * ixm;
+}
+
+__global__ void k_build_bordered(int n, const cplx* T, long long mat_stride, const double* out, int os,
+                                 const cplx* ub, const int* mcol, cplx* B) {
+    const int mat = blockIdx.y, n2 = 2 * n, m = mcol[mat];
+    const double sig = out[(long long)os * mat];
+    const cplx* Tm = T + (long long)mat * mat_stride;
+    const cplx* u = ub + (long long)n2 * mat;
+    cplx* Bm = B + (long long)n2 * n2 * mat;
+    const long long tot = (long long)n2 * n2;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e % n2), j = (int)(e / n2);
+        cplx v = mk(0.);
+        if (j == m) v = -u[i];
+        else {
+            if (i == j) v = mk(-sig);
+            else if (i < n && j >= n) v = Tm[i + (long long)(j - n) * n];
+            else if (i >= n && j < n) v = conj(Tm[j + (long long)(i - n) * n]);
+        }
+        Bm[e] = v;
+    }
+}
+
+// y = alpha [A x2; A^H x1] (+ y if acc), A = matrix mat of the batch, x = [x1; x2]
+__global__ void __launch_bounds__(256) k_wapply(int n, const cplx* A, long long mat_stride, const cplx* x, cplx* y,
+                                                double alpha, int acc) {
+    const int mat = blockIdx.x, n2 = 2 * n;
+    const cplx* Am = A + (long long)mat * mat_stride;
+    const cplx* x1 = x + (long long)n2 * mat;
+    const cplx* x2 = x1 + n;
+    cplx* y1 = y + (long long)n2 * mat;
+    cplx* y2 = y1 + n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        cplx sacc = mk(0.);
+        for (int j = 0; j < n; ++j) sacc += Am[i + (long long)j * n] * x2[j];
+        y1[i] = acc ? y1[i] + alpha * sacc : alpha * sacc;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int j = warp; j < n; j += nw) {
+        double sr = 0., si = 0.;
+        const cplx* col = Am + (long long)j * n;
+        for (int i = lane; i < n; i += 32) {
+            const cplx a = conj(col[i]), b = x1[i];
+            sr = fma(a.re, b.re, fma(-a.im, b.im, sr));
+            si = fma(a.re, b.im, fma(a.im, b.re, si));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sr += __shfl_xor_sync(0xffffffffu, sr, o);
+            si += __shfl_xor_sync(0xffffffffu, si, o);
+        }
+        if (lane == 0) y2[j] = acc ? y2[j] + alpha * mk(sr, si) : alpha * mk(sr, si);
+    }
+}
+
+__global__ void k_sv2_extract(int n, int nmat, cplx* ud, const int* mcol, cplx* tb) {
+    const int mat = blockIdx.x * blockDim.x + threadIdx.x;
+    if (mat >= nmat) return;
+    cplx* u = ud + 2LL * n * mat;
+    tb[mat] = u[mcol[mat]];
+    u[mcol[mat]] = mk(0.);
+}
+
+__global__ void k_sv2_axpy(int n, cplx* rhs, const cplx* ud, const cplx* tb) {
+    const int mat = blockIdx.x, n2 = 2 * n;
+    const cplx t2 = 2. * tb[mat];
+    for (int l = threadIdx.x; l < n2; l += blockDim.x) rhs[(long long)n2 * mat + l] -= t2 * ud[(long long)n2 * mat + l];
+}
+
+__global__ void k_sv2_out(int n, int nmat, const cplx* sol, const int* mcol, const int* info, double* out) {
+    const int mat = blockIdx.x * blockDim.x + threadIdx.x;
+    if (mat >= nmat) return;
+    out[3LL * mat + 2] = info[mat] ? CUDART_NAN : -sol[2LL * n * mat + mcol[mat]].re;
+}
+
+// ------------------------------------------------------------------ orchestration
+
+struct RsvdWork {
+    cplx *A = nullptr, *X = nullptr, *Y = nullptr, *Rf = nullptr, *uv = nullptr;
+    int *piv = nullptr, *perm = nullptr, *info = nullptr;
+    cplx *B = nullptr, *ub = nullptr, *ud = nullptr, *rhs = nullptr, *tb = nullptr;
+    int *piv2 = nullptr, *perm2 = nullptr, *info2 = nullptr, *mcol = nullptr;
+};
+
+// Carve the workspace (base == nullptr: only count).  Returns the bytes needed.
+size_t rsvd_carve(int n, int nmat, int s, int D, bool small, char* base, RsvdWork& w) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) -> char* {
+        char* p = base ? base + off : nullptr;
+        off += (bytes + 255) / 256 * 256;
+        return p;
+    };
+    const size_t nm = (size_t)nmat, nn = (size_t)n * n, c = sizeof(cplx), ii = sizeof(int);
+    if (!small) {
+        w.A = (cplx*)take(nm * nn * c);
+        w.piv = (int*)take(nm * n * ii);
+        w.perm = (int*)take(nm * n * ii);
+        w.info = (int*)take(nm * ii);
+        w.X = (cplx*)take(nm * n * s * c);
+        w.Y = (cplx*)take(nm * n * s * c);
+        w.Rf = (cplx*)take(nm * s * s * c);
+    }
+    if (D >= 1) w.uv = (cplx*)take(nm * 2 * n * c);
+    if (D == 2) {
+        w.B = (cplx*)take(nm * 4 * nn * c);
+        w.piv2 = (int*)take(nm * 2 * n * ii);
+        w.perm2 = (int*)take(nm * 2 * n * ii);
+        w.info2 = (int*)take(nm * ii);
+        w.ub = (cplx*)take(nm * 2 * n * c);
+        w.ud = (cplx*)take(nm * 2 * n * c);
+        w.rhs = (cplx*)take(nm * 2 * n * c);
+        w.tb = (cplx*)take(nm * c);
+        w.mcol = (int*)take(nm * ii);
+    }
+    return off;
+}
+
+bool rsvd_small_fits(int n, int s) { return rsvd_smem_bytes(n, s) <= 220 * 1024 && s <= kRsvdMaxS; }
+
+bool rsvd_supported(int n, int s, int D) {
+    if (s < 1 || s > kRsvdMaxS || s > n) return false;
+    if (!rsvd_small_fits(n, s) && !lu_solve_supported(n)) return false;
+    if (D == 2 && !lu_solve_supported(2 * n)) return false;
+    return true;
+}
+
+size_t rsvd_work_bytes(int n, int nmat, int s, int D) {
+    RsvdWork w;
+    return rsvd_carve(n, nmat, s, D, rsvd_small_fits(n, s), nullptr, w);
+}
+
+#define RS_CK(x)                                \
+    do {                                        \
+        cudaError_t e_ = (x);                   \
+        if (e_ != cudaSuccess) return e_;       \
+    } while (0)
+
+// sigma (D = 0), sigma' (D >= 1), sigma'' (D = 2) of nmat matrices of order n;
+// out[(D+1) m + t], status[m] (0 ok, 5 zero pivot in the LU of T).
+cudaError_t rsvd_batched(int n, int nmat, int s, int q, int D, const cplx* T, long long mat_stride,
+                         long long der_stride, const cplx* R, double* out, int* status, void* work,
+                         size_t work_bytes, cudaStream_t st, long long* launches) {
+    if (!rsvd_supported(n, s, D) || D < 0 || D > 2 || nmat < 1 || nmat > 65535) return cudaErrorInvalidValue;
+    const bool small = rsvd_small_fits(n, s);
+    RsvdWork w;
+    if (rsvd_carve(n, nmat, s, D, small, nullptr, w) > work_bytes) return cudaErrorInvalidValue;
+    rsvd_carve(n, nmat, s, D, small, static_cast<char*>(work), w);
+    long long nl = 0;
+    if (small) {
+        RS_CK(launch_rsvd_small(n, nmat, s, q, D, T, mat_stride, der_stride, R, out, status, w.uv, st));
+        ++nl;
+    } else {
+        const long long nn = (long long)n * n, ns = (long long)n * s;
+        const int cb = (int)std::min<long long>(1024, (nn + 255) / 256);
+        k_copy_mats<<<dim3(cb, nmat), 256, 0, st>>>((int)nn, T, mat_stride, w.A, nn);
+        RS_CK(lu_factor_batched(n, nmat, w.A, nn, w.piv, w.perm, w.info, st, &nl));
+        k_copy_mats<<<dim3((int)std::min<long long>(1024, (ns + 255) / 256), nmat), 256, 0, st>>>((int)ns, R, 0, w.X, ns);
+        RS_CK(lu_solve_batched(n, nmat, 0, w.A, nn, w.perm, s, w.X, ns, st));
+        k_qr_global<<<nmat, kRsvdThreads, 0, st>>>(n, s, w.X, ns, nullptr);
+        nl += 4;
+        for (int it = 0; it < q; ++it) {
+            RS_CK(lu_solve_batched(n, nmat, 1, w.A, nn, w.perm, s, w.X, ns, st));
+            k_qr_global<<<nmat, kRsvdThreads, 0, st>>>(n, s, w.X, ns, nullptr);
+            RS_CK(lu_solve_batched(n, nmat, 0, w.A, nn, w.perm, s, w.X, ns, st));
+            k_qr_global<<<nmat, kRsvdThreads, 0, st>>>(n, s, w.X, ns, nullptr);
+            nl += 4;
+        }
+        RS_CK(cudaMemcpyAsync(w.Y, w.X, (size_t)nmat * ns * sizeof(cplx), cudaMemcpyDeviceToDevice, st));
+        RS_CK(lu_solve_batched(n, nmat, 1, w.A, nn, w.perm, s, w.Y, ns, st));
+        k_qr_global<<<nmat, kRsvdThreads, 0, st>>>(n, s, w.Y, ns, w.Rf);
+        k_rsvd_tail<<<nmat, kRsvdThreads, 0, st>>>(n, s, D, w.X, w.Y, ns, w.Rf, T, mat_stride, der_stride, w.info,
+                                                    out, status, w.uv);
+        nl += 3;
+        RS_CK(cudaGetLastError());
+        if (D >= 1)
+            for (int it = 0; it < kRitzRefine; ++it) {
+                RS_CK(lu_solve_batched(n, nmat, 1, w.A, nn, w.perm, 1, w.uv + n, 2LL * n, st));
+                RS_CK(lu_solve_batched(n, nmat, 0, w.A, nn, w.perm, 1, w.uv + n, 2LL * n, st));
+                nl += 2;
+            }
+    }
+    if (D >= 1) {
+        k_rsvd_vec<<<nmat, kRsvdThreads, 0, st>>>(n, D, T, mat_stride, der_stride, out, w.uv);
+        ++nl;
+        RS_CK(cudaGetLastError());
+    }
+    if (D == 2) {
+        const int n2 = 2 * n;
+        const long long nn2 = (long long)n2 * n2;
+        k_sv2_prep<<<nmat, 256, 0, st>>>(n, w.uv, w.ub, w.mcol);
+        k_build_bordered<<<dim3((int)std::min<long long>(1024, (nn2 + 255) / 256), nmat), 256, 0, st>>>(
+            n, T, mat_stride, out, 3, w.ub, w.mcol, w.B);
+        RS_CK(lu_factor_batched(n2, nmat, w.B, nn2, w.piv2, w.perm2, w.info2, st, &nl));
+        k_wapply<<<nmat, 256, 0, st>>>(n, T + der_stride, mat_stride, w.ub, w.ud, -1., 0);
+        RS_CK(lu_solve_batched(n2, nmat, 0, w.B, nn2, w.perm2, 1, w.ud, n2, st));
+        k_sv2_extract<<<(nmat + 127) / 128, 128, 0, st>>>(n, nmat, w.ud, w.mcol, w.tb);
+        k_wapply<<<nmat, 256, 0, st>>>(n, T + 2 * der_stride, mat_stride, w.ub, w.rhs, 1., 0);
+        k_wapply<<<nmat, 256, 0, st>>>(n, T + der_stride, mat_stride, w.ud, w.rhs, 2., 1);
+        k_sv2_axpy<<<nmat, 256, 0, st>>>(n, w.rhs, w.ud, w.tb);
+        RS_CK(lu_solve_batched(n2, nmat, 0, w.B, nn2, w.perm2, 1, w.rhs, n2, st));
+        k_sv2_out<<<(nmat + 127) / 128, 128, 0, st>>>(n, nmat, w.rhs, w.mcol, w.info2, out);
+        nl += 10;
+        RS_CK(cudaGetLastError());
+    }
+    if (launches) *launches += nl;
+    return cudaSuccess;
 }
 
 }  // namespace hbem

@@ -147,16 +147,33 @@ int hbem_sv_dense_batch(int n, int nmat, unsigned d, const double* T_host, doubl
  * std::random_device, so its sketches are not reproducible).                     */
 int hbem_rand_sketch(int nr, int nc, unsigned long long seed, double* R_host);
 
-/* randomized_svd::sv (d = 0) and sv_der's sigma' (d = 1) (include/randsvd.hpp:53,64;
- * source/utilities/randsvd.cpp:99-169) for a batch: LU of T, q subspace iterations
- * with the n x s sketch R, sigma ~ 1/sigma_max(T^-H Q); sigma' from the Ritz vectors
- * of the sketch.  Matrices of order n with rsvd fitting in shared memory
- * (n <= 108 at s = 16); larger -> HBEM_ERR_UNSUPPORTED.  out_host[2m] = sigma,
- * out_host[2m + 1] = sigma' (0 for d = 0).  T_host: nmat blocks of d + 1 matrices. */
+/* randomized_svd::sv (d = 0), sv_der (d = 1) and sv_der2 (d = 2)
+ * (include/randsvd.hpp:53,64,77; source/utilities/randsvd.cpp:99-216) for a batch
+ * of nmat matrices of order n: LU of T, q subspace iterations with the n x s sketch
+ * R (s <= 32), sigma ~ 1/sigma_max(T^-H Q).  sigma' = Re u^H T' v from the Ritz
+ * vectors of the sketch; sigma'' by the reference's bordered 2n x 2n system (column
+ * m of W - sigma I replaced by -u).  Matrices whose LU and sketch fit in shared
+ * memory (n <= 108 at s = 16) run in one kernel per matrix, larger ones through the
+ * batched global-memory LU below.  out_host[(d+1) m + t] = sigma, sigma', sigma''.
+ * T_host: nmat blocks of d + 1 matrices (T, T', T'').  HBEM_ERR_SINGULAR if an LU of
+ * T meets a zero pivot; a singular bordered system gives sigma'' = NaN, as the
+ * reference's unguarded solve would.                                             */
 int hbem_rsvd_sv_batch(int n, int nmat, unsigned d, const double* T_host, const double* R_host, int s, int q,
                        double* out_host);
 int hbem_rsvd_sv_batch_device(int n, int nmat, unsigned d, const void* T_dev, long long mat_stride,
                               long long der_stride, const void* R_dev, int s, int q, double* out_host);
+
+/* Batched LU with partial pivoting, in place (Eigen::PartialPivLU<MatrixXcd> at
+ * source/utilities/randsvd.cpp:104,205): nmat column-major complex128 matrices of
+ * order n at A_dev + m * stride (elements).  piv_dev[m n + k] = row exchanged with
+ * row k at step k (0-based LAPACK ipiv).  info_host (may be NULL): per matrix 0 or
+ * 1 + the first step with a zero pivot; any zero pivot -> HBEM_ERR_SINGULAR.     */
+int hbem_lu_factor_batch_device(int n, int nmat, void* A_dev, long long stride, int* piv_dev, int* info_host);
+/* Solve with the factors (PartialPivLU::solve, and .adjoint().solve for trans = 1):
+ * X_m <- T_m^-1 X_m or T_m^-H X_m, nrhs columns at X_dev + m * xstride, leading
+ * dimension n.                                                                   */
+int hbem_lu_solve_batch_device(int n, int nmat, int trans, const void* LU_dev, long long stride, const int* piv_dev,
+                               int nrhs, void* X_dev, long long xstride);
 
 /* sigma_min(k) and its derivatives along a list of real wavenumbers, end to end:
  * gen_sol_op_*der + direct::sv_*der per k (examples/roots_newton_circle.cpp:111-138).

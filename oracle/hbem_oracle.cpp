@@ -740,7 +740,10 @@ static void assemble_dense(Builder &B, cd k_in, double c_in, int layers, int d,
         if (ret) { m -= m0; n -= n0; }
         return ret;
     };
-    /* 4-colour pair lists so concurrent scatters never collide (galerkin_builder.cpp:964-1013) */
+    /* 4-colour pair lists (galerkin_builder.cpp:964-1013).  The colouring does not keep
+     * concurrent scatters apart once square-case pairs are reordered to (max, min), nor
+     * across the cyclic P1 wrap for odd N, so the pair blocks are computed in parallel
+     * and scattered serially, in list order: deterministic sums.                  */
     int inits[4][2] = {{0, 0}, {1, 0}, {0, 1}, {1, 1}};
     for (int sc = 0; sc < 4; ++sc) {
         std::vector<std::pair<int, int>> ind;
@@ -749,24 +752,33 @@ static void assemble_dense(Builder &B, cd k_in, double c_in, int layers, int d,
                 if (!is_square) ind.push_back({i, j});
                 else if (is_required(i, j)) ind.push_back({std::max(i, j), std::min(i, j)});
             }
+        std::vector<Local> locs(ind.size());
+        std::vector<int> kinds(ind.size());
 #pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads)
         for (long q = 0; q < (long)ind.size(); ++q) {
             int i = ind[q].first, j = ind[q].second;
-            int step = (i != j && is_square) ? 2 : 1;
             bool comp_hs = is_square || is_required(i, j);
             Geo G;
-            Local Lc;
+            Local &Lc = locs[q];
             std::memset((void *)&Lc, 0, sizeof(Lc));
             bool swap = false;
             int kind;
             if (i == j) { kind = CNC; compute_coinciding(B, i, G); }
             else if (B.is_adjacent(i, j, swap)) { kind = ADJ; compute_adjacent(B, i, j, swap, G); }
             else { kind = GEN; compute_general(B, i, j, G); }
+            kinds[q] = kind;
             if (hasL[0]) double_layer(B, kind, swap, d, is_square, G, Lc);
             if (kind == CNC || comp_hs) {
                 if (hasL[1]) hypersingular(B, kind, swap, d, G, Lc);
                 if (hasL[2]) single_layer(B, kind, swap, d, G, Lc);
             }
+        }
+        for (long q = 0; q < (long)ind.size(); ++q) {
+            int i = ind[q].first, j = ind[q].second;
+            int step = (i != j && is_square) ? 2 : 1;
+            bool comp_hs = is_square || is_required(i, j);
+            const Local &Lc = locs[q];
+            int kind = kinds[q];
             /* local -> global (map_local_to_global, galerkin_builder.cpp:334-344) */
             for (int L = 0; L < 3; ++L) {
                 if (!hasL[L]) continue;

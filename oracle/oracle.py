@@ -437,6 +437,38 @@ def rsvd_sv_der(T, T1, R, q=0):
     return s, float(np.real(np.vdot(x, p)))
 
 
+def _wapply(A, x):
+    n = A.shape[0]
+    return np.concatenate([A @ x[n:], A.conj().T @ x[:n]])
+
+
+def rsvd_sv_der2(T, T1, T2, R, q=0):
+    """randomized_svd::sv_der2 (randsvd.cpp:171-216): x = unit null vector of
+    W - s I; m = argmax |x_l| (first); u = x / x_m; B = W - s I with column m
+    replaced by -u; u' = -B^-1 W'u, t = u'_m, u'_m = 0;
+    s'' = -[B^-1 (W''u + 2 (W'u' - t u'))]_m."""
+    n = T.shape[0]
+    s = rsvd_sv(T, R, q)
+    W = np.zeros((2 * n, 2 * n), complex)
+    W[:n, n:] = T; W[n:, :n] = T.conj().T
+    W -= s * np.eye(2 * n)
+    _, _, vh = np.linalg.svd(W)
+    x = vh[-1].conj()
+    x = x / np.linalg.norm(x)
+    d1 = float(np.real(np.vdot(x, _wapply(T1, x))))
+    m = int(np.argmax(np.abs(x)))
+    u = x / x[m]
+    B = W.copy()
+    B[:, m] = -u
+    lu = sla.lu_factor(B)
+    ud = -sla.lu_solve(lu, _wapply(T1, u))
+    t = ud[m]
+    ud[m] = 0.0
+    rhs = _wapply(T2, u) + 2.0 * (_wapply(T1, ud) - t * ud)
+    d2 = float(-np.real(sla.lu_solve(lu, rhs)[m]))
+    return s, d1, d2
+
+
 # ----------------------------------------------------------------- root finding
 
 EPS = np.finfo(float).eps

@@ -39,3 +39,57 @@ def test_rsvd_sv_der_close_to_dense_derivative():
         assert abs(g[0] - ref[0]) <= 1e-8 * ref[0]
         assert abs(g[1] - ref[1]) <= 1e-6 * max(abs(ref[1]), 1e-3)
 
+
+
+def _rel(a, b):
+    return abs(a - b) / max(abs(b), 1e-300)
+
+
+def test_rsvd_sv_der2_small_path_vs_oracle():
+    """sv_der2 (bordered 2n x 2n system) with the shared-memory LU path (n = 96)."""
+    mats = _mats([2.7, 4.05, 6.3], d=2)
+    n = mats[0][0].shape[0]
+    R = O.rand_sketch(n, 16, seed=3)
+    got = api.rsvd_sv(mats, R, q=3, d=2)
+    for m, g in zip(mats, got):
+        s, d1, d2 = O.rsvd_sv_der2(m[0], m[1], m[2], R, 3)
+        assert _rel(g[0], s) < 1e-10
+        assert abs(g[1] - d1) <= 1e-8 * max(abs(d1), 1e-2)
+        assert abs(g[2] - d2) <= 1e-7 * max(abs(d2), 1e-1)
+
+
+@pytest.mark.parametrize("q", [0, 2])
+def test_rsvd_global_path_vs_oracle(q):
+    """n = 160 (too large for one CTA's shared memory): batched global LU, solves,
+    QR; sigma, sigma', sigma'' against the oracle with the same sketch."""
+    mats = _mats([1.7, 3.9, 5.2], npan=80, order=7, d=2)
+    n = mats[0][0].shape[0]
+    R = O.rand_sketch(n, 12, seed=5)
+    got0 = api.rsvd_sv(mats, R, q=q, d=0)[:, 0]
+    got = api.rsvd_sv(mats, R, q=q, d=2)
+    for m, g0, g in zip(mats, got0, got):
+        s_ref = O.rsvd_sv(m[0], R, q)
+        assert _rel(g0, s_ref) < 1e-10 and _rel(g[0], s_ref) < 1e-10
+        if q == 2:
+            s, d1, d2 = O.rsvd_sv_der2(m[0], m[1], m[2], R, q)
+            assert abs(g[1] - d1) <= 1e-8 * max(abs(d1), 1e-2)
+            assert abs(g[2] - d2) <= 1e-7 * max(abs(d2), 1e-1)
+
+
+def test_rsvd_batched_scatterer_size():
+    """Star polygon with N = 800 line panels (T of order 1600, the largest scatterer
+    of the batching workload), sketch 12, two subspace steps, four wavenumbers in one
+    batch: sigma equals the oracle's rSVD with the same sketch, and is an upper bound
+    within 1e-6 of the dense sigma_min."""
+    kinds, par = geometry.polygon(*geometry.star_polygon(24, seed=2), 800)
+    so = api.SolutionsOperator(api.BuilderData((kinds, par), order=11))
+    ks = [3.0, 7.5, 12.25, 19.0]
+    mats = [[so.gen_sol_op(k, 1.0, 9.0)] for k in ks]
+    n = mats[0][0].shape[0]
+    R = api.randGaussian(n, 12, seed=2024)
+    got = api.rsvd_sv(mats, R, q=2, d=0)[:, 0]
+    for m, g in zip(mats, got):
+        ref = O.rsvd_sv(m[0], R, 2)
+        assert _rel(g, ref) < 1e-10
+    dense = np.linalg.svd(mats[1][0], compute_uv=False).min()
+    assert got[1] >= dense * (1 - 1e-12) and (got[1] - dense) / dense < 1e-6

@@ -232,13 +232,84 @@ def assembly_at_scale(torch, C, api, geometry, lib, peak):
             "assembly_fp64_tflops": achieved, "assembly_frac_of_measured_fp64": achieved / peak if peak else None}
 
 
+def dense_tail_at_scale(torch, C, api, geometry, lib, peak, nk=16):
+    """Largest scatterer of the batching configuration: star polygon (24 vertices,
+    seed 2), N = 800 line panels (T of order 1600), order 11, c_i = 9, c_o = 1; nk
+    wavenumbers uniform on [1, 30] assembled in one batch, then randomized_svd::sv
+    (sketch 12, 2 subspace steps) on all of them.  Reports T(k)/s for assembly and
+    for the rSVD, and the batched LU's algorithmic FP64 rate ((8/3) n^3 real flops
+    per matrix, CUDA events on the launching stream)."""
+    N, order = 800, 11
+    n = 2 * N
+    data = api.BuilderData(geometry.polygon(*geometry.star_polygon(24, seed=2), N), order=order)
+    so = api.SolutionsOperator(data)
+    ks = np.random.default_rng(3000).uniform(1.0, 30.0, nk)
+    T = torch.empty((nk, n, n), dtype=torch.complex128, device="cuda")
+    R = torch.from_numpy(np.ascontiguousarray(api.randGaussian(n, 12, seed=3000).T)).cuda()
+    A = torch.empty_like(T)
+    piv = torch.empty(nk * n, dtype=torch.int32, device="cuda")
+    out = np.zeros(nk)
+    ev = lambda: torch.cuda.Event(enable_timing=True)   # noqa: E731
+
+    def assemble():
+        C.check(lib.hbem_gen_sol_op_batch_device(so._h, C.dptr(ks), nk, 1.0, 9.0, 0, C.ctypes.c_void_p(T.data_ptr())))
+
+    def lu():
+        A.copy_(T)
+        C.check(lib.hbem_lu_factor_batch_device(n, nk, C.ctypes.c_void_p(A.data_ptr()), n * n,
+                                                C.ctypes.c_void_p(piv.data_ptr()), None))
+
+    def rsvd():
+        C.check(lib.hbem_rsvd_sv_batch_device(n, nk, 0, C.ctypes.c_void_p(T.data_ptr()), n * n, n * n,
+                                              C.ctypes.c_void_p(R.data_ptr()), 12, 2, C.dptr(out)))
+
+    out32 = np.zeros(nk)
+
+    def rsvd_mixed():
+        C.check(lib.hbem_rsvd_sv_batch_device_ex(n, nk, 0, C.ctypes.c_void_p(T.data_ptr()), n * n, n * n,
+                                                 C.ctypes.c_void_p(R.data_ptr()), 12, 2, 1, 3, C.dptr(out32)))
+
+    res = {}
+    for name, fn in (("assembly", assemble), ("lu", lu), ("rsvd", rsvd), ("rsvd_mixed", rsvd_mixed)):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = ev(), ev()
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        res[name] = e0.elapsed_time(e1)
+    A.copy_(T)
+    torch.cuda.synchronize()
+    e0, e1 = ev(), ev()
+    e0.record()
+    C.check(lib.hbem_lu_factor_batch_device(n, nk, C.ctypes.c_void_p(A.data_ptr()), n * n,
+                                            C.ctypes.c_void_p(piv.data_ptr()), None))
+    e1.record()
+    torch.cuda.synchronize()
+    lu_ms = e0.elapsed_time(e1)
+    lu_tf = nk * (8.0 / 3.0) * n ** 3 / (lu_ms * 1e-3) / 1e12
+    del T, A
+    return {"workload": "star polygon 24 vertices (seed 2), N=800 lines (T 1600x1600 c128), order 11, c_i=9, "
+                        "%d k in [1,30]; rSVD sketch 12, q=2" % nk,
+            "assembly_ms_per_T": res["assembly"] / nk, "rsvd_ms_per_T": res["rsvd"] / nk,
+            "lu_ms_per_T": lu_ms / nk, "lu_fp64_tflops": lu_tf,
+            "lu_frac_of_measured_fp64": lu_tf / peak if peak else None,
+            "T_per_s_assembly_plus_rsvd": 1e3 * nk / (res["assembly"] + res["rsvd"]),
+            "rsvd_mixed_ms_per_T": res["rsvd_mixed"] / nk,
+            "T_per_s_assembly_plus_rsvd_mixed": 1e3 * nk / (res["assembly"] + res["rsvd_mixed"]),
+            "rsvd_mixed_max_rel_err_vs_fp64": float(np.max(np.abs(out32 - out) / out)),
+            "sigma_min": [float(x) for x in out[:4]]}
+
+
 def run_gpu(args):
     rank, world, local = dist_env()
     import torch
     torch.cuda.set_device(local)
     if world > 1:
+        # independent replicas: the ranks meet only on the host (barrier, max time)
         import torch.distributed as dist
-        dist.init_process_group("nccl")
+        dist.init_process_group("gloo")
     from helmholtzbem_gb300 import _capi as C, api, geometry
 
     C.check(C.lib().hbem_set_device(local))
@@ -284,10 +355,10 @@ def run_gpu(args):
     launches, asm_ms, asm_l, asm_pts = (C.ctypes.c_longlong(), C.ctypes.c_double(), C.ctypes.c_longlong(),
                                         C.ctypes.c_longlong())
     lib.hbem_stats_read(C.ctypes.byref(launches), C.ctypes.byref(asm_ms), C.ctypes.byref(asm_l), C.ctypes.byref(asm_pts))
-    t = torch.tensor([tot_ms], device="cuda")
+    t = torch.tensor([tot_ms], dtype=torch.float64)
     if world > 1:
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        vv = torch.tensor([float(tot_v)], device="cuda")
+        vv = torch.tensor([float(tot_v)], dtype=torch.float64)
         torch.distributed.all_reduce(vv)
         tot_v_all = vv.item()
     else:
@@ -329,6 +400,7 @@ def run_gpu(args):
                 "avg_launch_ms": asm_ms.value / max(1, asm_l.value)}
 
     scale = assembly_at_scale(torch, C, api, geometry, lib, peak)
+    tail = dense_tail_at_scale(torch, C, api, geometry, lib, peak)
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
@@ -352,6 +424,7 @@ def run_gpu(args):
             "gpu_launches": int(launches.value),
             "roofline": roofline,
             "assembly_at_scale": scale,
+            "dense_tail_at_scale": tail,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }

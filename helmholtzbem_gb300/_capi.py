@@ -23,7 +23,7 @@ EXPORTS = [
     "hbem_solop_create", "hbem_solop_destroy", "hbem_mass_matrix", "hbem_gen_sol_op",
     "hbem_gen_sol_op_batch_device", "hbem_sv_dense_batch_device", "hbem_sv_dense_batch_noalloc",
     "hbem_sv_dense_batch", "hbem_sweep_sigma", "hbem_rand_sketch", "hbem_rsvd_sv_batch",
-    "hbem_rsvd_sv_batch_device", "hbem_lu_factor_batch_device", "hbem_lu_solve_batch_device",
+    "hbem_rsvd_sv_batch_device", "hbem_rsvd_sv_batch_device_ex", "hbem_lu_factor_batch_device", "hbem_lu_solve_batch_device",
     "hbem_find_resonances_plain", "hbem_rtsafe", "hbem_zbrent", "hbem_brent_min",
 ]
 
@@ -89,6 +89,8 @@ def load(path=LIB_PATH):
         "hbem_rsvd_sv_batch": (_i, [_i, _i, _u, _dp, _dp, _i, _i, _dp]),
         "hbem_rsvd_sv_batch_device": (_i, [_i, _i, _u, _vp, ctypes.c_longlong, ctypes.c_longlong, _vp, _i, _i,
                                            _dp]),
+        "hbem_rsvd_sv_batch_device_ex": (_i, [_i, _i, _u, _vp, ctypes.c_longlong, ctypes.c_longlong, _vp, _i, _i,
+                                              _i, _i, _dp]),
         "hbem_lu_factor_batch_device": (_i, [_i, _i, _vp, ctypes.c_longlong, _vp, _ip]),
         "hbem_lu_solve_batch_device": (_i, [_i, _i, _i, _vp, ctypes.c_longlong, _vp, _i, _vp, ctypes.c_longlong]),
         "hbem_find_resonances_plain": (_i, [_vp, _d, _d, _i, _d, _d, _d, _dp, _i, _ip, _dp, _ip]),

@@ -28,10 +28,10 @@ cudaError_t launch_svd_mixed(int n, int nmat, int D, int which, const cplx* T, l
                              cudaStream_t st);
 cudaError_t launch_hankel01(int n, const cplx* z, int complex_arg, cplx* h0, cplx* h1, cudaStream_t st);
 bool rsvd_supported(int n, int s, int D);
-size_t rsvd_work_bytes(int n, int nmat, int s, int D);
-cudaError_t rsvd_batched(int n, int nmat, int s, int q, int D, const cplx* T, long long mat_stride,
-                         long long der_stride, const cplx* R, double* out, int* status, void* work,
-                         size_t work_bytes, cudaStream_t st, long long* launches);
+size_t rsvd_work_bytes(int n, int nmat, int s, int D, int precision);
+cudaError_t rsvd_batched(int n, int nmat, int s, int q, int D, int precision, int refine, const cplx* T,
+                         long long mat_stride, long long der_stride, const cplx* R, double* out, int* status,
+                         void* work, size_t work_bytes, cudaStream_t st, long long* launches);
 cudaError_t lu_factor_batched(int n, int nmat, cplx* A, long long stride, int* piv, int* perm, int* info,
                               cudaStream_t st, long long* launches);
 cudaError_t lu_solve_batched(int n, int nmat, int trans, const cplx* LU, long long stride, const int* perm, int s,
@@ -688,9 +688,11 @@ int hbem_rand_sketch(int nr, int nc, unsigned long long seed, double* R_host) {
     return HBEM_OK;
 }
 
-int hbem_rsvd_sv_batch_device(int n, int nmat, unsigned d, const void* T_dev, long long mat_stride,
-                              long long der_stride, const void* R_dev, int s, int q, double* out_host) {
-    if (n < 2 || nmat < 1 || nmat > 65535 || d > 2 || !T_dev || !R_dev || !out_host || s < 1 || s > n || q < 0)
+int hbem_rsvd_sv_batch_device_ex(int n, int nmat, unsigned d, const void* T_dev, long long mat_stride,
+                                 long long der_stride, const void* R_dev, int s, int q, int precision, int refine,
+                                 double* out_host) {
+    if (n < 2 || nmat < 1 || nmat > 65535 || d > 2 || !T_dev || !R_dev || !out_host || s < 1 || s > n || q < 0 ||
+        precision < 0 || precision > 1 || refine < 1 || refine > 16)
         return fail(HBEM_ERR_INVALID, "rsvd_sv_batch: bad argument");
     if (!rsvd_supported(n, s, (int)d))
         return fail(HBEM_ERR_UNSUPPORTED, "rsvd_sv_batch: sketch wider than 32 columns, or a matrix too large for "
@@ -700,11 +702,12 @@ int hbem_rsvd_sv_batch_device(int n, int nmat, unsigned d, const void* T_dev, lo
     const size_t os = d + 1;
     HB_CK(out.ensure((size_t)nmat * os * sizeof(double)));
     HB_CK(status.ensure((size_t)nmat * sizeof(int)));
-    const size_t wb = rsvd_work_bytes(n, nmat, s, (int)d);
+    const size_t wb = rsvd_work_bytes(n, nmat, s, (int)d, precision);
     HB_CK(work.ensure(std::max<size_t>(wb, 256)));
     long long nl = 0;
-    HB_CK(rsvd_batched(n, nmat, s, q, (int)d, static_cast<const cplx*>(T_dev), mat_stride, der_stride,
-                       static_cast<const cplx*>(R_dev), out.as<double>(), status.as<int>(), work.p, work.cap, 0, &nl));
+    HB_CK(rsvd_batched(n, nmat, s, q, (int)d, precision, refine, static_cast<const cplx*>(T_dev), mat_stride,
+                       der_stride, static_cast<const cplx*>(R_dev), out.as<double>(), status.as<int>(), work.p,
+                       work.cap, 0, &nl));
     g_launches += nl;
     std::vector<int> st(nmat);
     HB_CK(cudaMemcpy(out_host, out.p, (size_t)nmat * os * sizeof(double), cudaMemcpyDeviceToHost));
@@ -712,6 +715,11 @@ int hbem_rsvd_sv_batch_device(int n, int nmat, unsigned d, const void* T_dev, lo
     for (int v : st)
         if (v) return fail(HBEM_ERR_SINGULAR, "rsvd_sv_batch: zero pivot in the LU of T");
     return HBEM_OK;
+}
+
+int hbem_rsvd_sv_batch_device(int n, int nmat, unsigned d, const void* T_dev, long long mat_stride,
+                              long long der_stride, const void* R_dev, int s, int q, double* out_host) {
+    return hbem_rsvd_sv_batch_device_ex(n, nmat, d, T_dev, mat_stride, der_stride, R_dev, s, q, 0, 1, out_host);
 }
 
 int hbem_rsvd_sv_batch(int n, int nmat, unsigned d, const double* T_host, const double* R_host, int s, int q,

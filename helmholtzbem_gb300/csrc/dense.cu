@@ -44,11 +44,8 @@ struct SvdJob {
     int a_in_smem;
 };
 
-// single-precision complex for the first Jacobi stage of the mixed-precision kernel
-struct cpf {
-    float re, im;
-};
-__device__ __forceinline__ cpf mkf(float r, float i) { cpf z; z.re = r; z.im = i; return z; }
+// single-precision complex (cplxf) for the first Jacobi stage of the mixed-precision kernel
+typedef cplxf cpf;
 
 __device__ __forceinline__ float warp_sumf(float x) {
 #pragma unroll

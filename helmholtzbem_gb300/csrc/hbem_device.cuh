@@ -46,6 +46,44 @@ __device__ __forceinline__ cplx csqrt(cplx z) {
 }
 __device__ __forceinline__ cplx cexp(cplx z) { double e = exp(z.re), s, c; sincos(z.im, &s, &c); return mk(e * c, e * s); }
 
+// complex<float> for the single-precision LU of the dense tail
+struct cplxf {
+    float re, im;
+};
+__host__ __device__ __forceinline__ cplxf mkf(float r, float i = 0.f) { cplxf z; z.re = r; z.im = i; return z; }
+__host__ __device__ __forceinline__ cplxf operator+(cplxf a, cplxf b) { return mkf(a.re + b.re, a.im + b.im); }
+__host__ __device__ __forceinline__ cplxf operator-(cplxf a, cplxf b) { return mkf(a.re - b.re, a.im - b.im); }
+__host__ __device__ __forceinline__ cplxf operator-(cplxf a) { return mkf(-a.re, -a.im); }
+__host__ __device__ __forceinline__ cplxf operator*(cplxf a, cplxf b) {
+    return mkf(fmaf(a.re, b.re, -a.im * b.im), fmaf(a.re, b.im, a.im * b.re));
+}
+__host__ __device__ __forceinline__ cplxf operator*(float s, cplxf a) { return mkf(s * a.re, s * a.im); }
+__host__ __device__ __forceinline__ cplxf& operator+=(cplxf& a, cplxf b) { a.re += b.re; a.im += b.im; return a; }
+__host__ __device__ __forceinline__ cplxf& operator-=(cplxf& a, cplxf b) { a.re -= b.re; a.im -= b.im; return a; }
+__host__ __device__ __forceinline__ cplxf conj(cplxf a) { return mkf(a.re, -a.im); }
+__host__ __device__ __forceinline__ float norm2(cplxf a) { return fmaf(a.re, a.re, a.im * a.im); }
+__device__ __forceinline__ cplxf cdiv(cplxf a, cplxf b) {
+    // scaled so that |b|^2 cannot overflow or underflow in single precision
+    const float s = fmaxf(fabsf(b.re), fabsf(b.im));
+    if (s == 0.f) return mkf(a.re / s, a.im / s);
+    const float br = b.re / s, bi = b.im / s, ar = a.re / s, ai = a.im / s;
+    const float d = 1.f / (br * br + bi * bi);
+    return mkf((ar * br + ai * bi) * d, (ai * br - ar * bi) * d);
+}
+
+// element-type helpers for code templated on cplx / cplxf
+template <class E> struct Elem;
+template <> struct Elem<cplx> {
+    typedef double real;
+    __device__ __forceinline__ static cplx zero() { return mk(0.); }
+    __device__ __forceinline__ static cplx one() { return mk(1.); }
+};
+template <> struct Elem<cplxf> {
+    typedef float real;
+    __device__ __forceinline__ static cplxf zero() { return mkf(0.f); }
+    __device__ __forceinline__ static cplxf one() { return mkf(1.f); }
+};
+
 constexpr double kEps = 2.220446049250313e-16;
 constexpr double kEulerGamma = 0.57721566490153286061;
 constexpr double kPi = 3.14159265358979323846;

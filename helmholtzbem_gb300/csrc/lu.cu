@@ -11,6 +11,8 @@
 // Matrices are column-major with leading dimension n (Eigen's layout); matrix m
 // starts at A + m * stride.  piv[m*n + k] = row exchanged with row k at step k
 // (LAPACK's ipiv, 0-based); perm[m*n + i] = source row of row i of P A.
+#include <algorithm>
+
 #include "hbem_device.cuh"
 
 namespace hbem {
@@ -21,18 +23,19 @@ constexpr int kLuTile = 64;
 constexpr int kLuSolveThreads = 512;
 constexpr int kLuSolveChunk = 16;      // right-hand sides held in registers at a time
 
-__global__ void __launch_bounds__(kLuPanelThreads) k_lu_panel(int n, int k0, int nb, cplx* A, long long stride,
+template <class E>
+__global__ void __launch_bounds__(kLuPanelThreads) k_lu_panel(int n, int k0, int nb, E* A, long long stride,
                                                               int* piv, int* info) {
-    cplx* M = A + (long long)blockIdx.x * stride;
+    E* M = A + (long long)blockIdx.x * stride;
     int* pv = piv + (long long)blockIdx.x * n;
     __shared__ double rv[32];
     __shared__ int ri[32];
-    __shared__ cplx prow[kLuNB];
+    __shared__ E prow[kLuNB];
     __shared__ int s_p;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int j = 0; j < nb; ++j) {
         const int c = k0 + j;
-        cplx* col = M + (long long)c * n;
+        E* col = M + (long long)c * n;
         double best = -1.;
         int bi = c;
         for (int i = c + threadIdx.x; i < n; i += blockDim.x) {
@@ -59,20 +62,20 @@ __global__ void __launch_bounds__(kLuPanelThreads) k_lu_panel(int n, int k0, int
         __syncthreads();
         const int p = s_p;
         if (threadIdx.x < nb) {
-            cplx* a = M + (long long)(k0 + threadIdx.x) * n;
-            const cplx x = a[c], y = a[p];
+            E* a = M + (long long)(k0 + threadIdx.x) * n;
+            const E x = a[c], y = a[p];
             if (p != c) { a[c] = y; a[p] = x; }
             prow[threadIdx.x] = (p != c) ? y : x;
         }
         __syncthreads();
-        const cplx d = prow[j];
-        const bool nz = norm2(d) > 0.;
-        const cplx id = nz ? cdiv(mk(1.), d) : mk(0.);
+        const E d = prow[j];
+        const bool nz = norm2(d) > 0;
+        const E id = nz ? cdiv(Elem<E>::one(), d) : Elem<E>::zero();
         for (int i = c + 1 + threadIdx.x; i < n; i += blockDim.x) {
-            cplx l = col[i];
+            E l = col[i];
             if (nz) { l = l * id; col[i] = l; }
             for (int cc = j + 1; cc < nb; ++cc) {
-                cplx* a = M + (long long)(k0 + cc) * n;
+                E* a = M + (long long)(k0 + cc) * n;
                 a[i] -= l * prow[cc];
             }
         }
@@ -81,23 +84,24 @@ __global__ void __launch_bounds__(kLuPanelThreads) k_lu_panel(int n, int k0, int
 }
 
 // grid (ceil(n/32), nmat): column block b covers columns [32 b, 32 b + 32).
-__global__ void __launch_bounds__(256) k_lu_swap_trsm(int n, int k0, int nb, cplx* A, long long stride,
+template <class E>
+__global__ void __launch_bounds__(256) k_lu_swap_trsm(int n, int k0, int nb, E* A, long long stride,
                                                       const int* piv) {
     const int col0 = blockIdx.x * kLuNB;
     if (col0 == k0) return;                            // the panel itself
-    cplx* M = A + (long long)blockIdx.y * stride;
+    E* M = A + (long long)blockIdx.y * stride;
     const int* pv = piv + (long long)blockIdx.y * n;
     const int ncols = min(kLuNB, n - col0);
     __shared__ int sp[kLuNB];
-    __shared__ cplx L11[kLuNB][kLuNB + 1];
+    __shared__ E L11[kLuNB][kLuNB + 1];
     if (threadIdx.x < nb) sp[threadIdx.x] = pv[k0 + threadIdx.x];
     __syncthreads();
     if (threadIdx.x < ncols) {
-        cplx* a = M + (long long)(col0 + threadIdx.x) * n;
+        E* a = M + (long long)(col0 + threadIdx.x) * n;
         for (int j = 0; j < nb; ++j) {
             const int p = sp[j];
             if (p != k0 + j) {
-                const cplx t = a[k0 + j];
+                const E t = a[k0 + j];
                 a[k0 + j] = a[p];
                 a[p] = t;
             }
@@ -111,39 +115,42 @@ __global__ void __launch_bounds__(256) k_lu_swap_trsm(int n, int k0, int nb, cpl
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int cc = warp; cc < ncols; cc += (blockDim.x >> 5)) {
-        cplx* a = M + (long long)(col0 + cc) * n + k0;
-        cplx x = lane < nb ? a[lane] : mk(0.);
+        E* a = M + (long long)(col0 + cc) * n + k0;
+        E x = lane < nb ? a[lane] : Elem<E>::zero();
         for (int k = 0; k < nb; ++k) {
-            const double xr = __shfl_sync(0xffffffffu, x.re, k), xi = __shfl_sync(0xffffffffu, x.im, k);
-            if (lane > k && lane < nb) x -= L11[lane][k] * mk(xr, xi);
+            E xk;
+            xk.re = __shfl_sync(0xffffffffu, x.re, k);
+            xk.im = __shfl_sync(0xffffffffu, x.im, k);
+            if (lane > k && lane < nb) x -= L11[lane][k] * xk;
         }
         if (lane < nb) a[lane] = x;
     }
 }
 
 // grid (tiles over trailing rows, tiles over trailing columns, nmat)
-__global__ void __launch_bounds__(256) k_lu_gemm(int n, int k0, int nb, cplx* A, long long stride) {
+template <class E>
+__global__ void __launch_bounds__(256) k_lu_gemm(int n, int k0, int nb, E* A, long long stride) {
     extern __shared__ double lu_smem[];
-    cplx* La = reinterpret_cast<cplx*>(lu_smem);          // [k][i], 32 x 64
-    cplx* Ub = La + kLuNB * kLuTile;                      // [k][j], 32 x 64
+    E* La = reinterpret_cast<E*>(lu_smem);                // [k][i], 32 x 64
+    E* Ub = La + kLuNB * kLuTile;                         // [k][j], 32 x 64
     const int t0 = k0 + nb;
     const int r0 = t0 + blockIdx.x * kLuTile, c0 = t0 + blockIdx.y * kLuTile;
-    cplx* M = A + (long long)blockIdx.z * stride;
+    E* M = A + (long long)blockIdx.z * stride;
     for (int e = threadIdx.x; e < kLuNB * kLuTile; e += blockDim.x) {
         const int i = e % kLuTile, k = e / kLuTile;
-        La[k * kLuTile + i] = (k < nb && r0 + i < n) ? M[(r0 + i) + (long long)(k0 + k) * n] : mk(0.);
+        La[k * kLuTile + i] = (k < nb && r0 + i < n) ? M[(r0 + i) + (long long)(k0 + k) * n] : Elem<E>::zero();
         const int kk = e % kLuNB, j = e / kLuNB;
-        Ub[kk * kLuTile + j] = (kk < nb && c0 + j < n) ? M[(k0 + kk) + (long long)(c0 + j) * n] : mk(0.);
+        Ub[kk * kLuTile + j] = (kk < nb && c0 + j < n) ? M[(k0 + kk) + (long long)(c0 + j) * n] : Elem<E>::zero();
     }
     __syncthreads();
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    cplx acc[4][4];
+    E acc[4][4];
 #pragma unroll
     for (int a = 0; a < 4; ++a)
 #pragma unroll
-        for (int b = 0; b < 4; ++b) acc[a][b] = mk(0.);
+        for (int b = 0; b < 4; ++b) acc[a][b] = Elem<E>::zero();
     for (int k = 0; k < nb; ++k) {
-        cplx av[4], bv[4];
+        E av[4], bv[4];
 #pragma unroll
         for (int a = 0; a < 4; ++a) av[a] = La[k * kLuTile + tx + 16 * a];
 #pragma unroll
@@ -184,16 +191,16 @@ __global__ void k_lu_perm(int n, const int* piv, int* perm) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) perm[(long long)blockIdx.x * n + i] = pm[i];
 }
 
-size_t lu_solve_smem_bytes(int n) {
-    return (size_t)n * sizeof(cplx) + (size_t)kLuNB * (kLuNB + 1) * sizeof(cplx) +
-           (size_t)kLuNB * kLuSolveChunk * sizeof(cplx);
+size_t lu_solve_smem_bytes(int n, size_t esz) {
+    return ((size_t)n + (size_t)kLuNB * (kLuNB + 1) + (size_t)kLuNB * kLuSolveChunk) * esz;
 }
 
 // Row permutation of the s columns of X in place through a shared-memory column
 // buffer: forward (X <- P X) or inverse (X <- P^T X).
-__device__ void permute_rows(cplx* X, int n, int s, const int* perm, cplx* buf, bool inverse) {
+template <class E>
+__device__ void permute_rows(E* X, int n, int s, const int* perm, E* buf, bool inverse) {
     for (int c = 0; c < s; ++c) {
-        cplx* x = X + (long long)c * n;
+        E* x = X + (long long)c * n;
         for (int i = threadIdx.x; i < n; i += blockDim.x) buf[i] = x[i];
         __syncthreads();
         if (!inverse)
@@ -205,10 +212,11 @@ __device__ void permute_rows(cplx* X, int n, int s, const int* perm, cplx* buf, 
 }
 
 // X <- T^-1 X (s columns), P T = L U stored in M.  Right-looking by 32-row blocks.
-__device__ void lu_solve_n(const cplx* M, const int* perm, int n, cplx* X, int s, cplx* sm) {
-    cplx* buf = sm;
-    cplx (*D)[kLuNB + 1] = reinterpret_cast<cplx (*)[kLuNB + 1]>(sm + n);
-    cplx* xb = sm + n + kLuNB * (kLuNB + 1);            // [c][k], kLuSolveChunk x 32
+template <class E>
+__device__ void lu_solve_n(const E* M, const int* perm, int n, E* X, int s, E* sm) {
+    E* buf = sm;
+    E (*D)[kLuNB + 1] = reinterpret_cast<E (*)[kLuNB + 1]>(sm + n);
+    E* xb = sm + n + kLuNB * (kLuNB + 1);            // [c][k], kLuSolveChunk x 32
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     permute_rows(X, n, s, perm, buf, false);
     for (int b0 = 0; b0 < n; b0 += kLuNB) {
@@ -221,21 +229,23 @@ __device__ void lu_solve_n(const cplx* M, const int* perm, int n, cplx* X, int s
         for (int cb = 0; cb < s; cb += kLuSolveChunk) {
             const int cs = min(kLuSolveChunk, s - cb);
             for (int c = warp; c < cs; c += nw) {
-                cplx* x = X + (long long)(cb + c) * n + b0;
-                cplx v = lane < bs ? x[lane] : mk(0.);
+                E* x = X + (long long)(cb + c) * n + b0;
+                E v = lane < bs ? x[lane] : Elem<E>::zero();
                 for (int k = 0; k < bs; ++k) {
-                    const double vr = __shfl_sync(0xffffffffu, v.re, k), vi = __shfl_sync(0xffffffffu, v.im, k);
-                    if (lane > k && lane < bs) v -= D[lane][k] * mk(vr, vi);
+                    E vk;
+                    vk.re = __shfl_sync(0xffffffffu, v.re, k);
+                    vk.im = __shfl_sync(0xffffffffu, v.im, k);
+                    if (lane > k && lane < bs) v -= D[lane][k] * vk;
                 }
                 if (lane < bs) { x[lane] = v; xb[c * kLuNB + lane] = v; }
             }
             __syncthreads();
             for (int i = b0 + bs + threadIdx.x; i < n; i += blockDim.x) {
-                cplx acc[kLuSolveChunk];
+                E acc[kLuSolveChunk];
 #pragma unroll
-                for (int c = 0; c < kLuSolveChunk; ++c) acc[c] = mk(0.);
+                for (int c = 0; c < kLuSolveChunk; ++c) acc[c] = Elem<E>::zero();
                 for (int k = 0; k < bs; ++k) {
-                    const cplx l = M[i + (long long)(b0 + k) * n];
+                    const E l = M[i + (long long)(b0 + k) * n];
 #pragma unroll
                     for (int c = 0; c < kLuSolveChunk; ++c)
                         if (c < cs) acc[c] += l * xb[c * kLuNB + k];
@@ -257,22 +267,24 @@ __device__ void lu_solve_n(const cplx* M, const int* perm, int n, cplx* X, int s
         for (int cb = 0; cb < s; cb += kLuSolveChunk) {
             const int cs = min(kLuSolveChunk, s - cb);
             for (int c = warp; c < cs; c += nw) {
-                cplx* x = X + (long long)(cb + c) * n + b0;
-                cplx v = lane < bs ? x[lane] : mk(0.);
+                E* x = X + (long long)(cb + c) * n + b0;
+                E v = lane < bs ? x[lane] : Elem<E>::zero();
                 for (int k = bs - 1; k >= 0; --k) {
                     if (lane == k) v = cdiv(v, D[k][k]);
-                    const double vr = __shfl_sync(0xffffffffu, v.re, k), vi = __shfl_sync(0xffffffffu, v.im, k);
-                    if (lane < k) v -= D[lane][k] * mk(vr, vi);
+                    E vk;
+                    vk.re = __shfl_sync(0xffffffffu, v.re, k);
+                    vk.im = __shfl_sync(0xffffffffu, v.im, k);
+                    if (lane < k) v -= D[lane][k] * vk;
                 }
                 if (lane < bs) { x[lane] = v; xb[c * kLuNB + lane] = v; }
             }
             __syncthreads();
             for (int i = threadIdx.x; i < b0; i += blockDim.x) {
-                cplx acc[kLuSolveChunk];
+                E acc[kLuSolveChunk];
 #pragma unroll
-                for (int c = 0; c < kLuSolveChunk; ++c) acc[c] = mk(0.);
+                for (int c = 0; c < kLuSolveChunk; ++c) acc[c] = Elem<E>::zero();
                 for (int k = 0; k < bs; ++k) {
-                    const cplx u = M[i + (long long)(b0 + k) * n];
+                    const E u = M[i + (long long)(b0 + k) * n];
 #pragma unroll
                     for (int c = 0; c < kLuSolveChunk; ++c)
                         if (c < cs) acc[c] += u * xb[c * kLuNB + k];
@@ -288,13 +300,14 @@ __device__ void lu_solve_n(const cplx* M, const int* perm, int n, cplx* X, int s
 
 // Warp-wide dot products sum_{k in [k_lo, k_hi)} conj(a[k]) X[k, c] for the cs
 // columns of a chunk; the sums end up in every lane.
-__device__ __forceinline__ void warp_dots_h(const cplx* a, const cplx* X, int n, int k_lo, int k_hi, int cs,
-                                            cplx (&acc)[kLuSolveChunk]) {
+template <class E>
+__device__ __forceinline__ void warp_dots_h(const E* a, const E* X, int n, int k_lo, int k_hi, int cs,
+                                            E (&acc)[kLuSolveChunk]) {
     const int lane = threadIdx.x & 31;
 #pragma unroll
-    for (int c = 0; c < kLuSolveChunk; ++c) acc[c] = mk(0.);
+    for (int c = 0; c < kLuSolveChunk; ++c) acc[c] = Elem<E>::zero();
     for (int k = k_lo + lane; k < k_hi; k += 32) {
-        const cplx u = conj(a[k]);
+        const E u = conj(a[k]);
 #pragma unroll
         for (int c = 0; c < kLuSolveChunk; ++c)
             if (c < cs) acc[c] += u * X[k + (long long)c * n];
@@ -312,9 +325,10 @@ __device__ __forceinline__ void warp_dots_h(const cplx* a, const cplx* X, int n,
 
 // X <- T^-H X:  T^H = U^H L^H P, so x = P^T L^-H U^-H b.  Left-looking by 32-row
 // blocks (the sums run down columns of U and L, which are contiguous).
-__device__ void lu_solve_h(const cplx* M, const int* perm, int n, cplx* X, int s, cplx* sm) {
-    cplx* buf = sm;
-    cplx (*D)[kLuNB + 1] = reinterpret_cast<cplx (*)[kLuNB + 1]>(sm + n);
+template <class E>
+__device__ void lu_solve_h(const E* M, const int* perm, int n, E* X, int s, E* sm) {
+    E* buf = sm;
+    E (*D)[kLuNB + 1] = reinterpret_cast<E (*)[kLuNB + 1]>(sm + n);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int b0 = 0; b0 < n; b0 += kLuNB) {               // U^H y = b
         const int bs = min(kLuNB, n - b0);
@@ -324,10 +338,10 @@ __device__ void lu_solve_h(const cplx* M, const int* perm, int n, cplx* X, int s
         }
         for (int cb = 0; cb < s; cb += kLuSolveChunk) {
             const int cs = min(kLuSolveChunk, s - cb);
-            cplx* Xc = X + (long long)cb * n;
+            E* Xc = X + (long long)cb * n;
             if (b0 > 0)
                 for (int r = warp; r < bs; r += nw) {
-                    cplx acc[kLuSolveChunk];
+                    E acc[kLuSolveChunk];
                     warp_dots_h(M + (long long)(b0 + r) * n, Xc, n, 0, b0, cs, acc);
                     if (lane == 0)
 #pragma unroll
@@ -336,12 +350,14 @@ __device__ void lu_solve_h(const cplx* M, const int* perm, int n, cplx* X, int s
                 }
             __syncthreads();
             for (int c = warp; c < cs; c += nw) {
-                cplx* x = Xc + (long long)c * n + b0;
-                cplx v = lane < bs ? x[lane] : mk(0.);
+                E* x = Xc + (long long)c * n + b0;
+                E v = lane < bs ? x[lane] : Elem<E>::zero();
                 for (int k = 0; k < bs; ++k) {
                     if (lane == k) v = cdiv(v, conj(D[k][k]));
-                    const double vr = __shfl_sync(0xffffffffu, v.re, k), vi = __shfl_sync(0xffffffffu, v.im, k);
-                    if (lane > k && lane < bs) v -= conj(D[k][lane]) * mk(vr, vi);
+                    E vk;
+                    vk.re = __shfl_sync(0xffffffffu, v.re, k);
+                    vk.im = __shfl_sync(0xffffffffu, v.im, k);
+                    if (lane > k && lane < bs) v -= conj(D[k][lane]) * vk;
                 }
                 if (lane < bs) x[lane] = v;
             }
@@ -356,10 +372,10 @@ __device__ void lu_solve_h(const cplx* M, const int* perm, int n, cplx* X, int s
         }
         for (int cb = 0; cb < s; cb += kLuSolveChunk) {
             const int cs = min(kLuSolveChunk, s - cb);
-            cplx* Xc = X + (long long)cb * n;
+            E* Xc = X + (long long)cb * n;
             if (b0 + bs < n)
                 for (int r = warp; r < bs; r += nw) {
-                    cplx acc[kLuSolveChunk];
+                    E acc[kLuSolveChunk];
                     warp_dots_h(M + (long long)(b0 + r) * n, Xc, n, b0 + bs, n, cs, acc);
                     if (lane == 0)
 #pragma unroll
@@ -368,11 +384,13 @@ __device__ void lu_solve_h(const cplx* M, const int* perm, int n, cplx* X, int s
                 }
             __syncthreads();
             for (int c = warp; c < cs; c += nw) {
-                cplx* x = Xc + (long long)c * n + b0;
-                cplx v = lane < bs ? x[lane] : mk(0.);
+                E* x = Xc + (long long)c * n + b0;
+                E v = lane < bs ? x[lane] : Elem<E>::zero();
                 for (int k = bs - 1; k >= 0; --k) {
-                    const double vr = __shfl_sync(0xffffffffu, v.re, k), vi = __shfl_sync(0xffffffffu, v.im, k);
-                    if (lane < k) v -= conj(D[k][lane]) * mk(vr, vi);
+                    E vk;
+                    vk.re = __shfl_sync(0xffffffffu, v.re, k);
+                    vk.im = __shfl_sync(0xffffffffu, v.im, k);
+                    if (lane < k) v -= conj(D[k][lane]) * vk;
                 }
                 if (lane < bs) x[lane] = v;
             }
@@ -383,29 +401,44 @@ __device__ void lu_solve_h(const cplx* M, const int* perm, int n, cplx* X, int s
 }
 
 // One CTA per matrix: X_m <- T_m^-1 X_m (trans = 0) or T_m^-H X_m (trans = 1).
-__global__ void __launch_bounds__(kLuSolveThreads) k_lu_solve(int n, int s, int trans, const cplx* LU,
-                                                              long long stride, const int* perm, cplx* X,
+// grid (column groups, nmat): CTA (g, m) solves columns [g cpc, g cpc + cpc) of X_m,
+// so that small batches still occupy the GPU (the factors are then re-read from L2).
+template <class E>
+__global__ void __launch_bounds__(kLuSolveThreads) k_lu_solve(int n, int s, int cpc, int trans, const E* LU,
+                                                              long long stride, const int* perm, E* X,
                                                               long long xstride) {
     extern __shared__ double lu_solve_sm[];
-    cplx* sm = reinterpret_cast<cplx*>(lu_solve_sm);
-    const cplx* M = LU + (long long)blockIdx.x * stride;
-    const int* pm = perm + (long long)blockIdx.x * n;
-    cplx* Xm = X + (long long)blockIdx.x * xstride;
-    if (trans) lu_solve_h(M, pm, n, Xm, s, sm);
-    else lu_solve_n(M, pm, n, Xm, s, sm);
+    E* sm = reinterpret_cast<E*>(lu_solve_sm);
+    const int c0 = blockIdx.x * cpc, cs = min(cpc, s - c0);
+    if (cs <= 0) return;
+    const E* M = LU + (long long)blockIdx.y * stride;
+    const int* pm = perm + (long long)blockIdx.y * n;
+    E* Xm = X + (long long)blockIdx.y * xstride + (long long)c0 * n;
+    if (trans) lu_solve_h(M, pm, n, Xm, cs, sm);
+    else lu_solve_n(M, pm, n, Xm, cs, sm);
 }
 
 constexpr size_t kLuSmemLimit = 220 * 1024;
 
-bool lu_solve_supported(int n) { return lu_solve_smem_bytes(n) <= kLuSmemLimit; }
+bool lu_solve_supported(int n) { return lu_solve_smem_bytes(n, sizeof(cplx)) <= kLuSmemLimit; }
+bool lu_solve_supported_f32(int n) { return lu_solve_smem_bytes(n, sizeof(cplxf)) <= kLuSmemLimit; }
 
-cudaError_t lu_perm_from_piv(int n, int nmat, const int* piv, int* perm, cudaStream_t st);
+cudaError_t lu_perm_from_piv(int n, int nmat, const int* piv, int* perm, cudaStream_t st) {
+    if (n < 1 || nmat < 1 || (size_t)n * sizeof(int) > kLuSmemLimit) return cudaErrorInvalidValue;
+    if ((size_t)n * sizeof(int) > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_lu_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLuSmemLimit);
+        if (e != cudaSuccess) return e;
+    }
+    k_lu_perm<<<nmat, 256, (size_t)n * sizeof(int), st>>>(n, piv, perm);
+    return cudaGetLastError();
+}
 
-cudaError_t lu_factor_batched(int n, int nmat, cplx* A, long long stride, int* piv, int* perm, int* info,
-                              cudaStream_t st, long long* launches) {
+template <class E>
+cudaError_t lu_factor_impl(int n, int nmat, E* A, long long stride, int* piv, int* perm, int* info, cudaStream_t st,
+                           long long* launches) {
     if (n < 1 || nmat < 1 || nmat > 65535 || (size_t)n * sizeof(int) > kLuSmemLimit) return cudaErrorInvalidValue;
-    const size_t gemm_smem = 2 * (size_t)kLuNB * kLuTile * sizeof(cplx);
-    cudaError_t e = cudaFuncSetAttribute(k_lu_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem);
+    const size_t gemm_smem = 2 * (size_t)kLuNB * kLuTile * sizeof(E);
+    cudaError_t e = cudaFuncSetAttribute(k_lu_gemm<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem);
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(info, 0, (size_t)nmat * sizeof(int), st);
     if (e != cudaSuccess) return e;
@@ -413,16 +446,16 @@ cudaError_t lu_factor_batched(int n, int nmat, cplx* A, long long stride, int* p
     const int ncb = (n + kLuNB - 1) / kLuNB;
     for (int k0 = 0; k0 < n; k0 += kLuNB) {
         const int nb = min(kLuNB, n - k0);
-        k_lu_panel<<<nmat, kLuPanelThreads, 0, st>>>(n, k0, nb, A, stride, piv, info);
+        k_lu_panel<E><<<nmat, kLuPanelThreads, 0, st>>>(n, k0, nb, A, stride, piv, info);
         ++nl;
         if (ncb > 1) {
-            k_lu_swap_trsm<<<dim3(ncb, nmat), 256, 0, st>>>(n, k0, nb, A, stride, piv);
+            k_lu_swap_trsm<E><<<dim3(ncb, nmat), 256, 0, st>>>(n, k0, nb, A, stride, piv);
             ++nl;
         }
         const int m = n - k0 - nb;
         if (m > 0) {
             const int tiles = (m + kLuTile - 1) / kLuTile;
-            k_lu_gemm<<<dim3(tiles, tiles, nmat), 256, gemm_smem, st>>>(n, k0, nb, A, stride);
+            k_lu_gemm<E><<<dim3(tiles, tiles, nmat), 256, gemm_smem, st>>>(n, k0, nb, A, stride);
             ++nl;
         }
     }
@@ -433,26 +466,36 @@ cudaError_t lu_factor_batched(int n, int nmat, cplx* A, long long stride, int* p
     return cudaGetLastError();
 }
 
+template <class E>
+cudaError_t lu_solve_impl(int n, int nmat, int trans, const E* LU, long long stride, const int* perm, int s, E* X,
+                          long long xstride, cudaStream_t st) {
+    const size_t smem = lu_solve_smem_bytes(n, sizeof(E));
+    if (n < 1 || nmat < 1 || nmat > 65535 || s < 1 || smem > kLuSmemLimit) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(k_lu_solve<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLuSmemLimit);
+    if (e != cudaSuccess) return e;
+    // at least ~2 CTAs per SM of the 152 when the batch is small
+    const int groups = std::max(1, std::min(s, (304 + nmat - 1) / nmat));
+    const int cpc = (s + groups - 1) / groups;
+    const int ng = (s + cpc - 1) / cpc;
+    k_lu_solve<E><<<dim3(ng, nmat), kLuSolveThreads, smem, st>>>(n, s, cpc, trans, LU, stride, perm, X, xstride);
+    return cudaGetLastError();
+}
+
+cudaError_t lu_factor_batched(int n, int nmat, cplx* A, long long stride, int* piv, int* perm, int* info,
+                              cudaStream_t st, long long* launches) {
+    return lu_factor_impl<cplx>(n, nmat, A, stride, piv, perm, info, st, launches);
+}
+cudaError_t lu_factor_batched_f32(int n, int nmat, cplxf* A, long long stride, int* piv, int* perm, int* info,
+                                  cudaStream_t st, long long* launches) {
+    return lu_factor_impl<cplxf>(n, nmat, A, stride, piv, perm, info, st, launches);
+}
 cudaError_t lu_solve_batched(int n, int nmat, int trans, const cplx* LU, long long stride, const int* perm, int s,
                              cplx* X, long long xstride, cudaStream_t st) {
-    if (n < 1 || nmat < 1 || s < 1 || !lu_solve_supported(n)) return cudaErrorInvalidValue;
-    const size_t smem = lu_solve_smem_bytes(n);
-    cudaError_t e = cudaFuncSetAttribute(k_lu_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLuSmemLimit);
-    if (e != cudaSuccess) return e;
-    k_lu_solve<<<nmat, kLuSolveThreads, smem, st>>>(n, s, trans, LU, stride, perm, X, xstride);
-    return cudaGetLastError();
+    return lu_solve_impl<cplx>(n, nmat, trans, LU, stride, perm, s, X, xstride, st);
+}
+cudaError_t lu_solve_batched_f32(int n, int nmat, int trans, const cplxf* LU, long long stride, const int* perm,
+                                 int s, cplxf* X, long long xstride, cudaStream_t st) {
+    return lu_solve_impl<cplxf>(n, nmat, trans, LU, stride, perm, s, X, xstride, st);
 }
 
-}  // namespace hbem
-
-namespace hbem {
-cudaError_t lu_perm_from_piv(int n, int nmat, const int* piv, int* perm, cudaStream_t st) {
-    if (n < 1 || nmat < 1 || (size_t)n * sizeof(int) > kLuSmemLimit) return cudaErrorInvalidValue;
-    if ((size_t)n * sizeof(int) > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_lu_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLuSmemLimit);
-        if (e != cudaSuccess) return e;
-    }
-    k_lu_perm<<<nmat, 256, (size_t)n * sizeof(int), st>>>(n, piv, perm);
-    return cudaGetLastError();
-}
 }  // namespace hbem

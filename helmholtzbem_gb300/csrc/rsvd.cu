@@ -548,26 +548,174 @@ __global__ void k_sv2_out(int n, int nmat, const cplx* sol, const int* mcol, con
     out[3LL * mat + 2] = info[mat] ? CUDART_NAN : -sol[2LL * n * mat + mcol[mat]].re;
 }
 
+#define RS_CK(x)                                \
+    do {                                        \
+        cudaError_t e_ = (x);                   \
+        if (e_ != cudaSuccess) return e_;       \
+    } while (0)
+
+// ------------------------------------------------------------------ mixed precision
+//
+// Complex-FP32 LU; the subspace iterations solve with the FP32 factors alone (an
+// O(eps_32 cond) perturbation of the sketch subspace changes the Ritz value only at
+// second order), while the final T^-H Q and the Ritz-vector solves are refined in
+// FP64: x <- x + LU32^-1 (b - op(T) x), residuals from the FP64 T.
+
+cudaError_t lu_factor_batched_f32(int n, int nmat, cplxf* A, long long stride, int* piv, int* perm, int* info,
+                                  cudaStream_t st, long long* launches);
+cudaError_t lu_solve_batched_f32(int n, int nmat, int trans, const cplxf* LU, long long stride, const int* perm,
+                                 int s, cplxf* X, long long xstride, cudaStream_t st);
+bool lu_solve_supported_f32(int n);
+
+__global__ void k_to_f32(long long len, const cplx* src, long long sstride, cplxf* dst, long long dstride) {
+    const cplx* a = src + (long long)blockIdx.y * sstride;
+    cplxf* b = dst + (long long)blockIdx.y * dstride;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < len; e += (long long)gridDim.x * blockDim.x)
+        b[e] = mkf((float)a[e].re, (float)a[e].im);
+}
+
+// dst = src (overwrite) or dst += src
+__global__ void k_acc_f64(long long len, const cplxf* src, long long sstride, cplx* dst, long long dstride,
+                          int overwrite) {
+    const cplxf* a = src + (long long)blockIdx.y * sstride;
+    cplx* b = dst + (long long)blockIdx.y * dstride;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < len; e += (long long)gridDim.x * blockDim.x) {
+        const cplx v = mk((double)a[e].re, (double)a[e].im);
+        b[e] = overwrite ? v : b[e] + v;
+    }
+}
+
+constexpr int kResChunk = 16;
+
+// Rres = B - T X, one thread per row, grid (ceil(n / 256), nmat)
+__global__ void __launch_bounds__(256) k_resid_n(int n, int s, const cplx* T, long long mat_stride, const cplx* X,
+                                                  long long xs, const cplx* B, long long bs, cplx* Rr, long long rs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const cplx* Tm = T + (long long)blockIdx.y * mat_stride;
+    const cplx* Xm = X + (long long)blockIdx.y * xs;
+    const cplx* Bm = B + (long long)blockIdx.y * bs;
+    cplx* Rm = Rr + (long long)blockIdx.y * rs;
+    for (int cb = 0; cb < s; cb += kResChunk) {
+        const int cs = min(kResChunk, s - cb);
+        cplx acc[kResChunk];
+#pragma unroll
+        for (int c = 0; c < kResChunk; ++c) acc[c] = mk(0.);
+        for (int r = 0; r < n; ++r) {
+            const cplx t = Tm[i + (long long)r * n];
+#pragma unroll
+            for (int c = 0; c < kResChunk; ++c)
+                if (c < cs) acc[c] += t * Xm[r + (long long)(cb + c) * n];
+        }
+#pragma unroll
+        for (int c = 0; c < kResChunk; ++c)
+            if (c < cs) Rm[i + (long long)(cb + c) * n] = Bm[i + (long long)(cb + c) * n] - acc[c];
+    }
+}
+
+// Rres = B - T^H X, one warp per row, grid (ceil(n / 8), nmat), 256 threads
+__global__ void __launch_bounds__(256) k_resid_h(int n, int s, const cplx* T, long long mat_stride, const cplx* X,
+                                                  long long xs, const cplx* B, long long bs, cplx* Rr, long long rs) {
+    const int lane = threadIdx.x & 31, i = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (i >= n) return;
+    const cplx* col = T + (long long)blockIdx.y * mat_stride + (long long)i * n;
+    const cplx* Xm = X + (long long)blockIdx.y * xs;
+    const cplx* Bm = B + (long long)blockIdx.y * bs;
+    cplx* Rm = Rr + (long long)blockIdx.y * rs;
+    for (int cb = 0; cb < s; cb += kResChunk) {
+        const int cs = min(kResChunk, s - cb);
+        cplx acc[kResChunk];
+#pragma unroll
+        for (int c = 0; c < kResChunk; ++c) acc[c] = mk(0.);
+        for (int r = lane; r < n; r += 32) {
+            const cplx t = conj(col[r]);
+#pragma unroll
+            for (int c = 0; c < kResChunk; ++c)
+                if (c < cs) acc[c] += t * Xm[r + (long long)(cb + c) * n];
+        }
+#pragma unroll
+        for (int c = 0; c < kResChunk; ++c) {
+            if (c >= cs) break;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                acc[c].re += __shfl_xor_sync(0xffffffffu, acc[c].re, o);
+                acc[c].im += __shfl_xor_sync(0xffffffffu, acc[c].im, o);
+            }
+            if (lane == 0) Rm[i + (long long)(cb + c) * n] = Bm[i + (long long)(cb + c) * n] - acc[c];
+        }
+    }
+}
+
+struct MixedBufs {
+    const cplxf* LU32;
+    const int* perm;
+    cplx* Bsave;
+    cplx* Rres;
+    cplxf* X32;
+};
+
+static dim3 grid_len(long long len, int nmat) {
+    return dim3((unsigned)std::min<long long>(1024, (len + 255) / 256), (unsigned)nmat);
+}
+
+// X_m <- op(T_m)^-1 X_m for ncol columns (leading dimension n, matrix stride xs):
+// iters = 1 is the plain FP32 solve, each further iteration one FP64 residual and
+// one FP32 correction.
+cudaError_t solve_mixed(int n, int nmat, int trans, const MixedBufs& mb, const cplx* T, long long mat_stride, cplx* X,
+                        int ncol, long long xs, int iters, cudaStream_t st, long long& nl) {
+    const long long len = (long long)n * ncol, nn = (long long)n * n;
+    const dim3 g = grid_len(len, nmat);
+    if (iters > 1) {
+        k_copy_mats<<<g, 256, 0, st>>>((int)len, X, xs, mb.Bsave, len);
+        ++nl;
+    }
+    k_to_f32<<<g, 256, 0, st>>>(len, X, xs, mb.X32, len);
+    RS_CK(lu_solve_batched_f32(n, nmat, trans, mb.LU32, nn, mb.perm, ncol, mb.X32, len, st));
+    k_acc_f64<<<g, 256, 0, st>>>(len, mb.X32, len, X, xs, 1);
+    nl += 3;
+    for (int it = 1; it < iters; ++it) {
+        if (trans)
+            k_resid_h<<<dim3((n + 7) / 8, nmat), 256, 0, st>>>(n, ncol, T, mat_stride, X, xs, mb.Bsave, len, mb.Rres, len);
+        else
+            k_resid_n<<<dim3((n + 255) / 256, nmat), 256, 0, st>>>(n, ncol, T, mat_stride, X, xs, mb.Bsave, len, mb.Rres,
+                                                                  len);
+        k_to_f32<<<g, 256, 0, st>>>(len, mb.Rres, len, mb.X32, len);
+        RS_CK(lu_solve_batched_f32(n, nmat, trans, mb.LU32, nn, mb.perm, ncol, mb.X32, len, st));
+        k_acc_f64<<<g, 256, 0, st>>>(len, mb.X32, len, X, xs, 0);
+        nl += 4;
+    }
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ orchestration
 
 struct RsvdWork {
     cplx *A = nullptr, *X = nullptr, *Y = nullptr, *Rf = nullptr, *uv = nullptr;
     int *piv = nullptr, *perm = nullptr, *info = nullptr;
+    cplxf *A32 = nullptr, *X32 = nullptr;
+    cplx *Bsave = nullptr, *Rres = nullptr;
     cplx *B = nullptr, *ub = nullptr, *ud = nullptr, *rhs = nullptr, *tb = nullptr;
     int *piv2 = nullptr, *perm2 = nullptr, *info2 = nullptr, *mcol = nullptr;
 };
 
 // Carve the workspace (base == nullptr: only count).  Returns the bytes needed.
-size_t rsvd_carve(int n, int nmat, int s, int D, bool small, char* base, RsvdWork& w) {
+size_t rsvd_carve(int n, int nmat, int s, int D, bool small, bool mixed, char* base, RsvdWork& w) {
     size_t off = 0;
     auto take = [&](size_t bytes) -> char* {
         char* p = base ? base + off : nullptr;
         off += (bytes + 255) / 256 * 256;
         return p;
     };
-    const size_t nm = (size_t)nmat, nn = (size_t)n * n, c = sizeof(cplx), ii = sizeof(int);
+    const size_t nm = (size_t)nmat, nn = (size_t)n * n, c = sizeof(cplx), cf = sizeof(cplxf), ii = sizeof(int);
     if (!small) {
-        w.A = (cplx*)take(nm * nn * c);
+        if (mixed) {
+            w.A32 = (cplxf*)take(nm * nn * cf);
+            w.X32 = (cplxf*)take(nm * n * s * cf);
+            w.Bsave = (cplx*)take(nm * n * s * c);
+            w.Rres = (cplx*)take(nm * n * s * c);
+        } else {
+            w.A = (cplx*)take(nm * nn * c);
+        }
         w.piv = (int*)take(nm * n * ii);
         w.perm = (int*)take(nm * n * ii);
         w.info = (int*)take(nm * ii);
@@ -599,59 +747,70 @@ bool rsvd_supported(int n, int s, int D) {
     return true;
 }
 
-size_t rsvd_work_bytes(int n, int nmat, int s, int D) {
+// precision 0: FP64 throughout; 1: complex-FP32 LU with FP64 refinement (matrices
+// that fit one CTA's shared memory always take the FP64 single-kernel path)
+size_t rsvd_work_bytes(int n, int nmat, int s, int D, int precision) {
     RsvdWork w;
-    return rsvd_carve(n, nmat, s, D, rsvd_small_fits(n, s), nullptr, w);
+    return rsvd_carve(n, nmat, s, D, rsvd_small_fits(n, s), precision == 1, nullptr, w);
 }
-
-#define RS_CK(x)                                \
-    do {                                        \
-        cudaError_t e_ = (x);                   \
-        if (e_ != cudaSuccess) return e_;       \
-    } while (0)
 
 // sigma (D = 0), sigma' (D >= 1), sigma'' (D = 2) of nmat matrices of order n;
 // out[(D+1) m + t], status[m] (0 ok, 5 zero pivot in the LU of T).
-cudaError_t rsvd_batched(int n, int nmat, int s, int q, int D, const cplx* T, long long mat_stride,
-                         long long der_stride, const cplx* R, double* out, int* status, void* work,
-                         size_t work_bytes, cudaStream_t st, long long* launches) {
-    if (!rsvd_supported(n, s, D) || D < 0 || D > 2 || nmat < 1 || nmat > 65535) return cudaErrorInvalidValue;
-    const bool small = rsvd_small_fits(n, s);
+cudaError_t rsvd_batched(int n, int nmat, int s, int q, int D, int precision, int refine, const cplx* T,
+                         long long mat_stride, long long der_stride, const cplx* R, double* out, int* status,
+                         void* work, size_t work_bytes, cudaStream_t st, long long* launches) {
+    if (!rsvd_supported(n, s, D) || D < 0 || D > 2 || nmat < 1 || nmat > 65535 || precision < 0 || precision > 1 ||
+        refine < 1 || refine > 16)
+        return cudaErrorInvalidValue;
+    const bool small = rsvd_small_fits(n, s), mixed = precision == 1 && !small;
     RsvdWork w;
-    if (rsvd_carve(n, nmat, s, D, small, nullptr, w) > work_bytes) return cudaErrorInvalidValue;
-    rsvd_carve(n, nmat, s, D, small, static_cast<char*>(work), w);
+    if (rsvd_carve(n, nmat, s, D, small, mixed, nullptr, w) > work_bytes) return cudaErrorInvalidValue;
+    rsvd_carve(n, nmat, s, D, small, mixed, static_cast<char*>(work), w);
     long long nl = 0;
     if (small) {
         RS_CK(launch_rsvd_small(n, nmat, s, q, D, T, mat_stride, der_stride, R, out, status, w.uv, st));
         ++nl;
     } else {
         const long long nn = (long long)n * n, ns = (long long)n * s;
-        const int cb = (int)std::min<long long>(1024, (nn + 255) / 256);
-        k_copy_mats<<<dim3(cb, nmat), 256, 0, st>>>((int)nn, T, mat_stride, w.A, nn);
-        RS_CK(lu_factor_batched(n, nmat, w.A, nn, w.piv, w.perm, w.info, st, &nl));
-        k_copy_mats<<<dim3((int)std::min<long long>(1024, (ns + 255) / 256), nmat), 256, 0, st>>>((int)ns, R, 0, w.X, ns);
-        RS_CK(lu_solve_batched(n, nmat, 0, w.A, nn, w.perm, s, w.X, ns, st));
+        const MixedBufs mb{w.A32, w.perm, w.Bsave, w.Rres, w.X32};
+        // op(T)^-1 on ncol columns: FP64 factors, or FP32 factors with `iters` refinement passes
+        auto solve = [&](int trans, cplx* X, int ncol, long long xs, int iters) -> cudaError_t {
+            if (!mixed) {
+                ++nl;
+                return lu_solve_batched(n, nmat, trans, w.A, nn, w.perm, ncol, X, xs, st);
+            }
+            return solve_mixed(n, nmat, trans, mb, T, mat_stride, X, ncol, xs, iters, st, nl);
+        };
+        if (mixed) {
+            k_to_f32<<<grid_len(nn, nmat), 256, 0, st>>>(nn, T, mat_stride, w.A32, nn);
+            RS_CK(lu_factor_batched_f32(n, nmat, w.A32, nn, w.piv, w.perm, w.info, st, &nl));
+        } else {
+            k_copy_mats<<<grid_len(nn, nmat), 256, 0, st>>>((int)nn, T, mat_stride, w.A, nn);
+            RS_CK(lu_factor_batched(n, nmat, w.A, nn, w.piv, w.perm, w.info, st, &nl));
+        }
+        k_copy_mats<<<grid_len(ns, nmat), 256, 0, st>>>((int)ns, R, 0, w.X, ns);
+        nl += 2;
+        RS_CK(solve(0, w.X, s, ns, 1));
         k_qr_global<<<nmat, kRsvdThreads, 0, st>>>(n, s, w.X, ns, nullptr);
-        nl += 4;
+        ++nl;
         for (int it = 0; it < q; ++it) {
-            RS_CK(lu_solve_batched(n, nmat, 1, w.A, nn, w.perm, s, w.X, ns, st));
+            RS_CK(solve(1, w.X, s, ns, 1));
             k_qr_global<<<nmat, kRsvdThreads, 0, st>>>(n, s, w.X, ns, nullptr);
-            RS_CK(lu_solve_batched(n, nmat, 0, w.A, nn, w.perm, s, w.X, ns, st));
+            RS_CK(solve(0, w.X, s, ns, 1));
             k_qr_global<<<nmat, kRsvdThreads, 0, st>>>(n, s, w.X, ns, nullptr);
-            nl += 4;
+            nl += 2;
         }
         RS_CK(cudaMemcpyAsync(w.Y, w.X, (size_t)nmat * ns * sizeof(cplx), cudaMemcpyDeviceToDevice, st));
-        RS_CK(lu_solve_batched(n, nmat, 1, w.A, nn, w.perm, s, w.Y, ns, st));
+        RS_CK(solve(1, w.Y, s, ns, refine));
         k_qr_global<<<nmat, kRsvdThreads, 0, st>>>(n, s, w.Y, ns, w.Rf);
         k_rsvd_tail<<<nmat, kRsvdThreads, 0, st>>>(n, s, D, w.X, w.Y, ns, w.Rf, T, mat_stride, der_stride, w.info,
                                                     out, status, w.uv);
-        nl += 3;
+        nl += 2;
         RS_CK(cudaGetLastError());
         if (D >= 1)
             for (int it = 0; it < kRitzRefine; ++it) {
-                RS_CK(lu_solve_batched(n, nmat, 1, w.A, nn, w.perm, 1, w.uv + n, 2LL * n, st));
-                RS_CK(lu_solve_batched(n, nmat, 0, w.A, nn, w.perm, 1, w.uv + n, 2LL * n, st));
-                nl += 2;
+                RS_CK(solve(1, w.uv + n, 1, 2LL * n, refine));
+                RS_CK(solve(0, w.uv + n, 1, 2LL * n, refine));
             }
     }
     if (D >= 1) {
@@ -663,8 +822,7 @@ cudaError_t rsvd_batched(int n, int nmat, int s, int q, int D, const cplx* T, lo
         const int n2 = 2 * n;
         const long long nn2 = (long long)n2 * n2;
         k_sv2_prep<<<nmat, 256, 0, st>>>(n, w.uv, w.ub, w.mcol);
-        k_build_bordered<<<dim3((int)std::min<long long>(1024, (nn2 + 255) / 256), nmat), 256, 0, st>>>(
-            n, T, mat_stride, out, 3, w.ub, w.mcol, w.B);
+        k_build_bordered<<<grid_len(nn2, nmat), 256, 0, st>>>(n, T, mat_stride, out, 3, w.ub, w.mcol, w.B);
         RS_CK(lu_factor_batched(n2, nmat, w.B, nn2, w.piv2, w.perm2, w.info2, st, &nl));
         k_wapply<<<nmat, 256, 0, st>>>(n, T + der_stride, mat_stride, w.ub, w.ud, -1., 0);
         RS_CK(lu_solve_batched(n2, nmat, 0, w.B, nn2, w.perm2, 1, w.ud, n2, st));

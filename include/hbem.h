@@ -162,6 +162,14 @@ int hbem_rsvd_sv_batch(int n, int nmat, unsigned d, const double* T_host, const 
                        double* out_host);
 int hbem_rsvd_sv_batch_device(int n, int nmat, unsigned d, const void* T_dev, long long mat_stride,
                               long long der_stride, const void* R_dev, int s, int q, double* out_host);
+/* The same with a precision choice for the global-memory path: precision 0 = FP64
+ * LU and solves; 1 = complex-FP32 LU (FP32 trailing updates), FP32 solves in the
+ * subspace iterations, and `refine` passes (>= 1; 1 = none) of FP64-residual
+ * iterative refinement for the final T^-H Q and the Ritz-vector solves.  Matrices
+ * on the shared-memory path are computed in FP64 whatever the choice.            */
+int hbem_rsvd_sv_batch_device_ex(int n, int nmat, unsigned d, const void* T_dev, long long mat_stride,
+                                 long long der_stride, const void* R_dev, int s, int q, int precision, int refine,
+                                 double* out_host);
 
 /* Batched LU with partial pivoting, in place (Eigen::PartialPivLU<MatrixXcd> at
  * source/utilities/randsvd.cpp:104,205): nmat column-major complex128 matrices of

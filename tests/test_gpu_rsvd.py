@@ -93,3 +93,34 @@ def test_rsvd_batched_scatterer_size():
         assert _rel(g, ref) < 1e-10
     dense = np.linalg.svd(mats[1][0], compute_uv=False).min()
     assert got[1] >= dense * (1 - 1e-12) and (got[1] - dense) / dense < 1e-6
+
+
+def _rsvd_device(mats, R, q, d, precision, refine):
+    """hbem_rsvd_sv_batch_device_ex on device copies of [T, T', ...] (column-major)."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    from helmholtzbem_gb300 import _capi as C
+    nmat, n = len(mats), mats[0][0].shape[0]
+    buf = np.stack([np.stack([np.asarray(m[t]).T for t in range(d + 1)]) for m in mats]).astype(np.complex128)
+    Td = torch.from_numpy(np.ascontiguousarray(buf)).cuda()
+    Rd = torch.from_numpy(np.ascontiguousarray(np.asarray(R, np.complex128).T)).cuda()
+    out = np.zeros((nmat, d + 1))
+    C.check(C.lib().hbem_rsvd_sv_batch_device_ex(n, nmat, d, ctypes.c_void_p(Td.data_ptr()), (d + 1) * n * n, n * n,
+                                                 ctypes.c_void_p(Rd.data_ptr()), R.shape[1], q, precision, refine,
+                                                 C.dptr(out)))
+    return out
+
+
+def test_rsvd_mixed_precision_matches_fp64():
+    """Complex-FP32 LU + FP64 refinement against the FP64 path on the same sketch:
+    n = 160 with sigma', sigma'' (bordered system in FP64), and the relative error of
+    each result reported by the assertion."""
+    mats = _mats([1.7, 3.9, 5.2], npan=80, order=7, d=2)
+    n = mats[0][0].shape[0]
+    R = O.rand_sketch(n, 12, seed=5)
+    ref = _rsvd_device(mats, R, 2, 2, 0, 1)
+    for refine in (3, 4):
+        got = _rsvd_device(mats, R, 2, 2, 1, refine)
+        assert np.max(np.abs(got[:, 0] - ref[:, 0]) / ref[:, 0]) < 1e-10
+        assert np.max(np.abs(got[:, 1] - ref[:, 1]) / np.maximum(np.abs(ref[:, 1]), 1e-2)) < 1e-8
+        assert np.max(np.abs(got[:, 2] - ref[:, 2]) / np.maximum(np.abs(ref[:, 2]), 1e-1)) < 1e-7

@@ -23,23 +23,36 @@ constexpr int kLuTile = 64;
 constexpr int kLuSolveThreads = 512;
 constexpr int kLuSolveChunk = 16;      // right-hand sides held in registers at a time
 
-template <class E>
+// Unblocked LU of the panel rows [k0, n) x columns [k0, k0 + nb).  STAGED: the
+// panel is copied to shared memory (column-major, leading dimension n - k0), factored
+// there and written back; otherwise it is factored in place in global memory (L2).
+template <class E, bool STAGED>
 __global__ void __launch_bounds__(kLuPanelThreads) k_lu_panel(int n, int k0, int nb, E* A, long long stride,
                                                               int* piv, int* info) {
+    extern __shared__ double panel_sm[];
+    E* P = reinterpret_cast<E*>(panel_sm);
     E* M = A + (long long)blockIdx.x * stride;
     int* pv = piv + (long long)blockIdx.x * n;
+    const int m = n - k0;
     __shared__ double rv[32];
     __shared__ int ri[32];
     __shared__ E prow[kLuNB];
     __shared__ int s_p;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    // element (row i, panel column cc)
+    auto at = [&](int i, int cc) -> E& {
+        return STAGED ? P[(i - k0) + cc * m] : M[i + (long long)(k0 + cc) * n];
+    };
+    if (STAGED) {
+        for (int e = threadIdx.x; e < m * nb; e += blockDim.x) P[e] = M[(k0 + e % m) + (long long)(k0 + e / m) * n];
+        __syncthreads();
+    }
     for (int j = 0; j < nb; ++j) {
         const int c = k0 + j;
-        E* col = M + (long long)c * n;
         double best = -1.;
         int bi = c;
         for (int i = c + threadIdx.x; i < n; i += blockDim.x) {
-            const double a = norm2(col[i]);
+            const double a = norm2(at(i, j));
             if (a > best) { best = a; bi = i; }
         }
 #pragma unroll
@@ -62,9 +75,10 @@ __global__ void __launch_bounds__(kLuPanelThreads) k_lu_panel(int n, int k0, int
         __syncthreads();
         const int p = s_p;
         if (threadIdx.x < nb) {
-            E* a = M + (long long)(k0 + threadIdx.x) * n;
-            const E x = a[c], y = a[p];
-            if (p != c) { a[c] = y; a[p] = x; }
+            E& xa = at(c, threadIdx.x);
+            E& ya = at(p, threadIdx.x);
+            const E x = xa, y = ya;
+            if (p != c) { xa = y; ya = x; }
             prow[threadIdx.x] = (p != c) ? y : x;
         }
         __syncthreads();
@@ -72,15 +86,14 @@ __global__ void __launch_bounds__(kLuPanelThreads) k_lu_panel(int n, int k0, int
         const bool nz = norm2(d) > 0;
         const E id = nz ? cdiv(Elem<E>::one(), d) : Elem<E>::zero();
         for (int i = c + 1 + threadIdx.x; i < n; i += blockDim.x) {
-            E l = col[i];
-            if (nz) { l = l * id; col[i] = l; }
-            for (int cc = j + 1; cc < nb; ++cc) {
-                E* a = M + (long long)(k0 + cc) * n;
-                a[i] -= l * prow[cc];
-            }
+            E l = at(i, j);
+            if (nz) { l = l * id; at(i, j) = l; }
+            for (int cc = j + 1; cc < nb; ++cc) at(i, cc) -= l * prow[cc];
         }
         __syncthreads();
     }
+    if (STAGED)
+        for (int e = threadIdx.x; e < m * nb; e += blockDim.x) M[(k0 + e % m) + (long long)(k0 + e / m) * n] = P[e];
 }
 
 // grid (ceil(n/32), nmat): column block b covers columns [32 b, 32 b + 32).
@@ -212,11 +225,11 @@ __device__ void permute_rows(E* X, int n, int s, const int* perm, E* buf, bool i
 }
 
 // X <- T^-1 X (s columns), P T = L U stored in M.  Right-looking by 32-row blocks.
-template <class E>
+template <class E, int CH>
 __device__ void lu_solve_n(const E* M, const int* perm, int n, E* X, int s, E* sm) {
     E* buf = sm;
     E (*D)[kLuNB + 1] = reinterpret_cast<E (*)[kLuNB + 1]>(sm + n);
-    E* xb = sm + n + kLuNB * (kLuNB + 1);            // [c][k], kLuSolveChunk x 32
+    E* xb = sm + n + kLuNB * (kLuNB + 1);            // [c][k], CH x 32
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     permute_rows(X, n, s, perm, buf, false);
     for (int b0 = 0; b0 < n; b0 += kLuNB) {
@@ -226,8 +239,8 @@ __device__ void lu_solve_n(const E* M, const int* perm, int n, E* X, int s, E* s
             D[r][k] = M[(b0 + r) + (long long)(b0 + k) * n];
         }
         __syncthreads();
-        for (int cb = 0; cb < s; cb += kLuSolveChunk) {
-            const int cs = min(kLuSolveChunk, s - cb);
+        for (int cb = 0; cb < s; cb += CH) {
+            const int cs = min(CH, s - cb);
             for (int c = warp; c < cs; c += nw) {
                 E* x = X + (long long)(cb + c) * n + b0;
                 E v = lane < bs ? x[lane] : Elem<E>::zero();
@@ -241,17 +254,17 @@ __device__ void lu_solve_n(const E* M, const int* perm, int n, E* X, int s, E* s
             }
             __syncthreads();
             for (int i = b0 + bs + threadIdx.x; i < n; i += blockDim.x) {
-                E acc[kLuSolveChunk];
+                E acc[CH];
 #pragma unroll
-                for (int c = 0; c < kLuSolveChunk; ++c) acc[c] = Elem<E>::zero();
+                for (int c = 0; c < CH; ++c) acc[c] = Elem<E>::zero();
                 for (int k = 0; k < bs; ++k) {
                     const E l = M[i + (long long)(b0 + k) * n];
 #pragma unroll
-                    for (int c = 0; c < kLuSolveChunk; ++c)
+                    for (int c = 0; c < CH; ++c)
                         if (c < cs) acc[c] += l * xb[c * kLuNB + k];
                 }
 #pragma unroll
-                for (int c = 0; c < kLuSolveChunk; ++c)
+                for (int c = 0; c < CH; ++c)
                     if (c < cs) X[i + (long long)(cb + c) * n] -= acc[c];
             }
             __syncthreads();
@@ -264,8 +277,8 @@ __device__ void lu_solve_n(const E* M, const int* perm, int n, E* X, int s, E* s
             D[r][k] = M[(b0 + r) + (long long)(b0 + k) * n];
         }
         __syncthreads();
-        for (int cb = 0; cb < s; cb += kLuSolveChunk) {
-            const int cs = min(kLuSolveChunk, s - cb);
+        for (int cb = 0; cb < s; cb += CH) {
+            const int cs = min(CH, s - cb);
             for (int c = warp; c < cs; c += nw) {
                 E* x = X + (long long)(cb + c) * n + b0;
                 E v = lane < bs ? x[lane] : Elem<E>::zero();
@@ -280,17 +293,17 @@ __device__ void lu_solve_n(const E* M, const int* perm, int n, E* X, int s, E* s
             }
             __syncthreads();
             for (int i = threadIdx.x; i < b0; i += blockDim.x) {
-                E acc[kLuSolveChunk];
+                E acc[CH];
 #pragma unroll
-                for (int c = 0; c < kLuSolveChunk; ++c) acc[c] = Elem<E>::zero();
+                for (int c = 0; c < CH; ++c) acc[c] = Elem<E>::zero();
                 for (int k = 0; k < bs; ++k) {
                     const E u = M[i + (long long)(b0 + k) * n];
 #pragma unroll
-                    for (int c = 0; c < kLuSolveChunk; ++c)
+                    for (int c = 0; c < CH; ++c)
                         if (c < cs) acc[c] += u * xb[c * kLuNB + k];
                 }
 #pragma unroll
-                for (int c = 0; c < kLuSolveChunk; ++c)
+                for (int c = 0; c < CH; ++c)
                     if (c < cs) X[i + (long long)(cb + c) * n] -= acc[c];
             }
             __syncthreads();
@@ -300,20 +313,20 @@ __device__ void lu_solve_n(const E* M, const int* perm, int n, E* X, int s, E* s
 
 // Warp-wide dot products sum_{k in [k_lo, k_hi)} conj(a[k]) X[k, c] for the cs
 // columns of a chunk; the sums end up in every lane.
-template <class E>
+template <class E, int CH>
 __device__ __forceinline__ void warp_dots_h(const E* a, const E* X, int n, int k_lo, int k_hi, int cs,
-                                            E (&acc)[kLuSolveChunk]) {
+                                            E (&acc)[CH]) {
     const int lane = threadIdx.x & 31;
 #pragma unroll
-    for (int c = 0; c < kLuSolveChunk; ++c) acc[c] = Elem<E>::zero();
+    for (int c = 0; c < CH; ++c) acc[c] = Elem<E>::zero();
     for (int k = k_lo + lane; k < k_hi; k += 32) {
         const E u = conj(a[k]);
 #pragma unroll
-        for (int c = 0; c < kLuSolveChunk; ++c)
+        for (int c = 0; c < CH; ++c)
             if (c < cs) acc[c] += u * X[k + (long long)c * n];
     }
 #pragma unroll
-    for (int c = 0; c < kLuSolveChunk; ++c) {
+    for (int c = 0; c < CH; ++c) {
         if (c >= cs) break;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -325,7 +338,7 @@ __device__ __forceinline__ void warp_dots_h(const E* a, const E* X, int n, int k
 
 // X <- T^-H X:  T^H = U^H L^H P, so x = P^T L^-H U^-H b.  Left-looking by 32-row
 // blocks (the sums run down columns of U and L, which are contiguous).
-template <class E>
+template <class E, int CH>
 __device__ void lu_solve_h(const E* M, const int* perm, int n, E* X, int s, E* sm) {
     E* buf = sm;
     E (*D)[kLuNB + 1] = reinterpret_cast<E (*)[kLuNB + 1]>(sm + n);
@@ -336,16 +349,16 @@ __device__ void lu_solve_h(const E* M, const int* perm, int n, E* X, int s, E* s
             const int r = e % bs, k = e / bs;
             D[r][k] = M[(b0 + r) + (long long)(b0 + k) * n];
         }
-        for (int cb = 0; cb < s; cb += kLuSolveChunk) {
-            const int cs = min(kLuSolveChunk, s - cb);
+        for (int cb = 0; cb < s; cb += CH) {
+            const int cs = min(CH, s - cb);
             E* Xc = X + (long long)cb * n;
             if (b0 > 0)
                 for (int r = warp; r < bs; r += nw) {
-                    E acc[kLuSolveChunk];
-                    warp_dots_h(M + (long long)(b0 + r) * n, Xc, n, 0, b0, cs, acc);
+                    E acc[CH];
+                    warp_dots_h<E, CH>(M + (long long)(b0 + r) * n, Xc, n, 0, b0, cs, acc);
                     if (lane == 0)
 #pragma unroll
-                        for (int c = 0; c < kLuSolveChunk; ++c)
+                        for (int c = 0; c < CH; ++c)
                             if (c < cs) Xc[b0 + r + (long long)c * n] -= acc[c];
                 }
             __syncthreads();
@@ -370,16 +383,16 @@ __device__ void lu_solve_h(const E* M, const int* perm, int n, E* X, int s, E* s
             const int r = e % bs, k = e / bs;
             D[r][k] = M[(b0 + r) + (long long)(b0 + k) * n];
         }
-        for (int cb = 0; cb < s; cb += kLuSolveChunk) {
-            const int cs = min(kLuSolveChunk, s - cb);
+        for (int cb = 0; cb < s; cb += CH) {
+            const int cs = min(CH, s - cb);
             E* Xc = X + (long long)cb * n;
             if (b0 + bs < n)
                 for (int r = warp; r < bs; r += nw) {
-                    E acc[kLuSolveChunk];
-                    warp_dots_h(M + (long long)(b0 + r) * n, Xc, n, b0 + bs, n, cs, acc);
+                    E acc[CH];
+                    warp_dots_h<E, CH>(M + (long long)(b0 + r) * n, Xc, n, b0 + bs, n, cs, acc);
                     if (lane == 0)
 #pragma unroll
-                        for (int c = 0; c < kLuSolveChunk; ++c)
+                        for (int c = 0; c < CH; ++c)
                             if (c < cs) Xc[b0 + r + (long long)c * n] -= acc[c];
                 }
             __syncthreads();
@@ -403,7 +416,7 @@ __device__ void lu_solve_h(const E* M, const int* perm, int n, E* X, int s, E* s
 // One CTA per matrix: X_m <- T_m^-1 X_m (trans = 0) or T_m^-H X_m (trans = 1).
 // grid (column groups, nmat): CTA (g, m) solves columns [g cpc, g cpc + cpc) of X_m,
 // so that small batches still occupy the GPU (the factors are then re-read from L2).
-template <class E>
+template <class E, int CH>
 __global__ void __launch_bounds__(kLuSolveThreads) k_lu_solve(int n, int s, int cpc, int trans, const E* LU,
                                                               long long stride, const int* perm, E* X,
                                                               long long xstride) {
@@ -414,8 +427,8 @@ __global__ void __launch_bounds__(kLuSolveThreads) k_lu_solve(int n, int s, int 
     const E* M = LU + (long long)blockIdx.y * stride;
     const int* pm = perm + (long long)blockIdx.y * n;
     E* Xm = X + (long long)blockIdx.y * xstride + (long long)c0 * n;
-    if (trans) lu_solve_h(M, pm, n, Xm, cs, sm);
-    else lu_solve_n(M, pm, n, Xm, cs, sm);
+    if (trans) lu_solve_h<E, CH>(M, pm, n, Xm, cs, sm);
+    else lu_solve_n<E, CH>(M, pm, n, Xm, cs, sm);
 }
 
 constexpr size_t kLuSmemLimit = 220 * 1024;
@@ -440,13 +453,19 @@ cudaError_t lu_factor_impl(int n, int nmat, E* A, long long stride, int* piv, in
     const size_t gemm_smem = 2 * (size_t)kLuNB * kLuTile * sizeof(E);
     cudaError_t e = cudaFuncSetAttribute(k_lu_gemm<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem);
     if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_lu_panel<E, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLuSmemLimit);
+    if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(info, 0, (size_t)nmat * sizeof(int), st);
     if (e != cudaSuccess) return e;
     long long nl = 0;
     const int ncb = (n + kLuNB - 1) / kLuNB;
     for (int k0 = 0; k0 < n; k0 += kLuNB) {
         const int nb = min(kLuNB, n - k0);
-        k_lu_panel<E><<<nmat, kLuPanelThreads, 0, st>>>(n, k0, nb, A, stride, piv, info);
+        const size_t psm = (size_t)(n - k0) * nb * sizeof(E);
+        if (psm <= kLuSmemLimit)
+            k_lu_panel<E, true><<<nmat, kLuPanelThreads, psm, st>>>(n, k0, nb, A, stride, piv, info);
+        else
+            k_lu_panel<E, false><<<nmat, kLuPanelThreads, 0, st>>>(n, k0, nb, A, stride, piv, info);
         ++nl;
         if (ncb > 1) {
             k_lu_swap_trsm<E><<<dim3(ncb, nmat), 256, 0, st>>>(n, k0, nb, A, stride, piv);
@@ -471,13 +490,29 @@ cudaError_t lu_solve_impl(int n, int nmat, int trans, const E* LU, long long str
                           long long xstride, cudaStream_t st) {
     const size_t smem = lu_solve_smem_bytes(n, sizeof(E));
     if (n < 1 || nmat < 1 || nmat > 65535 || s < 1 || smem > kLuSmemLimit) return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(k_lu_solve<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLuSmemLimit);
-    if (e != cudaSuccess) return e;
-    // at least ~2 CTAs per SM of the 152 when the batch is small
-    const int groups = std::max(1, std::min(s, (304 + nmat - 1) / nmat));
-    const int cpc = (s + groups - 1) / groups;
+    // columns per CTA: a power of two <= 16 (the register chunk is exactly that wide,
+    // so no lane computes for absent columns), the widest that still gives about two
+    // CTAs per SM of the 152, which re-reads the factors least
+    int cpc = 16;
+    while (cpc > 1 && (long long)nmat * ((s + cpc - 1) / cpc) < 304) cpc >>= 1;
+    while (cpc > 1 && cpc / 2 >= s) cpc >>= 1;
     const int ng = (s + cpc - 1) / cpc;
-    k_lu_solve<E><<<dim3(ng, nmat), kLuSolveThreads, smem, st>>>(n, s, cpc, trans, LU, stride, perm, X, xstride);
+    const dim3 grid(ng, nmat);
+    cudaError_t e = cudaSuccess;
+    switch (cpc) {
+#define HB_SOLVE_CASE(CHV)                                                                                       \
+    case CHV:                                                                                                    \
+        e = cudaFuncSetAttribute(k_lu_solve<E, CHV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLuSmemLimit); \
+        if (e != cudaSuccess) return e;                                                                          \
+        k_lu_solve<E, CHV><<<grid, kLuSolveThreads, smem, st>>>(n, s, cpc, trans, LU, stride, perm, X, xstride); \
+        break;
+        HB_SOLVE_CASE(1)
+        HB_SOLVE_CASE(2)
+        HB_SOLVE_CASE(4)
+        HB_SOLVE_CASE(8)
+        HB_SOLVE_CASE(16)
+#undef HB_SOLVE_CASE
+    }
     return cudaGetLastError();
 }
 

@@ -93,6 +93,10 @@ def test_rsvd_batched_scatterer_size():
         assert _rel(g, ref) < 1e-10
     dense = np.linalg.svd(mats[1][0], compute_uv=False).min()
     assert got[1] >= dense * (1 - 1e-12) and (got[1] - dense) / dense < 1e-6
+    # complex-FP32 LU (panels of more than 880 rows factored in global memory) with
+    # FP64 refinement: the same sigma to 1e-9
+    mixed = _rsvd_device(mats, R, 2, 0, 1, 3)[:, 0]
+    assert np.max(np.abs(mixed - got) / got) < 1e-9
 
 
 def _rsvd_device(mats, R, q, d, precision, refine):

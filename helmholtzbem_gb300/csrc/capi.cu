@@ -38,6 +38,7 @@ cudaError_t lu_solve_batched(int n, int nmat, int trans, const cplx* LU, long lo
                              cplx* X, long long xstride, cudaStream_t st);
 cudaError_t lu_perm_from_piv(int n, int nmat, const int* piv, int* perm, cudaStream_t st);
 bool lu_solve_supported(int n);
+void lu_set_cluster_panels(int on);
 }  // namespace hbem
 
 using namespace hbem;
@@ -304,6 +305,16 @@ int hbem_set_device(int device) {
     HB_CK(cudaSetDevice(device));
     g_device = device;
     return HBEM_OK;
+}
+
+int hbem_set_option(const char* name, int value) {
+    if (!name) return fail(HBEM_ERR_INVALID, "set_option: no name");
+    const std::string k(name);
+    if (k == "lu_cluster_panels") {
+        lu_set_cluster_panels(value);
+        return HBEM_OK;
+    }
+    return fail(HBEM_ERR_INVALID, "set_option: unknown option " + k);
 }
 
 int hbem_hankel01(int n, const double* z_host, int complex_arg, double* h0_host, double* h1_host) {

@@ -11,9 +11,13 @@
 // Matrices are column-major with leading dimension n (Eigen's layout); matrix m
 // starts at A + m * stride.  piv[m*n + k] = row exchanged with row k at step k
 // (LAPACK's ipiv, 0-based); perm[m*n + i] = source row of row i of P A.
+#include <cooperative_groups.h>
+
 #include <algorithm>
 
 #include "hbem_device.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace hbem {
 
@@ -94,6 +98,105 @@ __global__ void __launch_bounds__(kLuPanelThreads) k_lu_panel(int n, int k0, int
     }
     if (STAGED)
         for (int e = threadIdx.x; e < m * nb; e += blockDim.x) M[(k0 + e % m) + (long long)(k0 + e / m) * n] = P[e];
+}
+
+// Panels too tall for one CTA's shared memory: a cluster of CS CTAs per matrix (grid
+// nmat * CS), CTA r holding panel rows [k0 + r R, k0 + (r + 1) R) in its shared memory
+// (column-major, leading dimension R).  Per column: every CTA posts its pivot
+// candidate, all read all candidates through distributed shared memory (cluster
+// barrier 1), every CTA copies the pivot row, the owner of the pivot row copies the
+// row it will receive (barrier 2), the two owners write the exchanged rows, and each
+// CTA applies the rank-1 update to its own rows.
+template <class E>
+__global__ void __launch_bounds__(kLuPanelThreads) k_lu_panel_cluster(int n, int k0, int nb, int R, E* A,
+                                                                      long long stride, int* piv, int* info) {
+    cg::cluster_group cl = cg::this_cluster();
+    const int ncta = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+    const int mat = blockIdx.x / ncta;
+    extern __shared__ double panel_sm[];
+    E* P = reinterpret_cast<E*>(panel_sm);
+    __shared__ double cand_v;
+    __shared__ int cand_i;
+    __shared__ double rv[32];
+    __shared__ int ri[32];
+    __shared__ E prow[kLuNB], tmp[kLuNB];
+    __shared__ int s_p;
+    E* M = A + (long long)mat * stride;
+    int* pv = piv + (long long)mat * n;
+    const int r0 = k0 + rank * R, r1 = min(n, r0 + R), rows = max(0, r1 - r0);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int e = threadIdx.x; e < rows * nb; e += blockDim.x)
+        P[(e % rows) + (e / rows) * R] = M[(r0 + e % rows) + (long long)(k0 + e / rows) * n];
+    __syncthreads();
+    for (int j = 0; j < nb; ++j) {
+        const int c = k0 + j;
+        double best = -1.;
+        int bi = n;
+        for (int i = max(c, r0) + threadIdx.x; i < r1; i += blockDim.x) {
+            const double a = norm2(P[(i - r0) + j * R]);
+            if (a > best) { best = a; bi = i; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        if (lane == 0) { rv[warp] = best; ri[warp] = bi; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double b = rv[0];
+            int p = ri[0];
+            for (int w = 1; w < nw; ++w)
+                if (rv[w] > b || (rv[w] == b && ri[w] < p)) { b = rv[w]; p = ri[w]; }
+            cand_v = b;
+            cand_i = p;
+        }
+        cl.sync();                                                   // (1) candidates posted
+        if (threadIdx.x == 0) {
+            double b = -1.;
+            int p = n;
+            for (int q = 0; q < ncta; ++q) {
+                const double v = *cl.map_shared_rank(&cand_v, q);
+                const int i = *cl.map_shared_rank(&cand_i, q);
+                if (v > b || (v == b && i < p)) { b = v; p = i; }
+            }
+            s_p = p;
+            if (rank == 0) {
+                pv[c] = p;
+                if (b == 0. && info[mat] == 0) info[mat] = c + 1;
+            }
+        }
+        __syncthreads();
+        const int p = s_p;
+        const int rp = (p - k0) / R, rc = (c - k0) / R;
+        if (threadIdx.x < nb) {
+            const E* Pp = cl.map_shared_rank(P, rp);
+            prow[threadIdx.x] = Pp[(p - (k0 + rp * R)) + threadIdx.x * R];
+            if (rank == rp && p != c) {
+                const E* Pc = cl.map_shared_rank(P, rc);
+                tmp[threadIdx.x] = Pc[(c - (k0 + rc * R)) + threadIdx.x * R];
+            }
+        }
+        cl.sync();                                                   // (2) rows c and p read
+        if (threadIdx.x < nb && p != c) {
+            if (rank == rc) P[(c - r0) + threadIdx.x * R] = prow[threadIdx.x];
+            if (rank == rp) P[(p - r0) + threadIdx.x * R] = tmp[threadIdx.x];
+        }
+        __syncthreads();
+        const E d = prow[j];
+        const bool nz = norm2(d) > 0;
+        const E id = nz ? cdiv(Elem<E>::one(), d) : Elem<E>::zero();
+        for (int i = max(c + 1, r0) + threadIdx.x; i < r1; i += blockDim.x) {
+            E l = P[(i - r0) + j * R];
+            if (nz) { l = l * id; P[(i - r0) + j * R] = l; }
+            for (int cc = j + 1; cc < nb; ++cc) P[(i - r0) + cc * R] -= l * prow[cc];
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < rows * nb; e += blockDim.x)
+        M[(r0 + e % rows) + (long long)(k0 + e / rows) * n] = P[(e % rows) + (e / rows) * R];
+    cl.sync();   // no CTA leaves while another may still read its shared memory
 }
 
 // grid (ceil(n/32), nmat): column block b covers columns [32 b, 32 b + 32).
@@ -446,6 +549,63 @@ cudaError_t lu_perm_from_piv(int n, int nmat, const int* piv, int* perm, cudaStr
     return cudaGetLastError();
 }
 
+constexpr size_t kPanelClusterSmem = 200 * 1024;
+int g_lu_cluster_panels = 1;   // 0: tall panels in global memory (kept for comparison tests)
+
+void lu_set_cluster_panels(int on) { g_lu_cluster_panels = on ? 1 : 0; }
+
+// Cluster launch of the panel factorisation when the panel is too tall for one CTA.
+// Returns with *launched = false (nothing launched) when no cluster size up to 16
+// holds the panel or the device cannot co-schedule such a cluster.
+template <class E>
+cudaError_t launch_panel_cluster(int n, int k0, int nb, int nmat, E* A, long long stride, int* piv, int* info,
+                                 cudaStream_t st, bool* launched) {
+    *launched = false;
+    const int m = n - k0;
+    int cs = 2, ci = 0;
+    size_t R = 0, smem = 0;
+    for (; cs <= 16; cs *= 2, ++ci) {
+        R = (m + cs - 1) / cs;
+        smem = R * nb * sizeof(E);
+        if (smem <= kPanelClusterSmem) break;
+    }
+    if (cs > 16 || (long long)nmat * cs > 0x7fffffffLL) return cudaSuccess;
+    static int ok[4] = {-1, -1, -1, -1};     // per cluster size 2, 4, 8, 16: unknown / no / yes
+    cudaError_t e = cudaFuncSetAttribute(k_lu_panel_cluster<E>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kPanelClusterSmem);
+    if (e != cudaSuccess) return e;
+    if (cs == 16) {
+        e = cudaFuncSetAttribute(k_lu_panel_cluster<E>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return cudaSuccess;
+        }
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(nmat * cs));
+    cfg.blockDim = dim3(kLuPanelThreads);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (ok[ci] < 0) {
+        cfg.dynamicSmemBytes = kPanelClusterSmem;
+        int ncl = 0;
+        e = cudaOccupancyMaxActiveClusters(&ncl, k_lu_panel_cluster<E>, &cfg);
+        if (e != cudaSuccess) cudaGetLastError();
+        ok[ci] = (e == cudaSuccess && ncl > 0) ? 1 : 0;
+    }
+    if (!ok[ci]) return cudaSuccess;
+    cfg.dynamicSmemBytes = smem;
+    e = cudaLaunchKernelEx(&cfg, k_lu_panel_cluster<E>, n, k0, nb, (int)R, A, stride, piv, info);
+    *launched = e == cudaSuccess;
+    return e;
+}
+
 template <class E>
 cudaError_t lu_factor_impl(int n, int nmat, E* A, long long stride, int* piv, int* perm, int* info, cudaStream_t st,
                            long long* launches) {
@@ -462,10 +622,16 @@ cudaError_t lu_factor_impl(int n, int nmat, E* A, long long stride, int* piv, in
     for (int k0 = 0; k0 < n; k0 += kLuNB) {
         const int nb = min(kLuNB, n - k0);
         const size_t psm = (size_t)(n - k0) * nb * sizeof(E);
-        if (psm <= kLuSmemLimit)
+        if (psm <= kLuSmemLimit) {
             k_lu_panel<E, true><<<nmat, kLuPanelThreads, psm, st>>>(n, k0, nb, A, stride, piv, info);
-        else
-            k_lu_panel<E, false><<<nmat, kLuPanelThreads, 0, st>>>(n, k0, nb, A, stride, piv, info);
+        } else {
+            bool launched = false;
+            if (g_lu_cluster_panels) {
+                e = launch_panel_cluster<E>(n, k0, nb, nmat, A, stride, piv, info, st, &launched);
+                if (e != cudaSuccess) return e;
+            }
+            if (!launched) k_lu_panel<E, false><<<nmat, kLuPanelThreads, 0, st>>>(n, k0, nb, A, stride, piv, info);
+        }
         ++nl;
         if (ncb > 1) {
             k_lu_swap_trsm<E><<<dim3(ncb, nmat), 256, 0, st>>>(n, k0, nb, A, stride, piv);

@@ -236,6 +236,48 @@ __device__ void jacobi_thin(cplx* B, int n, int s, cplx* W, double* red) {
 }
 
 
+// The same one-sided Jacobi for a square s x s matrix (s <= 32) on one warp: lane r
+// holds row r, reductions by shuffles, no block-wide barriers.
+__device__ void jacobi_warp(cplx* B, int s, cplx* W) {
+    const int r = threadIdx.x & 31;
+    for (int e = r; e < s * s; e += 32) W[e] = mk((e % s) == (e / s) ? 1. : 0.);
+    __syncwarp();
+    const double tol = 1e-15;
+    for (int sweep = 0; sweep < 30; ++sweep) {
+        int rotated = 0;
+        for (int p = 0; p < s - 1; ++p)
+            for (int q = p + 1; q < s; ++q) {
+                const cplx x = r < s ? B[p * s + r] : mk(0.), y = r < s ? B[q * s + r] : mk(0.);
+                double al = norm2(x), be = norm2(y);
+                double gr = fma(x.re, y.re, x.im * y.im), gi = fma(x.re, y.im, -x.im * y.re);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    al += __shfl_xor_sync(0xffffffffu, al, o);
+                    be += __shfl_xor_sync(0xffffffffu, be, o);
+                    gr += __shfl_xor_sync(0xffffffffu, gr, o);
+                    gi += __shfl_xor_sync(0xffffffffu, gi, o);
+                }
+                const double g = hypot(gr, gi);
+                if (g == 0. || g <= tol * sqrt(al * be)) continue;
+                rotated = 1;
+                const double zeta = (be - al) / (2. * g);
+                const double t = (zeta >= 0. ? 1. : -1.) / (fabs(zeta) + sqrt(1. + zeta * zeta));
+                const double c = 1. / sqrt(1. + t * t), sn = c * t;
+                const cplx eph = mk(gr / g, -gi / g);
+                if (r < s) {
+                    const cplx ey = eph * y;
+                    B[p * s + r] = c * x - sn * ey;
+                    B[q * s + r] = sn * x + c * ey;
+                    const cplx wx = W[p * s + r], wy = eph * W[q * s + r];
+                    W[p * s + r] = c * wx - sn * wy;
+                    W[q * s + r] = sn * wx + c * wy;
+                }
+                __syncwarp();
+            }
+        if (!rotated) break;
+    }
+}
+
 struct RsvdJob {
     int n, nmat, s, q, D;
     const cplx* T;            // matrix m at T + m*mat_stride, T' at + der_stride
@@ -368,7 +410,7 @@ __global__ void __launch_bounds__(kRsvdThreads) k_rsvd_tail(int n, int s, int D,
     const int mat = blockIdx.x, os = D + 1;
     for (int e = threadIdx.x; e < s * s; e += blockDim.x) Rs[e] = Rf[(long long)mat * s * s + e];
     __syncthreads();
-    jacobi_thin(Rs, s, s, W, red);
+    if (threadIdx.x < 32) jacobi_warp(Rs, s, W);
     __syncthreads();
     double best = -1.;
     int bj = 0;

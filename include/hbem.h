@@ -50,6 +50,11 @@ const char* hbem_status_string(int status);
 const char* hbem_last_error(void);
 /* select the CUDA device used by handles created afterwards */
 int hbem_set_device(int device);
+/* Process-wide switches, for tests and measurements:
+ *   "lu_cluster_panels" (default 1): LU panels taller than one CTA's shared memory
+ *   are factored by a thread-block cluster holding the panel in distributed shared
+ *   memory; 0 factors them in global memory.                                        */
+int hbem_set_option(const char* name, int value);
 
 /* Instrumentation (no counterpart in the reference, which prints std::chrono
  * timings, gen_sol_op.cpp:89-99 and randsvd.cpp:27-47): kernel launches issued

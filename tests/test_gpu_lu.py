@@ -85,3 +85,31 @@ def test_lu_zero_pivot_reported():
     A = _dev(mats)
     st, _, info = _factor(A, n, nmat)
     assert st == 5 and info[0] == 0 and info[1] > 0
+
+
+@pytest.mark.parametrize("n", [1000, 1500])
+def test_cluster_panel_matches_global_panel(n):
+    """Panels taller than one CTA's shared memory (FP64: > 440 rows): the cluster
+    factorisation (rows spread over the CTAs' shared memory) gives the same pivots
+    and factors as the in-place global-memory panel."""
+    nmat = 2
+    mats = _mats(n, nmat, seed=n + 1)
+    res = []
+    for on in (1, 0):
+        check(C.lib().hbem_set_option(b"lu_cluster_panels", on))
+        A = _dev(mats)
+        st, piv, _ = _factor(A, n, nmat)
+        check(st)
+        res.append((A.cpu().numpy(), piv.cpu().numpy()))
+    check(C.lib().hbem_set_option(b"lu_cluster_panels", 1))
+    assert np.array_equal(res[0][1], res[1][1])
+    assert np.max(np.abs(res[0][0] - res[1][0])) <= 1e-13 * np.max(np.abs(res[1][0]))
+    b = np.random.default_rng(2).standard_normal((n, 3)) + 0j
+    X = torch.from_numpy(np.ascontiguousarray(np.stack([b.T] * nmat))).cuda()
+    A = _dev(mats)
+    st, piv, _ = _factor(A, n, nmat)
+    check(C.lib().hbem_lu_solve_batch_device(n, nmat, 0, ctypes.c_void_p(A.data_ptr()), n * n,
+                                             ctypes.c_void_p(piv.data_ptr()), 3, ctypes.c_void_p(X.data_ptr()), 3 * n))
+    for m in range(nmat):
+        ref = np.linalg.solve(mats[m], b)
+        assert np.linalg.norm(X.cpu().numpy()[m].T - ref) <= 1e-12 * np.linalg.norm(ref)

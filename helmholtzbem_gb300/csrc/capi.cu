@@ -39,6 +39,9 @@ cudaError_t lu_solve_batched(int n, int nmat, int trans, const cplx* LU, long lo
 cudaError_t lu_perm_from_piv(int n, int nmat, const int* piv, int* perm, cudaStream_t st);
 bool lu_solve_supported(int n);
 void lu_set_cluster_panels(int on);
+size_t svd_fast_smem_bytes(int n);
+cudaError_t launch_svd_fast(int n, int nmat, int D, const cplx* T, long long mat_stride, long long der_stride,
+                            double* out, int* status, cudaStream_t st);
 }  // namespace hbem
 
 using namespace hbem;
@@ -56,6 +59,7 @@ int g_timing = 0;
 double g_asm_ms = 0.;
 long long g_asm_launches = 0;
 long long g_asm_points = 0;   // quadrature points x media processed by timed launches
+int g_svd_fast = 1;           // dense sigma: FP32 Jacobi + FP64 refinement where it fits
 
 int fail(int code, const std::string& msg) {
     g_err = msg;
@@ -312,6 +316,10 @@ int hbem_set_option(const char* name, int value) {
     const std::string k(name);
     if (k == "lu_cluster_panels") {
         lu_set_cluster_panels(value);
+        return HBEM_OK;
+    }
+    if (k == "svd_fast") {
+        g_svd_fast = value ? 1 : 0;
         return HBEM_OK;
     }
     return fail(HBEM_ERR_INVALID, "set_option: unknown option " + k);
@@ -653,13 +661,28 @@ static int sv_batch(cudaStream_t st, int n, int nmat, unsigned d, const cplx* T,
         HB_CK(sig->ensure((size_t)nmat * n * sizeof(double)));
         dsig = sig->as<double>();
     }
+    std::vector<int> stat(nmat);
+    if (!sig_all_host && g_svd_fast && svd_fast_smem_bytes(n) <= 220 * 1024) {
+        // FP32 Jacobi + FP64 refinement; matrices it cannot finish (singular T, a
+        // far-field series that does not converge) are redone by the polished kernel
+        HB_CK(launch_svd_fast(n, nmat, (int)d, T, mat_stride, der_stride, out.as<double>(), status.as<int>(), st));
+        g_launches += 1;
+        HB_CK(cudaMemcpyAsync(stat.data(), status.p, (size_t)nmat * sizeof(int), cudaMemcpyDeviceToHost, st));
+        HB_CK(cudaStreamSynchronize(st));
+        bool redo = false;
+        for (int v : stat) redo |= v != 0;
+        if (!redo) {
+            HB_CK(cudaMemcpyAsync(out_host, out.p, (size_t)nmat * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+            HB_CK(cudaStreamSynchronize(st));
+            return HBEM_OK;
+        }
+    }
     HB_CK(launch_svd_mixed(n, nmat, (int)d, 0, T, mat_stride, der_stride, A.as<cplx>(), V.as<cplx>(),
                            out.as<double>(), dsig, status.as<int>(), st));
     g_launches += 1;
     HB_CK(cudaMemcpyAsync(out_host, out.p, (size_t)nmat * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (sig_all_host)
         HB_CK(cudaMemcpyAsync(sig_all_host, dsig, (size_t)nmat * n * sizeof(double), cudaMemcpyDeviceToHost, st));
-    std::vector<int> stat(nmat);
     HB_CK(cudaMemcpyAsync(stat.data(), status.p, (size_t)nmat * sizeof(int), cudaMemcpyDeviceToHost, st));
     HB_CK(cudaStreamSynchronize(st));
     for (int v : stat)

@@ -13,6 +13,7 @@
 // (|sigma_j - sigma| <= 1e-9 sigma) are left out of the first sum: a
 // perturbation that keeps the degeneracy does not couple them.
 #include "hbem_device.cuh"
+#include "smem_linalg.cuh"
 
 namespace hbem {
 
@@ -379,6 +380,414 @@ cudaError_t launch_svd_mixed(int n, int nmat, int D, int which, const cplx* T, l
     if (e != cudaSuccess) return e;
     SvdJob J{n, nmat, D, which, T, mat_stride, der_stride, gA, gV, out, sig_all, status, 1};
     k_svd_jacobi<true><<<nmat, kSvdThreads, svd_smem_bytes(n, true), st>>>(J);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- FP32 Jacobi + FP64 refinement
+//
+// sigma_min, sigma', sigma'' of one matrix per CTA with O(n^3) work only in FP32
+// (the Jacobi sweeps) and in one FP64 LU; everything else in FP64 is O(n^2 k):
+//  1. FP32 one-sided Jacobi: all singular triplets to the FP32 noise level.
+//  2. The near block: the right vectors of the k = min(n, 12) smallest FP32 singular
+//     values.  FP64 LU of T in shared memory; four block inverse iterations
+//     X <- qr(T^-1 T^-H X); Rayleigh-Ritz: T X = Q_Y R, SVD of the k x k factor R
+//     gives FP64 Ritz triplets (sigma_j, u_j, v_j).
+//  3. sigma = smallest Ritz value, sigma' = Re u^H T' v.
+//  4. sigma'' = Re u^H T'' v + the minus terms of the target and its degenerate
+//     partners D (relative gap <= 1e-9; their plus terms are left out as above) +
+//     the rest of the second-order sum as a resolvent, 2 Re b_f^H (sigma - W)^-1 b_f,
+//     b_f the Wielandt vector W' x projected off D.  (sigma - W)^-1 reduces to
+//     y = (T T^H - sigma^2)^+ r on the complement of the left vectors of D, solved by
+//     conjugate gradients preconditioned with (T T^H)^-1 = T^-H T^-1 from the same
+//     LU: the preconditioned spectrum is 1 - sigma^2 / sigma_j^2.
+// A CG that does not converge sets status 4 and a singular LU status 5; the host
+// then recomputes the batch with the FP64-polished Jacobi kernel.
+
+constexpr int kFastKmax = 12;
+constexpr int kFastInvIter = 4;
+constexpr int kFastNeumannMax = 200;   // preconditioned CG iteration cap
+
+struct SvdFastJob {
+    int n, nmat, D;
+    const cplx* T;
+    long long mat_stride, der_stride;
+    double* out;     // [nmat][3]
+    int* status;     // [nmat]
+};
+
+struct FastSmem {
+    size_t r0, x, y, w, rf, vec, coef, red, sig32, piv, redi, idx, sigb, ab, total;
+};
+
+__host__ __device__ inline FastSmem fast_layout(int n) {
+    FastSmem L;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 15) / 16 * 16; return o; };
+    const size_t c = sizeof(cplx), K = kFastKmax;
+    L.r0 = take((size_t)n * n * c);          // FP32 A32 | V32, then the FP64 LU of T
+    L.x = take((size_t)n * K * c);
+    L.y = take((size_t)n * K * c);
+    L.w = take(K * K * c);
+    L.rf = take(K * K * c);
+    L.vec = take(8 * (size_t)n * c);
+    L.coef = take(K * c);
+    L.red = take(128 * sizeof(double));
+    L.sig32 = take((size_t)n * sizeof(float));
+    L.piv = take((size_t)n * sizeof(int));
+    L.redi = take(32 * sizeof(int));
+    L.idx = take(K * sizeof(int));
+    L.sigb = take(K * sizeof(double));
+    L.ab = take(2 * K * c);
+    L.total = off;
+    return L;
+}
+
+size_t svd_fast_smem_bytes(int n) { return fast_layout(n).total; }
+
+// y = A x for the global column-major n x n matrix A (thread per row)
+static __device__ void gemv_n(const cplx* A, int n, const cplx* x, cplx* y) {
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        cplx a = mk(0.);
+        for (int c = 0; c < n; ++c) a += A[r + (long long)c * n] * x[c];
+        y[r] = a;
+    }
+    __syncthreads();
+}
+
+// y = A^H x (warp per column)
+static __device__ void gemv_h(const cplx* A, int n, const cplx* x, cplx* y) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int c = warp; c < n; c += nw) {
+        const cplx* col = A + (long long)c * n;
+        double sr = 0., si = 0.;
+        for (int r = lane; r < n; r += 32) {
+            const cplx a = conj(col[r]), b = x[r];
+            sr = fma(a.re, b.re, fma(-a.im, b.im, sr));
+            si = fma(a.re, b.im, fma(a.im, b.re, si));
+        }
+        sr = warp_sum(sr);
+        si = warp_sum(si);
+        if (lane == 0) y[c] = mk(sr, si);
+    }
+    __syncthreads();
+}
+
+// out[j] = B[:, j]^H x for the kb columns of B (n x kb, leading dimension n)
+static __device__ void dots_h(const cplx* B, int n, int kb, const cplx* x, cplx* out) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int j = warp; j < kb; j += nw) {
+        const cplx* b = B + (long long)j * n;
+        double sr = 0., si = 0.;
+        for (int r = lane; r < n; r += 32) {
+            const cplx a = conj(b[r]), v = x[r];
+            sr = fma(a.re, v.re, fma(-a.im, v.im, sr));
+            si = fma(a.re, v.im, fma(a.im, v.re, si));
+        }
+        sr = warp_sum(sr);
+        si = warp_sum(si);
+        if (lane == 0) out[j] = mk(sr, si);
+    }
+    __syncthreads();
+}
+
+// x <- x - B c  (B n x kb)
+static __device__ void sub_span(const cplx* B, int n, int kb, const cplx* c, cplx* x) {
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        cplx v = x[r];
+        for (int j = 0; j < kb; ++j) v -= B[r + (long long)j * n] * c[j];
+        x[r] = v;
+    }
+    __syncthreads();
+}
+
+static __device__ double dot_re(const cplx* a, const cplx* b, int n, double* red) {
+    double part = 0.;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) part += a[r].re * b[r].re + a[r].im * b[r].im;
+    return bsum(part, red);
+}
+
+// Rows of B (n x kb) times the kb x kb matrix M, in place, row by row.
+static __device__ void rows_times(cplx* B, int n, int kb, const cplx* M) {
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        cplx row[kFastKmax], outr[kFastKmax];
+#pragma unroll
+        for (int j = 0; j < kFastKmax; ++j) row[j] = j < kb ? B[r + (long long)j * n] : mk(0.);
+#pragma unroll
+        for (int j = 0; j < kFastKmax; ++j) {
+            cplx a = mk(0.);
+#pragma unroll
+            for (int l = 0; l < kFastKmax; ++l)
+                if (l < kb) a += row[l] * M[l + j * kb];
+            outr[j] = a;
+        }
+#pragma unroll
+        for (int j = 0; j < kFastKmax; ++j)
+            if (j < kb) B[r + (long long)j * n] = outr[j];
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
+    extern __shared__ double smraw[];
+    char* sb = reinterpret_cast<char*>(smraw);
+    const int n = J.n, mat = blockIdx.x;
+    const FastSmem L = fast_layout(n);
+    cplx* T64 = reinterpret_cast<cplx*>(sb + L.r0);
+    cpf* A32 = reinterpret_cast<cpf*>(sb + L.r0);
+    cpf* V32 = A32 + (long long)n * n;
+    cplx* X = reinterpret_cast<cplx*>(sb + L.x);
+    cplx* Y = reinterpret_cast<cplx*>(sb + L.y);
+    cplx* W = reinterpret_cast<cplx*>(sb + L.w);
+    cplx* Rf = reinterpret_cast<cplx*>(sb + L.rf);
+    cplx* vec = reinterpret_cast<cplx*>(sb + L.vec);
+    cplx* coef = reinterpret_cast<cplx*>(sb + L.coef);
+    double* red = reinterpret_cast<double*>(sb + L.red);
+    float* sig32 = reinterpret_cast<float*>(sb + L.sig32);
+    int* piv = reinterpret_cast<int*>(sb + L.piv);
+    int* redi = reinterpret_cast<int*>(sb + L.redi);
+    int* idx = reinterpret_cast<int*>(sb + L.idx);
+    double* sigb = reinterpret_cast<double*>(sb + L.sigb);
+    cplx* ab = reinterpret_cast<cplx*>(sb + L.ab);   // a_j, b_j
+    cplx *F = vec, *G = vec + n, *f1 = vec + 2 * n, *f2 = vec + 3 * n, *rr = vec + 4 * n, *acc = vec + 5 * n,
+         *term = vec + 6 * n, *z2 = vec + 7 * n;
+    __shared__ int s_rot, s_kb, s_im, s_sing, s_conv;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const cplx* T0 = J.T + (long long)mat * J.mat_stride;
+    double* out = J.out + 3LL * mat;
+
+    // 1. FP32 Jacobi
+    jacobi_fp32(T0, n, A32, V32, &s_rot);
+    for (int j = warp; j < n; j += nw) {
+        float s2 = 0.f;
+        for (int i = lane; i < n; i += 32) s2 = fmaf(A32[j * n + i].re, A32[j * n + i].re,
+                                                     fmaf(A32[j * n + i].im, A32[j * n + i].im, s2));
+        s2 = warp_sumf(s2);
+        if (lane == 0) sig32[j] = sqrtf(s2);
+    }
+    __syncthreads();
+    // 2. near block: the kb smallest FP32 singular values (all within 3 sigma_min)
+    if (threadIdx.x == 0) {
+        int i0 = 0;
+        for (int j = 1; j < n; ++j)
+            if (sig32[j] < sig32[i0]) i0 = j;
+        const int kb = min(n, kFastKmax);
+        (void)i0;
+        // selection of the kb smallest (ascending, ties by index)
+        for (int b = 0; b < kb; ++b) {
+            int best = -1;
+            for (int j = 0; j < n; ++j) {
+                bool used = false;
+                for (int l = 0; l < b; ++l) used |= idx[l] == j;
+                if (used) continue;
+                if (best < 0 || sig32[j] < sig32[best]) best = j;
+            }
+            idx[b] = best;
+        }
+        s_kb = kb;
+        s_sing = 0;
+    }
+    __syncthreads();
+    const int kb = s_kb;
+    for (int e = threadIdx.x; e < n * kb; e += blockDim.x) {
+        const cpf v = V32[idx[e / n] * n + e % n];
+        X[e] = mk((double)v.re, (double)v.im);
+    }
+    __syncthreads();
+    // FP64 LU of T over the FP32 work space
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) T64[e] = T0[e];
+    __syncthreads();
+    lu_smem(T64, n, piv, red, redi, &s_sing);
+    qr_cgs2(X, n, kb, coef, red);
+    for (int it = 0; it < kFastInvIter; ++it) {
+        solve_lu_h(T64, piv, n, X, kb);
+        solve_lu(T64, piv, n, X, kb);
+        qr_cgs2(X, n, kb, coef, red);
+    }
+    // Rayleigh-Ritz: Y = T X = Q_Y Rf, Rf W = Q_R Sigma
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        cplx a[kFastKmax];
+#pragma unroll
+        for (int j = 0; j < kFastKmax; ++j) a[j] = mk(0.);
+        for (int c = 0; c < n; ++c) {
+            const cplx t = T0[r + (long long)c * n];
+#pragma unroll
+            for (int j = 0; j < kFastKmax; ++j)
+                if (j < kb) a[j] += t * X[c + j * n];
+        }
+#pragma unroll
+        for (int j = 0; j < kFastKmax; ++j)
+            if (j < kb) Y[r + j * n] = a[j];
+    }
+    __syncthreads();
+    qr_cgs2(Y, n, kb, coef, red, Rf);
+    if (threadIdx.x < 32) jacobi_warp(Rf, kb, W);
+    __syncthreads();
+    if (threadIdx.x < kb) {
+        double s2 = 0.;
+        for (int r = 0; r < kb; ++r) s2 += norm2(Rf[threadIdx.x * kb + r]);
+        sigb[threadIdx.x] = sqrt(s2);
+    }
+    __syncthreads();
+    // Q_R = (Rf W) Sigma^-1 in place
+    for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
+        const double sj = sigb[e / kb];
+        Rf[e] = (sj > 0. ? 1. / sj : 0.) * Rf[e];
+    }
+    __syncthreads();
+    rows_times(X, n, kb, W);     // V_b = X W
+    rows_times(Y, n, kb, Rf);    // U_b = Q_Y Q_R
+    if (threadIdx.x == 0) {
+        int im = 0;
+        for (int j = 1; j < kb; ++j)
+            if (sigb[j] < sigb[im]) im = j;
+        s_im = im;
+        s_conv = 1;
+    }
+    __syncthreads();
+    const int im = s_im;
+    const double sg = sigb[im];
+    const cplx* u = Y + (long long)im * n;
+    const cplx* v = X + (long long)im * n;
+    if (threadIdx.x == 0) {
+        out[0] = sg;
+        out[1] = 0.;
+        out[2] = 0.;
+    }
+    if (J.D == 0) {
+        if (threadIdx.x == 0) J.status[mat] = s_sing ? 5 : 0;
+        return;
+    }
+    // 3. sigma'
+    const cplx* T1 = T0 + J.der_stride;
+    gemv_n(T1, n, v, F);
+    const double d1 = dot_re(u, F, n, red);
+    if (threadIdx.x == 0) out[1] = d1;
+    if (J.D == 1) {
+        if (threadIdx.x == 0) J.status[mat] = s_sing ? 5 : 0;
+        return;
+    }
+    // 4. sigma''
+    const cplx* T2 = T0 + 2 * J.der_stride;
+    gemv_n(T2, n, v, acc);
+    const double c0 = dot_re(u, acc, n, red + 32);
+    gemv_h(T1, n, u, G);
+    cplx* a_j = ab;
+    cplx* b_j = ab + kFastKmax;
+    dots_h(Y, n, kb, F, a_j);
+    dots_h(X, n, kb, G, b_j);
+    // D: the target and its numerically degenerate partners (relative gap <= 1e-9);
+    // their minus terms explicitly, every other triplet through the resolvent
+    if (threadIdx.x == 0) {
+        int nd = 0;
+        for (int j = 0; j < kb; ++j)
+            if (j == im || fabs(sigb[j] - sg) <= 1e-9 * sg) idx[nd++] = j;
+        s_kb = nd;
+    }
+    __syncthreads();
+    const int nd = s_kb;
+    double near_sum = 0.;
+    for (int l = 0; l < nd; ++l) {
+        const int j = idx[l];
+        const double sj = sigb[j];
+        const cplx mi = a_j[j] - b_j[j];
+        if (sg + sj > 0.) near_sum += 0.5 * norm2(mi) / (sg + sj);
+    }
+    // gather the D columns of U_b, V_b to the front (Y, X columns 0..nd-1)
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        cplx uu[kFastKmax], vv[kFastKmax];
+        for (int l = 0; l < nd; ++l) {
+            uu[l] = Y[e + (long long)idx[l] * n];
+            vv[l] = X[e + (long long)idx[l] * n];
+        }
+        for (int l = 0; l < nd; ++l) {
+            Y[e + (long long)l * n] = uu[l];
+            X[e + (long long)l * n] = vv[l];
+        }
+    }
+    __syncthreads();
+    // b_f = (P_U T' v; P_V T'^H u) / sqrt2 with P_U, P_V projecting off D
+    const double is2 = 0.70710678118654752440;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        f1[r] = is2 * F[r];
+        f2[r] = is2 * G[r];
+    }
+    __syncthreads();
+    dots_h(Y, n, nd, f1, coef);
+    sub_span(Y, n, nd, coef, f1);
+    dots_h(X, n, nd, f2, coef);
+    sub_span(X, n, nd, coef, f2);
+    // y = (T T^H - sigma^2)^+ (sigma f1 + T f2) on the complement of U_D: preconditioned
+    // CG with M = (T T^H)^-1 = T^-H T^-1 (eigenvalues of M A: 1 - sigma^2 / sigma_j^2)
+    gemv_n(T0, n, f2, rr);
+    for (int r = threadIdx.x; r < n; r += blockDim.x) rr[r] = sg * f1[r] + rr[r];   // residual (y = 0)
+    __syncthreads();
+    dots_h(Y, n, nd, rr, coef);
+    sub_span(Y, n, nd, coef, rr);
+    cplx* yv = acc;
+    cplx* pv = term;
+    cplx* zv = z2;      // preconditioned residual, later reused
+    cplx* ap = G;       // A p (T'^H u no longer needed)
+    cplx* tmp = F;      // T^H p (T' v no longer needed)
+    const double s2 = sg * sg;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) { yv[r] = mk(0.); zv[r] = rr[r]; }
+    __syncthreads();
+    solve_lu(T64, piv, n, zv, 1);                 // z = T^-H T^-1 res
+    solve_lu_h(T64, piv, n, zv, 1);
+    dots_h(Y, n, nd, zv, coef);
+    sub_span(Y, n, nd, coef, zv);
+    for (int r = threadIdx.x; r < n; r += blockDim.x) pv[r] = zv[r];
+    __syncthreads();
+    double rz = dot_re(rr, zv, n, red);
+    const double rz0 = rz;
+    int it = 0;
+    for (; it < kFastNeumannMax && rz > 1e-32 * rz0 && rz > 0.; ++it) {
+        gemv_h(T0, n, pv, tmp);                    // A p = T T^H p - sigma^2 p
+        gemv_n(T0, n, tmp, ap);
+        for (int r = threadIdx.x; r < n; r += blockDim.x) ap[r] = ap[r] - s2 * pv[r];
+        __syncthreads();
+        dots_h(Y, n, nd, ap, coef);
+        sub_span(Y, n, nd, coef, ap);
+        const double pap = dot_re(pv, ap, n, red + 32);
+        if (!(pap > 0.)) break;
+        const double alpha = rz / pap;
+        for (int r = threadIdx.x; r < n; r += blockDim.x) {
+            yv[r] += alpha * pv[r];
+            rr[r] -= alpha * ap[r];
+            zv[r] = rr[r];
+        }
+        __syncthreads();
+        solve_lu(T64, piv, n, zv, 1);
+        solve_lu_h(T64, piv, n, zv, 1);
+        dots_h(Y, n, nd, zv, coef);
+        sub_span(Y, n, nd, coef, zv);
+        const double rz1 = dot_re(rr, zv, n, red + 64);
+        const double beta = rz1 / rz;
+        rz = rz1;
+        for (int r = threadIdx.x; r < n; r += blockDim.x) pv[r] = zv[r] + beta * pv[r];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && rz > 1e-24 * rz0) s_conv = 0;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) yv[r] = -yv[r];   // z1
+    __syncthreads();
+    gemv_h(T0, n, yv, z2);
+    const double isg = sg > 0. ? 1. / sg : 0.;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) z2[r] = isg * (f2[r] + z2[r]);
+    __syncthreads();
+    const double far = dot_re(f1, yv, n, red) + dot_re(f2, z2, n, red + 32);
+    if (threadIdx.x == 0) {
+        out[2] = c0 + near_sum + 2. * far;
+        J.status[mat] = s_sing ? 5 : (s_conv ? 0 : 4);
+    }
+}
+
+cudaError_t launch_svd_fast(int n, int nmat, int D, const cplx* T, long long mat_stride, long long der_stride,
+                            double* out, int* status, cudaStream_t st) {
+    const size_t limit = 220 * 1024, smem = svd_fast_smem_bytes(n);
+    if (smem > limit || n < 2) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(k_svd_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit);
+    if (e != cudaSuccess) return e;
+    SvdFastJob J{n, nmat, D, T, mat_stride, der_stride, out, status};
+    k_svd_fast<<<nmat, kSvdThreads, smem, st>>>(J);
     return cudaGetLastError();
 }
 

@@ -1,0 +1,269 @@
+// Dense linear algebra on one CTA, operands in shared (or global) memory: block
+// sums, LU with partial pivoting and its two solve forms, classical Gram-Schmidt
+// QR (twice), and one-sided Jacobi for thin matrices.  Used by the randomized SVD
+// (rsvd.cu) and the dense singular-value kernels (dense.cu).
+#pragma once
+#include "hbem_device.cuh"
+
+namespace hbem {
+
+static __device__ __forceinline__ double bsum(double x, double* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    __syncthreads();
+    if (lane == 0) red[warp] = x;
+    __syncthreads();
+    double s = 0.;
+    for (int w = 0; w < nw; ++w) s += red[w];
+    return s;
+}
+
+// LU with partial pivoting of the n x n column-major matrix A (shared memory).
+// piv[k] = row exchanged with row k at step k.  Returns via *sing a zero-pivot flag.
+static __device__ void lu_smem(cplx* A, int n, int* piv, double* redv, int* redi, int* sing) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int k = 0; k < n; ++k) {
+        // pivot: largest |A[i,k]|, i >= k (ties: smallest i)
+        double best = -1.;
+        int bi = k;
+        for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
+            double a = norm2(A[i + (long long)k * n]);
+            if (a > best) { best = a; bi = i; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            double ob = __shfl_xor_sync(0xffffffffu, best, o);
+            int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        if (lane == 0) { redv[warp] = best; redi[warp] = bi; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double b = redv[0];
+            int p = redi[0];
+            for (int w = 1; w < nw; ++w)
+                if (redv[w] > b || (redv[w] == b && redi[w] < p)) { b = redv[w]; p = redi[w]; }
+            piv[k] = p;
+            if (b == 0.) *sing = 1;
+        }
+        __syncthreads();
+        const int p = piv[k];
+        if (p != k)
+            for (int j = threadIdx.x; j < n; j += blockDim.x) {
+                cplx t = A[k + (long long)j * n];
+                A[k + (long long)j * n] = A[p + (long long)j * n];
+                A[p + (long long)j * n] = t;
+            }
+        __syncthreads();
+        const cplx d = A[k + (long long)k * n];
+        if (norm2(d) > 0.) {
+            const cplx id = cdiv(mk(1.), d);
+            for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) A[i + (long long)k * n] = A[i + (long long)k * n] * id;
+        }
+        __syncthreads();
+        const int m = n - k - 1;
+        for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+            const int i = k + 1 + e % m, j = k + 1 + e / m;
+            A[i + (long long)j * n] -= A[i + (long long)k * n] * A[k + (long long)j * n];
+        }
+        __syncthreads();
+    }
+}
+
+// X <- T^-1 X  (s columns, leading dimension n), with P T = L U in A
+static __device__ void solve_lu(const cplx* A, const int* piv, int n, cplx* X, int s) {
+    for (int k = 0; k < n; ++k) {          // row exchanges in order
+        const int p = piv[k];
+        if (p != k)
+            for (int c = threadIdx.x; c < s; c += blockDim.x) {
+                cplx t = X[k + c * n];
+                X[k + c * n] = X[p + c * n];
+                X[p + c * n] = t;
+            }
+        __syncthreads();
+    }
+    for (int k = 0; k < n; ++k) {          // L y = P b (unit diagonal)
+        for (int e = threadIdx.x; e < (n - k - 1) * s; e += blockDim.x) {
+            const int i = k + 1 + e % (n - k - 1), c = e / (n - k - 1);
+            X[i + c * n] -= A[i + (long long)k * n] * X[k + c * n];
+        }
+        __syncthreads();
+    }
+    for (int k = n - 1; k >= 0; --k) {     // U x = y
+        for (int c = threadIdx.x; c < s; c += blockDim.x) X[k + c * n] = cdiv(X[k + c * n], A[k + (long long)k * n]);
+        __syncthreads();
+        for (int e = threadIdx.x; e < k * s; e += blockDim.x) {
+            const int i = e % k, c = e / k;
+            X[i + c * n] -= A[i + (long long)k * n] * X[k + c * n];
+        }
+        __syncthreads();
+    }
+}
+
+// X <- T^-H X:  T^H = U^H L^H P  =>  x = P^T L^-H U^-H b
+static __device__ void solve_lu_h(const cplx* A, const int* piv, int n, cplx* X, int s) {
+    for (int k = 0; k < n; ++k) {          // U^H y = b (lower triangular, diagonal conj(u_kk))
+        for (int c = threadIdx.x; c < s; c += blockDim.x) X[k + c * n] = cdiv(X[k + c * n], conj(A[k + (long long)k * n]));
+        __syncthreads();
+        for (int e = threadIdx.x; e < (n - k - 1) * s; e += blockDim.x) {
+            const int i = k + 1 + e % (n - k - 1), c = e / (n - k - 1);
+            X[i + c * n] -= conj(A[k + (long long)i * n]) * X[k + c * n];
+        }
+        __syncthreads();
+    }
+    for (int k = n - 1; k >= 0; --k) {     // L^H z = y (unit upper triangular)
+        for (int e = threadIdx.x; e < k * s; e += blockDim.x) {
+            const int i = e % k, c = e / k;
+            X[i + c * n] -= conj(A[k + (long long)i * n]) * X[k + c * n];
+        }
+        __syncthreads();
+    }
+    for (int k = n - 1; k >= 0; --k) {     // x = P^T z (exchanges in reverse order)
+        const int p = piv[k];
+        if (p != k)
+            for (int c = threadIdx.x; c < s; c += blockDim.x) {
+                cplx t = X[k + c * n];
+                X[k + c * n] = X[p + c * n];
+                X[p + c * n] = t;
+            }
+        __syncthreads();
+    }
+}
+
+// Orthonormalise the s columns of X (n x s) in place: classical Gram-Schmidt,
+// twice per column ("twice is enough").  coef: s entries of scratch.  If Rf is
+// given it receives the s x s upper-triangular factor (column-major), X = Q Rf.
+static __device__ void qr_cgs2(cplx* X, int n, int s, cplx* coef, double* red, cplx* Rf = nullptr) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int j = 0; j < s; ++j) {
+        cplx* xj = X + (long long)j * n;
+        if (Rf)
+            for (int i = threadIdx.x; i < s; i += blockDim.x) Rf[i + j * s] = mk(0.);
+        for (int pass = 0; pass < 2; ++pass) {
+            for (int i = warp; i < j; i += nw) {
+                const cplx* qi = X + i * n;
+                double cr = 0., ci = 0.;
+                for (int r = lane; r < n; r += 32) {
+                    cplx a = qi[r], b = xj[r];
+                    cr = fma(a.re, b.re, fma(a.im, b.im, cr));
+                    ci = fma(a.re, b.im, fma(-a.im, b.re, ci));
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    cr += __shfl_xor_sync(0xffffffffu, cr, o);
+                    ci += __shfl_xor_sync(0xffffffffu, ci, o);
+                }
+                if (lane == 0) coef[i] = mk(cr, ci);
+            }
+            __syncthreads();
+            if (Rf)
+                for (int i = threadIdx.x; i < j; i += blockDim.x) Rf[i + j * s] += coef[i];
+            for (int r = threadIdx.x; r < n; r += blockDim.x) {
+                cplx v = xj[r];
+                for (int i = 0; i < j; ++i) v -= X[(long long)i * n + r] * coef[i];
+                xj[r] = v;
+            }
+            __syncthreads();
+        }
+        double part = 0.;
+        for (int r = threadIdx.x; r < n; r += blockDim.x) part += norm2(xj[r]);
+        const double nrm = sqrt(bsum(part, red));
+        if (Rf && threadIdx.x == 0) Rf[j + j * s] = mk(nrm);
+        const double inv = nrm > 0. ? 1. / nrm : 0.;
+        for (int r = threadIdx.x; r < n; r += blockDim.x) xj[r] = inv * xj[r];
+        __syncthreads();
+    }
+}
+
+// One-sided Jacobi on the n x s matrix B (columns in place), W (s x s) accumulates
+// the right rotations.  Serial over pairs (s is small), each pair on the whole CTA.
+static __device__ void jacobi_thin(cplx* B, int n, int s, cplx* W, double* red) {
+    for (int e = threadIdx.x; e < s * s; e += blockDim.x) W[e] = mk((e % s) == (e / s) ? 1. : 0.);
+    __syncthreads();
+    const double tol = 1e-15;
+    for (int sweep = 0; sweep < 30; ++sweep) {
+        int rotated = 0;
+        for (int p = 0; p < s - 1; ++p)
+            for (int q = p + 1; q < s; ++q) {
+                cplx* bp = B + p * n;
+                cplx* bq = B + q * n;
+                double al = 0., be = 0., gr = 0., gi = 0.;
+                for (int r = threadIdx.x; r < n; r += blockDim.x) {
+                    cplx x = bp[r], y = bq[r];
+                    al += norm2(x);
+                    be += norm2(y);
+                    gr = fma(x.re, y.re, fma(x.im, y.im, gr));
+                    gi = fma(x.re, y.im, fma(-x.im, y.re, gi));
+                }
+                al = bsum(al, red);
+                be = bsum(be, red + 32);
+                gr = bsum(gr, red + 64);
+                gi = bsum(gi, red + 96);
+                double g = hypot(gr, gi);
+                if (g == 0. || g <= tol * sqrt(al * be)) continue;
+                rotated = 1;
+                double zeta = (be - al) / (2. * g);
+                double t = (zeta >= 0. ? 1. : -1.) / (fabs(zeta) + sqrt(1. + zeta * zeta));
+                double c = 1. / sqrt(1. + t * t), sn = c * t;
+                cplx eph = mk(gr / g, -gi / g);
+                for (int r = threadIdx.x; r < n; r += blockDim.x) {
+                    cplx x = bp[r], y = eph * bq[r];
+                    bp[r] = c * x - sn * y;
+                    bq[r] = sn * x + c * y;
+                }
+                for (int r = threadIdx.x; r < s; r += blockDim.x) {
+                    cplx x = W[p * s + r], y = eph * W[q * s + r];
+                    W[p * s + r] = c * x - sn * y;
+                    W[q * s + r] = sn * x + c * y;
+                }
+                __syncthreads();
+            }
+        if (!rotated) break;
+    }
+}
+
+
+// The same one-sided Jacobi for a square s x s matrix (s <= 32) on one warp: lane r
+// holds row r, reductions by shuffles, no block-wide barriers.
+static __device__ void jacobi_warp(cplx* B, int s, cplx* W) {
+    const int r = threadIdx.x & 31;
+    for (int e = r; e < s * s; e += 32) W[e] = mk((e % s) == (e / s) ? 1. : 0.);
+    __syncwarp();
+    const double tol = 1e-15;
+    for (int sweep = 0; sweep < 30; ++sweep) {
+        int rotated = 0;
+        for (int p = 0; p < s - 1; ++p)
+            for (int q = p + 1; q < s; ++q) {
+                const cplx x = r < s ? B[p * s + r] : mk(0.), y = r < s ? B[q * s + r] : mk(0.);
+                double al = norm2(x), be = norm2(y);
+                double gr = fma(x.re, y.re, x.im * y.im), gi = fma(x.re, y.im, -x.im * y.re);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    al += __shfl_xor_sync(0xffffffffu, al, o);
+                    be += __shfl_xor_sync(0xffffffffu, be, o);
+                    gr += __shfl_xor_sync(0xffffffffu, gr, o);
+                    gi += __shfl_xor_sync(0xffffffffu, gi, o);
+                }
+                const double g = hypot(gr, gi);
+                if (g == 0. || g <= tol * sqrt(al * be)) continue;
+                rotated = 1;
+                const double zeta = (be - al) / (2. * g);
+                const double t = (zeta >= 0. ? 1. : -1.) / (fabs(zeta) + sqrt(1. + zeta * zeta));
+                const double c = 1. / sqrt(1. + t * t), sn = c * t;
+                const cplx eph = mk(gr / g, -gi / g);
+                if (r < s) {
+                    const cplx ey = eph * y;
+                    B[p * s + r] = c * x - sn * ey;
+                    B[q * s + r] = sn * x + c * ey;
+                    const cplx wx = W[p * s + r], wy = eph * W[q * s + r];
+                    W[p * s + r] = c * wx - sn * wy;
+                    W[q * s + r] = sn * wx + c * wy;
+                }
+                __syncwarp();
+            }
+        if (!rotated) break;
+    }
+}
+
+}  // namespace hbem

@@ -53,7 +53,10 @@ int hbem_set_device(int device);
 /* Process-wide switches, for tests and measurements:
  *   "lu_cluster_panels" (default 1): LU panels taller than one CTA's shared memory
  *   are factored by a thread-block cluster holding the panel in distributed shared
- *   memory; 0 factors them in global memory.                                        */
+ *   memory; 0 factors them in global memory.
+ *   "svd_fast" (default 1): dense sigma_min / sigma' / sigma'' (direct::sv*) of matrices
+ *   up to order 100 by FP32 Jacobi plus FP64 refinement of the near singular triplets
+ *   (one FP64 LU per matrix); 0 always uses the FP64-polished Jacobi kernel.         */
 int hbem_set_option(const char* name, int value);
 
 /* Instrumentation (no counterpart in the reference, which prints std::chrono

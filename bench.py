@@ -3,11 +3,11 @@
 Workload (one step): the plain resonance search on the circular scatterer of
 the reference's CPU-runnable configuration -- radius 0.25, N = 50 circular-arc
 panels, c_i = 23.4, c_o = 1, Gauss order 11, continuous P1 spaces (T(k) is
-100 x 100 complex128) -- over k in [0.5, 10] on 200 grid points: sigma_min,
-sigma', sigma'' by dense SVD at every grid point, 3-point local minima,
-validation sigma'(left) < 0 < sigma'(right), quartic/Brent guess, safeguarded
-Newton on sigma' to |dk| <= 1e-8, then every root verified by a sign change of
-sigma' across [root - 1e-8, root + 1e-8].
+100 x 100 complex128) -- over k in [0.5, 10] on 200 grid points: sigma_min
+by dense SVD at every grid point, 3-point local minima, sigma' at both bracket
+ends and validation sigma'(left) < 0 < sigma'(right), quartic/Brent guess,
+safeguarded Newton on sigma' with sigma'' to |dk| <= 1e-8, then every root
+verified by a sign change of sigma' across [root - 1e-8, root + 1e-8].
 
   value : verified roots / s with the mesh resident on the device (builder and
           solutions operator created once, outside the timed region)
@@ -31,7 +31,8 @@ sys.path.insert(0, ROOT)
 
 CFG = dict(radius=0.25, N=50, c_i=23.4, c_o=1.0, order=11, k_min=0.5, k_max=10.0, npoints=200, tol=1e-8)
 WORKLOAD = ("plain sweep: circle r=0.25, N=50 arc panels, c_i=23.4, c_o=1, Gauss order 11, P1/P1 "
-            "(T 100x100 c128), k in [0.5,10] x 200, dense sigma/sigma'/sigma'', Newton to |dk|<=1e-8")
+            "(T 100x100 c128), k in [0.5,10] x 200, dense sigma on the grid, sigma' at bracket ends, "
+            "Newton on sigma' with sigma'' to |dk|<=1e-8")
 METRIC = "verified resonances/sec at |dk|<=1e-8 (plain sweep)"
 
 
@@ -126,12 +127,12 @@ def cpu_sample(npoints_sample, threads):
     h = (CFG["k_max"] - CFG["k_min"]) / (CFG["npoints"] - 1)
     ks = CFG["k_min"] + h * np.arange(npoints_sample)
 
-    def eval3(klist):
-        return np.array([O.sv_derivs(*oso.gen_sol_op(k, CFG["c_o"], CFG["c_i"], d=2, threads=threads))
+    def evald(klist, d):
+        return np.array([O.sv_derivs(*oso.gen_sol_op(k, CFG["c_o"], CFG["c_i"], d=d, threads=threads))
                          for k in klist])
 
     t0 = time.perf_counter()
-    roots, _ = O.plain_sweep(eval3, ks, tol=CFG["tol"])
+    roots, _ = O.plain_sweep(evald, ks, tol=CFG["tol"])
     verified = 0
     for r in roots:
         lo = O.sv_derivs(*oso.gen_sol_op(r - CFG["tol"], CFG["c_o"], CFG["c_i"], d=1, threads=threads))[1]

@@ -56,9 +56,14 @@ __device__ __forceinline__ float warp_sumf(float x) {
 
 // Stage 1 of the mixed-precision path: one-sided Jacobi of T in FP32 (A32 and V32
 // both in shared memory), to the FP32 noise level.  Only V32 is used afterwards.
-__device__ void jacobi_fp32(const cplx* T0, int n, cpf* A32, cpf* V32, int* s_rot) {
+// Each column pair of a round-robin step is handled by a group of G lanes (G = 8 for
+// n <= 128: the 64 groups of a 512-thread CTA take a whole step at once, with
+// 3-level shuffle reductions), G = 32 for larger n.
+template <int G>
+__device__ void jacobi_fp32_g(const cplx* T0, int n, cpf* A32, cpf* V32, int* s_rot) {
     const int np = n + (n & 1), m = np - 1;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int gl = threadIdx.x % G, grp = threadIdx.x / G, ngrp = blockDim.x / G;
+    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
         cplx t = T0[e];
         A32[e] = mkf((float)t.re, (float)t.im);
@@ -70,7 +75,7 @@ __device__ void jacobi_fp32(const cplx* T0, int n, cpf* A32, cpf* V32, int* s_ro
         if (threadIdx.x == 0) *s_rot = 0;
         __syncthreads();
         for (int r = 0; r < m; ++r) {
-            for (int k = warp; k < np / 2; k += nw) {
+            for (int k = grp; k < np / 2; k += ngrp) {
                 int p, q;
                 rr_pair(r, k, m, p, q);
                 if (p >= n || q >= n) continue;
@@ -78,24 +83,30 @@ __device__ void jacobi_fp32(const cplx* T0, int n, cpf* A32, cpf* V32, int* s_ro
                 cpf* ap = A32 + p * n;
                 cpf* aq = A32 + q * n;
                 float al = 0.f, be = 0.f, gr = 0.f, gi = 0.f;
-                for (int i = lane; i < n; i += 32) {
+                for (int i = gl; i < n; i += G) {
                     cpf x = ap[i], y = aq[i];
                     al = fmaf(x.re, x.re, fmaf(x.im, x.im, al));
                     be = fmaf(y.re, y.re, fmaf(y.im, y.im, be));
                     gr = fmaf(x.re, y.re, fmaf(x.im, y.im, gr));
                     gi = fmaf(x.re, y.im, fmaf(-x.im, y.re, gi));
                 }
-                al = warp_sumf(al); be = warp_sumf(be); gr = warp_sumf(gr); gi = warp_sumf(gi);
+#pragma unroll
+                for (int o = G / 2; o > 0; o >>= 1) {
+                    al += __shfl_xor_sync(gmask, al, o);
+                    be += __shfl_xor_sync(gmask, be, o);
+                    gr += __shfl_xor_sync(gmask, gr, o);
+                    gi += __shfl_xor_sync(gmask, gi, o);
+                }
                 float g = hypotf(gr, gi);
                 if (g == 0.f || g <= tol * sqrtf(al * be)) continue;
-                if (lane == 0) *s_rot = 1;
+                if (gl == 0) *s_rot = 1;
                 float zeta = (be - al) / (2.f * g);
                 float t = (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
                 float c = 1.f / sqrtf(1.f + t * t), s = c * t;
                 float er = gr / g, ei = -gi / g;
                 cpf* vp = V32 + p * n;
                 cpf* vq = V32 + q * n;
-                for (int i = lane; i < n; i += 32) {
+                for (int i = gl; i < n; i += G) {
                     cpf x = ap[i], y0 = aq[i];
                     cpf y = mkf(er * y0.re - ei * y0.im, er * y0.im + ei * y0.re);
                     ap[i] = mkf(c * x.re - s * y.re, c * x.im - s * y.im);
@@ -111,6 +122,11 @@ __device__ void jacobi_fp32(const cplx* T0, int n, cpf* A32, cpf* V32, int* s_ro
         if (*s_rot == 0) break;
         __syncthreads();
     }
+}
+
+__device__ void jacobi_fp32(const cplx* T0, int n, cpf* A32, cpf* V32, int* s_rot) {
+    if (n <= 128) jacobi_fp32_g<8>(T0, n, A32, V32, s_rot);
+    else jacobi_fp32_g<32>(T0, n, A32, V32, s_rot);
 }
 
 // Stage 2: V = orthonormalised columns of V32 in FP64 (classical Gram-Schmidt; one
@@ -136,7 +152,7 @@ __device__ void orthonormalise_fp64(const cpf* V32, int n, cplx* V, cplx* vcol, 
         double part = 0.;
         for (int r = threadIdx.x; r < n; r += blockDim.x) {
             cplx s = vcol[r];
-            for (int i = 0; i < j; ++i) s -= V[(long long)i * n + r] * coef[i];
+            for (int i = 0; i < j; ++i) cfms(s, V[(long long)i * n + r], coef[i]);
             vcol[r] = s;
             part += norm2(s);
         }
@@ -157,7 +173,7 @@ __device__ void product_fp64(const cplx* T0, const cplx* V, int n, cplx* A) {
         const int r = e % n, c = e / n;
         const cplx* vc = V + (long long)c * n;
         cplx s = mk(0.);
-        for (int k = 0; k < n; ++k) s += T0[r + (long long)k * n] * vc[k];
+        for (int k = 0; k < n; ++k) cfma(s, T0[r + (long long)k * n], vc[k]);
         A[e] = s;
     }
     __syncthreads();
@@ -289,11 +305,11 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_jacobi(SvdJob J) {
     // y = T' v  (thread per row),  z = T'^H u (thread per column)
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
         cplx y = mk(0.);
-        for (int c = 0; c < n; ++c) y += T1[r + (long long)c * n] * vi[c];
+        for (int c = 0; c < n; ++c) cfma(y, T1[r + (long long)c * n], vi[c]);
         uy[r] = y;
         cplx z = mk(0.);
         const cplx* col = T1 + (long long)r * n;
-        for (int i = 0; i < n; ++i) z += conj(col[i]) * ui[i];
+        for (int i = 0; i < n; ++i) cfma_c(z, col[i], ui[i]);
         uz[r] = z;
     }
     __syncthreads();
@@ -304,8 +320,8 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_jacobi(SvdJob J) {
         const cplx* vj = V + (long long)j * n;
         cplx a = mk(0.), b = mk(0.);
         for (int i = 0; i < n; ++i) {
-            a += conj(aj[i]) * uy[i];
-            b += conj(vj[i]) * uz[i];
+            cfma_c(a, aj[i], uy[i]);
+            cfma_c(b, vj[i], uz[i]);
         }
         double sj = sig[j];
         a = (sj > 0. ? 1. / sj : 0.) * a;
@@ -329,7 +345,7 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_jacobi(SvdJob J) {
     const cplx* T2 = T0 + 2 * J.der_stride;
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
         cplx y = mk(0.);
-        for (int c = 0; c < n; ++c) y += T2[r + (long long)c * n] * vi[c];
+        for (int c = 0; c < n; ++c) cfma(y, T2[r + (long long)c * n], vi[c]);
         uy[r] = y;
     }
     __syncthreads();
@@ -416,7 +432,7 @@ struct SvdFastJob {
 };
 
 struct FastSmem {
-    size_t r0, x, y, w, rf, vec, coef, red, sig32, piv, redi, idx, sigb, ab, total;
+    size_t r0, x, y, w, rf, vec, coef, red, sig32, piv, perm, redi, idx, sigb, ab, total;
 };
 
 __host__ __device__ inline FastSmem fast_layout(int n) {
@@ -429,11 +445,12 @@ __host__ __device__ inline FastSmem fast_layout(int n) {
     L.y = take((size_t)n * K * c);
     L.w = take(K * K * c);
     L.rf = take(K * K * c);
-    L.vec = take(8 * (size_t)n * c);
+    L.vec = take(9 * (size_t)n * c);
     L.coef = take(K * c);
     L.red = take(128 * sizeof(double));
     L.sig32 = take((size_t)n * sizeof(float));
     L.piv = take((size_t)n * sizeof(int));
+    L.perm = take((size_t)n * sizeof(int));
     L.redi = take(32 * sizeof(int));
     L.idx = take(K * sizeof(int));
     L.sigb = take(K * sizeof(double));
@@ -448,7 +465,7 @@ size_t svd_fast_smem_bytes(int n) { return fast_layout(n).total; }
 static __device__ void gemv_n(const cplx* A, int n, const cplx* x, cplx* y) {
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
         cplx a = mk(0.);
-        for (int c = 0; c < n; ++c) a += A[r + (long long)c * n] * x[c];
+        for (int c = 0; c < n; ++c) cfma(a, A[r + (long long)c * n], x[c]);
         y[r] = a;
     }
     __syncthreads();
@@ -494,7 +511,7 @@ static __device__ void dots_h(const cplx* B, int n, int kb, const cplx* x, cplx*
 static __device__ void sub_span(const cplx* B, int n, int kb, const cplx* c, cplx* x) {
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
         cplx v = x[r];
-        for (int j = 0; j < kb; ++j) v -= B[r + (long long)j * n] * c[j];
+        for (int j = 0; j < kb; ++j) cfms(v, B[r + (long long)j * n], c[j]);
         x[r] = v;
     }
     __syncthreads();
@@ -517,7 +534,7 @@ static __device__ void rows_times(cplx* B, int n, int kb, const cplx* M) {
             cplx a = mk(0.);
 #pragma unroll
             for (int l = 0; l < kFastKmax; ++l)
-                if (l < kb) a += row[l] * M[l + j * kb];
+                if (l < kb) cfma(a, row[l], M[l + j * kb]);
             outr[j] = a;
         }
 #pragma unroll
@@ -544,12 +561,13 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
     double* red = reinterpret_cast<double*>(sb + L.red);
     float* sig32 = reinterpret_cast<float*>(sb + L.sig32);
     int* piv = reinterpret_cast<int*>(sb + L.piv);
+    int* perm = reinterpret_cast<int*>(sb + L.perm);
     int* redi = reinterpret_cast<int*>(sb + L.redi);
     int* idx = reinterpret_cast<int*>(sb + L.idx);
     double* sigb = reinterpret_cast<double*>(sb + L.sigb);
     cplx* ab = reinterpret_cast<cplx*>(sb + L.ab);   // a_j, b_j
     cplx *F = vec, *G = vec + n, *f1 = vec + 2 * n, *f2 = vec + 3 * n, *rr = vec + 4 * n, *acc = vec + 5 * n,
-         *term = vec + 6 * n, *z2 = vec + 7 * n;
+         *term = vec + 6 * n, *z2 = vec + 7 * n, *sbuf = vec + 8 * n;
     __shared__ int s_rot, s_kb, s_im, s_sing, s_conv;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const cplx* T0 = J.T + (long long)mat * J.mat_stride;
@@ -597,10 +615,11 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) T64[e] = T0[e];
     __syncthreads();
     lu_smem(T64, n, piv, red, redi, &s_sing);
+    perm_from_piv(piv, n, perm);
     qr_cgs2(X, n, kb, coef, red);
     for (int it = 0; it < kFastInvIter; ++it) {
-        solve_lu_h(T64, piv, n, X, kb);
-        solve_lu(T64, piv, n, X, kb);
+        solve_lu_h_blk(T64, perm, n, X, kb, sbuf);
+        solve_lu_blk(T64, perm, n, X, kb, sbuf);
         qr_cgs2(X, n, kb, coef, red);
     }
     // Rayleigh-Ritz: Y = T X = Q_Y Rf, Rf W = Q_R Sigma
@@ -612,7 +631,7 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
             const cplx t = T0[r + (long long)c * n];
 #pragma unroll
             for (int j = 0; j < kFastKmax; ++j)
-                if (j < kb) a[j] += t * X[c + j * n];
+                if (j < kb) cfma(a[j], t, X[c + j * n]);
         }
 #pragma unroll
         for (int j = 0; j < kFastKmax; ++j)
@@ -731,8 +750,8 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
     const double s2 = sg * sg;
     for (int r = threadIdx.x; r < n; r += blockDim.x) { yv[r] = mk(0.); zv[r] = rr[r]; }
     __syncthreads();
-    solve_lu(T64, piv, n, zv, 1);                 // z = T^-H T^-1 res
-    solve_lu_h(T64, piv, n, zv, 1);
+    solve_lu_blk(T64, perm, n, zv, 1, sbuf);                 // z = T^-H T^-1 res
+    solve_lu_h_blk(T64, perm, n, zv, 1, sbuf);
     dots_h(Y, n, nd, zv, coef);
     sub_span(Y, n, nd, coef, zv);
     for (int r = threadIdx.x; r < n; r += blockDim.x) pv[r] = zv[r];
@@ -756,8 +775,8 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
             zv[r] = rr[r];
         }
         __syncthreads();
-        solve_lu(T64, piv, n, zv, 1);
-        solve_lu_h(T64, piv, n, zv, 1);
+        solve_lu_blk(T64, perm, n, zv, 1, sbuf);
+        solve_lu_h_blk(T64, perm, n, zv, 1, sbuf);
         dots_h(Y, n, nd, zv, coef);
         sub_span(Y, n, nd, coef, zv);
         const double rz1 = dot_re(rr, zv, n, red + 64);

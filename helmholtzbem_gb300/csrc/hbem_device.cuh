@@ -71,6 +71,41 @@ __device__ __forceinline__ cplxf cdiv(cplxf a, cplxf b) {
     return mkf((ar * br + ai * bi) * d, (ai * br - ar * bi) * d);
 }
 
+// Fused complex multiply-accumulate: four FMAs instead of the two multiplies, two
+// FMAs and two adds of acc += a * b (the compiler may not reassociate the latter).
+__device__ __forceinline__ void cfma(cplx& acc, cplx a, cplx b) {      // acc += a b
+    acc.re = fma(a.re, b.re, fma(-a.im, b.im, acc.re));
+    acc.im = fma(a.re, b.im, fma(a.im, b.re, acc.im));
+}
+__device__ __forceinline__ void cfms(cplx& acc, cplx a, cplx b) {      // acc -= a b
+    acc.re = fma(-a.re, b.re, fma(a.im, b.im, acc.re));
+    acc.im = fma(-a.re, b.im, fma(-a.im, b.re, acc.im));
+}
+__device__ __forceinline__ void cfma_c(cplx& acc, cplx a, cplx b) {    // acc += conj(a) b
+    acc.re = fma(a.re, b.re, fma(a.im, b.im, acc.re));
+    acc.im = fma(a.re, b.im, fma(-a.im, b.re, acc.im));
+}
+__device__ __forceinline__ void cfms_c(cplx& acc, cplx a, cplx b) {    // acc -= conj(a) b
+    acc.re = fma(-a.re, b.re, fma(-a.im, b.im, acc.re));
+    acc.im = fma(-a.re, b.im, fma(a.im, b.re, acc.im));
+}
+__device__ __forceinline__ void cfma(cplxf& acc, cplxf a, cplxf b) {
+    acc.re = fmaf(a.re, b.re, fmaf(-a.im, b.im, acc.re));
+    acc.im = fmaf(a.re, b.im, fmaf(a.im, b.re, acc.im));
+}
+__device__ __forceinline__ void cfms(cplxf& acc, cplxf a, cplxf b) {
+    acc.re = fmaf(-a.re, b.re, fmaf(a.im, b.im, acc.re));
+    acc.im = fmaf(-a.re, b.im, fmaf(-a.im, b.re, acc.im));
+}
+__device__ __forceinline__ void cfma_c(cplxf& acc, cplxf a, cplxf b) {
+    acc.re = fmaf(a.re, b.re, fmaf(a.im, b.im, acc.re));
+    acc.im = fmaf(a.re, b.im, fmaf(-a.im, b.re, acc.im));
+}
+__device__ __forceinline__ void cfms_c(cplxf& acc, cplxf a, cplxf b) {
+    acc.re = fmaf(-a.re, b.re, fmaf(-a.im, b.im, acc.re));
+    acc.im = fmaf(-a.re, b.im, fmaf(a.im, b.re, acc.im));
+}
+
 // element-type helpers for code templated on cplx / cplxf
 template <class E> struct Elem;
 template <> struct Elem<cplx> {

@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(kLuPanelThreads) k_lu_panel(int n, int k0, int
         for (int i = c + 1 + threadIdx.x; i < n; i += blockDim.x) {
             E l = at(i, j);
             if (nz) { l = l * id; at(i, j) = l; }
-            for (int cc = j + 1; cc < nb; ++cc) at(i, cc) -= l * prow[cc];
+            for (int cc = j + 1; cc < nb; ++cc) cfms(at(i, cc), l, prow[cc]);
         }
         __syncthreads();
     }
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(kLuPanelThreads) k_lu_panel_cluster(int n, int
         for (int i = max(c + 1, r0) + threadIdx.x; i < r1; i += blockDim.x) {
             E l = P[(i - r0) + j * R];
             if (nz) { l = l * id; P[(i - r0) + j * R] = l; }
-            for (int cc = j + 1; cc < nb; ++cc) P[(i - r0) + cc * R] -= l * prow[cc];
+            for (int cc = j + 1; cc < nb; ++cc) cfms(P[(i - r0) + cc * R], l, prow[cc]);
         }
         __syncthreads();
     }
@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(256) k_lu_swap_trsm(int n, int k0, int nb, E* 
             E xk;
             xk.re = __shfl_sync(0xffffffffu, x.re, k);
             xk.im = __shfl_sync(0xffffffffu, x.im, k);
-            if (lane > k && lane < nb) x -= L11[lane][k] * xk;
+            if (lane > k && lane < nb) cfms(x, L11[lane][k], xk);
         }
         if (lane < nb) a[lane] = x;
     }
@@ -351,7 +351,7 @@ __device__ void lu_solve_n(const E* M, const int* perm, int n, E* X, int s, E* s
                     E vk;
                     vk.re = __shfl_sync(0xffffffffu, v.re, k);
                     vk.im = __shfl_sync(0xffffffffu, v.im, k);
-                    if (lane > k && lane < bs) v -= D[lane][k] * vk;
+                    if (lane > k && lane < bs) cfms(v, D[lane][k], vk);
                 }
                 if (lane < bs) { x[lane] = v; xb[c * kLuNB + lane] = v; }
             }
@@ -364,7 +364,7 @@ __device__ void lu_solve_n(const E* M, const int* perm, int n, E* X, int s, E* s
                     const E l = M[i + (long long)(b0 + k) * n];
 #pragma unroll
                     for (int c = 0; c < CH; ++c)
-                        if (c < cs) acc[c] += l * xb[c * kLuNB + k];
+                        if (c < cs) cfma(acc[c], l, xb[c * kLuNB + k]);
                 }
 #pragma unroll
                 for (int c = 0; c < CH; ++c)
@@ -390,7 +390,7 @@ __device__ void lu_solve_n(const E* M, const int* perm, int n, E* X, int s, E* s
                     E vk;
                     vk.re = __shfl_sync(0xffffffffu, v.re, k);
                     vk.im = __shfl_sync(0xffffffffu, v.im, k);
-                    if (lane < k) v -= D[lane][k] * vk;
+                    if (lane < k) cfms(v, D[lane][k], vk);
                 }
                 if (lane < bs) { x[lane] = v; xb[c * kLuNB + lane] = v; }
             }
@@ -403,7 +403,7 @@ __device__ void lu_solve_n(const E* M, const int* perm, int n, E* X, int s, E* s
                     const E u = M[i + (long long)(b0 + k) * n];
 #pragma unroll
                     for (int c = 0; c < CH; ++c)
-                        if (c < cs) acc[c] += u * xb[c * kLuNB + k];
+                        if (c < cs) cfma(acc[c], u, xb[c * kLuNB + k]);
                 }
 #pragma unroll
                 for (int c = 0; c < CH; ++c)
@@ -426,7 +426,7 @@ __device__ __forceinline__ void warp_dots_h(const E* a, const E* X, int n, int k
         const E u = conj(a[k]);
 #pragma unroll
         for (int c = 0; c < CH; ++c)
-            if (c < cs) acc[c] += u * X[k + (long long)c * n];
+            if (c < cs) cfma(acc[c], u, X[k + (long long)c * n]);
     }
 #pragma unroll
     for (int c = 0; c < CH; ++c) {
@@ -473,7 +473,7 @@ __device__ void lu_solve_h(const E* M, const int* perm, int n, E* X, int s, E* s
                     E vk;
                     vk.re = __shfl_sync(0xffffffffu, v.re, k);
                     vk.im = __shfl_sync(0xffffffffu, v.im, k);
-                    if (lane > k && lane < bs) v -= conj(D[k][lane]) * vk;
+                    if (lane > k && lane < bs) cfms_c(v, D[k][lane], vk);
                 }
                 if (lane < bs) x[lane] = v;
             }
@@ -506,7 +506,7 @@ __device__ void lu_solve_h(const E* M, const int* perm, int n, E* X, int s, E* s
                     E vk;
                     vk.re = __shfl_sync(0xffffffffu, v.re, k);
                     vk.im = __shfl_sync(0xffffffffu, v.im, k);
-                    if (lane < k) v -= conj(D[k][lane]) * vk;
+                    if (lane < k) cfms_c(v, D[k][lane], vk);
                 }
                 if (lane < bs) x[lane] = v;
             }

@@ -195,18 +195,37 @@ int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npo
     const double h = (k_max - k_min) / (npoints - 1);
     for (int i = 0; i < npoints; ++i) ks[i] = k_min + i * h;
     int evals = npoints;
-    if (int r = hbem_sweep_sigma(s, ks.data(), npoints, c_o, c_i, 2, g.data())) return r;
-    if (grid_host) std::copy(g.begin(), g.end(), grid_host);
-    // 3-point minima, validated by the derivative signs at the bracket ends
+    // sigma on the grid (randomized_svd::sv / direct::sv at roots_newton_polygon_rsvd.cpp:172-177)
+    if (int r = hbem_sweep_sigma(s, ks.data(), npoints, c_o, c_i, 0, g.data())) return r;
+    for (int i = 0; i < npoints; ++i) g[3 * i + 1] = g[3 * i + 2] = NAN;
+    // 3-point local minima (:185-194)
+    std::vector<int> cidx;
+    for (int i = 0; i + 2 < npoints; ++i) {
+        const double L = g[3 * i], C = g[3 * (i + 1)], R = g[3 * (i + 2)];
+        if (L - C > 0. && R - C > 0.) cidx.push_back(i);
+    }
+    // sigma' at both bracket ends of every candidate in one batch (sv_der, :204-208)
+    std::vector<double> ends(2 * cidx.size()), der(6 * cidx.size());
+    for (size_t c = 0; c < cidx.size(); ++c) {
+        ends[2 * c] = ks[cidx[c]];
+        ends[2 * c + 1] = ks[cidx[c] + 2];
+    }
+    if (!ends.empty()) {
+        if (int r = hbem_sweep_sigma(s, ends.data(), (int)ends.size(), c_o, c_i, 1, der.data())) return r;
+        evals += (int)ends.size();
+    }
+    // validation sigma'(left) < 0 < sigma'(right), quartic Hermite model + Brent (:209-245)
     struct Cand { double a, guess; };
     std::vector<Cand> cands;
-    for (int i = 0; i + 2 < npoints; ++i) {
-        double L = g[3 * i], C = g[3 * (i + 1)], R = g[3 * (i + 2)];
-        if (!(L - C > 0. && R - C > 0.)) continue;
-        double d1 = g[3 * i + 1], d2 = g[3 * (i + 2) + 1];
+    for (size_t c = 0; c < cidx.size(); ++c) {
+        const int i = cidx[c];
+        const double d1 = der[3 * (2 * c) + 1], d2 = der[3 * (2 * c + 1) + 1];
+        g[3 * i + 1] = d1;
+        g[3 * (i + 2) + 1] = d2;
         if (!(d1 < 0. && d2 > 0.)) continue;
-        cands.push_back(Cand{ks[i], quartic_guess(ks[i], h, L, C, R, d1, d2, tol)});
+        cands.push_back(Cand{ks[i], quartic_guess(ks[i], h, g[3 * i], g[3 * (i + 1)], g[3 * (i + 2)], d1, d2, tol)});
     }
+    if (grid_host) std::copy(g.begin(), g.end(), grid_host);
     std::vector<Newton> nt(cands.size());
     for (size_t c = 0; c < cands.size(); ++c) nt[c].start(cands[c].a, cands[c].a + 2 * h, cands[c].guess, tol);
     // lock-step Newton rounds: one batched sigma', sigma'' evaluation per round

@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(kRsvdThreads) k_rsvd_small(RsvdJob J) {
     const cplx* w = W + bj * s;
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
         cplx v = mk(0.);
-        for (int c = 0; c < s; ++c) v += X[c * n + r] * w[c];
+        for (int c = 0; c < s; ++c) cfma(v, X[c * n + r], w[c]);
         vb[r] = v;
     }
     __syncthreads();
@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(kRsvdThreads) k_rsvd_tail(int n, int s, int D,
     cplx* v = uv + 2LL * n * mat + n;
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
         cplx b = mk(0.);
-        for (int c = 0; c < s; ++c) b += Qm[r + (long long)c * n] * tw[c];
+        for (int c = 0; c < s; ++c) cfma(b, Qm[r + (long long)c * n], tw[c]);
         v[r] = b;
     }
 }
@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(kRsvdThreads) k_rsvd_vec(int n, int D, const c
     part = 0.;
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
         cplx a = mk(0.);
-        for (int c = 0; c < n; ++c) a += Tm[r + (long long)c * n] * v[c];
+        for (int c = 0; c < n; ++c) cfma(a, Tm[r + (long long)c * n], v[c]);
         u[r] = a;
         part += norm2(a);
     }
@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(kRsvdThreads) k_rsvd_vec(int n, int D, const c
     part = 0.;
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
         cplx tv = mk(0.);
-        for (int c = 0; c < n; ++c) tv += T1[r + (long long)c * n] * v[c];
+        for (int c = 0; c < n; ++c) cfma(tv, T1[r + (long long)c * n], v[c]);
         const cplx ur = iu * u[r];
         u[r] = ur;
         part += ur.re * tv.re + ur.im * tv.im;
@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(256) k_wapply(int n, const cplx* A, long long 
     cplx* y2 = y1 + n;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         cplx sacc = mk(0.);
-        for (int j = 0; j < n; ++j) sacc += Am[i + (long long)j * n] * x2[j];
+        for (int j = 0; j < n; ++j) cfma(sacc, Am[i + (long long)j * n], x2[j]);
         y1[i] = acc ? y1[i] + alpha * sacc : alpha * sacc;
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -323,7 +323,7 @@ __global__ void k_sv2_extract(int n, int nmat, cplx* ud, const int* mcol, cplx* 
 __global__ void k_sv2_axpy(int n, cplx* rhs, const cplx* ud, const cplx* tb) {
     const int mat = blockIdx.x, n2 = 2 * n;
     const cplx t2 = 2. * tb[mat];
-    for (int l = threadIdx.x; l < n2; l += blockDim.x) rhs[(long long)n2 * mat + l] -= t2 * ud[(long long)n2 * mat + l];
+    for (int l = threadIdx.x; l < n2; l += blockDim.x) cfms(rhs[(long long)n2 * mat + l], t2, ud[(long long)n2 * mat + l]);
 }
 
 __global__ void k_sv2_out(int n, int nmat, const cplx* sol, const int* mcol, const int* info, double* out) {
@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(256) k_resid_n(int n, int s, const cplx* T, lo
             const cplx t = Tm[i + (long long)r * n];
 #pragma unroll
             for (int c = 0; c < kResChunk; ++c)
-                if (c < cs) acc[c] += t * Xm[r + (long long)(cb + c) * n];
+                if (c < cs) cfma(acc[c], t, Xm[r + (long long)(cb + c) * n]);
         }
 #pragma unroll
         for (int c = 0; c < kResChunk; ++c)
@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(256) k_resid_h(int n, int s, const cplx* T, lo
             const cplx t = conj(col[r]);
 #pragma unroll
             for (int c = 0; c < kResChunk; ++c)
-                if (c < cs) acc[c] += t * Xm[r + (long long)(cb + c) * n];
+                if (c < cs) cfma(acc[c], t, Xm[r + (long long)(cb + c) * n]);
         }
 #pragma unroll
         for (int c = 0; c < kResChunk; ++c) {

@@ -65,7 +65,7 @@ static __device__ void lu_smem(cplx* A, int n, int* piv, double* redv, int* redi
         const int m = n - k - 1;
         for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
             const int i = k + 1 + e % m, j = k + 1 + e / m;
-            A[i + (long long)j * n] -= A[i + (long long)k * n] * A[k + (long long)j * n];
+            cfms(A[i + (long long)j * n], A[i + (long long)k * n], A[k + (long long)j * n]);
         }
         __syncthreads();
     }
@@ -86,7 +86,7 @@ static __device__ void solve_lu(const cplx* A, const int* piv, int n, cplx* X, i
     for (int k = 0; k < n; ++k) {          // L y = P b (unit diagonal)
         for (int e = threadIdx.x; e < (n - k - 1) * s; e += blockDim.x) {
             const int i = k + 1 + e % (n - k - 1), c = e / (n - k - 1);
-            X[i + c * n] -= A[i + (long long)k * n] * X[k + c * n];
+            cfms(X[i + c * n], A[i + (long long)k * n], X[k + c * n]);
         }
         __syncthreads();
     }
@@ -95,7 +95,7 @@ static __device__ void solve_lu(const cplx* A, const int* piv, int n, cplx* X, i
         __syncthreads();
         for (int e = threadIdx.x; e < k * s; e += blockDim.x) {
             const int i = e % k, c = e / k;
-            X[i + c * n] -= A[i + (long long)k * n] * X[k + c * n];
+            cfms(X[i + c * n], A[i + (long long)k * n], X[k + c * n]);
         }
         __syncthreads();
     }
@@ -108,14 +108,14 @@ static __device__ void solve_lu_h(const cplx* A, const int* piv, int n, cplx* X,
         __syncthreads();
         for (int e = threadIdx.x; e < (n - k - 1) * s; e += blockDim.x) {
             const int i = k + 1 + e % (n - k - 1), c = e / (n - k - 1);
-            X[i + c * n] -= conj(A[k + (long long)i * n]) * X[k + c * n];
+            cfms_c(X[i + c * n], A[k + (long long)i * n], X[k + c * n]);
         }
         __syncthreads();
     }
     for (int k = n - 1; k >= 0; --k) {     // L^H z = y (unit upper triangular)
         for (int e = threadIdx.x; e < k * s; e += blockDim.x) {
             const int i = e % k, c = e / k;
-            X[i + c * n] -= conj(A[k + (long long)i * n]) * X[k + c * n];
+            cfms_c(X[i + c * n], A[k + (long long)i * n], X[k + c * n]);
         }
         __syncthreads();
     }
@@ -161,7 +161,7 @@ static __device__ void qr_cgs2(cplx* X, int n, int s, cplx* coef, double* red, c
                 for (int i = threadIdx.x; i < j; i += blockDim.x) Rf[i + j * s] += coef[i];
             for (int r = threadIdx.x; r < n; r += blockDim.x) {
                 cplx v = xj[r];
-                for (int i = 0; i < j; ++i) v -= X[(long long)i * n + r] * coef[i];
+                for (int i = 0; i < j; ++i) cfms(v, X[(long long)i * n + r], coef[i]);
                 xj[r] = v;
             }
             __syncthreads();
@@ -264,6 +264,150 @@ static __device__ void jacobi_warp(cplx* B, int s, cplx* W) {
             }
         if (!rotated) break;
     }
+}
+
+
+// ---------------------------------------------------------------- blocked solves
+//
+// The same two solves with the row exchanges composed into one permutation
+// (perm[i] = source row of row i of P T) and the triangular sweeps blocked by 32
+// rows: one warp per right-hand side solves the 32 x 32 diagonal block with
+// shuffles, then all threads update the remaining rows -- two barriers per block
+// instead of two per row.  buf: n entries of scratch; A, X may be in shared or
+// global memory.
+
+static __device__ void perm_from_piv(const int* piv, int n, int* perm) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = i;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int k = 0; k < n; ++k) {
+            const int p = piv[k];
+            if (p != k) { const int t = perm[k]; perm[k] = perm[p]; perm[p] = t; }
+        }
+    __syncthreads();
+}
+
+static __device__ void permute_cols(cplx* X, int n, int s, const int* perm, cplx* buf, bool inverse) {
+    for (int c = 0; c < s; ++c) {
+        cplx* x = X + (long long)c * n;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) buf[i] = x[i];
+        __syncthreads();
+        if (!inverse)
+            for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = buf[perm[i]];
+        else
+            for (int i = threadIdx.x; i < n; i += blockDim.x) x[perm[i]] = buf[i];
+        __syncthreads();
+    }
+}
+
+// X <- T^-1 X
+static __device__ void solve_lu_blk(const cplx* A, const int* perm, int n, cplx* X, int s, cplx* buf) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    permute_cols(X, n, s, perm, buf, false);
+    for (int b0 = 0; b0 < n; b0 += 32) {                       // L y = P b, L unit lower
+        const int bs = min(32, n - b0);
+        for (int c = warp; c < s; c += nw) {
+            cplx* x = X + (long long)c * n + b0;
+            cplx v = lane < bs ? x[lane] : mk(0.);
+            for (int k = 0; k < bs; ++k) {
+                cplx vk;
+                vk.re = __shfl_sync(0xffffffffu, v.re, k);
+                vk.im = __shfl_sync(0xffffffffu, v.im, k);
+                if (lane > k && lane < bs) cfms(v, A[(b0 + lane) + (long long)(b0 + k) * n], vk);
+            }
+            if (lane < bs) x[lane] = v;
+        }
+        __syncthreads();
+        const int rest = n - b0 - bs;
+        for (int e = threadIdx.x; e < rest * s; e += blockDim.x) {
+            const int i = b0 + bs + e % rest, c = e / rest;
+            const cplx* xb = X + (long long)c * n + b0;
+            cplx acc = mk(0.);
+            for (int k = 0; k < bs; ++k) cfma(acc, A[i + (long long)(b0 + k) * n], xb[k]);
+            X[i + (long long)c * n] -= acc;
+        }
+        __syncthreads();
+    }
+    for (int b0 = ((n - 1) / 32) * 32; b0 >= 0; b0 -= 32) {    // U x = y
+        const int bs = min(32, n - b0);
+        for (int c = warp; c < s; c += nw) {
+            cplx* x = X + (long long)c * n + b0;
+            cplx v = lane < bs ? x[lane] : mk(0.);
+            for (int k = bs - 1; k >= 0; --k) {
+                if (lane == k) v = cdiv(v, A[(b0 + k) + (long long)(b0 + k) * n]);
+                cplx vk;
+                vk.re = __shfl_sync(0xffffffffu, v.re, k);
+                vk.im = __shfl_sync(0xffffffffu, v.im, k);
+                if (lane < k) cfms(v, A[(b0 + lane) + (long long)(b0 + k) * n], vk);
+            }
+            if (lane < bs) x[lane] = v;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < b0 * s; e += blockDim.x) {
+            const int i = e % b0, c = e / b0;
+            const cplx* xb = X + (long long)c * n + b0;
+            cplx acc = mk(0.);
+            for (int k = 0; k < bs; ++k) cfma(acc, A[i + (long long)(b0 + k) * n], xb[k]);
+            X[i + (long long)c * n] -= acc;
+        }
+        __syncthreads();
+    }
+}
+
+// X <- T^-H X:  T^H = U^H L^H P, x = P^T L^-H U^-H b
+static __device__ void solve_lu_h_blk(const cplx* A, const int* perm, int n, cplx* X, int s, cplx* buf) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int b0 = 0; b0 < n; b0 += 32) {                       // U^H y = b (lower, diagonal conj(u_kk))
+        const int bs = min(32, n - b0);
+        for (int c = warp; c < s; c += nw) {
+            cplx* x = X + (long long)c * n + b0;
+            cplx v = lane < bs ? x[lane] : mk(0.);
+            for (int k = 0; k < bs; ++k) {
+                if (lane == k) v = cdiv(v, conj(A[(b0 + k) + (long long)(b0 + k) * n]));
+                cplx vk;
+                vk.re = __shfl_sync(0xffffffffu, v.re, k);
+                vk.im = __shfl_sync(0xffffffffu, v.im, k);
+                if (lane > k && lane < bs) cfms_c(v, A[(b0 + k) + (long long)(b0 + lane) * n], vk);
+            }
+            if (lane < bs) x[lane] = v;
+        }
+        __syncthreads();
+        const int rest = n - b0 - bs;
+        for (int e = threadIdx.x; e < rest * s; e += blockDim.x) {
+            const int i = b0 + bs + e % rest, c = e / rest;
+            const cplx* xb = X + (long long)c * n + b0;
+            const cplx* col = A + (long long)i * n + b0;        // U[b0.., i]
+            cplx acc = mk(0.);
+            for (int k = 0; k < bs; ++k) cfma_c(acc, col[k], xb[k]);
+            X[i + (long long)c * n] -= acc;
+        }
+        __syncthreads();
+    }
+    for (int b0 = ((n - 1) / 32) * 32; b0 >= 0; b0 -= 32) {    // L^H z = y (unit upper)
+        const int bs = min(32, n - b0);
+        for (int c = warp; c < s; c += nw) {
+            cplx* x = X + (long long)c * n + b0;
+            cplx v = lane < bs ? x[lane] : mk(0.);
+            for (int k = bs - 1; k >= 0; --k) {
+                cplx vk;
+                vk.re = __shfl_sync(0xffffffffu, v.re, k);
+                vk.im = __shfl_sync(0xffffffffu, v.im, k);
+                if (lane < k) cfms_c(v, A[(b0 + k) + (long long)(b0 + lane) * n], vk);
+            }
+            if (lane < bs) x[lane] = v;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < b0 * s; e += blockDim.x) {
+            const int i = e % b0, c = e / b0;
+            const cplx* xb = X + (long long)c * n + b0;
+            const cplx* col = A + (long long)i * n + b0;        // L[b0.., i]
+            cplx acc = mk(0.);
+            for (int k = 0; k < bs; ++k) cfma_c(acc, col[k], xb[k]);
+            X[i + (long long)c * n] -= acc;
+        }
+        __syncthreads();
+    }
+    permute_cols(X, n, s, perm, buf, true);
 }
 
 }  // namespace hbem

@@ -198,11 +198,13 @@ int hbem_sweep_sigma(hbem_solop s, const double* k_host, int nk, double c_o, dou
 
 /* Plain resonance search on [k_min, k_max] with npoints grid points
  * (examples/roots_newton_polygon_rsvd.cpp:172-265 with the dense sigma of
- * examples/roots_newton_circle.cpp): grid sweep of sigma, sigma', sigma''; 3-point
- * local minima; validation sigma'(left) < 0 < sigma'(right); quartic Hermite model
- * minimised by Brent; rtsafe on sigma' with sigma'' to tolerance tol.
+ * examples/roots_newton_circle.cpp): sigma on the grid; 3-point local minima;
+ * sigma' at both bracket ends (one batch), validation sigma'(left) < 0 <
+ * sigma'(right); quartic Hermite model minimised by Brent; rtsafe on sigma' with
+ * sigma'' to tolerance tol, all candidates' Newton steps in one batch per round.
  * roots_host receives up to max_roots roots, *nroots their count; grid_host
- * (npoints x 3, may be NULL) the grid values; *n_evals the number of T(k) evaluated. */
+ * (npoints x 3, may be NULL) sigma at every grid point and sigma' at the bracket
+ * ends (NaN where not evaluated); *n_evals the number of T(k) evaluated.        */
 int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npoints, double c_o, double c_i,
                                double tol, double* roots_host, int max_roots, int* nroots, double* grid_host,
                                int* n_evals);

@@ -597,32 +597,36 @@ def quartic_guess(a, h, f1, f0, f2, d1, d2, tol):
     return BrentMin(a, a + 2 * h, tol).minimize(lambda t: (((A * t + B) * t + C) * t + D) * t + E)
 
 
-def plain_sweep(eval3, ks, tol=1e-8):
-    """Plain sweep: sigma, sigma', sigma'' on the grid -> 3-point minima -> validate
-    sigma'(left) < 0 < sigma'(right) -> quartic + Brent guess -> rtsafe on sigma'.
-    ``eval3(list_of_k) -> array (len, 3)``.  Returns (roots, grid values)."""
+def plain_sweep(evald, ks, tol=1e-8):
+    """The plain search of examples/roots_newton_polygon_rsvd.cpp:172-265: sigma on
+    the grid -> 3-point local minima -> sigma' at both bracket ends, validation
+    sigma'(left) < 0 < sigma'(right) -> quartic Hermite + Brent guess -> rtsafe on
+    sigma' with sigma''.  ``evald(list_of_k, d) -> array (len, >= d + 1)`` gives sigma
+    and its first d derivatives.  Returns (roots, grid sigma)."""
     ks = np.asarray(ks, float)
-    vals = np.asarray(eval3(list(ks)))
+    sig = np.asarray(evald(list(ks), 0))[:, 0]
     h = ks[1] - ks[0]
+    cands = [i for i in range(len(ks) - 2) if sig[i] - sig[i + 1] > 0.0 and sig[i + 2] - sig[i + 1] > 0.0]
+    ends = []
+    for i in cands:
+        ends += [ks[i], ks[i + 2]]
+    der = np.asarray(evald(ends, 1))[:, 1] if ends else np.zeros(0)
     roots = []
-    for i in range(len(ks) - 2):
-        L, cval, R = vals[i, 0], vals[i + 1, 0], vals[i + 2, 0]
-        if not (L - cval > 0.0 and R - cval > 0.0):
-            continue
-        d1, d2 = vals[i, 1], vals[i + 2, 1]
+    for c, i in enumerate(cands):
+        d1, d2 = der[2 * c], der[2 * c + 1]
         if not (d1 < 0.0 < d2):
             continue
         a = ks[i]
-        guess = quartic_guess(a, h, L, cval, R, d1, d2, tol)
+        guess = quartic_guess(a, h, sig[i], sig[i + 1], sig[i + 2], d1, d2, tol)
 
         def fn(x, g=guess):
             return float("nan") if x == x else g
 
         def both(x):
-            r = eval3([x])[0]
+            r = evald([x], 2)[0]
             return r[1], r[2]
 
         root, ok, _ = rtsafe(fn, both, a, a + 2 * h, tol)
         if ok and root == root:
             roots.append(root)
-    return np.array(roots), vals
+    return np.array(roots), sig

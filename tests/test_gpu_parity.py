@@ -143,10 +143,11 @@ def test_find_resonances_plain_vs_oracle():
     c_o, c_i = 1.0, 23.4
     roots, grid, nev = so.find_resonances_plain(0.5, 6.0, 60, c_o, c_i, tol=1e-8)
 
-    def eval3(klist):
-        return np.array([O.sv_derivs(*oso.gen_sol_op(k, c_o, c_i, d=2)) for k in klist])
+    def evald(klist, d):
+        return np.array([O.sv_derivs(*oso.gen_sol_op(k, c_o, c_i, d=d)) for k in klist])
 
-    oroots, ogrid = O.plain_sweep(eval3, np.linspace(0.5, 6.0, 60), tol=1e-8)
+    oroots, osig = O.plain_sweep(evald, np.linspace(0.5, 6.0, 60), tol=1e-8)
+    assert np.max(np.abs(grid[:, 0] - osig) / osig) < 1e-10
     assert len(roots) == len(oroots) and len(roots) > 0
     assert np.max(np.abs(np.sort(roots) - np.sort(oroots))) <= 1e-8
     lo = so.sweep_sigma(roots - 1e-8, c_o, c_i, d=1)[:, 1]

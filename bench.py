@@ -44,6 +44,10 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample-points", type=int, default=60)
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline leg")
+    ap.add_argument("--profile-search", action="store_true",
+                    help="no timing: one plain search of the workload (for launch-list captures)")
+    ap.add_argument("--profile-dense-tail", action="store_true",
+                    help="no timing: FP64 and complex-FP32 LU + rSVD of 4 matrices of order 1600 (for captures)")
     ap.add_argument("--profile-case", action="store_true",
                     help="no timing: three sigma sweeps over 16 wavenumbers of the workload (for ncu captures)")
     return ap.parse_args()
@@ -59,6 +63,37 @@ def run_profile_case():
     for _ in range(3):
         out = so.sweep_sigma(ks, CFG["c_o"], CFG["c_i"], d=2)
     print("profile case done, sigma_min(k0) = %.6e" % out[0, 0])
+
+
+def run_profile_search():
+    """One plain search of the workload (grid, bracket-end sigma', Newton rounds)."""
+    from helmholtzbem_gb300 import api, geometry
+    data = api.BuilderData(geometry.circle(CFG["radius"], CFG["N"]), order=CFG["order"])
+    so = api.SolutionsOperator(data)
+    roots, grid, nev = so.find_resonances_plain(CFG["k_min"], CFG["k_max"], CFG["npoints"], CFG["c_o"], CFG["c_i"],
+                                                tol=CFG["tol"])
+    print("profile search done: %d roots, %d T(k) evaluations" % (roots.size, nev))
+
+
+def run_profile_dense_tail():
+    """Batched LU (complex128 and complex64) and randomized SVD (FP64 and mixed) of
+    four matrices of order 1600 from the star polygon N = 800 at k = 3, 7.5, 12.25, 19."""
+    import ctypes
+    import torch
+    from helmholtzbem_gb300 import _capi as C, api, geometry
+    data = api.BuilderData(geometry.polygon(*geometry.star_polygon(24, seed=2), 800), order=11)
+    so = api.SolutionsOperator(data)
+    n, nk = 1600, 4
+    ks = np.array([3.0, 7.5, 12.25, 19.0])
+    T = torch.empty((nk, n, n), dtype=torch.complex128, device="cuda")
+    L = C.lib()
+    C.check(L.hbem_gen_sol_op_batch_device(so._h, C.dptr(ks), nk, 1.0, 9.0, 0, ctypes.c_void_p(T.data_ptr())))
+    R = torch.from_numpy(np.ascontiguousarray(api.randGaussian(n, 12, seed=1).T)).cuda()
+    out = np.zeros(nk)
+    for prec in (0, 1):
+        C.check(L.hbem_rsvd_sv_batch_device_ex(n, nk, 0, ctypes.c_void_p(T.data_ptr()), n * n, n * n,
+                                               ctypes.c_void_p(R.data_ptr()), 12, 2, prec, 3, C.dptr(out)))
+    print("profile dense tail done, sigma = %s" % out)
 
 
 def dist_env():
@@ -395,7 +430,11 @@ def run_gpu(args):
     achieved = flops / (asm_ms.value * 1e-3) / 1e12 if asm_ms.value > 0 else 0.0
     peak = fp64_peak_tflops()
     roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak if peak else None, "traffic": None,
+                "frac": achieved / peak if peak else None,
+                # DRAM bytes (read + write) per assembly launch, averaged over the 28
+                # k_singular / k_general launches of one plain search of this workload
+                # (ncu dram__bytes_read.sum + dram__bytes_write.sum)
+                "traffic": 2.72e6, "traffic_unit": "bytes per launch",
                 "peak_source": "measured: cuBLAS DGEMM 8192^3 on this GPU (MEASURED_PEAKS.json has no FP64 entry)",
                 "kernel": "k_general + k_singular (panel-pair assembly)", "launches": asm_l.value,
                 "avg_launch_ms": asm_ms.value / max(1, asm_l.value)}
@@ -436,7 +475,11 @@ def run_gpu(args):
 
 def main():
     args = parse()
-    if args.profile_case:
+    if args.profile_search:
+        run_profile_search()
+    elif args.profile_dense_tail:
+        run_profile_dense_tail()
+    elif args.profile_case:
         run_profile_case()
     elif args.impl == "reference":
         run_reference(args)

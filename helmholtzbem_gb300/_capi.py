@@ -24,6 +24,7 @@ EXPORTS = [
     "hbem_gen_sol_op_batch_device", "hbem_sv_dense_batch_device", "hbem_sv_dense_batch_noalloc",
     "hbem_sv_dense_batch", "hbem_sweep_sigma", "hbem_rand_sketch", "hbem_rsvd_sv_batch",
     "hbem_rsvd_sv_batch_device", "hbem_rsvd_sv_batch_device_ex", "hbem_lu_factor_batch_device", "hbem_lu_solve_batch_device",
+    "hbem_cgemm_f32_batch_device",
     "hbem_find_resonances_plain", "hbem_rtsafe", "hbem_zbrent", "hbem_brent_min",
 ]
 
@@ -92,6 +93,9 @@ def load(path=LIB_PATH):
                                            _dp]),
         "hbem_rsvd_sv_batch_device_ex": (_i, [_i, _i, _u, _vp, ctypes.c_longlong, ctypes.c_longlong, _vp, _i, _i,
                                               _i, _i, _dp]),
+        "hbem_cgemm_f32_batch_device": (_i, [_i, _i, _i, _vp, ctypes.c_longlong, ctypes.c_longlong, _vp,
+                                             ctypes.c_longlong, ctypes.c_longlong, _vp, ctypes.c_longlong,
+                                             ctypes.c_longlong, _i, _i]),
         "hbem_lu_factor_batch_device": (_i, [_i, _i, _vp, ctypes.c_longlong, _vp, _ip]),
         "hbem_lu_solve_batch_device": (_i, [_i, _i, _i, _vp, ctypes.c_longlong, _vp, _i, _vp, ctypes.c_longlong]),
         "hbem_find_resonances_plain": (_i, [_vp, _d, _d, _i, _d, _d, _d, _dp, _i, _ip, _dp, _ip]),

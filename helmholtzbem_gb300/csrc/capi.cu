@@ -39,6 +39,9 @@ cudaError_t lu_solve_batched(int n, int nmat, int trans, const cplx* LU, long lo
 cudaError_t lu_perm_from_piv(int n, int nmat, const int* piv, int* perm, cudaStream_t st);
 bool lu_solve_supported(int n);
 void lu_set_cluster_panels(int on);
+cudaError_t launch_cgemm_f32(int m, int n, int k, const cplxf* A, long long lda, long long sa, const cplxf* B,
+                             long long ldb, long long sb, cplxf* C, long long ldc, long long sc, int nmat,
+                             int use_tc, int* err, cudaStream_t st);
 size_t svd_fast_smem_bytes(int n);
 cudaError_t launch_svd_fast(int n, int nmat, int D, const cplx* T, long long mat_stride, long long der_stride,
                             double* out, int* status, cudaStream_t st);
@@ -768,6 +771,25 @@ int hbem_rsvd_sv_batch(int n, int nmat, unsigned d, const double* T_host, const 
     HB_CK(cudaMemcpy(T.p, T_host, bytes, cudaMemcpyHostToDevice));
     HB_CK(cudaMemcpy(R.p, R_host, (size_t)n * s * sizeof(cplx), cudaMemcpyHostToDevice));
     return hbem_rsvd_sv_batch_device(n, nmat, d, T.p, (long long)((d + 1) * nn), (long long)nn, R.p, s, q, out_host);
+}
+
+int hbem_cgemm_f32_batch_device(int m, int n, int k, const void* A, long long lda, long long sa, const void* B,
+                                long long ldb, long long sb, void* C, long long ldc, long long sc, int nmat,
+                                int tensor_cores) {
+    if (m < 0 || n < 0 || k < 0 || nmat < 1 || nmat > 65535 || !A || !B || !C || lda < std::max(1, m) ||
+        ldb < std::max(1, k) || ldc < std::max(1, m) || (tensor_cores && k > 32))
+        return fail(HBEM_ERR_INVALID, "cgemm_f32_batch: bad argument");
+    HB_CK(cudaSetDevice(g_device));
+    static thread_local DBuf err;
+    HB_CK(err.ensure(sizeof(int)));
+    HB_CK(cudaMemsetAsync(err.p, 0, sizeof(int), 0));
+    HB_CK(launch_cgemm_f32(m, n, k, static_cast<const cplxf*>(A), lda, sa, static_cast<const cplxf*>(B), ldb, sb,
+                           static_cast<cplxf*>(C), ldc, sc, nmat, tensor_cores, err.as<int>(), 0));
+    g_launches += 1;
+    int h = 0;
+    HB_CK(cudaMemcpy(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) return fail(HBEM_ERR_NOCONV, "cgemm_f32_batch: a tensor-core completion wait timed out");
+    return HBEM_OK;
 }
 
 int hbem_lu_factor_batch_device(int n, int nmat, void* A_dev, long long stride, int* piv_dev, int* info_host) {

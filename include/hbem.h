@@ -179,6 +179,15 @@ int hbem_rsvd_sv_batch_device_ex(int n, int nmat, unsigned d, const void* T_dev,
                                  long long der_stride, const void* R_dev, int s, int q, int precision, int refine,
                                  double* out_host);
 
+/* Batched complex64 update C_m -= A_m B_m (column-major, leading dimensions lda, ldb,
+ * ldc, batch strides sa, sb, sc in elements): the trailing update of the LU's
+ * complex-FP32 factorisation (the FP32 stand-in for the trailing GEMMs of Eigen's
+ * PartialPivLU at source/utilities/randsvd.cpp:104).  tensor_cores = 1: tcgen05
+ * MMAs with 3xTF32 split products and FP32 accumulation (k <= 32); 0: FP32 FMA.  */
+int hbem_cgemm_f32_batch_device(int m, int n, int k, const void* A, long long lda, long long sa, const void* B,
+                                long long ldb, long long sb, void* C, long long ldc, long long sc, int nmat,
+                                int tensor_cores);
+
 /* Batched LU with partial pivoting, in place (Eigen::PartialPivLU<MatrixXcd> at
  * source/utilities/randsvd.cpp:104,205): nmat column-major complex128 matrices of
  * order n at A_dev + m * stride (elements).  piv_dev[m n + k] = row exchanged with

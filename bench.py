@@ -305,8 +305,16 @@ def dense_tail_at_scale(torch, C, api, geometry, lib, peak, nk=16):
         C.check(lib.hbem_rsvd_sv_batch_device_ex(n, nk, 0, C.ctypes.c_void_p(T.data_ptr()), n * n, n * n,
                                                  C.ctypes.c_void_p(R.data_ptr()), 12, 2, 1, 3, C.dptr(out32)))
 
+    def rsvd_mixed_fma():
+        C.check(lib.hbem_set_option(b"lu_tensor_cores", 0))
+        try:
+            rsvd_mixed()
+        finally:
+            C.check(lib.hbem_set_option(b"lu_tensor_cores", 1))
+
     res = {}
-    for name, fn in (("assembly", assemble), ("lu", lu), ("rsvd", rsvd), ("rsvd_mixed", rsvd_mixed)):
+    for name, fn in (("assembly", assemble), ("lu", lu), ("rsvd", rsvd), ("rsvd_mixed", rsvd_mixed),
+                     ("rsvd_mixed_fma", rsvd_mixed_fma)):
         fn()
         torch.cuda.synchronize()
         e0, e1 = ev(), ev()
@@ -333,6 +341,7 @@ def dense_tail_at_scale(torch, C, api, geometry, lib, peak, nk=16):
             "lu_frac_of_measured_fp64": lu_tf / peak if peak else None,
             "T_per_s_assembly_plus_rsvd": 1e3 * nk / (res["assembly"] + res["rsvd"]),
             "rsvd_mixed_ms_per_T": res["rsvd_mixed"] / nk,
+            "rsvd_mixed_lu_fp32_fma_ms_per_T": res["rsvd_mixed_fma"] / nk,
             "T_per_s_assembly_plus_rsvd_mixed": 1e3 * nk / (res["assembly"] + res["rsvd_mixed"]),
             "rsvd_mixed_max_rel_err_vs_fp64": float(np.max(np.abs(out32 - out) / out)),
             "sigma_min": [float(x) for x in out[:4]]}

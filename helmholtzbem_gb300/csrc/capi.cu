@@ -39,6 +39,7 @@ cudaError_t lu_solve_batched(int n, int nmat, int trans, const cplx* LU, long lo
 cudaError_t lu_perm_from_piv(int n, int nmat, const int* piv, int* perm, cudaStream_t st);
 bool lu_solve_supported(int n);
 void lu_set_cluster_panels(int on);
+void lu_set_tensor_cores(int on);
 cudaError_t launch_cgemm_f32(int m, int n, int k, const cplxf* A, long long lda, long long sa, const cplxf* B,
                              long long ldb, long long sb, cplxf* C, long long ldc, long long sc, int nmat,
                              int use_tc, int* err, cudaStream_t st);
@@ -319,6 +320,10 @@ int hbem_set_option(const char* name, int value) {
     const std::string k(name);
     if (k == "lu_cluster_panels") {
         lu_set_cluster_panels(value);
+        return HBEM_OK;
+    }
+    if (k == "lu_tensor_cores") {
+        lu_set_tensor_cores(value);
         return HBEM_OK;
     }
     if (k == "svd_fast") {
@@ -750,7 +755,8 @@ int hbem_rsvd_sv_batch_device_ex(int n, int nmat, unsigned d, const void* T_dev,
     HB_CK(cudaMemcpy(out_host, out.p, (size_t)nmat * os * sizeof(double), cudaMemcpyDeviceToHost));
     HB_CK(cudaMemcpy(st.data(), status.p, (size_t)nmat * sizeof(int), cudaMemcpyDeviceToHost));
     for (int v : st)
-        if (v) return fail(HBEM_ERR_SINGULAR, "rsvd_sv_batch: zero pivot in the LU of T");
+        if (v == 4) return fail(HBEM_ERR_NOCONV, "rsvd_sv_batch: a tensor-core completion wait timed out");
+        else if (v) return fail(HBEM_ERR_SINGULAR, "rsvd_sv_batch: zero pivot in the LU of T");
     return HBEM_OK;
 }
 

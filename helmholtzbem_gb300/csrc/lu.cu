@@ -14,6 +14,7 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "hbem_device.cuh"
 
@@ -551,8 +552,14 @@ cudaError_t lu_perm_from_piv(int n, int nmat, const int* piv, int* perm, cudaStr
 
 constexpr size_t kPanelClusterSmem = 200 * 1024;
 int g_lu_cluster_panels = 1;   // 0: tall panels in global memory (kept for comparison tests)
+int g_lu_tensor_cores = 1;     // complex64 trailing updates on the tensor cores
 
 void lu_set_cluster_panels(int on) { g_lu_cluster_panels = on ? 1 : 0; }
+void lu_set_tensor_cores(int on) { g_lu_tensor_cores = on ? 1 : 0; }
+
+cudaError_t launch_cgemm_f32(int m, int n, int k, const cplxf* A, long long lda, long long sa, const cplxf* B,
+                             long long ldb, long long sb, cplxf* C, long long ldc, long long sc, int nmat,
+                             int use_tc, int* err, cudaStream_t st);
 
 // Cluster launch of the panel factorisation when the panel is too tall for one CTA.
 // Returns with *launched = false (nothing launched) when no cluster size up to 16
@@ -608,7 +615,7 @@ cudaError_t launch_panel_cluster(int n, int k0, int nb, int nmat, E* A, long lon
 
 template <class E>
 cudaError_t lu_factor_impl(int n, int nmat, E* A, long long stride, int* piv, int* perm, int* info, cudaStream_t st,
-                           long long* launches) {
+                           long long* launches, int* tc_err) {
     if (n < 1 || nmat < 1 || nmat > 65535 || (size_t)n * sizeof(int) > kLuSmemLimit) return cudaErrorInvalidValue;
     const size_t gemm_smem = 2 * (size_t)kLuNB * kLuTile * sizeof(E);
     cudaError_t e = cudaFuncSetAttribute(k_lu_gemm<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem);
@@ -639,8 +646,22 @@ cudaError_t lu_factor_impl(int n, int nmat, E* A, long long stride, int* piv, in
         }
         const int m = n - k0 - nb;
         if (m > 0) {
-            const int tiles = (m + kLuTile - 1) / kLuTile;
-            k_lu_gemm<E><<<dim3(tiles, tiles, nmat), 256, gemm_smem, st>>>(n, k0, nb, A, stride);
+            bool done = false;
+            if constexpr (std::is_same<E, cplxf>::value) {
+                // complex64: A22 -= L21 U12 on the tensor cores (3xTF32) once the trailing
+                // block spans at least one 128-row tile
+                if (tc_err && g_lu_tensor_cores && m >= 128) {
+                    const int t0 = k0 + nb;
+                    e = launch_cgemm_f32(m, m, nb, A + t0 + (long long)k0 * n, n, stride, A + k0 + (long long)t0 * n,
+                                         n, stride, A + t0 + (long long)t0 * n, n, stride, nmat, 1, tc_err, st);
+                    if (e != cudaSuccess) return e;
+                    done = true;
+                }
+            }
+            if (!done) {
+                const int tiles = (m + kLuTile - 1) / kLuTile;
+                k_lu_gemm<E><<<dim3(tiles, tiles, nmat), 256, gemm_smem, st>>>(n, k0, nb, A, stride);
+            }
             ++nl;
         }
     }
@@ -684,11 +705,11 @@ cudaError_t lu_solve_impl(int n, int nmat, int trans, const E* LU, long long str
 
 cudaError_t lu_factor_batched(int n, int nmat, cplx* A, long long stride, int* piv, int* perm, int* info,
                               cudaStream_t st, long long* launches) {
-    return lu_factor_impl<cplx>(n, nmat, A, stride, piv, perm, info, st, launches);
+    return lu_factor_impl<cplx>(n, nmat, A, stride, piv, perm, info, st, launches, nullptr);
 }
 cudaError_t lu_factor_batched_f32(int n, int nmat, cplxf* A, long long stride, int* piv, int* perm, int* info,
-                                  cudaStream_t st, long long* launches) {
-    return lu_factor_impl<cplxf>(n, nmat, A, stride, piv, perm, info, st, launches);
+                                  cudaStream_t st, long long* launches, int* tc_err) {
+    return lu_factor_impl<cplxf>(n, nmat, A, stride, piv, perm, info, st, launches, tc_err);
 }
 cudaError_t lu_solve_batched(int n, int nmat, int trans, const cplx* LU, long long stride, const int* perm, int s,
                              cplx* X, long long xstride, cudaStream_t st) {

@@ -146,7 +146,8 @@ __global__ void __launch_bounds__(kRsvdThreads) k_qr_global(int n, int s, cplx* 
 __global__ void __launch_bounds__(kRsvdThreads) k_rsvd_tail(int n, int s, int D, const cplx* Q, const cplx* QB,
                                                              long long xstride, const cplx* Rf, const cplx* T,
                                                              long long mat_stride, long long der_stride,
-                                                             const int* info, double* out, int* status, cplx* uv) {
+                                                             const int* info, double* out, int* status, cplx* uv,
+                                                             const int* tc_err) {
     __shared__ cplx Rs[kRsvdMaxS * kRsvdMaxS], W[kRsvdMaxS * kRsvdMaxS], tw[kRsvdMaxS];
     __shared__ double red[128];
     const int mat = blockIdx.x, os = D + 1;
@@ -165,7 +166,7 @@ __global__ void __launch_bounds__(kRsvdThreads) k_rsvd_tail(int n, int s, int D,
     if (threadIdx.x == 0) {
         out[(long long)os * mat] = isn;
         for (int t = 1; t < os; ++t) out[(long long)os * mat + t] = 0.;
-        status[mat] = info[mat] ? 5 : 0;
+        status[mat] = info[mat] ? 5 : ((tc_err && *tc_err) ? 4 : 0);
     }
     if (D == 0) return;
     if (threadIdx.x < s) tw[threadIdx.x] = W[bj * s + threadIdx.x];   // w
@@ -346,7 +347,7 @@ __global__ void k_sv2_out(int n, int nmat, const cplx* sol, const int* mcol, con
 // FP64: x <- x + LU32^-1 (b - op(T) x), residuals from the FP64 T.
 
 cudaError_t lu_factor_batched_f32(int n, int nmat, cplxf* A, long long stride, int* piv, int* perm, int* info,
-                                  cudaStream_t st, long long* launches);
+                                  cudaStream_t st, long long* launches, int* tc_err);
 cudaError_t lu_solve_batched_f32(int n, int nmat, int trans, const cplxf* LU, long long stride, const int* perm,
                                  int s, cplxf* X, long long xstride, cudaStream_t st);
 bool lu_solve_supported_f32(int n);
@@ -477,6 +478,7 @@ struct RsvdWork {
     cplx *A = nullptr, *X = nullptr, *Y = nullptr, *Rf = nullptr, *uv = nullptr;
     int *piv = nullptr, *perm = nullptr, *info = nullptr;
     cplxf *A32 = nullptr, *X32 = nullptr;
+    int* tc_err = nullptr;
     cplx *Bsave = nullptr, *Rres = nullptr;
     cplx *B = nullptr, *ub = nullptr, *ud = nullptr, *rhs = nullptr, *tb = nullptr;
     int *piv2 = nullptr, *perm2 = nullptr, *info2 = nullptr, *mcol = nullptr;
@@ -494,6 +496,7 @@ size_t rsvd_carve(int n, int nmat, int s, int D, bool small, bool mixed, char* b
     if (!small) {
         if (mixed) {
             w.A32 = (cplxf*)take(nm * nn * cf);
+            w.tc_err = (int*)take(sizeof(int));
             w.X32 = (cplxf*)take(nm * n * s * cf);
             w.Bsave = (cplx*)take(nm * n * s * c);
             w.Rres = (cplx*)take(nm * n * s * c);
@@ -567,7 +570,8 @@ cudaError_t rsvd_batched(int n, int nmat, int s, int q, int D, int precision, in
         };
         if (mixed) {
             k_to_f32<<<grid_len(nn, nmat), 256, 0, st>>>(nn, T, mat_stride, w.A32, nn);
-            RS_CK(lu_factor_batched_f32(n, nmat, w.A32, nn, w.piv, w.perm, w.info, st, &nl));
+            RS_CK(cudaMemsetAsync(w.tc_err, 0, sizeof(int), st));
+            RS_CK(lu_factor_batched_f32(n, nmat, w.A32, nn, w.piv, w.perm, w.info, st, &nl, w.tc_err));
         } else {
             k_copy_mats<<<grid_len(nn, nmat), 256, 0, st>>>((int)nn, T, mat_stride, w.A, nn);
             RS_CK(lu_factor_batched(n, nmat, w.A, nn, w.piv, w.perm, w.info, st, &nl));
@@ -588,7 +592,7 @@ cudaError_t rsvd_batched(int n, int nmat, int s, int q, int D, int precision, in
         RS_CK(solve(1, w.Y, s, ns, refine));
         k_qr_global<<<nmat, kRsvdThreads, 0, st>>>(n, s, w.Y, ns, w.Rf);
         k_rsvd_tail<<<nmat, kRsvdThreads, 0, st>>>(n, s, D, w.X, w.Y, ns, w.Rf, T, mat_stride, der_stride, w.info,
-                                                    out, status, w.uv);
+                                                    out, status, w.uv, w.tc_err);
         nl += 2;
         RS_CK(cudaGetLastError());
         if (D >= 1)

@@ -15,8 +15,9 @@
 // the MMA for K-step kk starts at block kk / 4, byte offset 32 (kk % 4).
 // One elected thread issues the MMAs and commits them to an mbarrier; all threads
 // wait on it with an iteration cap (a timeout sets an error flag and the CTA still
-// releases its tensor memory); the four warps read their 32 TMEM lanes back with
-// tcgen05.ld and update C in global memory.
+// releases its tensor memory); eight warps read the accumulator back with tcgen05.ld
+// (warp w: TMEM lanes 32 (w % 4) .. + 31, column half w / 4) and update C in global
+// memory.  Each thread issues its operand and C loads in batches before using them.
 #include <cstdint>
 
 #include "hbem_device.cuh"
@@ -28,7 +29,7 @@ constexpr int kTcNc = 64;                    // complex columns per tile
 constexpr int kTcN = 2 * kTcNc;              // MMA N (real): [re | im]
 constexpr int kTcKc = 32;                    // complex K per launch (the LU panel width)
 constexpr int kTcK = 2 * kTcKc;              // real K: [re | im]
-constexpr int kTcThreads = 128;
+constexpr int kTcThreads = 256;
 constexpr uint32_t kTcKBlockBytes = 128u * 128u;           // 128 rows x 128 bytes
 constexpr uint32_t kTcOperandBytes = 2u * kTcKBlockBytes;  // two K blocks
 constexpr uint32_t kTcTmemCols = 256;        // allocation (the accumulator uses 128)
@@ -110,23 +111,40 @@ __global__ void __launch_bounds__(kTcThreads) k_cgemm_tc(TcJob J) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar)), "r"(1));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    // A' = [A_r | A_i]: row r, K index k (re) and 32 + k (im)
-    for (int e = tid; e < kTcM * kTcKc; e += kTcThreads) {
-        const int r = e % kTcM, k = e / kTcM;
-        cplxf a = mkf(0.f);
-        if (r0 + r < J.m && k < J.k) a = A[(r0 + r) + (long long)k * J.lda];
-        store_split(Ahi, Alo, sw128_offset(r, k), a.re);
-        store_split(Ahi, Alo, sw128_offset(r, kTcKc + k), a.im);
+    // A' = [A_r | A_i]: row r, K index k (re) and 32 + k (im); the loads of a thread
+    // are issued together (16 per thread) before the conversions and stores
+    {
+        constexpr int per = kTcM * kTcKc / kTcThreads;
+        cplxf a[per];
+#pragma unroll
+        for (int q = 0; q < per; ++q) {
+            const int e = tid + q * kTcThreads, r = e % kTcM, k = e / kTcM;
+            a[q] = (r0 + r < J.m && k < J.k) ? A[(r0 + r) + (long long)k * J.lda] : mkf(0.f);
+        }
+#pragma unroll
+        for (int q = 0; q < per; ++q) {
+            const int e = tid + q * kTcThreads, r = e % kTcM, k = e / kTcM;
+            store_split(Ahi, Alo, sw128_offset(r, k), a[q].re);
+            store_split(Ahi, Alo, sw128_offset(r, kTcKc + k), a[q].im);
+        }
     }
     // B' rows (N index): j -> (B_r ; -B_i), 64 + j -> (B_i ; B_r)
-    for (int e = tid; e < kTcKc * kTcNc; e += kTcThreads) {
-        const int k = e % kTcKc, j = e / kTcKc;
-        cplxf b = mkf(0.f);
-        if (k < J.k && c0 + j < J.n) b = B[k + (long long)(c0 + j) * J.ldb];
-        store_split(Bhi, Blo, sw128_offset(j, k), b.re);
-        store_split(Bhi, Blo, sw128_offset(j, kTcKc + k), -b.im);
-        store_split(Bhi, Blo, sw128_offset(kTcNc + j, k), b.im);
-        store_split(Bhi, Blo, sw128_offset(kTcNc + j, kTcKc + k), b.re);
+    {
+        constexpr int per = kTcKc * kTcNc / kTcThreads;
+        cplxf b[per];
+#pragma unroll
+        for (int q = 0; q < per; ++q) {
+            const int e = tid + q * kTcThreads, k = e % kTcKc, j = e / kTcKc;
+            b[q] = (k < J.k && c0 + j < J.n) ? B[k + (long long)(c0 + j) * J.ldb] : mkf(0.f);
+        }
+#pragma unroll
+        for (int q = 0; q < per; ++q) {
+            const int e = tid + q * kTcThreads, k = e % kTcKc, j = e / kTcKc;
+            store_split(Bhi, Blo, sw128_offset(j, k), b[q].re);
+            store_split(Bhi, Blo, sw128_offset(j, kTcKc + k), -b[q].im);
+            store_split(Bhi, Blo, sw128_offset(kTcNc + j, k), b[q].im);
+            store_split(Bhi, Blo, sw128_offset(kTcNc + j, kTcKc + k), b[q].re);
+        }
     }
     // generic-proxy shared-memory writes -> visible to the tensor core (async proxy)
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -169,10 +187,11 @@ __global__ void __launch_bounds__(kTcThreads) k_cgemm_tc(TcJob J) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     __syncthreads();
     if (!s_fail) {
-        // epilogue: warp w holds TMEM lanes (rows) 32 w .. 32 w + 31
-        const int row = r0 + warp * 32 + lane;
-        const uint32_t lane_base = taddr + ((uint32_t)(warp * 32) << 16);
-        for (int j0 = 0; j0 < kTcNc; j0 += 16) {
+        // epilogue: warp w reads TMEM lanes (rows) 32 (w % 4) .. + 31, column half w / 4
+        const int wq = warp & 3, half = warp >> 2;
+        const int row = r0 + wq * 32 + lane;
+        const uint32_t lane_base = taddr + ((uint32_t)(wq * 32) << 16);
+        for (int j0 = half * (kTcNc / 2); j0 < (half + 1) * (kTcNc / 2); j0 += 16) {
             uint32_t re[16], im[16];
             asm volatile(
                 "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
@@ -188,16 +207,18 @@ __global__ void __launch_bounds__(kTcThreads) k_cgemm_tc(TcJob J) {
                 : "r"(lane_base + (uint32_t)(kTcNc + j0)));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             if (row < J.m) {
+                cplxf c[16];
 #pragma unroll
                 for (int jj = 0; jj < 16; ++jj) {
                     const int col = c0 + j0 + jj;
-                    if (col < J.n) {
-                        cplxf* cp = C + row + (long long)col * J.ldc;
-                        cplxf c = *cp;
-                        c.re -= __uint_as_float(re[jj]);
-                        c.im -= __uint_as_float(im[jj]);
-                        *cp = c;
-                    }
+                    c[jj] = col < J.n ? C[row + (long long)col * J.ldc] : mkf(0.f);
+                }
+#pragma unroll
+                for (int jj = 0; jj < 16; ++jj) {
+                    const int col = c0 + j0 + jj;
+                    if (col < J.n)
+                        C[row + (long long)col * J.ldc] =
+                            mkf(c[jj].re - __uint_as_float(re[jj]), c[jj].im - __uint_as_float(im[jj]));
                 }
             }
         }

@@ -54,6 +54,8 @@ int hbem_set_device(int device);
  *   "lu_cluster_panels" (default 1): LU panels taller than one CTA's shared memory
  *   are factored by a thread-block cluster holding the panel in distributed shared
  *   memory; 0 factors them in global memory.
+ *   "lu_tensor_cores" (default 1): the complex-FP32 LU of the mixed-precision randomized
+ *   SVD does its trailing updates on the tensor cores (3xTF32); 0 uses FP32 FMA.
  *   "svd_fast" (default 1): dense sigma_min / sigma' / sigma'' (direct::sv*) of matrices
  *   up to order 100 by FP32 Jacobi plus FP64 refinement of the near singular triplets
  *   (one FP64 LU per matrix); 0 always uses the FP64-polished Jacobi kernel.         */

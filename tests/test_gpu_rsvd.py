@@ -97,6 +97,15 @@ def test_rsvd_batched_scatterer_size():
     # FP64 refinement: the same sigma to 1e-9
     mixed = _rsvd_device(mats, R, 2, 0, 1, 3)[:, 0]
     assert np.max(np.abs(mixed - got) / got) < 1e-9
+    # the same with the complex-FP32 LU's trailing updates in FP32 FMA instead of the
+    # tensor cores (3xTF32): both refine to the FP64 result
+    from helmholtzbem_gb300 import _capi as C
+    C.check(C.lib().hbem_set_option(b"lu_tensor_cores", 0))
+    try:
+        mixed_fma = _rsvd_device(mats, R, 2, 0, 1, 3)[:, 0]
+    finally:
+        C.check(C.lib().hbem_set_option(b"lu_tensor_cores", 1))
+    assert np.max(np.abs(mixed_fma - got) / got) < 1e-9
 
 
 def _rsvd_device(mats, R, q, d, precision, refine):

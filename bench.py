@@ -347,6 +347,53 @@ def dense_tail_at_scale(torch, C, api, geometry, lib, peak, nk=16):
             "sigma_min": [float(x) for x in out[:4]]}
 
 
+def precision_at_scale(torch, C, api, geometry, lib, ks=(40.0, 41.0)):
+    """Precision configuration: seeded Fourier-sum scatterer (seed 4000, 8 modes,
+    a_m, b_m ~ N(0, 0.05/m)), N = 4000 line panels (T 8000 x 8000), order 11, c_i = 9,
+    c_o = 1, sketch 16, q = 2.  sigma_min by the mixed path (complex-FP32 LU with
+    tensor-core trailing updates, FP64 refinement) and by the FP64 path on the same
+    sketch; the relative difference is the mixed path's error against FP64 (a dense
+    FP64 SVD of order 8000 is out of reach of a benchmark run)."""
+    import ctypes
+    N, n = 4000, 8000
+    a, b = geometry.random_fourier_coeffs(4000)
+    data = api.BuilderData(geometry.fourier_curve(a, b, N), order=11)
+    so = api.SolutionsOperator(data)
+    kk = np.array(ks, float)
+    nk = kk.size
+    T = torch.empty((nk, n, n), dtype=torch.complex128, device="cuda")
+    R = torch.from_numpy(np.ascontiguousarray(api.randGaussian(n, 16, seed=4000).T)).cuda()
+    ev = lambda: torch.cuda.Event(enable_timing=True)   # noqa: E731
+    out = {0: np.zeros(nk), 1: np.zeros(nk)}
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0, e1 = ev(), ev()
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    asm_ms = timed(lambda: C.check(lib.hbem_gen_sol_op_batch_device(so._h, C.dptr(kk), nk, 1.0, 9.0, 0,
+                                                                    ctypes.c_void_p(T.data_ptr()))))
+
+    def rsvd(prec):
+        C.check(lib.hbem_rsvd_sv_batch_device_ex(n, nk, 0, ctypes.c_void_p(T.data_ptr()), n * n, n * n,
+                                                 ctypes.c_void_p(R.data_ptr()), 16, 2, prec, 3, C.dptr(out[prec])))
+
+    rsvd(1)
+    mixed_ms = timed(lambda: rsvd(1))
+    fp64_ms = timed(lambda: rsvd(0))
+    err = np.abs(out[1] - out[0]) / out[0]
+    del T
+    return {"workload": "Fourier-sum scatterer (seed 4000), N=4000 lines (T 8000x8000 c128), order 11, c_i=9, "
+                        "k in %s; rSVD sketch 16, q=2" % list(ks),
+            "assembly_ms_per_T": asm_ms / nk, "rsvd_mixed_ms_per_T": mixed_ms / nk, "rsvd_fp64_ms_per_T": fp64_ms / nk,
+            "sigma_min_mixed": [float(x) for x in out[1]], "sigma_min_fp64": [float(x) for x in out[0]],
+            "rel_err_mixed_vs_fp64": [float(x) for x in err]}
+
+
 def run_gpu(args):
     rank, world, local = dist_env()
     import torch
@@ -450,6 +497,7 @@ def run_gpu(args):
 
     scale = assembly_at_scale(torch, C, api, geometry, lib, peak)
     tail = dense_tail_at_scale(torch, C, api, geometry, lib, peak)
+    prec = precision_at_scale(torch, C, api, geometry, lib)
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
@@ -474,6 +522,7 @@ def run_gpu(args):
             "roofline": roofline,
             "assembly_at_scale": scale,
             "dense_tail_at_scale": tail,
+            "precision_at_scale": prec,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }

@@ -83,3 +83,18 @@ def fourier_curve(a, b, N):
     xs, ys = r * np.cos(th), r * np.sin(th)
     panels = [(xs[i], ys[i], xs[(i + 1) % N], ys[(i + 1) % N], 0.0) for i in range(N)]
     return np.full(N, PANEL_LINE, np.int32), np.array(panels)
+
+
+def random_fourier_coeffs(seed, modes=8, scale=0.05, rmin=0.3):
+    """Seeded Fourier-sum radius r(t) = 1 + sum_m a_m cos mt + b_m sin mt with
+    a_m, b_m ~ N(0, scale / m), redrawn until min r >= rmin."""
+    rng = np.random.default_rng(seed)
+    while True:
+        sd = scale / np.arange(1, modes + 1)
+        a = rng.normal(0.0, sd)
+        b = rng.normal(0.0, sd)
+        th = np.linspace(0, 2 * np.pi, 2048, endpoint=False)
+        m = np.arange(1, modes + 1)
+        r = 1 + np.cos(np.outer(th, m)) @ a + np.sin(np.outer(th, m)) @ b
+        if r.min() >= rmin:
+            return a, b

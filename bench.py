@@ -394,6 +394,55 @@ def precision_at_scale(torch, C, api, geometry, lib, ks=(40.0, 41.0)):
             "rel_err_mixed_vs_fp64": [float(x) for x in err]}
 
 
+def batching_sample(torch, C, api, geometry, lib, nk=16):
+    """Batching configuration on a bounded sample: 8 seeded scatterers (s = 0..3 star
+    polygons with 8..40 vertices, s = 4..7 Fourier-sum curves, seed 3000 + s), N =
+    100, 200, ..., 800 line panels, c_i ~ U[2, 25], c_o = 1, order 11, nk wavenumbers
+    per scatterer uniform on [1, 30] (the configuration's 256 per scatterer, 2048 T(k)
+    in all, would take ~45 s of FP64 assembly); per scatterer one batched assembly and
+    one batched mixed-precision rSVD (sketch 12, q = 2).  Reports T(k)/s."""
+    import ctypes
+    tot_ms, tot_T, asm_ms_all, rs_ms_all, per = 0.0, 0, 0.0, 0.0, []
+    ev = lambda: torch.cuda.Event(enable_timing=True)   # noqa: E731
+    for sidx in range(8):
+        seed = 3000 + sidx
+        rng = np.random.default_rng(seed)
+        N = 100 * (sidx + 1)
+        if sidx < 4:
+            nv = int(rng.integers(8, 41))
+            mesh = geometry.polygon(*geometry.star_polygon(nv, seed=seed), N)
+        else:
+            a, b = geometry.random_fourier_coeffs(seed)
+            mesh = geometry.fourier_curve(a, b, N)
+        c_i = float(rng.uniform(2.0, 25.0))
+        ks = np.sort(rng.uniform(1.0, 30.0, nk))
+        so = api.SolutionsOperator(api.BuilderData(mesh, order=11))
+        n = 2 * N
+        T = torch.empty((nk, n, n), dtype=torch.complex128, device="cuda")
+        R = torch.from_numpy(np.ascontiguousarray(api.randGaussian(n, 12, seed=seed).T)).cuda()
+        out = np.zeros(nk)
+        torch.cuda.synchronize()
+        e0, e1, e2 = ev(), ev(), ev()
+        e0.record()
+        C.check(lib.hbem_gen_sol_op_batch_device(so._h, C.dptr(ks), nk, 1.0, c_i, 0, ctypes.c_void_p(T.data_ptr())))
+        e1.record()
+        C.check(lib.hbem_rsvd_sv_batch_device_ex(n, nk, 0, ctypes.c_void_p(T.data_ptr()), n * n, n * n,
+                                                 ctypes.c_void_p(R.data_ptr()), 12, 2, 1, 3, C.dptr(out)))
+        e2.record()
+        torch.cuda.synchronize()
+        a_ms, r_ms = e0.elapsed_time(e1), e1.elapsed_time(e2)
+        asm_ms_all += a_ms
+        rs_ms_all += r_ms
+        tot_ms += a_ms + r_ms
+        tot_T += nk
+        per.append({"N": N, "c_i": round(c_i, 3), "ms_per_T": (a_ms + r_ms) / nk, "sigma_min_min": float(out.min())})
+        del T
+    return {"workload": "8 scatterers (4 star polygons, 4 Fourier curves), N=100..800, order 11, %d k each in "
+                        "[1,30]; mixed rSVD sketch 12, q=2" % nk,
+            "T_per_s": 1e3 * tot_T / tot_ms, "assembly_share": asm_ms_all / tot_ms, "rsvd_share": rs_ms_all / tot_ms,
+            "per_scatterer": per}
+
+
 def run_gpu(args):
     rank, world, local = dist_env()
     import torch
@@ -498,6 +547,7 @@ def run_gpu(args):
     scale = assembly_at_scale(torch, C, api, geometry, lib, peak)
     tail = dense_tail_at_scale(torch, C, api, geometry, lib, peak)
     prec = precision_at_scale(torch, C, api, geometry, lib)
+    batch = batching_sample(torch, C, api, geometry, lib)
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
@@ -523,6 +573,7 @@ def run_gpu(args):
             "assembly_at_scale": scale,
             "dense_tail_at_scale": tail,
             "precision_at_scale": prec,
+            "batching_sample": batch,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }

@@ -443,6 +443,20 @@ def batching_sample(torch, C, api, geometry, lib, nk=16):
             "per_scatterer": per}
 
 
+def combine_ranks(tot_ms, tot_v, world):
+    """Replicas meet on the host only: the slowest rank's time and the verified roots
+    of all ranks (a gloo all-reduce when world > 1)."""
+    if world <= 1:
+        return float(tot_ms), float(tot_v)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(tot_ms)], dtype=torch.float64)
+    v = torch.tensor([float(tot_v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(v)
+    return t.item(), v.item()
+
+
 def run_gpu(args):
     rank, world, local = dist_env()
     import torch
@@ -496,15 +510,7 @@ def run_gpu(args):
     launches, asm_ms, asm_l, asm_pts = (C.ctypes.c_longlong(), C.ctypes.c_double(), C.ctypes.c_longlong(),
                                         C.ctypes.c_longlong())
     lib.hbem_stats_read(C.ctypes.byref(launches), C.ctypes.byref(asm_ms), C.ctypes.byref(asm_l), C.ctypes.byref(asm_pts))
-    t = torch.tensor([tot_ms], dtype=torch.float64)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        vv = torch.tensor([float(tot_v)], dtype=torch.float64)
-        torch.distributed.all_reduce(vv)
-        tot_v_all = vv.item()
-    else:
-        tot_v_all = float(tot_v)
-    ms = t.item()
+    ms, tot_v_all = combine_ranks(tot_ms, tot_v, world)
     value = tot_v_all / (ms * 1e-3)
 
     # end to end from host data through the C ABI: mesh upload, operator set-up,

@@ -24,7 +24,8 @@ EXPORTS = [
     "hbem_gen_sol_op_batch_device", "hbem_sv_dense_batch_device", "hbem_sv_dense_batch_noalloc",
     "hbem_sv_dense_batch", "hbem_sweep_sigma", "hbem_rand_sketch", "hbem_rsvd_sv_batch",
     "hbem_rsvd_sv_batch_device", "hbem_rsvd_sv_batch_device_ex", "hbem_lu_factor_batch_device", "hbem_lu_solve_batch_device",
-    "hbem_cgemm_f32_batch_device",
+    "hbem_cgemm_f32_batch_device", "hbem_solop_info", "hbem_sigma_rsvd_sweep", "hbem_opt_subdiv",
+    "hbem_find_resonances_adaptive",
     "hbem_find_resonances_plain", "hbem_rtsafe", "hbem_zbrent", "hbem_brent_min",
 ]
 
@@ -40,6 +41,7 @@ _up = ctypes.POINTER(ctypes.c_uint)
 
 FN = ctypes.CFUNCTYPE(ctypes.c_double, ctypes.c_double, ctypes.c_void_p)
 FN_BOTH = ctypes.CFUNCTYPE(None, ctypes.c_double, _dp, _dp, ctypes.c_void_p)
+FN_BATCH = ctypes.CFUNCTYPE(None, _dp, ctypes.c_int, _dp, ctypes.c_void_p)
 
 
 class HbemError(RuntimeError):
@@ -96,6 +98,12 @@ def load(path=LIB_PATH):
         "hbem_cgemm_f32_batch_device": (_i, [_i, _i, _i, _vp, ctypes.c_longlong, ctypes.c_longlong, _vp,
                                              ctypes.c_longlong, ctypes.c_longlong, _vp, ctypes.c_longlong,
                                              ctypes.c_longlong, _i, _i]),
+        "hbem_solop_info": (_i, [_vp, _ip]),
+        "hbem_sigma_rsvd_sweep": (_i, [_vp, _dp, _i, _d, _d, _i, _i, _i, ctypes.c_ulonglong, _dp]),
+        "hbem_opt_subdiv": (_i, [FN_BATCH, _vp, _d, _d, _i, _i, _d, ctypes.c_ulonglong, _dp, _dp, _i, _ip, _ip, _i,
+                                 _ip]),
+        "hbem_find_resonances_adaptive": (_i, [_vp, _d, _d, _d, _d, _i, _i, _d, _d, ctypes.c_ulonglong, _i, _i, _dp, _i,
+                                               _ip, _ip, _ip]),
         "hbem_lu_factor_batch_device": (_i, [_i, _i, _vp, ctypes.c_longlong, _vp, _ip]),
         "hbem_lu_solve_batch_device": (_i, [_i, _i, _i, _vp, ctypes.c_longlong, _vp, _i, _vp, ctypes.c_longlong]),
         "hbem_find_resonances_plain": (_i, [_vp, _d, _d, _i, _d, _d, _d, _dp, _i, _ip, _dp, _ip]),

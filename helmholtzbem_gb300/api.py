@@ -129,6 +129,28 @@ class SolutionsOperator:
         check(C.lib().hbem_sweep_sigma(self._h, dptr(ks), int(ks.size), float(c_o), float(c_i), int(d), dptr(out)))
         return out
 
+    def sigma_rsvd_sweep(self, ks, c_o, c_i, sketch=2, q=2, precision=0, seed=0):
+        """randomized_svd::sv along ks on a seeded sketch of width `sketch`."""
+        ks = np.ascontiguousarray(ks, np.float64)
+        out = np.zeros(ks.size)
+        check(C.lib().hbem_sigma_rsvd_sweep(self._h, dptr(ks), int(ks.size), float(c_o), float(c_i), int(sketch),
+                                            int(q), int(precision), int(seed), dptr(out)))
+        return out
+
+    def find_resonances_adaptive(self, k_min, k_max, c_o, c_i, batch_size=16, limit=10, sample_tol=None, tol=1e-6,
+                                 seed=0, sketch=2, q=2, max_roots=4096):
+        """examples/find_resonances.cpp's search: opt_subdiv sampling, rational
+        interpolation, Brent refinement.  Returns (roots, n_samples, n_evals)."""
+        if sample_tol is None:
+            sample_tol = 1e-4 * (k_max - k_min)
+        roots = np.zeros(max_roots)
+        nr, ns, ne = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(C.lib().hbem_find_resonances_adaptive(self._h, float(k_min), float(k_max), float(c_o), float(c_i),
+                                                    int(batch_size), int(limit), float(sample_tol), float(tol),
+                                                    int(seed), int(sketch), int(q), dptr(roots), int(max_roots),
+                                                    ctypes.byref(nr), ctypes.byref(ns), ctypes.byref(ne)))
+        return roots[:min(nr.value, max_roots)].copy(), ns.value, ne.value
+
     def find_resonances_plain(self, k_min, k_max, npoints, c_o, c_i, tol=1e-8, max_roots=4096):
         roots = np.zeros(max_roots)
         grid = np.zeros((npoints, 3))
@@ -218,3 +240,22 @@ def rsvd_sv(Ts, R, q=0, d=0):
     check(C.lib().hbem_rsvd_sv_batch(n, nmat, int(d), buf.ctypes.data_as(C._dp), Rc.ctypes.data_as(C._dp), int(s),
                                      int(q), dptr(out)))
     return out
+
+def opt_subdiv(f, x_min, x_max, batch_size, limit, tol, seed=0, max_points=100000):
+    """opt_subdiv for a batched Python function f(xs) -> ys: returns (x, y, minima)."""
+    def _f(xp, n, yp, user):
+        xs = np.ctypeslib.as_array(xp, shape=(n,)).copy()
+        ys = np.asarray(f(xs), np.float64)
+        for i in range(n):
+            yp[i] = float(ys[i])
+
+    cb = C.FN_BATCH(_f)
+    x = np.zeros(max_points)
+    y = np.zeros(max_points)
+    mins = np.zeros(max_points, np.int32)
+    npnt, nmin = ctypes.c_int(), ctypes.c_int()
+    check(C.lib().hbem_opt_subdiv(cb, None, float(x_min), float(x_max), int(batch_size), int(limit), float(tol),
+                                  int(seed), dptr(x), dptr(y), max_points, ctypes.byref(npnt), iptr(mins), max_points,
+                                  ctypes.byref(nmin)))
+    n = min(npnt.value, max_points)
+    return x[:n].copy(), y[:n].copy(), mins[:min(nmin.value, max_points)].copy()

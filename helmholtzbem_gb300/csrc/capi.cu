@@ -838,6 +838,40 @@ int hbem_lu_solve_batch_device(int n, int nmat, int trans, const void* LU_dev, l
     return HBEM_OK;
 }
 
+int hbem_solop_info(hbem_solop s, int* npanels) {
+    if (!s || !npanels) return fail(HBEM_ERR_INVALID, "solop_info: bad argument");
+    *npanels = s->b->n;
+    return HBEM_OK;
+}
+
+int hbem_sigma_rsvd_sweep(hbem_solop s, const double* k_host, int nk, double c_o, double c_i, int sketch, int q,
+                          int precision, unsigned long long seed, double* sigma_out) {
+    if (!s || !k_host || !sigma_out || nk < 1 || sketch < 1 || q < 0 || precision < 0 || precision > 1)
+        return fail(HBEM_ERR_INVALID, "sigma_rsvd_sweep: bad argument");
+    hbem_builder b = s->b;
+    HB_CK(cudaSetDevice(b->device));
+    const int n = 2 * b->n;
+    if (sketch > n) return fail(HBEM_ERR_INVALID, "sigma_rsvd_sweep: sketch wider than the matrix");
+    const size_t mat = (size_t)n * n;
+    static thread_local DBuf R;
+    std::vector<double> Rh(2 * (size_t)n * sketch);
+    if (int r = hbem_rand_sketch(n, sketch, seed, Rh.data())) return r;
+    HB_CK(R.ensure(Rh.size() * sizeof(double)));
+    HB_CK(cudaMemcpy(R.p, Rh.data(), Rh.size() * sizeof(double), cudaMemcpyHostToDevice));
+    int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)nk, ((size_t)2 << 30) / (mat * sizeof(cplx))));
+    chunk = std::min(chunk, 65535);
+    HB_CK(s->d_T.ensure((size_t)chunk * mat * sizeof(cplx)));
+    for (int k0 = 0; k0 < nk; k0 += chunk) {
+        const int kn = std::min(chunk, nk - k0);
+        if (int r = gen_T_batch(s, k_host + k0, nullptr, kn, c_o, c_i, 0, s->d_T.as<cplx>())) return r;
+        HB_CK(cudaStreamSynchronize(b->st));
+        if (int r = hbem_rsvd_sv_batch_device_ex(n, kn, 0, s->d_T.p, (long long)mat, (long long)mat, R.p, sketch, q,
+                                                 precision, 3, sigma_out + k0))
+            return r;
+    }
+    return HBEM_OK;
+}
+
 int hbem_sweep_sigma(hbem_solop s, const double* k_host, int nk, double c_o, double c_i, unsigned d, double* out_host) {
     if (!s || !k_host || !out_host || nk < 1 || d > 2) return fail(HBEM_ERR_INVALID, "bad argument");
     hbem_builder b = s->b;

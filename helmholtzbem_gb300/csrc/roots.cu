@@ -10,6 +10,8 @@
 // resonance search runs many rtsafe iterations in lock step so every Newton
 // round is one batched GPU evaluation of sigma' and sigma''.
 #include <algorithm>
+#include <cstdint>
+#include <functional>
 #include <cmath>
 #include <limits>
 #include <string>
@@ -112,6 +114,253 @@ double quartic_guess(double a, double h, double f1, double f0, double f2, double
     double A = scale * p1 / a2, B = -scale * (4. * p1 + p2) / a, C = scale * (6. * p1 + 3 * p2 + p3);
     double D = d1 - scale * a * (4. * p1 + 3. * p2 + 2. * p3), E = f1 - a * d1 + scale * a2 * (p1 + p2 + p3);
     return localmin([&](double t) { return (((A * t + B) * t + C) * t + D) * t + E; }, a, a + 2 * h, tol);
+}
+
+// ------------------------------------------------------------------ adaptive sampler pieces
+
+// SplitMix64 (Steele, Lea and Flood 2014): seeded stand-in for the reference's
+// std::random_device-seeded mt19937; uniform in [0, 1) from the top 53 bits, normal
+// deviates by the Box-Muller transform.
+struct SplitMix {
+    uint64_t s;
+    explicit SplitMix(uint64_t seed) : s(seed) {}
+    uint64_t next() {
+        uint64_t z = (s += 0x9e3779b97f4a7c15ULL);
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+        return z ^ (z >> 31);
+    }
+    double uniform() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
+    double normal(double mu, double sd) {
+        double u1 = uniform(), u2 = uniform();
+        if (u1 <= 0.) u1 = 1.0 / 9007199254740992.0;
+        return mu + sd * std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * M_PI * u2);
+    }
+};
+
+// Monotone cubic interpolation of M. Steffen, A&A 239 (1990) 443-450: slopes
+// (sign s_{i-1} + sign s_i) min(|s_{i-1}|, |s_i|, |p_i| / 2) at interior nodes, the
+// parabola-through-three-points boundary slopes limited to [0, 2 s] (eqs. 26-27).
+struct Steffen {
+    std::vector<double> x, y, yp;
+    bool init(const std::vector<std::pair<double, double>>& xy, size_t n) {
+        if (n < 3) return false;
+        x.resize(n); y.resize(n); yp.resize(n);
+        for (size_t i = 0; i < n; ++i) { x[i] = xy[i].first; y[i] = xy[i].second; }
+        std::vector<double> h(n - 1), sl(n - 1);
+        for (size_t i = 0; i + 1 < n; ++i) {
+            h[i] = x[i + 1] - x[i];
+            if (!(h[i] > 0.)) return false;
+            sl[i] = (y[i + 1] - y[i]) / h[i];
+        }
+        auto sgn = [](double v) { return (double)((v > 0.) - (v < 0.)); };
+        for (size_t i = 1; i + 1 < n; ++i) {
+            const double p = (sl[i - 1] * h[i] + sl[i] * h[i - 1]) / (h[i - 1] + h[i]);
+            yp[i] = (sgn(sl[i - 1]) + sgn(sl[i])) * std::min(std::min(std::fabs(sl[i - 1]), std::fabs(sl[i])),
+                                                              0.5 * std::fabs(p));
+        }
+        auto bound = [](double s0, double s1, double h0, double h1) {
+            const double p = s0 * (1. + h0 / (h0 + h1)) - s1 * h0 / (h0 + h1);
+            if (p * s0 <= 0.) return 0.;
+            return std::fabs(p) > 2. * std::fabs(s0) ? 2. * s0 : p;
+        };
+        yp[0] = bound(sl[0], sl[1], h[0], h[1]);
+        yp[n - 1] = bound(sl[n - 2], sl[n - 3], h[n - 2], h[n - 3]);
+        return true;
+    }
+    // false outside [x_0, x_{n-1}]
+    bool eval(double t, double& v) const {
+        if (!(t >= x.front() && t <= x.back())) return false;
+        size_t i = std::upper_bound(x.begin(), x.end(), t) - x.begin();
+        i = i == 0 ? 0 : std::min(i - 1, x.size() - 2);
+        const double h = x[i + 1] - x[i], sl = (y[i + 1] - y[i]) / h, dt = t - x[i];
+        const double a = (yp[i] + yp[i + 1] - 2. * sl) / (h * h), b = (3. * sl - 2. * yp[i] - yp[i + 1]) / h;
+        v = y[i] + dt * (yp[i] + dt * (b + dt * a));
+        return true;
+    }
+};
+
+// Barycentric rational interpolant of M. S. Floater and K. Hormann, Numer. Math. 107
+// (2007) 315-331, blending order d (the reference uses order 5 through
+// boost::math::barycentric_rational).
+struct BaryRat {
+    std::vector<double> x, y, w;
+    void init(const double* xs, const double* ys, int n, int d) {
+        x.assign(xs, xs + n);
+        y.assign(ys, ys + n);
+        w.assign(n, 0.);
+        for (int k = 0; k < n; ++k)
+            for (int i = std::max(0, k - d); i <= std::min(k, n - 1 - d); ++i) {
+                double prod = 1.;
+                for (int j = i; j <= i + d; ++j)
+                    if (j != k) prod /= (x[k] - x[j]);
+                w[k] += (i % 2 ? -1. : 1.) * prod;
+            }
+    }
+    double operator()(double t) const {
+        double num = 0., den = 0.;
+        for (size_t k = 0; k < x.size(); ++k) {
+            if (t == x[k]) return y[k];
+            const double c = w[k] / (t - x[k]);
+            num += c * y[k];
+            den += c;
+        }
+        return num / den;
+    }
+};
+
+// One proposal of Brent's minimiser: parabolic step through (x, w, v) when it is
+// acceptable, else a golden-section step into the larger part of [a, b].
+struct BrentState {
+    double a, b, x, w, v, fx, fw, fv, d = 0., e = 0.;
+    double propose(double tol1) {
+        const double tol2 = 2. * tol1, xm = 0.5 * (a + b);
+        bool golden = true;
+        if (std::fabs(e) > tol1) {
+            double r = (x - w) * (fx - fv), q = (x - v) * (fx - fw), p = (x - v) * q - (x - w) * r;
+            q = 2. * (q - r);
+            if (q > 0.) p = -p;
+            q = std::fabs(q);
+            const double et = e;
+            e = d;
+            if (!(std::fabs(p) >= std::fabs(0.5 * q * et) || p <= q * (a - x) || p >= q * (b - x))) {
+                d = p / q;
+                const double uu = x + d;
+                if (uu - a < tol2 || b - uu < tol2) d = xm - x > 0. ? tol1 : -tol1;
+                golden = false;
+            }
+        }
+        if (golden) {
+            e = x >= xm ? a - x : b - x;
+            d = 0.3819660 * e;
+        }
+        return std::fabs(d) >= tol1 ? x + d : x + (d > 0. ? tol1 : -tol1);
+    }
+    void update(double u, double fu) {
+        if (fu <= fx) {
+            if (u >= x) a = x; else b = x;
+            v = w; fv = fw; w = x; fw = fx; x = u; fx = fu;
+        } else {
+            if (u < x) a = u; else b = u;
+            if (fu <= fw || w == x) { v = w; fv = fw; w = u; fw = fu; }
+            else if (fu <= fv || v == x || v == w) { v = u; fv = fu; }
+        }
+    }
+};
+
+// brent_guess (find_roots.cpp:1233-1313): Brent's minimisation on [a, b] started from
+// a guess with known value, tolerance max(tol, sqrt eps) |x| + 1e-10.
+template <class F>
+double brent_guess(double a, double b, double guess, double fguess, F&& f, double tol) {
+    const double tolc = std::max(tol, std::sqrt(kEps));
+    BrentState S{a, b, guess, guess, guess, fguess, fguess, fguess};
+    for (int ic = 0; ic < 100; ++ic) {
+        const double xm = 0.5 * (S.a + S.b), tol1 = tolc * std::fabs(S.x) + 1e-10;
+        if (std::fabs(S.x - xm) <= 2. * tol1 - 0.5 * (S.b - S.a)) break;
+        const double u = S.propose(tol1);
+        S.update(u, f(u));
+    }
+    return S.x;
+}
+
+// Brent minimisation as a resumable state machine, for many candidates in lock step
+// (brent_gsl, find_roots.cpp:1426-1473): the bracket must hold f(guess) < f(a), f(b)
+// (the condition the reference's GSL minimiser sets); converged when |b - a| < tol
+// min(|a|, |b|) (GSL's interval test with relative error tol), at most 100 steps.
+struct BrentSearch {
+    BrentState S;
+    double tol = 0., u = 0.;
+    int it = 0;
+    bool done = false, ok = false;
+    void start(double a0, double fa, double b0, double fb, double guess, double fg, double tol_in) {
+        S = BrentState{a0, b0, guess, guess, guess, fg, fg, fg};
+        tol = tol_in;
+        if (!(fg < fa && fg < fb) || !(a0 < guess && guess < b0)) { done = true; ok = false; return; }
+        u = S.propose(std::sqrt(kEps) * std::fabs(S.x) + 1e-10);
+    }
+    void feed(double fu) {
+        ++it;
+        S.update(u, fu);
+        const double lo = std::min(std::fabs(S.a), std::fabs(S.b));
+        if (std::fabs(S.b - S.a) < tol * lo || it >= 100) { done = true; ok = true; return; }
+        u = S.propose(std::sqrt(kEps) * std::fabs(S.x) + 1e-10);
+    }
+};
+
+typedef std::function<int(const double*, int, double*)> BatchEval;
+
+// opt_subdiv (find_roots.cpp:1615-1726): batches of random abscissae -- uniform on
+// odd iterations, normal about the centre of the spline error on even ones -- kept
+// at least tol (x_max - x_min) away from earlier samples; stops when the number of
+// interior local minima has not grown for `limit` batches.  Restated with its
+// behaviour kept: the two end-point evaluations are overwritten by the first batch.
+int opt_subdiv_impl(const BatchEval& f, double x_min, double x_max, int batch, int limit, double tol, uint64_t seed,
+                    std::vector<std::pair<double, double>>& xy, std::vector<int>& p) {
+    const double d = x_max - x_min;
+    double ends[2] = {x_min, x_max}, fe[2];
+    if (int r = f(ends, 2, fe)) return r;
+    xy.assign({{x_min, fe[0]}, {x_max, fe[1]}});
+    size_t n = 0, mc = 0;
+    int count = 0;
+    unsigned iter = 0;
+    double sigma = -1., mu = 0.;
+    SplitMix rng(seed);
+    std::vector<double> xt(batch), yt(batch);
+    p.clear();
+    while (count < limit && ++iter < 1000) {
+        Steffen sp;
+        const bool have = n > 3 && sp.init(xy, n);
+        for (int i = 0; i < batch; ++i) {
+            double x0 = x_min;
+            for (int tries = 0; tries < 100000; ++tries) {
+                if (iter % 2 || sigma < 0. || sigma > 3. * d || !(sigma == sigma)) {
+                    x0 = x_min + rng.uniform() * d;
+                } else {
+                    int g = 0;
+                    do x0 = rng.normal(mu, sigma);
+                    while ((x0 <= x_min || x0 >= x_max) && ++g < 1000);
+                    if (x0 <= x_min || x0 >= x_max) x0 = x_min + rng.uniform() * d;
+                }
+                bool near = false;
+                for (auto& q : xy)
+                    if (std::fabs(x0 - q.first) < tol * d) { near = true; break; }
+                if (!near) break;
+            }
+            xt[i] = x0;
+        }
+        xy.resize(n + batch);
+        if (int r = f(xt.data(), batch, yt.data())) return r;
+        for (int i = 0; i < batch; ++i) xy[n + i] = {xt[i], yt[i]};
+        if (have) {
+            double erravg = 0., errmax = 0., m = 0.;
+            int cnt = 0;
+            for (size_t i = n; i < xy.size(); ++i) {
+                double ys;
+                if (sp.eval(xy[i].first, ys)) {
+                    const double err = std::fabs(xy[i].second - ys);
+                    erravg += err;
+                    errmax = std::max(errmax, err);
+                    m += err * xy[i].first;
+                    ++cnt;
+                }
+            }
+            if (cnt >= 2 && erravg > 0. && errmax > erravg / cnt) {
+                erravg /= cnt;
+                sigma = d * erravg * (cnt - 1.) / (6. * (errmax - erravg));
+                mu = m / (erravg * cnt);
+            } else {
+                sigma = -1.;
+            }
+        }
+        std::sort(xy.begin(), xy.end());
+        n += batch;
+        p.clear();
+        for (size_t i = 1; i + 1 < n; ++i)
+            if (xy[i].second < std::min(xy[i - 1].second, xy[i + 1].second)) p.push_back((int)i);
+        if (p.size() > mc) { count = 0; mc = p.size(); }
+        else ++count;
+    }
+    return HBEM_OK;
 }
 
 }  // namespace
@@ -247,6 +496,112 @@ int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npo
             ++cnt;
         }
     *nroots = cnt;
+    if (n_evals) *n_evals = evals;
+    return HBEM_OK;
+}
+
+int hbem_opt_subdiv(hbem_fn_batch f, void* user, double x_min, double x_max, int batch_size, int limit, double tol,
+                    unsigned long long seed, double* x_out, double* y_out, int max_points, int* n_points,
+                    int* minima_out, int max_minima, int* n_minima) {
+    if (!f || !(x_max > x_min) || batch_size < 1 || limit < 1 || !(tol >= 0.) || !n_points || !n_minima)
+        return HBEM_ERR_INVALID;
+    std::vector<std::pair<double, double>> xy;
+    std::vector<int> p;
+    BatchEval ev = [&](const double* xs, int n, double* ys) {
+        f(xs, n, ys, user);
+        return (int)HBEM_OK;
+    };
+    if (int r = opt_subdiv_impl(ev, x_min, x_max, batch_size, limit, tol, seed, xy, p)) return r;
+    *n_points = (int)xy.size();
+    for (size_t i = 0; i < xy.size() && (int)i < max_points; ++i) {
+        if (x_out) x_out[i] = xy[i].first;
+        if (y_out) y_out[i] = xy[i].second;
+    }
+    *n_minima = (int)p.size();
+    for (size_t i = 0; i < p.size() && (int)i < max_minima; ++i)
+        if (minima_out) minima_out[i] = p[i];
+    return HBEM_OK;
+}
+
+int hbem_find_resonances_adaptive(hbem_solop s, double k_min, double k_max, double c_o, double c_i, int batch_size,
+                                  int limit, double sample_tol, double tol, unsigned long long seed, int sketch,
+                                  int q, double* roots_host, int max_roots, int* nroots, int* n_samples,
+                                  int* n_evals) {
+    if (!s || !(k_max > k_min) || batch_size < 1 || limit < 1 || !(tol > 0.) || sketch < 1 || q < 0 || !nroots)
+        return HBEM_ERR_INVALID;
+    int N = 0;
+    if (int r = hbem_solop_info(s, &N)) return r;
+    const int n = 2 * N;
+    if (sketch > n) return HBEM_ERR_INVALID;
+    int evals = 0;
+    // sampling evaluator: randomized_svd::sv on a sketch of width `sketch`
+    // (examples/find_resonances.cpp:135-139)
+    BatchEval f_sample = [&](const double* ks, int nk, double* ys) {
+        evals += nk;
+        return hbem_sigma_rsvd_sweep(s, ks, nk, c_o, c_i, sketch, q, 0, seed, ys);
+    };
+    // local-search evaluator (the reference: arnoldi::sv): dense sigma_min for T up to
+    // order 100, else the randomized estimate on a 16-wide sketch with q + 1 steps
+    BatchEval f_fine = [&](const double* ks, int nk, double* ys) {
+        evals += nk;
+        if (n <= 100) {
+            std::vector<double> out(3 * (size_t)nk);
+            if (int r = hbem_sweep_sigma(s, ks, nk, c_o, c_i, 0, out.data())) return r;
+            for (int i = 0; i < nk; ++i) ys[i] = out[3 * (size_t)i];
+            return (int)HBEM_OK;
+        }
+        return hbem_sigma_rsvd_sweep(s, ks, nk, c_o, c_i, std::min(n, std::max(16, sketch)), q + 1, 0, seed + 1, ys);
+    };
+    std::vector<std::pair<double, double>> xy;
+    std::vector<int> loc;
+    if (int r = opt_subdiv_impl(f_sample, k_min, k_max, batch_size, limit, sample_tol, seed, xy, loc)) return r;
+    const int np = (int)xy.size();
+    if (n_samples) *n_samples = np;
+    std::vector<double> kv(np), rsv(np);
+    for (int i = 0; i < np; ++i) { kv[i] = xy[i].first; rsv[i] = xy[i].second; }
+    // improve each candidate on a barycentric rational interpolant of its convex
+    // neighbourhood (find_resonances.cpp:179-208)
+    const size_t nc = loc.size();
+    std::vector<double> A(nc), B(nc), G(nc);
+    for (size_t c = 0; c < nc; ++c) {
+        const int pos = loc[c];
+        int il = pos, ir = pos;
+        while (ir + 1 < np && rsv[ir - 1] + rsv[ir + 1] > 2. * rsv[ir]) ++ir;
+        while (il > 0 && rsv[il - 1] + rsv[il + 1] > 2. * rsv[il]) --il;
+        const int cnt = ir - il + 1;
+        BaryRat interp;
+        interp.init(&kv[il], &rsv[il], cnt, std::min(5, cnt - 1));
+        A[c] = kv[pos - 1];
+        B[c] = kv[pos + 1];
+        double g = brent_guess(A[c], B[c], kv[pos], interp(kv[pos]), interp, tol);
+        if (!(g > A[c] && g < B[c])) g = kv[pos];
+        G[c] = g;
+    }
+    // lock-step Brent searches, one batched evaluation per round (find_resonances.cpp:225-237)
+    std::vector<BrentSearch> bs(nc);
+    if (nc) {
+        std::vector<double> xs(3 * nc), ys(3 * nc);
+        for (size_t c = 0; c < nc; ++c) { xs[3 * c] = A[c]; xs[3 * c + 1] = B[c]; xs[3 * c + 2] = G[c]; }
+        if (int r = f_fine(xs.data(), (int)xs.size(), ys.data())) return r;
+        for (size_t c = 0; c < nc; ++c) bs[c].start(A[c], ys[3 * c], B[c], ys[3 * c + 1], G[c], ys[3 * c + 2], tol);
+    }
+    for (int round = 0; round < 200; ++round) {
+        std::vector<double> xs;
+        std::vector<size_t> who;
+        for (size_t c = 0; c < nc; ++c)
+            if (!bs[c].done) { xs.push_back(bs[c].u); who.push_back(c); }
+        if (xs.empty()) break;
+        std::vector<double> ys(xs.size());
+        if (int r = f_fine(xs.data(), (int)xs.size(), ys.data())) return r;
+        for (size_t w = 0; w < who.size(); ++w) bs[who[w]].feed(ys[w]);
+    }
+    std::vector<double> roots;
+    for (auto& b : bs)
+        if (b.ok && std::isfinite(b.S.x)) roots.push_back(b.S.x);
+    std::sort(roots.begin(), roots.end());
+    *nroots = (int)roots.size();
+    for (size_t i = 0; i < roots.size() && (int)i < max_roots; ++i)
+        if (roots_host) roots_host[i] = roots[i];
     if (n_evals) *n_evals = evals;
     return HBEM_OK;
 }

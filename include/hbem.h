@@ -202,6 +202,15 @@ int hbem_lu_factor_batch_device(int n, int nmat, void* A_dev, long long stride, 
 int hbem_lu_solve_batch_device(int n, int nmat, int trans, const void* LU_dev, long long stride, const int* piv_dev,
                                int nrhs, void* X_dev, long long xstride);
 
+/* Number of panels N of the operator's mesh (T is 2N x 2N).                       */
+int hbem_solop_info(hbem_solop s, int* npanels);
+
+/* sigma_min(k) along a list of real wavenumbers by randomized_svd::sv on a seeded
+ * sketch of width `sketch` with q subspace steps (the sampling evaluator of
+ * examples/find_resonances.cpp:135-139); precision as hbem_rsvd_sv_batch_device_ex. */
+int hbem_sigma_rsvd_sweep(hbem_solop s, const double* k_host, int nk, double c_o, double c_i, int sketch, int q,
+                          int precision, unsigned long long seed, double* sigma_out);
+
 /* sigma_min(k) and its derivatives along a list of real wavenumbers, end to end:
  * gen_sol_op_*der + direct::sv_*der per k (examples/roots_newton_circle.cpp:111-138).
  * out_host[3i + t]. */
@@ -220,10 +229,28 @@ int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npo
                                double tol, double* roots_host, int max_roots, int* nroots, double* grid_host,
                                int* n_evals);
 
+/* Adaptive resonance search (examples/find_resonances.cpp:128-250 with the sampler
+ * opt_subdiv, source/utilities/find_roots.cpp:1615-1726): batches of batch_size
+ * random wavenumbers (seeded; uniform, then normal about the error of a Steffen
+ * monotone spline through the samples) with sigma_min by randomized_svd::sv on a
+ * `sketch`-wide sketch with q steps, until the number of local minima has not grown
+ * for `limit` batches (samples kept sample_tol (k_max - k_min) apart); each minimum
+ * improved on a Floater-Hormann rational interpolant (order 5) and refined by Brent
+ * minimisation of sigma_min (dense sigma for T up to order 100, else a 16-wide
+ * sketch) to relative interval tol, all candidates in one batch per round.  The
+ * mesh is the caller's (the reference's panel-count choice is left to it).
+ * roots_host: up to max_roots minima, *nroots their count; *n_samples, *n_evals
+ * (may be NULL) the sample count and the T(k) evaluations.                        */
+int hbem_find_resonances_adaptive(hbem_solop s, double k_min, double k_max, double c_o, double c_i, int batch_size,
+                                  int limit, double sample_tol, double tol, unsigned long long seed, int sketch,
+                                  int q, double* roots_host, int max_roots, int* nroots, int* n_samples,
+                                  int* n_evals);
+
 /* ------------------------------------------------------------------ root finding (host) */
 
 typedef double (*hbem_fn)(double x, void* user);
 typedef void (*hbem_fn_both)(double x, double* f, double* df, void* user);
+typedef void (*hbem_fn_batch)(const double* x, int n, double* y, void* user);
 
 /* rtsafe (include/find_roots.hpp:37-49; source/utilities/find_roots.cpp:117-217):
  * safeguarded Newton; returns the root, sets *root_found and *num_iter. */
@@ -234,6 +261,14 @@ double hbem_zbrent(hbem_fn f, void* user, double x1, double x2, double tol, int*
 /* BrentMinimizer(a, b, tol).local_min_rc driven to completion
  * (include/find_roots.hpp:181-233; source/utilities/find_roots.cpp:1003-1184) */
 double hbem_brent_min(hbem_fn f, void* user, double a, double b, double tol);
+
+/* opt_subdiv (find_roots.cpp:1615-1726) for any batched function f: samples sorted
+ * by x into x_out / y_out (up to max_points; *n_points their number) and the
+ * indices of interior local minima into minima_out (*n_minima).  The reference
+ * seeds from std::random_device; here `seed` (SplitMix64, Box-Muller normals).   */
+int hbem_opt_subdiv(hbem_fn_batch f, void* user, double x_min, double x_max, int batch_size, int limit, double tol,
+                    unsigned long long seed, double* x_out, double* y_out, int max_points, int* n_points,
+                    int* minima_out, int max_minima, int* n_minima);
 
 #ifdef __cplusplus
 }

@@ -630,3 +630,265 @@ def plain_sweep(evald, ks, tol=1e-8):
         if ok and root == root:
             roots.append(root)
     return np.array(roots), sig
+
+
+# ----------------------------------------------------------------- adaptive search
+
+_M64 = (1 << 64) - 1
+
+
+class SplitMix:
+    """SplitMix64 (Steele, Lea, Flood 2014): the seeded generator of the adaptive
+    sampler (the reference seeds std::mt19937 from std::random_device)."""
+
+    def __init__(self, seed):
+        self.s = seed & _M64
+
+    def next(self):
+        self.s = (self.s + 0x9E3779B97F4A7C15) & _M64
+        z = self.s
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _M64
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _M64
+        return z ^ (z >> 31)
+
+    def uniform(self):
+        return (self.next() >> 11) * (1.0 / 9007199254740992.0)
+
+    def normal(self, mu, sd):
+        u1, u2 = self.uniform(), self.uniform()
+        if u1 <= 0.0:
+            u1 = 1.0 / 9007199254740992.0
+        return mu + sd * math.sqrt(-2.0 * math.log(u1)) * math.cos(2.0 * math.pi * u2)
+
+
+def steffen_slopes(x, y):
+    """Slopes of Steffen's monotone cubic (A&A 239 (1990) 443), boundary eqs. 26-27."""
+    n = len(x)
+    h = np.diff(x)
+    s = np.diff(y) / h
+    yp = np.zeros(n)
+    for i in range(1, n - 1):
+        p = (s[i - 1] * h[i] + s[i] * h[i - 1]) / (h[i - 1] + h[i])
+        yp[i] = (np.sign(s[i - 1]) + np.sign(s[i])) * min(abs(s[i - 1]), abs(s[i]), 0.5 * abs(p))
+
+    def bound(s0, s1, h0, h1):
+        p = s0 * (1.0 + h0 / (h0 + h1)) - s1 * h0 / (h0 + h1)
+        if p * s0 <= 0.0:
+            return 0.0
+        return 2.0 * s0 if abs(p) > 2.0 * abs(s0) else p
+
+    yp[0] = bound(s[0], s[1], h[0], h[1])
+    yp[n - 1] = bound(s[n - 2], s[n - 3], h[n - 2], h[n - 3])
+    return yp
+
+
+def steffen_eval(x, y, yp, t):
+    if not (x[0] <= t <= x[-1]):
+        return None
+    i = int(np.searchsorted(x, t, side="right")) - 1
+    i = min(max(i, 0), len(x) - 2)
+    h = x[i + 1] - x[i]
+    sl = (y[i + 1] - y[i]) / h
+    dt = t - x[i]
+    a = (yp[i] + yp[i + 1] - 2.0 * sl) / (h * h)
+    b = (3.0 * sl - 2.0 * yp[i] - yp[i + 1]) / h
+    return y[i] + dt * (yp[i] + dt * (b + dt * a))
+
+
+def floater_hormann(xs, ys, d):
+    """Barycentric rational interpolant of Floater and Hormann (2007), order d."""
+    n = len(xs)
+    w = np.zeros(n)
+    for k in range(n):
+        for i in range(max(0, k - d), min(k, n - 1 - d) + 1):
+            prod = 1.0
+            for j in range(i, i + d + 1):
+                if j != k:
+                    prod /= (xs[k] - xs[j])
+            w[k] += (-1.0 if i % 2 else 1.0) * prod
+
+    def r(t):
+        num = den = 0.0
+        for k in range(n):
+            if t == xs[k]:
+                return ys[k]
+            c = w[k] / (t - xs[k])
+            num += c * ys[k]
+            den += c
+        return num / den
+    return r
+
+
+class _Brent:
+    """Brent's minimiser state: parabolic step through (x, w, v) or golden section."""
+
+    def __init__(self, a, b, x, fx):
+        self.a, self.b = a, b
+        self.x = self.w = self.v = x
+        self.fx = self.fw = self.fv = fx
+        self.d = self.e = 0.0
+
+    def propose(self, tol1):
+        a, b, x, w, v = self.a, self.b, self.x, self.w, self.v
+        fx, fw, fv = self.fx, self.fw, self.fv
+        tol2 = 2.0 * tol1
+        xm = 0.5 * (a + b)
+        golden = True
+        if abs(self.e) > tol1:
+            r = (x - w) * (fx - fv)
+            q = (x - v) * (fx - fw)
+            p = (x - v) * q - (x - w) * r
+            q = 2.0 * (q - r)
+            if q > 0.0:
+                p = -p
+            q = abs(q)
+            et = self.e
+            self.e = self.d
+            if not (abs(p) >= abs(0.5 * q * et) or p <= q * (a - x) or p >= q * (b - x)):
+                self.d = p / q
+                u = x + self.d
+                if u - a < tol2 or b - u < tol2:
+                    self.d = tol1 if xm - x > 0.0 else -tol1
+                golden = False
+        if golden:
+            self.e = a - x if x >= xm else b - x
+            self.d = 0.3819660 * self.e
+        return x + self.d if abs(self.d) >= tol1 else x + (tol1 if self.d > 0 else -tol1)
+
+    def update(self, u, fu):
+        if fu <= self.fx:
+            if u >= self.x:
+                self.a = self.x
+            else:
+                self.b = self.x
+            self.v, self.fv, self.w, self.fw, self.x, self.fx = self.w, self.fw, self.x, self.fx, u, fu
+        else:
+            if u < self.x:
+                self.a = u
+            else:
+                self.b = u
+            if fu <= self.fw or self.w == self.x:
+                self.v, self.fv, self.w, self.fw = self.w, self.fw, u, fu
+            elif fu <= self.fv or self.v == self.x or self.v == self.w:
+                self.v, self.fv = u, fu
+
+
+def brent_guess(a, b, guess, fguess, f, tol):
+    """brent_guess (find_roots.cpp:1233-1313)."""
+    tolc = max(tol, math.sqrt(EPS))
+    S = _Brent(a, b, guess, fguess)
+    for _ in range(100):
+        xm = 0.5 * (S.a + S.b)
+        tol1 = tolc * abs(S.x) + 1e-10
+        if abs(S.x - xm) <= 2.0 * tol1 - 0.5 * (S.b - S.a):
+            break
+        u = S.propose(tol1)
+        S.update(u, f(u))
+    return S.x
+
+
+def brent_search(a, fa, b, fb, guess, fg, f, tol):
+    """brent_gsl (find_roots.cpp:1426-1473) restated: requires f(guess) < f(a), f(b);
+    stops when |b - a| < tol min(|a|, |b|) or after 100 steps.  None if the bracket
+    is refused."""
+    if not (fg < fa and fg < fb and a < guess < b):
+        return None
+    S = _Brent(a, b, guess, fg)
+    for _ in range(100):
+        u = S.propose(math.sqrt(EPS) * abs(S.x) + 1e-10)
+        S.update(u, f(u))
+        if abs(S.b - S.a) < tol * min(abs(S.a), abs(S.b)):
+            break
+    return S.x
+
+
+def opt_subdiv(fbatch, x_min, x_max, batch, limit, tol, seed):
+    """opt_subdiv (find_roots.cpp:1615-1726), seeded; returns sorted (x, y) and the
+    indices of interior local minima."""
+    d = x_max - x_min
+    fe = fbatch([x_min, x_max])
+    xy = [(x_min, fe[0]), (x_max, fe[1])]
+    n, count, mc, it = 0, 0, 0, 0
+    sigma, mu = -1.0, 0.0
+    rng = SplitMix(seed)
+    p = []
+    while count < limit:
+        it += 1
+        if it >= 1000:
+            break
+        have = False
+        if n > 3:
+            xs = np.array([q[0] for q in xy[:n]])
+            ys = np.array([q[1] for q in xy[:n]])
+            if np.all(np.diff(xs) > 0):
+                yp = steffen_slopes(xs, ys)
+                have = True
+        xt = []
+        for _ in range(batch):
+            x0 = x_min
+            for _tries in range(100000):
+                if it % 2 or sigma < 0.0 or sigma > 3.0 * d or sigma != sigma:
+                    x0 = x_min + rng.uniform() * d
+                else:
+                    g = 0
+                    while True:
+                        x0 = rng.normal(mu, sigma)
+                        g += 1
+                        if not (x0 <= x_min or x0 >= x_max) or g >= 1000:
+                            break
+                    if x0 <= x_min or x0 >= x_max:
+                        x0 = x_min + rng.uniform() * d
+                if not any(abs(x0 - q[0]) < tol * d for q in xy):
+                    break
+            xt.append(x0)
+        del xy[n:]
+        yt = fbatch(xt)
+        xy += list(zip(xt, yt))
+        if have:
+            errs = []
+            for xv, yv in xy[n:]:
+                s_ = steffen_eval(xs, ys, yp, xv)
+                if s_ is not None:
+                    errs.append((abs(yv - s_), xv))
+            cnt = len(errs)
+            tot = sum(e_ for e_, _ in errs)
+            emax = max((e_ for e_, _ in errs), default=0.0)
+            if cnt >= 2 and tot > 0.0 and emax > tot / cnt:
+                avg = tot / cnt
+                sigma = d * avg * (cnt - 1.0) / (6.0 * (emax - avg))
+                mu = sum(e_ * xv for e_, xv in errs) / (avg * cnt)
+            else:
+                sigma = -1.0
+        xy.sort()
+        n += batch
+        p = [i for i in range(1, n - 1) if xy[i][1] < min(xy[i - 1][1], xy[i + 1][1])]
+        if len(p) > mc:
+            count, mc = 0, len(p)
+        else:
+            count += 1
+    return np.array([q[0] for q in xy]), np.array([q[1] for q in xy]), p
+
+
+def find_resonances_adaptive(f_sample, f_fine, k_min, k_max, batch, limit, sample_tol, tol, seed):
+    """The search of examples/find_resonances.cpp:128-250 (mesh given): opt_subdiv
+    with f_sample, rational interpolation + brent_guess per minimum, Brent on f_fine."""
+    kv, rsv, loc = opt_subdiv(f_sample, k_min, k_max, batch, limit, sample_tol, seed)
+    np_ = len(kv)
+    roots = []
+    for pos in loc:
+        il = ir = pos
+        while ir + 1 < np_ and rsv[ir - 1] + rsv[ir + 1] > 2.0 * rsv[ir]:
+            ir += 1
+        while il > 0 and rsv[il - 1] + rsv[il + 1] > 2.0 * rsv[il]:
+            il -= 1
+        cnt = ir - il + 1
+        interp = floater_hormann(kv[il:ir + 1], rsv[il:ir + 1], min(5, cnt - 1))
+        a, b = kv[pos - 1], kv[pos + 1]
+        g = brent_guess(a, b, kv[pos], interp(kv[pos]), interp, tol)
+        if not (a < g < b):
+            g = kv[pos]
+        fa, fb, fg = f_fine([a, b, g])
+        r = brent_search(a, fa, b, fb, g, fg, lambda x: f_fine([x])[0], tol)
+        if r is not None and math.isfinite(r):
+            roots.append(r)
+    return np.sort(np.array(roots)), np_

@@ -457,6 +457,27 @@ def combine_ranks(tot_ms, tot_v, world):
     return t.item(), v.item()
 
 
+def adaptive_search(torch, so, plain_roots):
+    """The reference's find_resonances search (opt_subdiv sampling with randomized
+    sigma on a 2-wide sketch, q = 2, batches of 64; rational-interpolation guess;
+    Brent on the dense sigma to relative interval 1e-9) on the bench workload, one run
+    after a warm-up, and how many of its minima coincide with the plain search's
+    roots (within 1e-6)."""
+    import time
+    kw = dict(batch_size=64, limit=10, tol=1e-9, seed=1, sketch=2, q=2)
+    so.find_resonances_adaptive(CFG["k_min"], CFG["k_max"], CFG["c_o"], CFG["c_i"], **kw)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    roots, ns, ne = so.find_resonances_adaptive(CFG["k_min"], CFG["k_max"], CFG["c_o"], CFG["c_i"], **kw)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    match = sum(1 for r in roots if plain_roots.size and np.min(np.abs(plain_roots - r)) <= 1e-6)
+    return {"workload": "adaptive search (opt_subdiv, batch 64, limit 10, sketch 2, q 2; Brent on dense sigma, "
+                        "relative interval 1e-9), same scatterer and k range as the bench line",
+            "seconds": dt, "minima": int(roots.size), "samples": ns, "T_evals": ne,
+            "minima_matching_plain_roots": int(match), "plain_roots": int(plain_roots.size)}
+
+
 def run_gpu(args):
     rank, world, local = dist_env()
     import torch
@@ -554,6 +575,7 @@ def run_gpu(args):
     tail = dense_tail_at_scale(torch, C, api, geometry, lib, peak)
     prec = precision_at_scale(torch, C, api, geometry, lib)
     batch = batching_sample(torch, C, api, geometry, lib)
+    adapt = adaptive_search(torch, so, step(so)[1])
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
@@ -580,6 +602,7 @@ def run_gpu(args):
             "dense_tail_at_scale": tail,
             "precision_at_scale": prec,
             "batching_sample": batch,
+            "adaptive_search": adapt,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }

@@ -25,7 +25,7 @@ EXPORTS = [
     "hbem_sv_dense_batch", "hbem_sweep_sigma", "hbem_rand_sketch", "hbem_rsvd_sv_batch",
     "hbem_rsvd_sv_batch_device", "hbem_rsvd_sv_batch_device_ex", "hbem_lu_factor_batch_device", "hbem_lu_solve_batch_device",
     "hbem_cgemm_f32_batch_device", "hbem_solop_info", "hbem_sigma_rsvd_sweep", "hbem_opt_subdiv",
-    "hbem_find_resonances_adaptive",
+    "hbem_find_resonances_adaptive", "hbem_arnoldi_sv_batch", "hbem_arnoldi_sv_batch_device",
     "hbem_find_resonances_plain", "hbem_rtsafe", "hbem_zbrent", "hbem_brent_min",
 ]
 
@@ -95,6 +95,9 @@ def load(path=LIB_PATH):
                                            _dp]),
         "hbem_rsvd_sv_batch_device_ex": (_i, [_i, _i, _u, _vp, ctypes.c_longlong, ctypes.c_longlong, _vp, _i, _i,
                                               _i, _i, _dp]),
+        "hbem_arnoldi_sv_batch": (_i, [_i, _i, _u, _i, _d, _dp, _dp, _ip]),
+        "hbem_arnoldi_sv_batch_device": (_i, [_i, _i, _u, _i, _d, _vp, ctypes.c_longlong, ctypes.c_longlong, _dp, _ip,
+                                              _ip]),
         "hbem_cgemm_f32_batch_device": (_i, [_i, _i, _i, _vp, ctypes.c_longlong, ctypes.c_longlong, _vp,
                                              ctypes.c_longlong, ctypes.c_longlong, _vp, ctypes.c_longlong,
                                              ctypes.c_longlong, _i, _i]),

@@ -241,6 +241,31 @@ def rsvd_sv(Ts, R, q=0, d=0):
                                      int(q), dptr(out)))
     return out
 
+def arnoldi_sv(Ts, count=1, acc=0.0, d=0, return_status=False):
+    """arnoldi::sv (d = 0) / sv_1st_der (d = 1) / sv_2nd_der (d = 2) for a batch
+    (include/singular_values_arnoldi.hpp:29-66): Ts is a list of [T], [T, T'] or
+    [T, T', T''].  Returns (nmat, count, d + 1): the count smallest singular values
+    in ascending order with their derivatives.  A matrix whose iteration reaches the
+    cap keeps its last iterate and raises HbemError (status 4) unless return_status
+    is set, in which case (values, status, ...) is returned with per-matrix status
+    0 converged / 5 singular / 6 iteration cap."""
+    nmat = len(Ts)
+    n = Ts[0][0].shape[0]
+    buf = np.zeros((nmat, d + 1, n, n), np.complex128)
+    for m, mats in enumerate(Ts):
+        for t in range(d + 1):
+            buf[m, t] = np.asarray(mats[t]).T
+    out = np.zeros((nmat, count, d + 1))
+    status = np.zeros(nmat, np.int32)
+    rc = C.lib().hbem_arnoldi_sv_batch(n, nmat, int(d), int(count), float(acc), buf.ctypes.data_as(C._dp),
+                                       dptr(out), iptr(status))
+    if return_status:
+        if rc not in (0, 4, 5):
+            check(rc)
+        return out, status
+    check(rc)
+    return out
+
 def opt_subdiv(f, x_min, x_max, batch_size, limit, tol, seed=0, max_points=100000):
     """opt_subdiv for a batched Python function f(xs) -> ys: returns (x, y, minima)."""
     def _f(xp, n, yp, user):

@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libhbem.so")
-SOURCES = ["assemble.cu", "solop.cu", "dense.cu", "lu.cu", "tc_gemm.cu", "rsvd.cu", "capi.cu", "roots.cu"]
+SOURCES = ["assemble.cu", "solop.cu", "dense.cu", "lu.cu", "tc_gemm.cu", "rsvd.cu", "arnoldi.cu", "capi.cu", "roots.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xcompiler", "-Wall", "-Wno-deprecated-gpu-targets"]

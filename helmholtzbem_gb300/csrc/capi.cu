@@ -44,6 +44,12 @@ cudaError_t launch_cgemm_f32(int m, int n, int k, const cplxf* A, long long lda,
                              long long ldb, long long sb, cplxf* C, long long ldc, long long sc, int nmat,
                              int use_tc, int* err, cudaStream_t st);
 size_t svd_fast_smem_bytes(int n);
+bool arnoldi_supported(int n, int count, int D);
+size_t arnoldi_work_bytes(int n, int nmat, int count, int D);
+cudaError_t arnoldi_batched(int n, int nmat, int count, int D, double tol, int maxit, unsigned long long seed,
+                            const cplx* T, long long mat_stride, long long der_stride, double* out, void* work,
+                            size_t work_bytes, int* status_host, int* iters_host, cudaStream_t st,
+                            long long* launches);
 cudaError_t launch_svd_fast(int n, int nmat, int D, const cplx* T, long long mat_stride, long long der_stride,
                             double* out, int* status, cudaStream_t st);
 }  // namespace hbem
@@ -64,6 +70,7 @@ double g_asm_ms = 0.;
 long long g_asm_launches = 0;
 long long g_asm_points = 0;   // quadrature points x media processed by timed launches
 int g_svd_fast = 1;           // dense sigma: FP32 Jacobi + FP64 refinement where it fits
+int g_arnoldi_maxit = 1000;   // block iterations of hbem_arnoldi_sv_batch*
 
 int fail(int code, const std::string& msg) {
     g_err = msg;
@@ -328,6 +335,11 @@ int hbem_set_option(const char* name, int value) {
     }
     if (k == "svd_fast") {
         g_svd_fast = value ? 1 : 0;
+        return HBEM_OK;
+    }
+    if (k == "arnoldi_maxit") {
+        if (value < 1) return fail(HBEM_ERR_INVALID, "set_option: arnoldi_maxit must be >= 1");
+        g_arnoldi_maxit = value;
         return HBEM_OK;
     }
     return fail(HBEM_ERR_INVALID, "set_option: unknown option " + k);
@@ -777,6 +789,68 @@ int hbem_rsvd_sv_batch(int n, int nmat, unsigned d, const double* T_host, const 
     HB_CK(cudaMemcpy(T.p, T_host, bytes, cudaMemcpyHostToDevice));
     HB_CK(cudaMemcpy(R.p, R_host, (size_t)n * s * sizeof(cplx), cudaMemcpyHostToDevice));
     return hbem_rsvd_sv_batch_device(n, nmat, d, T.p, (long long)((d + 1) * nn), (long long)nn, R.p, s, q, out_host);
+}
+
+int hbem_arnoldi_sv_batch_device(int n, int nmat, unsigned d, int count, double acc, const void* T_dev,
+                                 long long mat_stride, long long der_stride, double* out_host, int* status_host,
+                                 int* iters_host) {
+    if (n < 2 || nmat < 1 || nmat > 65535 || d > 2 || count < 1 || count > n || !T_dev || !out_host ||
+        !(acc >= 0.) || (long long)nmat * count > 65535)
+        return fail(HBEM_ERR_INVALID, "arnoldi_sv_batch: bad argument");
+    HB_CK(cudaSetDevice(g_device));
+    // ARPACK takes tol <= 0 as machine precision; the FP64 residual of the block
+    // iteration bottoms out near a few tens of eps
+    const double tol = std::max(acc > 0. ? acc : kMachEps, 64. * kMachEps);
+    const size_t os = d + 1, nout = (size_t)nmat * count * os;
+    std::vector<int> stat(nmat, 0), iters(nmat, 0);
+    if (arnoldi_supported(n, count, (int)d)) {
+        static thread_local DBuf out, work;
+        HB_CK(out.ensure(nout * sizeof(double)));
+        HB_CK(work.ensure(std::max<size_t>(arnoldi_work_bytes(n, nmat, count, (int)d), 256)));
+        long long nl = 0;
+        HB_CK(arnoldi_batched(n, nmat, count, (int)d, tol, g_arnoldi_maxit, 0x5eedULL,
+                              static_cast<const cplx*>(T_dev), mat_stride, der_stride, out.as<double>(), work.p,
+                              work.cap, stat.data(), iters.data(), 0, &nl));
+        g_launches += nl;
+        HB_CK(cudaMemcpy(out_host, out.p, nout * sizeof(double), cudaMemcpyDeviceToHost));
+    } else {
+        // more singular values than the block holds: all n of them by the dense Jacobi
+        // kernel, the count smallest kept (derivatives only through the block path)
+        if (d > 0)
+            return fail(HBEM_ERR_UNSUPPORTED, "arnoldi_sv_batch: derivatives need count <= 28 (block of 32 columns)");
+        static thread_local DBuf A, V, out3, sdev, sig;
+        std::vector<double> o3((size_t)nmat * 3), all((size_t)nmat * n);
+        const int r = sv_batch(0, n, nmat, 0, static_cast<const cplx*>(T_dev), mat_stride, 0, A, V, out3, sdev, &sig,
+                               o3.data(), all.data());
+        if (r) return r;
+        for (int m = 0; m < nmat; ++m) {
+            std::sort(all.begin() + (size_t)m * n, all.begin() + (size_t)(m + 1) * n);
+            for (int j = 0; j < count; ++j) out_host[(size_t)m * count + j] = all[(size_t)m * n + j];
+        }
+    }
+    if (status_host) std::copy(stat.begin(), stat.end(), status_host);
+    if (iters_host) std::copy(iters.begin(), iters.end(), iters_host);
+    int worst = 0;
+    for (int m = 0; m < nmat; ++m) {
+        if (stat[m] == 5)
+            for (size_t e = (size_t)m * count * os; e < (size_t)(m + 1) * count * os; ++e) out_host[e] = NAN;
+        worst = std::max(worst, stat[m]);
+    }
+    if (worst == 5) return fail(HBEM_ERR_SINGULAR, "arnoldi_sv_batch: zero pivot in the LU of T");
+    if (worst == 6) return fail(HBEM_ERR_NOCONV, "arnoldi_sv_batch: maximum number of iterations taken");
+    return HBEM_OK;
+}
+
+int hbem_arnoldi_sv_batch(int n, int nmat, unsigned d, int count, double acc, const double* T_host,
+                          double* out_host, int* status_host) {
+    if (n < 2 || nmat < 1 || d > 2 || !T_host || !out_host) return fail(HBEM_ERR_INVALID, "arnoldi_sv_batch: bad argument");
+    HB_CK(cudaSetDevice(g_device));
+    static thread_local DBuf T;
+    const size_t nn = (size_t)n * n, bytes = (size_t)nmat * (d + 1) * nn * sizeof(cplx);
+    HB_CK(T.ensure(bytes));
+    HB_CK(cudaMemcpy(T.p, T_host, bytes, cudaMemcpyHostToDevice));
+    return hbem_arnoldi_sv_batch_device(n, nmat, d, count, acc, T.p, (long long)((d + 1) * nn), (long long)nn,
+                                        out_host, status_host, nullptr);
 }
 
 int hbem_cgemm_f32_batch_device(int m, int n, int k, const void* A, long long lda, long long sa, const void* B,

@@ -182,8 +182,9 @@ __global__ void __launch_bounds__(kRsvdThreads) k_rsvd_tail(int n, int s, int D,
 
 // After the inverse-iteration steps: v <- v / |v|, u = T v / |T v|, and
 // sigma' = Re u^H T' v (the Wielandt form x^H W' x with x = (u; v)/sqrt2).
+// Vector blockIdx.x belongs to matrix blockIdx.x / per.
 __global__ void __launch_bounds__(kRsvdThreads) k_rsvd_vec(int n, int D, const cplx* T, long long mat_stride,
-                                                            long long der_stride, double* out, cplx* uv) {
+                                                            long long der_stride, double* out, cplx* uv, int per) {
     __shared__ double red[128];
     const int mat = blockIdx.x, os = D + 1;
     cplx* u = uv + 2LL * n * mat;
@@ -194,7 +195,7 @@ __global__ void __launch_bounds__(kRsvdThreads) k_rsvd_vec(int n, int D, const c
     const double iv = nv > 0. ? 1. / nv : 0.;
     for (int r = threadIdx.x; r < n; r += blockDim.x) v[r] = iv * v[r];
     __syncthreads();
-    const cplx* Tm = T + (long long)mat * mat_stride;
+    const cplx* Tm = T + (long long)(mat / per) * mat_stride;
     part = 0.;
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
         cplx a = mk(0.);
@@ -260,11 +261,11 @@ __global__ void __launch_bounds__(256) k_sv2_prep(int n, const cplx* uv, cplx* u
     for (int l = threadIdx.x; l < n2; l += blockDim.x) ub[(long long)n2 * mat + l] = x[l] * ixm;
 }
 
-__global__ void k_build_bordered(int n, const cplx* T, long long mat_stride, const double* out, int os,
+__global__ void k_build_bordered(int n, const cplx* T, long long mat_stride, int per, const double* out, int os,
                                  const cplx* ub, const int* mcol, cplx* B) {
     const int mat = blockIdx.y, n2 = 2 * n, m = mcol[mat];
     const double sig = out[(long long)os * mat];
-    const cplx* Tm = T + (long long)mat * mat_stride;
+    const cplx* Tm = T + (long long)(mat / per) * mat_stride;
     const cplx* u = ub + (long long)n2 * mat;
     cplx* Bm = B + (long long)n2 * n2 * mat;
     const long long tot = (long long)n2 * n2;
@@ -281,11 +282,11 @@ __global__ void k_build_bordered(int n, const cplx* T, long long mat_stride, con
     }
 }
 
-// y = alpha [A x2; A^H x1] (+ y if acc), A = matrix mat of the batch, x = [x1; x2]
-__global__ void __launch_bounds__(256) k_wapply(int n, const cplx* A, long long mat_stride, const cplx* x, cplx* y,
-                                                double alpha, int acc) {
+// y = alpha [A x2; A^H x1] (+ y if acc), A = matrix mat / per of the batch, x = [x1; x2]
+__global__ void __launch_bounds__(256) k_wapply(int n, const cplx* A, long long mat_stride, int per, const cplx* x,
+                                                cplx* y, double alpha, int acc) {
     const int mat = blockIdx.x, n2 = 2 * n;
-    const cplx* Am = A + (long long)mat * mat_stride;
+    const cplx* Am = A + (long long)(mat / per) * mat_stride;
     const cplx* x1 = x + (long long)n2 * mat;
     const cplx* x2 = x1 + n;
     cplx* y1 = y + (long long)n2 * mat;
@@ -474,6 +475,14 @@ cudaError_t solve_mixed(int n, int nmat, int trans, const MixedBufs& mb, const c
 
 // ------------------------------------------------------------------ orchestration
 
+struct Sv2Work {
+    cplx *B = nullptr, *ub = nullptr, *ud = nullptr, *rhs = nullptr, *tb = nullptr;
+    int *piv2 = nullptr, *perm2 = nullptr, *info2 = nullptr, *mcol = nullptr;
+};
+cudaError_t sv_der_from_vectors(int n, int nvec, int per, int D, const cplx* T, long long mat_stride,
+                                long long der_stride, double* out, cplx* uv, const Sv2Work& w, cudaStream_t st,
+                                long long& nl);
+
 struct RsvdWork {
     cplx *A = nullptr, *X = nullptr, *Y = nullptr, *Rf = nullptr, *uv = nullptr;
     int *piv = nullptr, *perm = nullptr, *info = nullptr;
@@ -483,6 +492,13 @@ struct RsvdWork {
     cplx *B = nullptr, *ub = nullptr, *ud = nullptr, *rhs = nullptr, *tb = nullptr;
     int *piv2 = nullptr, *perm2 = nullptr, *info2 = nullptr, *mcol = nullptr;
 };
+
+static Sv2Work sv2_work(const RsvdWork& w) {
+    Sv2Work v;
+    v.B = w.B; v.ub = w.ub; v.ud = w.ud; v.rhs = w.rhs; v.tb = w.tb;
+    v.piv2 = w.piv2; v.perm2 = w.perm2; v.info2 = w.info2; v.mcol = w.mcol;
+    return v;
+}
 
 // Carve the workspace (base == nullptr: only count).  Returns the bytes needed.
 size_t rsvd_carve(int n, int nmat, int s, int D, bool small, bool mixed, char* base, RsvdWork& w) {
@@ -601,30 +617,72 @@ cudaError_t rsvd_batched(int n, int nmat, int s, int q, int D, int precision, in
                 RS_CK(solve(0, w.uv + n, 1, 2LL * n, refine));
             }
     }
-    if (D >= 1) {
-        k_rsvd_vec<<<nmat, kRsvdThreads, 0, st>>>(n, D, T, mat_stride, der_stride, out, w.uv);
-        ++nl;
-        RS_CK(cudaGetLastError());
-    }
-    if (D == 2) {
-        const int n2 = 2 * n;
-        const long long nn2 = (long long)n2 * n2;
-        k_sv2_prep<<<nmat, 256, 0, st>>>(n, w.uv, w.ub, w.mcol);
-        k_build_bordered<<<grid_len(nn2, nmat), 256, 0, st>>>(n, T, mat_stride, out, 3, w.ub, w.mcol, w.B);
-        RS_CK(lu_factor_batched(n2, nmat, w.B, nn2, w.piv2, w.perm2, w.info2, st, &nl));
-        k_wapply<<<nmat, 256, 0, st>>>(n, T + der_stride, mat_stride, w.ub, w.ud, -1., 0);
-        RS_CK(lu_solve_batched(n2, nmat, 0, w.B, nn2, w.perm2, 1, w.ud, n2, st));
-        k_sv2_extract<<<(nmat + 127) / 128, 128, 0, st>>>(n, nmat, w.ud, w.mcol, w.tb);
-        k_wapply<<<nmat, 256, 0, st>>>(n, T + 2 * der_stride, mat_stride, w.ub, w.rhs, 1., 0);
-        k_wapply<<<nmat, 256, 0, st>>>(n, T + der_stride, mat_stride, w.ud, w.rhs, 2., 1);
-        k_sv2_axpy<<<nmat, 256, 0, st>>>(n, w.rhs, w.ud, w.tb);
-        RS_CK(lu_solve_batched(n2, nmat, 0, w.B, nn2, w.perm2, 1, w.rhs, n2, st));
-        k_sv2_out<<<(nmat + 127) / 128, 128, 0, st>>>(n, nmat, w.rhs, w.mcol, w.info2, out);
-        nl += 10;
-        RS_CK(cudaGetLastError());
-    }
+    if (D >= 1) RS_CK(sv_der_from_vectors(n, nmat, 1, D, T, mat_stride, der_stride, out, w.uv, sv2_work(w), st, nl));
     if (launches) *launches += nl;
     return cudaSuccess;
+}
+
+// sigma' (D >= 1) and sigma'' (D = 2) of nvec singular triplets whose right vectors
+// v sit in the v halves of uv ([nvec][2n]) and whose sigma sits in out[(D+1) t];
+// triplet t belongs to matrix t / per.  v is normalised, u = T v / |T v|, sigma' =
+// Re u^H T' v; sigma'' by the bordered system above.
+cudaError_t sv_der_from_vectors(int n, int nvec, int per, int D, const cplx* T, long long mat_stride,
+                                long long der_stride, double* out, cplx* uv, const Sv2Work& w, cudaStream_t st,
+                                long long& nl) {
+    k_rsvd_vec<<<nvec, kRsvdThreads, 0, st>>>(n, D, T, mat_stride, der_stride, out, uv, per);
+    ++nl;
+    RS_CK(cudaGetLastError());
+    if (D < 2) return cudaSuccess;
+    const int n2 = 2 * n;
+    const long long nn2 = (long long)n2 * n2;
+    k_sv2_prep<<<nvec, 256, 0, st>>>(n, uv, w.ub, w.mcol);
+    k_build_bordered<<<grid_len(nn2, nvec), 256, 0, st>>>(n, T, mat_stride, per, out, 3, w.ub, w.mcol, w.B);
+    RS_CK(lu_factor_batched(n2, nvec, w.B, nn2, w.piv2, w.perm2, w.info2, st, &nl));
+    k_wapply<<<nvec, 256, 0, st>>>(n, T + der_stride, mat_stride, per, w.ub, w.ud, -1., 0);
+    RS_CK(lu_solve_batched(n2, nvec, 0, w.B, nn2, w.perm2, 1, w.ud, n2, st));
+    k_sv2_extract<<<(nvec + 127) / 128, 128, 0, st>>>(n, nvec, w.ud, w.mcol, w.tb);
+    k_wapply<<<nvec, 256, 0, st>>>(n, T + 2 * der_stride, mat_stride, per, w.ub, w.rhs, 1., 0);
+    k_wapply<<<nvec, 256, 0, st>>>(n, T + der_stride, mat_stride, per, w.ud, w.rhs, 2., 1);
+    k_sv2_axpy<<<nvec, 256, 0, st>>>(n, w.rhs, w.ud, w.tb);
+    RS_CK(lu_solve_batched(n2, nvec, 0, w.B, nn2, w.perm2, 1, w.rhs, n2, st));
+    k_sv2_out<<<(nvec + 127) / 128, 128, 0, st>>>(n, nvec, w.rhs, w.mcol, w.info2, out);
+    nl += 10;
+    return cudaGetLastError();
+}
+
+// Workspace of sv_der_from_vectors for nvec triplets (base == nullptr: only count).
+size_t sv2_carve(int n, int nvec, int D, char* base, Sv2Work& w) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) -> char* {
+        char* p = base ? base + off : nullptr;
+        off += (bytes + 255) / 256 * 256;
+        return p;
+    };
+    if (D < 2) return 0;
+    const size_t nv = (size_t)nvec, nn = (size_t)n * n, c = sizeof(cplx), ii = sizeof(int);
+    w.B = (cplx*)take(nv * 4 * nn * c);
+    w.piv2 = (int*)take(nv * 2 * n * ii);
+    w.perm2 = (int*)take(nv * 2 * n * ii);
+    w.info2 = (int*)take(nv * ii);
+    w.ub = (cplx*)take(nv * 2 * n * c);
+    w.ud = (cplx*)take(nv * 2 * n * c);
+    w.rhs = (cplx*)take(nv * 2 * n * c);
+    w.tb = (cplx*)take(nv * c);
+    w.mcol = (int*)take(nv * ii);
+    return off;
+}
+
+// Launchers shared with the block iteration of arnoldi.cu
+cudaError_t qr_global_batched(int n, int nmat, int s, cplx* X, long long xstride, cplx* Rf, cudaStream_t st) {
+    if (s < 1 || s > kRsvdMaxS) return cudaErrorInvalidValue;
+    k_qr_global<<<nmat, kRsvdThreads, 0, st>>>(n, s, X, xstride, Rf);
+    return cudaGetLastError();
+}
+
+cudaError_t copy_mats_batched(long long nn, int nmat, const cplx* src, long long sstride, cplx* dst,
+                              long long dstride, cudaStream_t st) {
+    k_copy_mats<<<grid_len(nn, nmat), 256, 0, st>>>((int)nn, src, sstride, dst, dstride);
+    return cudaGetLastError();
 }
 
 }  // namespace hbem

@@ -58,7 +58,8 @@ int hbem_set_device(int device);
  *   SVD does its trailing updates on the tensor cores (3xTF32); 0 uses FP32 FMA.
  *   "svd_fast" (default 1): dense sigma_min / sigma' / sigma'' (direct::sv*) of matrices
  *   up to order 100 by FP32 Jacobi plus FP64 refinement of the near singular triplets
- *   (one FP64 LU per matrix); 0 always uses the FP64-polished Jacobi kernel.         */
+ *   (one FP64 LU per matrix); 0 always uses the FP64-polished Jacobi kernel.
+ *   "arnoldi_maxit" (default 1000, >= 1): iteration cap of hbem_arnoldi_sv_batch*.  */
 int hbem_set_option(const char* name, int value);
 
 /* Instrumentation (no counterpart in the reference, which prints std::chrono
@@ -180,6 +181,31 @@ int hbem_rsvd_sv_batch_device(int n, int nmat, unsigned d, const void* T_dev, lo
 int hbem_rsvd_sv_batch_device_ex(int n, int nmat, unsigned d, const void* T_dev, long long mat_stride,
                                  long long der_stride, const void* R_dev, int s, int q, int precision, int refine,
                                  double* out_host);
+
+/* arnoldi::sv (d = 0), sv_1st_der (d = 1) and sv_2nd_der (d = 2)
+ * (include/singular_values_arnoldi.hpp:29-66; source/utilities/singular_values_arnoldi.cpp:19-246)
+ * for a batch of nmat matrices of order n: the `count` smallest singular values in
+ * ascending order, each with its k-derivatives.  The reference runs ARPACK on
+ * [0 T^-H; T^-1 0] through one LU of T; here a block subspace iteration on
+ * T^-1 T^-H (32 columns at most, seeded start block) with a Rayleigh-Ritz step per
+ * iteration stops when every wanted Ritz pair of that operator has residual
+ * <= acc |theta| (ARPACK's test; acc <= 0 means machine precision, and acc is
+ * raised to 64 eps, the FP64 floor of the iteration).  out_host[(d+1)(m count + j) + t]
+ * = sigma_j, sigma_j', sigma_j'' (t <= d).  sigma' = Re u^H T' v of the Ritz triplet;
+ * sigma'' by the reference's bordered 2n x 2n system.  count up to 28 (or up to n
+ * when n <= 32) runs the block iteration; larger counts with d = 0 take all n
+ * singular values from the dense Jacobi kernel, larger counts with d > 0 give
+ * HBEM_ERR_UNSUPPORTED.  status_host / iters_host (may be NULL): per matrix 0
+ * converged, 5 zero pivot in the LU of T (results NaN), 6 iteration cap reached
+ * (set_option "arnoldi_maxit", default 1000; results are the last iterate's) and the
+ * number of block iterations.  Returns HBEM_ERR_SINGULAR / HBEM_ERR_NOCONV when any
+ * matrix has status 5 / 6, with out_host filled either way.  T_host: nmat blocks
+ * of d + 1 matrices (T, T', T'').                                                */
+int hbem_arnoldi_sv_batch(int n, int nmat, unsigned d, int count, double acc, const double* T_host,
+                          double* out_host, int* status_host);
+int hbem_arnoldi_sv_batch_device(int n, int nmat, unsigned d, int count, double acc, const void* T_dev,
+                                 long long mat_stride, long long der_stride, double* out_host, int* status_host,
+                                 int* iters_host);
 
 /* Batched complex64 update C_m -= A_m B_m (column-major, leading dimensions lda, ldb,
  * ldc, batch strides sa, sb, sc in elements): the trailing update of the LU's

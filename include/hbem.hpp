@@ -6,6 +6,7 @@
 //   BuilderData, GalerkinBuilder, LayerType   include/galerkin_builder.hpp:24-277
 //   SolutionsOperator                         include/gen_sol_op.hpp:16-128
 //   direct::sv, sv_1st_der, sv_2nd_der        include/singular_values.hpp
+//   arnoldi::sv, sv_1st_der, sv_2nd_der       include/singular_values_arnoldi.hpp:29-66
 //   rtsafe, zbrent, BrentMinimizer            include/find_roots.hpp:37-67,181-233
 //
 // Matrices: hbem::MatrixXcd / MatrixXd (column-major, data()/rows()/cols()/
@@ -204,6 +205,46 @@ inline std::vector<double> sv_2nd_der(const MatrixXcd& T, const MatrixXcd& T_der
     return sv_all(m, 2);
 }
 }  // namespace direct
+
+// arnoldi::sv returns the count smallest singular values in ascending order;
+// sv_1st_der / sv_2nd_der return count x 2 / count x 3 matrices (sigma, sigma',
+// sigma'').  acc is ARPACK's relative residual tolerance (machine precision by
+// default).  Where the reference's ARPACK run stops at its iteration cap it prints
+// a message and returns what it has; here the cap returns the last iterate too.
+namespace arnoldi {
+inline std::vector<double> run(const MatrixXcd* const* mats, unsigned d, unsigned count, double acc) {
+    const int n = (int)mats[0]->rows();
+    std::vector<std::complex<double>> buf((size_t)(d + 1) * n * n);
+    for (unsigned t = 0; t <= d; ++t)
+        for (long j = 0; j < n; ++j)
+            for (long i = 0; i < n; ++i) buf[(size_t)t * n * n + i + (size_t)j * n] = (*mats[t])(i, j);
+    std::vector<double> out((size_t)count * (d + 1));
+    const int st = hbem_arnoldi_sv_batch(n, 1, d, (int)count, acc, reinterpret_cast<const double*>(buf.data()),
+                                         out.data(), nullptr);
+    if (st != HBEM_ERR_NOCONV) throw_if(st);
+    return out;
+}
+inline MatrixXd to_matrix(const std::vector<double>& v, unsigned count, unsigned cols) {
+    MatrixXd r((long)count, (long)cols);
+    for (unsigned i = 0; i < count; ++i)
+        for (unsigned t = 0; t < cols; ++t) r(i, t) = v[(size_t)i * cols + t];
+    return r;
+}
+inline std::vector<double> sv(const MatrixXcd& T, unsigned count, double acc = 2.220446049250313e-16) {
+    const MatrixXcd* m[1] = {&T};
+    return run(m, 0, count, acc);
+}
+inline MatrixXd sv_1st_der(const MatrixXcd& T, const MatrixXcd& T_der, unsigned count,
+                           double acc = 2.220446049250313e-16) {
+    const MatrixXcd* m[2] = {&T, &T_der};
+    return to_matrix(run(m, 1, count, acc), count, 2);
+}
+inline MatrixXd sv_2nd_der(const MatrixXcd& T, const MatrixXcd& T_der, const MatrixXcd& T_der2, unsigned count,
+                           double acc = 2.220446049250313e-16) {
+    const MatrixXcd* m[3] = {&T, &T_der, &T_der2};
+    return to_matrix(run(m, 2, count, acc), count, 3);
+}
+}  // namespace arnoldi
 
 namespace detail {
 inline double call_fn(double x, void* u) { return (*static_cast<std::function<double(double)>*>(u))(x); }

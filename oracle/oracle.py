@@ -24,7 +24,19 @@ Pieces and the reference code each one restates:
   reverse-communication minimiser (find_roots.cpp:1003-1184), restated from
   Brent (1973) and Press et al.'s published descriptions;
 * the plain sweep / bracket / validate / quartic / Newton pattern of
-  examples/roots_newton_polygon_rsvd.cpp:172-265.
+  examples/roots_newton_polygon_rsvd.cpp:172-265;
+* ``opt_subdiv`` and the adaptive ``find_resonances`` driver
+  (source/utilities/find_roots.cpp:1186-1460) with the Steffen spline,
+  Floater-Hormann interpolant and GSL-style Brent minimiser restated from their
+  published descriptions;
+* ``arnoldi::sv / sv_1st_der / sv_2nd_der``
+  (source/utilities/singular_values_arnoldi.cpp:19-246): the reference drives
+  ARPACK (arpack++ headers cloned unpinned from github.com/m-reuter/arpackpp by
+  cmake/functions/Getarpackpp.cmake, over the system ARPACK library; neither is
+  in the reference tree).  ``arnoldi_sv_arpack`` makes the same ARPACK call --
+  znaupd/zneupd on [0 T^-H; T^-1 0], 2 count eigenvalues of largest magnitude,
+  tol = acc -- through scipy's bundled ARPACK-NG; ``arnoldi_block`` restates the
+  block iteration the GPU uses in its place.
 
 Parity status: Hankel values pinned by the reference's known answers
 (test/googletest/solutions_test.cpp:55-72) and by mpmath/scipy; matrices,
@@ -467,6 +479,78 @@ def rsvd_sv_der2(T, T1, T2, R, q=0):
     rhs = _wapply(T2, u) + 2.0 * (_wapply(T1, ud) - t * ud)
     d2 = float(-np.real(sla.lu_solve(lu, rhs)[m]))
     return s, d1, d2
+
+
+# ----------------------------------------------------------------- arnoldi::sv
+
+def arnoldi_sv_arpack(T, count, acc=0.0):
+    """arnoldi::sv (singular_values_arnoldi.cpp:19-66): ARPACK on the Hermitian
+    operator M = [0 T^-H; T^-1 0] (applied through one LU of T, :22-23,46-47), the
+    2 count eigenvalues of largest magnitude ("LM", :28), sigma = |1 / Re theta|
+    (:56) in ascending order.  The eigenvalues come in pairs +-1/sigma_j, so the
+    sorted magnitudes are taken two at a time."""
+    from scipy.sparse.linalg import LinearOperator, eigs
+    n = T.shape[0]
+    lu = sla.lu_factor(T)
+
+    def mv(x):
+        x = np.asarray(x).reshape(-1)
+        return np.concatenate([sla.lu_solve(lu, x[n:], trans=2), sla.lu_solve(lu, x[:n])])
+
+    op = LinearOperator((2 * n, 2 * n), matvec=mv, dtype=np.complex128)
+    theta = eigs(op, k=2 * count, which="LM", tol=acc, v0=np.ones(2 * n, complex), return_eigenvectors=False)
+    sig = np.sort(np.abs(1.0 / theta.real))
+    return sig[0::2][:count]
+
+
+_ARN_GOLDEN = 0x9E3779B97F4A7C15
+_M64 = (1 << 64) - 1
+
+
+def arnoldi_start(n, p, seed):
+    """The seeded start block of the GPU block iteration: entry (r, c) from a
+    SplitMix64 hash of seed + golden * (1 + (c << 32 | r)), real and imaginary parts
+    the top and bottom 24 bits scaled to [-1/2, 1/2)."""
+    R = np.zeros((n, p), complex)
+    for c in range(p):
+        for r in range(n):
+            z = (seed + _ARN_GOLDEN * (1 + ((c << 32) | r))) & _M64
+            z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _M64
+            z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _M64
+            z ^= z >> 31
+            R[r, c] = complex((z >> 40) / 16777216.0 - 0.5, (z & 0xFFFFFF) / 16777216.0 - 0.5)
+    return R
+
+
+def arnoldi_block_size(n, count):
+    return min(n, 32, max(12, 2 * count))
+
+
+def arnoldi_block(T, count, acc, seed=0x5EED, maxit=1000):
+    """Block subspace iteration on T^-1 T^-H with a Rayleigh-Ritz step per
+    iteration, stopped by ARPACK's residual test on M = [0 T^-H; T^-1 0]:
+    T^-H Q = QB RB, RB = Z S W^H; the residual of the Ritz pair (s_j, (QB z_j; Q w_j)
+    / sqrt2) is (0; T^-1 QB z_j - s_j Q w_j) / sqrt2, converged when its norm is
+    <= tol s_j for the count largest s_j.  tol = max(acc or eps, 64 eps).
+    Returns (sigma ascending, V (n x count right vectors), iterations, converged)."""
+    n = T.shape[0]
+    eps = np.finfo(float).eps
+    tol = max(acc if acc > 0 else eps, 64 * eps)
+    p = arnoldi_block_size(n, count)
+    lu = sla.lu_factor(T)
+    Q, _ = np.linalg.qr(sla.lu_solve(lu, arnoldi_start(n, p, seed)))
+    it = 1
+    while True:
+        QB, RB = np.linalg.qr(sla.lu_solve(lu, Q, trans=2))
+        Z, s, Wh = np.linalg.svd(RB)
+        W = Wh.conj().T
+        Y = sla.lu_solve(lu, QB)
+        conv = all(np.linalg.norm(Y @ Z[:, j] - s[j] * (Q @ W[:, j])) <= math.sqrt(2) * tol * s[j]
+                   for j in range(count))
+        if conv or it >= maxit:
+            return 1.0 / s[:count], Q @ W[:, :count], it, conv
+        Q, _ = np.linalg.qr(Y)
+        it += 1
 
 
 # ----------------------------------------------------------------- root finding

@@ -27,7 +27,10 @@ int main() {
     } catch (const std::runtime_error&) {
         threw = true;
     }
-    std::printf("%.17e %.17e %.17e %.17e %.17e %d %d\n", r[0], r[1], r[2], std::abs(V1(3, 5)), root, (int)found,
-                (int)threw);
+    // arnoldi::sv as in examples/roots_brent_circle_arnoldi.cpp:121 (count 1)
+    const double a0 = arnoldi::sv(T, 1, 1e-12)[0];
+    const MatrixXd a2 = arnoldi::sv_2nd_der(T, T_der, T_der2, 1, 1e-12);
+    std::printf("%.17e %.17e %.17e %.17e %.17e %d %d %.17e %.17e\n", r[0], r[1], r[2], std::abs(V1(3, 5)), root,
+                (int)found, (int)threw, a0, a2(0, 0));
     return (found && threw) ? 0 : 1;
 }

@@ -38,3 +38,4 @@ def test_facade_runs_and_matches_python(tmp_path):
     ref = api.sv_dense([so.gen_sol_op_2nd_der(2.5, 1.0, 23.4)], d=2)[0]
     assert np.allclose(vals[:3], ref, rtol=1e-12, atol=0)
     assert abs(vals[4] - np.pi / 2) < 1e-12 and vals[5] == 1 and vals[6] == 1
+    assert abs(vals[7] - ref[0]) <= 1e-11 * ref[0] and abs(vals[8] - ref[0]) <= 1e-11 * ref[0]

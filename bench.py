@@ -457,6 +457,90 @@ def combine_ranks(tot_ms, tot_v, world):
     return t.item(), v.item()
 
 
+def arnoldi_at_scale(torch, C, api, geometry, lib):
+    """arnoldi::sv / sv_2nd_der on the GPU (block iteration on T^-1 T^-H, ARPACK's
+    residual test).  Small: the bench scatterer (circle N=50, T 100x100), 64 k on
+    [0.5, 10], count 1, acc 1e-12, with and without derivatives (one CTA per
+    matrix).  Large: the dense-tail scatterer (star polygon N=800, T 1600x1600),
+    16 k, count 1, acc 1e-10 (batched global-memory LU), beside the randomized
+    sigma on the same matrices.  Returns the timings and the matrices the CPU
+    ARPACK comparison uses."""
+    import ctypes
+    ev = lambda: torch.cuda.Event(enable_timing=True)   # noqa: E731
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = ev(), ev()
+        e0.record()
+        r = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), r
+
+    def arn(T, n, nmat, d, count, acc, ms, ds):
+        out = np.zeros((nmat, count, d + 1))
+        st = (ctypes.c_int * nmat)()
+        it = (ctypes.c_int * nmat)()
+        C.check(lib.hbem_arnoldi_sv_batch_device(n, nmat, d, count, acc, ctypes.c_void_p(T.data_ptr()), ms, ds,
+                                                 C.dptr(out), st, it))
+        return out, list(it)
+
+    res = {}
+    so = api.SolutionsOperator(api.BuilderData(geometry.circle(CFG["radius"], CFG["N"]), order=CFG["order"]))
+    ks = np.linspace(0.5, 10.0, 64)
+    n = 2 * CFG["N"]
+    T3 = torch.empty((64, 3, n, n), dtype=torch.complex128, device="cuda")
+    C.check(lib.hbem_gen_sol_op_batch_device(so._h, C.dptr(ks), 64, CFG["c_o"], CFG["c_i"], 2,
+                                             ctypes.c_void_p(T3.data_ptr())))
+    ms0, (o0, it0) = timed(lambda: arn(T3, n, 64, 0, 1, 1e-12, 3 * n * n, n * n))
+    ms2, (o2, _) = timed(lambda: arn(T3, n, 64, 2, 1, 1e-12, 3 * n * n, n * n))
+    res["small"] = {"workload": "circle N=50 (T 100x100), 64 k in [0.5,10], count 1, acc 1e-12",
+                    "ms_per_T_sv": ms0 / 64, "ms_per_T_sv_2nd_der": ms2 / 64,
+                    "iterations_mean": float(np.mean(it0)), "iterations_max": int(np.max(it0))}
+    small_host = [T3[i, 0].cpu().numpy().T.copy() for i in range(4)]
+    small_sig = o0[:4, 0, 0].copy()
+    del T3
+    N = 800
+    n = 2 * N
+    so = api.SolutionsOperator(api.BuilderData(geometry.polygon(*geometry.star_polygon(24, seed=2), N), order=11))
+    ks = np.random.default_rng(3000).uniform(1.0, 30.0, 16)
+    T = torch.empty((16, n, n), dtype=torch.complex128, device="cuda")
+    C.check(lib.hbem_gen_sol_op_batch_device(so._h, C.dptr(ks), 16, 1.0, 9.0, 0, ctypes.c_void_p(T.data_ptr())))
+    msl, (ol, itl) = timed(lambda: arn(T, n, 16, 0, 1, 1e-10, n * n, n * n))
+    R = torch.from_numpy(np.ascontiguousarray(api.randGaussian(n, 12, seed=3000).T)).cuda()
+    rs = np.zeros(16)
+    msr, _ = timed(lambda: C.check(lib.hbem_rsvd_sv_batch_device(n, 16, 0, ctypes.c_void_p(T.data_ptr()), n * n,
+                                                                 n * n, ctypes.c_void_p(R.data_ptr()), 12, 2,
+                                                                 C.dptr(rs))))
+    res["large"] = {"workload": "star polygon 24 vertices (seed 2), N=800 (T 1600x1600), 16 k in [1,30], count 1, "
+                                "acc 1e-10",
+                    "ms_per_T_sv": msl / 16, "iterations_mean": float(np.mean(itl)), "iterations_max": int(np.max(itl)),
+                    "rsvd_ms_per_T (sketch 12, q 2)": msr / 16,
+                    "rsvd_rel_excess_over_arnoldi_max": float(np.max((rs - ol[:, 0, 0]) / ol[:, 0, 0]))}
+    large_host = [T[0].cpu().numpy().T.copy()]
+    large_sig = ol[:1, 0, 0].copy()
+    del T, R
+    return res, (small_host, small_sig, large_host, large_sig)
+
+
+def arnoldi_cpu(mats):
+    """The reference's arnoldi::sv call (ARPACK on [0 T^-H; T^-1 0] through one LU)
+    made through scipy's ARPACK on the host: ms per matrix and the largest relative
+    difference from the GPU result."""
+    import time
+    from oracle import oracle as O
+    small_host, small_sig, large_host, large_sig = mats
+    out = {}
+    for name, Ts, sig, acc in (("small", small_host, small_sig, 1e-12), ("large", large_host, large_sig, 1e-10)):
+        t0 = time.perf_counter()
+        ref = np.array([O.arnoldi_sv_arpack(T, 1, acc)[0] for T in Ts])
+        dt = time.perf_counter() - t0
+        out[name] = {"arpack_ms_per_T": 1e3 * dt / len(Ts), "matrices": len(Ts),
+                     "max_rel_diff_gpu_vs_arpack": float(np.max(np.abs(sig - ref) / ref))}
+    return out
+
+
 def adaptive_search(torch, so, plain_roots):
     """The reference's find_resonances search (opt_subdiv sampling with randomized
     sigma on a 2-wide sketch, q = 2, batches of 64; rational-interpolation guess;
@@ -576,6 +660,7 @@ def run_gpu(args):
     prec = precision_at_scale(torch, C, api, geometry, lib)
     batch = batching_sample(torch, C, api, geometry, lib)
     adapt = adaptive_search(torch, so, step(so)[1])
+    arnoldi, arn_mats = arnoldi_at_scale(torch, C, api, geometry, lib)
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
@@ -586,6 +671,10 @@ def run_gpu(args):
                    "sample": "first %d of %d grid points + Newton/verification of their roots" % (npts, CFG["npoints"])}
         except Exception as ex:   # the baseline must not hide the GPU line
             cpu = {"value": None, "unit": "resonances/s", "cores": threads, "kind": "port", "error": str(ex)[:200]}
+        try:
+            arnoldi["cpu_arpack"] = arnoldi_cpu(arn_mats)
+        except Exception as ex:
+            arnoldi["cpu_arpack"] = {"error": str(ex)[:200]}
 
     if rank == 0:
         line = {
@@ -603,6 +692,7 @@ def run_gpu(args):
             "precision_at_scale": prec,
             "batching_sample": batch,
             "adaptive_search": adapt,
+            "arnoldi_at_scale": arnoldi,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }

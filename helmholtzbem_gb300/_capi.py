@@ -26,6 +26,8 @@ EXPORTS = [
     "hbem_rsvd_sv_batch_device", "hbem_rsvd_sv_batch_device_ex", "hbem_lu_factor_batch_device", "hbem_lu_solve_batch_device",
     "hbem_cgemm_f32_batch_device", "hbem_solop_info", "hbem_sigma_rsvd_sweep", "hbem_opt_subdiv",
     "hbem_find_resonances_adaptive", "hbem_arnoldi_sv_batch", "hbem_arnoldi_sv_batch_device",
+    "hbem_scatterer_read", "hbem_polygon_length", "hbem_auto_num_panels", "hbem_polygon_panels",
+    "hbem_polygon_panels_graded", "hbem_choose_num_panels",
     "hbem_find_resonances_plain", "hbem_rtsafe", "hbem_zbrent", "hbem_brent_min",
 ]
 
@@ -95,6 +97,12 @@ def load(path=LIB_PATH):
                                            _dp]),
         "hbem_rsvd_sv_batch_device_ex": (_i, [_i, _i, _u, _vp, ctypes.c_longlong, ctypes.c_longlong, _vp, _i, _i,
                                               _i, _i, _dp]),
+        "hbem_scatterer_read": (_i, [ctypes.c_char_p, _d, _dp, _dp, _i, _ip]),
+        "hbem_polygon_length": (_d, [_dp, _dp, _i]),
+        "hbem_auto_num_panels": (_u, [_dp, _dp, _i, _d]),
+        "hbem_polygon_panels": (_i, [_dp, _dp, _i, _u, _dp, _i, _ip]),
+        "hbem_polygon_panels_graded": (_i, [_dp, _dp, _i, _u, _d, _dp, _i, _ip]),
+        "hbem_choose_num_panels": (_i, [_dp, _dp, _i, _d, _d, _d, _up]),
         "hbem_arnoldi_sv_batch": (_i, [_i, _i, _u, _i, _d, _dp, _dp, _ip]),
         "hbem_arnoldi_sv_batch_device": (_i, [_i, _i, _u, _i, _d, _vp, ctypes.c_longlong, ctypes.c_longlong, _dp, _ip,
                                               _ip]),

@@ -13,10 +13,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libhbem.so")
-SOURCES = ["assemble.cu", "solop.cu", "dense.cu", "lu.cu", "tc_gemm.cu", "rsvd.cu", "arnoldi.cu", "capi.cu", "roots.cu"]
+SOURCES = ["assemble.cu", "solop.cu", "dense.cu", "lu.cu", "tc_gemm.cu", "rsvd.cu", "arnoldi.cu", "capi.cu", "roots.cu",
+           "scatterer.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Host code: no floating-point contraction, so that x86-64 and aarch64 hosts (where
+# the compiler would otherwise fuse a*b+c into FMAs) give bit-identical results.
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-         "-Xcompiler", "-Wall", "-Wno-deprecated-gpu-targets"]
+         "-Xcompiler", "-Wall", "-Xcompiler", "-ffp-contract=off", "-Wno-deprecated-gpu-targets"]
 
 
 def nvcc():
@@ -31,6 +34,7 @@ def _stale(obj, src):
         return True
     deps = [src] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     deps.append(os.path.join(HERE, "..", "include", "hbem.h"))
+    deps.append(os.path.abspath(__file__))
     t = os.path.getmtime(obj)
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
@@ -41,7 +45,7 @@ def build(verbose=False, ptxas_info=False):
     jobs = []
     for s in SOURCES:
         src = os.path.join(CSRC, s)
-        obj = os.path.join(OUT_DIR, s.replace(".cu", ".o"))
+        obj = os.path.join(OUT_DIR, os.path.splitext(s)[0] + ".o")
         objs.append(obj)
         if _stale(obj, src) or ptxas_info:
             cmd = [nvcc()] + ARCH + FLAGS + (["-Xptxas", "-v"] if ptxas_info else []) + ["-c", src, "-o", obj]

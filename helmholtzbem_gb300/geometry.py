@@ -4,11 +4,15 @@ Restates the reference's mesh constructors:
 * ``ParametrizedCircularArc(center, r, phi0, phi1).split(N)``
   (source/parametrizations/parametrized_circular_arc.cpp:141-152)
 * ``ParametrizedLine(p, q).split(m)`` (source/parametrizations/parametrized_line.cpp:112-131)
-* ``scatterer::make_N_polygonal_panels(x, y, N)`` (source/utilities/scatterer.cpp:114-156)
+* ``scatterer::read``, ``length``, ``auto_num_panels``, ``make_N_polygonal_panels``,
+  ``make_polygonal_panels`` (source/utilities/scatterer.cpp:30-277) and the panel
+  count of examples/find_resonances.cpp:111-124, through the host code of libhbem
 plus the synthetic scatterers of the benchmark configurations (seeded star
 polygons; Fourier-sum curves sampled into line panels).
 """
+import ctypes
 import math
+import os
 
 import numpy as np
 
@@ -40,32 +44,77 @@ def split_line(p, q, m):
     return out
 
 
+def _poly_arrays(x, y):
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.ascontiguousarray(y, np.float64)
+    if x.shape != y.shape or x.ndim != 1:
+        raise ValueError("x and y must be 1-D arrays of equal length")
+    return x, y
+
+
+def _panels_from(fn, x, y, *args):
+    from . import _capi as C
+    x, y = _poly_arrays(x, y)
+    n = ctypes.c_int()
+    C.check(fn(C.dptr(x), C.dptr(y), int(x.size), *args, None, 0, ctypes.byref(n)))
+    par = np.zeros((n.value, 5))
+    C.check(fn(C.dptr(x), C.dptr(y), int(x.size), *args, C.dptr(par), n.value, ctypes.byref(n)))
+    return np.full(n.value, PANEL_LINE, np.int32), par
+
+
 def polygon(x, y, N):
-    """Edge panel counts proportional to edge length, corrected one panel at a time
-    on the edge that minimises the variance of the panel lengths."""
-    x = np.asarray(x, float)
-    y = np.asarray(y, float)
-    n = x.size
-    d = np.array([math.hypot(x[(i + 1) % n] - x[i], y[(i + 1) % n] - y[i]) for i in range(n)])
-    alpha = N / float(np.sum(d))
-    m = np.array([float(np.round(alpha * di)) for di in d])
-    cs = int(np.sum(m))
-    while cs != N:
-        step = -1 if cs > N else 1
-        best, i_best = np.inf, 0
-        for i in range(n):
-            m[i] += step
-            a = d / m
-            var = float(np.mean((a - np.mean(a)) ** 2))
-            if var < best:
-                best, i_best = var, i
-            m[i] -= step
-        m[i_best] += step
-        cs += step
-    panels = []
-    for i in range(n):
-        panels += split_line((x[i], y[i]), (x[(i + 1) % n], y[(i + 1) % n]), int(m[i]))
-    return np.full(len(panels), PANEL_LINE, np.int32), np.array(panels)
+    """scatterer::make_N_polygonal_panels: exactly N line panels, edge counts
+    proportional to the edge lengths and corrected one panel at a time on the edge
+    that minimises the variance of the panel lengths (host code of libhbem)."""
+    from . import _capi as C
+    return _panels_from(C.lib().hbem_polygon_panels, x, y, ctypes.c_uint(int(N)))
+
+
+def polygon_graded(x, y, N, refinement_factor=0.5):
+    """scatterer::make_polygonal_panels: about N line panels graded geometrically
+    towards the corners (host code of libhbem)."""
+    from . import _capi as C
+    return _panels_from(C.lib().hbem_polygon_panels_graded, x, y, ctypes.c_uint(int(N)),
+                        ctypes.c_double(float(refinement_factor)))
+
+
+def read_scatterer(fname, scale=1.0):
+    """scatterer::read: vertices (x, y) of a polygon file with one "x,y" per line;
+    raises ValueError where the reference returns false."""
+    from . import _capi as C
+    n = ctypes.c_int()
+    if C.lib().hbem_scatterer_read(os.fsencode(fname), float(scale), None, None, 0, ctypes.byref(n)) != 0:
+        raise ValueError("failed to read scatterer from file " + str(fname))
+    x = np.zeros(n.value)
+    y = np.zeros(n.value)
+    C.check(C.lib().hbem_scatterer_read(os.fsencode(fname), float(scale), C.dptr(x), C.dptr(y), n.value,
+                                        ctypes.byref(n)))
+    return x, y
+
+
+def polygon_length(x, y):
+    """scatterer::length: perimeter of the closed polygon."""
+    from . import _capi as C
+    x, y = _poly_arrays(x, y)
+    return float(C.lib().hbem_polygon_length(C.dptr(x), C.dptr(y), int(x.size)))
+
+
+def auto_num_panels(x, y, f):
+    """scatterer::auto_num_panels: round(perimeter / (f * shortest side))."""
+    from . import _capi as C
+    x, y = _poly_arrays(x, y)
+    return int(C.lib().hbem_auto_num_panels(C.dptr(x), C.dptr(y), int(x.size), float(f)))
+
+
+def choose_num_panels(x, y, k_max, degf=10.0, rfac=0.5):
+    """The panel count of examples/find_resonances.cpp:111-124 (Brent's minimiser
+    matching the longest graded panel to 2 pi / (degf k_max))."""
+    from . import _capi as C
+    x, y = _poly_arrays(x, y)
+    out = ctypes.c_uint()
+    C.check(C.lib().hbem_choose_num_panels(C.dptr(x), C.dptr(y), int(x.size), float(k_max), float(degf),
+                                           float(rfac), ctypes.byref(out)))
+    return int(out.value)
 
 
 def star_polygon(nvert, seed, amp=0.3):

@@ -120,6 +120,37 @@ int hbem_gen_sol_op(hbem_solop s, double k_re, double k_im, double c_o, double c
 int hbem_gen_sol_op_batch_device(hbem_solop s, const double* k_host, int nk, double c_o, double c_i, unsigned d,
                                  void* T_dev);
 
+/* ------------------------------------------------------------------ scatterers (host only) */
+
+/* scatterer::read (include/scatterer.hpp:39; source/utilities/scatterer.cpp:30-82): one
+ * vertex "x,y" per line, whitespace anywhere ignored, empty lines skipped; every
+ * field must parse as a double (a '#' line is rejected, as the reference's parser
+ * does); the widest row must have two fields (a shorter row is padded with zeros).
+ * Coordinates are multiplied by scale.  With x_host or y_host NULL only *nvert is
+ * returned.  HBEM_ERR_INVALID on an unreadable or malformed file or cap < nvert.  */
+int hbem_scatterer_read(const char* fname, double scale, double* x_host, double* y_host, int cap, int* nvert);
+/* scatterer::length (scatterer.cpp:84-93): perimeter of the closed polygon */
+double hbem_polygon_length(const double* x, const double* y, int n);
+/* scatterer::auto_num_panels (scatterer.cpp:95-112): round(perimeter / (f shortest side)) */
+unsigned hbem_auto_num_panels(const double* x, const double* y, int n, double f);
+/* scatterer::make_N_polygonal_panels (scatterer.cpp:114-155): exactly N line panels,
+ * evenly split per edge, counts proportional to the edge lengths.  params: 5 doubles
+ * per panel (x1 y1 x2 y2 0, kind HBEM_PANEL_LINE); with params NULL only *npanels is
+ * returned.                                                                       */
+int hbem_polygon_panels(const double* x, const double* y, int n, unsigned N, double* params, int cap,
+                        int* npanels);
+/* scatterer::make_polygonal_panels (scatterer.cpp:157-277): about N line panels graded
+ * geometrically towards the corners (the first panel at a corner is rf + (1 - rf)(1 -
+ * cos angle)/2 times the uniform length); edges with fewer than three panels, or
+ * refinement_factor >= 1, are split evenly.                                        */
+int hbem_polygon_panels_graded(const double* x, const double* y, int n, unsigned N, double refinement_factor,
+                               double* params, int cap, int* npanels);
+/* Panel count of examples/find_resonances.cpp:111-124: Brent's minimiser on
+ * [N0, N0 / rfac], N0 = degf L k_max / (2 pi), of |2 pi / (degf k_max) - longest panel
+ * of make_polygonal_panels(round N, rfac)|; *npanels = round of the minimiser.       */
+int hbem_choose_num_panels(const double* x, const double* y, int n, double k_max, double degf, double rfac,
+                           unsigned* npanels);
+
 /* ------------------------------------------------------------------ singular values */
 
 /* direct::sv / sv_1st_der / sv_2nd_der for the smallest singular value

@@ -7,6 +7,8 @@
 //   SolutionsOperator                         include/gen_sol_op.hpp:16-128
 //   direct::sv, sv_1st_der, sv_2nd_der        include/singular_values.hpp
 //   arnoldi::sv, sv_1st_der, sv_2nd_der       include/singular_values_arnoldi.hpp:29-66
+//   scatterer::read, length, auto_num_panels,
+//     make_N_polygonal_panels, make_polygonal_panels   include/scatterer.hpp:39-84
 //   rtsafe, zbrent, BrentMinimizer            include/find_roots.hpp:37-67,181-233
 //
 // Matrices: hbem::MatrixXcd / MatrixXd (column-major, data()/rows()/cols()/
@@ -32,7 +34,9 @@ namespace hbem {
 #ifdef HBEM_USE_EIGEN
 using MatrixXcd = Eigen::MatrixXcd;
 using MatrixXd = Eigen::MatrixXd;
+using VectorXd = Eigen::VectorXd;
 #else
+using VectorXd = std::vector<double>;
 template <class T>
 class Matrix {
     std::vector<T> d_;
@@ -82,6 +86,44 @@ struct Mesh {
         return m;
     }
 };
+
+// Scatterer files and polygonal meshes.  Where the reference returns a PanelVector
+// of ParametrizedLine panels, these return the Mesh of the same line panels.
+namespace scatterer {
+inline bool read(const std::string& fname, VectorXd& x, VectorXd& y, double scale = 1.0) {
+    int n = 0;
+    if (hbem_scatterer_read(fname.c_str(), scale, nullptr, nullptr, 0, &n) != HBEM_OK) return false;
+    x.resize(n);
+    y.resize(n);
+    return hbem_scatterer_read(fname.c_str(), scale, x.data(), y.data(), n, &n) == HBEM_OK;
+}
+inline double length(const VectorXd& x, const VectorXd& y) {
+    return hbem_polygon_length(x.data(), y.data(), (int)x.size());
+}
+inline unsigned int auto_num_panels(const VectorXd& x, const VectorXd& y, double f) {
+    return hbem_auto_num_panels(x.data(), y.data(), (int)x.size(), f);
+}
+inline Mesh lines_from(const std::vector<double>& par) {
+    Mesh m;
+    for (size_t p = 0; p + 4 < par.size(); p += 5) m.add_line(par[p], par[p + 1], par[p + 2], par[p + 3]);
+    return m;
+}
+inline Mesh make_N_polygonal_panels(const VectorXd& x, const VectorXd& y, unsigned N) {
+    int np = 0;
+    throw_if(hbem_polygon_panels(x.data(), y.data(), (int)x.size(), N, nullptr, 0, &np));
+    std::vector<double> par((size_t)np * 5);
+    throw_if(hbem_polygon_panels(x.data(), y.data(), (int)x.size(), N, par.data(), np, &np));
+    return lines_from(par);
+}
+inline Mesh make_polygonal_panels(const VectorXd& x, const VectorXd& y, unsigned N, double refinement_factor = 0.5) {
+    int np = 0;
+    throw_if(hbem_polygon_panels_graded(x.data(), y.data(), (int)x.size(), N, refinement_factor, nullptr, 0, &np));
+    std::vector<double> par((size_t)np * 5);
+    throw_if(
+        hbem_polygon_panels_graded(x.data(), y.data(), (int)x.size(), N, refinement_factor, par.data(), np, &np));
+    return lines_from(par);
+}
+}  // namespace scatterer
 
 enum class LayerType : unsigned { NONE = 0, DOUBLE = 1, SINGLE = 2, HYPERSINGULAR = 4, ALL = 7 };
 inline LayerType operator|(LayerType a, LayerType b) { return (LayerType)((unsigned)a | (unsigned)b); }

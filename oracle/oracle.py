@@ -161,23 +161,122 @@ def _line_split(p, q, m):
     return out
 
 
+def _norm2d(dx, dy):
+    return math.sqrt(dx * dx + dy * dy)
+
+
+def _fdiv(a, b):
+    """a / b with IEEE semantics (inf / nan instead of an exception)."""
+    if b == 0.0:
+        if a == 0.0 or a != a:
+            return math.nan
+        return math.copysign(math.inf, a) * math.copysign(1.0, b)
+    return a / b
+
+
+def _cpow(a, b):
+    """C pow for integer-valued exponents: poles and overflow give +-inf."""
+    try:
+        return math.pow(a, b)
+    except (ValueError, ZeroDivisionError, OverflowError):
+        odd = b == int(b) and int(b) % 2 != 0
+        if a != a or b != b:
+            return math.nan
+        return math.copysign(math.inf, a) if odd else math.inf
+
+
+def _round_half_away(v):
+    """std::round for v >= 0 (half away from zero), exact for |v| < 2**52."""
+    fl = math.floor(v)
+    return fl + 1.0 if v - fl >= 0.5 else float(fl)
+
+
+def _mean_var(d, k):
+    n = len(d)
+    s = 0.0
+    for i in range(n):
+        s += _fdiv(d[i], k[i])
+    mu = s / n
+    q = 0.0
+    for i in range(n):
+        a = _fdiv(d[i], k[i]) - mu
+        q += a * a
+    return mu, q / n
+
+
+def polygon_length(x, y):
+    """scatterer::length (source/utilities/scatterer.cpp:84-93)."""
+    n = len(x)
+    L = 0.0
+    for i in range(n):
+        L += _norm2d(x[(i + 1) % n] - x[i], y[(i + 1) % n] - y[i])
+    return L
+
+
+def auto_num_panels(x, y, f):
+    """scatterer::auto_num_panels (scatterer.cpp:95-112)."""
+    n = len(x)
+    min_s, dsum = float("inf"), 0.0
+    for i in range(n):
+        j = i + 1 if i < n - 1 else 0
+        l = _norm2d(x[j] - x[i], y[j] - y[i])
+        dsum += l
+        min_s = min(min_s, l)
+    return int(_round_half_away(dsum / (min_s * f)))
+
+
+def read_scatterer(fname, scale=1.0):
+    """scatterer::read (scatterer.cpp:30-82): whitespace removed, empty lines skipped,
+    comma-separated fields parsed like std::stod (leading number, rest ignored);
+    widest row must have 2 fields, shorter rows padded with 0.  None on failure."""
+    import re
+    num = re.compile(r"[+-]?(?:(?:\d+\.?\d*|\.\d+)(?:[eE][+-]?\d+)?|inf(?:inity)?|nan)", re.I)
+    rows = []
+    with open(fname) as fh:
+        for line in fh:
+            t = "".join(ch for ch in line if not ch.isspace())
+            if not t:
+                continue
+            fields = t.split(",")
+            if fields and fields[-1] == "":
+                fields = fields[:-1]
+            row = []
+            for fld in fields:
+                m = num.match(fld)
+                if not m:
+                    return None
+                v = float(m.group(0))
+                if math.isinf(v) and not re.match(r"[+-]?inf", fld, re.I):
+                    return None            # overflow: std::stod throws out_of_range
+                row.append(v)
+            rows.append(row)
+    if not rows or max(len(r) for r in rows) != 2:
+        return None
+    x = np.array([scale * (r[0] if len(r) > 0 else 0.0) for r in rows])
+    y = np.array([scale * (r[1] if len(r) > 1 else 0.0) for r in rows])
+    return x, y
+
+
 def polygon_panels(x, y, N):
-    """scatterer::make_N_polygonal_panels: edge panel counts proportional to length,
-    adjusted one panel at a time to the variance-minimising edge until they sum to N."""
-    x = np.asarray(x, float); y = np.asarray(y, float)
-    n = x.size
-    d = np.array([math.hypot(x[(i + 1) % n] - x[i], y[(i + 1) % n] - y[i]) for i in range(n)])
-    length = float(np.sum(d))
+    """scatterer::make_N_polygonal_panels (scatterer.cpp:114-155): edge panel counts
+    proportional to length, adjusted one panel at a time to the variance-minimising
+    edge until they sum to N."""
+    x = [float(v) for v in x]; y = [float(v) for v in y]
+    n = len(x)
+    length = polygon_length(x, y)
     alpha = N / length
-    m = np.array([float(np.round(alpha * di)) for di in d])
-    cs = int(np.sum(m))
+    d, m = [], []
+    for i in range(n):
+        j = 0 if i == n - 1 else i + 1
+        d.append(_norm2d(x[i] - x[j], y[i] - y[j]))
+        m.append(_round_half_away(alpha * d[i]))
+    cs = int(sum(m))
     while cs != N:
         kstep = -1 if cs > N else 1
-        best, i_min = np.inf, 0
+        best, i_min = float("inf"), 0
         for i in range(n):
             m[i] += kstep
-            a = d / m
-            var = float(np.mean((a - np.mean(a)) ** 2))
+            _, var = _mean_var(d, m)
             if var < best:
                 best, i_min = var, i
             m[i] -= kstep
@@ -188,6 +287,128 @@ def polygon_panels(x, y, N):
         panels += _line_split((x[i], y[i]), (x[(i + 1) % n], y[(i + 1) % n]), int(m[i]))
     kinds = np.full(len(panels), KIND_LINE, np.int32)
     return kinds, np.array(panels)
+
+
+def polygon_panels_graded(x, y, N, rf=0.5):
+    """scatterer::make_polygonal_panels (scatterer.cpp:157-277).  Edge shares
+    k_i = N d_i / L (the solution of the reference's proportionality system), floor or
+    floor + 1 per edge in decreasing-share order by the evenness objective; per edge
+    with >= 3 panels, geometric grading from both corners: Newton (from rf, <= 5001
+    steps, |step| <= eps) for the ratio alpha of each split position j, the j with the
+    closest end factors d1, d2 kept; uniform split if the graded walk misses the far
+    corner by more than 1e-3 of a uniform panel."""
+    x = [float(v) for v in x]; y = [float(v) for v in y]
+    n = len(x)
+    eps, eps2 = np.finfo(float).eps, 1e-3
+    d = []
+    for i in range(n):
+        j = i + 1 if i < n - 1 else 0
+        d.append(_norm2d(x[j] - x[i], y[j] - y[i]))
+    L = 0.0
+    for i in range(n):
+        L += d[i]
+    k = [float(N) * d[i] / L for i in range(n)]
+    dd = sorted([(k[i], i) for i in range(n)])[::-1]
+
+    def obj(send):
+        mu, var = _mean_var(d, k)
+        ks = 0.0
+        for i in range(n):
+            ks += k[i]
+        return _fdiv(math.sqrt(var) if var == var else math.nan, mu) + send * abs(float(N) / ks - 1.0)
+
+    for i in range(n):
+        j = dd[i][1]
+        k[j] = float(math.floor(k[j]))
+        f1 = obj(1.0)
+        k[j] += 1.0
+        f2 = obj(1.0)
+        if f1 == f1 and f1 < f2:
+            k[j] -= 1.0
+    panels = []
+    for i in range(n):
+        p0 = (x[n - 1], y[n - 1]) if i == 0 else (x[i - 1], y[i - 1])
+        p1 = (x[i], y[i])
+        p2 = (x[i + 1], y[i + 1]) if i < n - 1 else (x[0], y[0])
+        i3 = i + 2 if i < n - 2 else i - n + 2
+        p3 = (x[i3], y[i3])
+        D = (_fdiv(p2[0] - p1[0], k[i]), _fdiv(p2[1] - p1[1], k[i]))
+        n_i = int(k[i])
+        a0, a1 = (p0[0] - p1[0], p0[1] - p1[1]), (p2[0] - p1[0], p2[1] - p1[1])
+        f1 = (1.0 - _fdiv(a0[0] * a1[0] + a0[1] * a1[1], _norm2d(*a0) * _norm2d(*a1))) / 2.0
+        b0, b1 = (p1[0] - p2[0], p1[1] - p2[1]), (p3[0] - p2[0], p3[1] - p2[1])
+        f2 = (1.0 - _fdiv(b0[0] * b1[0] + b0[1] * b1[1], _norm2d(*b0) * _norm2d(*b1))) / 2.0
+        f1 = rf + (1.0 - rf) * f1
+        f2 = rf + (1.0 - rf) * f2
+        if rf >= 1.0 or n_i < 3:
+            for j in range(n_i):
+                a = (p1[0] + D[0] * float(j), p1[1] + D[1] * float(j))
+                b = (p1[0] + D[0] * float(j + 1), p1[1] + D[1] * float(j + 1)) if j + 1 < n_i else p2
+                panels.append((a[0], a[1], b[0], b[1], 0.0))
+            continue
+        j_best, alpha_best, d1_best, d2_best = 0, 0.0, 0.0, 0.0
+        for j in range(1, n_i):
+            def f(t):
+                return (f1 * _cpow(t, float(1 - j)) + f2 * _cpow(t, float(j + 1 - n_i)) - t * (f1 + f2)
+                        - float(n_i) * (1.0 - t))
+
+            def f_der(t):
+                return (float(n_i) - f1 - f2 - f1 * (j - 1.0) * _cpow(t, float(-j))
+                        - f2 * (n_i - j - 1.0) * _cpow(t, float(j - n_i)))
+            alpha_next, it = rf, 0
+            while True:
+                alpha = alpha_next
+                alpha_next = alpha - _fdiv(f(alpha), f_der(alpha))
+                it += 1
+                if not (abs(alpha_next - alpha) > eps and it <= 5000):
+                    break
+            d1 = _fdiv(f1, _cpow(alpha, float(j - 1)))
+            d2 = _fdiv(f2, _cpow(alpha, float(n_i - j - 1)))
+            if not j_best or abs(d1 - d2) < abs(d1_best - d2_best):
+                d1_best, d2_best, j_best, alpha_best = d1, d2, j, alpha
+        mark = len(panels)
+        pos = p1
+        for j in range(n_i):
+            if j < j_best:
+                pw = _cpow(alpha_best, float(j_best - 1 - j))
+                step = (D[0] * d1_best * pw, D[1] * d1_best * pw)
+            else:
+                pw = _cpow(alpha_best, float(j - j_best))
+                step = (D[0] * d2_best * pw, D[1] * d2_best * pw)
+            nxt = (pos[0] + step[0], pos[1] + step[1])
+            b = nxt if j + 1 < n_i else p2
+            panels.append((pos[0], pos[1], b[0], b[1], 0.0))
+            pos = nxt
+        if _fdiv(_norm2d(pos[0] - p2[0], pos[1] - p2[1]), _norm2d(*D)) > eps2:
+            del panels[mark:]
+            pos = p1
+            for j in range(n_i):
+                nxt = (pos[0] + D[0], pos[1] + D[1])
+                b = nxt if j + 1 < n_i else p2
+                panels.append((pos[0], pos[1], b[0], b[1], 0.0))
+                pos = nxt
+    kinds = np.full(len(panels), KIND_LINE, np.int32)
+    return kinds, np.array(panels).reshape(-1, 5)
+
+
+def max_panel_length(par):
+    r = 0.0
+    for p in par:
+        r = max(r, _norm2d(p[2] - p[0], p[3] - p[1]))
+    return r
+
+
+def choose_num_panels(x, y, k_max, degf=10.0, rfac=0.5):
+    """Panel count of examples/find_resonances.cpp:111-124: Brent's minimiser on
+    [N0, N0 / rfac], N0 = degf L k_max / (2 pi), of |2 pi / (degf k_max) - longest
+    graded panel|, rounded."""
+    L = polygon_length(x, y)
+    Np0 = degf * L * k_max * 0.5 * 0.31830988618379067154
+    target = 2.0 * math.pi / (degf * k_max)
+
+    def f(Np):
+        return abs(target - max_panel_length(polygon_panels_graded(x, y, int(_round_half_away(Np)), rfac)[1]))
+    return int(_round_half_away(BrentMin(Np0, Np0 / rfac, 1e-3).minimize(f)))
 
 
 def star_polygon(nvert, seed, amp=0.3):

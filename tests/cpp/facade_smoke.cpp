@@ -5,7 +5,7 @@
 
 #include "hbem.hpp"
 
-int main() {
+int main(int argc, char** argv) {
     using namespace hbem;
     Mesh mesh = Mesh::circle(0., 0., 0.25, 16);
     BuilderData builder_data(mesh, P1, P1, 7);
@@ -30,7 +30,26 @@ int main() {
     // arnoldi::sv as in examples/roots_brent_circle_arnoldi.cpp:121 (count 1)
     const double a0 = arnoldi::sv(T, 1, 1e-12)[0];
     const MatrixXd a2 = arnoldi::sv_2nd_der(T, T_der, T_der2, 1, 1e-12);
-    std::printf("%.17e %.17e %.17e %.17e %.17e %d %d %.17e %.17e\n", r[0], r[1], r[2], std::abs(V1(3, 5)), root,
-                (int)found, (int)threw, a0, a2(0, 0));
+    // scatterer file -> corner-graded polygon mesh, as examples/roots_brent_polygon.cpp:72-121 does
+    double sq_sigma = -1.;
+    int sq_panels = -1;
+    if (argc > 1) {
+        if (FILE* fp = std::fopen(argv[1], "w")) {
+            std::fputs("0,0\n 1, 0\n\n1,1\r\n0,1\n", fp);
+            std::fclose(fp);
+        }
+        VectorXd px, py;
+        if (scatterer::read(argv[1], px, py, 0.5)) {
+            Mesh sq = scatterer::make_polygonal_panels(px, py, 24, 0.5);
+            sq_panels = sq.size();
+            BuilderData sq_data(sq, P1, P1, 7);
+            SolutionsOperator sq_so(sq_data);
+            MatrixXcd Tsq;
+            sq_so.gen_sol_op(3.0, 1.0, 4.0, Tsq);
+            sq_sigma = direct::sv(Tsq);
+        }
+    }
+    std::printf("%.17e %.17e %.17e %.17e %.17e %d %d %.17e %.17e %d %.17e\n", r[0], r[1], r[2], std::abs(V1(3, 5)),
+                root, (int)found, (int)threw, a0, a2(0, 0), sq_panels, sq_sigma);
     return (found && threw) ? 0 : 1;
 }

@@ -21,7 +21,7 @@ def _lib_or_skip():
 
 def test_header_matches_exports():
     src = open(os.path.join(ROOT, "include", "hbem.h")).read()
-    declared = set(re.findall(r"^\s*(?:const char\*|double|int|void)\s+(hbem_\w+)\s*\(", src, re.M))
+    declared = set(re.findall(r"^\s*(?:const char\*|double|int|unsigned|void)\s+(hbem_\w+)\s*\(", src, re.M))
     assert declared == set(_capi.EXPORTS)
 
 

@@ -29,7 +29,7 @@ def test_facade_compiles(tmp_path):
 @pytest.mark.gpu
 def test_facade_runs_and_matches_python(tmp_path):
     exe = _compile(tmp_path)
-    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    r = subprocess.run([exe, str(tmp_path / "square.dat")], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     vals = [float(v) for v in r.stdout.split()]
     from helmholtzbem_gb300 import api, geometry
@@ -39,3 +39,8 @@ def test_facade_runs_and_matches_python(tmp_path):
     assert np.allclose(vals[:3], ref, rtol=1e-12, atol=0)
     assert abs(vals[4] - np.pi / 2) < 1e-12 and vals[5] == 1 and vals[6] == 1
     assert abs(vals[7] - ref[0]) <= 1e-11 * ref[0] and abs(vals[8] - ref[0]) <= 1e-11 * ref[0]
+    # scatterer::read + make_polygonal_panels + SolutionsOperator on the graded square
+    sq = geometry.polygon_graded([0.0, 0.5, 0.5, 0.0], [0.0, 0.0, 0.5, 0.5], 24, 0.5)
+    assert int(vals[9]) == len(sq[0])
+    ssq = api.sv_dense([[api.SolutionsOperator(api.BuilderData(sq, order=7)).gen_sol_op(3.0, 1.0, 4.0)]])[0][0]
+    assert abs(vals[10] - ssq) <= 1e-12 * ssq

@@ -28,6 +28,7 @@ EXPORTS = [
     "hbem_find_resonances_adaptive", "hbem_arnoldi_sv_batch", "hbem_arnoldi_sv_batch_device",
     "hbem_scatterer_read", "hbem_polygon_length", "hbem_auto_num_panels", "hbem_polygon_panels",
     "hbem_polygon_panels_graded", "hbem_choose_num_panels",
+    "hbem_incoming_load", "hbem_incoming_eval", "hbem_tp_solve", "hbem_tp_field_grid", "hbem_field_stats",
     "hbem_find_resonances_plain", "hbem_rtsafe", "hbem_zbrent", "hbem_brent_min",
 ]
 
@@ -103,6 +104,12 @@ def load(path=LIB_PATH):
         "hbem_polygon_panels": (_i, [_dp, _dp, _i, _u, _dp, _i, _ip]),
         "hbem_polygon_panels_graded": (_i, [_dp, _dp, _i, _u, _d, _dp, _i, _ip]),
         "hbem_choose_num_panels": (_i, [_dp, _dp, _i, _d, _d, _d, _up]),
+        "hbem_incoming_load": (_i, [ctypes.c_char_p, _dp, _i, _ip]),
+        "hbem_incoming_eval": (_i, [_dp, _i, _d, _d, _dp, _i, _dp, _dp]),
+        "hbem_tp_solve": (_i, [_vp, _dp, _i, _d, _d, _d, _d, _dp]),
+        "hbem_tp_field_grid": (_i, [_vp, _dp, _i, _d, _d, _d, _d, _u, _d, _d, _d, _d, _i, _i, _i, _dp, _dp, _dp,
+                                    _dp]),
+        "hbem_field_stats": (None, [_dp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
         "hbem_arnoldi_sv_batch": (_i, [_i, _i, _u, _i, _d, _dp, _dp, _ip]),
         "hbem_arnoldi_sv_batch_device": (_i, [_i, _i, _u, _i, _d, _vp, ctypes.c_longlong, ctypes.c_longlong, _dp, _ip,
                                               _ip]),

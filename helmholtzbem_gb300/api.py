@@ -5,6 +5,7 @@ Names, argument meaning and error behaviour follow the reference classes
 include/find_roots.hpp); every call goes through the C ABI of libhbem.so.
 """
 import ctypes
+import os
 
 import numpy as np
 
@@ -265,6 +266,76 @@ def arnoldi_sv(Ts, count=1, acc=0.0, d=0, return_status=False):
         return out, status
     check(rc)
     return out
+
+# ---------------------------------------------------------------- incoming waves, transmission problem
+
+WAVE_TYPES = {"Plane": 0, "CircularJ": 1, "CircularY": 2, "FourierHankel1": 3, "FourierHankel2": 4, "Herglotz": 5}
+
+
+def wave(kind, amplitude=1.0, x0=(0.0, 0.0), angle=0.0, eps=0.0, order=0):
+    """One incoming-wave record (incoming::wavespec_t): kind is a WAVE_TYPES name."""
+    return np.array([WAVE_TYPES[kind], amplitude, x0[0], x0[1], angle, eps, order], np.float64)
+
+
+def _waves(waves):
+    w = np.ascontiguousarray(np.asarray(waves, np.float64).reshape(-1, 7))
+    return w, w.shape[0]
+
+
+def incoming_load(fname):
+    """incoming::load: the wave records of a file; raises ValueError where the
+    reference returns false."""
+    n = ctypes.c_int()
+    if C.lib().hbem_incoming_load(os.fsencode(fname), None, 0, ctypes.byref(n)) != 0:
+        raise ValueError("failed to read incoming wave from file " + str(fname))
+    out = np.zeros((n.value, 7))
+    check(C.lib().hbem_incoming_load(os.fsencode(fname), dptr(out), n.value, ctypes.byref(n)))
+    return out
+
+
+def incoming_eval(waves, k, xy):
+    """incoming::compute and compute_del at the points xy (m x 2): (u (m), grad (m x 2))."""
+    w, nw = _waves(waves)
+    k = complex(k)
+    xy = np.ascontiguousarray(np.asarray(xy, np.float64).reshape(-1, 2))
+    m = xy.shape[0]
+    u = np.zeros(m, np.complex128)
+    du = np.zeros((m, 2), np.complex128)
+    check(C.lib().hbem_incoming_eval(dptr(w), nw, k.real, k.imag, dptr(xy), m, u.ctypes.data_as(C._dp),
+                                     du.ctypes.data_as(C._dp)))
+    return u, du
+
+
+def tp_solve(solop, waves, k, c_o, c_i):
+    """tp::direct_second_kind::solve: the 2N traces (Dirichlet, Neumann) of the
+    transmission problem for the incoming wave; solop must be unprojected."""
+    w, nw = _waves(waves)
+    k = complex(k)
+    out = np.zeros(2 * solop.data.npanels, np.complex128)
+    check(C.lib().hbem_tp_solve(solop._h, dptr(w), nw, k.real, k.imag, float(c_o), float(c_i),
+                                out.ctypes.data_as(C._dp)))
+    return out
+
+
+def tp_field_grid(solop, waves, k, c_o, c_i, order_green, lower_left, upper_right, nx, ny, total_field=False,
+                  traces=None):
+    """tp::direct_second_kind::solve_in_rectangle: (S, grid_X, grid_Y), each nx x ny,
+    S[i, j] the field at (grid_X[i, j], grid_Y[i, j])."""
+    w, nw = _waves(waves)
+    k = complex(k)
+    S = np.zeros((ny, nx), np.complex128)
+    gx = np.zeros((ny, nx))
+    gy = np.zeros((ny, nx))
+    tr = None
+    if traces is not None:
+        tr = np.ascontiguousarray(np.asarray(traces, np.complex128))
+    check(C.lib().hbem_tp_field_grid(solop._h, dptr(w), nw, k.real, k.imag, float(c_o), float(c_i), int(order_green),
+                                     float(lower_left[0]), float(lower_left[1]), float(upper_right[0]),
+                                     float(upper_right[1]), int(nx), int(ny), 1 if total_field else 0,
+                                     tr.ctypes.data_as(C._dp) if tr is not None else None,
+                                     S.ctypes.data_as(C._dp), dptr(gx), dptr(gy)))
+    return S.T.copy(), gx.T.copy(), gy.T.copy()
+
 
 def opt_subdiv(f, x_min, x_max, batch_size, limit, tol, seed=0, max_points=100000):
     """opt_subdiv for a batched Python function f(xs) -> ys: returns (x, y, minima)."""

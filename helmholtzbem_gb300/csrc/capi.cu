@@ -966,3 +966,35 @@ int hbem_sweep_sigma(hbem_solop s, const double* k_host, int nk, double c_o, dou
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- accessors for other translation units
+
+namespace hbem {
+
+// host panel data and settings of a solutions operator's mesh
+int solop_mesh(hbem_solop s, int* n, const int** kinds, const double** par, int* proj, int* device) {
+    if (!s) return fail(HBEM_ERR_INVALID, "null solutions operator");
+    *n = s->b->n;
+    *kinds = s->b->kind.data();
+    *par = s->b->par.data();
+    *proj = s->proj;
+    *device = s->b->device;
+    return HBEM_OK;
+}
+
+// T(k) of the operator (projected or not, as created) into T_dev (2N x 2N), synchronised
+int solop_gen_T(hbem_solop s, double k_re, double k_im, double c_o, double c_i, void* T_dev) {
+    if (int r = gen_T_batch(s, &k_re, &k_im, 1, c_o, c_i, 0, static_cast<cplx*>(T_dev))) return r;
+    HB_CK(cudaStreamSynchronize(s->b->st));
+    return HBEM_OK;
+}
+
+hbem_builder solop_builder(hbem_solop s) { return s ? s->b : nullptr; }
+
+// Gauss-Legendre rule on [a, b] (getGaussQR, include/gauleg.hpp:35-79)
+void gauss_rule(double a, double b, int n, double* x, double* w) { gauss_legendre(a, b, n, x, w); }
+
+// launch counter shared by every entry point
+void count_launches(long long n) { g_launches += n; }
+
+}  // namespace hbem

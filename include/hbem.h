@@ -151,6 +151,47 @@ int hbem_polygon_panels_graded(const double* x, const double* y, int n, unsigned
 int hbem_choose_num_panels(const double* x, const double* y, int n, double k_max, double degf, double rfac,
                            unsigned* npanels);
 
+/* ------------------------------------------------------------------ transmission problem and fields */
+
+/* Incoming waves: records of 7 doubles {type, amplitude, x0, y0, angle, eps, order}
+ * (incoming::wavespec_t, include/incoming.hpp:28-43); type 0 Plane, 1 CircularJ,
+ * 2 CircularY, 3 FourierHankel1, 4 FourierHankel2, 5 Herglotz.  Circular and
+ * Fourier-Hankel records need a real wavenumber (HBEM_ERR_UNSUPPORTED otherwise). */
+enum { HBEM_WAVE_PLANE = 0, HBEM_WAVE_CIRCULAR_J = 1, HBEM_WAVE_CIRCULAR_Y = 2, HBEM_WAVE_FOURIER_HANKEL1 = 3,
+       HBEM_WAVE_FOURIER_HANKEL2 = 4, HBEM_WAVE_HERGLOTZ = 5 };
+/* incoming::load (source/utilities/incoming.cpp:48-92): one record per line,
+ * "Type, amplitude, x0, y0, angle[, eps]" or "Type, amplitude, x0, y0, order";
+ * whitespace ignored, empty and '#' lines skipped.  With waves NULL only *nwaves is
+ * returned.  HBEM_ERR_INVALID where the reference returns false.                */
+int hbem_incoming_load(const char* fname, double* waves, int cap, int* nwaves);
+/* incoming::compute / compute_del (incoming.cpp:95-147) at npts points xy (x, y
+ * pairs): u_host npts complex, du_host (may be NULL) npts x (du/dx, du/dy).      */
+int hbem_incoming_eval(const double* waves, int nwaves, double k_re, double k_im, const double* xy_host, int npts,
+                       double* u_host, double* du_host);
+/* tp::direct_second_kind::solve (include/solvers.hpp:101-107, solvers.cpp:116-164)
+ * on the mesh of s, which must be created with proj = 0 (the reference builds an
+ * unprojected SolutionsOperator): T(k) x = [-K_o + M/2, V_o; W_o, K_o^T + M/2] (u_inc,
+ * du_inc/dn at the panel start points).  traces_host: 2N complex (Dirichlet, then
+ * Neumann coefficients).  HBEM_ERR_NONFINITE / HBEM_ERR_SINGULAR with the
+ * reference's messages.                                                          */
+int hbem_tp_solve(hbem_solop s, const double* waves, int nwaves, double k_re, double k_im, double c_o, double c_i,
+                  double* traces_host);
+/* tp::direct_second_kind::solve_in_rectangle (include/solvers.hpp:137-200,
+ * solvers.cpp:165-391): the scattered (total_field = 0) or total field on the
+ * nx x ny grid of [ll, ur] (x index fastest, column-major like Eigen::ArrayXXcd),
+ * by the Green representation with order_green Gauss points per panel over the
+ * traces splined along arc length; grid points on the boundary take the Dirichlet
+ * trace, panels closer than 1e-2 / |kappa| are integrated by a graded composite rule.
+ * traces_host: the 2N traces of hbem_tp_solve, or NULL to solve first (then s must
+ * be unprojected).  grid_x_host, grid_y_host (may be NULL): the grid coordinates.  */
+int hbem_tp_field_grid(hbem_solop s, const double* waves, int nwaves, double k_re, double k_im, double c_o,
+                       double c_i, unsigned order_green, double ll_x, double ll_y, double ur_x, double ur_y, int nx,
+                       int ny, int total_field, const double* traces_host, double* field_host, double* grid_x_host,
+                       double* grid_y_host);
+/* Instrumentation of the last hbem_tp_field_grid call of this thread: CUDA-event time
+ * of the grid kernel, (grid point, boundary node) pairs it summed, near pairs.     */
+void hbem_field_stats(double* grid_kernel_ms, long long* point_node_pairs, long long* near_pairs);
+
 /* ------------------------------------------------------------------ singular values */
 
 /* direct::sv / sv_1st_der / sv_2nd_der for the smallest singular value

@@ -1197,3 +1197,323 @@ def find_resonances_adaptive(f_sample, f_fine, k_min, k_max, batch, limit, sampl
         if r is not None and math.isfinite(r):
             roots.append(r)
     return np.sort(np.array(roots)), np_
+
+
+# ----------------------------------------------------------------- transmission problem and fields
+
+WAVE_TYPES = {"Plane": 0, "CircularJ": 1, "CircularY": 2, "FourierHankel1": 3, "FourierHankel2": 4, "Herglotz": 5}
+
+
+def incoming_load(fname):
+    """incoming::load (source/utilities/incoming.cpp:48-92): records of 7 floats
+    (type, amplitude, x0, y0, angle, eps, order); None where the reference returns
+    false."""
+    import re
+    num = re.compile(r"[+-]?(?:(?:\d+\.?\d*|\.\d+)(?:[eE][+-]?\d+)?|inf(?:inity)?|nan)", re.I)
+    out = []
+    with open(fname) as fh:
+        for line in fh:
+            s = "".join(ch for ch in line if not ch.isspace())
+            if not s or s[0] == "#":
+                continue
+            fields = s.split(",")
+            if fields and fields[-1] == "" and len(fields) > 1:
+                fields = fields[:-1]
+            if fields[0] not in WAVE_TYPES:
+                return None
+            t = WAVE_TYPES[fields[0]]
+            rec = [float(t), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0]
+            need = ["d", "d", "d"] + (["d"] if t in (0, 5) else ["i"]) + (["d"] if t == 5 else [])
+            slots = [1, 2, 3] + ([4] if t in (0, 5) else [6]) + ([5] if t == 5 else [])
+            if len(fields) - 1 != len(need):
+                return None
+            for kind, slot, fld in zip(need, slots, fields[1:]):
+                if kind == "d":
+                    m = num.match(fld)
+                    if not m:
+                        return None
+                    rec[slot] = float(m.group(0))
+                else:
+                    m = re.match(r"[+-]?\d+", fld)
+                    if not m:
+                        return None
+                    rec[slot] = float(int(m.group(0)))
+            out.append(rec)
+    return np.array(out).reshape(-1, 7)
+
+
+def wave_eval(waves, k, x, y):
+    """incoming::compute / compute_del (incoming.cpp:95-229) at one point:
+    (u, du/dx, du/dy)."""
+    from scipy.special import jv, yv
+    k = complex(k)
+    u = 0j
+    g = np.zeros(2, complex)
+    gx, gw = gauss(21)
+    for w in np.asarray(waves, float).reshape(-1, 7):
+        t, amp, x0, y0, ang, eps, order = int(w[0]), w[1], w[2], w[3], w[4], w[5], int(w[6])
+        px, py = x - x0, y - y0
+        if t == 0:
+            e = np.exp(1j * k * (px * math.cos(ang) + py * math.sin(ang)))
+            u += amp * e
+            g += amp * 1j * k * e * np.array([math.cos(ang), math.sin(ang)])
+        elif t == 5:
+            th = ang - eps + 2 * eps * gx
+            e = np.exp(1j * k * (px * np.cos(th) + py * np.sin(th)))
+            u += amp * np.sum(e * gw)
+            g += amp * 1j * k * np.array([np.sum(np.cos(th) * e * gw), np.sum(np.sin(th) * e * gw)])
+        else:
+            r = math.hypot(px, py)
+            th = math.atan2(py, px)
+            s, c = math.sin(th), math.cos(th)
+            eil = np.exp(1j * order * th)
+            ysg = -1.0 if t == 4 else 1.0
+            useJ, useY = t != 2, t != 1
+
+            def F(l):
+                v = 0j
+                if useJ:
+                    v += jv(l, k * r)
+                if useY:
+                    v += 1j * ysg * yv(l, k * r)
+                return v
+            u += amp * F(order) * eil
+            gg = np.zeros(2, complex)
+            if useJ:
+                dfdr = k * (jv(order - 1, k * r) - jv(order + 1, k * r)) / 2
+                dfdt = 1j * order * jv(order, k * r)
+                if r == 0:
+                    if abs(order) == 1:
+                        gg += [dfdr * c - 1j * s * k * 0.5, dfdr * s + 1j * c * k * 0.5]
+                    else:
+                        gg += [dfdr * c, dfdr * s]
+                else:
+                    gg += [dfdr * c - dfdt * s / r, dfdr * s + dfdt * c / r]
+            if useY and r != 0:
+                dfdr = 1j * ysg * k * (yv(order - 1, k * r) - yv(order + 1, k * r)) / 2
+                dfdt = 1j * order * 1j * ysg * yv(order, k * r)
+                gg += [dfdr * c - dfdt * s / r, dfdr * s + dfdt * c / r]
+            g += amp * gg * eil
+    return u, g[0], g[1]
+
+
+def _panel01(kind, P, t):
+    """operator[] and Derivative_01 of a line / circular-arc panel on [0, 1]."""
+    if kind == KIND_LINE:
+        tx, ty = P[2] - P[0], P[3] - P[1]
+        return t * tx + P[0], t * ty + P[1], tx, ty
+    d = P[4] - P[3]
+    a = t * d + P[3]
+    return P[0] + P[2] * math.cos(a), P[1] + P[2] * math.sin(a), -P[2] * d * math.sin(a), P[2] * d * math.cos(a)
+
+
+def _panel_length(kind, P):
+    if kind == KIND_LINE:
+        ax, ay = (-(P[2] - P[0]) + (P[2] + P[0])) * 0.5, (-(P[3] - P[1]) + (P[3] + P[1])) * 0.5
+        bx, by = ((P[2] - P[0]) + (P[2] + P[0])) * 0.5, ((P[3] - P[1]) + (P[3] + P[1])) * 0.5
+        return math.sqrt((bx - ax) ** 2 + (by - ay) ** 2)
+    return P[2] * (P[4] - P[3])
+
+
+def tp_solve(kinds, par, order, waves, k, c_o, c_i):
+    """tp::direct_second_kind::solve (solvers.cpp:116-164): unprojected T(k) x = A_o
+    u_inc_N with A_o = [-K_o + M/2, V_o; W_o, K_o^T + M/2], u_inc_N the incoming wave and
+    its normal derivative at the panel start points (continuous_space.hpp:67-101)."""
+    b = Builder(kinds, par, order)
+    so = SolutionsOperator(b, proj=False)
+    T = so.gen_sol_op(k, c_o, c_i)[0]
+    L = b.assemble(k, c_o, LAYER_ALL, 0)
+    K, V, W = L["K"][0], L["V"][0], L["W"][0]
+    M = b.mass()
+    N = len(kinds)
+    uD = np.zeros(N, complex)
+    uN = np.zeros(N, complex)
+    for i in range(N):
+        px, py, tx, ty = _panel01(kinds[i], par[i], 0.0)
+        u, ux, uy = wave_eval(waves, k, px, py)
+        tn = math.hypot(tx, ty)
+        uD[i] = u
+        uN[i] = (ty / tn) * ux + (-tx / tn) * uy
+    A = np.block([[-K + 0.5 * M, V], [W, K.T + 0.5 * M]])
+    return np.linalg.solve(T, A @ np.concatenate([uD, uN]))
+
+
+def akima_periodic(t, y):
+    """Akima (1970) slopes on the periodic knots t[0..n] (y[n] = y[0]), unrounded
+    corners (Wodicka) where both weights vanish; returns per-interval (b, c, d) of
+    y_i + b h + c h^2 + d h^3."""
+    n = len(t) - 1
+    m = [(y[j + 1] - y[j]) / (t[j + 1] - t[j]) for j in range(n)]
+
+    def Mj(j):
+        return m[j % n]
+    tl, tr = [0.0] * (n + 1), [0.0] * (n + 1)
+    for i in range(n + 1):
+        w1, w2 = abs(Mj(i + 1) - Mj(i)), abs(Mj(i - 1) - Mj(i - 2))
+        if w1 + w2 == 0.0:
+            tl[i], tr[i] = Mj(i - 1), Mj(i)
+        else:
+            tl[i] = tr[i] = (w1 * Mj(i - 1) + w2 * Mj(i)) / (w1 + w2)
+    b, c, d = [], [], []
+    for i in range(n):
+        h = t[i + 1] - t[i]
+        b.append(tr[i])
+        c.append((3 * m[i] - 2 * tr[i] - tl[i + 1]) / h)
+        d.append((tr[i] + tl[i + 1] - 2 * m[i]) / (h * h))
+    return np.array(b), np.array(c), np.array(d)
+
+
+class TraceSpline:
+    """ComplexSpline(mesh, traces) (cspline.cpp:30-53): knots at the panel start arc
+    lengths, closed periodically."""
+
+    def __init__(self, kinds, par, values):
+        N = len(kinds)
+        self.knots = [0.0]
+        for i in range(N):
+            self.knots.append(self.knots[-1] + _panel_length(kinds[i], par[i]))
+        self.coef = []
+        for part in (np.real, np.imag):
+            y = list(part(np.asarray(values))) + [float(part(values[0]))]
+            b, c, d = akima_periodic(self.knots, y)
+            self.coef.append((np.array(y[:-1]), b, c, d))
+
+    def __call__(self, s):
+        i = int(np.searchsorted(self.knots, s, side="right")) - 1
+        i = max(0, min(len(self.knots) - 2, i))
+        h = s - self.knots[i]
+        out = []
+        for y, b, c, d in self.coef:
+            out.append(y[i] + h * (b[i] + h * (c[i] + h * d[i])))
+        return complex(out[0], out[1])
+
+
+def _panel_dist(kind, P, x, y):
+    if kind == KIND_LINE:
+        hx, hy = P[2] - P[0], P[3] - P[1]
+        u = ((x - P[0]) * hx + (y - P[1]) * hy) / (hx * hx + hy * hy)
+        u = max(0.0, min(1.0, u))
+        return math.hypot(x - (P[0] + u * hx), y - (P[1] + u * hy)), u
+    best, t = None, 0.0
+    for tt in (0.0, 1.0):
+        px, py, _, _ = _panel01(kind, P, tt)
+        dd = math.hypot(x - px, y - py)
+        if best is None or dd < best:
+            best, t = dd, tt
+    rho = math.hypot(x - P[0], y - P[1])
+    D = P[4] - P[3]
+    if rho > 0 and D != 0:
+        th = math.atan2(y - P[1], x - P[0])
+        for s in range(-2, 3):
+            u = (th + s * 2 * math.pi - P[3]) / D
+            if 0 <= u <= 1 and abs(rho - P[2]) < best:
+                best, t = abs(rho - P[2]), u
+    return best, t
+
+
+def inside_mesh(kinds, par, x, y):
+    """scatterer::inside_mesh (scatterer.cpp:287-315) with the segment test for arcs."""
+    c, nseg = False, 0
+    for kind, P in zip(kinds, par):
+        x1, y1, _, _ = _panel01(kind, P, 0.0)
+        x2, y2, _, _ = _panel01(kind, P, 1.0)
+        if (((y1 <= y) and (y < y2)) or ((y2 <= y) and (y < y1))) and (x < (x2 - x1) * (y - y1) / (y2 - y1) + x1):
+            c = not c
+        if kind == KIND_LINE:
+            continue
+        if (x2 - x1) * (x - x1) + (y2 - y1) * (y - y1) <= 0 or (x1 - x2) * (x - x2) + (y1 - y2) * (y - y2) <= 0:
+            continue
+        hx, hy = x2 - x1, y2 - y1
+        u = max(0.0, min(1.0, ((x - x1) * hx + (y - y1) * hy) / (hx * hx + hy * hy)))
+        if math.hypot(x - (x1 + u * hx), y - (y1 + u * hy)) > 2 * P[2] * (P[4] - P[3]):
+            continue
+        half = 0.5 * (P[4] - P[3])
+        rx, ry = x - P[0], y - P[1]
+        if rx * rx + ry * ry < P[2] ** 2 and rx * math.cos(P[3] + half) + ry * math.sin(P[3] + half) > P[2] * math.cos(half):
+            nseg += 1
+    return (not c) if nseg % 2 else c
+
+
+def field_points(kinds, par, traces, waves, k, c_o, c_i, order_green, pts, total_field=False):
+    """solve_in_rectangle's lifting (in_solve, solvers.cpp:165-321) at the given points:
+    Green representation over the splined traces with order_green Gauss points per
+    panel; on-boundary points take the Dirichlet trace; panels with d |kappa| < 1e-2
+    integrated adaptively (scipy quad, break point at the nearest point)."""
+    from scipy.special import hankel1
+    from scipy.integrate import quad
+    N = len(kinds)
+    sD = TraceSpline(kinds, par, traces[:N])
+    sN = TraceSpline(kinds, par, traces[N:])
+    xg, wg = gauss(order_green)
+    k = complex(k)
+    plen = [_panel_length(kinds[i], par[i]) for i in range(N)]
+    csum = [0.0] * N
+    for i in range(1, N):
+        csum[i] = csum[i - 1] + plen[i - 1]
+    nodes = []
+    for i in range(N):
+        for j in range(order_green):
+            px, py, tx, ty = _panel01(kinds[i], par[i], xg[j])
+            tn = math.hypot(tx, ty)
+            nx, ny = ty / tn, -tx / tn
+            s = csum[i] + xg[j] * plen[i]
+            tdi, tni = sD(s), sN(s)
+            u, ux, uy = wave_eval(waves, k, px, py)
+            nodes.append((i, px, py, nx, ny, tn * wg[j], tdi, tni, tdi - u, tni - (nx * ux + ny * uy)))
+
+    def H(kap, r):
+        return hankel1(0, kap * r), hankel1(1, kap * r)
+    out = []
+    for (x, y) in pts:
+        inside = inside_mesh(kinds, par, x, y)
+        scale = (1 if inside else -1) * 0.25j
+        kap = k * math.sqrt(c_i if inside else c_o)
+        near, onb = {}, None
+        for i in range(N):
+            d, t = _panel_dist(kinds[i], par[i], x, y)
+            if d < 1e2 * np.finfo(float).eps:
+                onb = (i, t)
+                break
+            if d * abs(kap) < 1e-2:
+                near[i] = t
+        if onb is not None:
+            out.append(sD(csum[onb[0]] + onb[1] * plen[onb[0]]))
+            continue
+        total = 0j
+        rows = {}
+        for (i, px, py, nx, ny, D, tdi, tni, tdo, tno) in nodes:
+            zx, zy = x - px, y - py
+            r = math.hypot(zx, zy)
+            if r <= 0:
+                continue
+            h0, h1 = H(kap, r)
+            tD, tN = (tdi, tni) if inside else (tdo, tno)
+            v = (h0 * tN - kap * h1 * tD * (zx * nx + zy * ny) / r) * D
+            total += v
+            rows[i] = rows.get(i, 0j) + v
+        for i, tmin in near.items():
+            def f(t, part):
+                px, py, tx, ty = _panel01(kinds[i], par[i], t)
+                d = math.hypot(x - px, y - py)
+                if d == 0:
+                    return 0.0
+                tn = math.hypot(tx, ty)
+                nx, ny = ty / tn, -tx / tn
+                h0, h1 = H(kap, d)
+                s = csum[i] + t * plen[i]
+                tD, tN = sD(s), sN(s)
+                if not inside:
+                    u, ux, uy = wave_eval(waves, k, px, py)
+                    tD -= u
+                    tN -= nx * ux + ny * uy
+                val = (h0 * tN - kap * h1 * tD * (nx * (x - px) + ny * (y - py)) / d) * tn
+                return val.real if part == 0 else val.imag
+            pts_b = [tmin] if 0 < tmin < 1 else None
+            re_ = quad(f, 0, 1, args=(0,), points=pts_b, epsabs=0, epsrel=1e-12, limit=400)[0]
+            im_ = quad(f, 0, 1, args=(1,), points=pts_b, epsabs=0, epsrel=1e-12, limit=400)[0]
+            total += complex(re_, im_) - rows.get(i, 0j)
+        v = scale * total
+        if total_field and not inside:
+            v += wave_eval(waves, k, x, y)[0]
+        out.append(v)
+    return np.array(out)

@@ -223,6 +223,14 @@ struct FieldJob {
     int near_cap;
 };
 
+// grid point g: x = ll_x + i h_x, y = ll_y + j h_y, rounded as the host (and the
+// reference) round them -- no fused multiply-add, so points on a coordinate line
+// through a mesh vertex fall on the same side of it everywhere
+__device__ __forceinline__ void grid_xy(const FieldJob& J, int g, double& x, double& y) {
+    x = __dadd_rn(J.llx, __dmul_rn((double)(g % J.nx), J.hx));
+    y = __dadd_rn(J.lly, __dmul_rn((double)(g / J.nx), J.hy));
+}
+
 __device__ __forceinline__ void hankel_pair(bool real_k, double kre, double kim, double r, cplx& h0, cplx& h1) {
     if (real_k) hankel01_real(kre * r, h0, h1);
     else hankel01_cplx(kre * r, kim * r, h0, h1);
@@ -263,8 +271,7 @@ __global__ void __launch_bounds__(kFieldThreads) k_field_grid(FieldJob J) {
     double x = 0., y = 0.;
     bool inside = false;
     if (active) {
-        x = J.llx + (g % J.nx) * J.hx;
-        y = J.lly + (g / J.nx) * J.hy;
+        grid_xy(J, g, x, y);
         inside = inside_mesh(J.npan, J.kind, J.par, x, y);
         const double akap = inside ? J.abs_ki : J.abs_ko;
         int fl = inside ? 1 : 0;
@@ -337,7 +344,8 @@ __global__ void __launch_bounds__(256) k_field_near(FieldJob J, const NearEntry*
     if (e >= nent) return;
     const NearEntry E = ent[e];
     const int g = E.g, i = E.panel;
-    const double x = J.llx + (g % J.nx) * J.hx, y = J.lly + (g / J.nx) * J.hy;
+    double x, y;
+    grid_xy(J, g, x, y);
     const bool inside = (J.flag[g] & 3) == 1;
     const double kr = inside ? J.kire : J.kore, ki = inside ? J.kiim : J.koim;
     // regular Gauss sum of the panel (what the grid kernel added)
@@ -407,8 +415,9 @@ __global__ void k_field_finalize(FieldJob J, cplx* S) {
     cplx v = inside ? mk(-0.25 * a.im, 0.25 * a.re) : mk(0.25 * a.im, -0.25 * a.re);
     if (J.total && !inside) {
         cplx u, ux, uy;
-        wave_eval(J.waves, J.nw, J.g21, J.kre, J.kim, J.llx + (g % J.nx) * J.hx, J.lly + (g / J.nx) * J.hy, false, u,
-                  ux, uy);
+        double x, y;
+        grid_xy(J, g, x, y);
+        wave_eval(J.waves, J.nw, J.g21, J.kre, J.kim, x, y, false, u, ux, uy);
         v += u;
     }
     S[g] = v;

@@ -17,6 +17,7 @@ verified by a sign change of sigma' across [root - 1e-8, root + 1e-8].
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl {gb300,reference}]
 """
 import argparse
+import math
 import json
 import os
 import statistics
@@ -50,7 +51,22 @@ def parse():
                     help="no timing: FP64 and complex-FP32 LU + rSVD of 4 matrices of order 1600 (for captures)")
     ap.add_argument("--profile-case", action="store_true",
                     help="no timing: three sigma sweeps over 16 wavenumbers of the workload (for ncu captures)")
+    ap.add_argument("--profile-field", action="store_true",
+                    help="no timing: the field-at-scale scatterer lifted on a 160 x 160 grid (for ncu captures)")
     return ap.parse_args()
+
+
+def run_profile_field():
+    """The field_at_scale scatterer and wave, traces solved once, total field on a
+    160 x 160 grid over [-1.6, 1.6]^2 with 16 Gauss points per panel."""
+    from helmholtzbem_gb300 import api, geometry
+    x, y = geometry.star_polygon(24, seed=2)
+    so = api.SolutionsOperator(api.BuilderData(geometry.polygon_graded(x, y, 400, 0.5), order=11), proj=False)
+    w = api.wave("Plane", 1.0, angle=math.pi / 3)
+    tr = api.tp_solve(so, w, 10.0, 1.0, 4.0)
+    S, _, _ = api.tp_field_grid(so, w, 10.0, 1.0, 4.0, 16, (-1.6, -1.6), (1.6, 1.6), 160, 160, total_field=True,
+                                traces=tr)
+    print("profile field done, max |u| = %.6e" % float(np.max(np.abs(S))))
 
 
 def run_profile_case():
@@ -524,6 +540,61 @@ def arnoldi_at_scale(torch, C, api, geometry, lib):
     return res, (small_host, small_sig, large_host, large_sig)
 
 
+FIELD_FLOPS_PER_PAIR = 200.0   # per (grid point, boundary node): Hankel pair ~170, geometry + terms ~30
+
+
+def field_at_scale(torch, C, api, geometry, lib, peak):
+    """tp::direct_second_kind::solve_in_rectangle at a plot-sized workload: star
+    polygon (24 vertices, seed 2) with 400 corner-graded panels, c_i = 4, c_o = 1,
+    k = 10, plane wave at 60 degrees; traces by the transmission solve, then the total
+    field on a 400 x 400 grid over [-1.6, 1.6]^2 with 16 Gauss points per panel.
+    Reports the solve and lifting times (host to host, through the C ABI) and the
+    grid kernel's CUDA-event time and FP64 rate."""
+    import ctypes
+    import time
+    x, y = geometry.star_polygon(24, seed=2)
+    kinds, par = geometry.polygon_graded(x, y, 400, 0.5)
+    so = api.SolutionsOperator(api.BuilderData((kinds, par), order=11), proj=False)
+    w = api.wave("Plane", 1.0, angle=math.pi / 3)
+    k, c_o, c_i, order, n = 10.0, 1.0, 4.0, 16, 400
+    api.tp_solve(so, w, k, c_o, c_i)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tr = api.tp_solve(so, w, k, c_o, c_i)
+    t1 = time.perf_counter()
+    api.tp_field_grid(so, w, k, c_o, c_i, order, (-1.6, -1.6), (1.6, 1.6), n, n, total_field=True, traces=tr)
+    t2 = time.perf_counter()
+    S, gx, gy = api.tp_field_grid(so, w, k, c_o, c_i, order, (-1.6, -1.6), (1.6, 1.6), n, n, total_field=True,
+                                  traces=tr)
+    t3 = time.perf_counter()
+    ms, units, near = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_longlong()
+    lib.hbem_field_stats(ctypes.byref(ms), ctypes.byref(units), ctypes.byref(near))
+    tf = units.value * FIELD_FLOPS_PER_PAIR / (ms.value * 1e-3) / 1e12 if ms.value > 0 else None
+    sample = {"kinds": kinds, "par": par, "traces": tr, "wave": w, "k": k, "c_o": c_o, "c_i": c_i, "order": order,
+              "pts": np.c_[gx.ravel()[::1597], gy.ravel()[::1597]], "gpu": S.ravel()[::1597]}
+    return {"workload": "star polygon 24 vertices (seed 2), 400 graded panels (rf 0.5), c_i=4, c_o=1, k=10, plane "
+                        "wave; total field on a 400x400 grid over [-1.6,1.6]^2, 16 Gauss points per panel",
+            "tp_solve_ms": 1e3 * (t1 - t0), "field_grid_ms_e2e": 1e3 * (t3 - t2),
+            "grid_kernel_ms": ms.value, "point_node_pairs": units.value, "near_pairs": near.value,
+            "grid_kernel_fp64_tflops": tf, "grid_kernel_frac_of_measured_fp64": (tf / peak) if (tf and peak) else None,
+            "points_per_s_e2e": n * n / (t3 - t2)}, sample
+
+
+def field_cpu(sample):
+    """The same Green sum on the host for a sample of grid points (every 1597th):
+    numpy/scipy, the oracle's restatement of the lifting; seconds per point and the
+    largest relative difference from the GPU values."""
+    import time
+    from oracle import oracle as O
+    pts = [tuple(p) for p in sample["pts"]]
+    t0 = time.perf_counter()
+    ref = O.field_points(sample["kinds"], sample["par"], sample["traces"], sample["wave"], sample["k"], sample["c_o"],
+                         sample["c_i"], sample["order"], pts, total_field=True)
+    dt = time.perf_counter() - t0
+    return {"points": len(pts), "ms_per_point": 1e3 * dt / len(pts), "cores": 1, "kind": "port",
+            "max_rel_diff_gpu_vs_oracle": float(np.max(np.abs(sample["gpu"] - ref)) / np.max(np.abs(ref)))}
+
+
 def arnoldi_cpu(mats):
     """The reference's arnoldi::sv call (ARPACK on [0 T^-H; T^-1 0] through one LU)
     made through scipy's ARPACK on the host: ms per matrix and the largest relative
@@ -661,6 +732,7 @@ def run_gpu(args):
     batch = batching_sample(torch, C, api, geometry, lib)
     adapt = adaptive_search(torch, so, step(so)[1])
     arnoldi, arn_mats = arnoldi_at_scale(torch, C, api, geometry, lib)
+    field, field_sample = field_at_scale(torch, C, api, geometry, lib, peak)
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
@@ -675,6 +747,10 @@ def run_gpu(args):
             arnoldi["cpu_arpack"] = arnoldi_cpu(arn_mats)
         except Exception as ex:
             arnoldi["cpu_arpack"] = {"error": str(ex)[:200]}
+        try:
+            field["cpu_port"] = field_cpu(field_sample)
+        except Exception as ex:
+            field["cpu_port"] = {"error": str(ex)[:200]}
 
     if rank == 0:
         line = {
@@ -693,6 +769,7 @@ def run_gpu(args):
             "batching_sample": batch,
             "adaptive_search": adapt,
             "arnoldi_at_scale": arnoldi,
+            "field_at_scale": field,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }
@@ -709,6 +786,8 @@ def main():
         run_profile_dense_tail()
     elif args.profile_case:
         run_profile_case()
+    elif args.profile_field:
+        run_profile_field()
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -46,8 +46,9 @@ cudaError_t lu_solve_batched(int n, int nmat, int trans, const cplx* LU, long lo
 
 namespace {
 
-constexpr int kFieldThreads = 128;
-constexpr int kNodeTile = 64;
+constexpr int kFieldSlices = 4;               // warps per CTA, each a share of panels / nodes
+constexpr int kFieldThreads = 32 * kFieldSlices;
+constexpr int kNodeTile = 128;
 constexpr int kNearOrder = 12;        // Gauss points per graded sub-interval
 constexpr int kNearLevels = 60;       // cap on the geometric levels per side
 constexpr double kMachEpsF = 2.220446049250313e-16;
@@ -148,34 +149,32 @@ __device__ double fpan_dist(const double* P, int kind, double x, double y, doubl
     return best;
 }
 
-// scatterer::inside_mesh (scatterer.cpp:287-315): even-odd crossing count of the
-// polygon of panel end points, flipped once per arc panel whose circular segment
-// (between chord and arc) holds the point; arcs are tested only where the reference
-// tests them (foot point inside the chord, chord distance <= 2 x signed length)
-__device__ bool inside_mesh(int npan, const int* kind, const double* par, double x, double y) {
-    bool c = false;
-    int nseg = 0;
-    for (int i = 0; i < npan; ++i) {
-        const double* P = par + 5 * i;
-        double x1, y1, x2, y2, tx, ty, tn;
-        fpan(P, kind[i], 0., x1, y1, tx, ty, tn);
-        fpan(P, kind[i], 1., x2, y2, tx, ty, tn);
-        if ((((y1 <= y) && (y < y2)) || ((y2 <= y) && (y < y1))) && (x < (x2 - x1) * (y - y1) / (y2 - y1) + x1))
-            c = !c;
-        if (kind[i] == HBEM_PANEL_LINE) continue;
-        if ((x2 - x1) * (x - x1) + (y2 - y1) * (y - y1) <= 0. || (x1 - x2) * (x - x2) + (y1 - y2) * (y - y2) <= 0.)
-            continue;
-        const double hx = x2 - x1, hy = y2 - y1;
-        const double u = fmax(0., fmin(1., ((x - x1) * hx + (y - y1) * hy) / (hx * hx + hy * hy)));
-        const double cdx = x - (x1 + u * hx), cdy = y - (y1 + u * hy);
-        const double len = P[2] * (P[4] - P[3]);             // ParametrizedCircularArc::length (signed)
-        if (sqrt(cdx * cdx + cdy * cdy) > 2. * len) continue;
-        const double rx = x - P[0], ry = y - P[1], half = 0.5 * (P[4] - P[3]);
-        double sm, cm;
-        sincos(P[3] + half, &sm, &cm);
-        if (rx * rx + ry * ry < P[2] * P[2] && rx * cm + ry * sm > P[2] * cos(half)) ++nseg;
-    }
-    return (nseg & 1) ? !c : c;
+// scatterer::inside_mesh (scatterer.cpp:287-315), one panel's share: whether the
+// leftward ray from the point crosses the chord between the panel's end points
+// (half-open in y), and, for an arc, whether the point lies in the circular segment
+// between chord and arc (tested only where the reference tests it: foot point inside
+// the chord, chord distance <= 2 x signed length).  The point is inside when the
+// crossings and the segments are odd in number together (crossings parity, flipped by
+// an odd segment count).
+__device__ __forceinline__ void inside_share(const double* P, int kind, double x, double y, int& cross, int& seg) {
+    double x1, y1, x2, y2, tx, ty, tn;
+    fpan(P, kind, 0., x1, y1, tx, ty, tn);
+    fpan(P, kind, 1., x2, y2, tx, ty, tn);
+    cross = ((((y1 <= y) && (y < y2)) || ((y2 <= y) && (y < y1))) && (x < (x2 - x1) * (y - y1) / (y2 - y1) + x1)) ? 1
+                                                                                                                 : 0;
+    seg = 0;
+    if (kind == HBEM_PANEL_LINE) return;
+    if ((x2 - x1) * (x - x1) + (y2 - y1) * (y - y1) <= 0. || (x1 - x2) * (x - x2) + (y1 - y2) * (y - y2) <= 0.)
+        return;
+    const double hx = x2 - x1, hy = y2 - y1;
+    const double u = fmax(0., fmin(1., ((x - x1) * hx + (y - y1) * hy) / (hx * hx + hy * hy)));
+    const double cdx = x - (x1 + u * hx), cdy = y - (y1 + u * hy);
+    const double len = P[2] * (P[4] - P[3]);             // ParametrizedCircularArc::length (signed)
+    if (sqrt(cdx * cdx + cdy * cdy) > 2. * len) return;
+    const double rx = x - P[0], ry = y - P[1], half = 0.5 * (P[4] - P[3]);
+    double sm, cm;
+    sincos(P[3] + half, &sm, &cm);
+    if (rx * rx + ry * ry < P[2] * P[2] && rx * cm + ry * sm > P[2] * cos(half)) seg = 1;
 }
 
 // ------------------------------------------------------------------ trace splines (device)
@@ -262,26 +261,45 @@ __global__ void k_field_nodes(FieldJob J, const double* xg, const double* wg, FN
     out[q] = n;
 }
 
-// one thread per grid point: inside test, boundary / near-panel tests, Green sum
+// 32 grid points per CTA, one per lane; the CTA's four warps split the panels for the
+// inside / boundary / near tests and the boundary nodes of every shared-memory tile
+// for the Green sum, then combine through shared memory.
 __global__ void __launch_bounds__(kFieldThreads) k_field_grid(FieldJob J) {
     __shared__ FNode tile[kNodeTile];
-    const int G = J.nx * J.ny;
-    const int g = blockIdx.x * kFieldThreads + threadIdx.x;
-    bool active = g < G;
+    __shared__ int s_cross[kFieldSlices][32], s_seg[kFieldSlices][32], s_onb[kFieldSlices][32];
+    __shared__ double s_bt[kFieldSlices][32];
+    __shared__ cplx s_part[kFieldSlices][32];
+    const int G = J.nx * J.ny, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int g = blockIdx.x * 32 + lane;
     double x = 0., y = 0.;
-    bool inside = false;
-    if (active) {
+    int cross = 0, seg = 0, onb = 0x7fffffff;
+    double bt = 0.;
+    if (g < G) {
         grid_xy(J, g, x, y);
-        inside = inside_mesh(J.npan, J.kind, J.par, x, y);
+        for (int i = w; i < J.npan; i += kFieldSlices) {
+            int c, sg;
+            inside_share(J.par + 5 * i, J.kind[i], x, y, c, sg);
+            cross ^= c;
+            seg += sg;
+        }
+    }
+    s_cross[w][lane] = cross;
+    s_seg[w][lane] = seg;
+    __syncthreads();
+    for (int q = 0; q < kFieldSlices; ++q)
+        if (q != w) {
+            cross ^= s_cross[q][lane];
+            seg += s_seg[q][lane];
+        }
+    const bool inside = (seg & 1) ? !cross : (cross != 0);
+    if (g < G) {
         const double akap = inside ? J.abs_ki : J.abs_ko;
-        int fl = inside ? 1 : 0;
-        for (int i = 0; i < J.npan; ++i) {
+        for (int i = w; i < J.npan; i += kFieldSlices) {
             double t;
             const double d = fpan_dist(J.par + 5 * i, J.kind[i], x, y, t);
             if (d < 1e2 * kMachEpsF) {            // on the boundary: the Dirichlet trace
-                fl = 2 | (i << 2);
-                J.bnd_t[g] = t;
-                active = false;
+                onb = i;
+                bt = t;
                 break;
             }
             if (d * akap < 1e-2) {
@@ -289,18 +307,32 @@ __global__ void __launch_bounds__(kFieldThreads) k_field_grid(FieldJob J) {
                 if (slot < J.near_cap) J.near[slot] = NearEntry{g, i, t};
             }
         }
-        J.flag[g] = fl;
+    }
+    s_onb[w][lane] = onb;
+    s_bt[w][lane] = bt;
+    __syncthreads();
+    for (int q = 0; q < kFieldSlices; ++q)       // the first panel in index order
+        if (s_onb[q][lane] < onb) {
+            onb = s_onb[q][lane];
+            bt = s_bt[q][lane];
+        }
+    const bool active = g < G && onb == 0x7fffffff;
+    if (g < G && w == 0) {
+        J.flag[g] = onb != 0x7fffffff ? (2 | (onb << 2)) : (inside ? 1 : 0);
+        if (onb != 0x7fffffff) J.bnd_t[g] = bt;
     }
     const double kr = inside ? J.kire : J.kore, ki = inside ? J.kiim : J.koim;
     cplx sum = mk(0.);
     const int M = J.npan * J.nq;
+    constexpr int kPerWarp = kNodeTile / kFieldSlices;
     for (int base = 0; base < M; base += kNodeTile) {
         const int cnt = min(kNodeTile, M - base);
         __syncthreads();
         for (int e = threadIdx.x; e < cnt; e += kFieldThreads) tile[e] = J.nodes[base + e];
         __syncthreads();
         if (!active) continue;
-        for (int e = 0; e < cnt; ++e) {
+        const int e1 = min(cnt, (w + 1) * kPerWarp);
+        for (int e = w * kPerWarp; e < e1; ++e) {
             const FNode& nd = tile[e];
             const double zx = x - nd.yx, zy = y - nd.yy, r = sqrt(zx * zx + zy * zy);
             if (!(r > 0.)) continue;
@@ -312,7 +344,13 @@ __global__ void __launch_bounds__(kFieldThreads) k_field_grid(FieldJob J) {
             sum += nd.D * term;
         }
     }
-    if (g < G) J.acc[g] = sum;
+    s_part[w][lane] = sum;
+    __syncthreads();
+    if (w == 0 && g < G) {
+        cplx tot = s_part[0][lane];
+        for (int q = 1; q < kFieldSlices; ++q) tot += s_part[q][lane];
+        J.acc[g] = tot;
+    }
 }
 
 // f(t) of the near-panel integral (the integrand of solvers.cpp:275-293)
@@ -853,7 +891,7 @@ int hbem_tp_field_grid(hbem_solop s, const double* waves, int nwaves, double k_r
         J.near_cap = cap;
         FD_CK(cudaMemset(F.nearcnt.p, 0, sizeof(int)));
         cudaEventRecord(e0, 0);
-        k_field_grid<<<(unsigned)((G + kFieldThreads - 1) / kFieldThreads), kFieldThreads>>>(J);
+        k_field_grid<<<(unsigned)((G + 31) / 32), kFieldThreads>>>(J);
         cudaEventRecord(e1, 0);
         FD_CK(cudaGetLastError());
         FD_CK(cudaMemcpy(&nnear, F.nearcnt.p, sizeof(int), cudaMemcpyDeviceToHost));

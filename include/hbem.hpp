@@ -9,6 +9,8 @@
 //   arnoldi::sv, sv_1st_der, sv_2nd_der       include/singular_values_arnoldi.hpp:29-66
 //   scatterer::read, length, auto_num_panels,
 //     make_N_polygonal_panels, make_polygonal_panels   include/scatterer.hpp:39-84
+//   incoming::load, compute, compute_del      include/incoming.hpp
+//   tp::direct_second_kind::solve, solve_in_rectangle   include/solvers.hpp:101-200
 //   rtsafe, zbrent, BrentMinimizer            include/find_roots.hpp:37-67,181-233
 //
 // Matrices: hbem::MatrixXcd / MatrixXd (column-major, data()/rows()/cols()/
@@ -287,6 +289,102 @@ inline MatrixXd sv_2nd_der(const MatrixXcd& T, const MatrixXcd& T_der, const Mat
     return to_matrix(run(m, 2, count, acc), count, 3);
 }
 }  // namespace arnoldi
+
+// Incoming waves as records (incoming::wavespec_t); the reference's drivers wrap
+// incoming::compute / compute_del in lambdas for tp::direct_second_kind, here the
+// records themselves are passed and evaluated on the GPU.
+namespace incoming {
+enum class WaveType { Plane = 0, CircularJ = 1, CircularY = 2, FourierHankel1 = 3, FourierHankel2 = 4, Herglotz = 5 };
+struct wavespec_t {
+    WaveType type = WaveType::Plane;
+    double amplitude = 1., eps = 0., angle = 0.;
+    int order = 0;
+    double x0[2] = {0., 0.};
+};
+typedef std::vector<wavespec_t> wave;
+inline std::vector<double> records(const wave& w) {
+    std::vector<double> r;
+    for (const auto& p : w)
+        r.insert(r.end(), {double(int(p.type)), p.amplitude, p.x0[0], p.x0[1], p.angle, p.eps, double(p.order)});
+    return r;
+}
+inline bool load(const std::string& fname, wave& w) {
+    int n = 0;
+    if (hbem_incoming_load(fname.c_str(), nullptr, 0, &n) != HBEM_OK) return false;
+    std::vector<double> r((size_t)n * 7);
+    if (hbem_incoming_load(fname.c_str(), r.data(), n, &n) != HBEM_OK) return false;
+    for (int q = 0; q < n; ++q) {
+        wavespec_t p;
+        p.type = (WaveType)(int)r[7 * q];
+        p.amplitude = r[7 * q + 1];
+        p.x0[0] = r[7 * q + 2];
+        p.x0[1] = r[7 * q + 3];
+        p.angle = r[7 * q + 4];
+        p.eps = r[7 * q + 5];
+        p.order = (int)r[7 * q + 6];
+        w.push_back(p);
+    }
+    return true;
+}
+// u and grad u at one point (incoming::compute / compute_del)
+inline std::complex<double> compute(const wave& w, double x, double y, const std::complex<double>& k,
+                                    std::complex<double>* grad = nullptr) {
+    const auto r = records(w);
+    const double xy[2] = {x, y};
+    double u[2], du[4];
+    throw_if(hbem_incoming_eval(r.data(), (int)w.size(), k.real(), k.imag(), xy, 1, u, du));
+    if (grad) {
+        grad[0] = {du[0], du[1]};
+        grad[1] = {du[2], du[3]};
+    }
+    return {u[0], u[1]};
+}
+}  // namespace incoming
+
+// The transmission problem for an incoming wave (tp::direct_second_kind, solvers.hpp):
+// traces (Dirichlet then Neumann coefficients, 2N) and the field on a grid.
+namespace tp {
+namespace direct_second_kind {
+inline std::vector<std::complex<double>> solve(const Mesh& mesh, const incoming::wave& u_inc, unsigned order,
+                                               const std::complex<double>& k, double c_o, double c_i) {
+    BuilderData data(mesh, P1, P1, order);
+    SolutionsOperator so(data, false);
+    const auto r = incoming::records(u_inc);
+    std::vector<std::complex<double>> tr(2 * (size_t)mesh.size());
+    throw_if(hbem_tp_solve(so.handle(), r.data(), (int)u_inc.size(), k.real(), k.imag(), c_o, c_i,
+                           reinterpret_cast<double*>(tr.data())));
+    return tr;
+}
+// S(i, j), grid_X(i, j), grid_Y(i, j): i along x, j along y
+inline MatrixXcd solve_in_rectangle(const Mesh& mesh, const incoming::wave& u_inc, unsigned order_galerkin,
+                                    unsigned order_green, const std::complex<double>& k, double c_o, double c_i,
+                                    const double lower_left_corner[2], const double upper_right_corner[2],
+                                    unsigned grid_size_x, unsigned grid_size_y, MatrixXd& grid_X, MatrixXd& grid_Y,
+                                    bool total_field) {
+    BuilderData data(mesh, P1, P1, order_galerkin);
+    SolutionsOperator so(data, false);
+    const auto r = incoming::records(u_inc);
+    const size_t G = (size_t)grid_size_x * grid_size_y;
+    std::vector<std::complex<double>> S(G);
+    std::vector<double> gx(G), gy(G);
+    throw_if(hbem_tp_field_grid(so.handle(), r.data(), (int)u_inc.size(), k.real(), k.imag(), c_o, c_i, order_green,
+                                lower_left_corner[0], lower_left_corner[1], upper_right_corner[0],
+                                upper_right_corner[1], (int)grid_size_x, (int)grid_size_y, total_field ? 1 : 0,
+                                nullptr, reinterpret_cast<double*>(S.data()), gx.data(), gy.data()));
+    MatrixXcd out((long)grid_size_x, (long)grid_size_y);
+    grid_X.resize((long)grid_size_x, (long)grid_size_y);
+    grid_Y.resize((long)grid_size_x, (long)grid_size_y);
+    for (unsigned j = 0; j < grid_size_y; ++j)
+        for (unsigned i = 0; i < grid_size_x; ++i) {
+            const size_t g = i + (size_t)j * grid_size_x;
+            out(i, j) = S[g];
+            grid_X(i, j) = gx[g];
+            grid_Y(i, j) = gy[g];
+        }
+    return out;
+}
+}  // namespace direct_second_kind
+}  // namespace tp
 
 namespace detail {
 inline double call_fn(double x, void* u) { return (*static_cast<std::function<double(double)>*>(u))(x); }

@@ -49,7 +49,15 @@ int main(int argc, char** argv) {
             sq_sigma = direct::sv(Tsq);
         }
     }
-    std::printf("%.17e %.17e %.17e %.17e %.17e %d %d %.17e %.17e %d %.17e\n", r[0], r[1], r[2], std::abs(V1(3, 5)),
-                root, (int)found, (int)threw, a0, a2(0, 0), sq_panels, sq_sigma);
+    // transmission problem on the circle and its total field (examples/plot_solution_polygon.cpp:169-181)
+    incoming::wave w(1);
+    w[0].type = incoming::WaveType::Plane;
+    w[0].angle = 0.5;
+    const double ll[2] = {-0.5, -0.5}, ur[2] = {0.5, 0.5};
+    MatrixXd gX, gY;
+    MatrixXcd S = tp::direct_second_kind::solve_in_rectangle(mesh, w, 7, 10, 2.5, 1.0, 4.0, ll, ur, 9, 7, gX, gY, true);
+    std::printf("%.17e %.17e %.17e %.17e %.17e %d %d %.17e %.17e %d %.17e %.17e %.17e %.17e\n", r[0], r[1], r[2],
+                std::abs(V1(3, 5)), root, (int)found, (int)threw, a0, a2(0, 0), sq_panels, sq_sigma, S(2, 5).real(),
+                S(2, 5).imag(), gY(2, 5));
     return (found && threw) ? 0 : 1;
 }

@@ -44,3 +44,8 @@ def test_facade_runs_and_matches_python(tmp_path):
     assert int(vals[9]) == len(sq[0])
     ssq = api.sv_dense([[api.SolutionsOperator(api.BuilderData(sq, order=7)).gen_sol_op(3.0, 1.0, 4.0)]])[0][0]
     assert abs(vals[10] - ssq) <= 1e-12 * ssq
+    # tp::direct_second_kind::solve_in_rectangle on the circle mesh, total field
+    so_u = api.SolutionsOperator(api.BuilderData(geometry.circle(0.25, 16), order=7), proj=False)
+    S, gx, gy = api.tp_field_grid(so_u, api.wave("Plane", angle=0.5), 2.5, 1.0, 4.0, 10, (-0.5, -0.5), (0.5, 0.5),
+                                  9, 7, total_field=True)
+    assert abs(complex(vals[11], vals[12]) - S[2, 5]) <= 1e-12 * abs(S[2, 5]) and vals[13] == gy[2, 5]

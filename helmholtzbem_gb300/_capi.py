@@ -29,6 +29,8 @@ EXPORTS = [
     "hbem_scatterer_read", "hbem_polygon_length", "hbem_auto_num_panels", "hbem_polygon_panels",
     "hbem_polygon_panels_graded", "hbem_choose_num_panels",
     "hbem_incoming_load", "hbem_incoming_eval", "hbem_tp_solve", "hbem_tp_field_grid", "hbem_field_stats",
+    "hbem_mlp_create", "hbem_mlp_destroy", "hbem_mlp_num_params", "hbem_mlp_get_params", "hbem_mlp_set_params",
+    "hbem_mlp_forward", "hbem_mlp_gradients", "hbem_mlp_train_step", "hbem_bf16_gemm_device",
     "hbem_find_resonances_plain", "hbem_rtsafe", "hbem_zbrent", "hbem_brent_min",
 ]
 
@@ -41,6 +43,7 @@ _vp = ctypes.c_void_p
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
 _up = ctypes.POINTER(ctypes.c_uint)
+_fp = ctypes.POINTER(ctypes.c_float)
 
 FN = ctypes.CFUNCTYPE(ctypes.c_double, ctypes.c_double, ctypes.c_void_p)
 FN_BOTH = ctypes.CFUNCTYPE(None, ctypes.c_double, _dp, _dp, ctypes.c_void_p)
@@ -110,6 +113,16 @@ def load(path=LIB_PATH):
         "hbem_tp_field_grid": (_i, [_vp, _dp, _i, _d, _d, _d, _d, _u, _d, _d, _d, _d, _i, _i, _i, _dp, _dp, _dp,
                                     _dp]),
         "hbem_field_stats": (None, [_dp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
+        "hbem_mlp_create": (_i, [_i, _i, _i, _i, ctypes.c_ulonglong, ctypes.POINTER(_vp)]),
+        "hbem_mlp_destroy": (_i, [_vp]),
+        "hbem_mlp_num_params": (_i, [_vp, ctypes.POINTER(ctypes.c_longlong)]),
+        "hbem_mlp_get_params": (_i, [_vp, _fp]),
+        "hbem_mlp_set_params": (_i, [_vp, _fp]),
+        "hbem_mlp_forward": (_i, [_vp, _fp, _i, _fp]),
+        "hbem_mlp_gradients": (_i, [_vp, _fp, _fp, _i, _fp, _fp]),
+        "hbem_mlp_train_step": (_i, [_vp, _fp, _fp, _i, ctypes.c_float, _fp]),
+        "hbem_bf16_gemm_device": (_i, [_i, _i, _i, _vp, ctypes.c_longlong, _vp, ctypes.c_longlong, _vp,
+                                       ctypes.c_longlong, _i]),
         "hbem_arnoldi_sv_batch": (_i, [_i, _i, _u, _i, _d, _dp, _dp, _ip]),
         "hbem_arnoldi_sv_batch_device": (_i, [_i, _i, _u, _i, _d, _vp, ctypes.c_longlong, ctypes.c_longlong, _dp, _ip,
                                               _ip]),

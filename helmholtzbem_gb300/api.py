@@ -337,6 +337,61 @@ def tp_field_grid(solop, waves, k, c_o, c_i, order_green, lower_left, upper_righ
     return S.T.copy(), gx.T.copy(), gy.T.copy()
 
 
+# ---------------------------------------------------------------- proposal network
+
+class MLP:
+    """The learned proposal's network (BF16 products, FP32 accumulation and master
+    weights, Adam) on the GPU: n_in -> width (GELU) x depth -> n_out."""
+
+    def __init__(self, n_in, width, depth, n_out, seed=0):
+        self.dims = [n_in] + [width] * depth + [n_out]
+        h = ctypes.c_void_p()
+        check(C.lib().hbem_mlp_create(int(n_in), int(width), int(depth), int(n_out), int(seed), ctypes.byref(h)))
+        self._h = h
+        c = ctypes.c_longlong()
+        check(C.lib().hbem_mlp_num_params(self._h, ctypes.byref(c)))
+        self.num_params = c.value
+
+    def __del__(self):
+        if getattr(self, "_h", None) and C._lib is not None:
+            C._lib.hbem_mlp_destroy(self._h)
+            self._h = None
+
+    @staticmethod
+    def _f(a):
+        return np.ascontiguousarray(np.asarray(a, np.float32))
+
+    def get_params(self):
+        p = np.zeros(self.num_params, np.float32)
+        check(C.lib().hbem_mlp_get_params(self._h, p.ctypes.data_as(C._fp)))
+        return p
+
+    def set_params(self, p):
+        p = self._f(p)
+        check(C.lib().hbem_mlp_set_params(self._h, p.ctypes.data_as(C._fp)))
+
+    def forward(self, X):
+        X = self._f(X)
+        Y = np.zeros((X.shape[0], self.dims[-1]), np.float32)
+        check(C.lib().hbem_mlp_forward(self._h, X.ctypes.data_as(C._fp), X.shape[0], Y.ctypes.data_as(C._fp)))
+        return Y
+
+    def gradients(self, X, T):
+        X, T = self._f(X), self._f(T)
+        g = np.zeros(self.num_params, np.float32)
+        loss = ctypes.c_float()
+        check(C.lib().hbem_mlp_gradients(self._h, X.ctypes.data_as(C._fp), T.ctypes.data_as(C._fp), X.shape[0],
+                                         ctypes.byref(loss), g.ctypes.data_as(C._fp)))
+        return loss.value, g
+
+    def train_step(self, X, T, lr):
+        X, T = self._f(X), self._f(T)
+        loss = ctypes.c_float()
+        check(C.lib().hbem_mlp_train_step(self._h, X.ctypes.data_as(C._fp), T.ctypes.data_as(C._fp), X.shape[0],
+                                          float(lr), ctypes.byref(loss)))
+        return loss.value
+
+
 def opt_subdiv(f, x_min, x_max, batch_size, limit, tol, seed=0, max_points=100000):
     """opt_subdiv for a batched Python function f(xs) -> ys: returns (x, y, minima)."""
     def _f(xp, n, yp, user):

@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libhbem.so")
 SOURCES = ["assemble.cu", "solop.cu", "dense.cu", "lu.cu", "tc_gemm.cu", "rsvd.cu", "arnoldi.cu", "capi.cu", "roots.cu",
-           "scatterer.cpp", "fields.cu"]
+           "scatterer.cpp", "fields.cu", "mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Host code: no floating-point contraction, so that x86-64 and aarch64 hosts (where
 # the compiler would otherwise fuse a*b+c into FMAs) give bit-identical results.

@@ -40,6 +40,7 @@ cudaError_t lu_perm_from_piv(int n, int nmat, const int* piv, int* perm, cudaStr
 bool lu_solve_supported(int n);
 void lu_set_cluster_panels(int on);
 void lu_set_tensor_cores(int on);
+void mlp_set_tensor_cores(int on);
 cudaError_t launch_cgemm_f32(int m, int n, int k, const cplxf* A, long long lda, long long sa, const cplxf* B,
                              long long ldb, long long sb, cplxf* C, long long ldc, long long sc, int nmat,
                              int use_tc, int* err, cudaStream_t st);
@@ -335,6 +336,10 @@ int hbem_set_option(const char* name, int value) {
     }
     if (k == "svd_fast") {
         g_svd_fast = value ? 1 : 0;
+        return HBEM_OK;
+    }
+    if (k == "mlp_tensor_cores") {
+        mlp_set_tensor_cores(value);
         return HBEM_OK;
     }
     if (k == "arnoldi_maxit") {

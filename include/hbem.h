@@ -59,7 +59,8 @@ int hbem_set_device(int device);
  *   "svd_fast" (default 1): dense sigma_min / sigma' / sigma'' (direct::sv*) of matrices
  *   up to order 100 by FP32 Jacobi plus FP64 refinement of the near singular triplets
  *   (one FP64 LU per matrix); 0 always uses the FP64-polished Jacobi kernel.
- *   "arnoldi_maxit" (default 1000, >= 1): iteration cap of hbem_arnoldi_sv_batch*.  */
+ *   "arnoldi_maxit" (default 1000, >= 1): iteration cap of hbem_arnoldi_sv_batch*.
+ *   "mlp_tensor_cores" (default 1): the MLP's BF16 products on tcgen05; 0 uses FP32 FMA. */
 int hbem_set_option(const char* name, int value);
 
 /* Instrumentation (no counterpart in the reference, which prints std::chrono
@@ -191,6 +192,31 @@ int hbem_tp_field_grid(hbem_solop s, const double* waves, int nwaves, double k_r
 /* Instrumentation of the last hbem_tp_field_grid call of this thread: CUDA-event time
  * of the grid kernel, (grid point, boundary node) pairs it summed, near pairs.     */
 void hbem_field_stats(double* grid_kernel_ms, long long* point_node_pairs, long long* near_pairs);
+
+/* ------------------------------------------------------------------ learned proposal network */
+
+/* The multilayer perceptron of the learned resonance proposal (no counterpart in the
+ * reference): n_in -> width (GELU) x depth -> n_out, BF16 products with FP32
+ * accumulation on the tensor cores, FP32 master weights and Adam.  Parameters and
+ * gradients as one FP32 vector: per layer W (out x in, row-major) then b.         */
+typedef struct hbem_mlp_s* hbem_mlp;
+int hbem_mlp_create(int n_in, int width, int depth, int n_out, unsigned long long seed, hbem_mlp* out);
+int hbem_mlp_destroy(hbem_mlp m);
+int hbem_mlp_num_params(hbem_mlp m, long long* count);
+int hbem_mlp_get_params(hbem_mlp m, float* host);
+int hbem_mlp_set_params(hbem_mlp m, const float* host);
+/* Y (batch x n_out) from X (batch x n_in), row-major host arrays */
+int hbem_mlp_forward(hbem_mlp m, const float* X_host, int batch, float* Y_host);
+/* mean squared error against T (batch x n_out) and, when grads_host is not NULL, its
+ * gradient with respect to the parameters */
+int hbem_mlp_gradients(hbem_mlp m, const float* X_host, const float* T_host, int batch, float* loss_host,
+                       float* grads_host);
+/* one Adam step (beta 0.9 / 0.999, eps 1e-8) on that loss */
+int hbem_mlp_train_step(hbem_mlp m, const float* X_host, const float* T_host, int batch, float lr, float* loss_host);
+/* C (FP32, M x N, row-major, ldc) = A (BF16, M x K, lda) B (BF16, N x K, ldb)^T on the
+ * device: the network's product kernel; M, N multiples of 128, K of 64.            */
+int hbem_bf16_gemm_device(int M, int N, int K, const void* A, long long lda, const void* B, long long ldb, void* C,
+                          long long ldc, int tensor_cores);
 
 /* ------------------------------------------------------------------ singular values */
 

@@ -1517,3 +1517,81 @@ def field_points(kinds, par, traces, waves, k, c_o, c_i, order_green, pts, total
             v += wave_eval(waves, k, x, y)[0]
         out.append(v)
     return np.array(out)
+
+
+# ----------------------------------------------------------------- proposal network (MLP)
+
+def bf16_round(x):
+    """Round float32 values to bfloat16 (round to nearest even), returned as float32."""
+    a = np.ascontiguousarray(np.asarray(x, np.float32))
+    u = a.view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32).reshape(a.shape)
+
+
+def _gelu(z):
+    from scipy.special import erf
+    z = np.asarray(z, np.float64)
+    return 0.5 * z * (1.0 + erf(z / math.sqrt(2.0)))
+
+
+def _gelu_grad(z):
+    from scipy.special import erf
+    z = np.asarray(z, np.float64)
+    return 0.5 * (1.0 + erf(z / math.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / math.sqrt(2.0 * math.pi)
+
+
+class MLPOracle:
+    """The proposal network restated in numpy: layers W (out x in), b; GELU on the
+    hidden layers; mean squared error.  bf16=True rounds the products' operands and the
+    stored activations to bfloat16 as the GPU does (products accumulated in float64
+    here, in FP32 on the GPU); bf16=False is the exact float64 network."""
+
+    def __init__(self, params, dims, bf16=True):
+        self.dims = dims            # [n_in, width, ..., n_out]
+        self.bf16 = bf16
+        self.W, self.b = [], []
+        off = 0
+        for i, o in zip(dims[:-1], dims[1:]):
+            self.W.append(np.asarray(params[off:off + o * i], np.float64).reshape(o, i))
+            off += o * i
+            self.b.append(np.asarray(params[off:off + o], np.float64))
+            off += o
+
+    def _r(self, x):
+        return bf16_round(x).astype(np.float64) if self.bf16 else np.asarray(x, np.float64)
+
+    def _f32(self, x):
+        return np.asarray(x, np.float32).astype(np.float64) if self.bf16 else x
+
+    def forward(self, X, keep=False):
+        H = self._r(X)
+        Hs, Zs = [H], []
+        L = len(self.W)
+        for l in range(L):
+            Z = self._f32(H @ self._r(self.W[l]).T) + self.b[l]
+            Z = self._f32(Z)
+            Zs.append(Z)
+            if l < L - 1:
+                H = self._r(_gelu(Z))
+                Hs.append(H)
+        return (Zs[-1], Hs, Zs) if keep else Zs[-1]
+
+    def gradients(self, X, T):
+        Y, Hs, Zs = self.forward(X, keep=True)
+        count = Y.size
+        loss = float(np.sum((Y - T) ** 2) / count)
+        G = self._f32(2.0 * (Y - T) / count)
+        grads = []
+        for l in range(len(self.W) - 1, -1, -1):
+            Gr = self._r(G)
+            dW = self._f32(Gr.T @ Hs[l])
+            db = self._f32(G.sum(axis=0))
+            grads.append((dW, db))
+            if l == 0:
+                break
+            dH = self._f32(Gr @ self._r(self.W[l]))
+            G = self._f32(dH * _gelu_grad(Zs[l - 1]))
+        grads.reverse()
+        flat = np.concatenate([np.concatenate([dW.ravel(), db]) for dW, db in grads])
+        return loss, flat

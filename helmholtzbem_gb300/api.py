@@ -152,6 +152,16 @@ class SolutionsOperator:
                                                     ctypes.byref(nr), ctypes.byref(ns), ctypes.byref(ne)))
         return roots[:min(nr.value, max_roots)].copy(), ns.value, ne.value
 
+    def refine_brackets(self, a, b, c_o, c_i, tol=1e-8, max_shift=3, max_roots=4096):
+        """Local minima of sigma_min from candidate brackets [a_i, b_i]: (roots, n_evals)."""
+        a = np.ascontiguousarray(a, np.float64)
+        b = np.ascontiguousarray(b, np.float64)
+        out = np.zeros(max_roots)
+        nr, ne = ctypes.c_int(), ctypes.c_int()
+        check(C.lib().hbem_refine_brackets(self._h, dptr(a), dptr(b), int(a.size), float(c_o), float(c_i), float(tol),
+                                           int(max_shift), dptr(out), max_roots, ctypes.byref(nr), ctypes.byref(ne)))
+        return out[:min(nr.value, max_roots)].copy(), ne.value
+
     def find_resonances_plain(self, k_min, k_max, npoints, c_o, c_i, tol=1e-8, max_roots=4096):
         roots = np.zeros(max_roots)
         grid = np.zeros((npoints, 3))

@@ -500,6 +500,74 @@ int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npo
     return HBEM_OK;
 }
 
+// Local minima of sigma_min from candidate brackets (the confirmation step of the
+// learned proposal; the Newton phase of the plain search above): sigma' at both ends
+// of every bracket in one batch; a bracket with sigma'(a) < 0 < sigma'(b) goes to
+// Newton from the secant zero of sigma'; one whose ends both rise (fall) is moved one
+// width to the left (right), at most max_shift times; brackets that hold a maximum are
+// dropped.  Newton rounds run in lock step (one batched sigma', sigma'' evaluation per
+// round); roots closer than tol to an earlier one are merged.
+int hbem_refine_brackets(hbem_solop s, const double* a_host, const double* b_host, int ncand, double c_o, double c_i,
+                         double tol, int max_shift, double* roots_host, int max_roots, int* nroots, int* n_evals) {
+    if (!s || ncand < 0 || (ncand > 0 && (!a_host || !b_host)) || !(tol > 0.) || max_shift < 0 || !nroots)
+        return HBEM_ERR_INVALID;
+    struct Br { double a, b, da, db; };
+    std::vector<Br> live, valid;
+    for (int c = 0; c < ncand; ++c)
+        if (b_host[c] > a_host[c]) live.push_back(Br{a_host[c], b_host[c], 0., 0.});
+    int evals = 0;
+    for (int round = 0; round <= max_shift && !live.empty(); ++round) {
+        std::vector<double> ends(2 * live.size()), der(6 * live.size());
+        for (size_t c = 0; c < live.size(); ++c) {
+            ends[2 * c] = live[c].a;
+            ends[2 * c + 1] = live[c].b;
+        }
+        if (int r = hbem_sweep_sigma(s, ends.data(), (int)ends.size(), c_o, c_i, 1, der.data())) return r;
+        evals += (int)ends.size();
+        std::vector<Br> next;
+        for (size_t c = 0; c < live.size(); ++c) {
+            Br br = live[c];
+            br.da = der[6 * c + 1];
+            br.db = der[6 * c + 4];
+            const double w = br.b - br.a;
+            if (br.da < 0. && br.db > 0.) valid.push_back(br);
+            else if (br.da >= 0. && br.db > 0.) next.push_back(Br{br.a - w, br.a, 0., 0.});
+            else if (br.da < 0. && br.db <= 0.) next.push_back(Br{br.b, br.b + w, 0., 0.});
+        }
+        live.swap(next);
+    }
+    std::vector<Newton> nt(valid.size());
+    for (size_t c = 0; c < valid.size(); ++c) {
+        const Br& br = valid[c];
+        const double guess = br.a - br.da * (br.b - br.a) / (br.db - br.da);
+        nt[c].start(br.a, br.b, guess, tol);
+    }
+    for (int round = 0; round < kMaxIt; ++round) {
+        std::vector<double> xs;
+        std::vector<size_t> who;
+        for (size_t c = 0; c < nt.size(); ++c)
+            if (!nt[c].done) { xs.push_back(nt[c].rts); who.push_back(c); }
+        if (xs.empty()) break;
+        std::vector<double> out(3 * xs.size());
+        if (int r = hbem_sweep_sigma(s, xs.data(), (int)xs.size(), c_o, c_i, 2, out.data())) return r;
+        evals += (int)xs.size();
+        for (size_t q = 0; q < who.size(); ++q) nt[who[q]].feed(out[3 * q + 1], out[3 * q + 2]);
+    }
+    std::vector<double> roots;
+    for (auto& x : nt)
+        if (x.done && x.found && x.rts == x.rts) {
+            bool dup = false;
+            for (double r : roots) dup |= std::fabs(r - x.rts) <= tol;
+            if (!dup) roots.push_back(x.rts);
+        }
+    std::sort(roots.begin(), roots.end());
+    *nroots = (int)roots.size();
+    for (size_t i = 0; i < roots.size() && (int)i < max_roots; ++i)
+        if (roots_host) roots_host[i] = roots[i];
+    if (n_evals) *n_evals = evals;
+    return HBEM_OK;
+}
+
 int hbem_opt_subdiv(hbem_fn_batch f, void* user, double x_min, double x_max, int batch_size, int limit, double tol,
                     unsigned long long seed, double* x_out, double* y_out, int max_points, int* n_points,
                     int* minima_out, int max_minima, int* n_minima) {

@@ -193,6 +193,15 @@ int hbem_tp_field_grid(hbem_solop s, const double* waves, int nwaves, double k_r
  * of the grid kernel, (grid point, boundary node) pairs it summed, near pairs.     */
 void hbem_field_stats(double* grid_kernel_ms, long long* point_node_pairs, long long* near_pairs);
 
+/* Local minima of sigma_min from candidate brackets [a_i, b_i] (the confirmation step
+ * of the learned proposal; the Newton phase of hbem_find_resonances_plain): brackets
+ * with sigma'(a) < 0 < sigma'(b) go to safeguarded Newton on sigma' (rtsafe, from the
+ * secant zero of sigma'); brackets whose ends both rise or both fall are moved one
+ * width left or right, at most max_shift times.  Roots ascending, merged within tol;
+ * *n_evals counts the sigma evaluations.                                           */
+int hbem_refine_brackets(hbem_solop s, const double* a_host, const double* b_host, int ncand, double c_o, double c_i,
+                         double tol, int max_shift, double* roots_host, int max_roots, int* nroots, int* n_evals);
+
 /* ------------------------------------------------------------------ learned proposal network */
 
 /* The multilayer perceptron of the learned resonance proposal (no counterpart in the

@@ -31,7 +31,7 @@ EXPORTS = [
     "hbem_incoming_load", "hbem_incoming_eval", "hbem_tp_solve", "hbem_tp_field_grid", "hbem_field_stats",
     "hbem_mlp_create", "hbem_mlp_destroy", "hbem_mlp_num_params", "hbem_mlp_get_params", "hbem_mlp_set_params",
     "hbem_mlp_forward", "hbem_mlp_gradients", "hbem_mlp_train_step", "hbem_bf16_gemm_device",
-    "hbem_refine_brackets",
+    "hbem_refine_brackets", "hbem_sweep_sigma_multi", "hbem_find_resonances_plain_multi", "hbem_refine_brackets_multi",
     "hbem_find_resonances_plain", "hbem_rtsafe", "hbem_zbrent", "hbem_brent_min",
 ]
 
@@ -114,6 +114,9 @@ def load(path=LIB_PATH):
         "hbem_tp_field_grid": (_i, [_vp, _dp, _i, _d, _d, _d, _d, _u, _d, _d, _d, _d, _i, _i, _i, _dp, _dp, _dp,
                                     _dp]),
         "hbem_field_stats": (None, [_dp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
+        "hbem_sweep_sigma_multi": (_i, [_vp, _i, _ip, _dp, _dp, _d, _u, _dp]),
+        "hbem_find_resonances_plain_multi": (_i, [_vp, _i, _dp, _dp, _i, _d, _dp, _d, _dp, _i, _ip, _ip]),
+        "hbem_refine_brackets_multi": (_i, [_vp, _i, _ip, _dp, _dp, _d, _dp, _d, _i, _dp, _i, _ip, _ip]),
         "hbem_refine_brackets": (_i, [_vp, _dp, _dp, _i, _d, _d, _d, _i, _dp, _i, _ip, _ip]),
         "hbem_mlp_create": (_i, [_i, _i, _i, _i, ctypes.c_ulonglong, ctypes.POINTER(_vp)]),
         "hbem_mlp_destroy": (_i, [_vp]),

@@ -347,6 +347,58 @@ def tp_field_grid(solop, waves, k, c_o, c_i, order_green, lower_left, upper_righ
     return S.T.copy(), gx.T.copy(), gy.T.copy()
 
 
+# ---------------------------------------------------------------- many scatterers at once
+
+def _ops(ops):
+    return (ctypes.c_void_p * len(ops))(*[o._h.value for o in ops])
+
+
+def sweep_sigma_multi(ops, ks, c_o, c_i, d=0):
+    """sigma (and derivatives up to d) of operator i at the wavenumbers ks[i] with inner
+    index c_i[i], all scatterers in flight together: list of (len(ks[i]), 3) arrays."""
+    counts = np.array([len(k) for k in ks], np.int32)
+    flat = np.ascontiguousarray(np.concatenate([np.asarray(k, np.float64) for k in ks]))
+    ci = np.ascontiguousarray(c_i, np.float64)
+    out = np.zeros((flat.size, 3))
+    check(C.lib().hbem_sweep_sigma_multi(_ops(ops), len(ops), iptr(counts), dptr(flat), dptr(ci), float(c_o), int(d),
+                                         dptr(out)))
+    return np.split(out, np.cumsum(counts)[:-1])
+
+
+def _split_roots(roots, counts):
+    return np.split(roots[:int(np.sum(counts))].copy(), np.cumsum(counts)[:-1])
+
+
+def find_resonances_plain_multi(ops, k_min, k_max, npoints, c_o, c_i, tol=1e-8, max_roots=65536):
+    """The plain search on window [k_min[i], k_max[i]] of operator i, all in lock step:
+    (list of root arrays, sigma evaluations)."""
+    n = len(ops)
+    roots = np.zeros(max_roots)
+    counts = np.zeros(n, np.int32)
+    ne = ctypes.c_int()
+    check(C.lib().hbem_find_resonances_plain_multi(_ops(ops), n, dptr(np.ascontiguousarray(k_min, np.float64)),
+                                                   dptr(np.ascontiguousarray(k_max, np.float64)), int(npoints),
+                                                   float(c_o), dptr(np.ascontiguousarray(c_i, np.float64)),
+                                                   float(tol), dptr(roots), max_roots, iptr(counts), ctypes.byref(ne)))
+    return _split_roots(roots, counts), ne.value
+
+
+def refine_brackets_multi(ops, a, b, c_o, c_i, tol=1e-8, max_shift=3, max_roots=65536):
+    """hbem_refine_brackets for every operator in lock step: brackets a[i], b[i] of
+    operator i: (list of root arrays, sigma evaluations)."""
+    n = len(ops)
+    counts = np.array([len(x) for x in a], np.int32)
+    af = np.ascontiguousarray(np.concatenate([np.asarray(x, np.float64) for x in a]) if n else np.zeros(0))
+    bf = np.ascontiguousarray(np.concatenate([np.asarray(x, np.float64) for x in b]) if n else np.zeros(0))
+    roots = np.zeros(max_roots)
+    rc = np.zeros(n, np.int32)
+    ne = ctypes.c_int()
+    check(C.lib().hbem_refine_brackets_multi(_ops(ops), n, iptr(counts), dptr(af), dptr(bf), float(c_o),
+                                             dptr(np.ascontiguousarray(c_i, np.float64)), float(tol), int(max_shift),
+                                             dptr(roots), max_roots, iptr(rc), ctypes.byref(ne)))
+    return _split_roots(roots, rc), ne.value
+
+
 # ---------------------------------------------------------------- proposal network
 
 class MLP:

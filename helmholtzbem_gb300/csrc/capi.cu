@@ -970,6 +970,83 @@ int hbem_sweep_sigma(hbem_solop s, const double* k_host, int nk, double c_o, dou
     return HBEM_OK;
 }
 
+// Many scatterers at once: every operator's T(k) batch and dense-SVD launch are
+// enqueued on its own stream before any is waited for, so the small per-scatterer
+// launches (one CTA per matrix in the SVD) run side by side on the GPU.
+int hbem_sweep_sigma_multi(const hbem_solop* ops, int nops, const int* counts, const double* k_host,
+                           const double* c_i_host, double c_o, unsigned d, double* out_host) {
+    if (!ops || nops < 1 || !counts || !k_host || !c_i_host || !out_host || d > 2)
+        return fail(HBEM_ERR_INVALID, "sweep_sigma_multi: bad argument");
+    size_t total = 0;
+    bool fast = g_svd_fast != 0;
+    for (int i = 0; i < nops; ++i) {
+        if (!ops[i] || counts[i] < 0) return fail(HBEM_ERR_INVALID, "sweep_sigma_multi: bad argument");
+        total += (size_t)counts[i];
+        fast &= svd_fast_smem_bytes(2 * ops[i]->b->n) <= 220 * 1024;
+    }
+    if (!fast) {   // orders the fast kernel does not take: one operator after the other
+        size_t off = 0;
+        for (int i = 0; i < nops; ++i) {
+            if (counts[i] > 0)
+                if (int r = hbem_sweep_sigma(ops[i], k_host + off, counts[i], c_o, c_i_host[i], d, out_host + 3 * off))
+                    return r;
+            off += (size_t)counts[i];
+        }
+        return HBEM_OK;
+    }
+    static thread_local double* pin = nullptr;
+    static thread_local size_t pin_cap = 0;
+    const size_t need = total * 3 * sizeof(double) + total * sizeof(int);
+    if (need > pin_cap) {
+        if (pin) cudaFreeHost(pin);
+        pin = nullptr;
+        pin_cap = 0;
+        HB_CK(cudaMallocHost(&pin, need));
+        pin_cap = need;
+    }
+    int* pstat = reinterpret_cast<int*>(pin + total * 3);
+    size_t off = 0;
+    for (int i = 0; i < nops; ++i) {
+        hbem_solop s = ops[i];
+        const int kn = counts[i];
+        if (kn > 0) {
+            hbem_builder b = s->b;
+            HB_CK(cudaSetDevice(b->device));
+            const int n = 2 * b->n;
+            const size_t mat = (size_t)n * n;
+            HB_CK(s->d_T.ensure((size_t)kn * (d + 1) * mat * sizeof(cplx)));
+            HB_CK(s->d_out.ensure((size_t)kn * 3 * sizeof(double)));
+            HB_CK(s->d_status.ensure((size_t)kn * sizeof(int)));
+            if (int r = gen_T_batch(s, k_host + off, nullptr, kn, c_o, c_i_host[i], d, s->d_T.as<cplx>())) return r;
+            HB_CK(launch_svd_fast(n, kn, (int)d, s->d_T.as<cplx>(), (long long)(d + 1) * mat, (long long)mat,
+                                  s->d_out.as<double>(), s->d_status.as<int>(), b->st));
+            g_launches += 1;
+            HB_CK(cudaMemcpyAsync(pin + 3 * off, s->d_out.p, (size_t)kn * 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                                  b->st));
+            HB_CK(cudaMemcpyAsync(pstat + off, s->d_status.p, (size_t)kn * sizeof(int), cudaMemcpyDeviceToHost, b->st));
+        }
+        off += (size_t)kn;
+    }
+    for (int i = 0; i < nops; ++i)
+        if (counts[i] > 0) HB_CK(cudaStreamSynchronize(ops[i]->b->st));
+    std::copy(pin, pin + total * 3, out_host);
+    // matrices the fast kernel could not finish: redone by the polished kernel
+    off = 0;
+    for (int i = 0; i < nops; ++i) {
+        bool redo = false;
+        for (int q = 0; q < counts[i]; ++q) redo |= pstat[off + q] != 0;
+        if (redo) {
+            const int save = g_svd_fast;
+            g_svd_fast = 0;
+            const int r = hbem_sweep_sigma(ops[i], k_host + off, counts[i], c_o, c_i_host[i], d, out_host + 3 * off);
+            g_svd_fast = save;
+            if (r) return r;
+        }
+        off += (size_t)counts[i];
+    }
+    return HBEM_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------- accessors for other translation units

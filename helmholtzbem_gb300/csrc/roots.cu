@@ -568,6 +568,184 @@ int hbem_refine_brackets(hbem_solop s, const double* a_host, const double* b_hos
     return HBEM_OK;
 }
 
+// ---------------------------------------------------------------- many scatterers in lock step
+//
+// The plain search and the bracket refinement above, run for many (scatterer,
+// k-window) pairs at once: every phase (grid, bracket ends, each Newton round) is one
+// hbem_sweep_sigma_multi call over all pairs, so the per-scatterer launches overlap.
+
+namespace {
+
+struct MultiSigma {
+    const hbem_solop* ops;
+    int nops;
+    double c_o;
+    const double* c_i;
+    int evals = 0;
+    // ks[i]: the points of operator i; out[i]: 3 values per point
+    int operator()(const std::vector<std::vector<double>>& ks, unsigned d, std::vector<std::vector<double>>& out) {
+        std::vector<int> counts(nops);
+        std::vector<double> flat;
+        for (int i = 0; i < nops; ++i) {
+            counts[i] = (int)ks[i].size();
+            flat.insert(flat.end(), ks[i].begin(), ks[i].end());
+        }
+        out.assign(nops, {});
+        if (flat.empty()) return HBEM_OK;
+        std::vector<double> res(3 * flat.size());
+        if (int r = hbem_sweep_sigma_multi(ops, nops, counts.data(), flat.data(), c_i, c_o, d, res.data())) return r;
+        evals += (int)flat.size();
+        size_t off = 0;
+        for (int i = 0; i < nops; ++i) {
+            out[i].assign(res.begin() + 3 * off, res.begin() + 3 * (off + counts[i]));
+            off += counts[i];
+        }
+        return HBEM_OK;
+    }
+};
+
+struct Job1 {
+    int op;
+    Newton nt;
+};
+
+// lock-step Newton over all (operator, candidate) states
+int newton_multi(MultiSigma& ev, std::vector<Job1>& jobs) {
+    for (int round = 0; round < kMaxIt; ++round) {
+        std::vector<std::vector<double>> xs(ev.nops);
+        std::vector<std::vector<size_t>> who(ev.nops);
+        bool any = false;
+        for (size_t c = 0; c < jobs.size(); ++c)
+            if (!jobs[c].nt.done) {
+                xs[jobs[c].op].push_back(jobs[c].nt.rts);
+                who[jobs[c].op].push_back(c);
+                any = true;
+            }
+        if (!any) break;
+        std::vector<std::vector<double>> out;
+        if (int r = ev(xs, 2, out)) return r;
+        for (int i = 0; i < ev.nops; ++i)
+            for (size_t q = 0; q < who[i].size(); ++q) jobs[who[i][q]].nt.feed(out[i][3 * q + 1], out[i][3 * q + 2]);
+    }
+    return HBEM_OK;
+}
+
+int collect_roots(int nops, const std::vector<Job1>& jobs, double tol, double* roots_host, int max_roots,
+                  int* root_counts) {
+    int total = 0;
+    for (int i = 0; i < nops; ++i) {
+        std::vector<double> r;
+        for (const auto& j : jobs)
+            if (j.op == i && j.nt.done && j.nt.found && j.nt.rts == j.nt.rts) {
+                bool dup = false;
+                for (double x : r) dup |= std::fabs(x - j.nt.rts) <= tol;
+                if (!dup) r.push_back(j.nt.rts);
+            }
+        std::sort(r.begin(), r.end());
+        if (root_counts) root_counts[i] = (int)r.size();
+        for (double x : r) {
+            if (roots_host && total < max_roots) roots_host[total] = x;
+            ++total;
+        }
+    }
+    return total;
+}
+
+}  // namespace
+
+int hbem_find_resonances_plain_multi(const hbem_solop* ops, int nops, const double* k_min, const double* k_max,
+                                     int npoints, double c_o, const double* c_i, double tol, double* roots_host,
+                                     int max_roots, int* root_counts, int* n_evals) {
+    if (!ops || nops < 1 || !k_min || !k_max || !c_i || npoints < 3 || !(tol > 0.)) return HBEM_ERR_INVALID;
+    MultiSigma ev{ops, nops, c_o, c_i};
+    std::vector<std::vector<double>> grid(nops), g;
+    std::vector<double> h(nops);
+    for (int i = 0; i < nops; ++i) {
+        if (!(k_max[i] > k_min[i])) return HBEM_ERR_INVALID;
+        h[i] = (k_max[i] - k_min[i]) / (npoints - 1);
+        for (int j = 0; j < npoints; ++j) grid[i].push_back(k_min[i] + j * h[i]);
+    }
+    if (int r = ev(grid, 0, g)) return r;
+    // 3-point minima, then sigma' at both bracket ends of all of them
+    std::vector<std::vector<int>> cidx(nops);
+    std::vector<std::vector<double>> ends(nops), der;
+    for (int i = 0; i < nops; ++i)
+        for (int j = 0; j + 2 < npoints; ++j) {
+            const double L = g[i][3 * j], Cc = g[i][3 * (j + 1)], R = g[i][3 * (j + 2)];
+            if (L - Cc > 0. && R - Cc > 0.) {
+                cidx[i].push_back(j);
+                ends[i].push_back(grid[i][j]);
+                ends[i].push_back(grid[i][j + 2]);
+            }
+        }
+    if (int r = ev(ends, 1, der)) return r;
+    std::vector<Job1> jobs;
+    for (int i = 0; i < nops; ++i)
+        for (size_t c = 0; c < cidx[i].size(); ++c) {
+            const int j = cidx[i][c];
+            const double d1 = der[i][3 * (2 * c) + 1], d2 = der[i][3 * (2 * c + 1) + 1];
+            if (!(d1 < 0. && d2 > 0.)) continue;
+            Job1 jb;
+            jb.op = i;
+            jb.nt.start(grid[i][j], grid[i][j] + 2 * h[i],
+                        quartic_guess(grid[i][j], h[i], g[i][3 * j], g[i][3 * (j + 1)], g[i][3 * (j + 2)], d1, d2, tol),
+                        tol);
+            jobs.push_back(jb);
+        }
+    if (int r = newton_multi(ev, jobs)) return r;
+    collect_roots(nops, jobs, 0., roots_host, max_roots, root_counts);
+    if (n_evals) *n_evals = ev.evals;
+    return HBEM_OK;
+}
+
+int hbem_refine_brackets_multi(const hbem_solop* ops, int nops, const int* counts, const double* a_host,
+                               const double* b_host, double c_o, const double* c_i, double tol, int max_shift,
+                               double* roots_host, int max_roots, int* root_counts, int* n_evals) {
+    if (!ops || nops < 1 || !counts || !c_i || !(tol > 0.) || max_shift < 0) return HBEM_ERR_INVALID;
+    MultiSigma ev{ops, nops, c_o, c_i};
+    struct Br { int op; double a, b, da, db; };
+    std::vector<Br> live, valid;
+    size_t off = 0;
+    for (int i = 0; i < nops; ++i) {
+        for (int c = 0; c < counts[i]; ++c)
+            if (b_host[off + c] > a_host[off + c]) live.push_back(Br{i, a_host[off + c], b_host[off + c], 0., 0.});
+        off += (size_t)counts[i];
+    }
+    for (int round = 0; round <= max_shift && !live.empty(); ++round) {
+        std::vector<std::vector<double>> ends(nops), der;
+        std::vector<std::vector<size_t>> who(nops);
+        for (size_t c = 0; c < live.size(); ++c) {
+            ends[live[c].op].push_back(live[c].a);
+            ends[live[c].op].push_back(live[c].b);
+            who[live[c].op].push_back(c);
+        }
+        if (int r = ev(ends, 1, der)) return r;
+        std::vector<Br> next;
+        for (int i = 0; i < nops; ++i)
+            for (size_t q = 0; q < who[i].size(); ++q) {
+                Br br = live[who[i][q]];
+                br.da = der[i][6 * q + 1];
+                br.db = der[i][6 * q + 4];
+                const double w = br.b - br.a;
+                if (br.da < 0. && br.db > 0.) valid.push_back(br);
+                else if (br.da >= 0. && br.db > 0.) next.push_back(Br{br.op, br.a - w, br.a, 0., 0.});
+                else if (br.da < 0. && br.db <= 0.) next.push_back(Br{br.op, br.b, br.b + w, 0., 0.});
+            }
+        live.swap(next);
+    }
+    std::vector<Job1> jobs;
+    for (const Br& br : valid) {
+        Job1 jb;
+        jb.op = br.op;
+        jb.nt.start(br.a, br.b, br.a - br.da * (br.b - br.a) / (br.db - br.da), tol);
+        jobs.push_back(jb);
+    }
+    if (int r = newton_multi(ev, jobs)) return r;
+    collect_roots(nops, jobs, tol, roots_host, max_roots, root_counts);
+    if (n_evals) *n_evals = ev.evals;
+    return HBEM_OK;
+}
+
 int hbem_opt_subdiv(hbem_fn_batch f, void* user, double x_min, double x_max, int batch_size, int limit, double tol,
                     unsigned long long seed, double* x_out, double* y_out, int max_points, int* n_points,
                     int* minima_out, int max_minima, int* n_minima) {

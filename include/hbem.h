@@ -202,6 +202,23 @@ void hbem_field_stats(double* grid_kernel_ms, long long* point_node_pairs, long 
 int hbem_refine_brackets(hbem_solop s, const double* a_host, const double* b_host, int ncand, double c_o, double c_i,
                          double tol, int max_shift, double* roots_host, int max_roots, int* nroots, int* n_evals);
 
+/* Many scatterers at once (no counterpart in the reference, whose drivers loop over
+ * scatterers): hbem_sweep_sigma for operator i at counts[i] consecutive wavenumbers of
+ * k_host with inner index c_i_host[i]; each operator's T(k) batch and dense SVD are
+ * enqueued on its own stream before any is awaited.  out_host: 3 values per point. */
+int hbem_sweep_sigma_multi(const hbem_solop* ops, int nops, const int* counts, const double* k_host,
+                           const double* c_i_host, double c_o, unsigned d, double* out_host);
+/* hbem_find_resonances_plain and hbem_refine_brackets for nops (operator, window)
+ * pairs in lock step: every phase is one hbem_sweep_sigma_multi call.  Roots are
+ * concatenated in operator order, root_counts[i] of them for operator i; brackets of
+ * operator i are the counts[i] consecutive entries of a_host, b_host.             */
+int hbem_find_resonances_plain_multi(const hbem_solop* ops, int nops, const double* k_min, const double* k_max,
+                                     int npoints, double c_o, const double* c_i, double tol, double* roots_host,
+                                     int max_roots, int* root_counts, int* n_evals);
+int hbem_refine_brackets_multi(const hbem_solop* ops, int nops, const int* counts, const double* a_host,
+                               const double* b_host, double c_o, const double* c_i, double tol, int max_shift,
+                               double* roots_host, int max_roots, int* root_counts, int* n_evals);
+
 /* ------------------------------------------------------------------ learned proposal network */
 
 /* The multilayer perceptron of the learned resonance proposal (no counterpart in the

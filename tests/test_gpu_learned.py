@@ -29,6 +29,20 @@ def test_small_training_run_and_evaluation():
     assert np.all(np.isfinite(Y)) and Y.min() < -1.0
     net, losses = L.train(X, Y, epochs=40, batch=64, lr=1e-3, seed=1)
     assert np.mean(losses[-4:]) < np.mean(losses[:4]) / 5
-    res = L.evaluate(net, list(range(20000, 20004)), plain_points=105)
-    assert res["windows"] == 4 and 0.0 <= (res["recall"] or 0.0) <= 1.0
-    assert res["learned_evals"] > 0 and res["plain_evals"] > 0
+    res = L.evaluate(net, list(range(20000, 20004)), plain_points=105, coarse_points=25)
+    assert res["windows"] == 4
+    # the batched plain search is the same search: the same roots
+    assert res["plain_batched"]["roots"] == res["plain"]["roots"] and res["plain_batched"]["recall"] == 1.0
+    for m in ("learned_batched", "coarse_batched", "learned_coarse_batched"):
+        assert 0.0 <= res[m]["recall"] <= 1.0 and res[m]["evals"] > 0
+
+
+def test_sweep_sigma_multi_matches_single_operator_sweeps():
+    cases = [L.draw(s) for s in (20010, 20011, 20012)]
+    ops = [L.operator(a, b) for (a, b, _, _) in cases]
+    ks = [L.window(c[3])[::16] for c in cases]
+    ci = [c[2] for c in cases]
+    multi = api.sweep_sigma_multi(ops, ks, 1.0, ci, d=2)
+    for so, k, c, m in zip(ops, ks, ci, multi):
+        single = so.sweep_sigma(k, 1.0, c, d=2)
+        assert np.array_equal(single, m)

@@ -26,7 +26,8 @@ def test_features_layout():
     x = L.features(a, b, c, k0)
     assert x.shape == (34,) and x.dtype == np.float32
     assert np.allclose(x[:8], 20 * a) and np.all(x[8:16] == 0) and np.allclose(x[16:24], 20 * b)
-    assert np.isclose(x[32], c / 25) and np.isclose(x[33], k0 / 10)
+    assert np.isclose(x[32], np.sqrt(c) / 5) and np.isclose(x[33], k0 * np.sqrt(c) * 0.25 / 12.5)
+    assert L.draw(7, 2)[2] == c and L.draw(7, 2)[3] != k0 and L.draw(7, 0)[3] == k0
 
 
 def test_mesh_is_scaled_and_closed():

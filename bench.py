@@ -595,6 +595,42 @@ def field_cpu(sample):
             "max_rel_diff_gpu_vs_oracle": float(np.max(np.abs(sample["gpu"] - ref)) / np.max(np.abs(ref)))}
 
 
+def learned_vs_plain(torch, api, windows=40):
+    """The learned proposal (network shipped with the package) against the plain search
+    on held-out scatterer windows (seeds 20000..), every root confirmed by Newton on
+    sigma'; and the same network on the benchmark circle, windows of width 2 from 0.5."""
+    from helmholtzbem_gb300 import learned as L
+    net = L.default_network()
+    res = L.evaluate(net, list(range(20000, 20000 + windows)))
+    # the bench circle (arcs; the network was trained on line panels of the same family)
+    so = api.SolutionsOperator(api.BuilderData(geometry_circle(), order=CFG["order"]))
+    plain, _, _ = so.find_resonances_plain(CFG["k_min"], CFG["k_max"], CFG["npoints"], CFG["c_o"], CFG["c_i"],
+                                           tol=CFG["tol"])
+    k0s = np.arange(CFG["k_min"], CFG["k_max"], L.FAMILY["width"])
+    cases = [(np.zeros(8), np.zeros(8), CFG["c_i"], float(k)) for k in k0s]
+    mins, _ = L.propose(net, cases)
+    h = L.FAMILY["width"] / (L.FAMILY["npts"] - 1)
+    lo = np.concatenate([L.window(c[3])[m] - 2 * h for c, m in zip(cases, mins)])
+    hi = np.concatenate([L.window(c[3])[m] + 2 * h for c, m in zip(cases, mins)])
+    keep = (lo < CFG["k_max"]) & (hi > CFG["k_min"])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    roots, ev = so.refine_brackets(lo[keep], hi[keep], CFG["c_o"], CFG["c_i"], tol=CFG["tol"])
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    hit = int(sum(np.min(np.abs(roots - p)) <= 1e-6 for p in plain)) if roots.size else 0
+    res["bench_circle"] = {"plain_roots": int(plain.size), "learned_roots": int(roots.size), "found_plain_roots": hit,
+                           "learned_seconds": t, "learned_evals": ev}
+    res["workload"] = ("held-out Fourier scatterers (scale 0.25, N=50 lines, c_i ~ U[2,25]), one width-2 window "
+                       "each; plain = 210-point grid + Newton per window")
+    return res
+
+
+def geometry_circle():
+    from helmholtzbem_gb300 import geometry
+    return geometry.circle(CFG["radius"], CFG["N"])
+
+
 def arnoldi_cpu(mats):
     """The reference's arnoldi::sv call (ARPACK on [0 T^-H; T^-1 0] through one LU)
     made through scipy's ARPACK on the host: ms per matrix and the largest relative
@@ -733,6 +769,7 @@ def run_gpu(args):
     adapt = adaptive_search(torch, so, step(so)[1])
     arnoldi, arn_mats = arnoldi_at_scale(torch, C, api, geometry, lib)
     field, field_sample = field_at_scale(torch, C, api, geometry, lib, peak)
+    learned = learned_vs_plain(torch, api)
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
@@ -770,6 +807,7 @@ def run_gpu(args):
             "adaptive_search": adapt,
             "arnoldi_at_scale": arnoldi,
             "field_at_scale": field,
+            "learned_vs_plain": learned,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
         }

@@ -201,15 +201,25 @@ def evaluate(net, seeds, plain_points=210, coarse_points=43, tol=1e-8, match=1e-
 
 
 def save(net, path):
-    np.savez_compressed(path, params=net.get_params(), dims=np.array(net.dims))
+    """Parameters stored in float16 (the products run in bfloat16 anyway)."""
+    np.savez_compressed(path, params=net.get_params().astype(np.float16), dims=np.array(net.dims))
 
 
 def load(path):
     d = np.load(path)
     dims = [int(v) for v in d["dims"]]
     net = api.MLP(dims[0], dims[1], len(dims) - 2, dims[-1])
-    net.set_params(d["params"])
+    net.set_params(d["params"].astype(np.float32))
     return net
+
+
+def default_network():
+    """The network shipped with the package: trained by
+    `python -m helmholtzbem_gb300.learned --train 4000 --test 200 --epochs 300`
+    (16,000 windows of scatterers 10000..13999, 300 epochs, batch 256, Adam 1e-3 with
+    cosine decay)."""
+    import os
+    return load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "proposal_mlp.npz"))
 
 
 if __name__ == "__main__":

@@ -33,6 +33,8 @@ EXPORTS = [
     "hbem_mlp_forward", "hbem_mlp_gradients", "hbem_mlp_train_step", "hbem_bf16_gemm_device",
     "hbem_refine_brackets", "hbem_sweep_sigma_multi", "hbem_find_resonances_plain_multi", "hbem_refine_brackets_multi",
     "hbem_find_resonances_plain", "hbem_rtsafe", "hbem_zbrent", "hbem_brent_min",
+    "hbem_brent_rc_create", "hbem_brent_rc_step", "hbem_brent_rc_destroy", "hbem_brent_guess", "hbem_brent_gsl",
+    "hbem_brent_gsl_with_values",
 ]
 
 _lib = None
@@ -146,6 +148,12 @@ def load(path=LIB_PATH):
         "hbem_rtsafe": (_d, [FN, FN_BOTH, _vp, _d, _d, _d, _ip, _up]),
         "hbem_zbrent": (_d, [FN, _vp, _d, _d, _d, _ip, _up]),
         "hbem_brent_min": (_d, [FN, _vp, _d, _d, _d]),
+        "hbem_brent_rc_create": (_i, [_d, _d, _d, ctypes.POINTER(_vp)]),
+        "hbem_brent_rc_step": (_d, [_vp, _ip, _d]),
+        "hbem_brent_rc_destroy": (_i, [_vp]),
+        "hbem_brent_guess": (_d, [FN, _vp, _d, _d, _d, _d, _d, _up]),
+        "hbem_brent_gsl": (_d, [FN, _vp, _d, _d, _d, _d, _up]),
+        "hbem_brent_gsl_with_values": (_d, [FN, _vp, _d, _d, _d, _d, _d, _d, _d, _up]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -215,6 +215,43 @@ def brent_min(f, a, b, tol):
     return C.lib().hbem_brent_min(cb, None, float(a), float(b), float(tol))
 
 
+class BrentMinimizer:
+    """BrentMinimizer(a, b, tol).local_min_rc(status, value) with reverse
+    communication (include/find_roots.hpp:181-233): returns (arg, status)."""
+
+    def __init__(self, a, b, tol):
+        if not a < b:
+            raise RuntimeError("a < b is required for Brent algorithm!")
+        h = ctypes.c_void_p()
+        check(C.lib().hbem_brent_rc_create(float(a), float(b), float(tol), ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and C._lib is not None:
+            C._lib.hbem_brent_rc_destroy(self._h)
+            self._h = None
+
+    def local_min_rc(self, status, value=0.0):
+        st = ctypes.c_int(int(status))
+        arg = C.lib().hbem_brent_rc_step(self._h, ctypes.byref(st), float(value))
+        return arg, st.value
+
+
+def brent_guess(a, b, guess, fguess, f, tol):
+    cb = C.FN(lambda x, u: float(f(x)))
+    ic = ctypes.c_uint()
+    r = C.lib().hbem_brent_guess(cb, None, float(a), float(b), float(guess), float(fguess), float(tol), ctypes.byref(ic))
+    return r, ic.value
+
+
+def brent_gsl_with_values(a, fa, b, fb, guess, fguess, f, tol):
+    cb = C.FN(lambda x, u: float(f(x)))
+    ic = ctypes.c_uint()
+    r = C.lib().hbem_brent_gsl_with_values(cb, None, float(a), float(fa), float(b), float(fb), float(guess),
+                                           float(fguess), float(tol), ctypes.byref(ic))
+    return r, ic.value
+
+
 def hankel01(z):
     """H0^(1), H1^(1) on the device; real path for a real array, complex path otherwise."""
     z = np.asarray(z)

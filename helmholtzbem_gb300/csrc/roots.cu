@@ -251,15 +251,17 @@ struct BrentState {
 // brent_guess (find_roots.cpp:1233-1313): Brent's minimisation on [a, b] started from
 // a guess with known value, tolerance max(tol, sqrt eps) |x| + 1e-10.
 template <class F>
-double brent_guess(double a, double b, double guess, double fguess, F&& f, double tol) {
+double brent_guess(double a, double b, double guess, double fguess, F&& f, double tol, unsigned* count = nullptr) {
     const double tolc = std::max(tol, std::sqrt(kEps));
     BrentState S{a, b, guess, guess, guess, fguess, fguess, fguess};
-    for (int ic = 0; ic < 100; ++ic) {
+    unsigned ic = 0;
+    for (; ic < 100; ++ic) {
         const double xm = 0.5 * (S.a + S.b), tol1 = tolc * std::fabs(S.x) + 1e-10;
         if (std::fabs(S.x - xm) <= 2. * tol1 - 0.5 * (S.b - S.a)) break;
         const double u = S.propose(tol1);
         S.update(u, f(u));
     }
+    if (count) *count = ic;
     return S.x;
 }
 
@@ -429,6 +431,105 @@ double hbem_zbrent(hbem_fn f, void* user, double x1, double x2, double tol, int*
         fb = f(b, user);
     }
     return 0.0;
+}
+
+// BrentMinimizer::local_min_rc (find_roots.cpp:1003-1184): localmin above as a
+// reverse-communication state machine; the caller evaluates f at the returned point
+// while *status > 0 (the iterates are those of hbem_brent_min).
+namespace {
+struct BrentRC {
+    double A, B, tol, eps, a = 0., b = 0., d = 0., e = 0., fu = 0., fv = 0., fw = 0., fx = 0., u = 0., v = 0., w = 0.,
+                                    x = 0.;
+};
+}  // namespace
+
+int hbem_brent_rc_create(double a, double b, double tol, void** handle) {
+    if (!handle || !(a < b) || !(tol > 0.)) return HBEM_ERR_INVALID;
+    *handle = new BrentRC{a, b, tol, std::sqrt(tol)};
+    return HBEM_OK;
+}
+
+int hbem_brent_rc_destroy(void* handle) {
+    delete static_cast<BrentRC*>(handle);
+    return HBEM_OK;
+}
+
+double hbem_brent_rc_step(void* handle, int* status, double value) {
+    BrentRC* R = static_cast<BrentRC*>(handle);
+    if (!R || !status) return NAN;
+    const double c = 0.5 * (3.0 - std::sqrt(5.0));
+    if (*status == 0) {
+        R->a = R->A;
+        R->b = R->B;
+        R->v = R->a + c * (R->b - R->a);
+        R->w = R->x = R->v;
+        R->e = R->d = 0.;
+        *status = 1;
+        return R->x;
+    }
+    if (*status == 1) {
+        R->fx = R->fv = R->fw = value;
+    } else {
+        const double u = R->u, fu = value;
+        if (fu <= R->fx) {
+            if (R->x <= u) R->a = R->x; else R->b = R->x;
+            R->v = R->w; R->fv = R->fw; R->w = R->x; R->fw = R->fx; R->x = u; R->fx = fu;
+        } else {
+            if (u < R->x) R->a = u; else R->b = u;
+            if (fu <= R->fw || R->w == R->x) { R->v = R->w; R->fv = R->fw; R->w = u; R->fw = fu; }
+            else if (fu <= R->fv || R->v == R->x || R->v == R->w) { R->v = u; R->fv = fu; }
+        }
+    }
+    const double mid = 0.5 * (R->a + R->b), tol1 = R->eps * std::fabs(R->x) + R->tol / 3.0, tol2 = 2.0 * tol1;
+    if (std::fabs(R->x - mid) <= tol2 - 0.5 * (R->b - R->a)) {
+        *status = 0;
+        return R->x;
+    }
+    bool golden = std::fabs(R->e) <= tol1;
+    if (!golden) {
+        double r = (R->x - R->w) * (R->fx - R->fv), q = (R->x - R->v) * (R->fx - R->fw),
+               p = (R->x - R->v) * q - (R->x - R->w) * r;
+        q = 2.0 * (q - r);
+        if (q > 0.0) p = -p;
+        q = std::fabs(q);
+        r = R->e;
+        R->e = R->d;
+        if (std::fabs(0.5 * q * r) <= std::fabs(p) || p <= q * (R->a - R->x) || q * (R->b - R->x) <= p) {
+            golden = true;
+        } else {
+            R->d = p / q;
+            const double uu = R->x + R->d, sg = (mid - R->x) < 0. ? -1. : 1.;
+            if ((uu - R->a) < tol2 || (R->b - uu) < tol2) R->d = tol1 * sg;
+        }
+    }
+    if (golden) {
+        R->e = (mid <= R->x) ? R->a - R->x : R->b - R->x;
+        R->d = c * R->e;
+    }
+    R->u = std::fabs(R->d) >= tol1 ? R->x + R->d : R->x + tol1 * (R->d < 0. ? -1. : 1.);
+    *status = 2;
+    return R->u;
+}
+
+double hbem_brent_guess(hbem_fn f, void* user, double a, double b, double guess, double fguess, double tol,
+                        unsigned* num_iter) {
+    if (!f || !(a < b)) return NAN;
+    return brent_guess(a, b, guess, fguess, [&](double x) { return f(x, user); }, tol, num_iter);
+}
+
+double hbem_brent_gsl_with_values(hbem_fn f, void* user, double a, double fa, double b, double fb, double guess,
+                                  double fguess, double tol, unsigned* num_iter) {
+    if (!f) return NAN;
+    BrentSearch bs;
+    bs.start(a, fa, b, fb, guess, fguess, tol);
+    while (!bs.done) bs.feed(f(bs.u, user));
+    if (num_iter) *num_iter = (unsigned)bs.it;
+    return bs.ok ? bs.S.x : NAN;
+}
+
+double hbem_brent_gsl(hbem_fn f, void* user, double a, double b, double guess, double tol, unsigned* num_iter) {
+    if (!f) return NAN;
+    return hbem_brent_gsl_with_values(f, user, a, f(a, user), b, f(b, user), guess, f(guess, user), tol, num_iter);
 }
 
 double hbem_brent_min(hbem_fn f, void* user, double a, double b, double tol) {

@@ -408,6 +408,22 @@ double hbem_rtsafe(hbem_fn f, hbem_fn_both f_both, void* user, double x1, double
                    unsigned* num_iter);
 /* zbrent (include/find_roots.hpp:51-67; source/utilities/find_roots.cpp:19-115) */
 double hbem_zbrent(hbem_fn f, void* user, double x1, double x2, double tol, int* root_found, unsigned* num_iter);
+/* BrentMinimizer(a, b, tol).local_min_rc(status, value) (include/find_roots.hpp:181-233),
+ * reverse communication: create, then call step with *status = 0 first; while the
+ * returned *status > 0 evaluate f at the returned point and pass the value back;
+ * *status = 0 returns the estimated minimiser.                                   */
+int hbem_brent_rc_create(double a, double b, double tol, void** handle);
+double hbem_brent_rc_step(void* handle, int* status, double value);
+int hbem_brent_rc_destroy(void* handle);
+/* brent_guess (find_roots.hpp:256; find_roots.cpp:1233-1313) and brent_gsl /
+ * brent_gsl_with_values (find_roots.hpp:262-265; find_roots.cpp:1426-1473: Brent's
+ * minimiser as GSL documents it, relative interval tolerance tol, 100 iterations at
+ * most); NaN when f(guess) is not below f(a) and f(b), where GSL refuses the bracket. */
+double hbem_brent_guess(hbem_fn f, void* user, double a, double b, double guess, double fguess, double tol,
+                        unsigned* num_iter);
+double hbem_brent_gsl(hbem_fn f, void* user, double a, double b, double guess, double tol, unsigned* num_iter);
+double hbem_brent_gsl_with_values(hbem_fn f, void* user, double a, double fa, double b, double fb, double guess,
+                                  double fguess, double tol, unsigned* num_iter);
 /* BrentMinimizer(a, b, tol).local_min_rc driven to completion
  * (include/find_roots.hpp:181-233; source/utilities/find_roots.cpp:1003-1184) */
 double hbem_brent_min(hbem_fn f, void* user, double a, double b, double tol);

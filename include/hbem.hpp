@@ -11,7 +11,9 @@
 //     make_N_polygonal_panels, make_polygonal_panels   include/scatterer.hpp:39-84
 //   incoming::load, compute, compute_del      include/incoming.hpp
 //   tp::direct_second_kind::solve, solve_in_rectangle   include/solvers.hpp:101-200
-//   rtsafe, zbrent, BrentMinimizer            include/find_roots.hpp:37-67,181-233
+//   rtsafe, zbrent, BrentMinimizer, brent_guess, brent_gsl(_with_values), opt_subdiv
+//                                             include/find_roots.hpp:37-67,181-289
+//   randomized_svd::sv, sv_der, sv_der2, randGaussian, timers   include/randsvd.hpp:23-77
 //
 // Matrices: hbem::MatrixXcd / MatrixXd (column-major, data()/rows()/cols()/
 // resize()/operator()), or Eigen's types when HBEM_USE_EIGEN is defined before
@@ -19,6 +21,8 @@
 // reference; status codes stay inside.
 #pragma once
 
+#include <algorithm>
+#include <chrono>
 #include <complex>
 #include <functional>
 #include <stdexcept>
@@ -418,16 +422,124 @@ inline double zbrent(std::function<double(double)> f, double x1, double x2, doub
     return r;
 }
 
-// BrentMinimizer(a, b, tol): the reference's reverse-communication interface is
-// replaced by a callback; minimize(f) returns the estimated minimiser.
+// BrentMinimizer(a, b, tol).local_min_rc(status, value): reverse communication as in
+// the reference (status 0 to start; evaluate f at the returned point while status > 0);
+// minimize(f) runs the same iteration with a callback.
 class BrentMinimizer {
     double a_, b_, tol_;
+    void* rc_ = nullptr;
 
 public:
     BrentMinimizer(double a, double b, double tol) : a_(a), b_(b), tol_(tol) {
         if (!(a < b)) throw std::runtime_error("a < b is required for Brent algorithm!");
+        throw_if(hbem_brent_rc_create(a, b, tol, &rc_));
     }
+    BrentMinimizer(const BrentMinimizer&) = delete;
+    BrentMinimizer& operator=(const BrentMinimizer&) = delete;
+    ~BrentMinimizer() { hbem_brent_rc_destroy(rc_); }
+    double local_min_rc(int& status, double value) { return hbem_brent_rc_step(rc_, &status, value); }
     double minimize(std::function<double(double)> f) const { return hbem_brent_min(detail::call_fn, &f, a_, b_, tol_); }
 };
+
+// brent_guess, brent_gsl, brent_gsl_with_values (include/find_roots.hpp:256-265);
+// brent_gsl's progress callbacks are not supported
+inline double brent_guess(double a, double b, double guess, double fguess, const std::function<double(double)>& f,
+                          double tol, unsigned int& ic) {
+    std::function<double(double)> g = f;
+    return hbem_brent_guess(detail::call_fn, &g, a, b, guess, fguess, tol, &ic);
+}
+inline double brent_gsl(double a, double b, double guess, std::function<double(double)>& f, double tol,
+                        unsigned int& ic) {
+    return hbem_brent_gsl(detail::call_fn, &f, a, b, guess, tol, &ic);
+}
+inline double brent_gsl_with_values(double a, double fa, double b, double fb, double guess, double fguess,
+                                    std::function<double(double)>& f, double tol, unsigned int& ic) {
+    return hbem_brent_gsl_with_values(detail::call_fn, &f, a, fa, b, fb, guess, fguess, tol, &ic);
+}
+
+namespace detail {
+inline void call_batch(const double* x, int n, double* y, void* u) {
+    auto& f = *static_cast<const std::function<double(double)>*>(u);
+    for (int i = 0; i < n; ++i) y[i] = f(x[i]);
+}
+}  // namespace detail
+
+// opt_subdiv(f, x_min, x_max, batch_size, limit, tol, x, y, p) (include/find_roots.hpp:287-289);
+// the random abscissae come from a seeded generator (the reference seeds from
+// std::random_device)
+inline size_t opt_subdiv(const std::function<double(double)>& f, double x_min, double x_max, size_t batch_size,
+                         size_t limit, double tol, std::vector<double>& x, std::vector<double>& y,
+                         std::vector<size_t>& p, unsigned long long seed = 0) {
+    const int cap = 1 << 20;
+    std::vector<double> xs(cap), ys(cap);
+    std::vector<int> mins(cap);
+    int np = 0, nm = 0;
+    throw_if(hbem_opt_subdiv(detail::call_batch, const_cast<std::function<double(double)>*>(&f), x_min, x_max,
+                             (int)batch_size, (int)limit, tol, seed, xs.data(), ys.data(), cap, &np, mins.data(), cap,
+                             &nm));
+    x.assign(xs.begin(), xs.begin() + std::min(np, cap));
+    y.assign(ys.begin(), ys.begin() + std::min(np, cap));
+    p.assign(mins.begin(), mins.begin() + std::min(nm, cap));
+    return p.size();
+}
+
+// randomized_svd::sv / sv_der / sv_der2 / randGaussian (include/randsvd.hpp:23-77),
+// one matrix per call through the batched GPU path.  The reference's per-phase
+// timers (LU, QR, subspace iterations, SVD) are one fused GPU call here:
+// get_svd_time() returns the time of the whole calls, the others 0.
+namespace randomized_svd {
+namespace detail {
+inline double& timer() {
+    static double t = 0.;
+    return t;
+}
+inline bool& enabled() {
+    static bool on = false;
+    return on;
+}
+inline std::vector<double> run(const MatrixXcd* const* mats, unsigned d, const MatrixXcd& R, int q) {
+    const int n = (int)mats[0]->rows(), s = (int)R.cols();
+    std::vector<std::complex<double>> buf((size_t)(d + 1) * n * n), rb((size_t)n * s);
+    for (unsigned t = 0; t <= d; ++t)
+        for (long j = 0; j < n; ++j)
+            for (long i = 0; i < n; ++i) buf[(size_t)t * n * n + i + (size_t)j * n] = (*mats[t])(i, j);
+    for (long j = 0; j < s; ++j)
+        for (long i = 0; i < n; ++i) rb[i + (size_t)j * n] = R(i, j);
+    std::vector<double> out(d + 1);
+    const auto t0 = std::chrono::steady_clock::now();
+    throw_if(hbem_rsvd_sv_batch(n, 1, d, reinterpret_cast<const double*>(buf.data()),
+                                reinterpret_cast<const double*>(rb.data()), s, q, out.data()));
+    if (enabled()) timer() += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return out;
+}
+}  // namespace detail
+inline void benchmarking(bool yes) { detail::enabled() = yes; }
+inline void reset_timer() { detail::timer() = 0.; }
+inline double get_lu_time() { return 0.; }
+inline double get_qr_time() { return 0.; }
+inline double get_sub_iter_time() { return 0.; }
+inline double get_svd_time() { return detail::timer(); }
+inline MatrixXcd randGaussian(int nr, int nc, unsigned long long seed = 0) {
+    std::vector<std::complex<double>> r((size_t)nr * nc);
+    throw_if(hbem_rand_sketch(nr, nc, seed, reinterpret_cast<double*>(r.data())));
+    MatrixXcd R(nr, nc);
+    for (long j = 0; j < nc; ++j)
+        for (long i = 0; i < nr; ++i) R(i, j) = r[i + (size_t)j * nr];
+    return R;
+}
+inline double sv(const MatrixXcd& T, const MatrixXcd& R, int q = 0) {
+    const MatrixXcd* m[1] = {&T};
+    return detail::run(m, 0, R, q)[0];
+}
+inline std::vector<double> sv_der(const MatrixXcd& T, const MatrixXcd& T_der, const MatrixXcd& R, int q = 0) {
+    const MatrixXcd* m[2] = {&T, &T_der};
+    return detail::run(m, 1, R, q);
+}
+inline std::vector<double> sv_der2(const MatrixXcd& T, const MatrixXcd& T_der, const MatrixXcd& T_der2,
+                                   const MatrixXcd& R, int q = 0) {
+    const MatrixXcd* m[3] = {&T, &T_der, &T_der2};
+    return detail::run(m, 2, R, q);
+}
+}  // namespace randomized_svd
 
 }  // namespace hbem

@@ -56,8 +56,16 @@ int main(int argc, char** argv) {
     const double ll[2] = {-0.5, -0.5}, ur[2] = {0.5, 0.5};
     MatrixXd gX, gY;
     MatrixXcd S = tp::direct_second_kind::solve_in_rectangle(mesh, w, 7, 10, 2.5, 1.0, 4.0, ll, ur, 9, 7, gX, gY, true);
-    std::printf("%.17e %.17e %.17e %.17e %.17e %d %d %.17e %.17e %d %.17e %.17e %.17e %.17e\n", r[0], r[1], r[2],
-                std::abs(V1(3, 5)), root, (int)found, (int)threw, a0, a2(0, 0), sq_panels, sq_sigma, S(2, 5).real(),
-                S(2, 5).imag(), gY(2, 5));
+    // randomized_svd::sv on a seeded sketch, and BrentMinimizer's reverse communication as in
+    // examples/find_resonances.cpp:116-121
+    MatrixXcd R = randomized_svd::randGaussian((int)T.rows(), 12, 3);
+    const double rs = randomized_svd::sv(T, R, 2);
+    BrentMinimizer br(2.0, 4.0, 1e-8);
+    int status = 0;
+    double arg = br.local_min_rc(status, 0.);
+    while (status) arg = br.local_min_rc(status, std::cos(arg));
+    std::printf("%.17e %.17e %.17e %.17e %.17e %d %d %.17e %.17e %d %.17e %.17e %.17e %.17e %.17e %.17e\n", r[0], r[1],
+                r[2], std::abs(V1(3, 5)), root, (int)found, (int)threw, a0, a2(0, 0), sq_panels, sq_sigma,
+                S(2, 5).real(), S(2, 5).imag(), gY(2, 5), rs, arg);
     return (found && threw) ? 0 : 1;
 }

@@ -93,3 +93,32 @@ def test_rand_sketch_distribution():
     assert R.real.min() >= 0 and R.real.max() <= s and R.imag.min() >= 0 and R.imag.max() <= s
     assert abs(R.real.mean() - 0.5 * s) < 0.02 and abs(R.imag.mean() - 0.5 * s) < 0.02
     assert np.array_equal(R, api.randGaussian(400, 50, seed=11))
+
+
+def test_brent_reverse_communication_matches_callback_and_oracle():
+    """BrentMinimizer::local_min_rc driven by hand gives the iterates of the callback
+    form and of the oracle's restatement (the panel-count loop of find_resonances)."""
+    api = _api()
+    from oracle import oracle as O
+    f = lambda x: (x - 1.3) ** 2 * (1 + 0.3 * math.sin(5 * x)) + 0.1 * x
+    br = api.BrentMinimizer(0.2, 3.0, 1e-3)
+    arg, st = br.local_min_rc(0)
+    n = 0
+    while st:
+        arg, st = br.local_min_rc(st, f(arg))
+        n += 1
+    assert n > 3
+    assert arg == api.brent_min(f, 0.2, 3.0, 1e-3) == O.BrentMin(0.2, 3.0, 1e-3).minimize(f)
+
+
+def test_brent_guess_and_gsl_with_values_match_oracle():
+    api = _api()
+    from oracle import oracle as O
+    f = lambda x: math.cos(3 * x) + 0.1 * x * x
+    g, _ = api.brent_guess(0.5, 1.6, 1.0, f(1.0), f, 1e-10)
+    assert g == O.brent_guess(0.5, 1.6, 1.0, f(1.0), f, 1e-10)
+    h, it = api.brent_gsl_with_values(0.5, f(0.5), 1.6, f(1.6), 1.0, f(1.0), f, 1e-9)
+    assert h == O.brent_search(0.5, f(0.5), 1.6, f(1.6), 1.0, f(1.0), f, 1e-9) and it > 0
+    # a bracket the GSL minimiser refuses: NaN
+    r, _ = api.brent_gsl_with_values(0.5, f(0.5), 1.6, f(1.6), 0.6, f(0.6) + 10, f, 1e-9)
+    assert math.isnan(r)

@@ -49,3 +49,6 @@ def test_facade_runs_and_matches_python(tmp_path):
     S, gx, gy = api.tp_field_grid(so_u, api.wave("Plane", angle=0.5), 2.5, 1.0, 4.0, 10, (-0.5, -0.5), (0.5, 0.5),
                                   9, 7, total_field=True)
     assert abs(complex(vals[11], vals[12]) - S[2, 5]) <= 1e-12 * abs(S[2, 5]) and vals[13] == gy[2, 5]
+    # randomized sigma: an estimate from above, close on the 12-wide sketch with 2 subspace steps
+    assert ref[0] * (1 - 1e-12) <= vals[14] <= ref[0] * (1 + 1e-3)
+    assert abs(vals[15] - np.pi) < 1e-6

@@ -19,7 +19,7 @@ EXPORTS = [
     "hbem_version", "hbem_status_string", "hbem_last_error", "hbem_set_device", "hbem_set_option", "hbem_hankel01",
     "hbem_stats_enable_timing", "hbem_stats_reset", "hbem_stats_read",
     "hbem_builder_create", "hbem_builder_destroy", "hbem_builder_info", "hbem_builder_is_adjacent",
-    "hbem_assemble_dense", "hbem_get_layer", "hbem_get_layer_device",
+    "hbem_assemble_dense", "hbem_assemble_dense_sub", "hbem_get_layer", "hbem_get_layer_device",
     "hbem_solop_create", "hbem_solop_destroy", "hbem_mass_matrix", "hbem_gen_sol_op",
     "hbem_gen_sol_op_batch_device", "hbem_sv_dense_batch_device", "hbem_sv_dense_batch_noalloc",
     "hbem_sv_dense_batch", "hbem_sweep_sigma", "hbem_rand_sketch", "hbem_rsvd_sv_batch",
@@ -87,6 +87,7 @@ def load(path=LIB_PATH):
         "hbem_builder_info": (_i, [_vp, _ip, _ip, _ip, _ip, _ip]),
         "hbem_builder_is_adjacent": (_i, [_vp, _i, _i, _ip, _ip]),
         "hbem_assemble_dense": (_i, [_vp, _d, _d, _d, _u, _u]),
+        "hbem_assemble_dense_sub": (_i, [_vp, _d, _d, _d, _u, _u, _u, _u, _u, _u]),
         "hbem_get_layer": (_i, [_vp, _u, _u, _dp]),
         "hbem_get_layer_device": (_i, [_vp, _u, _u, ctypes.POINTER(_vp)]),
         "hbem_solop_create": (_i, [_vp, _i, ctypes.POINTER(_vp)]),

@@ -66,13 +66,16 @@ class GalerkinBuilder:
     def __init__(self, data: BuilderData):
         self.data = data
 
-    def assembleDense(self, k, c, layers=LayerType_ALL, d=0):
+    def assembleDense(self, k, c, layers=LayerType_ALL, d=0, row=0, col=0, rows=0, cols=0):
         k = complex(k)
-        check(C.lib().hbem_assemble_dense(self.data._h, k.real, k.imag, float(c), int(layers), int(d)))
+        n = self.data.npanels
+        self._shape = (rows or n, cols or n)
+        check(C.lib().hbem_assemble_dense_sub(self.data._h, k.real, k.imag, float(c), int(layers), int(d), int(row),
+                                              int(col), int(rows), int(cols)))
 
     def _get(self, layer, d):
         n = self.data.npanels
-        out = np.zeros((n, n), np.complex128, order="F")
+        out = np.zeros(getattr(self, "_shape", (n, n)), np.complex128, order="F")
         check(C.lib().hbem_get_layer(self.data._h, layer, int(d), out.ctypes.data_as(C._dp)))
         return out
 

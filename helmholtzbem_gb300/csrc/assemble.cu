@@ -524,6 +524,59 @@ __device__ __forceinline__ cplx layer_entry(const cplx* locj, int N, int L, int 
     return s;
 }
 
+// The same with the sub-matrix rule of GalerkinBuilder::assembleDense(k, c, layers, d,
+// row, col, rows, cols) (galerkin_builder.cpp:918-1009): only panel pairs {i, j} with
+// i in [row, row + rows) and j in [col, col + cols) (either order) contribute, in both
+// orientations, to the dof block [row, row + rows) x [col, col + cols).
+__device__ __forceinline__ bool in_sub(int i, int j, int row, int rows, int col, int cols) {
+    return (i >= row && i < row + rows && j >= col && j < col + cols) ||
+           (j >= row && j < row + rows && i >= col && i < col + cols);
+}
+
+__device__ __forceinline__ cplx layer_entry_sub(const cplx* locj, int N, int L, int t, int D1, int m, int n, int row,
+                                                int rows, int col, int cols) {
+    cplx s = mk(0.);
+    for (int a = 0; a < 2; ++a) {
+        int i = p1_panel(m, a, N);
+        for (int b = 0; b < 2; ++b) {
+            int j = p1_panel(n, b, N);
+            if (!in_sub(i, j, row, rows, col, cols)) continue;
+            const cplx* blk;
+            int e;
+            if (L == 0) {
+                if (i >= j) { blk = locj + tri_index(i, j) * D1 * kLocPerD + t * kLocPerD + 0; e = 2 * a + b; }
+                else { blk = locj + tri_index(j, i) * D1 * kLocPerD + t * kLocPerD + 4; e = 2 * a + b; }
+            } else {
+                int off = (L == 1) ? 8 : 12;
+                if (i >= j) { blk = locj + tri_index(i, j) * D1 * kLocPerD + t * kLocPerD + off; e = 2 * a + b; }
+                else { blk = locj + tri_index(j, i) * D1 * kLocPerD + t * kLocPerD + off; e = 2 * b + a; }
+            }
+            s += blk[e];
+        }
+    }
+    return s;
+}
+
+// sub-matrix layers: out[L][t] rows x cols col-major, x i/4
+__global__ void k_gather_layers_sub(int N, int D1, int layers, const cplx* loc, long long npair, int job, int row,
+                                    int rows, int col, int cols, cplx* out) {
+    long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long tot = (long long)rows * cols;
+    if (idx >= tot) return;
+    const int m = row + (int)(idx % rows), n = col + (int)(idx / rows);
+    const cplx* lj = loc + (long long)job * npair * D1 * kLocPerD;
+    int slot = 0;
+    const int lbit[3] = {1, 4, 2};   // K, W, V
+    for (int L = 0; L < 3; ++L) {
+        if (!(layers & lbit[L])) continue;
+        for (int t = 0; t < D1; ++t) {
+            cplx v = layer_entry_sub(lj, N, L, t, D1, m, n, row, rows, col, cols);
+            out[(long long)(slot * D1 + t) * tot + idx] = mk(-0.25 * v.im, 0.25 * v.re);
+        }
+        ++slot;
+    }
+}
+
 // T(k) and its derivatives for nk wavenumbers; jobs are (k, c_i), (k, c_o) interleaved.
 // T is column-major 2N x 2N per (k, t); blocks (gen_sol_op.cpp:59-74):
 //   T11 = K_i - K_o + M,  T12 = V_o - V_i,  T21 = W_o - W_i,  T22 = K_o - K_i + M^T
@@ -639,6 +692,15 @@ cudaError_t launch_gather_T(int N, int d, const cplx* loc, const double* Mmass, 
     long long tot = 4LL * N * N;
     dim3 g((unsigned)((tot + 255) / 256), nk);
     k_gather_T<<<g, 256, 0, st>>>(N, d + 1, loc, npair, Mmass, T);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_layers_sub(int N, int d, int layers, const cplx* loc, int job, int row, int rows, int col,
+                                     int cols, cplx* out, cudaStream_t st) {
+    long long npair = (long long)N * (N + 1) / 2;
+    long long tot = (long long)rows * cols;
+    k_gather_layers_sub<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(N, d + 1, layers, loc, npair, job, row, rows,
+                                                                       col, cols, out);
     return cudaGetLastError();
 }
 

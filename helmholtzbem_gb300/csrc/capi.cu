@@ -19,6 +19,8 @@ cudaError_t launch_local(const DevMesh& M, const SingularTask* tasks, int ntasks
                          bool real_k, int d, cplx* loc, cudaStream_t st);
 cudaError_t launch_gather_T(int N, int d, const cplx* loc, const double* Mmass, int nk, cplx* T, cudaStream_t st);
 cudaError_t launch_gather_layers(int N, int d, int layers, const cplx* loc, int job, cplx* out, cudaStream_t st);
+cudaError_t launch_gather_layers_sub(int N, int d, int layers, const cplx* loc, int job, int row, int rows, int col,
+                                     int cols, cplx* out, cudaStream_t st);
 cudaError_t launch_projection(int N, const double* id, const double* sb, const double* lr, cplx* T, int nmat,
                               cudaStream_t st);
 cudaError_t launch_svd(int n, int nmat, int D, int which, const cplx* T, long long mat_stride, long long der_stride,
@@ -242,7 +244,7 @@ struct hbem_builder_s {
     cudaStream_t st = nullptr;
     DBuf d_kind, d_par, d_xg, d_wg, d_xc, d_wc, d_gpt, d_gtan, d_gtn, d_ends, d_flags, d_tasks;
     DBuf d_loc, d_jobs, d_layers;
-    int asm_layers = 0, asm_d = -1;
+    int asm_layers = 0, asm_d = -1, asm_rows = 0, asm_cols = 0;
 
     long long npair() const { return (long long)n * (n + 1) / 2; }
     DevMesh view() const {
@@ -468,7 +470,16 @@ static int check_kc(double k_im, double c) {
 }
 
 int hbem_assemble_dense(hbem_builder b, double k_re, double k_im, double c, unsigned layers, unsigned d) {
+    return hbem_assemble_dense_sub(b, k_re, k_im, c, layers, d, 0, 0, 0, 0);
+}
+
+int hbem_assemble_dense_sub(hbem_builder b, double k_re, double k_im, double c, unsigned layers, unsigned d,
+                            unsigned row, unsigned col, unsigned rows, unsigned cols) {
     if (!b) return fail(HBEM_ERR_INVALID, "null builder");
+    if (rows == 0) rows = (unsigned)b->n;
+    if (cols == 0) cols = (unsigned)b->n;
+    if ((size_t)row + rows > (size_t)b->n || (size_t)col + cols > (size_t)b->n)
+        return fail(HBEM_ERR_INVALID, "sub-matrix outside the panel range");
     if (int r = check_kc(k_im, c)) return r;
     if (d > 2) return fail(HBEM_ERR_INVALID, "Invalid order of derivative");
     if (layers == 0 || layers > 7) return fail(HBEM_ERR_INVALID, "bad layer mask");
@@ -479,15 +490,21 @@ int hbem_assemble_dense(hbem_builder b, double k_re, double k_im, double c, unsi
     std::vector<Job> jobs{Job{k_re, k_im, c}};
     HB_CK(upload(b->d_jobs, jobs, b->st));
     int nl = ((layers & 1) != 0) + ((layers & 2) != 0) + ((layers & 4) != 0);
-    HB_CK(b->d_layers.ensure((size_t)nl * (d + 1) * b->n * b->n * sizeof(cplx)));
+    HB_CK(b->d_layers.ensure((size_t)nl * (d + 1) * rows * cols * sizeof(cplx)));
     bool real_k = (k_im == 0. && k_re > 0.);
     HB_CK(local_assembly(b->view(), b->d_tasks.as<SingularTask>(), (int)b->tasks.size(), b->n, b->d_jobs.as<Job>(), 1,
                          real_k, (int)d, b->d_loc.as<cplx>(), b->st));
-    HB_CK(launch_gather_layers(b->n, (int)d, (int)layers, b->d_loc.as<cplx>(), 0, b->d_layers.as<cplx>(), b->st));
+    if (rows == (unsigned)b->n && cols == (unsigned)b->n)
+        HB_CK(launch_gather_layers(b->n, (int)d, (int)layers, b->d_loc.as<cplx>(), 0, b->d_layers.as<cplx>(), b->st));
+    else
+        HB_CK(launch_gather_layers_sub(b->n, (int)d, (int)layers, b->d_loc.as<cplx>(), 0, (int)row, (int)rows,
+                                       (int)col, (int)cols, b->d_layers.as<cplx>(), b->st));
     g_launches += 1;
     HB_CK(cudaStreamSynchronize(b->st));
     b->asm_layers = (int)layers;
     b->asm_d = (int)d;
+    b->asm_rows = (int)rows;
+    b->asm_cols = (int)cols;
     return HBEM_OK;
 }
 
@@ -504,7 +521,7 @@ static int layer_slot(hbem_builder b, unsigned layer, unsigned d, size_t* off) {
         if ((unsigned)L == layer) break;
         if (b->asm_layers & L) ++slot;
     }
-    *off = ((size_t)slot * (b->asm_d + 1) + d) * b->n * b->n;
+    *off = ((size_t)slot * (b->asm_d + 1) + d) * b->asm_rows * b->asm_cols;
     return HBEM_OK;
 }
 
@@ -512,7 +529,8 @@ int hbem_get_layer(hbem_builder b, unsigned layer, unsigned d, double* host_out)
     size_t off;
     if (int r = layer_slot(b, layer, d, &off)) return r;
     if (!host_out) return fail(HBEM_ERR_INVALID, "null output");
-    HB_CK(cudaMemcpy(host_out, b->d_layers.as<cplx>() + off, (size_t)b->n * b->n * sizeof(cplx), cudaMemcpyDeviceToHost));
+    HB_CK(cudaMemcpy(host_out, b->d_layers.as<cplx>() + off, (size_t)b->asm_rows * b->asm_cols * sizeof(cplx),
+                     cudaMemcpyDeviceToHost));
     return HBEM_OK;
 }
 

@@ -97,6 +97,14 @@ int hbem_builder_is_adjacent(hbem_builder b, int i, int j, int* adjacent, int* s
  * (include/galerkin_builder.hpp:221-222; source/galerkin_builder.cpp:918-1018).
  * Errors as the reference: c < 1, Im k < 0 or d > 2 -> HBEM_ERR_INVALID.       */
 int hbem_assemble_dense(hbem_builder b, double k_re, double k_im, double c, unsigned layers, unsigned d);
+/* assembleDense(k, c, layers, d, row, col, rows, cols) with the reference's sub-matrix
+ * rule (galerkin_builder.cpp:918-1009): only panel pairs with one panel in
+ * [row, row + rows) and the other in [col, col + cols) contribute, to the dof block
+ * [row, row + rows) x [col, col + cols); rows, cols = 0 mean N.  Every layer is
+ * rows x cols (the reference sizes V rows x rows and W cols x cols).  hbem_get_layer*
+ * then return rows x cols matrices.                                               */
+int hbem_assemble_dense_sub(hbem_builder b, double k_re, double k_im, double c, unsigned layers, unsigned d,
+                            unsigned row, unsigned col, unsigned rows, unsigned cols);
 /* getDoubleLayer / getHypersingular / getSingleLayer(d) (include/galerkin_builder.hpp:262-276):
  * copies the N x N complex matrix to host_out; HBEM_ERR_INVALID if the layer or
  * derivative was not assembled by the last hbem_assemble_dense.                  */

@@ -164,9 +164,10 @@ class GalerkinBuilder {
     const BuilderData& data_;
     mutable MatrixXcd cache_[3][3];
 
+    long rows_ = 0, cols_ = 0;
     const MatrixXcd& fetch(unsigned layer, int slot, size_t d) const {
         MatrixXcd& m = cache_[slot][d > 2 ? 2 : d];
-        m.resize((long)data_.getNumPanels(), (long)data_.getNumPanels());
+        m.resize(rows_, cols_);
         throw_if(hbem_get_layer(data_.handle(), layer, (unsigned)d, reinterpret_cast<double*>(m.data())));
         return m;
     }
@@ -174,8 +175,12 @@ class GalerkinBuilder {
 public:
     explicit GalerkinBuilder(const BuilderData& data) : data_(data) {}
     const BuilderData& getData() const { return data_; }
-    void assembleDense(const std::complex<double>& k, double c, LayerType layers = LayerType::ALL, size_t d = 0) {
-        throw_if(hbem_assemble_dense(data_.handle(), k.real(), k.imag(), c, (unsigned)layers, (unsigned)d));
+    void assembleDense(const std::complex<double>& k, double c, LayerType layers = LayerType::ALL, size_t d = 0,
+                       size_t row = 0, size_t col = 0, size_t rows = 0, size_t cols = 0) {
+        throw_if(hbem_assemble_dense_sub(data_.handle(), k.real(), k.imag(), c, (unsigned)layers, (unsigned)d,
+                                         (unsigned)row, (unsigned)col, (unsigned)rows, (unsigned)cols));
+        rows_ = rows ? (long)rows : (long)data_.getNumPanels();
+        cols_ = cols ? (long)cols : (long)data_.getNumPanels();
     }
     const MatrixXcd& getDoubleLayer(size_t d = 0) const { return fetch(HBEM_LAYER_DOUBLE, 0, d); }
     const MatrixXcd& getHypersingular(size_t d = 0) const { return fetch(HBEM_LAYER_HYPERSINGULAR, 1, d); }

@@ -76,6 +76,23 @@ def test_assemble_layers_vs_oracle(mesh, k):
         assert rel(gb.getSingleLayer(t), ref["V"][t]) < 1e-12
 
 
+@pytest.mark.parametrize("sub", [(3, 10, 12, 7), (0, 0, 5, 20), (8, 8, 9, 9), (17, 2, 7, 5)])
+def test_assemble_submatrix_vs_oracle(sub):
+    """assembleDense(k, c, layers, d, row, col, rows, cols): the reference's sub-matrix
+    rule (panel pairs inside the row / column panel ranges only) against the oracle."""
+    row, col, rows, cols = sub
+    (kinds, par), order = MESHES[list(MESHES)[0]]()
+    data = api.BuilderData((kinds, par), order=order)
+    gb = api.GalerkinBuilder(data)
+    ob = O.Builder(kinds, par, order)
+    gb.assembleDense(2.9, 4.0, api.LayerType_ALL, 1, row, col, rows, cols)
+    ref = ob.assemble(2.9, 4.0, O.LAYER_ALL, 1, row=row, col=col, rows=rows, cols=cols)
+    for t in range(2):
+        for got, name in ((gb.getDoubleLayer(t), "K"), (gb.getHypersingular(t), "W"), (gb.getSingleLayer(t), "V")):
+            assert got.shape == (rows, cols)
+            assert rel(got, ref[name][t]) < 1e-12
+
+
 def test_geometry_matches_oracle_geometry():
     a = geometry.polygon(*geometry.star_polygon(24, seed=2), 1000)
     b = O.polygon_panels(*O.star_polygon(24, seed=2), 1000)

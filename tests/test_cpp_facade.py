@@ -51,4 +51,5 @@ def test_facade_runs_and_matches_python(tmp_path):
     assert abs(complex(vals[11], vals[12]) - S[2, 5]) <= 1e-12 * abs(S[2, 5]) and vals[13] == gy[2, 5]
     # randomized sigma: an estimate from above, close on the 12-wide sketch with 2 subspace steps
     assert ref[0] * (1 - 1e-12) <= vals[14] <= ref[0] * (1 + 1e-3)
-    assert abs(vals[15] - np.pi) < 1e-6
+    # reverse communication: the same iterates as the callback form (Brent's tolerance sqrt(tol) |x|)
+    assert vals[15] == api.brent_min(np.cos, 2.0, 4.0, 1e-8) and abs(vals[15] - np.pi) < 1e-3

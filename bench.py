@@ -274,7 +274,7 @@ def assembly_at_scale(torch, C, api, geometry, lib, peak):
                                         C.ctypes.c_longlong())
     lib.hbem_stats_read(C.ctypes.byref(launches), C.ctypes.byref(asm_ms), C.ctypes.byref(asm_l),
                         C.ctypes.byref(asm_pts))
-    achieved = asm_pts.value * 480.0 / (asm_ms.value * 1e-3) / 1e12 if asm_ms.value > 0 else 0.0
+    achieved = assembly_flops(C, lib) / (asm_ms.value * 1e-3) / 1e12 if asm_ms.value > 0 else 0.0
     del T
     return {"workload": "star polygon 24 vertices (seed 2), N=1000 lines, order 16, k=20, c_i=4, c_o=1, "
                         "T/T'/T'' 2000x2000 c128 projected",
@@ -282,6 +282,21 @@ def assembly_at_scale(torch, C, api, geometry, lib, peak):
             "quad_points_per_T_set": asm_pts.value // reps,
             "assembly_ms_per_T_set": asm_ms.value / reps,
             "assembly_fp64_tflops": achieved, "assembly_frac_of_measured_fp64": achieved / peak if peak else None}
+
+
+def assembly_flops(C, lib):
+    """Algorithmic FP64 flops of the timed assembly launches: per quadrature point and
+    medium F(d) = 130 (Hankel pair) + 50 (geometry and weights) + 100 (d + 1) (kernel
+    values and moment updates of orders 0..d); singular-pair points whose geometry
+    comes from the builder's k-independent table do not repeat the 50."""
+    split = (C.ctypes.c_longlong * 9)()
+    lib.hbem_stats_read_points(split)
+    f = 0.0
+    for d in range(3):
+        f += split[d] * (180.0 + 100.0 * (d + 1))
+        f += split[3 + d] * (130.0 + 100.0 * (d + 1))
+        f += split[6 + d] * (180.0 + 100.0 * (d + 1))
+    return f
 
 
 def dense_tail_at_scale(torch, C, api, geometry, lib, peak, nk=16):
@@ -745,11 +760,9 @@ def run_gpu(args):
         del s2, d2
     d2h = int(roots.nbytes + CFG["npoints"] * 3 * 8)
 
-    # roofline of the dominant kernel (panel-pair assembly, FP64 CUDA-core bound).
-    # Algorithmic work: F_pt(d) = 180 + 100 (d + 1) FP64 flops per quadrature point and
-    # medium; asm_pts counts points x media over the timed launches.
-    d = 2
-    flops = asm_pts.value * (180.0 + 100.0 * (d + 1))
+    # roofline of the dominant kernel (panel-pair assembly, FP64 CUDA-core bound):
+    # algorithmic work of the timed launches by derivative order and point kind
+    flops = assembly_flops(C, lib)
     achieved = flops / (asm_ms.value * 1e-3) / 1e12 if asm_ms.value > 0 else 0.0
     peak = fp64_peak_tflops()
     roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",

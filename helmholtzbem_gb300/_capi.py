@@ -17,7 +17,7 @@ SPACE_P0, SPACE_P1 = 1, 2
 # every symbol include/hbem.h declares
 EXPORTS = [
     "hbem_version", "hbem_status_string", "hbem_last_error", "hbem_set_device", "hbem_set_option", "hbem_hankel01",
-    "hbem_stats_enable_timing", "hbem_stats_reset", "hbem_stats_read",
+    "hbem_stats_enable_timing", "hbem_stats_reset", "hbem_stats_read", "hbem_stats_read_points",
     "hbem_builder_create", "hbem_builder_destroy", "hbem_builder_info", "hbem_builder_is_adjacent",
     "hbem_assemble_dense", "hbem_assemble_dense_sub", "hbem_get_layer", "hbem_get_layer_device",
     "hbem_solop_create", "hbem_solop_destroy", "hbem_mass_matrix", "hbem_gen_sol_op",
@@ -80,6 +80,7 @@ def load(path=LIB_PATH):
         "hbem_hankel01": (_i, [_i, _dp, _i, _dp, _dp]),
         "hbem_stats_enable_timing": (None, [_i]),
         "hbem_stats_reset": (None, []),
+        "hbem_stats_read_points": (None, [ctypes.POINTER(ctypes.c_longlong)]),
         "hbem_stats_read": (None, [ctypes.POINTER(ctypes.c_longlong), _dp, ctypes.POINTER(ctypes.c_longlong),
                                    ctypes.POINTER(ctypes.c_longlong)]),
         "hbem_builder_create": (_i, [_i, _ip, _dp, _i, _i, _i, ctypes.POINTER(_vp)]),

@@ -416,6 +416,76 @@ __device__ __forceinline__ void block_reduce(AccT& A, double* red /* [nwarps][si
     }
 }
 
+// Point data of a singular pair (see kSGeoFields): the geometry part of the
+// quadrature, the same for every wavenumber and medium.
+__device__ __forceinline__ void singular_fields(const DevMesh& M, const SingularTask& T, int Kset, double xa, double xb,
+                                                double wa, double wb, double* f) {
+    SPoint P;
+    singular_point(M, T, Kset, xa, xb, P);
+    const double wab = wa * wb;
+    f[0] = norm2(P.v);
+    f[1] = sqrt(f[0]);
+    f[2] = 2. * (P.ti.im * P.tj.im + P.ti.re * P.tj.re);
+    // v x tau_j |tau_i| and tau_i x v |tau_j|; for a coincident pair the second is the
+    // double layer of set 1 (the reference uses v = gamma(s) - gamma(t) for both sets)
+    f[3] = (P.v.re * P.tj.im - P.v.im * P.tj.re) * P.tin;
+    f[4] = (P.v.im * P.ti.re - P.v.re * P.ti.im) * P.tjn;
+    f[5] = (T.kind == PK_COINC ? xb : xa) * wab;
+    f[6] = P.x;
+    f[7] = P.y;
+}
+
+// Tabulate singular_fields for every task, set and point: [task][set][field][point].
+__global__ void __launch_bounds__(256) k_singular_geo(DevMesh M, const SingularTask* tasks, double* geo) {
+    const SingularTask T = tasks[blockIdx.x];
+    const int nc = M.nc, tot = nc * nc;
+    double* G = geo + (long long)blockIdx.x * 2 * kSGeoFields * tot;
+    const int nset = T.kind == PK_COINC ? 1 : 2;
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+        const int a = e % nc, b = e / nc;
+        for (int Kset = 0; Kset < nset; ++Kset) {
+            double f[kSGeoFields];
+            singular_fields(M, T, Kset, M.xc[a], M.xc[b], M.wc[a], M.wc[b], f);
+#pragma unroll
+            for (int q = 0; q < kSGeoFields; ++q) G[((long long)Kset * kSGeoFields + q) * tot + e] = f[q];
+        }
+    }
+}
+
+// Kernel values and moment updates of one point of a singular pair from its fields.
+template <int D, bool RK, bool CURVED>
+__device__ __forceinline__ void singular_accumulate(Acc<D, CURVED>& A, const KConst& K, int kind, uint8_t fl,
+                                                    int Kset, const double* f) {
+    const double vn2 = f[0], vn = f[1];
+    cplx h0, h1;
+    hankel_at<RK>(K, vn, h0, h1);
+    const KVals<D, RK> kv = kernel_values<D, RK>(K, vn, vn2, h0, h1);
+    double wm[4];
+    if (kind == PK_COINC) {
+        // one point serves both triangles: set 0 has (x, y) = (s, t), set 1 (t, s);
+        // V and W kernels are symmetric in s <-> t: both sets in one moment update
+        const double w = f[5], s = f[6], t = f[7];
+        const double wsym[4] = {2. * w, w * (s + t), w * (s + t), 2. * w * s * t};
+        acc_s<D, RK, CURVED>(A, wsym, kv, f[2], !(fl & PF_TDT0_ZERO));
+        if (!(fl & PF_DL0_ZERO)) {
+            mom_weights(w, s, t, wm);
+            acc_dl<D, RK, CURVED>(A, wm, kv, f[3]);
+        }
+        if (!(fl & PF_DL1_ZERO)) {
+            mom_weights(w, t, s, wm);
+            acc_dl<D, RK, CURVED>(A, wm, kv, f[4]);
+        }
+    } else {
+        const uint8_t dlz = Kset == 0 ? PF_DL0_ZERO : PF_DL1_ZERO;
+        const uint8_t dltz = Kset == 0 ? PF_DLT0_ZERO : PF_DLT1_ZERO;
+        const uint8_t tdz = Kset == 0 ? PF_TDT0_ZERO : PF_TDT1_ZERO;
+        mom_weights(f[5], f[6], f[7], wm);
+        acc_s<D, RK, CURVED>(A, wm, kv, f[2], !(fl & tdz));
+        if (!(fl & dlz)) acc_dl<D, RK, CURVED>(A, wm, kv, f[3]);
+        if (!(fl & dltz)) acc_dlt<D, RK, CURVED>(A, wm, kv, f[4]);
+    }
+}
+
 template <int D, bool RK, bool CURVED>
 __global__ void __launch_bounds__(128) k_singular(DevMesh M, const SingularTask* tasks, const Job* jobs, cplx* loc,
                                                   long long npair) {
@@ -431,52 +501,23 @@ __global__ void __launch_bounds__(128) k_singular(DevMesh M, const SingularTask*
     const long long pid = tri_index(T.i, T.j);
     const uint8_t fl = M.flags[pid];
     const int nc = M.nc, tot = nc * nc;
+    const int nset = T.kind == PK_COINC ? 1 : 2;
+    // point data from the table when the builder made one, else computed here
+    const double* G = M.sgeo ? M.sgeo + (long long)blockIdx.x * 2 * kSGeoFields * tot : nullptr;
     Acc<D, CURVED> A;
     A.zero();
     for (int e = threadIdx.x; e < tot; e += blockDim.x) {
         const int a = e % nc, b = e / nc;
-        const double wab = swc[a] * swc[b];
-        if (T.kind == PK_COINC) {
-            // one point serves both triangles: set 0 has (x, y) = (s, t), set 1 (t, s)
-            SPoint P;
-            singular_point(M, T, 0, sxc[a], sxc[b], P);
-            const double w = sxc[b] * wab;
-            const double vn2 = norm2(P.v), vn = sqrt(vn2);
-            cplx h0, h1;
-            hankel_at<RK>(K, vn, h0, h1);
-            const KVals<D, RK> kv = kernel_values<D, RK>(K, vn, vn2, h0, h1);
-            const double s = P.x, t = P.y;
-            // V and W kernels are symmetric in s <-> t: both sets in one moment update
-            const double wsym[4] = {2. * w, w * (s + t), w * (s + t), 2. * w * s * t};
-            acc_s<D, RK, CURVED>(A, wsym, kv, 2. * (P.ti.im * P.tj.im + P.ti.re * P.tj.re), !(fl & PF_TDT0_ZERO));
-            double wm[4];
-            if (!(fl & PF_DL0_ZERO)) {
-                mom_weights(w, s, t, wm);
-                acc_dl<D, RK, CURVED>(A, wm, kv, (P.v.re * P.tj.im - P.v.im * P.tj.re) * P.tin);
-            }
-            if (!(fl & PF_DL1_ZERO)) {
-                mom_weights(w, t, s, wm);
-                acc_dl<D, RK, CURVED>(A, wm, kv, (P.v.im * P.ti.re - P.v.re * P.ti.im) * P.tjn);
-            }
-        } else {
-            const double w = sxc[a] * wab;
 #pragma unroll 1
-            for (int Kset = 0; Kset < 2; ++Kset) {
-                SPoint P;
-                singular_point(M, T, Kset, sxc[a], sxc[b], P);
-                const double vn2 = norm2(P.v), vn = sqrt(vn2);
-                cplx h0, h1;
-                hankel_at<RK>(K, vn, h0, h1);
-                const KVals<D, RK> kv = kernel_values<D, RK>(K, vn, vn2, h0, h1);
-                const uint8_t dlz = Kset == 0 ? PF_DL0_ZERO : PF_DL1_ZERO;
-                const uint8_t dltz = Kset == 0 ? PF_DLT0_ZERO : PF_DLT1_ZERO;
-                const uint8_t tdz = Kset == 0 ? PF_TDT0_ZERO : PF_TDT1_ZERO;
-                double wm[4];
-                mom_weights(w, P.x, P.y, wm);
-                acc_s<D, RK, CURVED>(A, wm, kv, 2. * (P.ti.im * P.tj.im + P.ti.re * P.tj.re), !(fl & tdz));
-                if (!(fl & dlz)) acc_dl<D, RK, CURVED>(A, wm, kv, (P.v.re * P.tj.im - P.v.im * P.tj.re) * P.tin);
-                if (!(fl & dltz)) acc_dlt<D, RK, CURVED>(A, wm, kv, (P.v.im * P.ti.re - P.v.re * P.ti.im) * P.tjn);
+        for (int Kset = 0; Kset < nset; ++Kset) {
+            double f[kSGeoFields];
+            if (G) {
+#pragma unroll
+                for (int q = 0; q < kSGeoFields; ++q) f[q] = __ldg(G + ((long long)Kset * kSGeoFields + q) * tot + e);
+            } else {
+                singular_fields(M, T, Kset, sxc[a], sxc[b], swc[a], swc[b], f);
             }
+            singular_accumulate<D, RK, CURVED>(A, K, T.kind, fl, Kset, f);
         }
     }
     block_reduce(A, red);
@@ -666,6 +707,16 @@ static cudaError_t launch_local_t(const DevMesh& M, const SingularTask* tasks, i
                                   cplx* loc, cudaStream_t st) {
     if (M.lines) return launch_local_c<D, RK, false>(M, tasks, ntasks, jobs, njobs, loc, st);
     return launch_local_c<D, RK, true>(M, tasks, ntasks, jobs, njobs, loc, st);
+}
+
+size_t singular_geo_bytes(int nc, int ntasks) {
+    return (size_t)ntasks * 2 * kSGeoFields * (size_t)nc * nc * sizeof(double);
+}
+
+cudaError_t launch_singular_geo(const DevMesh& M, const SingularTask* tasks, int ntasks, double* geo,
+                                cudaStream_t st) {
+    if (ntasks > 0) k_singular_geo<<<ntasks, 256, 0, st>>>(M, tasks, geo);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_flags(const DevMesh& M, const SingularTask* tasks, int ntasks, uint8_t* flags, cudaStream_t st) {

@@ -51,7 +51,13 @@ struct DevMesh {
     const double* gtn;        // [n][p] tangent norms
     const cplx* ends;         // [n][2] start/end (the [-1,1] map at -1/+1)
     const uint8_t* flags;     // [n(n+1)/2] per lower-triangle pair
+    const double* sgeo = nullptr;   // [ntasks][2][kSGeoFields][nc*nc] singular-pair point data, or null
 };
+
+// k-independent data of one composite quadrature point of a singular pair:
+//   coincident (set 0 serves both triangles): |v|^2, |v|, 2 tau_i.tau_j, dl0, dl1, w, s, t
+//   adjacent (set K):                         |v|^2, |v|, 2 tau_i.tau_j, dl, dlt, w, x, y
+constexpr int kSGeoFields = 8;
 
 // one (k, c) job
 struct Job {

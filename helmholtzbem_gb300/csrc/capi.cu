@@ -3,9 +3,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <random>
 #include <vector>
@@ -15,6 +17,9 @@
 
 namespace hbem {
 cudaError_t launch_flags(const DevMesh& M, const SingularTask* tasks, int ntasks, uint8_t* flags, cudaStream_t st);
+size_t singular_geo_bytes(int nc, int ntasks);
+cudaError_t launch_singular_geo(const DevMesh& M, const SingularTask* tasks, int ntasks, double* geo,
+                                cudaStream_t st);
 cudaError_t launch_local(const DevMesh& M, const SingularTask* tasks, int ntasks, const Job* jobs, int njobs,
                          bool real_k, int d, cplx* loc, cudaStream_t st);
 cudaError_t launch_gather_T(int N, int d, const cplx* loc, const double* Mmass, int nk, cplx* T, cudaStream_t st);
@@ -66,14 +71,23 @@ int g_device = 0;
 const double kMachEps = 2.220446049250313e-16;
 
 // instrumentation: kernel launches issued, and CUDA-event timing of the
-// panel-pair assembly launches on the stream they run on
-long long g_launches = 0;
+// panel-pair assembly launches on the stream they run on (atomic: entry points may
+// be called from several host threads on different operators)
+std::atomic<long long> g_launches{0};
 int g_timing = 0;
+std::mutex g_stats_mu;
 double g_asm_ms = 0.;
-long long g_asm_launches = 0;
-long long g_asm_points = 0;   // quadrature points x media processed by timed launches
+std::atomic<long long> g_asm_launches{0};
+std::atomic<long long> g_asm_points{0};   // quadrature points x media processed by timed launches
+// the same split by derivative order and by kind: [d] general pairs, [3 + d] singular
+// pairs whose point data came from the builder's table, [6 + d] singular pairs that
+// computed it in the kernel
+std::atomic<long long> g_asm_split[9];
 int g_svd_fast = 1;           // dense sigma: FP32 Jacobi + FP64 refinement where it fits
 int g_arnoldi_maxit = 1000;   // block iterations of hbem_arnoldi_sv_batch*
+int g_plain_speculate = 1;    // plain search: speculative bisection points in small Newton rounds
+int g_singular_table = 1;     // singular pairs read their k-independent point data from a table
+const size_t kSingularTableMax = (size_t)256 << 20;
 
 int fail(int code, const std::string& msg) {
     g_err = msg;
@@ -86,12 +100,18 @@ int fail(int code, const std::string& msg) {
         if (e_ != cudaSuccess) return fail(HBEM_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-// growable device buffer
+// growable device buffer; requests below 64 MiB grow to the next power of two so
+// that batches of varying size (Newton rounds) do not reallocate every call
 struct DBuf {
     void* p = nullptr;
     size_t cap = 0;
     cudaError_t ensure(size_t bytes) {
         if (bytes <= cap) return cudaSuccess;
+        if (bytes < ((size_t)64 << 20)) {
+            size_t r = 256;
+            while (r < bytes) r <<= 1;
+            bytes = r;
+        }
         if (p) cudaFree(p);
         p = nullptr;
         cap = 0;
@@ -214,12 +234,17 @@ cudaError_t local_assembly(const DevMesh& M, const SingularTask* tasks, int ntas
         cudaEventSynchronize(e1);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
-        g_asm_ms += ms;
+        {
+            std::lock_guard<std::mutex> lk(g_stats_mu);
+            g_asm_ms += ms;
+        }
         g_asm_launches += 1;
         long long nc2 = (long long)M.nc * M.nc;
         long long nadj = ntasks - ncoinc;
         long long gen = (long long)M.n * (M.n + 1) / 2 - ntasks;
         g_asm_points += (long long)njobs * (ncoinc * nc2 + nadj * 2 * nc2 + gen * (long long)M.p * M.p);
+        g_asm_split[d] += (long long)njobs * gen * M.p * M.p;
+        g_asm_split[(M.sgeo ? 3 : 6) + d] += (long long)njobs * (ncoinc * nc2 + nadj * 2 * nc2);
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
     }
@@ -244,6 +269,7 @@ struct hbem_builder_s {
     cudaStream_t st = nullptr;
     DBuf d_kind, d_par, d_xg, d_wg, d_xc, d_wc, d_gpt, d_gtan, d_gtn, d_ends, d_flags, d_tasks;
     DBuf d_loc, d_jobs, d_layers;
+    DBuf d_sgeo;   // k-independent point data of the singular pairs (when within kSingularTableMax)
     int asm_layers = 0, asm_d = -1, asm_rows = 0, asm_cols = 0;
 
     long long npair() const { return (long long)n * (n + 1) / 2; }
@@ -255,6 +281,7 @@ struct hbem_builder_s {
         M.xc = d_xc.as<double>(); M.wc = d_wc.as<double>();
         M.gpt = d_gpt.as<cplx>(); M.gtan = d_gtan.as<cplx>(); M.gtn = d_gtn.as<double>();
         M.ends = d_ends.as<cplx>(); M.flags = d_flags.as<uint8_t>();
+        M.sgeo = g_singular_table ? d_sgeo.as<double>() : nullptr;
         return M;
     }
     // BuilderData::is_adjacent (galerkin_builder.cpp:189-201)
@@ -266,7 +293,7 @@ struct hbem_builder_s {
     }
     ~hbem_builder_s() {
         for (DBuf* b : {&d_kind, &d_par, &d_xg, &d_wg, &d_xc, &d_wc, &d_gpt, &d_gtan, &d_gtn, &d_ends, &d_flags,
-                        &d_tasks, &d_loc, &d_jobs, &d_layers})
+                        &d_tasks, &d_loc, &d_jobs, &d_layers, &d_sgeo})
             b->release();
         if (st) cudaStreamDestroy(st);
     }
@@ -290,17 +317,29 @@ void hbem_stats_enable_timing(int enable) { g_timing = enable ? 1 : 0; }
 
 void hbem_stats_reset(void) {
     g_launches = 0;
-    g_asm_ms = 0.;
+    {
+        std::lock_guard<std::mutex> lk(g_stats_mu);
+        g_asm_ms = 0.;
+    }
     g_asm_launches = 0;
     g_asm_points = 0;
+    for (auto& x : g_asm_split) x = 0;
 }
 
 void hbem_stats_read(long long* launches, double* assembly_ms, long long* assembly_launches,
                      long long* assembly_points) {
     if (launches) *launches = g_launches;
-    if (assembly_ms) *assembly_ms = g_asm_ms;
+    if (assembly_ms) {
+        std::lock_guard<std::mutex> lk(g_stats_mu);
+        *assembly_ms = g_asm_ms;
+    }
     if (assembly_launches) *assembly_launches = g_asm_launches;
     if (assembly_points) *assembly_points = g_asm_points;
+}
+
+void hbem_stats_read_points(long long* split9) {
+    if (split9)
+        for (int i = 0; i < 9; ++i) split9[i] = g_asm_split[i];
 }
 
 const char* hbem_status_string(int s) {
@@ -342,6 +381,14 @@ int hbem_set_option(const char* name, int value) {
     }
     if (k == "mlp_tensor_cores") {
         mlp_set_tensor_cores(value);
+        return HBEM_OK;
+    }
+    if (k == "singular_table") {
+        g_singular_table = value ? 1 : 0;
+        return HBEM_OK;
+    }
+    if (k == "plain_speculate") {
+        g_plain_speculate = value ? 1 : 0;
         return HBEM_OK;
     }
     if (k == "arnoldi_maxit") {
@@ -429,6 +476,16 @@ int hbem_builder_create(int npanels, const int* kinds, const double* params, int
     if (e == cudaSuccess) e = upload(b->d_tasks, b->tasks, b->st);
     if (e == cudaSuccess) e = launch_flags(b->view(), b->d_tasks.as<SingularTask>(), (int)b->tasks.size(),
                                            b->d_flags.as<uint8_t>(), b->st);
+    const size_t geo_bytes = singular_geo_bytes(b->nc, (int)b->tasks.size());
+    if (e == cudaSuccess && geo_bytes > 0 && geo_bytes <= kSingularTableMax) {
+        e = b->d_sgeo.ensure(geo_bytes);
+        if (e == cudaSuccess) {
+            DevMesh M = b->view();
+            M.sgeo = nullptr;
+            e = launch_singular_geo(M, b->d_tasks.as<SingularTask>(), (int)b->tasks.size(), b->d_sgeo.as<double>(),
+                                    b->st);
+        }
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
     if (e != cudaSuccess) {
         std::string msg = cudaGetErrorString(e);
@@ -1096,5 +1153,12 @@ void gauss_rule(double a, double b, int n, double* x, double* w) { gauss_legendr
 
 // launch counter shared by every entry point
 void count_launches(long long n) { g_launches += n; }
+
+// The plain search's Newton rounds add speculative bisection points where sigma comes
+// from the one-CTA dense kernel (its per-evaluation latency, not the GPU's
+// throughput, bounds a round, so a few more matrices per round cost little).
+int plain_speculate_ok(hbem_solop s) {
+    return s && g_plain_speculate && g_svd_fast && svd_fast_smem_bytes(2 * s->b->n) <= 220 * 1024;
+}
 
 }  // namespace hbem

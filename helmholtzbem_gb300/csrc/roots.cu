@@ -10,6 +10,7 @@
 // resonance search runs many rtsafe iterations in lock step so every Newton
 // round is one batched GPU evaluation of sigma' and sigma''.
 #include <algorithm>
+#include <array>
 #include <cstdint>
 #include <functional>
 #include <cmath>
@@ -18,6 +19,10 @@
 #include <vector>
 
 #include "../../include/hbem.h"
+
+namespace hbem {
+int plain_speculate_ok(hbem_solop s);
+}  // namespace hbem
 
 namespace {
 
@@ -57,6 +62,18 @@ struct Newton {
             if (temp == rts) { finish(true); return; }
         }
         if (std::fabs(dx) < tol) { finish(true); return; }
+    }
+    // the points a bisection step could move to after the next feed (f < 0 moves xl
+    // to rts, otherwise xh; the first feed, at the initial guess, moves neither),
+    // computed with the same operations as feed() so that they compare equal
+    int bisect_next(double* c) const {
+        if (first) {
+            c[0] = xl + 0.5 * (xh - xl);
+            return 1;
+        }
+        c[0] = rts + 0.5 * (xh - rts);
+        c[1] = xl + 0.5 * (rts - xl);
+        return 2;
     }
 };
 
@@ -365,6 +382,69 @@ int opt_subdiv_impl(const BatchEval& f, double x_min, double x_max, int batch, i
     return HBEM_OK;
 }
 
+// ---------------------------------------------------------------- Newton rounds with speculation
+//
+// The Newton phase of the plain search (examples/roots_newton_polygon_rsvd.cpp:209-265)
+// for candidates whose brackets have been validated.  Every round is one batched
+// sigma', sigma'' evaluation; a round with at most kSpecRound active candidates also
+// evaluates the one or two points a bisection step of rtsafe could move to next
+// (Newton::bisect_next).  When that step follows, its point is already known and costs
+// no round of its own.  Each candidate is fed exactly the values it would be fed
+// without speculation, so its iterates are unchanged; the rounds are latency bound
+// (one dense-sigma CTA per matrix), so a few more matrices per round cost little.
+// evals counts the evaluations the search used (unused speculative points excluded).
+constexpr int kSpecRound = 8;
+
+int newton_rounds(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, int& evals) {
+    std::vector<std::vector<std::array<double, 3>>> cache(nt.size());   // (k, sigma', sigma'')
+    struct Req { size_t cand; bool spec; };
+    std::vector<Req> who;
+    std::vector<double> xs, out;
+    for (int round = 0; round < kMaxIt; ++round) {
+        // points already evaluated speculatively
+        for (size_t c = 0; c < nt.size(); ++c)
+            while (!nt[c].done) {
+                auto it = std::find_if(cache[c].begin(), cache[c].end(),
+                                       [&](const std::array<double, 3>& e) { return e[0] == nt[c].rts; });
+                if (it == cache[c].end()) break;
+                nt[c].feed((*it)[1], (*it)[2]);
+                ++evals;
+            }
+        xs.clear();
+        who.clear();
+        for (size_t c = 0; c < nt.size(); ++c)
+            if (!nt[c].done) {
+                xs.push_back(nt[c].rts);
+                who.push_back(Req{c, false});
+            }
+        if (xs.empty()) break;
+        if (xs.size() <= (size_t)kSpecRound)
+            for (size_t c = 0; c < nt.size(); ++c) {
+                if (nt[c].done) continue;
+                cache[c].clear();
+                double sp[2];
+                const int m = nt[c].bisect_next(sp);
+                for (int j = 0; j < m; ++j)
+                    if (sp[j] != nt[c].rts) {
+                        xs.push_back(sp[j]);
+                        who.push_back(Req{c, true});
+                    }
+            }
+        out.assign(3 * xs.size(), 0.);
+        if (int r = hbem_sweep_sigma(s, xs.data(), (int)xs.size(), c_o, c_i, 2, out.data())) return r;
+        for (size_t q = 0; q < who.size(); ++q) {
+            const double* o = &out[3 * q];
+            if (who[q].spec) {
+                cache[who[q].cand].push_back({xs[q], o[1], o[2]});
+            } else {
+                nt[who[q].cand].feed(o[1], o[2]);
+                ++evals;
+            }
+        }
+    }
+    return HBEM_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -578,17 +658,22 @@ int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npo
     if (grid_host) std::copy(g.begin(), g.end(), grid_host);
     std::vector<Newton> nt(cands.size());
     for (size_t c = 0; c < cands.size(); ++c) nt[c].start(cands[c].a, cands[c].a + 2 * h, cands[c].guess, tol);
-    // lock-step Newton rounds: one batched sigma', sigma'' evaluation per round
-    for (int round = 0; round < kMaxIt; ++round) {
-        std::vector<double> xs;
-        std::vector<size_t> who;
-        for (size_t c = 0; c < nt.size(); ++c)
-            if (!nt[c].done) { xs.push_back(nt[c].rts); who.push_back(c); }
-        if (xs.empty()) break;
-        std::vector<double> out(3 * xs.size());
-        if (int r = hbem_sweep_sigma(s, xs.data(), (int)xs.size(), c_o, c_i, 2, out.data())) return r;
-        evals += (int)xs.size();
-        for (size_t q = 0; q < who.size(); ++q) nt[who[q]].feed(out[3 * q + 1], out[3 * q + 2]);
+    // lock-step Newton rounds: one batched sigma', sigma'' evaluation per round (with
+    // speculative bisection points where the dense sigma is latency bound)
+    if (hbem::plain_speculate_ok(s)) {
+        if (int r = newton_rounds(s, nt, c_o, c_i, evals)) return r;
+    } else {
+        for (int round = 0; round < kMaxIt; ++round) {
+            std::vector<double> xs;
+            std::vector<size_t> who;
+            for (size_t c = 0; c < nt.size(); ++c)
+                if (!nt[c].done) { xs.push_back(nt[c].rts); who.push_back(c); }
+            if (xs.empty()) break;
+            std::vector<double> out(3 * xs.size());
+            if (int r = hbem_sweep_sigma(s, xs.data(), (int)xs.size(), c_o, c_i, 2, out.data())) return r;
+            evals += (int)xs.size();
+            for (size_t q = 0; q < who.size(); ++q) nt[who[q]].feed(out[3 * q + 1], out[3 * q + 2]);
+        }
     }
     int cnt = 0;
     for (auto& x : nt)

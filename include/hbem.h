@@ -60,18 +60,28 @@ int hbem_set_device(int device);
  *   up to order 100 by FP32 Jacobi plus FP64 refinement of the near singular triplets
  *   (one FP64 LU per matrix); 0 always uses the FP64-polished Jacobi kernel.
  *   "arnoldi_maxit" (default 1000, >= 1): iteration cap of hbem_arnoldi_sv_batch*.
- *   "mlp_tensor_cores" (default 1): the MLP's BF16 products on tcgen05; 0 uses FP32 FMA. */
+ *   "mlp_tensor_cores" (default 1): the MLP's BF16 products on tcgen05; 0 uses FP32 FMA.
+ *   "singular_table" (default 1): coincident / adjacent panel pairs read the
+ *   k-independent data of their composite quadrature points (distance, tangent and
+ *   normal products, weights) from a table the builder makes once (up to 256 MB);
+ *   0 computes it in the kernel for every wavenumber and medium.
+ *   "plain_speculate" (default 1): speculative bisection points in the plain
+ *   search's small Newton rounds (hbem_find_resonances_plain).                    */
 int hbem_set_option(const char* name, int value);
 
 /* Instrumentation (no counterpart in the reference, which prints std::chrono
  * timings, gen_sol_op.cpp:89-99 and randsvd.cpp:27-47): kernel launches issued
  * by this library, and -- when timing is enabled -- CUDA-event time, launch count
  * and processed (quadrature point x medium) count of the panel-pair assembly
- * launches, timed on the stream they run on.  Not thread-safe.                 */
+ * launches, timed on the stream they run on.                 */
 void hbem_stats_enable_timing(int enable);
 void hbem_stats_reset(void);
 void hbem_stats_read(long long* launches, double* assembly_ms, long long* assembly_launches,
                      long long* assembly_points);
+/* The timed assembly's (point x medium) count split9[9] by kind and derivative
+ * order d: [d] general pairs, [3 + d] singular pairs reading their k-independent
+ * point data from the builder's table, [6 + d] singular pairs computing it.      */
+void hbem_stats_read_points(long long* split9);
 
 /* H0^(1), H1^(1) of n arguments on the device: complex_bessel::Hankel1Real01::h1_01
  * for real x (include/cbessel.hpp:236-288) when complex_arg == 0 (z_host holds n
@@ -382,7 +392,13 @@ int hbem_sweep_sigma(hbem_solop s, const double* k_host, int nk, double c_o, dou
  * sigma'' to tolerance tol, all candidates' Newton steps in one batch per round.
  * roots_host receives up to max_roots roots, *nroots their count; grid_host
  * (npoints x 3, may be NULL) sigma at every grid point and sigma' at the bracket
- * ends (NaN where not evaluated); *n_evals the number of T(k) evaluated.        */
+ * ends (NaN where not evaluated); *n_evals the number of T(k) evaluated.
+ * Where the one-CTA dense sigma kernel takes the order (2N <= 100), Newton rounds
+ * with at most 8 active candidates also evaluate the one or two points a bisection
+ * step of rtsafe could move to next (option "plain_speculate", default 1); when the
+ * step follows, its point needs no round of its own.  Every candidate is fed the
+ * same values as without speculation, so the roots are the same; *n_evals counts
+ * the evaluations the search used (unused speculative points excluded).          */
 int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npoints, double c_o, double c_i,
                                double tol, double* roots_host, int max_roots, int* nroots, double* grid_host,
                                int* n_evals);

@@ -229,3 +229,23 @@ def test_config2_full_size_properties():
     Tm = so.gen_sol_op(20.0 - h, 1.0, 4.0)
     assert rel((Tp - Tm) / (2 * h), T1) < 1e-6
     assert rel((Tp - 2 * T + Tm) / h ** 2, T2) < 1e-3
+
+
+@pytest.mark.parametrize("curved", [True, False])
+def test_singular_table_matches_on_the_fly(curved):
+    """Singular pairs read their k-independent point data from the builder's table
+    (default) or compute it in the kernel: the same T(k), T', T'' to rounding."""
+    from helmholtzbem_gb300 import _capi as C
+    mesh = geometry.circle(0.25, 24) if curved else geometry.polygon(*geometry.star_polygon(12, seed=3), 40)
+    so = api.SolutionsOperator(api.BuilderData(mesh, order=9))
+    ks = [0.7, 3.3, 9.1]
+    C.check(C.lib().hbem_set_option(b"singular_table", 1))
+    a = [so.gen_sol_op_2nd_der(k, 1.0, 23.4) for k in ks]
+    C.check(C.lib().hbem_set_option(b"singular_table", 0))
+    try:
+        b = [so.gen_sol_op_2nd_der(k, 1.0, 23.4) for k in ks]
+    finally:
+        C.check(C.lib().hbem_set_option(b"singular_table", 1))
+    for ta, tb in zip(a, b):
+        for x, y in zip(ta, tb):
+            assert rel(x, y) <= 1e-14

@@ -1,0 +1,44 @@
+"""The plain search's Newton rounds with speculative bisection points against the
+same search without them: the same roots, the same grid, the same evaluation
+count (speculation only changes which round a value is computed in)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+from helmholtzbem_gb300 import api, geometry, _capi as C  # noqa: E402
+from helmholtzbem_gb300._capi import check  # noqa: E402
+
+
+def _both(so, *args, **kw):
+    check(C.lib().hbem_set_option(b"plain_speculate", 1))
+    fast = so.find_resonances_plain(*args, **kw)
+    check(C.lib().hbem_set_option(b"plain_speculate", 0))
+    try:
+        slow = so.find_resonances_plain(*args, **kw)
+    finally:
+        check(C.lib().hbem_set_option(b"plain_speculate", 1))
+    return fast, slow
+
+
+@pytest.mark.parametrize("N,c_i,npoints", [(50, 23.4, 200), (40, 9.0, 120), (24, 23.4, 64)])
+def test_speculative_newton_matches_plain_rounds(N, c_i, npoints):
+    so = api.SolutionsOperator(api.BuilderData(geometry.circle(0.25, N), order=11))
+    (r1, g1, n1), (r0, g0, n0) = _both(so, 0.5, 10.0, npoints, 1.0, c_i, tol=1e-8)
+    assert r0.size > 0
+    assert r1.size == r0.size
+    # sigma at a wavenumber does not depend on the batch it was computed in, so each
+    # candidate's iterates agree (to rounding of the batched evaluation)
+    assert np.max(np.abs(r1 - r0)) <= 1e-10
+    assert n1 == n0
+    assert np.array_equal(np.isnan(g1), np.isnan(g0))
+    assert np.max(np.abs(g1[:, 0] - g0[:, 0]) / g0[:, 0]) <= 1e-13
+    ends = ~np.isnan(g0[:, 1])
+    assert np.max(np.abs(g1[ends, 1] - g0[ends, 1])) <= 1e-10 * max(1.0, np.max(np.abs(g0[ends, 1])))
+
+
+def test_plain_search_repeats():
+    so = api.SolutionsOperator(api.BuilderData(geometry.circle(0.25, 30), order=9))
+    a = so.find_resonances_plain(0.5, 8.0, 96, 1.0, 23.4, tol=1e-8)
+    b = so.find_resonances_plain(0.5, 8.0, 96, 1.0, 23.4, tol=1e-8)
+    assert np.array_equal(a[0], b[0]) and a[2] == b[2] and np.array_equal(a[1], b[1], equal_nan=True)

@@ -59,7 +59,8 @@ cudaError_t arnoldi_batched(int n, int nmat, int count, int D, double tol, int m
                             size_t work_bytes, int* status_host, int* iters_host, cudaStream_t st,
                             long long* launches);
 cudaError_t launch_svd_fast(int n, int nmat, int D, const cplx* T, long long mat_stride, long long der_stride,
-                            double* out, int* status, cudaStream_t st);
+                            double* out, int* status, cudaStream_t st, cplxf* vpool = nullptr,
+                            const int* warm_slot = nullptr, const int* out_slot = nullptr);
 }  // namespace hbem
 
 using namespace hbem;
@@ -86,6 +87,7 @@ std::atomic<long long> g_asm_split[9];
 int g_svd_fast = 1;           // dense sigma: FP32 Jacobi + FP64 refinement where it fits
 int g_arnoldi_maxit = 1000;   // block iterations of hbem_arnoldi_sv_batch*
 int g_plain_speculate = 1;    // plain search: speculative bisection points in small Newton rounds
+int g_plain_warm_start = 1;   // plain search: dense-kernel Jacobi warm-started from nearby V sets
 int g_singular_table = 1;     // singular pairs read their k-independent point data from a table
 const size_t kSingularTableMax = (size_t)256 << 20;
 
@@ -304,8 +306,11 @@ struct hbem_solop_s {
     int proj = 1;
     std::vector<double> M;    // N x N column-major
     DBuf d_M, d_id, d_sb, d_lr, d_T, d_svdA, d_svdV, d_out, d_status, d_sig;
+    DBuf d_vpool, d_slots;   // FP32 V sets of the dense kernel's warm starts, slot lists
     ~hbem_solop_s() {
-        for (DBuf* x : {&d_M, &d_id, &d_sb, &d_lr, &d_T, &d_svdA, &d_svdV, &d_out, &d_status, &d_sig}) x->release();
+        for (DBuf* x : {&d_M, &d_id, &d_sb, &d_lr, &d_T, &d_svdA, &d_svdV, &d_out, &d_status, &d_sig, &d_vpool,
+                        &d_slots})
+            x->release();
     }
 };
 
@@ -385,6 +390,10 @@ int hbem_set_option(const char* name, int value) {
     }
     if (k == "singular_table") {
         g_singular_table = value ? 1 : 0;
+        return HBEM_OK;
+    }
+    if (k == "plain_warm_start") {
+        g_plain_warm_start = value ? 1 : 0;
         return HBEM_OK;
     }
     if (k == "plain_speculate") {
@@ -750,7 +759,8 @@ int hbem_gen_sol_op_batch_device(hbem_solop s, const double* k_host, int nk, dou
 
 static int sv_batch(cudaStream_t st, int n, int nmat, unsigned d, const cplx* T, long long mat_stride,
                     long long der_stride, DBuf& A, DBuf& V, DBuf& out, DBuf& status, DBuf* sig, double* out_host,
-                    double* sig_all_host) {
+                    double* sig_all_host, cplxf* vpool = nullptr, const int* warm_slot = nullptr,
+                    const int* out_slot = nullptr) {
     const size_t nn = (size_t)n * n;
     HB_CK(V.ensure((size_t)nmat * nn * sizeof(cplx)));
     HB_CK(A.ensure(n > 100 ? (size_t)nmat * nn * sizeof(cplx) : sizeof(cplx)));
@@ -765,7 +775,8 @@ static int sv_batch(cudaStream_t st, int n, int nmat, unsigned d, const cplx* T,
     if (!sig_all_host && g_svd_fast && svd_fast_smem_bytes(n) <= 220 * 1024) {
         // FP32 Jacobi + FP64 refinement; matrices it cannot finish (singular T, a
         // far-field series that does not converge) are redone by the polished kernel
-        HB_CK(launch_svd_fast(n, nmat, (int)d, T, mat_stride, der_stride, out.as<double>(), status.as<int>(), st));
+        HB_CK(launch_svd_fast(n, nmat, (int)d, T, mat_stride, der_stride, out.as<double>(), status.as<int>(), st,
+                              vpool, warm_slot, out_slot));
         g_launches += 1;
         HB_CK(cudaMemcpyAsync(stat.data(), status.p, (size_t)nmat * sizeof(int), cudaMemcpyDeviceToHost, st));
         HB_CK(cudaStreamSynchronize(st));
@@ -1159,6 +1170,48 @@ void count_launches(long long n) { g_launches += n; }
 // throughput, bounds a round, so a few more matrices per round cost little).
 int plain_speculate_ok(hbem_solop s) {
     return s && g_plain_speculate && g_svd_fast && svd_fast_smem_bytes(2 * s->b->n) <= 220 * 1024;
+}
+
+int plain_warm_start_ok() { return g_plain_warm_start; }
+
+// hbem_sweep_sigma through the one-CTA dense kernel with warm starts: a pool of npool
+// FP32 V sets (2N x 2N each) held by the operator; wavenumber i starts its FP32
+// Jacobi from slot warm_slot[i] and leaves its V set in slot out_slot[i] (-1: none).
+// The pool's contents survive between calls while npool does not grow.  Returns
+// HBEM_ERR_UNSUPPORTED when the dense kernel does not take the order or the batch.
+int sweep_sigma_warm(hbem_solop s, const double* k_host, int nk, double c_o, double c_i, unsigned d,
+                     const int* warm_slot, const int* out_slot, int npool, double* out_host) {
+    if (!s || !k_host || !out_host || nk < 1 || d > 2 || npool < 1 || !warm_slot || !out_slot)
+        return fail(HBEM_ERR_INVALID, "sweep_sigma_warm: bad argument");
+    hbem_builder b = s->b;
+    const int n = 2 * b->n;
+    const size_t mat = (size_t)n * n;
+    if (!g_svd_fast || svd_fast_smem_bytes(n) > 220 * 1024 || (size_t)nk * (d + 1) * mat * sizeof(cplx) > ((size_t)2 << 30))
+        return fail(HBEM_ERR_UNSUPPORTED, "sweep_sigma_warm: the dense fast kernel does not take this batch");
+    for (int i = 0; i < nk; ++i)
+        if (warm_slot[i] >= npool || out_slot[i] >= npool)
+            return fail(HBEM_ERR_INVALID, "sweep_sigma_warm: slot outside the pool");
+    HB_CK(cudaSetDevice(b->device));
+    const size_t pool_bytes = (size_t)npool * mat * sizeof(cplxf);
+    if (pool_bytes > s->d_vpool.cap) {
+        DBuf grown;
+        HB_CK(grown.ensure(pool_bytes));
+        if (s->d_vpool.p) {
+            HB_CK(cudaMemcpyAsync(grown.p, s->d_vpool.p, s->d_vpool.cap, cudaMemcpyDeviceToDevice, b->st));
+            HB_CK(cudaStreamSynchronize(b->st));
+        }
+        s->d_vpool.release();
+        s->d_vpool = grown;
+    }
+    std::vector<int> slots(2 * (size_t)nk);
+    std::copy(warm_slot, warm_slot + nk, slots.begin());
+    std::copy(out_slot, out_slot + nk, slots.begin() + nk);
+    HB_CK(upload(s->d_slots, slots, b->st));
+    HB_CK(s->d_T.ensure((size_t)nk * (d + 1) * mat * sizeof(cplx)));
+    if (int r = gen_T_batch(s, k_host, nullptr, nk, c_o, c_i, d, s->d_T.as<cplx>())) return r;
+    return sv_batch(b->st, n, nk, d, s->d_T.as<cplx>(), (long long)(d + 1) * mat, (long long)mat, s->d_svdA,
+                    s->d_svdV, s->d_out, s->d_status, nullptr, out_host, nullptr, s->d_vpool.as<cplxf>(),
+                    s->d_slots.as<int>(), s->d_slots.as<int>() + nk);
 }
 
 }  // namespace hbem

@@ -59,17 +59,45 @@ __device__ __forceinline__ float warp_sumf(float x) {
 // Each column pair of a round-robin step is handled by a group of G lanes (G = 8 for
 // n <= 128: the 64 groups of a 512-thread CTA take a whole step at once, with
 // 3-level shuffle reductions), G = 32 for larger n.
+//
+// Warm start (Vw != null, n x n unitary to FP32 working precision, typically the V32
+// of a nearby wavenumber): the sweeps start from A = T Vw, V = Vw instead of A = T,
+// V = I.  The stopping rule is the same, so the result has the cold start's accuracy;
+// when T Vw is nearly column-orthogonal far fewer sweeps are needed.  rowbuf: one row
+// of n entries per warp (shared memory).
 template <int G>
-__device__ void jacobi_fp32_g(const cplx* T0, int n, cpf* A32, cpf* V32, int* s_rot) {
+__device__ void jacobi_fp32_g(const cplx* T0, int n, cpf* A32, cpf* V32, int* s_rot, const cpf* Vw, cpf* rowbuf) {
     const int np = n + (n & 1), m = np - 1;
     const int gl = threadIdx.x % G, grp = threadIdx.x / G, ngrp = blockDim.x / G;
     const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
         cplx t = T0[e];
         A32[e] = mkf((float)t.re, (float)t.im);
-        V32[e] = mkf((e % n) == (e / n) ? 1.f : 0.f, 0.f);
+        V32[e] = Vw ? Vw[e] : mkf((e % n) == (e / n) ? 1.f : 0.f, 0.f);
     }
     __syncthreads();
+    if (Vw) {
+        // A <- A V row by row: each warp copies its row to rowbuf, then its lanes form
+        // the row's entries (only the warp's own row of A is read or written)
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        cpf* rb = rowbuf + (long long)warp * n;
+        for (int i = warp; i < n; i += nw) {
+            for (int c = lane; c < n; c += 32) rb[c] = A32[i + (long long)c * n];
+            __syncwarp();
+            for (int j = lane; j < n; j += 32) {
+                const cpf* vj = V32 + (long long)j * n;
+                float ar = 0.f, ai = 0.f;
+                for (int c = 0; c < n; ++c) {
+                    const cpf a = rb[c], v = vj[c];
+                    ar = fmaf(a.re, v.re, fmaf(-a.im, v.im, ar));
+                    ai = fmaf(a.re, v.im, fmaf(a.im, v.re, ai));
+                }
+                A32[i + (long long)j * n] = mkf(ar, ai);
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+    }
     const float tol = 4e-6f;
     for (int sweep = 0; sweep < 30; ++sweep) {
         if (threadIdx.x == 0) *s_rot = 0;
@@ -124,9 +152,10 @@ __device__ void jacobi_fp32_g(const cplx* T0, int n, cpf* A32, cpf* V32, int* s_
     }
 }
 
-__device__ void jacobi_fp32(const cplx* T0, int n, cpf* A32, cpf* V32, int* s_rot) {
-    if (n <= 128) jacobi_fp32_g<8>(T0, n, A32, V32, s_rot);
-    else jacobi_fp32_g<32>(T0, n, A32, V32, s_rot);
+__device__ void jacobi_fp32(const cplx* T0, int n, cpf* A32, cpf* V32, int* s_rot, const cpf* Vw = nullptr,
+                            cpf* rowbuf = nullptr) {
+    if (n <= 128) jacobi_fp32_g<8>(T0, n, A32, V32, s_rot, Vw, rowbuf);
+    else jacobi_fp32_g<32>(T0, n, A32, V32, s_rot, Vw, rowbuf);
 }
 
 // Stage 2: V = orthonormalised columns of V32 in FP64 (classical Gram-Schmidt; one
@@ -429,6 +458,11 @@ struct SvdFastJob {
     long long mat_stride, der_stride;
     double* out;     // [nmat][3]
     int* status;     // [nmat]
+    // optional pool of n x n FP32 right-singular-vector sets: matrix m starts its FP32
+    // Jacobi from slot warm_slot[m] (>= 0) and stores its V32 in slot out_slot[m] (>= 0)
+    cpf* vpool;
+    const int* warm_slot;
+    const int* out_slot;
 };
 
 struct FastSmem {
@@ -568,13 +602,20 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
     cplx* ab = reinterpret_cast<cplx*>(sb + L.ab);   // a_j, b_j
     cplx *F = vec, *G = vec + n, *f1 = vec + 2 * n, *f2 = vec + 3 * n, *rr = vec + 4 * n, *acc = vec + 5 * n,
          *term = vec + 6 * n, *z2 = vec + 7 * n, *sbuf = vec + 8 * n;
-    __shared__ int s_rot, s_kb, s_im, s_sing, s_conv;
+    __shared__ int s_rot, s_kb, s_im, s_sing, s_conv, s_iters;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const cplx* T0 = J.T + (long long)mat * J.mat_stride;
     double* out = J.out + 3LL * mat;
 
-    // 1. FP32 Jacobi
-    jacobi_fp32(T0, n, A32, V32, &s_rot);
+    // 1. FP32 Jacobi, from the pool's V set of a nearby wavenumber when given
+    const long long nn = (long long)n * n;
+    const int wslot = (J.vpool && J.warm_slot) ? J.warm_slot[mat] : -1;
+    const int oslot = (J.vpool && J.out_slot) ? J.out_slot[mat] : -1;
+    jacobi_fp32(T0, n, A32, V32, &s_rot, wslot >= 0 ? J.vpool + wslot * nn : nullptr, reinterpret_cast<cpf*>(X));
+    if (oslot >= 0) {
+        cpf* dst = J.vpool + oslot * nn;
+        for (long long e = threadIdx.x; e < nn; e += blockDim.x) dst[e] = V32[e];
+    }
     for (int j = warp; j < n; j += nw) {
         float s2 = 0.f;
         for (int i = lane; i < n; i += 32) s2 = fmaf(A32[j * n + i].re, A32[j * n + i].re,
@@ -603,6 +644,32 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
         }
         s_kb = kb;
         s_sing = 0;
+        // Block inverse iterations: the start block's components outside the kb
+        // smallest singular directions shrink by (sigma_1 / sigma_kb+1)^2 per iteration.
+        // Four iterations at a ratio of 1/3 (a factor 3^-8) are the least reduction the
+        // kernel accepts; with a margin of 100 (and the FP32 values' absolute error
+        // 4 eps32 sigma_max added to the ratio) fewer iterations reach it when the
+        // smallest singular value is well separated, as it is near a resonance.
+        int iters = kFastInvIter;
+        if (n > kb) {
+            float smax = 0.f, snext = -1.f;
+            for (int j = 0; j < n; ++j) {
+                smax = fmaxf(smax, sig32[j]);
+                bool used = false;
+                for (int l = 0; l < kb; ++l) used |= idx[l] == j;
+                if (!used && (snext < 0.f || sig32[j] < snext)) snext = sig32[j];
+            }
+            const double err = 4.0 * 1.1920928955078125e-7 * (double)smax;
+            const double lo = (double)snext - err;
+            if (lo > 0.) {
+                const double r = ((double)sig32[idx[0]] + err) / lo;
+                if (r < 1.) {
+                    const double need = log(100.0 * 6561.0) / (2.0 * log(1.0 / r));
+                    iters = min(kFastInvIter, max(1, (int)ceil(need)));
+                }
+            }
+        }
+        s_iters = iters;
     }
     __syncthreads();
     const int kb = s_kb;
@@ -617,7 +684,8 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
     lu_smem(T64, n, piv, red, redi, &s_sing);
     perm_from_piv(piv, n, perm);
     qr_cgs2(X, n, kb, coef, red);
-    for (int it = 0; it < kFastInvIter; ++it) {
+    const int inv_iters = s_iters;
+    for (int it = 0; it < inv_iters; ++it) {
         solve_lu_h_blk(T64, perm, n, X, kb, sbuf);
         solve_lu_blk(T64, perm, n, X, kb, sbuf);
         qr_cgs2(X, n, kb, coef, red);
@@ -800,12 +868,13 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
 }
 
 cudaError_t launch_svd_fast(int n, int nmat, int D, const cplx* T, long long mat_stride, long long der_stride,
-                            double* out, int* status, cudaStream_t st) {
+                            double* out, int* status, cudaStream_t st, cplxf* vpool, const int* warm_slot,
+                            const int* out_slot) {
     const size_t limit = 220 * 1024, smem = svd_fast_smem_bytes(n);
     if (smem > limit || n < 2) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(k_svd_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit);
     if (e != cudaSuccess) return e;
-    SvdFastJob J{n, nmat, D, T, mat_stride, der_stride, out, status};
+    SvdFastJob J{n, nmat, D, T, mat_stride, der_stride, out, status, vpool, warm_slot, out_slot};
     k_svd_fast<<<nmat, kSvdThreads, smem, st>>>(J);
     return cudaGetLastError();
 }

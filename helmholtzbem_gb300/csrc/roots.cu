@@ -22,6 +22,9 @@
 
 namespace hbem {
 int plain_speculate_ok(hbem_solop s);
+int plain_warm_start_ok();
+int sweep_sigma_warm(hbem_solop s, const double* k_host, int nk, double c_o, double c_i, unsigned d,
+                     const int* warm_slot, const int* out_slot, int npool, double* out_host);
 }  // namespace hbem
 
 namespace {
@@ -395,11 +398,20 @@ int opt_subdiv_impl(const BatchEval& f, double x_min, double x_max, int batch, i
 // evals counts the evaluations the search used (unused speculative points excluded).
 constexpr int kSpecRound = 8;
 
-int newton_rounds(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, int& evals) {
+// With warm starts (first_warm != null): candidate c's dense-sigma evaluations start
+// their FP32 Jacobi from the V set of its previous evaluated point, the first from
+// pool slot first_warm[c] (a grid point beside the guess); its main points alternate
+// between its two own slots slot_base + 2c, slot_base + 2c + 1, speculative points
+// only read.
+int newton_rounds(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, int& evals,
+                  const std::vector<int>* first_warm = nullptr, int slot_base = 0) {
     std::vector<std::vector<std::array<double, 3>>> cache(nt.size());   // (k, sigma', sigma'')
     struct Req { size_t cand; bool spec; };
     std::vector<Req> who;
     std::vector<double> xs, out;
+    std::vector<int> cur, wslot, oslot;
+    if (first_warm) cur = *first_warm;
+    const int npool = slot_base + 2 * (int)nt.size();
     for (int round = 0; round < kMaxIt; ++round) {
         // points already evaluated speculatively
         for (size_t c = 0; c < nt.size(); ++c)
@@ -431,7 +443,22 @@ int newton_rounds(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i,
                     }
             }
         out.assign(3 * xs.size(), 0.);
-        if (int r = hbem_sweep_sigma(s, xs.data(), (int)xs.size(), c_o, c_i, 2, out.data())) return r;
+        if (first_warm) {
+            wslot.assign(xs.size(), -1);
+            oslot.assign(xs.size(), -1);
+            for (size_t q = 0; q < who.size(); ++q) {
+                const int c = (int)who[q].cand, own0 = slot_base + 2 * c;
+                wslot[q] = cur[c];
+                if (!who[q].spec) oslot[q] = cur[c] == own0 ? own0 + 1 : own0;
+            }
+            if (int r = hbem::sweep_sigma_warm(s, xs.data(), (int)xs.size(), c_o, c_i, 2, wslot.data(), oslot.data(),
+                                               npool, out.data()))
+                return r;
+            for (size_t q = 0; q < who.size(); ++q)
+                if (!who[q].spec) cur[who[q].cand] = oslot[q];
+        } else if (int r = hbem_sweep_sigma(s, xs.data(), (int)xs.size(), c_o, c_i, 2, out.data())) {
+            return r;
+        }
         for (size_t q = 0; q < who.size(); ++q) {
             const double* o = &out[3 * q];
             if (who[q].spec) {
@@ -625,8 +652,23 @@ int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npo
     const double h = (k_max - k_min) / (npoints - 1);
     for (int i = 0; i < npoints; ++i) ks[i] = k_min + i * h;
     int evals = npoints;
+    // where sigma comes from the one-CTA dense kernel, every evaluation leaves its FP32
+    // V set in a pool slot (grid point i: slot i) and later evaluations near it start
+    // their Jacobi sweeps there
+    bool warm = hbem::plain_speculate_ok(s) && hbem::plain_warm_start_ok();
+    std::vector<int> wslot, oslot;
     // sigma on the grid (randomized_svd::sv / direct::sv at roots_newton_polygon_rsvd.cpp:172-177)
-    if (int r = hbem_sweep_sigma(s, ks.data(), npoints, c_o, c_i, 0, g.data())) return r;
+    if (warm) {
+        wslot.assign(npoints, -1);
+        oslot.resize(npoints);
+        for (int i = 0; i < npoints; ++i) oslot[i] = i;
+        const int r = hbem::sweep_sigma_warm(s, ks.data(), npoints, c_o, c_i, 0, wslot.data(), oslot.data(), npoints,
+                                             g.data());
+        if (r == HBEM_ERR_UNSUPPORTED) warm = false;
+        else if (r) return r;
+    }
+    if (!warm)
+        if (int r = hbem_sweep_sigma(s, ks.data(), npoints, c_o, c_i, 0, g.data())) return r;
     for (int i = 0; i < npoints; ++i) g[3 * i + 1] = g[3 * i + 2] = NAN;
     // 3-point local minima (:185-194)
     std::vector<int> cidx;
@@ -641,12 +683,26 @@ int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npo
         ends[2 * c + 1] = ks[cidx[c] + 2];
     }
     if (!ends.empty()) {
-        if (int r = hbem_sweep_sigma(s, ends.data(), (int)ends.size(), c_o, c_i, 1, der.data())) return r;
+        if (warm) {
+            // the bracket ends are grid points: their own V sets
+            wslot.resize(ends.size());
+            oslot.assign(ends.size(), -1);
+            for (size_t c = 0; c < cidx.size(); ++c) {
+                wslot[2 * c] = cidx[c];
+                wslot[2 * c + 1] = cidx[c] + 2;
+            }
+            if (int r = hbem::sweep_sigma_warm(s, ends.data(), (int)ends.size(), c_o, c_i, 1, wslot.data(),
+                                               oslot.data(), npoints, der.data()))
+                return r;
+        } else if (int r = hbem_sweep_sigma(s, ends.data(), (int)ends.size(), c_o, c_i, 1, der.data())) {
+            return r;
+        }
         evals += (int)ends.size();
     }
     // validation sigma'(left) < 0 < sigma'(right), quartic Hermite model + Brent (:209-245)
     struct Cand { double a, guess; };
     std::vector<Cand> cands;
+    std::vector<int> first_warm;   // grid point beside the guess (its V set starts the first Newton point)
     for (size_t c = 0; c < cidx.size(); ++c) {
         const int i = cidx[c];
         const double d1 = der[3 * (2 * c) + 1], d2 = der[3 * (2 * c + 1) + 1];
@@ -654,6 +710,8 @@ int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npo
         g[3 * (i + 2) + 1] = d2;
         if (!(d1 < 0. && d2 > 0.)) continue;
         cands.push_back(Cand{ks[i], quartic_guess(ks[i], h, g[3 * i], g[3 * (i + 1)], g[3 * (i + 2)], d1, d2, tol)});
+        const double gs = cands.back().guess;
+        first_warm.push_back(gs - ks[i] < 0.5 * h ? i : (gs - ks[i] < 1.5 * h ? i + 1 : i + 2));
     }
     if (grid_host) std::copy(g.begin(), g.end(), grid_host);
     std::vector<Newton> nt(cands.size());
@@ -661,7 +719,7 @@ int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npo
     // lock-step Newton rounds: one batched sigma', sigma'' evaluation per round (with
     // speculative bisection points where the dense sigma is latency bound)
     if (hbem::plain_speculate_ok(s)) {
-        if (int r = newton_rounds(s, nt, c_o, c_i, evals)) return r;
+        if (int r = newton_rounds(s, nt, c_o, c_i, evals, warm ? &first_warm : nullptr, npoints)) return r;
     } else {
         for (int round = 0; round < kMaxIt; ++round) {
             std::vector<double> xs;

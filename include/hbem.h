@@ -66,7 +66,10 @@ int hbem_set_device(int device);
  *   normal products, weights) from a table the builder makes once (up to 256 MB);
  *   0 computes it in the kernel for every wavenumber and medium.
  *   "plain_speculate" (default 1): speculative bisection points in the plain
- *   search's small Newton rounds (hbem_find_resonances_plain).                    */
+ *   search's small Newton rounds (hbem_find_resonances_plain).
+ *   "plain_warm_start" (default 1): in the plain search, the dense kernel's FP32
+ *   Jacobi at a bracket end or Newton point starts from the right singular vectors
+ *   of the nearest wavenumber already evaluated (same stopping rule, fewer sweeps). */
 int hbem_set_option(const char* name, int value);
 
 /* Instrumentation (no counterpart in the reference, which prints std::chrono

@@ -42,3 +42,23 @@ def test_plain_search_repeats():
     a = so.find_resonances_plain(0.5, 8.0, 96, 1.0, 23.4, tol=1e-8)
     b = so.find_resonances_plain(0.5, 8.0, 96, 1.0, 23.4, tol=1e-8)
     assert np.array_equal(a[0], b[0]) and a[2] == b[2] and np.array_equal(a[1], b[1], equal_nan=True)
+
+
+@pytest.mark.parametrize("N,c_i,npoints", [(50, 23.4, 200), (36, 9.0, 96)])
+def test_warm_started_jacobi_matches_cold(N, c_i, npoints):
+    """Bracket ends and Newton points start the dense kernel's FP32 Jacobi from the
+    V set of the nearest evaluated wavenumber: the same roots (the FP64 refinement
+    after the Jacobi stage sets the accuracy, not the start)."""
+    so = api.SolutionsOperator(api.BuilderData(geometry.circle(0.25, N), order=11))
+    check(C.lib().hbem_set_option(b"plain_warm_start", 1))
+    r1, g1, n1 = so.find_resonances_plain(0.5, 10.0, npoints, 1.0, c_i, tol=1e-8)
+    check(C.lib().hbem_set_option(b"plain_warm_start", 0))
+    try:
+        r0, g0, n0 = so.find_resonances_plain(0.5, 10.0, npoints, 1.0, c_i, tol=1e-8)
+    finally:
+        check(C.lib().hbem_set_option(b"plain_warm_start", 1))
+    assert r0.size > 0 and r1.size == r0.size and n1 == n0
+    assert np.max(np.abs(r1 - r0)) <= 1e-10
+    assert np.max(np.abs(g1[:, 0] - g0[:, 0]) / g0[:, 0]) <= 1e-12
+    ends = ~np.isnan(g0[:, 1])
+    assert np.max(np.abs(g1[ends, 1] - g0[ends, 1])) <= 1e-9 * max(1.0, np.max(np.abs(g0[ends, 1])))

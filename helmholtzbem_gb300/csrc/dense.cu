@@ -602,7 +602,7 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
     cplx* ab = reinterpret_cast<cplx*>(sb + L.ab);   // a_j, b_j
     cplx *F = vec, *G = vec + n, *f1 = vec + 2 * n, *f2 = vec + 3 * n, *rr = vec + 4 * n, *acc = vec + 5 * n,
          *term = vec + 6 * n, *z2 = vec + 7 * n, *sbuf = vec + 8 * n;
-    __shared__ int s_rot, s_kb, s_im, s_sing, s_conv, s_iters;
+    __shared__ int s_rot, s_kb, s_im, s_sing, s_conv, s_iters, s_next;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const cplx* T0 = J.T + (long long)mat * J.mat_stride;
     double* out = J.out + 3LL * mat;
@@ -624,24 +624,28 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
         if (lane == 0) sig32[j] = sqrtf(s2);
     }
     __syncthreads();
-    // 2. near block: the kb smallest FP32 singular values (all within 3 sigma_min)
-    if (threadIdx.x == 0) {
-        int i0 = 0;
-        for (int j = 1; j < n; ++j)
-            if (sig32[j] < sig32[i0]) i0 = j;
-        const int kb = min(n, kFastKmax);
-        (void)i0;
-        // selection of the kb smallest (ascending, ties by index)
-        for (int b = 0; b < kb; ++b) {
-            int best = -1;
-            for (int j = 0; j < n; ++j) {
-                bool used = false;
-                for (int l = 0; l < b; ++l) used |= idx[l] == j;
-                if (used) continue;
-                if (best < 0 || sig32[j] < sig32[best]) best = j;
+    // 2. near block: the kb smallest FP32 singular values (ascending, ties by index):
+    // column j goes to position rank(j) when that is below kb; the column of rank kb
+    // (the next singular value) bounds the inverse iterations' convergence below
+    if (threadIdx.x == 0) s_next = -1;
+    __syncthreads();
+    {
+        const int kbs = min(n, kFastKmax);
+        // NaN (non-finite T) sorts as +inf, so the ranks stay a permutation of 0..n-1
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+            const float sj = isnan(sig32[j]) ? INFINITY : sig32[j];
+            int rank = 0;
+            for (int i = 0; i < n; ++i) {
+                const float si = isnan(sig32[i]) ? INFINITY : sig32[i];
+                rank += (si < sj || (si == sj && i < j)) ? 1 : 0;
             }
-            idx[b] = best;
+            if (rank < kbs) idx[rank] = j;
+            if (rank == kbs) s_next = j;   // exactly one column when n > kb
         }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int kb = min(n, kFastKmax);
         s_kb = kb;
         s_sing = 0;
         // Block inverse iterations: the start block's components outside the kb
@@ -651,14 +655,10 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
         // 4 eps32 sigma_max added to the ratio) fewer iterations reach it when the
         // smallest singular value is well separated, as it is near a resonance.
         int iters = kFastInvIter;
-        if (n > kb) {
-            float smax = 0.f, snext = -1.f;
-            for (int j = 0; j < n; ++j) {
-                smax = fmaxf(smax, sig32[j]);
-                bool used = false;
-                for (int l = 0; l < kb; ++l) used |= idx[l] == j;
-                if (!used && (snext < 0.f || sig32[j] < snext)) snext = sig32[j];
-            }
+        if (n > kb && s_next >= 0) {
+            float smax = 0.f;
+            for (int j = 0; j < n; ++j) smax = fmaxf(smax, sig32[j]);
+            const float snext = sig32[s_next];
             const double err = 4.0 * 1.1920928955078125e-7 * (double)smax;
             const double lo = (double)snext - err;
             if (lo > 0.) {
@@ -683,32 +683,37 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
     __syncthreads();
     lu_smem(T64, n, piv, red, redi, &s_sing);
     perm_from_piv(piv, n, perm);
+    // U's diagonal replaced by its reciprocals: the solves below multiply
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const cplx d = T64[k + (long long)k * n];
+        T64[k + (long long)k * n] = norm2(d) > 0. ? cdiv(mk(1.), d) : mk(0.);
+    }
+    __syncthreads();
     qr_cgs2(X, n, kb, coef, red);
     const int inv_iters = s_iters;
-    for (int it = 0; it < inv_iters; ++it) {
-        solve_lu_h_blk(T64, perm, n, X, kb, sbuf);
-        solve_lu_blk(T64, perm, n, X, kb, sbuf);
+    for (int it = 0; it < inv_iters; ++it) {   // Y is free until the Rayleigh-Ritz step
+        solve_lu_h_blk(T64, perm, n, X, kb, sbuf, Y, true);
+        solve_lu_blk(T64, perm, n, X, kb, sbuf, Y, true);
         qr_cgs2(X, n, kb, coef, red);
     }
-    // Rayleigh-Ritz: Y = T X = Q_Y Rf, Rf W = Q_R Sigma
-    for (int r = threadIdx.x; r < n; r += blockDim.x) {
-        cplx a[kFastKmax];
-#pragma unroll
-        for (int j = 0; j < kFastKmax; ++j) a[j] = mk(0.);
-        for (int c = 0; c < n; ++c) {
-            const cplx t = T0[r + (long long)c * n];
-#pragma unroll
-            for (int j = 0; j < kFastKmax; ++j)
-                if (j < kb) cfma(a[j], t, X[c + j * n]);
+    // Rayleigh-Ritz: Y = T X = Q_Y Rf, Rf W = Q_R Sigma.  One thread per entry of Y:
+    // consecutive threads take consecutive rows (coalesced reads of T's columns from
+    // global memory), X's entries are shared-memory broadcasts.
+    for (int e = threadIdx.x; e < n * kb; e += blockDim.x) {
+        const int r = e % n, j = e / n;
+        const cplx* xj = X + (long long)j * n;
+        cplx a0 = mk(0.), a1 = mk(0.);
+        int c = 0;
+        for (; c + 1 < n; c += 2) {
+            cfma(a0, T0[r + (long long)c * n], xj[c]);
+            cfma(a1, T0[r + (long long)(c + 1) * n], xj[c + 1]);
         }
-#pragma unroll
-        for (int j = 0; j < kFastKmax; ++j)
-            if (j < kb) Y[r + j * n] = a[j];
+        if (c < n) cfma(a0, T0[r + (long long)c * n], xj[c]);
+        Y[e] = a0 + a1;
     }
     __syncthreads();
     qr_cgs2(Y, n, kb, coef, red, Rf);
-    if (threadIdx.x < 32) jacobi_warp(Rf, kb, W);
-    __syncthreads();
+    jacobi_cta(Rf, kb, W, &s_rot);
     if (threadIdx.x < kb) {
         double s2 = 0.;
         for (int r = 0; r < kb; ++r) s2 += norm2(Rf[threadIdx.x * kb + r]);
@@ -818,8 +823,8 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
     const double s2 = sg * sg;
     for (int r = threadIdx.x; r < n; r += blockDim.x) { yv[r] = mk(0.); zv[r] = rr[r]; }
     __syncthreads();
-    solve_lu_blk(T64, perm, n, zv, 1, sbuf);                 // z = T^-H T^-1 res
-    solve_lu_h_blk(T64, perm, n, zv, 1, sbuf);
+    solve_lu_blk(T64, perm, n, zv, 1, sbuf, nullptr, true);                 // z = T^-H T^-1 res
+    solve_lu_h_blk(T64, perm, n, zv, 1, sbuf, nullptr, true);
     dots_h(Y, n, nd, zv, coef);
     sub_span(Y, n, nd, coef, zv);
     for (int r = threadIdx.x; r < n; r += blockDim.x) pv[r] = zv[r];
@@ -843,8 +848,8 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
             zv[r] = rr[r];
         }
         __syncthreads();
-        solve_lu_blk(T64, perm, n, zv, 1, sbuf);
-        solve_lu_h_blk(T64, perm, n, zv, 1, sbuf);
+        solve_lu_blk(T64, perm, n, zv, 1, sbuf, nullptr, true);
+        solve_lu_h_blk(T64, perm, n, zv, 1, sbuf, nullptr, true);
         dots_h(Y, n, nd, zv, coef);
         sub_span(Y, n, nd, coef, zv);
         const double rz1 = dot_re(rr, zv, n, red + 64);

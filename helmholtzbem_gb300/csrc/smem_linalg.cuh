@@ -267,6 +267,72 @@ static __device__ void jacobi_warp(cplx* B, int s, cplx* W) {
 }
 
 
+// The same one-sided Jacobi for a square s x s matrix (s <= 32) on the whole CTA:
+// the column pairs of a round-robin step go to different warps (lane r holds row
+// r of both columns), one barrier per step instead of one pair after the other on a
+// single warp.  The reductions are broadcast from lane 0, so every lane applies the
+// same rotation.  flag: one shared int of scratch.
+static __device__ void jacobi_cta(cplx* B, int s, cplx* W, int* flag) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int e = threadIdx.x; e < s * s; e += blockDim.x) W[e] = mk((e % s) == (e / s) ? 1. : 0.);
+    const int sp = s + (s & 1), m = sp - 1, npairs = sp / 2;
+    // a pair counts as orthogonal once |x^H y| <= 2 s eps |x||y|: the computed inner
+    // product of two s-vectors carries rounding of that order, so a tighter test
+    // (1e-15 for s = 12) would keep rotating on noise until the sweep cap
+    const double tol = 2.0 * s * 2.220446049250313e-16;
+    __syncthreads();
+    for (int sweep = 0; sweep < 30; ++sweep) {
+        if (threadIdx.x == 0) *flag = 0;
+        __syncthreads();
+        for (int r = 0; r < m; ++r) {
+            for (int k = warp; k < npairs; k += nw) {
+                // round-robin ("circle") schedule: column 0 fixed, the others rotate
+                int p, q;
+                if (k == 0) { p = 0; q = r + 1; }
+                else { p = (r + k) % m + 1; q = (r - k + m) % m + 1; }
+                if (p >= s || q >= s) continue;
+                if (p > q) { const int t = p; p = q; q = t; }
+                const cplx x = lane < s ? B[p * s + lane] : mk(0.), y = lane < s ? B[q * s + lane] : mk(0.);
+                double al = norm2(x), be = norm2(y);
+                double gr = fma(x.re, y.re, x.im * y.im), gi = fma(x.re, y.im, -x.im * y.re);
+                // rows >= s hold zeros: for s <= 16 the lower half-warp has the sums
+                for (int o = s <= 16 ? 8 : 16; o > 0; o >>= 1) {
+                    al += __shfl_xor_sync(0xffffffffu, al, o);
+                    be += __shfl_xor_sync(0xffffffffu, be, o);
+                    gr += __shfl_xor_sync(0xffffffffu, gr, o);
+                    gi += __shfl_xor_sync(0xffffffffu, gi, o);
+                }
+                al = __shfl_sync(0xffffffffu, al, 0);
+                be = __shfl_sync(0xffffffffu, be, 0);
+                gr = __shfl_sync(0xffffffffu, gr, 0);
+                gi = __shfl_sync(0xffffffffu, gi, 0);
+                // rotation from |g|^2 and one reciprocal square root: shorter dependent
+                // chain than hypot and the divisions by |g|
+                const double g2 = fma(gr, gr, gi * gi);
+                if (g2 == 0. || g2 <= (tol * tol) * (al * be)) continue;
+                if (lane == 0) *flag = 1;
+                const double ig = rsqrt(g2);
+                const double zeta = (be - al) * (0.5 * ig);
+                const double t = (zeta >= 0. ? 1. : -1.) / (fabs(zeta) + sqrt(fma(zeta, zeta, 1.)));
+                const double c = rsqrt(fma(t, t, 1.)), sn = c * t;
+                const cplx eph = mk(gr * ig, -gi * ig);
+                if (lane < s) {
+                    const cplx ey = eph * y;
+                    B[p * s + lane] = c * x - sn * ey;
+                    B[q * s + lane] = sn * x + c * ey;
+                    const cplx wx = W[p * s + lane], wy = eph * W[q * s + lane];
+                    W[p * s + lane] = c * wx - sn * wy;
+                    W[q * s + lane] = sn * wx + c * wy;
+                }
+            }
+            __syncthreads();
+        }
+        if (*flag == 0) break;
+        __syncthreads();
+    }
+}
+
+
 // ---------------------------------------------------------------- blocked solves
 //
 // The same two solves with the row exchanges composed into one permutation
@@ -287,7 +353,19 @@ static __device__ void perm_from_piv(const int* piv, int n, int* perm) {
     __syncthreads();
 }
 
-static __device__ void permute_cols(cplx* X, int n, int s, const int* perm, cplx* buf, bool inverse) {
+static __device__ void permute_cols(cplx* X, int n, int s, const int* perm, cplx* buf, bool inverse,
+                                    cplx* wide = nullptr) {
+    if (wide) {   // all columns in one pass through an n x s scratch
+        for (int e = threadIdx.x; e < n * s; e += blockDim.x) wide[e] = X[e];
+        __syncthreads();
+        for (int e = threadIdx.x; e < n * s; e += blockDim.x) {
+            const int i = e % n, c = e / n;
+            if (!inverse) X[e] = wide[perm[i] + (long long)c * n];
+            else X[perm[i] + (long long)c * n] = wide[e];
+        }
+        __syncthreads();
+        return;
+    }
     for (int c = 0; c < s; ++c) {
         cplx* x = X + (long long)c * n;
         for (int i = threadIdx.x; i < n; i += blockDim.x) buf[i] = x[i];
@@ -300,10 +378,12 @@ static __device__ void permute_cols(cplx* X, int n, int s, const int* perm, cplx
     }
 }
 
-// X <- T^-1 X
-static __device__ void solve_lu_blk(const cplx* A, const int* perm, int n, cplx* X, int s, cplx* buf) {
+// X <- T^-1 X.  wide (optional): n x s scratch for a one-pass row permutation;
+// inv_diag: A's diagonal holds 1 / u_kk (multiplications instead of divisions).
+static __device__ void solve_lu_blk(const cplx* A, const int* perm, int n, cplx* X, int s, cplx* buf,
+                                    cplx* wide = nullptr, bool inv_diag = false) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    permute_cols(X, n, s, perm, buf, false);
+    permute_cols(X, n, s, perm, buf, false, wide);
     for (int b0 = 0; b0 < n; b0 += 32) {                       // L y = P b, L unit lower
         const int bs = min(32, n - b0);
         for (int c = warp; c < s; c += nw) {
@@ -334,7 +414,10 @@ static __device__ void solve_lu_blk(const cplx* A, const int* perm, int n, cplx*
             cplx* x = X + (long long)c * n + b0;
             cplx v = lane < bs ? x[lane] : mk(0.);
             for (int k = bs - 1; k >= 0; --k) {
-                if (lane == k) v = cdiv(v, A[(b0 + k) + (long long)(b0 + k) * n]);
+                if (lane == k) {
+                    const cplx d = A[(b0 + k) + (long long)(b0 + k) * n];
+                    v = inv_diag ? v * d : cdiv(v, d);
+                }
                 cplx vk;
                 vk.re = __shfl_sync(0xffffffffu, v.re, k);
                 vk.im = __shfl_sync(0xffffffffu, v.im, k);
@@ -354,8 +437,9 @@ static __device__ void solve_lu_blk(const cplx* A, const int* perm, int n, cplx*
     }
 }
 
-// X <- T^-H X:  T^H = U^H L^H P, x = P^T L^-H U^-H b
-static __device__ void solve_lu_h_blk(const cplx* A, const int* perm, int n, cplx* X, int s, cplx* buf) {
+// X <- T^-H X:  T^H = U^H L^H P, x = P^T L^-H U^-H b (wide, inv_diag as in solve_lu_blk)
+static __device__ void solve_lu_h_blk(const cplx* A, const int* perm, int n, cplx* X, int s, cplx* buf,
+                                      cplx* wide = nullptr, bool inv_diag = false) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int b0 = 0; b0 < n; b0 += 32) {                       // U^H y = b (lower, diagonal conj(u_kk))
         const int bs = min(32, n - b0);
@@ -363,7 +447,10 @@ static __device__ void solve_lu_h_blk(const cplx* A, const int* perm, int n, cpl
             cplx* x = X + (long long)c * n + b0;
             cplx v = lane < bs ? x[lane] : mk(0.);
             for (int k = 0; k < bs; ++k) {
-                if (lane == k) v = cdiv(v, conj(A[(b0 + k) + (long long)(b0 + k) * n]));
+                if (lane == k) {
+                    const cplx d = conj(A[(b0 + k) + (long long)(b0 + k) * n]);
+                    v = inv_diag ? v * d : cdiv(v, d);
+                }
                 cplx vk;
                 vk.re = __shfl_sync(0xffffffffu, v.re, k);
                 vk.im = __shfl_sync(0xffffffffu, v.im, k);
@@ -407,7 +494,7 @@ static __device__ void solve_lu_h_blk(const cplx* A, const int* perm, int n, cpl
         }
         __syncthreads();
     }
-    permute_cols(X, n, s, perm, buf, true);
+    permute_cols(X, n, s, perm, buf, true, wide);
 }
 
 }  // namespace hbem

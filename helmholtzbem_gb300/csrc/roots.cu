@@ -36,7 +36,7 @@ const int kMaxIt = 1000;
 struct Newton {
     double xl, xh, rts, dx, dxold, f, df, tol;
     int it = 0;
-    bool first = true, done = false, found = false;
+    bool first = true, done = false, found = false, bisected = false;
     void start(double x1, double x2, double guess, double tol_in) {
         // the reference's "initial guess" entry (fct(x1) is NaN): xl = x1, xh = x2
         xl = x1; xh = x2; rts = guess; tol = tol_in;
@@ -56,8 +56,10 @@ struct Newton {
             dxold = dx;
             dx = 0.5 * (xh - xl);
             rts = xl + dx;
+            bisected = true;
             if (std::fabs(xl - rts) < kEps) { finish(true); return; }
         } else {
+            bisected = false;
             dxold = dx;
             dx = f / df;
             double temp = rts;
@@ -389,12 +391,14 @@ int opt_subdiv_impl(const BatchEval& f, double x_min, double x_max, int batch, i
 //
 // The Newton phase of the plain search (examples/roots_newton_polygon_rsvd.cpp:209-265)
 // for candidates whose brackets have been validated.  Every round is one batched
-// sigma', sigma'' evaluation; a round with at most kSpecRound active candidates also
-// evaluates the one or two points a bisection step of rtsafe could move to next
+// sigma', sigma'' evaluation; in a round with at most kSpecRound active candidates,
+// a candidate at its first point or just after a bisection step also has the one or
+// two points a further bisection step of rtsafe could move to evaluated
 // (Newton::bisect_next).  When that step follows, its point is already known and costs
 // no round of its own.  Each candidate is fed exactly the values it would be fed
-// without speculation, so its iterates are unchanged; the rounds are latency bound
-// (one dense-sigma CTA per matrix), so a few more matrices per round cost little.
+// without speculation, so its iterates are unchanged.  A round's cost is a fixed part
+// (one dense-sigma CTA per matrix runs for milliseconds) plus a part per point (the
+// assembly of T, T', T''), so speculation pays where bisection steps run in series.
 // evals counts the evaluations the search used (unused speculative points excluded).
 constexpr int kSpecRound = 8;
 
@@ -432,7 +436,9 @@ int newton_rounds(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i,
         if (xs.empty()) break;
         if (xs.size() <= (size_t)kSpecRound)
             for (size_t c = 0; c < nt.size(); ++c) {
-                if (nt[c].done) continue;
+                // bisection steps come in runs: speculate at the first point and after a
+                // bisection, not after a Newton step (which usually converges on)
+                if (nt[c].done || !(nt[c].first || nt[c].bisected)) continue;
                 cache[c].clear();
                 double sp[2];
                 const int m = nt[c].bisect_next(sp);

@@ -396,9 +396,10 @@ int hbem_sweep_sigma(hbem_solop s, const double* k_host, int nk, double c_o, dou
  * roots_host receives up to max_roots roots, *nroots their count; grid_host
  * (npoints x 3, may be NULL) sigma at every grid point and sigma' at the bracket
  * ends (NaN where not evaluated); *n_evals the number of T(k) evaluated.
- * Where the one-CTA dense sigma kernel takes the order (2N <= 100), Newton rounds
- * with at most 8 active candidates also evaluate the one or two points a bisection
- * step of rtsafe could move to next (option "plain_speculate", default 1); when the
+ * Where the one-CTA dense sigma kernel takes the order (2N <= 100), in Newton
+ * rounds with at most 8 active candidates a candidate at its first point or just
+ * after a bisection step also has the one or two points a further bisection step of
+ * rtsafe could move to evaluated (option "plain_speculate", default 1); when that
  * step follows, its point needs no round of its own.  Every candidate is fed the
  * same values as without speculation, so the roots are the same; *n_evals counts
  * the evaluations the search used (unused speculative points excluded).          */

@@ -17,6 +17,7 @@ namespace hbem {
 struct KConst {
     cplx k, ks, k2ch, ks_inv, ks_two;
     double c, sqrtc;
+    double ks_re_inv, lg_ks;   // real k: 1 / ks, log(ks / 2) + gamma
 };
 
 __device__ __forceinline__ KConst make_kconst(const Job& jb) {
@@ -28,6 +29,8 @@ __device__ __forceinline__ KConst make_kconst(const Job& jb) {
     K.k2ch = 0.5 * (K.ks * K.ks);
     K.ks_inv = cdiv(mk(1.), K.ks);
     K.ks_two = 2.0 * K.ks;
+    K.ks_re_inv = K.ks.re > 0. ? 1.0 / K.ks.re : 0.;
+    K.lg_ks = K.ks.re > 0. ? log(0.5 * K.ks.re) + kEulerGamma : 0.;
     return K;
 }
 
@@ -63,6 +66,19 @@ __device__ __forceinline__ void hankel_at(const KConst& K, double vn, cplx& h0, 
     else hankel01_cplx(vn * K.ks.re, vn * K.ks.im, h0, h1);
 }
 
+// the same with 1/|v| and log|v| given (k-independent point data): for real k the
+// series branch needs neither a division nor a logarithm
+template <bool RK>
+__device__ __forceinline__ void hankel_at_pre(const KConst& K, double vn, double ivn, double lvn, cplx& h0,
+                                              cplx& h1) {
+    if (RK) {
+        if (vn > 0.) hankel01_real_pre(K.ks.re * vn, K.ks_re_inv * ivn, K.lg_ks + lvn, h0, h1);
+        else hankel01_real(0., h0, h1);
+    } else {
+        hankel01_cplx(vn * K.ks.re, vn * K.ks.im, h0, h1);
+    }
+}
+
 // complex scalar times complex, specialised for real ks
 template <bool RK>
 __device__ __forceinline__ cplx kmul(cplx a, cplx z) { return RK ? a.re * z : a * z; }
@@ -74,10 +90,11 @@ struct KVals {
 };
 
 template <int D, bool RK>
-__device__ __forceinline__ KVals<D, RK> kernel_values(const KConst& K, double vn, double vn2, cplx h0, cplx h1) {
+__device__ __forceinline__ KVals<D, RK> kernel_values(const KConst& K, double vn, double vn2, double ivn, cplx h0,
+                                                      cplx h1) {
     KVals<D, RK> kv;
     kv.s[0] = h0;
-    kv.d[0] = vn > 0. ? kmul<RK>(K.ks, (1.0 / vn) * h1) : mk(0.);
+    kv.d[0] = vn > 0. ? kmul<RK>(K.ks, ivn * h1) : mk(0.);
     if (D > 0) {
         cplx hv = vn * h1;
         kv.s[1] = hv;
@@ -377,7 +394,7 @@ __global__ void __launch_bounds__(128) k_general(DevMesh M, const Job* jobs, cpl
             const double vn2 = norm2(v), vn = sqrt(vn2);
             cplx h0, h1;
             hankel_at<RK>(K, vn, h0, h1);
-            const KVals<D, RK> kv = kernel_values<D, RK>(K, vn, vn2, h0, h1);
+            const KVals<D, RK> kv = kernel_values<D, RK>(K, vn, vn2, vn > 0. ? 1.0 / vn : 0., h0, h1);
             double wm[4];
             mom_weights(wa * sw[b], s, sx[b], wm);
             acc_s<D, RK, CURVED>(A, wm, kv, 2. * (ti.im * tj.im + ti.re * tj.re), !tz);
@@ -433,6 +450,8 @@ __device__ __forceinline__ void singular_fields(const DevMesh& M, const Singular
     f[5] = (T.kind == PK_COINC ? xb : xa) * wab;
     f[6] = P.x;
     f[7] = P.y;
+    f[8] = f[1] > 0. ? 1.0 / f[1] : 0.;
+    f[9] = f[1] > 0. ? log(f[1]) : 0.;
 }
 
 // Tabulate singular_fields for every task, set and point: [task][set][field][point].
@@ -458,8 +477,8 @@ __device__ __forceinline__ void singular_accumulate(Acc<D, CURVED>& A, const KCo
                                                     int Kset, const double* f) {
     const double vn2 = f[0], vn = f[1];
     cplx h0, h1;
-    hankel_at<RK>(K, vn, h0, h1);
-    const KVals<D, RK> kv = kernel_values<D, RK>(K, vn, vn2, h0, h1);
+    hankel_at_pre<RK>(K, vn, f[8], f[9], h0, h1);
+    const KVals<D, RK> kv = kernel_values<D, RK>(K, vn, vn2, f[8], h0, h1);
     double wm[4];
     if (kind == PK_COINC) {
         // one point serves both triangles: set 0 has (x, y) = (s, t), set 1 (t, s);

@@ -55,9 +55,10 @@ struct DevMesh {
 };
 
 // k-independent data of one composite quadrature point of a singular pair:
-//   coincident (set 0 serves both triangles): |v|^2, |v|, 2 tau_i.tau_j, dl0, dl1, w, s, t
-//   adjacent (set K):                         |v|^2, |v|, 2 tau_i.tau_j, dl, dlt, w, x, y
-constexpr int kSGeoFields = 8;
+//   coincident (set 0 serves both triangles): |v|^2, |v|, 2 tau_i.tau_j, dl0, dl1, w, s, t,
+//   adjacent (set K):                         |v|^2, |v|, 2 tau_i.tau_j, dl, dlt, w, x, y,
+// then 1/|v| and log|v| for both (0 where |v| = 0)
+constexpr int kSGeoFields = 10;
 
 // one (k, c) job
 struct Job {

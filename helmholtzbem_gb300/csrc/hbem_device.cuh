@@ -140,7 +140,11 @@ __device__ __forceinline__ double horner_pq(const double* c, double w) {
     return r;
 }
 
-static __device__ __noinline__ void hankel01_real(double x, cplx& h0, cplx& h1) {
+// PRE: the caller supplies ix = 1/x and lg = log(x/2) + gamma (the assembly has them
+// from k-independent tables: log(x/2) = log(k sqrt(c)/2) + log|v|), which saves the
+// logarithm and the division of the ascending-series branch.
+template <bool PRE>
+static __device__ __forceinline__ void hankel01_real_t(double x, double ix_in, double lg_in, cplx& h0, cplx& h1) {
     double j0, j1, y0, y1;
     if (x <= 0.) {
         h0 = mk(1., 0.); h1 = mk(0., 0.);
@@ -148,8 +152,8 @@ static __device__ __noinline__ void hankel01_real(double x, cplx& h0, cplx& h1) 
     }
     if (x < 1e-8) {
         j0 = 1.; j1 = 0.5 * x;
-        y0 = (2. / kPi) * (log(j1) + kEulerGamma);
-        y1 = -(2. / kPi) / x;
+        y0 = (2. / kPi) * (PRE ? lg_in : (log(j1) + kEulerGamma));
+        y1 = PRE ? -(2. / kPi) * ix_in : -(2. / kPi) / x;
     } else if (x < 8.) {
         const double mx2_4 = -0.25 * x * x;
         double t = 1.;
@@ -164,13 +168,13 @@ static __device__ __noinline__ void hankel01_real(double x, cplx& h0, cplx& h1) 
             y1 = fma(-HBEM_SER_HK1[k], t, y1);
             if ((__double2hiint(t) & 0x7fffffff) < ((1023 - 55) << 20)) break;
         }
-        const double ix = 1.0 / x;
+        const double ix = PRE ? ix_in : 1.0 / x;
         j1 *= 0.5 * x;
-        double lg = log(0.5 * x) + kEulerGamma;
+        const double lg = PRE ? lg_in : log(0.5 * x) + kEulerGamma;
         y0 = (2. / kPi) * fma(lg, j0, y0);
         y1 = (1. / kPi) * (y1 * x + 2.0 * (lg * j1 + (j0 - 2.0) * ix));
     } else if (x <= 1e6) {
-        double ix = 1.0 / x, w = 64. * ix * ix;
+        double ix = PRE ? ix_in : 1.0 / x, w = 64. * ix * ix;
         double P0 = 1. + horner_pq(HBEM_F0, w);
         double Q0 = (horner_pq(HBEM_G0, w) - 0.125) * ix;
         double P1 = 1. + horner_pq(HBEM_F1, w);
@@ -191,6 +195,15 @@ static __device__ __noinline__ void hankel01_real(double x, cplx& h0, cplx& h1) 
     }
     h0 = mk(j0, y0);
     h1 = mk(j1, y1);
+}
+
+static __device__ __noinline__ void hankel01_real(double x, cplx& h0, cplx& h1) {
+    hankel01_real_t<false>(x, 0., 0., h0, h1);
+}
+
+// x > 0 with ix = 1/x and lg = log(x/2) + gamma given
+static __device__ __noinline__ void hankel01_real_pre(double x, double ix, double lg, cplx& h0, cplx& h1) {
+    hankel01_real_t<true>(x, ix, lg, h0, h1);
 }
 
 // ---------------------------------------------------------------- complex argument

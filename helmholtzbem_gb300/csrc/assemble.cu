@@ -357,6 +357,7 @@ __global__ void k_flags_singular(DevMesh M, const SingularTask* tasks, uint8_t* 
 
 // ------------------------------------------------------------------ local-block kernels
 
+// General pairs, one thread per pair.
 template <int D, bool RK, bool CURVED>
 __global__ void __launch_bounds__(128) k_general(DevMesh M, const Job* jobs, cplx* loc, long long npair) {
     __shared__ double sx[64], sw[64];
@@ -406,6 +407,73 @@ __global__ void __launch_bounds__(128) k_general(DevMesh M, const Job* jobs, cpl
     const cplx t0i = tgi[0], t0j = tgj[0];
     store_local<D, CURVED>(A, K, false, false, tni[0] * tnj[0], 2. * (t0i.im * t0j.im + t0i.re * t0j.re), tz,
                            loc + ((long long)job * npair + pid) * (D + 1) * kLocPerD);
+}
+
+template <int D, bool RK, bool CURVED>
+__global__ void __launch_bounds__(128) k_general_w(DevMesh M, const Job* jobs, cplx* loc, long long npair, int ppw) {
+    __shared__ double sx[64], sw[64];
+    for (int t = threadIdx.x; t < M.p; t += blockDim.x) { sx[t] = M.xg[t]; sw[t] = M.wg[t]; }
+    __syncthreads();
+    // k_general with one warp per pair, its lanes over the p x p Gauss points: for
+    // launches with few pairs x media (the Newton rounds of a small scatterer) a thread
+    // per pair leaves most of the GPU idle.  Each warp takes ppw consecutive pairs.
+    const int lane = threadIdx.x & 31;
+    const long long nlow = (long long)M.n * (M.n - 1) / 2;   // strictly lower pairs
+    const long long q0 = (blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5)) * ppw;
+    if (q0 >= nlow) return;   // whole warp
+    const int job = blockIdx.y;
+    const KConst K = make_kconst(jobs[job]);
+    const int p = M.p;
+    for (long long q = q0; q < q0 + ppw && q < nlow; ++q) {
+        long long i = (long long)((1.0 + sqrt(8.0 * (double)q + 1.0)) * 0.5);
+        while (i * (i - 1) / 2 > q) --i;
+        while ((i + 1) * i / 2 <= q) ++i;
+        const long long j = q - i * (i - 1) / 2;
+        const long long pid = tri_index(i, j);
+        const uint8_t fl = M.flags[pid];
+        if (fl & 0x80) continue;   // coincident / adjacent: singular kernel (whole warp)
+        const bool use_dl = !(fl & PF_DL0_ZERO), use_dlt = !(fl & PF_DLT0_ZERO), tz = (fl & PF_TDT0_ZERO) != 0;
+        const cplx* pti = M.gpt + i * p;
+        const cplx* ptj = M.gpt + j * p;
+        const cplx* tgi = M.gtan + i * p;
+        const cplx* tgj = M.gtan + j * p;
+        const double* tni = M.gtn + i * p;
+        const double* tnj = M.gtn + j * p;
+        Acc<D, CURVED> A;
+        A.zero();
+        for (int e = lane; e < p * p; e += 32) {
+            const int a = e / p, b = e - a * p;
+            const cplx xi = pti[a], ti = tgi[a];
+            const double tin = tni[a], s = sx[a], wa = sw[a];
+            const cplx yj = ptj[b], tj = tgj[b];
+            const double tjn = tnj[b];
+            const cplx v = xi - yj;
+            const double vn2 = norm2(v), vn = sqrt(vn2);
+            cplx h0, h1;
+            hankel_at<RK>(K, vn, h0, h1);
+            const KVals<D, RK> kv = kernel_values<D, RK>(K, vn, vn2, vn > 0. ? 1.0 / vn : 0., h0, h1);
+            double wm[4];
+            mom_weights(wa * sw[b], s, sx[b], wm);
+            acc_s<D, RK, CURVED>(A, wm, kv, 2. * (ti.im * tj.im + ti.re * tj.re), !tz);
+            // general: zero test on v x tau_j before the norm (galerkin_builder.cpp:475-499)
+            if (use_dl) acc_dl<D, RK, CURVED>(A, wm, kv, (v.re * tj.im - v.im * tj.re) * tin);
+            if (use_dlt) acc_dlt<D, RK, CURVED>(A, wm, kv, (v.im * ti.re - v.re * ti.im) * tjn);
+        }
+        constexpr int NV = (int)(sizeof(Acc<D, CURVED>) / sizeof(double));
+        double* av = reinterpret_cast<double*>(&A);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            double x = av[v];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            av[v] = x;
+        }
+        if (lane == 0) {
+            const cplx t0i = tgi[0], t0j = tgj[0];
+            store_local<D, CURVED>(A, K, false, false, tni[0] * tnj[0], 2. * (t0i.im * t0j.im + t0i.re * t0j.re),
+                                   tz, loc + ((long long)job * npair + pid) * (D + 1) * kLocPerD);
+        }
+    }
 }
 
 template <class AccT>
@@ -709,8 +777,18 @@ static cudaError_t launch_local_c(const DevMesh& M, const SingularTask* tasks, i
     long long npair = (long long)M.n * (M.n + 1) / 2;
     long long nlow = (long long)M.n * (M.n - 1) / 2;
     if (nlow > 0) {
-        dim3 g((unsigned)((nlow + 127) / 128), njobs);
-        k_general<D, RK, CURVED><<<g, 128, 0, st>>>(M, jobs, loc, npair);
+        if (nlow * njobs >= 152LL * 16 * 32) {
+            // enough pairs x media for a thread per pair to fill the GPU
+            dim3 g((unsigned)((nlow + 127) / 128), njobs);
+            k_general<D, RK, CURVED><<<g, 128, 0, st>>>(M, jobs, loc, npair);
+        } else {
+            // few: a warp per pair, ppw pairs per warp keeping ~8k warps in the launch
+            const long long want = std::max(1LL, nlow * njobs / 8192);
+            const int ppw = (int)std::min(16LL, want);
+            const long long per_cta = 4LL * ppw;
+            dim3 g((unsigned)((nlow + per_cta - 1) / per_cta), njobs);
+            k_general_w<D, RK, CURVED><<<g, 128, 0, st>>>(M, jobs, loc, npair, ppw);
+        }
     }
     if (ntasks > 0) {
         constexpr int NV = (int)(sizeof(Acc<D, CURVED>) / sizeof(double));

@@ -8,6 +8,13 @@ with, in w = 64/x^2 in (0, 1],
 F*, G* polynomials of degree DEG (least squares on Chebyshev points, samples from
 mpmath at 40 digits), evaluated by Horner's rule.  Absolute error < 3e-18 on (0,1].
 
+For 2 <= x < 8 the device evaluates J0, Y0, J1, Y1 by Taylor polynomials of degree
+TAY_DEG about the centres 2.25, 2.75, ..., 7.75 (|x - centre| <= 1/4).  The
+coefficients f^(m)(c)/m! come from the derivative rule
+    Z_nu^(m)(x) = 2^-m sum_k (-1)^k C(m, k) Z_(nu - m + 2k)(x)
+at 40 digits.  Truncation: below (1/4)^18/18! for J and (1/9)^18 relative for Y (whose
+Taylor radius about c is c >= 2.25); the series' cancellation for 4 <= x < 8 is gone.
+
 Usage (from the repository root):
     python helmholtzbem_gb300/csrc/gen_hankel_tables.py > helmholtzbem_gb300/csrc/hankel_tables.h
 """
@@ -64,6 +71,33 @@ def main():
         print("static __device__ __constant__ double %s[%d] = {" % (name, ser_n + 1))
         print(",\n".join("  %.17e" % v for v in vals_))
         print("};")
+    taylor_tables()
+
+
+TAY_X0, TAY_W, TAY_N, TAY_DEG = 2, 0.5, 12, 17
+
+
+def taylor_tables():
+    """HBEM_TAY[i][m][f]: coefficient of (x - c_i)^m, c_i = 2.25 + i/2, for f = J0, Y0,
+    J1, Y1 (global memory: the interval differs from lane to lane)."""
+    print("#define HBEM_TAY_N %d" % TAY_N)
+    print("#define HBEM_TAY_DEG %d" % TAY_DEG)
+    print("static __device__ __align__(16) const double HBEM_TAY[%d][%d][4] = {" % (TAY_N, TAY_DEG + 1))
+    blocks = []
+    for i in range(TAY_N):
+        c = mp.mpf(TAY_X0) + mp.mpf(TAY_W) * i + mp.mpf(TAY_W) / 2
+        rows = []
+        for m in range(TAY_DEG + 1):
+            vals = []
+            for fn, nu in ((mp.besselj, 0), (mp.bessely, 0), (mp.besselj, 1), (mp.bessely, 1)):
+                d = mp.mpf(0)
+                for k in range(m + 1):
+                    d += (-1) ** k * mp.binomial(m, k) * fn(nu - m + 2 * k, c)
+                vals.append(d / (mp.mpf(2) ** m * mp.factorial(m)))
+            rows.append("  {" + ", ".join("%.17e" % float(v) for v in vals) + "}")
+        blocks.append(" {\n" + ",\n".join(rows) + "}")
+    print(",\n".join(blocks))
+    print("};")
 
 
 if __name__ == "__main__":

@@ -129,7 +129,10 @@ constexpr double kPi = 3.14159265358979323846;
 // reference's vectorised evaluator (Hankel1Real01::jy_01, cbessel.cpp:1858-1997):
 //   x <= 0        J0 = 1, everything else 0
 //   x < 1e-8      limiting forms (DLMF 10.7.2-4)
-//   x < 8         ascending series with harmonic numbers (DLMF 10.8.1-2)
+//   x < 2         ascending series with harmonic numbers (DLMF 10.8.1-2)
+//   2 <= x < 8    Taylor polynomials of degree 17 about 2.25, 2.75, ..., 7.75
+//                 (the reference uses the series up to 8; the polynomials avoid its
+//                 cancellation and cost a quarter of its operations there)
 //   x <= 1e6      modulus/phase amplitudes P, Q in w = 64/x^2 (DLMF 10.17),
 //                 phases through sin x +- cos x so the argument is used exactly
 //   x > 1e6       leading-order asymptotic form (DLMF 10.17.3, first term)
@@ -154,6 +157,23 @@ static __device__ __forceinline__ void hankel01_real_t(double x, double ix_in, d
         j0 = 1.; j1 = 0.5 * x;
         y0 = (2. / kPi) * (PRE ? lg_in : (log(j1) + kEulerGamma));
         y1 = PRE ? -(2. / kPi) * ix_in : -(2. / kPi) / x;
+    } else if (x >= 2. && x < 8.) {
+        // Taylor polynomials about the centre of the x's quarter-width interval
+        // (coefficients from mpmath; no logarithm, no division)
+        const int iv = min(HBEM_TAY_N - 1, (int)((x - 2.) * 2.));
+        const double h = x - (2.25 + 0.5 * iv);
+        const double2* c = reinterpret_cast<const double2*>(&HBEM_TAY[iv][0][0]);
+        double2 a = __ldg(c + 2 * HBEM_TAY_DEG), b = __ldg(c + 2 * HBEM_TAY_DEG + 1);
+        j0 = a.x; y0 = a.y; j1 = b.x; y1 = b.y;
+#pragma unroll
+        for (int m = HBEM_TAY_DEG - 1; m >= 0; --m) {
+            a = __ldg(c + 2 * m);
+            b = __ldg(c + 2 * m + 1);
+            j0 = fma(j0, h, a.x);
+            y0 = fma(y0, h, a.y);
+            j1 = fma(j1, h, b.x);
+            y1 = fma(y1, h, b.y);
+        }
     } else if (x < 8.) {
         const double mx2_4 = -0.25 * x * x;
         double t = 1.;

@@ -366,6 +366,9 @@ __global__ void __launch_bounds__(128) k_general(DevMesh M, const Job* jobs, cpl
     long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     long long nlow = (long long)M.n * (M.n - 1) / 2;   // strictly lower pairs
     if (q >= nlow) return;
+    // neighbouring threads take pairs of similar panel distance, so a warp's lanes
+    // mostly follow the same Hankel branch and series length
+    if (M.gorder) q = M.gorder[q];
     long long i = (long long)((1.0 + sqrt(8.0 * (double)q + 1.0)) * 0.5);
     while (i * (i - 1) / 2 > q) --i;
     while ((i + 1) * i / 2 <= q) ++i;

@@ -51,6 +51,7 @@ struct DevMesh {
     const double* gtn;        // [n][p] tangent norms
     const cplx* ends;         // [n][2] start/end (the [-1,1] map at -1/+1)
     const uint8_t* flags;     // [n(n+1)/2] per lower-triangle pair
+    const int* gorder = nullptr;   // [n(n-1)/2] strictly-lower pairs by distance (thread-per-pair order), or null
     const double* sgeo = nullptr;   // [ntasks][2][kSGeoFields][nc*nc] singular-pair point data, or null
 };
 

@@ -272,6 +272,7 @@ struct hbem_builder_s {
     DBuf d_kind, d_par, d_xg, d_wg, d_xc, d_wc, d_gpt, d_gtan, d_gtn, d_ends, d_flags, d_tasks;
     DBuf d_loc, d_jobs, d_layers;
     DBuf d_sgeo;   // k-independent point data of the singular pairs (when within kSingularTableMax)
+    DBuf d_gorder; // strictly-lower pair indices sorted by panel-midpoint distance
     int asm_layers = 0, asm_d = -1, asm_rows = 0, asm_cols = 0;
 
     long long npair() const { return (long long)n * (n + 1) / 2; }
@@ -284,6 +285,7 @@ struct hbem_builder_s {
         M.gpt = d_gpt.as<cplx>(); M.gtan = d_gtan.as<cplx>(); M.gtn = d_gtn.as<double>();
         M.ends = d_ends.as<cplx>(); M.flags = d_flags.as<uint8_t>();
         M.sgeo = g_singular_table ? d_sgeo.as<double>() : nullptr;
+        M.gorder = d_gorder.as<int>();
         return M;
     }
     // BuilderData::is_adjacent (galerkin_builder.cpp:189-201)
@@ -295,7 +297,7 @@ struct hbem_builder_s {
     }
     ~hbem_builder_s() {
         for (DBuf* b : {&d_kind, &d_par, &d_xg, &d_wg, &d_xc, &d_wc, &d_gpt, &d_gtan, &d_gtn, &d_ends, &d_flags,
-                        &d_tasks, &d_loc, &d_jobs, &d_layers, &d_sgeo})
+                        &d_tasks, &d_loc, &d_jobs, &d_layers, &d_sgeo, &d_gorder})
             b->release();
         if (st) cudaStreamDestroy(st);
     }
@@ -485,6 +487,21 @@ int hbem_builder_create(int npanels, const int* kinds, const double* params, int
     if (e == cudaSuccess) e = upload(b->d_tasks, b->tasks, b->st);
     if (e == cudaSuccess) e = launch_flags(b->view(), b->d_tasks.as<SingularTask>(), (int)b->tasks.size(),
                                            b->d_flags.as<uint8_t>(), b->st);
+    // general pairs in order of the distance between their panels' middle Gauss points
+    // (ties by index): the thread-per-pair kernel's warps then see similar distances
+    if (e == cudaSuccess && n > 1 && (long long)n * (n - 1) / 2 < (1LL << 31)) {
+        const long long nlow = (long long)n * (n - 1) / 2;
+        std::vector<float> key((size_t)nlow);
+        std::vector<int> ord((size_t)nlow);
+        for (long long i = 1, q = 0; i < n; ++i)
+            for (long long j = 0; j < i; ++j, ++q) {
+                const cplx a = gpt[(size_t)i * p + p / 2], c = gpt[(size_t)j * p + p / 2];
+                key[(size_t)q] = (float)std::hypot(a.re - c.re, a.im - c.im);
+                ord[(size_t)q] = (int)q;
+            }
+        std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return key[(size_t)x] < key[(size_t)y]; });
+        e = upload(b->d_gorder, ord, b->st);
+    }
     const size_t geo_bytes = singular_geo_bytes(b->nc, (int)b->tasks.size());
     if (e == cudaSuccess && geo_bytes > 0 && geo_bytes <= kSingularTableMax) {
         e = b->d_sgeo.ensure(geo_bytes);

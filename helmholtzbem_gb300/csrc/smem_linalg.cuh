@@ -230,7 +230,9 @@ static __device__ void jacobi_warp(cplx* B, int s, cplx* W) {
     const int r = threadIdx.x & 31;
     for (int e = r; e < s * s; e += 32) W[e] = mk((e % s) == (e / s) ? 1. : 0.);
     __syncwarp();
-    const double tol = 1e-15;
+    // orthogonal once |x^H y| <= 2 s eps |x||y|, the rounding level of the computed
+    // inner product (a tighter test keeps rotating on noise up to the sweep cap)
+    const double tol = 2.0 * s * 2.220446049250313e-16;
     for (int sweep = 0; sweep < 30; ++sweep) {
         int rotated = 0;
         for (int p = 0; p < s - 1; ++p)

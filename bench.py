@@ -767,10 +767,12 @@ def run_gpu(args):
     peak = fp64_peak_tflops()
     roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak if peak else None,
-                # DRAM bytes (read + write) per assembly launch, averaged over the 28
-                # k_singular / k_general launches of one plain search of this workload
-                # (ncu dram__bytes_read.sum + dram__bytes_write.sum)
-                "traffic": 2.72e6, "traffic_unit": "bytes per launch",
+                # DRAM bytes (read + write) per assembly launch, averaged over the 24
+                # k_singular / k_general(_w) launches of one plain search of this workload
+                # (ncu dram__bytes_read.sum + dram__bytes_write.sum, caches flushed
+                # between launches): the singular launches read the 68 MB point table,
+                # the grid's general launch writes 63 MB of pair blocks
+                "traffic": 3.0e7, "traffic_unit": "bytes per launch",
                 "peak_source": "measured: cuBLAS DGEMM 8192^3 on this GPU (MEASURED_PEAKS.json has no FP64 entry)",
                 "kernel": "k_general + k_singular (panel-pair assembly)", "launches": asm_l.value,
                 "avg_launch_ms": asm_ms.value / max(1, asm_l.value)}

@@ -75,11 +75,13 @@ struct ArnJob {
     int* iters;       // [nmat]
 };
 
-// Ritz step on one warp: Jacobi on the p x p factor Rs (in place: columns s_j z_j),
-// W its right vectors; nrm[j] = s_j^2; ord[0..count) = columns by decreasing s_j.
-static __device__ void arn_ritz(cplx* Rs, cplx* W, int p, int count, double* nrm, int* ord) {
+// Ritz step: Jacobi on the p x p factor Rs (in place: columns s_j z_j), W its right
+// vectors; nrm[j] = s_j^2; ord[0..count) = columns by decreasing s_j.  With flag
+// (a shared int) the Jacobi runs on the whole CTA (jacobi_cta), else on warp 0.
+static __device__ void arn_ritz(cplx* Rs, cplx* W, int p, int count, double* nrm, int* ord, int* flag = nullptr) {
+    if (flag) jacobi_cta(Rs, p, W, flag);
     if (threadIdx.x < 32) {
-        jacobi_warp(Rs, p, W);
+        if (!flag) jacobi_warp(Rs, p, W);
         const int lane = threadIdx.x;
         if (lane < p) {
             double a = 0.;
@@ -179,7 +181,7 @@ __global__ void __launch_bounds__(kArnThreads) k_arn_small(ArnJob J) {
     int* perm = piv + n;                             // n
     int* ord = perm + n;                             // kArnMaxP
     int* redi = ord + kArnMaxP;                      // 32
-    __shared__ int s_sing;
+    __shared__ int s_sing, s_rot;
     if (threadIdx.x == 0) s_sing = 0;
     const cplx* T0 = J.T + (long long)mat * J.mat_stride;
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) A[e] = T0[e];
@@ -192,18 +194,21 @@ __global__ void __launch_bounds__(kArnThreads) k_arn_small(ArnJob J) {
         return;
     }
     perm_from_piv(piv, n, perm);
-    solve_lu_blk(A, perm, n, X, p, buf);
+    // U's diagonal replaced by its reciprocals: the solves multiply
+    for (int k = threadIdx.x; k < n; k += blockDim.x) A[k + (long long)k * n] = cdiv(mk(1.), A[k + (long long)k * n]);
+    __syncthreads();
+    solve_lu_blk(A, perm, n, X, p, buf, nullptr, true);
     qr_cgs2(X, n, p, coef, red);
     int it = 1;
     bool conv = false;
     for (;; ++it) {
         for (int e = threadIdx.x; e < n * p; e += blockDim.x) Y[e] = X[e];
         __syncthreads();
-        solve_lu_h_blk(A, perm, n, Y, p, buf);
+        solve_lu_h_blk(A, perm, n, Y, p, buf, nullptr, true);
         qr_cgs2(Y, n, p, coef, red, Rs);
         __syncthreads();
-        arn_ritz(Rs, W, p, J.count, nrm, ord);
-        solve_lu_blk(A, perm, n, Y, p, buf);
+        arn_ritz(Rs, W, p, J.count, nrm, ord, &s_rot);
+        solve_lu_blk(A, perm, n, Y, p, buf, nullptr, true);
         __syncthreads();
         conv = arn_converged(X, Y, n, p, Rs, W, nrm, ord, J.count, J.tol, red);
         if (conv || it >= J.maxit) break;

@@ -345,9 +345,12 @@ int opt_subdiv_impl(const BatchEval& f, double x_min, double x_max, int batch, i
                     while ((x0 <= x_min || x0 >= x_max) && ++g < 1000);
                     if (x0 <= x_min || x0 >= x_max) x0 = x_min + rng.uniform() * d;
                 }
-                bool near = false;
-                for (auto& q : xy)
-                    if (std::fabs(x0 - q.first) < tol * d) { near = true; break; }
+                // xy holds the previous samples sorted by x: only the two neighbours of
+                // x0 can be within tol d of it (same test as a scan of every sample)
+                auto it = std::lower_bound(xy.begin(), xy.end(), x0,
+                                           [](const std::pair<double, double>& q, double x) { return q.first < x; });
+                bool near = (it != xy.end() && std::fabs(x0 - it->first) < tol * d) ||
+                            (it != xy.begin() && std::fabs(x0 - (it - 1)->first) < tol * d);
                 if (!near) break;
             }
             xt[i] = x0;
@@ -1073,12 +1076,45 @@ int hbem_find_resonances_adaptive(hbem_solop s, double k_min, double k_max, doub
         if (!(g > A[c] && g < B[c])) g = kv[pos];
         G[c] = g;
     }
-    // lock-step Brent searches, one batched evaluation per round (find_resonances.cpp:225-237)
+    // lock-step Brent searches, one batched evaluation per round (find_resonances.cpp:225-237).
+    // With the dense kernel, each candidate's evaluations start the FP32 Jacobi from the
+    // V set of its previous one (pool slots 2c, 2c + 1 alternate; the guess G starts it).
+    const bool warm = n <= 100 && hbem::plain_speculate_ok(s) && hbem::plain_warm_start_ok();
+    std::vector<int> cur(nc, -1), wslot, oslot;
+    const int npool = std::max(1, 2 * (int)nc);
+    auto fine = [&](const std::vector<double>& xs, const std::vector<size_t>& who, bool first, double* ys) {
+        if (!warm) return f_fine(xs.data(), (int)xs.size(), ys);
+        evals += (int)xs.size();
+        wslot.assign(xs.size(), -1);
+        oslot.assign(xs.size(), -1);
+        for (size_t q = 0; q < xs.size(); ++q) {
+            const int c = (int)who[q];
+            if (first) {
+                if (q % 3 == 2) oslot[q] = 2 * c;   // the guess G
+            } else {
+                wslot[q] = cur[c];
+                oslot[q] = cur[c] == 2 * c ? 2 * c + 1 : 2 * c;
+            }
+        }
+        std::vector<double> out(3 * xs.size());
+        if (int r = hbem::sweep_sigma_warm(s, xs.data(), (int)xs.size(), c_o, c_i, 0, wslot.data(), oslot.data(), npool,
+                                           out.data()))
+            return r;
+        for (size_t q = 0; q < xs.size(); ++q) {
+            ys[q] = out[3 * q];
+            if (oslot[q] >= 0) cur[who[q]] = oslot[q];
+        }
+        return (int)HBEM_OK;
+    };
     std::vector<BrentSearch> bs(nc);
     if (nc) {
         std::vector<double> xs(3 * nc), ys(3 * nc);
-        for (size_t c = 0; c < nc; ++c) { xs[3 * c] = A[c]; xs[3 * c + 1] = B[c]; xs[3 * c + 2] = G[c]; }
-        if (int r = f_fine(xs.data(), (int)xs.size(), ys.data())) return r;
+        std::vector<size_t> who(3 * nc);
+        for (size_t c = 0; c < nc; ++c) {
+            xs[3 * c] = A[c]; xs[3 * c + 1] = B[c]; xs[3 * c + 2] = G[c];
+            who[3 * c] = who[3 * c + 1] = who[3 * c + 2] = c;
+        }
+        if (int r = fine(xs, who, true, ys.data())) return r;
         for (size_t c = 0; c < nc; ++c) bs[c].start(A[c], ys[3 * c], B[c], ys[3 * c + 1], G[c], ys[3 * c + 2], tol);
     }
     for (int round = 0; round < 200; ++round) {
@@ -1088,7 +1124,7 @@ int hbem_find_resonances_adaptive(hbem_solop s, double k_min, double k_max, doub
             if (!bs[c].done) { xs.push_back(bs[c].u); who.push_back(c); }
         if (xs.empty()) break;
         std::vector<double> ys(xs.size());
-        if (int r = f_fine(xs.data(), (int)xs.size(), ys.data())) return r;
+        if (int r = fine(xs, who, false, ys.data())) return r;
         for (size_t w = 0; w < who.size(); ++w) bs[who[w]].feed(ys[w]);
     }
     std::vector<double> roots;

@@ -41,7 +41,8 @@ __global__ void __launch_bounds__(kRsvdThreads) k_rsvd_small(RsvdJob J) {
     double* red = reinterpret_cast<double*>(coef + s);   // 128
     int* piv = reinterpret_cast<int*>(red + 128);   // n
     int* redi = piv + n;                            // 32
-    cplx* vb = reinterpret_cast<cplx*>(piv + (n + 32 + 3) / 4 * 4);   // n, 16-byte aligned
+    int* perm = redi + 32;                          // n
+    cplx* vb = reinterpret_cast<cplx*>(piv + (2 * n + 32 + 3) / 4 * 4);   // n, 16-byte aligned
     __shared__ int s_sing;
     if (threadIdx.x == 0) s_sing = 0;
     const cplx* T0 = J.T + (long long)mat * J.mat_stride;
@@ -49,19 +50,26 @@ __global__ void __launch_bounds__(kRsvdThreads) k_rsvd_small(RsvdJob J) {
     for (int e = threadIdx.x; e < n * s; e += blockDim.x) X[e] = J.R[e];
     __syncthreads();
     lu_smem(A, n, piv, red, redi, &s_sing);
+    // blocked solves: rows permuted once, U's diagonal replaced by its reciprocals
+    perm_from_piv(piv, n, perm);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const cplx d = A[k + (long long)k * n];
+        A[k + (long long)k * n] = norm2(d) > 0. ? cdiv(mk(1.), d) : mk(0.);
+    }
+    __syncthreads();
     // Q = qr(T^-1 R)
-    solve_lu(A, piv, n, X, s);
+    solve_lu_blk(A, perm, n, X, s, vb, nullptr, true);
     qr_cgs2(X, n, s, coef, red);
     for (int it = 0; it < J.q; ++it) {
-        solve_lu_h(A, piv, n, X, s);
+        solve_lu_h_blk(A, perm, n, X, s, vb, nullptr, true);
         qr_cgs2(X, n, s, coef, red);
-        solve_lu(A, piv, n, X, s);
+        solve_lu_blk(A, perm, n, X, s, vb, nullptr, true);
         qr_cgs2(X, n, s, coef, red);
     }
     // B = T^-H Q (keep Q in X, B in Y)
     for (int e = threadIdx.x; e < n * s; e += blockDim.x) Y[e] = X[e];
     __syncthreads();
-    solve_lu_h(A, piv, n, Y, s);
+    solve_lu_h_blk(A, perm, n, Y, s, vb, nullptr, true);
     jacobi_thin(Y, n, s, W, red);
     // largest column of B W
     double best = -1.;
@@ -90,16 +98,16 @@ __global__ void __launch_bounds__(kRsvdThreads) k_rsvd_small(RsvdJob J) {
         vb[r] = v;
     }
     __syncthreads();
-    for (int it = 0; it < kRitzRefine; ++it) {
-        solve_lu_h(A, piv, n, vb, 1);
-        solve_lu(A, piv, n, vb, 1);
+    for (int it = 0; it < kRitzRefine; ++it) {   // Y is free now: row-permutation scratch
+        solve_lu_h_blk(A, perm, n, vb, 1, Y, nullptr, true);
+        solve_lu_blk(A, perm, n, vb, 1, Y, nullptr, true);
     }
     for (int r = threadIdx.x; r < n; r += blockDim.x) J.uv[2LL * n * mat + n + r] = vb[r];
 }
 
 size_t rsvd_smem_bytes(int n, int s) {
     return ((size_t)n * n + 2 * (size_t)n * s + (size_t)s * s + s) * sizeof(cplx) + 128 * sizeof(double) +
-           (((size_t)n + 32 + 3) / 4 * 4) * sizeof(int) + (size_t)n * sizeof(cplx);
+           (((size_t)2 * n + 32 + 3) / 4 * 4) * sizeof(int) + (size_t)n * sizeof(cplx);
 }
 
 cudaError_t launch_rsvd_small(int n, int nmat, int s, int q, int D, const cplx* T, long long mat_stride,

@@ -181,7 +181,8 @@ static __device__ void qr_cgs2(cplx* X, int n, int s, cplx* coef, double* red, c
 static __device__ void jacobi_thin(cplx* B, int n, int s, cplx* W, double* red) {
     for (int e = threadIdx.x; e < s * s; e += blockDim.x) W[e] = mk((e % s) == (e / s) ? 1. : 0.);
     __syncthreads();
-    const double tol = 1e-15;
+    // orthogonal at the rounding level of an n-term inner product (see jacobi_cta)
+    const double tol = fmax(1e-15, 2.0 * n * 2.220446049250313e-16);
     for (int sweep = 0; sweep < 30; ++sweep) {
         int rotated = 0;
         for (int p = 0; p < s - 1; ++p)

@@ -862,23 +862,59 @@ struct Job1 {
     Newton nt;
 };
 
-// lock-step Newton over all (operator, candidate) states
+// lock-step Newton over all (operator, candidate) states; the speculative bisection
+// points of newton_rounds once at most kSpecRound candidates are left (the late,
+// latency-bound rounds), with the same feeding rule, so the iterates are unchanged
 int newton_multi(MultiSigma& ev, std::vector<Job1>& jobs) {
+    std::vector<std::vector<std::array<double, 3>>> cache(jobs.size());   // (k, sigma', sigma'')
+    bool spec_ok = true;   // every operator's sigma from the latency-bound dense kernel
+    for (int i = 0; i < ev.nops; ++i) spec_ok &= hbem::plain_speculate_ok(ev.ops[i]) != 0;
     for (int round = 0; round < kMaxIt; ++round) {
-        std::vector<std::vector<double>> xs(ev.nops);
-        std::vector<std::vector<size_t>> who(ev.nops);
-        bool any = false;
-        for (size_t c = 0; c < jobs.size(); ++c)
-            if (!jobs[c].nt.done) {
-                xs[jobs[c].op].push_back(jobs[c].nt.rts);
-                who[jobs[c].op].push_back(c);
-                any = true;
+        size_t active = 0;
+        for (size_t c = 0; c < jobs.size(); ++c) {
+            Newton& nt = jobs[c].nt;
+            while (!nt.done) {
+                auto it = std::find_if(cache[c].begin(), cache[c].end(),
+                                       [&](const std::array<double, 3>& e) { return e[0] == nt.rts; });
+                if (it == cache[c].end()) break;
+                nt.feed((*it)[1], (*it)[2]);
+                ++ev.evals;
             }
-        if (!any) break;
+            active += nt.done ? 0 : 1;
+        }
+        if (!active) break;
+        std::vector<std::vector<double>> xs(ev.nops);
+        std::vector<std::vector<std::pair<size_t, bool>>> who(ev.nops);   // (job, speculative)
+        for (size_t c = 0; c < jobs.size(); ++c) {
+            Newton& nt = jobs[c].nt;
+            if (nt.done) continue;
+            xs[jobs[c].op].push_back(nt.rts);
+            who[jobs[c].op].push_back({c, false});
+            if (spec_ok && active <= (size_t)kSpecRound && (nt.first || nt.bisected)) {
+                cache[c].clear();
+                double sp[2];
+                const int m = nt.bisect_next(sp);
+                for (int j = 0; j < m; ++j)
+                    if (sp[j] != nt.rts) {
+                        xs[jobs[c].op].push_back(sp[j]);
+                        who[jobs[c].op].push_back({c, true});
+                    }
+            }
+        }
         std::vector<std::vector<double>> out;
+        const int before = ev.evals;
         if (int r = ev(xs, 2, out)) return r;
+        ev.evals = before;   // counted below: only the points the iterations use
         for (int i = 0; i < ev.nops; ++i)
-            for (size_t q = 0; q < who[i].size(); ++q) jobs[who[i][q]].nt.feed(out[i][3 * q + 1], out[i][3 * q + 2]);
+            for (size_t q = 0; q < who[i].size(); ++q) {
+                const size_t c = who[i][q].first;
+                if (who[i][q].second) {
+                    cache[c].push_back({xs[i][q], out[i][3 * q + 1], out[i][3 * q + 2]});
+                } else {
+                    jobs[c].nt.feed(out[i][3 * q + 1], out[i][3 * q + 2]);
+                    ++ev.evals;
+                }
+            }
     }
     return HBEM_OK;
 }

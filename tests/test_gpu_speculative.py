@@ -62,3 +62,26 @@ def test_warm_started_jacobi_matches_cold(N, c_i, npoints):
     assert np.max(np.abs(g1[:, 0] - g0[:, 0]) / g0[:, 0]) <= 1e-12
     ends = ~np.isnan(g0[:, 1])
     assert np.max(np.abs(g1[ends, 1] - g0[ends, 1])) <= 1e-9 * max(1.0, np.max(np.abs(g0[ends, 1])))
+
+
+def test_batched_plain_search_with_speculation_matches_plain_rounds():
+    """The plain search over several scatterers in lock step (speculative bisection
+    points in the late rounds) against the same search without speculation."""
+    from helmholtzbem_gb300 import learned as L
+    cases = [L.draw(s) for s in (20101, 20102, 20103, 20104)]
+    ops = [L.operator(a, b) for (a, b, _, _) in cases]
+    lo = [c[3] for c in cases]
+    hi = [c[3] + 2.0 for c in cases]
+    ci = [c[2] for c in cases]
+    check(C.lib().hbem_set_option(b"plain_speculate", 1))
+    r1, n1 = api.find_resonances_plain_multi(ops, lo, hi, 96, 1.0, ci, tol=1e-8)
+    check(C.lib().hbem_set_option(b"plain_speculate", 0))
+    try:
+        r0, n0 = api.find_resonances_plain_multi(ops, lo, hi, 96, 1.0, ci, tol=1e-8)
+    finally:
+        check(C.lib().hbem_set_option(b"plain_speculate", 1))
+    assert n1 == n0 and sum(len(r) for r in r0) > 0
+    for a, b in zip(r1, r0):
+        assert len(a) == len(b)
+        if len(a):
+            assert np.max(np.abs(np.asarray(a) - np.asarray(b))) <= 1e-10

@@ -51,6 +51,9 @@ def parse():
                     help="no timing: FP64 and complex-FP32 LU + rSVD of 4 matrices of order 1600 (for captures)")
     ap.add_argument("--profile-case", action="store_true",
                     help="no timing: three sigma sweeps over 16 wavenumbers of the workload (for ncu captures)")
+    ap.add_argument("--full-configs", action="store_true",
+                    help="one run of the batching configuration at its full size (8 scatterers x 256 k) and "
+                         "of the precision configuration at all eight wavenumbers 40..47; prints one JSON line")
     ap.add_argument("--profile-field", action="store_true",
                     help="no timing: the field-at-scale scatterer lifted on a 160 x 160 grid (for ncu captures)")
     return ap.parse_args()
@@ -831,9 +834,24 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+def run_full_configs():
+    """The batching configuration with all 256 wavenumbers per scatterer (2048 T(k))
+    and the precision configuration at k = 40, ..., 47, each once (a few tens of
+    seconds of GPU time, so not part of the default run)."""
+    import torch
+    from helmholtzbem_gb300 import _capi as C, api, geometry
+    lib = C.lib()
+    torch.cuda.set_device(0)
+    batch = batching_sample(torch, C, api, geometry, lib, nk=256)
+    prec = precision_at_scale(torch, C, api, geometry, lib, ks=tuple(float(k) for k in range(40, 48)))
+    print(json.dumps({"batching_full": batch, "precision_full": prec}))
+
+
 def main():
     args = parse()
-    if args.profile_search:
+    if args.full_configs:
+        run_full_configs()
+    elif args.profile_search:
         run_profile_search()
     elif args.profile_dense_tail:
         run_profile_dense_tail()

@@ -7,6 +7,7 @@ with, in w = 64/x^2 in (0, 1],
     P_0 = 1 + F0(w),  x Q_0 = -1/8 + G0(w),  P_1 = 1 + F1(w),  x Q_1 = 3/8 + G1(w),
 F*, G* polynomials of degree DEG (least squares on Chebyshev points, samples from
 mpmath at 40 digits), evaluated by Horner's rule.  Absolute error < 3e-18 on (0,1].
+For x >= 16 (w <= 1/4) a second set of degree DEG_FAR reaches < 2e-18 there.
 
 For 2 <= x < 8 the device evaluates J0, Y0, J1, Y1 by Taylor polynomials of degree
 TAY_DEG about the centres 2.25, 2.75, ..., 7.75 (|x - centre| <= 1/4).  The
@@ -24,6 +25,7 @@ import numpy as np
 mp.mp.dps = 40
 DEG = 14
 M = 64
+DEG_FAR, W_FAR = 8, 0.25   # x >= 16: absolute error < 2e-18 on (0, 1/4]
 
 
 def targets(w):
@@ -52,6 +54,17 @@ def main():
         mono = np.polynomial.chebyshev.cheb2poly(cf)
         P = np.polynomial.Polynomial(mono)(np.polynomial.Polynomial([-1.0, 2.0]))
         print("static __device__ __constant__ double %s[%d] = {" % (name, DEG + 1))
+        print(",\n".join("  %.17e" % v for v in P.coef))
+        print("};")
+    # x >= 16 (w <= 1/4): the same amplitudes to the same accuracy with degree DEG_FAR
+    wf = (y + 1) / 2 * W_FAR
+    valsf = np.array([[float(v) for v in targets(w)] for w in wf])
+    print("#define HBEM_PQ_DEG_FAR %d" % DEG_FAR)
+    for name, c in zip(["HBEM_F0F", "HBEM_G0F", "HBEM_F1F", "HBEM_G1F"], range(4)):
+        cf = np.polynomial.chebyshev.chebfit(y, valsf[:, c], DEG_FAR)
+        mono = np.polynomial.chebyshev.cheb2poly(cf)
+        P = np.polynomial.Polynomial(mono)(np.polynomial.Polynomial([-1.0, 2.0 / W_FAR]))
+        print("static __device__ __constant__ double %s[%d] = {" % (name, DEG_FAR + 1))
         print(",\n".join("  %.17e" % v for v in P.coef))
         print("};")
     # ascending-series constants, index k = 1..SER_N (entry 0 unused):

@@ -133,13 +133,20 @@ constexpr double kPi = 3.14159265358979323846;
 //   2 <= x < 8    Taylor polynomials of degree 17 about 2.25, 2.75, ..., 7.75
 //                 (the reference uses the series up to 8; the polynomials avoid its
 //                 cancellation and cost a quarter of its operations there)
-//   x <= 1e6      modulus/phase amplitudes P, Q in w = 64/x^2 (DLMF 10.17),
+//   x <= 1e6      modulus/phase amplitudes P, Q in w = 64/x^2 (DLMF 10.17; degree 14
+//                 on 8 <= x < 16, degree 8 beyond),
 //                 phases through sin x +- cos x so the argument is used exactly
 //   x > 1e6       leading-order asymptotic form (DLMF 10.17.3, first term)
 __device__ __forceinline__ double horner_pq(const double* c, double w) {
     double r = c[HBEM_PQ_DEG];
 #pragma unroll
     for (int k = HBEM_PQ_DEG - 1; k >= 0; --k) r = fma(r, w, c[k]);
+    return r;
+}
+__device__ __forceinline__ double horner_pq_far(const double* c, double w) {
+    double r = c[HBEM_PQ_DEG_FAR];
+#pragma unroll
+    for (int k = HBEM_PQ_DEG_FAR - 1; k >= 0; --k) r = fma(r, w, c[k]);
     return r;
 }
 
@@ -195,10 +202,18 @@ static __device__ __forceinline__ void hankel01_real_t(double x, double ix_in, d
         y1 = (1. / kPi) * (y1 * x + 2.0 * (lg * j1 + (j0 - 2.0) * ix));
     } else if (x <= 1e6) {
         double ix = PRE ? ix_in : 1.0 / x, w = 64. * ix * ix;
-        double P0 = 1. + horner_pq(HBEM_F0, w);
-        double Q0 = (horner_pq(HBEM_G0, w) - 0.125) * ix;
-        double P1 = 1. + horner_pq(HBEM_F1, w);
-        double Q1 = (horner_pq(HBEM_G1, w) + 0.375) * ix;
+        double P0, Q0, P1, Q1;
+        if (x >= 16.) {   // w <= 1/4: the degree-8 fit of the same amplitudes
+            P0 = 1. + horner_pq_far(HBEM_F0F, w);
+            Q0 = (horner_pq_far(HBEM_G0F, w) - 0.125) * ix;
+            P1 = 1. + horner_pq_far(HBEM_F1F, w);
+            Q1 = (horner_pq_far(HBEM_G1F, w) + 0.375) * ix;
+        } else {
+            P0 = 1. + horner_pq(HBEM_F0, w);
+            Q0 = (horner_pq(HBEM_G0, w) - 0.125) * ix;
+            P1 = 1. + horner_pq(HBEM_F1, w);
+            Q1 = (horner_pq(HBEM_G1, w) + 0.375) * ix;
+        }
         double sx, cx;
         sincos(x, &sx, &cx);
         double r = rsqrt(kPi * x);

@@ -66,6 +66,17 @@ __device__ __forceinline__ void hankel_at(const KConst& K, double vn, cplx& h0, 
     else hankel01_cplx(vn * K.ks.re, vn * K.ks.im, h0, h1);
 }
 
+// the same with 1/|v| given (real k: no division for 1/x)
+template <bool RK>
+__device__ __forceinline__ void hankel_at_ix(const KConst& K, double vn, double ivn, cplx& h0, cplx& h1) {
+    if (RK) {
+        if (vn > 0.) hankel01_real_ix(K.ks.re * vn, K.ks_re_inv * ivn, h0, h1);
+        else hankel01_real(0., h0, h1);
+    } else {
+        hankel01_cplx(vn * K.ks.re, vn * K.ks.im, h0, h1);
+    }
+}
+
 // the same with 1/|v| and log|v| given (k-independent point data): for real k the
 // series branch needs neither a division nor a logarithm
 template <bool RK>
@@ -396,9 +407,10 @@ __global__ void __launch_bounds__(128) k_general(DevMesh M, const Job* jobs, cpl
             const double tjn = tnj[b];
             const cplx v = xi - yj;
             const double vn2 = norm2(v), vn = sqrt(vn2);
+            const double ivn = vn > 0. ? 1.0 / vn : 0.;
             cplx h0, h1;
-            hankel_at<RK>(K, vn, h0, h1);
-            const KVals<D, RK> kv = kernel_values<D, RK>(K, vn, vn2, vn > 0. ? 1.0 / vn : 0., h0, h1);
+            hankel_at_ix<RK>(K, vn, ivn, h0, h1);
+            const KVals<D, RK> kv = kernel_values<D, RK>(K, vn, vn2, ivn, h0, h1);
             double wm[4];
             mom_weights(wa * sw[b], s, sx[b], wm);
             acc_s<D, RK, CURVED>(A, wm, kv, 2. * (ti.im * tj.im + ti.re * tj.re), !tz);
@@ -452,9 +464,10 @@ __global__ void __launch_bounds__(128) k_general_w(DevMesh M, const Job* jobs, c
             const double tjn = tnj[b];
             const cplx v = xi - yj;
             const double vn2 = norm2(v), vn = sqrt(vn2);
+            const double ivn = vn > 0. ? 1.0 / vn : 0.;
             cplx h0, h1;
-            hankel_at<RK>(K, vn, h0, h1);
-            const KVals<D, RK> kv = kernel_values<D, RK>(K, vn, vn2, vn > 0. ? 1.0 / vn : 0., h0, h1);
+            hankel_at_ix<RK>(K, vn, ivn, h0, h1);
+            const KVals<D, RK> kv = kernel_values<D, RK>(K, vn, vn2, ivn, h0, h1);
             double wm[4];
             mom_weights(wa * sw[b], s, sx[b], wm);
             acc_s<D, RK, CURVED>(A, wm, kv, 2. * (ti.im * tj.im + ti.re * tj.re), !tz);

@@ -322,6 +322,7 @@ __global__ void __launch_bounds__(kFieldThreads) k_field_grid(FieldJob J) {
         if (onb != 0x7fffffff) J.bnd_t[g] = bt;
     }
     const double kr = inside ? J.kire : J.kore, ki = inside ? J.kiim : J.koim;
+    const double ikr = kr > 0. ? 1.0 / kr : 0.;
     cplx sum = mk(0.);
     const int M = J.npan * J.nq;
     constexpr int kPerWarp = kNodeTile / kFieldSlices;
@@ -334,11 +335,14 @@ __global__ void __launch_bounds__(kFieldThreads) k_field_grid(FieldJob J) {
         const int e1 = min(cnt, (w + 1) * kPerWarp);
         for (int e = w * kPerWarp; e < e1; ++e) {
             const FNode& nd = tile[e];
-            const double zx = x - nd.yx, zy = y - nd.yy, r = sqrt(zx * zx + zy * zy);
-            if (!(r > 0.)) continue;
+            const double zx = x - nd.yx, zy = y - nd.yy, r2 = zx * zx + zy * zy;
+            if (!(r2 > 0.)) continue;
+            // 1/r once: the normal projection and (real k) the Hankel pair's 1/x use it
+            const double ir = rsqrt(r2), r = r2 * ir;
             cplx h0, h1;
-            hankel_pair(J.real_k, kr, ki, r, h0, h1);
-            const double zn = (zx * nd.nx + zy * nd.ny) / r;
+            if (J.real_k) hankel01_real_ix(kr * r, ikr * ir, h0, h1);
+            else hankel01_cplx(kr * r, ki * r, h0, h1);
+            const double zn = (zx * nd.nx + zy * nd.ny) * ir;
             const cplx tD = inside ? nd.tdi : nd.tdo, tN = inside ? nd.tni : nd.tno;
             cplx term = h0 * tN - (mk(kr, ki) * zn) * (h1 * tD);
             sum += nd.D * term;

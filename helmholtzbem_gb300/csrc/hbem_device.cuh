@@ -153,7 +153,7 @@ __device__ __forceinline__ double horner_pq_far(const double* c, double w) {
 // PRE: the caller supplies ix = 1/x and lg = log(x/2) + gamma (the assembly has them
 // from k-independent tables: log(x/2) = log(k sqrt(c)/2) + log|v|), which saves the
 // logarithm and the division of the ascending-series branch.
-template <bool PRE>
+template <bool PRE, bool PRE_IX = PRE>
 static __device__ __forceinline__ void hankel01_real_t(double x, double ix_in, double lg_in, cplx& h0, cplx& h1) {
     double j0, j1, y0, y1;
     if (x <= 0.) {
@@ -163,7 +163,7 @@ static __device__ __forceinline__ void hankel01_real_t(double x, double ix_in, d
     if (x < 1e-8) {
         j0 = 1.; j1 = 0.5 * x;
         y0 = (2. / kPi) * (PRE ? lg_in : (log(j1) + kEulerGamma));
-        y1 = PRE ? -(2. / kPi) * ix_in : -(2. / kPi) / x;
+        y1 = PRE_IX ? -(2. / kPi) * ix_in : -(2. / kPi) / x;
     } else if (x >= 2. && x < 8.) {
         // Taylor polynomials about the centre of the x's quarter-width interval
         // (coefficients from mpmath; no logarithm, no division)
@@ -195,13 +195,13 @@ static __device__ __forceinline__ void hankel01_real_t(double x, double ix_in, d
             y1 = fma(-HBEM_SER_HK1[k], t, y1);
             if ((__double2hiint(t) & 0x7fffffff) < ((1023 - 55) << 20)) break;
         }
-        const double ix = PRE ? ix_in : 1.0 / x;
+        const double ix = PRE_IX ? ix_in : 1.0 / x;
         j1 *= 0.5 * x;
         const double lg = PRE ? lg_in : log(0.5 * x) + kEulerGamma;
         y0 = (2. / kPi) * fma(lg, j0, y0);
         y1 = (1. / kPi) * (y1 * x + 2.0 * (lg * j1 + (j0 - 2.0) * ix));
     } else if (x <= 1e6) {
-        double ix = PRE ? ix_in : 1.0 / x, w = 64. * ix * ix;
+        double ix = PRE_IX ? ix_in : 1.0 / x, w = 64. * ix * ix;
         double P0, Q0, P1, Q1;
         if (x >= 16.) {   // w <= 1/4: the degree-8 fit of the same amplitudes
             P0 = 1. + horner_pq_far(HBEM_F0F, w);
@@ -239,6 +239,11 @@ static __device__ __noinline__ void hankel01_real(double x, cplx& h0, cplx& h1) 
 // x > 0 with ix = 1/x and lg = log(x/2) + gamma given
 static __device__ __noinline__ void hankel01_real_pre(double x, double ix, double lg, cplx& h0, cplx& h1) {
     hankel01_real_t<true>(x, ix, lg, h0, h1);
+}
+
+// x > 0 with ix = 1/x given (the logarithm, needed only below x = 2, computed here)
+static __device__ __noinline__ void hankel01_real_ix(double x, double ix, cplx& h0, cplx& h1) {
+    hankel01_real_t<false, true>(x, ix, 0., h0, h1);
 }
 
 // ---------------------------------------------------------------- complex argument

@@ -707,8 +707,11 @@ def run_gpu(args):
         roots, grid, nev = solop.find_resonances_plain(CFG["k_min"], CFG["k_max"], CFG["npoints"], CFG["c_o"],
                                                        CFG["c_i"], tol=CFG["tol"])
         if roots.size:
-            lo = solop.sweep_sigma(roots - CFG["tol"], CFG["c_o"], CFG["c_i"], d=1)[:, 1]
-            hi = solop.sweep_sigma(roots + CFG["tol"], CFG["c_o"], CFG["c_i"], d=1)[:, 1]
+            # verification: sigma' changes sign across [root - tol, root + tol]; both
+            # ends of every root in one batched evaluation
+            d1 = solop.sweep_sigma(np.concatenate([roots - CFG["tol"], roots + CFG["tol"]]), CFG["c_o"], CFG["c_i"],
+                                   d=1)[:, 1]
+            lo, hi = d1[:roots.size], d1[roots.size:]
             ver = int(np.sum((lo <= 0.0) & (hi >= 0.0)))
         else:
             ver = 0
@@ -761,7 +764,7 @@ def run_gpu(args):
         e2e_ms += e0.elapsed_time(e1)
         e2e_v += v
         del s2, d2
-    d2h = int(roots.nbytes + CFG["npoints"] * 3 * 8)
+    d2h = int(roots.nbytes + CFG["npoints"] * 3 * 8 + 2 * roots.size * 3 * 8)   # roots, grid, verification
 
     # roofline of the dominant kernel (panel-pair assembly, FP64 CUDA-core bound):
     # algorithmic work of the timed launches by derivative order and point kind

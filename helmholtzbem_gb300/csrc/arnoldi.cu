@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(kArnThreads) k_arn_small(ArnJob J) {
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) A[e] = T0[e];
     for (int e = threadIdx.x; e < n * p; e += blockDim.x) X[e] = arn_start(J.seed, e % n, e / n);
     __syncthreads();
-    lu_smem(A, n, piv, red, redi, &s_sing);
+    lu_smem(A, n, piv, red, redi, &s_sing, buf);
     __syncthreads();
     if (s_sing) {
         arn_fail(J, mat, 5);

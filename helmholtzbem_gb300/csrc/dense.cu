@@ -681,7 +681,7 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
     // FP64 LU of T over the FP32 work space
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) T64[e] = T0[e];
     __syncthreads();
-    lu_smem(T64, n, piv, red, redi, &s_sing);
+    lu_smem(T64, n, piv, red, redi, &s_sing, sbuf);
     perm_from_piv(piv, n, perm);
     // U's diagonal replaced by its reciprocals: the solves below multiply
     for (int k = threadIdx.x; k < n; k += blockDim.x) {

@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(kRsvdThreads) k_rsvd_small(RsvdJob J) {
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) A[e] = T0[e];
     for (int e = threadIdx.x; e < n * s; e += blockDim.x) X[e] = J.R[e];
     __syncthreads();
-    lu_smem(A, n, piv, red, redi, &s_sing);
+    lu_smem(A, n, piv, red, redi, &s_sing, vb);
     // blocked solves: rows permuted once, U's diagonal replaced by its reciprocals
     perm_from_piv(piv, n, perm);
     for (int k = threadIdx.x; k < n; k += blockDim.x) {

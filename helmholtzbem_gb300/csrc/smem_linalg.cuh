@@ -21,51 +21,55 @@ static __device__ __forceinline__ double bsum(double x, double* red) {
 
 // LU with partial pivoting of the n x n column-major matrix A (shared memory).
 // piv[k] = row exchanged with row k at step k.  Returns via *sing a zero-pivot flag.
-static __device__ void lu_smem(cplx* A, int n, int* piv, double* redv, int* redi, int* sing) {
+// Per step: warp 0 finds the pivot (largest |A[i,k]|^2, i >= k, ties to the smallest
+// i), exchanges the two rows and scales column k into lbuf (n entries of scratch) and
+// A; after one barrier all warps update the trailing matrix, a warp per column and
+// its lanes over the rows; a second barrier ends the step.  redv, redi: unused
+// (kept for the callers' layouts).
+static __device__ void lu_smem(cplx* A, int n, int* piv, double* redv, int* redi, int* sing, cplx* lbuf) {
+    (void)redv;
+    (void)redi;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int k = 0; k < n; ++k) {
-        // pivot: largest |A[i,k]|, i >= k (ties: smallest i)
-        double best = -1.;
-        int bi = k;
-        for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
-            double a = norm2(A[i + (long long)k * n]);
-            if (a > best) { best = a; bi = i; }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            double ob = __shfl_xor_sync(0xffffffffu, best, o);
-            int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-        }
-        if (lane == 0) { redv[warp] = best; redi[warp] = bi; }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double b = redv[0];
-            int p = redi[0];
-            for (int w = 1; w < nw; ++w)
-                if (redv[w] > b || (redv[w] == b && redi[w] < p)) { b = redv[w]; p = redi[w]; }
-            piv[k] = p;
-            if (b == 0.) *sing = 1;
-        }
-        __syncthreads();
-        const int p = piv[k];
-        if (p != k)
-            for (int j = threadIdx.x; j < n; j += blockDim.x) {
-                cplx t = A[k + (long long)j * n];
-                A[k + (long long)j * n] = A[p + (long long)j * n];
-                A[p + (long long)j * n] = t;
+        if (warp == 0) {
+            double best = -1.;
+            int bi = k;
+            for (int i = k + lane; i < n; i += 32) {
+                const double a = norm2(A[i + (long long)k * n]);
+                if (a > best) { best = a; bi = i; }
             }
-        __syncthreads();
-        const cplx d = A[k + (long long)k * n];
-        if (norm2(d) > 0.) {
-            const cplx id = cdiv(mk(1.), d);
-            for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) A[i + (long long)k * n] = A[i + (long long)k * n] * id;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            const int p = bi;   // the same on every lane
+            if (lane == 0) {
+                piv[k] = p;
+                if (best == 0.) *sing = 1;
+            }
+            if (p != k)
+                for (int j = lane; j < n; j += 32) {
+                    const cplx t = A[k + (long long)j * n];
+                    A[k + (long long)j * n] = A[p + (long long)j * n];
+                    A[p + (long long)j * n] = t;
+                }
+            __syncwarp();
+            const cplx d = A[k + (long long)k * n];
+            const bool nz = norm2(d) > 0.;
+            const cplx id = nz ? cdiv(mk(1.), d) : mk(0.);
+            for (int i = k + 1 + lane; i < n; i += 32) {
+                cplx l = A[i + (long long)k * n];
+                if (nz) l = l * id;
+                A[i + (long long)k * n] = l;
+                lbuf[i] = l;
+            }
         }
         __syncthreads();
-        const int m = n - k - 1;
-        for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-            const int i = k + 1 + e % m, j = k + 1 + e / m;
-            cfms(A[i + (long long)j * n], A[i + (long long)k * n], A[k + (long long)j * n]);
+        for (int j = k + 1 + warp; j < n; j += nw) {
+            const cplx u = A[k + (long long)j * n];
+            for (int i = k + 1 + lane; i < n; i += 32) cfms(A[i + (long long)j * n], lbuf[i], u);
         }
         __syncthreads();
     }

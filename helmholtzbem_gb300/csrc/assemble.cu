@@ -60,13 +60,7 @@ struct Acc {
     }
 };
 
-template <bool RK>
-__device__ __forceinline__ void hankel_at(const KConst& K, double vn, cplx& h0, cplx& h1) {
-    if (RK) hankel01_real(K.ks.re * vn, h0, h1);
-    else hankel01_cplx(vn * K.ks.re, vn * K.ks.im, h0, h1);
-}
-
-// the same with 1/|v| given (real k: no division for 1/x)
+// H0, H1 at ks |v| with 1/|v| given (real k: no division for 1/x)
 template <bool RK>
 __device__ __forceinline__ void hankel_at_ix(const KConst& K, double vn, double ivn, cplx& h0, cplx& h1) {
     if (RK) {
@@ -77,8 +71,8 @@ __device__ __forceinline__ void hankel_at_ix(const KConst& K, double vn, double 
     }
 }
 
-// the same with 1/|v| and log|v| given (k-independent point data): for real k the
-// series branch needs neither a division nor a logarithm
+// H0, H1 at ks |v| with 1/|v| and log|v| given (k-independent point data): for real k
+// the series branch needs neither a division nor a logarithm
 template <bool RK>
 __device__ __forceinline__ void hankel_at_pre(const KConst& K, double vn, double ivn, double lvn, cplx& h0,
                                               cplx& h1) {

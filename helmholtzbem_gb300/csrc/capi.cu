@@ -60,7 +60,9 @@ cudaError_t arnoldi_batched(int n, int nmat, int count, int D, double tol, int m
                             long long* launches);
 cudaError_t launch_svd_fast(int n, int nmat, int D, const cplx* T, long long mat_stride, long long der_stride,
                             double* out, int* status, cudaStream_t st, cplxf* vpool = nullptr,
-                            const int* warm_slot = nullptr, const int* out_slot = nullptr);
+                            const int* warm_slot = nullptr, const int* out_slot = nullptr, cplx* uv = nullptr);
+cudaError_t launch_sigma1_uv(int n, int nmat, const cplx* T1, long long mat_stride, const cplx* uv, const int* idx,
+                             double* d1, cudaStream_t st);
 }  // namespace hbem
 
 using namespace hbem;
@@ -309,9 +311,11 @@ struct hbem_solop_s {
     std::vector<double> M;    // N x N column-major
     DBuf d_M, d_id, d_sb, d_lr, d_T, d_svdA, d_svdV, d_out, d_status, d_sig;
     DBuf d_vpool, d_slots;   // FP32 V sets of the dense kernel's warm starts, slot lists
+    DBuf d_uv, d_d1;         // singular vectors of sigma_min kept by sweep_sigma_warm, sigma' scratch
+    int uv_count = 0;        // wavenumbers whose (u, v) d_uv holds (0: none valid)
     ~hbem_solop_s() {
         for (DBuf* x : {&d_M, &d_id, &d_sb, &d_lr, &d_T, &d_svdA, &d_svdV, &d_out, &d_status, &d_sig, &d_vpool,
-                        &d_slots})
+                        &d_slots, &d_uv, &d_d1})
             x->release();
     }
 };
@@ -777,7 +781,8 @@ int hbem_gen_sol_op_batch_device(hbem_solop s, const double* k_host, int nk, dou
 static int sv_batch(cudaStream_t st, int n, int nmat, unsigned d, const cplx* T, long long mat_stride,
                     long long der_stride, DBuf& A, DBuf& V, DBuf& out, DBuf& status, DBuf* sig, double* out_host,
                     double* sig_all_host, cplxf* vpool = nullptr, const int* warm_slot = nullptr,
-                    const int* out_slot = nullptr) {
+                    const int* out_slot = nullptr, cplx* uv = nullptr, int* fast_ok = nullptr) {
+    if (fast_ok) *fast_ok = 0;
     const size_t nn = (size_t)n * n;
     HB_CK(V.ensure((size_t)nmat * nn * sizeof(cplx)));
     HB_CK(A.ensure(n > 100 ? (size_t)nmat * nn * sizeof(cplx) : sizeof(cplx)));
@@ -793,7 +798,7 @@ static int sv_batch(cudaStream_t st, int n, int nmat, unsigned d, const cplx* T,
         // FP32 Jacobi + FP64 refinement; matrices it cannot finish (singular T, a
         // far-field series that does not converge) are redone by the polished kernel
         HB_CK(launch_svd_fast(n, nmat, (int)d, T, mat_stride, der_stride, out.as<double>(), status.as<int>(), st,
-                              vpool, warm_slot, out_slot));
+                              vpool, warm_slot, out_slot, uv));
         g_launches += 1;
         HB_CK(cudaMemcpyAsync(stat.data(), status.p, (size_t)nmat * sizeof(int), cudaMemcpyDeviceToHost, st));
         HB_CK(cudaStreamSynchronize(st));
@@ -802,6 +807,7 @@ static int sv_batch(cudaStream_t st, int n, int nmat, unsigned d, const cplx* T,
         if (!redo) {
             HB_CK(cudaMemcpyAsync(out_host, out.p, (size_t)nmat * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
             HB_CK(cudaStreamSynchronize(st));
+            if (fast_ok) *fast_ok = 1;
             return HBEM_OK;
         }
     }
@@ -1197,7 +1203,7 @@ int plain_warm_start_ok() { return g_plain_warm_start; }
 // The pool's contents survive between calls while npool does not grow.  Returns
 // HBEM_ERR_UNSUPPORTED when the dense kernel does not take the order or the batch.
 int sweep_sigma_warm(hbem_solop s, const double* k_host, int nk, double c_o, double c_i, unsigned d,
-                     const int* warm_slot, const int* out_slot, int npool, double* out_host) {
+                     const int* warm_slot, const int* out_slot, int npool, double* out_host, int keep_uv) {
     if (!s || !k_host || !out_host || nk < 1 || d > 2 || npool < 1 || !warm_slot || !out_slot)
         return fail(HBEM_ERR_INVALID, "sweep_sigma_warm: bad argument");
     hbem_builder b = s->b;
@@ -1226,9 +1232,45 @@ int sweep_sigma_warm(hbem_solop s, const double* k_host, int nk, double c_o, dou
     HB_CK(upload(s->d_slots, slots, b->st));
     HB_CK(s->d_T.ensure((size_t)nk * (d + 1) * mat * sizeof(cplx)));
     if (int r = gen_T_batch(s, k_host, nullptr, nk, c_o, c_i, d, s->d_T.as<cplx>())) return r;
-    return sv_batch(b->st, n, nk, d, s->d_T.as<cplx>(), (long long)(d + 1) * mat, (long long)mat, s->d_svdA,
-                    s->d_svdV, s->d_out, s->d_status, nullptr, out_host, nullptr, s->d_vpool.as<cplxf>(),
-                    s->d_slots.as<int>(), s->d_slots.as<int>() + nk);
+    if (keep_uv) {
+        s->uv_count = 0;
+        HB_CK(s->d_uv.ensure((size_t)nk * 2 * n * sizeof(cplx)));
+    }
+    int fast_ok = 0;
+    if (int r = sv_batch(b->st, n, nk, d, s->d_T.as<cplx>(), (long long)(d + 1) * mat, (long long)mat, s->d_svdA,
+                         s->d_svdV, s->d_out, s->d_status, nullptr, out_host, nullptr, s->d_vpool.as<cplxf>(),
+                         s->d_slots.as<int>(), s->d_slots.as<int>() + nk, keep_uv ? s->d_uv.as<cplx>() : nullptr,
+                         &fast_ok))
+        return r;
+    // the vectors are those of sigma only where the fast kernel's results were kept
+    if (keep_uv && fast_ok) s->uv_count = nk;
+    return HBEM_OK;
+}
+
+// sigma' at ne wavenumbers that an earlier sweep_sigma_warm(keep_uv) evaluated, from
+// the singular vectors it kept: T and T' are assembled, then sigma' = Re u^H T' v
+// (no second SVD; these are the same vectors up to rounding).  idx[e] is the position
+// of wavenumber e in that sweep.  Returns HBEM_ERR_UNSUPPORTED when no vectors are kept.
+int sigma1_from_kept(hbem_solop s, const double* k_host, const int* idx, int ne, double c_o, double c_i,
+                     double* d1_host) {
+    if (!s || !k_host || !idx || !d1_host || ne < 1) return fail(HBEM_ERR_INVALID, "sigma1_from_kept: bad argument");
+    for (int e = 0; e < ne; ++e)
+        if (idx[e] < 0 || idx[e] >= s->uv_count) return fail(HBEM_ERR_UNSUPPORTED, "sigma1_from_kept: no vectors");
+    hbem_builder b = s->b;
+    HB_CK(cudaSetDevice(b->device));
+    const int n = 2 * b->n;
+    const size_t mat = (size_t)n * n;
+    HB_CK(s->d_T.ensure((size_t)ne * 2 * mat * sizeof(cplx)));
+    if (int r = gen_T_batch(s, k_host, nullptr, ne, c_o, c_i, 1, s->d_T.as<cplx>())) return r;
+    std::vector<int> id(idx, idx + ne);
+    HB_CK(upload(s->d_slots, id, b->st));
+    HB_CK(s->d_d1.ensure((size_t)ne * sizeof(double)));
+    HB_CK(launch_sigma1_uv(n, ne, s->d_T.as<cplx>() + mat, (long long)(2 * mat), s->d_uv.as<cplx>(),
+                           s->d_slots.as<int>(), s->d_d1.as<double>(), b->st));
+    g_launches += 1;
+    HB_CK(cudaMemcpyAsync(d1_host, s->d_d1.p, (size_t)ne * sizeof(double), cudaMemcpyDeviceToHost, b->st));
+    HB_CK(cudaStreamSynchronize(b->st));
+    return HBEM_OK;
 }
 
 }  // namespace hbem

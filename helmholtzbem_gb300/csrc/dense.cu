@@ -463,6 +463,7 @@ struct SvdFastJob {
     cpf* vpool;
     const int* warm_slot;
     const int* out_slot;
+    cplx* uv;        // optional [nmat][2n]: u, v of sigma_min
 };
 
 struct FastSmem {
@@ -745,6 +746,11 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
         out[1] = 0.;
         out[2] = 0.;
     }
+    if (J.uv)
+        for (int r = threadIdx.x; r < n; r += blockDim.x) {
+            J.uv[2LL * n * mat + r] = u[r];
+            J.uv[2LL * n * mat + n + r] = v[r];
+        }
     if (J.D == 0) {
         if (threadIdx.x == 0) J.status[mat] = s_sing ? 5 : 0;
         return;
@@ -872,14 +878,40 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
     }
 }
 
+// sigma' = Re u^H T' v for nmat derivative matrices T'_m (column-major n x n at
+// T1 + m * mat_stride) with the singular vectors (u, v) = uv + 2 n idx[m] of the same
+// wavenumber from an earlier dense-sigma launch: one CTA per matrix, a thread per row.
+__global__ void __launch_bounds__(128) k_sigma1_uv(int n, const cplx* T1, long long mat_stride, const cplx* uv,
+                                                   const int* idx, double* d1) {
+    __shared__ double red[32];
+    const int m = blockIdx.x;
+    const cplx* A = T1 + (long long)m * mat_stride;
+    const cplx* u = uv + 2LL * n * idx[m];
+    const cplx* v = u + n;
+    double part = 0.;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        cplx w = mk(0.);
+        for (int c = 0; c < n; ++c) cfma(w, A[r + (long long)c * n], v[c]);
+        part += u[r].re * w.re + u[r].im * w.im;
+    }
+    const double tot = bsum(part, red);
+    if (threadIdx.x == 0) d1[m] = tot;
+}
+
+cudaError_t launch_sigma1_uv(int n, int nmat, const cplx* T1, long long mat_stride, const cplx* uv, const int* idx,
+                             double* d1, cudaStream_t st) {
+    k_sigma1_uv<<<nmat, 128, 0, st>>>(n, T1, mat_stride, uv, idx, d1);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_svd_fast(int n, int nmat, int D, const cplx* T, long long mat_stride, long long der_stride,
                             double* out, int* status, cudaStream_t st, cplxf* vpool, const int* warm_slot,
-                            const int* out_slot) {
+                            const int* out_slot, cplx* uv) {
     const size_t limit = 220 * 1024, smem = svd_fast_smem_bytes(n);
     if (smem > limit || n < 2) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(k_svd_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit);
     if (e != cudaSuccess) return e;
-    SvdFastJob J{n, nmat, D, T, mat_stride, der_stride, out, status, vpool, warm_slot, out_slot};
+    SvdFastJob J{n, nmat, D, T, mat_stride, der_stride, out, status, vpool, warm_slot, out_slot, uv};
     k_svd_fast<<<nmat, kSvdThreads, smem, st>>>(J);
     return cudaGetLastError();
 }

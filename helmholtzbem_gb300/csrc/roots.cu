@@ -24,7 +24,9 @@ namespace hbem {
 int plain_speculate_ok(hbem_solop s);
 int plain_warm_start_ok();
 int sweep_sigma_warm(hbem_solop s, const double* k_host, int nk, double c_o, double c_i, unsigned d,
-                     const int* warm_slot, const int* out_slot, int npool, double* out_host);
+                     const int* warm_slot, const int* out_slot, int npool, double* out_host, int keep_uv = 0);
+int sigma1_from_kept(hbem_solop s, const double* k_host, const int* idx, int ne, double c_o, double c_i,
+                     double* d1_host);
 }  // namespace hbem
 
 namespace {
@@ -672,7 +674,7 @@ int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npo
         oslot.resize(npoints);
         for (int i = 0; i < npoints; ++i) oslot[i] = i;
         const int r = hbem::sweep_sigma_warm(s, ks.data(), npoints, c_o, c_i, 0, wslot.data(), oslot.data(), npoints,
-                                             g.data());
+                                             g.data(), 1);
         if (r == HBEM_ERR_UNSUPPORTED) warm = false;
         else if (r) return r;
     }
@@ -692,15 +694,28 @@ int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npo
         ends[2 * c + 1] = ks[cidx[c] + 2];
     }
     if (!ends.empty()) {
-        if (warm) {
-            // the bracket ends are grid points: their own V sets
-            wslot.resize(ends.size());
-            oslot.assign(ends.size(), -1);
-            for (size_t c = 0; c < cidx.size(); ++c) {
-                wslot[2 * c] = cidx[c];
-                wslot[2 * c + 1] = cidx[c] + 2;
+        // the bracket ends are grid points: sigma' from the grid's own singular vectors
+        // (sv_der there would redo the same SVD), else their V sets start the Jacobi
+        std::vector<int> gidx(ends.size());
+        for (size_t c = 0; c < cidx.size(); ++c) {
+            gidx[2 * c] = cidx[c];
+            gidx[2 * c + 1] = cidx[c] + 2;
+        }
+        std::vector<double> d1v(ends.size());
+        const int kept = warm ? hbem::sigma1_from_kept(s, ends.data(), gidx.data(), (int)ends.size(), c_o, c_i,
+                                                       d1v.data())
+                              : (int)HBEM_ERR_UNSUPPORTED;
+        if (kept == HBEM_OK) {
+            for (size_t e = 0; e < ends.size(); ++e) {
+                der[3 * e] = g[3 * (size_t)gidx[e]];
+                der[3 * e + 1] = d1v[e];
+                der[3 * e + 2] = 0.;
             }
-            if (int r = hbem::sweep_sigma_warm(s, ends.data(), (int)ends.size(), c_o, c_i, 1, wslot.data(),
+        } else if (kept != HBEM_ERR_UNSUPPORTED) {
+            return kept;
+        } else if (warm) {
+            oslot.assign(ends.size(), -1);
+            if (int r = hbem::sweep_sigma_warm(s, ends.data(), (int)ends.size(), c_o, c_i, 1, gidx.data(),
                                                oslot.data(), npoints, der.data()))
                 return r;
         } else if (int r = hbem_sweep_sigma(s, ends.data(), (int)ends.size(), c_o, c_i, 1, der.data())) {

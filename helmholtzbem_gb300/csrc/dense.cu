@@ -496,12 +496,20 @@ __host__ __device__ inline FastSmem fast_layout(int n) {
 
 size_t svd_fast_smem_bytes(int n) { return fast_layout(n).total; }
 
-// y = A x for the global column-major n x n matrix A (thread per row)
+// y = A x for the global column-major n x n matrix A: four consecutive lanes per
+// row, each over every fourth column (four times the loads in flight of a thread per
+// row), summed by shuffles within the four
 static __device__ void gemv_n(const cplx* A, int n, const cplx* x, cplx* y) {
-    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    const int sub = threadIdx.x & 3;
+    const unsigned gmask = 0xFu << (threadIdx.x & 28);
+    for (int r = threadIdx.x >> 2; r < n; r += blockDim.x >> 2) {
         cplx a = mk(0.);
-        for (int c = 0; c < n; ++c) cfma(a, A[r + (long long)c * n], x[c]);
-        y[r] = a;
+        for (int c = sub; c < n; c += 4) cfma(a, A[r + (long long)c * n], x[c]);
+        a.re += __shfl_xor_sync(gmask, a.re, 1);
+        a.im += __shfl_xor_sync(gmask, a.im, 1);
+        a.re += __shfl_xor_sync(gmask, a.re, 2);
+        a.im += __shfl_xor_sync(gmask, a.im, 2);
+        if (sub == 0) y[r] = a;
     }
     __syncthreads();
 }

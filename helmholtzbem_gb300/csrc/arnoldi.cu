@@ -180,14 +180,13 @@ __global__ void __launch_bounds__(kArnThreads) k_arn_small(ArnJob J) {
     int* piv = reinterpret_cast<int*>(nrm + kArnMaxP);  // n
     int* perm = piv + n;                             // n
     int* ord = perm + n;                             // kArnMaxP
-    int* redi = ord + kArnMaxP;                      // 32
     __shared__ int s_sing, s_rot;
     if (threadIdx.x == 0) s_sing = 0;
     const cplx* T0 = J.T + (long long)mat * J.mat_stride;
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) A[e] = T0[e];
     for (int e = threadIdx.x; e < n * p; e += blockDim.x) X[e] = arn_start(J.seed, e % n, e / n);
     __syncthreads();
-    lu_smem(A, n, piv, red, redi, &s_sing, buf);
+    lu_smem(A, n, piv, &s_sing, buf);
     __syncthreads();
     if (s_sing) {
         arn_fail(J, mat, 5);

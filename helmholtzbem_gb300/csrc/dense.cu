@@ -605,7 +605,6 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
     float* sig32 = reinterpret_cast<float*>(sb + L.sig32);
     int* piv = reinterpret_cast<int*>(sb + L.piv);
     int* perm = reinterpret_cast<int*>(sb + L.perm);
-    int* redi = reinterpret_cast<int*>(sb + L.redi);
     int* idx = reinterpret_cast<int*>(sb + L.idx);
     double* sigb = reinterpret_cast<double*>(sb + L.sigb);
     cplx* ab = reinterpret_cast<cplx*>(sb + L.ab);   // a_j, b_j
@@ -690,7 +689,7 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
     // FP64 LU of T over the FP32 work space
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) T64[e] = T0[e];
     __syncthreads();
-    lu_smem(T64, n, piv, red, redi, &s_sing, sbuf);
+    lu_smem(T64, n, piv, &s_sing, sbuf);
     perm_from_piv(piv, n, perm);
     // U's diagonal replaced by its reciprocals: the solves below multiply
     for (int k = threadIdx.x; k < n; k += blockDim.x) {

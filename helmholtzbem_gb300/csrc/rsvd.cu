@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(kRsvdThreads) k_rsvd_small(RsvdJob J) {
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) A[e] = T0[e];
     for (int e = threadIdx.x; e < n * s; e += blockDim.x) X[e] = J.R[e];
     __syncthreads();
-    lu_smem(A, n, piv, red, redi, &s_sing, vb);
+    lu_smem(A, n, piv, &s_sing, vb);
     // blocked solves: rows permuted once, U's diagonal replaced by its reciprocals
     perm_from_piv(piv, n, perm);
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
@@ -157,7 +157,6 @@ __global__ void __launch_bounds__(kRsvdThreads) k_rsvd_tail(int n, int s, int D,
                                                              const int* info, double* out, int* status, cplx* uv,
                                                              const int* tc_err) {
     __shared__ cplx Rs[kRsvdMaxS * kRsvdMaxS], W[kRsvdMaxS * kRsvdMaxS], tw[kRsvdMaxS];
-    __shared__ double red[128];
     const int mat = blockIdx.x, os = D + 1;
     for (int e = threadIdx.x; e < s * s; e += blockDim.x) Rs[e] = Rf[(long long)mat * s * s + e];
     __syncthreads();

@@ -24,11 +24,8 @@ static __device__ __forceinline__ double bsum(double x, double* red) {
 // Per step: warp 0 finds the pivot (largest |A[i,k]|^2, i >= k, ties to the smallest
 // i), exchanges the two rows and scales column k into lbuf (n entries of scratch) and
 // A; after one barrier all warps update the trailing matrix, a warp per column and
-// its lanes over the rows; a second barrier ends the step.  redv, redi: unused
-// (kept for the callers' layouts).
-static __device__ void lu_smem(cplx* A, int n, int* piv, double* redv, int* redi, int* sing, cplx* lbuf) {
-    (void)redv;
-    (void)redi;
+// its lanes over the rows; a second barrier ends the step.
+static __device__ void lu_smem(cplx* A, int n, int* piv, int* sing, cplx* lbuf) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int k = 0; k < n; ++k) {
         if (warp == 0) {

@@ -810,16 +810,22 @@ int hbem_refine_brackets(hbem_solop s, const double* a_host, const double* b_hos
         const double guess = br.a - br.da * (br.b - br.a) / (br.db - br.da);
         nt[c].start(br.a, br.b, guess, tol);
     }
-    for (int round = 0; round < kMaxIt; ++round) {
-        std::vector<double> xs;
-        std::vector<size_t> who;
-        for (size_t c = 0; c < nt.size(); ++c)
-            if (!nt[c].done) { xs.push_back(nt[c].rts); who.push_back(c); }
-        if (xs.empty()) break;
-        std::vector<double> out(3 * xs.size());
-        if (int r = hbem_sweep_sigma(s, xs.data(), (int)xs.size(), c_o, c_i, 2, out.data())) return r;
-        evals += (int)xs.size();
-        for (size_t q = 0; q < who.size(); ++q) nt[who[q]].feed(out[3 * q + 1], out[3 * q + 2]);
+    // lock-step Newton rounds, with speculative bisection points where the dense sigma
+    // is latency bound (the plain search's rounds)
+    if (hbem::plain_speculate_ok(s)) {
+        if (int r = newton_rounds(s, nt, c_o, c_i, evals)) return r;
+    } else {
+        for (int round = 0; round < kMaxIt; ++round) {
+            std::vector<double> xs;
+            std::vector<size_t> who;
+            for (size_t c = 0; c < nt.size(); ++c)
+                if (!nt[c].done) { xs.push_back(nt[c].rts); who.push_back(c); }
+            if (xs.empty()) break;
+            std::vector<double> out(3 * xs.size());
+            if (int r = hbem_sweep_sigma(s, xs.data(), (int)xs.size(), c_o, c_i, 2, out.data())) return r;
+            evals += (int)xs.size();
+            for (size_t q = 0; q < who.size(); ++q) nt[who[q]].feed(out[3 * q + 1], out[3 * q + 2]);
+        }
     }
     std::vector<double> roots;
     for (auto& x : nt)

@@ -122,3 +122,17 @@ def test_brent_guess_and_gsl_with_values_match_oracle():
     # a bracket the GSL minimiser refuses: NaN
     r, _ = api.brent_gsl_with_values(0.5, f(0.5), 1.6, f(1.6), 0.6, f(0.6) + 10, f, 1e-9)
     assert math.isnan(r)
+
+
+def test_every_documented_option_is_accepted():
+    """The switches hbem.h documents for hbem_set_option: each accepts its default
+    (no GPU involved), an unknown name is refused with a message."""
+    L = _lib_or_skip()
+    src = open(os.path.join(ROOT, "include", "hbem.h")).read()
+    block = src[src.index("Process-wide switches"):src.index("int hbem_set_option")]
+    documented = re.findall(r'"(\w+)" \(default (\d+)', block)
+    assert {"svd_fast", "singular_table", "plain_speculate", "plain_warm_start"} <= {n for n, _ in documented}
+    for name, default in documented:
+        assert L.hbem_set_option(name.encode(), int(default)) == 0, name
+    assert L.hbem_set_option(b"no_such_switch", 1) == 1
+    assert b"unknown option" in L.hbem_last_error()

@@ -43,7 +43,6 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-sample-points", type=int, default=60)
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline leg")
     ap.add_argument("--profile-search", action="store_true",
                     help="no timing: one plain search of the workload (for launch-list captures)")
@@ -172,52 +171,60 @@ class ClockSampler:
 
 # ------------------------------------------------------------------ CPU leg (oracle port)
 
-def cpu_sample(npoints_sample, threads):
-    """Plain sweep of the oracle port on the first npoints_sample grid points of the
-    workload (same spacing), all host threads: returns (verified roots, seconds)."""
+L2_NOTE = "GPU arm: a 256 MB buffer (> 129 MB L2) is written between timed steps; CPU arm: not applicable"
+CONFIG = {"workload": WORKLOAD, "l2": L2_NOTE}
+
+
+def grid_ks():
+    h = (CFG["k_max"] - CFG["k_min"]) / (CFG["npoints"] - 1)
+    return CFG["k_min"] + h * np.arange(CFG["npoints"])
+
+
+def sweep_pool():
+    """The oracle port of the reference's plain search with the reference driver's
+    parallel structure (grid, bracket ends and Newton searches over all host cores)."""
     from oracle import oracle as O
     kinds, par = O.circle_panels(CFG["radius"], CFG["N"])
-    oso = O.SolutionsOperator(O.Builder(kinds, par, CFG["order"]))
-    h = (CFG["k_max"] - CFG["k_min"]) / (CFG["npoints"] - 1)
-    ks = CFG["k_min"] + h * np.arange(npoints_sample)
+    return O.SweepPool(kinds, par, CFG["order"], CFG["c_o"], CFG["c_i"])
 
-    def evald(klist, d):
-        return np.array([O.sv_derivs(*oso.gen_sol_op(k, CFG["c_o"], CFG["c_i"], d=d, threads=threads))
-                         for k in klist])
 
+def cpu_search(pool):
+    """One step of the workload on the host cores: the plain search over all 200 grid
+    points plus the verification of its roots.  Returns (verified, seconds, roots, grid
+    sigma, evaluations)."""
     t0 = time.perf_counter()
-    roots, _ = O.plain_sweep(evald, ks, tol=CFG["tol"])
-    verified = 0
-    for r in roots:
-        lo = O.sv_derivs(*oso.gen_sol_op(r - CFG["tol"], CFG["c_o"], CFG["c_i"], d=1, threads=threads))[1]
-        hi = O.sv_derivs(*oso.gen_sol_op(r + CFG["tol"], CFG["c_o"], CFG["c_i"], d=1, threads=threads))[1]
-        verified += int(lo <= 0.0 <= hi)
-    return verified, time.perf_counter() - t0, ks.size
+    roots, sig, nev = pool.plain_sweep(grid_ks(), tol=CFG["tol"])
+    ok = pool.verify(roots, tol=CFG["tol"])
+    return int(ok.sum()), time.perf_counter() - t0, roots, sig, nev + 2 * roots.size
+
+
+CPU_SAMPLE = "the whole workload per step: all 200 grid points, bracket ends, Newton searches and verification"
 
 
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    threads = os.cpu_count() or 1
-    import oracle.oracle as O
-    O.lib()   # build the CPU port if needed (outside the timed region)
-    for _ in range(max(0, args.warmup)):
-        cpu_sample(6, threads)
-    tot_v, tot_t = 0, 0.0
-    for _ in range(args.steps):
-        v, t, npts = cpu_sample(args.cpu_sample_points, threads)
-        tot_v += v
-        tot_t += t
+    pool = sweep_pool()   # worker processes start outside the timed region
+    try:
+        for _ in range(max(0, args.warmup)):
+            pool.evald(list(grid_ks()[:pool.workers]), 0)   # bounded warm-up: one grid point per worker
+        tot_v, tot_t = 0, 0.0
+        for _ in range(args.steps):
+            v, t, _, _, _ = cpu_search(pool)
+            tot_v += v
+            tot_t += t
+    finally:
+        pool.close()
     val = tot_v / tot_t if tot_t > 0 else 0.0
-    sample = "first %d of the %d grid points (same spacing) + Newton/verification of their roots" % (
-        args.cpu_sample_points, CFG["npoints"])
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": "resonances/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / max(1, args.steps),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "cpu_sample": sample},
-        "cpu_baseline": {"value": val, "unit": "resonances/s", "cores": threads, "kind": "port", "sample": sample},
+        "config": CONFIG,
+        "workload_stats": {"roots_per_step": tot_v / max(1, args.steps)},
+        "cpu_baseline": {"value": val, "unit": "resonances/s", "cores": pool.workers, "kind": "port",
+                         "sample": CPU_SAMPLE},
         "e2e": {"value": val, "unit": "resonances/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -687,6 +694,22 @@ def adaptive_search(torch, so, plain_roots):
             "minima_matching_plain_roots": int(match), "plain_roots": int(plain_roots.size)}
 
 
+def roots_parity(roots, grid_sigma, oroots, osig, source):
+    """The GPU search's roots and grid sigma against the oracle's on the same workload:
+    the oracle port run in this process (oroots, osig), else the committed fixture."""
+    if oroots is None:
+        with open(os.path.join(ROOT, "tests", "golden", "plain_search_circle_N50.json")) as f:
+            gold = json.load(f)
+        oroots, osig = np.array(gold["roots"]), np.array(gold["grid_sigma"])
+    roots, oroots = np.sort(np.asarray(roots)), np.sort(np.asarray(oroots))
+    same = roots.size == oroots.size
+    dk = float(np.max(np.abs(roots - oroots))) if same and roots.size else None
+    ds = float(np.max(np.abs(grid_sigma - osig) / osig)) if grid_sigma is not None else None
+    return {"oracle": source, "gpu_roots": int(roots.size), "oracle_roots": int(oroots.size),
+            "max_abs_dk": dk, "grid_sigma_max_rel_diff": ds,
+            "roots_match_oracle": bool(same and dk is not None and dk <= CFG["tol"])}
+
+
 def run_gpu(args):
     rank, world, local = dist_env()
     import torch
@@ -702,10 +725,12 @@ def run_gpu(args):
     data = api.BuilderData(mesh, order=CFG["order"])
     so = api.SolutionsOperator(data)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # > L2 (129 MB)
+    last_grid = [None]
 
     def step(solop):
         roots, grid, nev = solop.find_resonances_plain(CFG["k_min"], CFG["k_max"], CFG["npoints"], CFG["c_o"],
                                                        CFG["c_i"], tol=CFG["tol"])
+        last_grid[0] = grid[:, 0].copy()
         if roots.size:
             # verification: sigma' changes sign across [root - tol, root + tol]; both
             # ends of every root in one batched evaluation
@@ -793,14 +818,20 @@ def run_gpu(args):
     learned = learned_vs_plain(torch, api)
 
     cpu = None
+    parity = roots_parity(roots, last_grid[0], None, None, "committed fixture tests/golden/plain_search_circle_N50.json")
     if rank == 0 and not args.skip_cpu:
-        threads = os.cpu_count() or 1
         try:
-            v, tsec, npts = cpu_sample(args.cpu_sample_points, threads)
-            cpu = {"value": v / tsec if tsec > 0 else None, "unit": "resonances/s", "cores": threads, "kind": "port",
-                   "sample": "first %d of %d grid points + Newton/verification of their roots" % (npts, CFG["npoints"])}
+            pool = sweep_pool()
+            try:
+                v, tsec, oroots, osig, _ = cpu_search(pool)
+            finally:
+                pool.close()
+            cpu = {"value": v / tsec if tsec > 0 else None, "unit": "resonances/s", "cores": pool.workers,
+                   "kind": "port", "sample": CPU_SAMPLE + " (one step)"}
+            parity = roots_parity(roots, last_grid[0], oroots, osig, "oracle port, same run")
         except Exception as ex:   # the baseline must not hide the GPU line
-            cpu = {"value": None, "unit": "resonances/s", "cores": threads, "kind": "port", "error": str(ex)[:200]}
+            cpu = {"value": None, "unit": "resonances/s", "cores": os.cpu_count(), "kind": "port",
+                   "error": str(ex)[:200]}
         try:
             arnoldi["cpu_arpack"] = arnoldi_cpu(arn_mats)
         except Exception as ex:
@@ -815,8 +846,9 @@ def run_gpu(args):
             "metric": METRIC, "value": value, "unit": "resonances/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "l2": "256 MB buffer written between timed steps",
-                       "roots_per_step": tot_v / args.steps, "T_evals_per_step": nev_tot / args.steps},
+            "config": CONFIG,
+            "workload_stats": {"roots_per_step": tot_v / args.steps, "T_evals_per_step": nev_tot / args.steps},
+            "parity": parity,
             "e2e": {"value": e2e_v / (e2e_ms * 1e-3), "unit": "resonances/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches.value),

@@ -16,7 +16,8 @@ SPACE_P0, SPACE_P1 = 1, 2
 
 # every symbol include/hbem.h declares
 EXPORTS = [
-    "hbem_version", "hbem_status_string", "hbem_last_error", "hbem_set_device", "hbem_set_option", "hbem_hankel01",
+    "hbem_version", "hbem_status_string", "hbem_last_error", "hbem_set_device", "hbem_set_option", "hbem_get_option",
+    "hbem_hankel01",
     "hbem_stats_enable_timing", "hbem_stats_reset", "hbem_stats_read", "hbem_stats_read_points",
     "hbem_builder_create", "hbem_builder_destroy", "hbem_builder_info", "hbem_builder_is_adjacent",
     "hbem_assemble_dense", "hbem_assemble_dense_sub", "hbem_get_layer", "hbem_get_layer_device",
@@ -77,6 +78,7 @@ def load(path=LIB_PATH):
         "hbem_last_error": (ctypes.c_char_p, []),
         "hbem_set_device": (_i, [_i]),
         "hbem_set_option": (_i, [ctypes.c_char_p, _i]),
+        "hbem_get_option": (_i, [ctypes.c_char_p, _ip]),
         "hbem_hankel01": (_i, [_i, _dp, _i, _dp, _dp]),
         "hbem_stats_enable_timing": (None, [_i]),
         "hbem_stats_reset": (None, []),

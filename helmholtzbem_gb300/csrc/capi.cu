@@ -48,6 +48,9 @@ bool lu_solve_supported(int n);
 void lu_set_cluster_panels(int on);
 void lu_set_tensor_cores(int on);
 void mlp_set_tensor_cores(int on);
+int lu_get_cluster_panels();
+int lu_get_tensor_cores();
+int mlp_get_tensor_cores();
 cudaError_t launch_cgemm_f32(int m, int n, int k, const cplxf* A, long long lda, long long sa, const cplxf* B,
                              long long ldb, long long sb, cplxf* C, long long ldc, long long sc, int nmat,
                              int use_tc, int* err, cudaStream_t st);
@@ -86,7 +89,12 @@ std::atomic<long long> g_asm_points{0};   // quadrature points x media processed
 // pairs whose point data came from the builder's table, [6 + d] singular pairs that
 // computed it in the kernel
 std::atomic<long long> g_asm_split[9];
-int g_svd_fast = 1;           // dense sigma: FP32 Jacobi + FP64 refinement where it fits
+std::atomic<int> g_svd_fast{1};   // dense sigma: FP32 Jacobi + FP64 refinement where it fits
+// per host thread: set while a sweep redoes, with the polished kernel, matrices the
+// fast kernel could not finish; other threads keep the process-wide setting
+thread_local int t_svd_polished_only = 0;
+std::atomic<int> g_svd_force_redo{0};   // test hook: every fast-kernel result goes through the fallback
+inline bool svd_fast_on() { return g_svd_fast.load(std::memory_order_relaxed) && !t_svd_polished_only; }
 int g_arnoldi_maxit = 1000;   // block iterations of hbem_arnoldi_sv_batch*
 int g_plain_speculate = 1;    // plain search: speculative bisection points in small Newton rounds
 int g_plain_warm_start = 1;   // plain search: dense-kernel Jacobi warm-started from nearby V sets
@@ -390,6 +398,10 @@ int hbem_set_option(const char* name, int value) {
         g_svd_fast = value ? 1 : 0;
         return HBEM_OK;
     }
+    if (k == "svd_fast_force_redo") {
+        g_svd_force_redo = value ? 1 : 0;
+        return HBEM_OK;
+    }
     if (k == "mlp_tensor_cores") {
         mlp_set_tensor_cores(value);
         return HBEM_OK;
@@ -412,6 +424,22 @@ int hbem_set_option(const char* name, int value) {
         return HBEM_OK;
     }
     return fail(HBEM_ERR_INVALID, "set_option: unknown option " + k);
+}
+
+int hbem_get_option(const char* name, int* value) {
+    if (!name || !value) return fail(HBEM_ERR_INVALID, "get_option: bad argument");
+    const std::string k(name);
+    if (k == "lu_cluster_panels") *value = lu_get_cluster_panels();
+    else if (k == "lu_tensor_cores") *value = lu_get_tensor_cores();
+    else if (k == "svd_fast") *value = g_svd_fast.load();
+    else if (k == "svd_fast_force_redo") *value = g_svd_force_redo.load();
+    else if (k == "mlp_tensor_cores") *value = mlp_get_tensor_cores();
+    else if (k == "singular_table") *value = g_singular_table;
+    else if (k == "plain_warm_start") *value = g_plain_warm_start;
+    else if (k == "plain_speculate") *value = g_plain_speculate;
+    else if (k == "arnoldi_maxit") *value = g_arnoldi_maxit;
+    else return fail(HBEM_ERR_INVALID, "get_option: unknown option " + k);
+    return HBEM_OK;
 }
 
 int hbem_hankel01(int n, const double* z_host, int complex_arg, double* h0_host, double* h1_host) {
@@ -794,7 +822,7 @@ static int sv_batch(cudaStream_t st, int n, int nmat, unsigned d, const cplx* T,
         dsig = sig->as<double>();
     }
     std::vector<int> stat(nmat);
-    if (!sig_all_host && g_svd_fast && svd_fast_smem_bytes(n) <= 220 * 1024) {
+    if (!sig_all_host && svd_fast_on() && svd_fast_smem_bytes(n) <= 220 * 1024) {
         // FP32 Jacobi + FP64 refinement; matrices it cannot finish (singular T, a
         // far-field series that does not converge) are redone by the polished kernel
         HB_CK(launch_svd_fast(n, nmat, (int)d, T, mat_stride, der_stride, out.as<double>(), status.as<int>(), st,
@@ -802,7 +830,7 @@ static int sv_batch(cudaStream_t st, int n, int nmat, unsigned d, const cplx* T,
         g_launches += 1;
         HB_CK(cudaMemcpyAsync(stat.data(), status.p, (size_t)nmat * sizeof(int), cudaMemcpyDeviceToHost, st));
         HB_CK(cudaStreamSynchronize(st));
-        bool redo = false;
+        bool redo = g_svd_force_redo.load(std::memory_order_relaxed) != 0;
         for (int v : stat) redo |= v != 0;
         if (!redo) {
             HB_CK(cudaMemcpyAsync(out_host, out.p, (size_t)nmat * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1087,7 +1115,7 @@ int hbem_sweep_sigma_multi(const hbem_solop* ops, int nops, const int* counts, c
     if (!ops || nops < 1 || !counts || !k_host || !c_i_host || !out_host || d > 2)
         return fail(HBEM_ERR_INVALID, "sweep_sigma_multi: bad argument");
     size_t total = 0;
-    bool fast = g_svd_fast != 0;
+    bool fast = svd_fast_on();
     for (int i = 0; i < nops; ++i) {
         if (!ops[i] || counts[i] < 0) return fail(HBEM_ERR_INVALID, "sweep_sigma_multi: bad argument");
         total += (size_t)counts[i];
@@ -1142,13 +1170,13 @@ int hbem_sweep_sigma_multi(const hbem_solop* ops, int nops, const int* counts, c
     // matrices the fast kernel could not finish: redone by the polished kernel
     off = 0;
     for (int i = 0; i < nops; ++i) {
-        bool redo = false;
+        bool redo = g_svd_force_redo.load(std::memory_order_relaxed) != 0;
         for (int q = 0; q < counts[i]; ++q) redo |= pstat[off + q] != 0;
         if (redo) {
-            const int save = g_svd_fast;
-            g_svd_fast = 0;
+            const int save = t_svd_polished_only;
+            t_svd_polished_only = 1;
             const int r = hbem_sweep_sigma(ops[i], k_host + off, counts[i], c_o, c_i_host[i], d, out_host + 3 * off);
-            g_svd_fast = save;
+            t_svd_polished_only = save;
             if (r) return r;
         }
         off += (size_t)counts[i];
@@ -1192,7 +1220,7 @@ void count_launches(long long n) { g_launches += n; }
 // from the one-CTA dense kernel (its per-evaluation latency, not the GPU's
 // throughput, bounds a round, so a few more matrices per round cost little).
 int plain_speculate_ok(hbem_solop s) {
-    return s && g_plain_speculate && g_svd_fast && svd_fast_smem_bytes(2 * s->b->n) <= 220 * 1024;
+    return s && g_plain_speculate && svd_fast_on() && svd_fast_smem_bytes(2 * s->b->n) <= 220 * 1024;
 }
 
 int plain_warm_start_ok() { return g_plain_warm_start; }
@@ -1209,7 +1237,7 @@ int sweep_sigma_warm(hbem_solop s, const double* k_host, int nk, double c_o, dou
     hbem_builder b = s->b;
     const int n = 2 * b->n;
     const size_t mat = (size_t)n * n;
-    if (!g_svd_fast || svd_fast_smem_bytes(n) > 220 * 1024 || (size_t)nk * (d + 1) * mat * sizeof(cplx) > ((size_t)2 << 30))
+    if (!svd_fast_on() || svd_fast_smem_bytes(n) > 220 * 1024 || (size_t)nk * (d + 1) * mat * sizeof(cplx) > ((size_t)2 << 30))
         return fail(HBEM_ERR_UNSUPPORTED, "sweep_sigma_warm: the dense fast kernel does not take this batch");
     for (int i = 0; i < nk; ++i)
         if (warm_slot[i] >= npool || out_slot[i] >= npool)

@@ -944,6 +944,17 @@ namespace {
 std::mutex g_noalloc_mu;
 constexpr int kMaxDevices = 64;
 void* g_noalloc_ptr[kMaxDevices] = {nullptr};   // device address of the scratch, per device
+
+// p points into device (or managed) memory that device dev can use directly
+bool on_device(const void* p, int dev) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();   // the failed query's error is not the caller's
+        return false;
+    }
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == dev;
+}
 }  // namespace
 
 // See include/hbem.h.  The matrix must fit in shared memory (n <= 116) because the
@@ -962,11 +973,22 @@ extern "C" int hbem_sv_dense_batch_noalloc(int n, int nmat, unsigned d, const vo
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return set_error(HBEM_ERR_CUDA, cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return set_error(HBEM_ERR_INVALID, "sv_dense_batch_noalloc: device ordinal out of range");
+    // the kernel reads T and writes out / status on the current device: pointers to
+    // host memory or to another device are refused here (no allocation involved)
+    const void* ptrs[3] = {T_dev, out_dev, status_dev};
+    for (const void* q : ptrs) {
+        if (!on_device(q, dev))
+            return set_error(HBEM_ERR_INVALID,
+                             "sv_dense_batch_noalloc: T_dev, out_dev and status_dev must be memory of the current device");
+    }
     void* scratch = nullptr;
     {
         // first call on a device: resolve the device address of the fixed array with
-        // that device current (the host-side name is only a stand-in, not a device address)
+        // that device current (the host-side name is only a stand-in, not a device
+        // address).  A cached address that no longer maps this device's memory (the
+        // device was reset since) is resolved again.
         std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (g_noalloc_ptr[dev] && !on_device(g_noalloc_ptr[dev], dev)) g_noalloc_ptr[dev] = nullptr;
         if (!g_noalloc_ptr[dev]) {
             void* p = nullptr;
             e = cudaGetSymbolAddress(&p, g_noalloc_scratch);

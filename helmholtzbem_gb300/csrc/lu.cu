@@ -556,6 +556,8 @@ int g_lu_tensor_cores = 1;     // complex64 trailing updates on the tensor cores
 
 void lu_set_cluster_panels(int on) { g_lu_cluster_panels = on ? 1 : 0; }
 void lu_set_tensor_cores(int on) { g_lu_tensor_cores = on ? 1 : 0; }
+int lu_get_cluster_panels() { return g_lu_cluster_panels; }
+int lu_get_tensor_cores() { return g_lu_tensor_cores; }
 
 cudaError_t launch_cgemm_f32(int m, int n, int k, const cplxf* A, long long lda, long long sa, const cplxf* B,
                              long long ldb, long long sb, cplxf* C, long long ldc, long long sc, int nmat,

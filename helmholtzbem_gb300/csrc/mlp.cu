@@ -332,6 +332,7 @@ cudaError_t gemm_bf16(int M, int N, int K, const __nv_bfloat16* A, long long lda
 }
 
 void mlp_set_tensor_cores(int on) { g_mlp_tensor_cores = on != 0; }
+int mlp_get_tensor_cores() { return g_mlp_tensor_cores ? 1 : 0; }
 
 }  // namespace hbem
 

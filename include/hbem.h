@@ -59,6 +59,10 @@ int hbem_set_device(int device);
  *   "svd_fast" (default 1): dense sigma_min / sigma' / sigma'' (direct::sv*) of matrices
  *   up to order 100 by FP32 Jacobi plus FP64 refinement of the near singular triplets
  *   (one FP64 LU per matrix); 0 always uses the FP64-polished Jacobi kernel.
+ *   Matrices the fast kernel cannot finish are redone by the polished kernel; that
+ *   fallback is per call and per host thread and leaves this switch unchanged.
+ *   "svd_fast_force_redo" (default 0): 1 sends every fast-kernel result through that
+ *   fallback as well (more work, same results), so tests can exercise it.
  *   "arnoldi_maxit" (default 1000, >= 1): iteration cap of hbem_arnoldi_sv_batch*.
  *   "mlp_tensor_cores" (default 1): the MLP's BF16 products on tcgen05; 0 uses FP32 FMA.
  *   "singular_table" (default 1): coincident / adjacent panel pairs read the
@@ -71,6 +75,8 @@ int hbem_set_device(int device);
  *   Jacobi at a bracket end or Newton point starts from the right singular vectors
  *   of the nearest wavenumber already evaluated (same stopping rule, fewer sweeps). */
 int hbem_set_option(const char* name, int value);
+/* the current value of one of the switches above */
+int hbem_get_option(const char* name, int* value);
 
 /* Instrumentation (no counterpart in the reference, which prints std::chrono
  * timings, gen_sol_op.cpp:89-99 and randsvd.cpp:27-47): kernel launches issued
@@ -287,8 +293,15 @@ int hbem_sv_dense_batch_device(int n, int nmat, unsigned d, const void* T_dev, l
  * Working memory is a fixed 8 MiB array inside the library's device image
  * (held on every GPU that loads the library until the process exits).  Limits:
  * n <= 116 and nmat * n * n <= 524288; larger requests return HBEM_ERR_INVALID.
+ * T_dev, out_dev and status_dev must be device (or managed) memory of the current
+ * device; other pointers return HBEM_ERR_INVALID.
  * The first call on each device resolves the array's device address (with that
- * device current); make that first call before any stream capture.  All calls
+ * device current); make that first call before any stream capture.  Under lazy
+ * module loading (CUDA_MODULE_LOADING=LAZY, the CUDA 12+ default) that first call
+ * also loads the library's dense-SVD module with its array, which allocates and
+ * synchronises once: make it during set-up, outside the section that must not
+ * allocate.  After a device reset (cudaDeviceReset) the array is gone; the next
+ * call notices that and resolves it again, with the same one-time cost.  All calls
  * share the array and it keeps the previous call's contents: calls whose work
  * overlaps on the GPU (different streams, or concurrent host threads) race on it. */
 int hbem_sv_dense_batch_noalloc(int n, int nmat, unsigned d, const void* T_dev, long long mat_stride,

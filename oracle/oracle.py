@@ -937,6 +937,125 @@ def plain_sweep(evald, ks, tol=1e-8):
     return np.array(roots), sig
 
 
+# ----------------------------------------------------------------- the plain search over host cores
+
+# The reference's driver runs the plain search with std::execution::par
+# (examples/roots_newton_polygon_rsvd.cpp:172-177 over the grid wavenumbers,
+# :202-207 over the bracket ends, :254-265 over the candidates' Newton searches),
+# and each assembleDense is parallel inside (galerkin_builder.cpp:964-1013).
+# ``SweepPool`` gives the same structure on the host cores: a pool of worker
+# processes (started with ``spawn``), each holding its own operator, takes the
+# grid and the bracket ends one wavenumber per task and one Newton search per
+# candidate; a worker's assembly uses the cores the pool leaves idle.
+
+_WORKER = {}
+
+
+def _pool_init(kinds, params, order, c_o, c_i, qtest, qtrial):
+    _WORKER["so"] = SolutionsOperator(Builder(kinds, params, order, qtest, qtrial))
+    _WORKER["c"] = (c_o, c_i)
+
+
+def _pool_eval(task):
+    k, d, threads = task
+    c_o, c_i = _WORKER["c"]
+    return sv_derivs(*_WORKER["so"].gen_sol_op(k, c_o, c_i, d=d, threads=threads))
+
+
+def _pool_newton(task):
+    a, b, guess, tol, threads = task
+    c_o, c_i = _WORKER["c"]
+    so = _WORKER["so"]
+
+    def fn(x):
+        return float("nan") if x == x else guess
+
+    def both(x):
+        r = sv_derivs(*so.gen_sol_op(x, c_o, c_i, d=2, threads=threads))
+        return r[1], r[2]
+
+    return rtsafe(fn, both, a, b, tol)
+
+
+class SweepPool:
+    """Worker processes for the plain search of one scatterer and medium pair.
+    ``workers`` processes (default: all host cores) with one BLAS thread each."""
+
+    def __init__(self, kinds, params, order, c_o, c_i, workers=None, qtest=2, qtrial=2):
+        import concurrent.futures as cf
+        import multiprocessing as mp
+        lib()   # the shared library exists before the workers load it
+        self.workers = int(workers or os.cpu_count() or 1)
+        saved = {v: os.environ.get(v) for v in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS")}
+        for v in saved:
+            os.environ[v] = "1"
+        try:
+            self.ex = cf.ProcessPoolExecutor(max_workers=self.workers, mp_context=mp.get_context("spawn"),
+                                             initializer=_pool_init,
+                                             initargs=(np.asarray(kinds, np.int32), np.asarray(params, np.float64),
+                                                       order, float(c_o), float(c_i), qtest, qtrial))
+            list(self.ex.map(_pool_eval, [(1.0, 0, 1)] * self.workers))   # start every worker now
+        finally:
+            for v, old in saved.items():
+                if old is None:
+                    os.environ.pop(v, None)
+                else:
+                    os.environ[v] = old
+
+    def close(self):
+        self.ex.shutdown(wait=True)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def evald(self, klist, d):
+        """sigma and its first d derivatives at every wavenumber of klist, one task each;
+        the assembly of a task takes the cores the batch leaves idle."""
+        if len(klist) == 0:
+            return np.zeros((0, d + 1))
+        threads = max(1, self.workers // len(klist))
+        return np.array(list(self.ex.map(_pool_eval, [(float(k), d, threads) for k in klist])))
+
+    def plain_sweep(self, ks, tol=1e-8):
+        """``plain_sweep`` with the reference driver's parallel structure: returns
+        (roots, grid sigma, evaluations)."""
+        ks = np.asarray(ks, float)
+        sig = self.evald(list(ks), 0)[:, 0]
+        nev = ks.size
+        h = ks[1] - ks[0]
+        cands = [i for i in range(len(ks) - 2) if sig[i] - sig[i + 1] > 0.0 and sig[i + 2] - sig[i + 1] > 0.0]
+        ends = []
+        for i in cands:
+            ends += [ks[i], ks[i + 2]]
+        der = self.evald(ends, 1)[:, 1] if ends else np.zeros(0)
+        nev += len(ends)
+        tasks = []
+        for c, i in enumerate(cands):
+            d1, d2 = der[2 * c], der[2 * c + 1]
+            if not (d1 < 0.0 < d2):
+                continue
+            guess = quartic_guess(ks[i], h, sig[i], sig[i + 1], sig[i + 2], d1, d2, tol)
+            tasks.append((ks[i], ks[i] + 2 * h, guess, tol))
+        threads = max(1, self.workers // max(1, len(tasks)))
+        roots = []
+        for root, ok, it in self.ex.map(_pool_newton, [t + (threads,) for t in tasks]):
+            nev += it
+            if ok and root == root:
+                roots.append(root)
+        return np.array(roots), sig, nev
+
+    def verify(self, roots, tol=1e-8):
+        """Roots whose sigma' changes sign from root - tol to root + tol."""
+        roots = np.asarray(roots, float)
+        if roots.size == 0:
+            return np.zeros(0, bool)
+        d1 = self.evald(list(roots - tol) + list(roots + tol), 1)[:, 1]
+        return (d1[:roots.size] <= 0.0) & (d1[roots.size:] >= 0.0)
+
+
 # ----------------------------------------------------------------- adaptive search
 
 _M64 = (1 << 64) - 1

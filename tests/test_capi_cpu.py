@@ -132,7 +132,11 @@ def test_every_documented_option_is_accepted():
     block = src[src.index("Process-wide switches"):src.index("int hbem_set_option")]
     documented = re.findall(r'"(\w+)" \(default (\d+)', block)
     assert {"svd_fast", "singular_table", "plain_speculate", "plain_warm_start"} <= {n for n, _ in documented}
+    import ctypes
+    v = ctypes.c_int(-1)
     for name, default in documented:
         assert L.hbem_set_option(name.encode(), int(default)) == 0, name
+        assert L.hbem_get_option(name.encode(), ctypes.byref(v)) == 0 and v.value == int(default), name
     assert L.hbem_set_option(b"no_such_switch", 1) == 1
+    assert L.hbem_get_option(b"no_such_switch", ctypes.byref(v)) == 1
     assert b"unknown option" in L.hbem_last_error()

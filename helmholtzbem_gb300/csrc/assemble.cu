@@ -637,26 +637,45 @@ __global__ void __launch_bounds__(128) k_singular(DevMesh M, const SingularTask*
 // function 1 (1-t)  (continuous_space.hpp:38-47).
 __device__ __forceinline__ int p1_panel(int m, int a, int N) { return a == 0 ? (m == 0 ? N - 1 : m - 1) : m; }
 
+// Spaces of a layer matrix.  `sp` bit 0: the test space is P0, bit 1: the trial space
+// is P0 (DiscontinuousSpace<0>, discontinuous_space.hpp:33-127: one dof per panel,
+// LocGlobMap(1, n, N) = n, shape function 1).  The pair blocks hold the integrals of
+// the two P1 local functions t and 1 - t of each panel; since t + (1 - t) = 1 (and
+// the derivatives, +1 and -1, sum to 0), the P0 integral of a panel is the sum of its
+// two P1 entries: a P0 dof m takes both local functions of panel m.
+__device__ __forceinline__ int dof_panel(int m, int a, int N, bool p0) { return p0 ? m : p1_panel(m, a, N); }
+
+// row / column spaces of layer L (galerkin_builder.cpp:936-946): the double layer is
+// test x trial, the hypersingular trial x trial, the single layer test x test
+__device__ __forceinline__ bool row_p0(int L, int sp) { return L == 1 ? (sp & 2) != 0 : (sp & 1) != 0; }
+__device__ __forceinline__ bool col_p0(int L, int sp) { return L == 2 ? (sp & 1) != 0 : (sp & 2) != 0; }
+
+// the P1 local entry (a on panel i, b on panel j) of layer L from the pair blocks
+__device__ __forceinline__ cplx pair_entry(const cplx* locj, int L, int t, int D1, int i, int j, int a, int b) {
+    const cplx* blk;
+    int e;
+    if (L == 0) {
+        if (i >= j) { blk = locj + tri_index(i, j) * D1 * kLocPerD + t * kLocPerD + 0; e = 2 * a + b; }
+        else { blk = locj + tri_index(j, i) * D1 * kLocPerD + t * kLocPerD + 4; e = 2 * a + b; }
+    } else {
+        int off = (L == 1) ? 8 : 12;
+        if (i >= j) { blk = locj + tri_index(i, j) * D1 * kLocPerD + t * kLocPerD + off; e = 2 * a + b; }
+        else { blk = locj + tri_index(j, i) * D1 * kLocPerD + t * kLocPerD + off; e = 2 * b + a; }
+    }
+    return blk[e];
+}
+
 // layer value (before the i/4 factor) at dofs (m, n): L = 0 double layer, 1 hypersingular, 2 single layer
-__device__ __forceinline__ cplx layer_entry(const cplx* locj, int N, int L, int t, int D1, int m, int n) {
+__device__ __forceinline__ cplx layer_entry(const cplx* locj, int N, int L, int t, int D1, int m, int n, int sp) {
     cplx s = mk(0.);
+    const bool rp0 = row_p0(L, sp), cp0 = col_p0(L, sp);
 #pragma unroll
     for (int a = 0; a < 2; ++a) {
-        int i = p1_panel(m, a, N);
+        int i = dof_panel(m, a, N, rp0);
 #pragma unroll
         for (int b = 0; b < 2; ++b) {
-            int j = p1_panel(n, b, N);
-            const cplx* blk;
-            int e;
-            if (L == 0) {
-                if (i >= j) { blk = locj + tri_index(i, j) * D1 * kLocPerD + t * kLocPerD + 0; e = 2 * a + b; }
-                else { blk = locj + tri_index(j, i) * D1 * kLocPerD + t * kLocPerD + 4; e = 2 * a + b; }
-            } else {
-                int off = (L == 1) ? 8 : 12;
-                if (i >= j) { blk = locj + tri_index(i, j) * D1 * kLocPerD + t * kLocPerD + off; e = 2 * a + b; }
-                else { blk = locj + tri_index(j, i) * D1 * kLocPerD + t * kLocPerD + off; e = 2 * b + a; }
-            }
-            s += blk[e];
+            int j = dof_panel(n, b, N, cp0);
+            s += pair_entry(locj, L, t, D1, i, j, a, b);
         }
     }
     return s;
@@ -665,31 +684,26 @@ __device__ __forceinline__ cplx layer_entry(const cplx* locj, int N, int L, int 
 // The same with the sub-matrix rule of GalerkinBuilder::assembleDense(k, c, layers, d,
 // row, col, rows, cols) (galerkin_builder.cpp:918-1009): only panel pairs {i, j} with
 // i in [row, row + rows) and j in [col, col + cols) (either order) contribute, in both
-// orientations, to the dof block [row, row + rows) x [col, col + cols).
+// orientations, to the dof block [row, row + rows) x [col, col + cols).  With test !=
+// trial spaces the double layer takes ordered pairs only (row panel i in the row
+// range, column panel j in the column range; galerkin_builder.cpp:966-971,997-1001).
 __device__ __forceinline__ bool in_sub(int i, int j, int row, int rows, int col, int cols) {
     return (i >= row && i < row + rows && j >= col && j < col + cols) ||
            (j >= row && j < row + rows && i >= col && i < col + cols);
 }
 
 __device__ __forceinline__ cplx layer_entry_sub(const cplx* locj, int N, int L, int t, int D1, int m, int n, int row,
-                                                int rows, int col, int cols) {
+                                                int rows, int col, int cols, int sp) {
     cplx s = mk(0.);
+    const bool rp0 = row_p0(L, sp), cp0 = col_p0(L, sp);
+    const bool ordered = L == 0 && (sp == 1 || sp == 2);
     for (int a = 0; a < 2; ++a) {
-        int i = p1_panel(m, a, N);
+        int i = dof_panel(m, a, N, rp0);
         for (int b = 0; b < 2; ++b) {
-            int j = p1_panel(n, b, N);
-            if (!in_sub(i, j, row, rows, col, cols)) continue;
-            const cplx* blk;
-            int e;
-            if (L == 0) {
-                if (i >= j) { blk = locj + tri_index(i, j) * D1 * kLocPerD + t * kLocPerD + 0; e = 2 * a + b; }
-                else { blk = locj + tri_index(j, i) * D1 * kLocPerD + t * kLocPerD + 4; e = 2 * a + b; }
-            } else {
-                int off = (L == 1) ? 8 : 12;
-                if (i >= j) { blk = locj + tri_index(i, j) * D1 * kLocPerD + t * kLocPerD + off; e = 2 * a + b; }
-                else { blk = locj + tri_index(j, i) * D1 * kLocPerD + t * kLocPerD + off; e = 2 * b + a; }
-            }
-            s += blk[e];
+            int j = dof_panel(n, b, N, cp0);
+            const bool take = ordered ? (i >= row && i < row + rows && j >= col && j < col + cols)
+                                      : in_sub(i, j, row, rows, col, cols);
+            if (take) s += pair_entry(locj, L, t, D1, i, j, a, b);
         }
     }
     return s;
@@ -697,7 +711,7 @@ __device__ __forceinline__ cplx layer_entry_sub(const cplx* locj, int N, int L, 
 
 // sub-matrix layers: out[L][t] rows x cols col-major, x i/4
 __global__ void k_gather_layers_sub(int N, int D1, int layers, const cplx* loc, long long npair, int job, int row,
-                                    int rows, int col, int cols, cplx* out) {
+                                    int rows, int col, int cols, int sp, cplx* out) {
     long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long tot = (long long)rows * cols;
     if (idx >= tot) return;
@@ -708,7 +722,7 @@ __global__ void k_gather_layers_sub(int N, int D1, int layers, const cplx* loc, 
     for (int L = 0; L < 3; ++L) {
         if (!(layers & lbit[L])) continue;
         for (int t = 0; t < D1; ++t) {
-            cplx v = layer_entry_sub(lj, N, L, t, D1, m, n, row, rows, col, cols);
+            cplx v = layer_entry_sub(lj, N, L, t, D1, m, n, row, rows, col, cols, sp);
             out[(long long)(slot * D1 + t) * tot + idx] = mk(-0.25 * v.im, 0.25 * v.re);
         }
         ++slot;
@@ -718,7 +732,7 @@ __global__ void k_gather_layers_sub(int N, int D1, int layers, const cplx* loc, 
 // T(k) and its derivatives for nk wavenumbers; jobs are (k, c_i), (k, c_o) interleaved.
 // T is column-major 2N x 2N per (k, t); blocks (gen_sol_op.cpp:59-74):
 //   T11 = K_i - K_o + M,  T12 = V_o - V_i,  T21 = W_o - W_i,  T22 = K_o - K_i + M^T
-__global__ void k_gather_T(int N, int D1, const cplx* loc, long long npair, const double* Mmass, cplx* T) {
+__global__ void k_gather_T(int N, int D1, const cplx* loc, long long npair, const double* Mmass, int sp, cplx* T) {
     const long long n2 = 2LL * N;
     long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (idx >= n2 * n2) return;
@@ -734,8 +748,8 @@ __global__ void k_gather_T(int N, int D1, const cplx* loc, long long npair, cons
     else if (bm && !bn) { L = 1; sgn = -1.; }     // W_o - W_i
     else { L = 0; sgn = -1.; }                    // K_o - K_i
     for (int t = 0; t < D1; ++t) {
-        cplx vi = layer_entry(li, N, L, t, D1, mm, nn);
-        cplx vo = layer_entry(lo, N, L, t, D1, mm, nn);
+        cplx vi = layer_entry(li, N, L, t, D1, mm, nn, sp);
+        cplx vo = layer_entry(lo, N, L, t, D1, mm, nn, sp);
         cplx d = sgn * (vi - vo);
         cplx val = mk(-0.25 * d.im, 0.25 * d.re);   // x i/4
         if (t == 0 && bm == bn) val.re += bm ? Mmass[nn + (long long)mm * N] : Mmass[mm + (long long)nn * N];
@@ -744,7 +758,8 @@ __global__ void k_gather_T(int N, int D1, const cplx* loc, long long npair, cons
 }
 
 // Separate layer matrices (GalerkinBuilder getters) for job `job`: out[L][t] N x N col-major, x i/4.
-__global__ void k_gather_layers(int N, int D1, int layers, const cplx* loc, long long npair, int job, cplx* out) {
+__global__ void k_gather_layers(int N, int D1, int layers, const cplx* loc, long long npair, int job, int sp,
+                                cplx* out) {
     long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     long long nn2 = (long long)N * N;
     if (idx >= nn2) return;
@@ -755,7 +770,7 @@ __global__ void k_gather_layers(int N, int D1, int layers, const cplx* loc, long
     for (int L = 0; L < 3; ++L) {
         if (!(layers & lbit[L])) continue;
         for (int t = 0; t < D1; ++t) {
-            cplx v = layer_entry(lj, N, L, t, D1, m, n);
+            cplx v = layer_entry(lj, N, L, t, D1, m, n, sp);
             out[(long long)(slot * D1 + t) * nn2 + idx] = mk(-0.25 * v.im, 0.25 * v.re);
         }
         ++slot;
@@ -845,27 +860,29 @@ cudaError_t launch_local(const DevMesh& M, const SingularTask* tasks, int ntasks
     return launch_local_t<2, false>(M, tasks, ntasks, jobs, njobs, loc, st);
 }
 
-cudaError_t launch_gather_T(int N, int d, const cplx* loc, const double* Mmass, int nk, cplx* T, cudaStream_t st) {
+cudaError_t launch_gather_T(int N, int d, const cplx* loc, const double* Mmass, int nk, int sp, cplx* T,
+                            cudaStream_t st) {
     long long npair = (long long)N * (N + 1) / 2;
     long long tot = 4LL * N * N;
     dim3 g((unsigned)((tot + 255) / 256), nk);
-    k_gather_T<<<g, 256, 0, st>>>(N, d + 1, loc, npair, Mmass, T);
+    k_gather_T<<<g, 256, 0, st>>>(N, d + 1, loc, npair, Mmass, sp, T);
     return cudaGetLastError();
 }
 
 cudaError_t launch_gather_layers_sub(int N, int d, int layers, const cplx* loc, int job, int row, int rows, int col,
-                                     int cols, cplx* out, cudaStream_t st) {
+                                     int cols, int sp, cplx* out, cudaStream_t st) {
     long long npair = (long long)N * (N + 1) / 2;
     long long tot = (long long)rows * cols;
     k_gather_layers_sub<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(N, d + 1, layers, loc, npair, job, row, rows,
-                                                                       col, cols, out);
+                                                                       col, cols, sp, out);
     return cudaGetLastError();
 }
 
-cudaError_t launch_gather_layers(int N, int d, int layers, const cplx* loc, int job, cplx* out, cudaStream_t st) {
+cudaError_t launch_gather_layers(int N, int d, int layers, const cplx* loc, int job, int sp, cplx* out,
+                                 cudaStream_t st) {
     long long npair = (long long)N * (N + 1) / 2;
     long long tot = (long long)N * N;
-    k_gather_layers<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(N, d + 1, layers, loc, npair, job, out);
+    k_gather_layers<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(N, d + 1, layers, loc, npair, job, sp, out);
     return cudaGetLastError();
 }
 

@@ -22,10 +22,12 @@ cudaError_t launch_singular_geo(const DevMesh& M, const SingularTask* tasks, int
                                 cudaStream_t st);
 cudaError_t launch_local(const DevMesh& M, const SingularTask* tasks, int ntasks, const Job* jobs, int njobs,
                          bool real_k, int d, cplx* loc, cudaStream_t st);
-cudaError_t launch_gather_T(int N, int d, const cplx* loc, const double* Mmass, int nk, cplx* T, cudaStream_t st);
-cudaError_t launch_gather_layers(int N, int d, int layers, const cplx* loc, int job, cplx* out, cudaStream_t st);
+cudaError_t launch_gather_T(int N, int d, const cplx* loc, const double* Mmass, int nk, int sp, cplx* T,
+                            cudaStream_t st);
+cudaError_t launch_gather_layers(int N, int d, int layers, const cplx* loc, int job, int sp, cplx* out,
+                                 cudaStream_t st);
 cudaError_t launch_gather_layers_sub(int N, int d, int layers, const cplx* loc, int job, int row, int rows, int col,
-                                     int cols, cplx* out, cudaStream_t st);
+                                     int cols, int sp, cplx* out, cudaStream_t st);
 cudaError_t launch_projection(int N, const double* id, const double* sb, const double* lr, cplx* T, int nmat,
                               cudaStream_t st);
 cudaError_t launch_svd(int n, int nmat, int D, int which, const cplx* T, long long mat_stride, long long der_stride,
@@ -286,6 +288,9 @@ struct hbem_builder_s {
     int asm_layers = 0, asm_d = -1, asm_rows = 0, asm_cols = 0;
 
     long long npair() const { return (long long)n * (n + 1) / 2; }
+    // the gather's space bits: 1 test space P0, 2 trial space P0
+    int sp() const { return (qtest == HBEM_SPACE_P0 ? 1 : 0) | (qtrial == HBEM_SPACE_P0 ? 2 : 0); }
+    bool p1p1() const { return qtest == HBEM_SPACE_P1 && qtrial == HBEM_SPACE_P1; }
     DevMesh view() const {
         DevMesh M;
         M.n = n; M.p = p; M.nc = nc; M.lines = lines;
@@ -463,8 +468,8 @@ int hbem_builder_create(int npanels, const int* kinds, const double* params, int
                         hbem_builder* out) {
     if (!out || !kinds || !params || npanels < 3 || order < 2 || order > 32)
         return fail(HBEM_ERR_INVALID, "builder: need >= 3 panels and 2 <= order <= 32");
-    if (q_test != HBEM_SPACE_P1 || q_trial != HBEM_SPACE_P1)
-        return fail(HBEM_ERR_UNSUPPORTED, "builder: the GPU path assembles P1/P1 spaces");
+    if ((q_test != HBEM_SPACE_P0 && q_test != HBEM_SPACE_P1) || (q_trial != HBEM_SPACE_P0 && q_trial != HBEM_SPACE_P1))
+        return fail(HBEM_ERR_INVALID, "builder: spaces are P0 (1) or P1 (2)");
     for (int i = 0; i < npanels; ++i)
         if (kinds[i] != HBEM_PANEL_LINE && kinds[i] != HBEM_PANEL_ARC) return fail(HBEM_ERR_INVALID, "builder: bad panel kind");
     HB_CK(cudaSetDevice(g_device));
@@ -610,10 +615,11 @@ int hbem_assemble_dense_sub(hbem_builder b, double k_re, double k_im, double c, 
     HB_CK(local_assembly(b->view(), b->d_tasks.as<SingularTask>(), (int)b->tasks.size(), b->n, b->d_jobs.as<Job>(), 1,
                          real_k, (int)d, b->d_loc.as<cplx>(), b->st));
     if (rows == (unsigned)b->n && cols == (unsigned)b->n)
-        HB_CK(launch_gather_layers(b->n, (int)d, (int)layers, b->d_loc.as<cplx>(), 0, b->d_layers.as<cplx>(), b->st));
+        HB_CK(launch_gather_layers(b->n, (int)d, (int)layers, b->d_loc.as<cplx>(), 0, b->sp(), b->d_layers.as<cplx>(),
+                                   b->st));
     else
         HB_CK(launch_gather_layers_sub(b->n, (int)d, (int)layers, b->d_loc.as<cplx>(), 0, (int)row, (int)rows,
-                                       (int)col, (int)cols, b->d_layers.as<cplx>(), b->st));
+                                       (int)col, (int)cols, b->sp(), b->d_layers.as<cplx>(), b->st));
     g_launches += 1;
     HB_CK(cudaStreamSynchronize(b->st));
     b->asm_layers = (int)layers;
@@ -663,6 +669,10 @@ int hbem_solop_create(hbem_builder b, int proj, hbem_solop* out) {
     if (!b || !out) return fail(HBEM_ERR_INVALID, "null argument");
     HB_CK(cudaSetDevice(b->device));
     const int N = b->n;
+    if (proj && b->qtest != b->qtrial)
+        return fail(HBEM_ERR_UNSUPPORTED,
+                    "solutions operator: the projection needs test space = trial space (the mass matrix of P0 x P1 "
+                    "is not symmetric)");
     hbem_solop s = new hbem_solop_s();
     s->b = b;
     s->proj = proj ? 1 : 0;
@@ -671,18 +681,22 @@ int hbem_solop_create(hbem_builder b, int proj, hbem_solop* out) {
     const int mo = b->lines ? 2 * std::max(b->qtest, b->qtrial) : b->p;
     std::vector<double> x(mo), w(mo);
     gauss_legendre(0., 1., mo, x.data(), w.data());
+    // local functions (continuous_space.hpp:38-47, discontinuous_space.hpp:38-44): P1
+    // t (dof i + 1) and 1 - t (dof i) on panel i; P0 the constant 1 (dof i)
+    auto shape = [](int q, int l, double t) { return q == HBEM_SPACE_P0 ? 1. : (l == 0 ? t : 1. - t); };
+    auto dof = [N](int q, int l, int i) { return q == HBEM_SPACE_P0 ? i : (l == 0 ? (i + 1) % N : i); };
     s->M.assign((size_t)N * N, 0.);
     for (int i = 0; i < N; ++i) {
         HPanel P{b->kind[i], &b->par[5 * (size_t)i]};
-        for (int ii = 0; ii < 2; ++ii)
-            for (int jj = 0; jj < 2; ++jj) {
-                int II = ii == 0 ? (i + 1) % N : i, JJ = jj == 0 ? (i + 1) % N : i;
+        for (int ii = 0; ii < b->qtest; ++ii)
+            for (int jj = 0; jj < b->qtrial; ++jj) {
+                int II = dof(b->qtest, ii, i), JJ = dof(b->qtrial, jj, i);
                 double sum = 0.;
                 for (int k = 0; k < mo; ++k) {
                     cplx pt, tan;
                     double tn;
                     P.at01(x[k], pt, tan, tn);
-                    double F = (jj == 0 ? x[k] : 1. - x[k]) * tn, G = ii == 0 ? x[k] : 1. - x[k];
+                    double F = shape(b->qtrial, jj, x[k]) * tn, G = shape(b->qtest, ii, x[k]);
                     sum = sum + w[k] * F * G;
                 }
                 s->M[II + (size_t)JJ * N] += sum;
@@ -770,7 +784,7 @@ static int gen_T_batch(hbem_solop s, const double* k_host, const double* kim_hos
         HB_CK(local_assembly(b->view(), b->d_tasks.as<SingularTask>(), (int)b->tasks.size(), b->n, b->d_jobs.as<Job>(),
                              2 * kn, real_k, (int)d, b->d_loc.as<cplx>(), b->st));
         cplx* Tk = T_dev + (size_t)k0 * (d + 1) * mat;
-        HB_CK(launch_gather_T(N, (int)d, b->d_loc.as<cplx>(), s->d_M.as<double>(), kn, Tk, b->st));
+        HB_CK(launch_gather_T(N, (int)d, b->d_loc.as<cplx>(), s->d_M.as<double>(), kn, b->sp(), Tk, b->st));
         g_launches += 1;
         if (s->proj) {
             HB_CK(launch_projection(N, s->d_id.as<double>(), s->d_sb.as<double>(), s->d_lr.as<double>(), Tk,
@@ -1193,6 +1207,8 @@ namespace hbem {
 // host panel data and settings of a solutions operator's mesh
 int solop_mesh(hbem_solop s, int* n, const int** kinds, const double** par, int* proj, int* device) {
     if (!s) return fail(HBEM_ERR_INVALID, "null solutions operator");
+    if (!s->b->p1p1())
+        return fail(HBEM_ERR_UNSUPPORTED, "the transmission problem needs P1 test and trial spaces (its traces are P1)");
     *n = s->b->n;
     *kinds = s->b->kind.data();
     *par = s->b->par.data();

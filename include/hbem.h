@@ -102,8 +102,13 @@ int hbem_hankel01(int n, const double* z_host, int complex_arg, double* h0_host,
 
 /* BuilderData(mesh, test_space, trial_space, order) + GalerkinBuilder(data)
  * (include/galerkin_builder.hpp:43-46, 200; source/galerkin_builder.cpp:17-187).
- * The mesh is given as panels; this build assembles square P1/P1 spaces
- * (q_test == q_trial == HBEM_SPACE_P1) and returns HBEM_ERR_UNSUPPORTED otherwise. */
+ * The mesh is given as panels; q_test, q_trial select ContinuousSpace<1>
+ * (HBEM_SPACE_P1, include/continuous_space.hpp:33-152) or DiscontinuousSpace<0>
+ * (HBEM_SPACE_P0, include/discontinuous_space.hpp:33-127) for the test and trial
+ * spaces.  As in the reference, the double layer is test x trial, the hypersingular
+ * trial x trial and the single layer test x test (galerkin_builder.cpp:936-946);
+ * with test != trial spaces the double layer takes every ordered panel pair
+ * (the non-square branch, galerkin_builder.cpp:966-1009).                         */
 int hbem_builder_create(int npanels, const int* kinds, const double* params, int order, int q_test, int q_trial,
                         hbem_builder* out);
 int hbem_builder_destroy(hbem_builder b);
@@ -134,7 +139,11 @@ int hbem_get_layer_device(hbem_builder b, unsigned layer, unsigned d, const void
 /* ------------------------------------------------------------------ solutions operator */
 
 /* SolutionsOperator(builder_data, proj) (include/gen_sol_op.hpp:40-60;
- * source/utilities/gen_sol_op.cpp:23-43): mass matrix and projection factor. */
+ * source/utilities/gen_sol_op.cpp:23-43): mass matrix of the builder's test and
+ * trial spaces and projection factor.  proj != 0 needs test space = trial space:
+ * for P0 x P1 the mass matrix is not symmetric and the reference's LDL^T would read
+ * only its lower triangle (HBEM_ERR_UNSUPPORTED here).  The transmission problem
+ * (hbem_tp_*) needs P1/P1.                                                      */
 int hbem_solop_create(hbem_builder b, int proj, hbem_solop* out);
 int hbem_solop_destroy(hbem_solop s);
 /* SolutionsOperator::mass_matrix() (include/gen_sol_op.hpp:105): N x N real, column-major */

@@ -39,10 +39,14 @@ Pieces and the reference code each one restates:
   block iteration the GPU uses in its place.
 
 Parity status: Hankel values pinned by the reference's known answers
-(test/googletest/solutions_test.cpp:55-72) and by mpmath/scipy; matrices,
-singular values and roots are NOT pinned by reference fixtures (none exist for
-this path in the reference tree) -- parity unpinned at that level, checked
-analytically instead.
+(test/googletest/solutions_test.cpp:55-72) and by mpmath/scipy.  The operator
+matrices (V, K, W and their k-derivatives, P1 and P0 spaces) are cross-checked to
+~1e-14 against a second, independent restatement of the reference's per-operator
+assembly files (``legacy_ops.py``: numpy quadrature nodes, scipy Hankel
+functions).  The reference tree holds no golden rows, singular values or roots
+for this path (its operator tests read files from the author's machine), so
+parity with the reference's own outputs stays unpinned at that level; singular
+values and roots are checked analytically and by perturbation theory instead.
 """
 from __future__ import annotations
 

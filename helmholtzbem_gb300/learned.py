@@ -143,8 +143,11 @@ def evaluate(net, seeds, plain_points=210, coarse_points=43, tol=1e-8, match=1e-
       coarse_batched   -- a coarse_points-point grid of true sigma per window
       learned_coarse_batched -- the coarse grid plus true sigma at the network's
                           predicted minima (what the network adds to the coarse grid)
-    Returns per method: roots, recall against plain, roots not in plain, sigma
-    evaluations, seconds, verified resonances per second."""
+    Returns per method: roots, recall against plain, roots not in plain (false
+    positives: Newton converged to a stationary point of sigma_min that the plain
+    search does not report), sigma evaluations, seconds, and resonances per second
+    counting only the roots that match a plain root (`res_per_s`) or every root
+    returned (`res_per_s_all`)."""
     import torch
     cases = [draw(s) for s in seeds]
     ops = [operator(a, b) for (a, b, _, _) in cases]
@@ -156,8 +159,9 @@ def evaluate(net, seeds, plain_points=210, coarse_points=43, tol=1e-8, match=1e-
     def record(name, roots, evals, t):
         n = sum(r.size for r in roots)
         hit, extra = _match(res_plain, roots, match) if name != "plain" else (n, 0)
-        res[name] = {"roots": n, "recall": hit / max(1, n_plain), "not_in_plain": extra, "evals": evals,
-                     "seconds": t, "res_per_s": n / t if t > 0 else None}
+        res[name] = {"roots": n, "matched": hit, "recall": hit / max(1, n_plain), "not_in_plain": extra,
+                     "evals": evals, "seconds": t, "res_per_s": hit / t if t > 0 else None,
+                     "res_per_s_all": n / t if t > 0 else None}
 
     ops[0].find_resonances_plain(k0[0], k0[0] + W, plain_points, c_o, ci[0], tol=tol)      # warm-up
     torch.cuda.synchronize()

@@ -49,9 +49,14 @@ def test_sweep_sigma_multi_matches_single_operator_sweeps():
 
 
 def test_shipped_network_proposes_most_resonances():
-    """The packaged network on held-out windows: most plain-search roots are found from
-    its proposals alone (0.85 on 100 windows when it was trained)."""
+    """The packaged network on the 40 held-out windows of the benchmark (seeds
+    20000..20039): 75 of the plain search's 91 roots are found from its proposals
+    alone (recall 0.824 measured), and the network adds recall to a coarse grid."""
     net = L.default_network()
-    res = L.evaluate(net, list(range(20050, 20062)), plain_points=210, coarse_points=43)
-    assert res["learned_batched"]["recall"] >= 0.6
-    assert res["learned_coarse_batched"]["recall"] >= res["coarse_batched"]["recall"] - 0.1
+    res = L.evaluate(net, list(range(20000, 20040)), plain_points=210, coarse_points=43)
+    assert res["plain"]["roots"] == 91
+    assert res["learned_batched"]["recall"] >= 0.82
+    # resonances per second count only roots that match a plain root
+    lb = res["learned_batched"]
+    assert abs(lb["res_per_s"] * lb["seconds"] - lb["matched"]) < 1e-6 * lb["matched"]
+    assert res["learned_coarse_batched"]["recall"] >= res["coarse_batched"]["recall"]

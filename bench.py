@@ -457,16 +457,9 @@ def precision_at_scale(torch, C, api, geometry, lib, ks=(40.0, 41.0)):
                                       "fp64_rsvd": [float(x) for x in np.abs(out[0] - arn) / arn]}}
 
 
-def batching_sample(torch, C, api, geometry, lib, nk=16):
-    """Batching configuration on a bounded sample: 8 seeded scatterers (s = 0..3 star
-    polygons with 8..40 vertices, s = 4..7 Fourier-sum curves, seed 3000 + s), N =
-    100, 200, ..., 800 line panels, c_i ~ U[2, 25], c_o = 1, order 11, nk wavenumbers
-    per scatterer uniform on [1, 30] (the configuration's 256 per scatterer, 2048 T(k)
-    in all, would take ~45 s of FP64 assembly); per scatterer one batched assembly and
-    one batched mixed-precision rSVD (sketch 12, q = 2).  Reports T(k)/s."""
-    import ctypes
-    tot_ms, tot_T, asm_ms_all, rs_ms_all, per = 0.0, 0, 0.0, 0.0, []
-    ev = lambda: torch.cuda.Event(enable_timing=True)   # noqa: E731
+def batching_scatterers(geometry, api, nk):
+    """The 8 seeded scatterers of the batching configuration with their c_i and k."""
+    out = []
     for sidx in range(8):
         seed = 3000 + sidx
         rng = np.random.default_rng(seed)
@@ -479,10 +472,40 @@ def batching_sample(torch, C, api, geometry, lib, nk=16):
             mesh = geometry.fourier_curve(a, b, N)
         c_i = float(rng.uniform(2.0, 25.0))
         ks = np.sort(rng.uniform(1.0, 30.0, nk))
-        so = api.SolutionsOperator(api.BuilderData(mesh, order=11))
+        out.append((seed, N, mesh, c_i, ks, api.SolutionsOperator(api.BuilderData(mesh, order=11))))
+    return out
+
+
+def batching_sample(torch, C, api, geometry, lib, nk=16, peak=None):
+    """Batching configuration on a bounded sample: 8 seeded scatterers (s = 0..3 star
+    polygons with 8..40 vertices, s = 4..7 Fourier-sum curves, seed 3000 + s), N =
+    100, 200, ..., 800 line panels, c_i ~ U[2, 25], c_o = 1, order 11, nk wavenumbers
+    per scatterer uniform on [1, 30] (the configuration's 256 per scatterer, 2048 T(k)
+    in all, run under --full-configs); sigma_min by the mixed-precision rSVD (sketch 12,
+    q = 2).  Two ways: one batched assembly per scatterer, and every scatterer's
+    panel pairs in one assembly launch (hbem_gen_sol_op_multi_device).  Reports T(k)/s
+    and the assembly's FP64 rate."""
+    import ctypes
+    ev = lambda: torch.cuda.Event(enable_timing=True)   # noqa: E731
+    scat = batching_scatterers(geometry, api, nk)
+    sketches = [torch.from_numpy(np.ascontiguousarray(api.randGaussian(2 * N, 12, seed=seed).T)).cuda()
+                for (seed, N, _, _, _, _) in scat]
+
+    def rsvd_all(Ts):
+        outs = []
+        for (seed, N, _, _, ks, _), T, R in zip(scat, Ts, sketches):
+            n = 2 * N
+            out = np.zeros(len(ks))
+            C.check(lib.hbem_rsvd_sv_batch_device_ex(n, len(ks), 0, ctypes.c_void_p(T.data_ptr()), n * n, n * n,
+                                                     ctypes.c_void_p(R.data_ptr()), 12, 2, 1, 3, C.dptr(out)))
+            outs.append(out)
+        return outs
+
+    # (a) one batched assembly per scatterer
+    tot_ms, asm_ms_all, rs_ms_all, per = 0.0, 0.0, 0.0, []
+    for (seed, N, _, c_i, ks, so), R in zip(scat, sketches):
         n = 2 * N
         T = torch.empty((nk, n, n), dtype=torch.complex128, device="cuda")
-        R = torch.from_numpy(np.ascontiguousarray(api.randGaussian(n, 12, seed=seed).T)).cuda()
         out = np.zeros(nk)
         torch.cuda.synchronize()
         e0, e1, e2 = ev(), ev(), ev()
@@ -497,13 +520,43 @@ def batching_sample(torch, C, api, geometry, lib, nk=16):
         asm_ms_all += a_ms
         rs_ms_all += r_ms
         tot_ms += a_ms + r_ms
-        tot_T += nk
         per.append({"N": N, "c_i": round(c_i, 3), "ms_per_T": (a_ms + r_ms) / nk, "sigma_min_min": float(out.min())})
         del T
+    tot_T = 8 * nk
+    # (b) every scatterer in one assembly launch, then the rSVDs
+    ops = [x[5] for x in scat]
+    kss = [x[4] for x in scat]
+    cis = [x[3] for x in scat]
+    Ts = [torch.empty((nk, 1, 2 * N, 2 * N), dtype=torch.complex128, device="cuda") for (_, N, _, _, _, _) in scat]
+    api.gen_sol_op_multi_device(ops, kss, 1.0, cis, d=0, out=Ts)   # warm-up
+    torch.cuda.synchronize()
+    lib.hbem_stats_reset()
+    lib.hbem_stats_enable_timing(1)
+    e0, e1, e2 = ev(), ev(), ev()
+    e0.record()
+    api.gen_sol_op_multi_device(ops, kss, 1.0, cis, d=0, out=Ts)
+    e1.record()
+    outs = rsvd_all(Ts)
+    e2.record()
+    torch.cuda.synchronize()
+    lib.hbem_stats_enable_timing(0)
+    launches, a_ms, a_l, a_pts = (C.ctypes.c_longlong(), C.ctypes.c_double(), C.ctypes.c_longlong(),
+                                  C.ctypes.c_longlong())
+    lib.hbem_stats_read(C.ctypes.byref(launches), C.ctypes.byref(a_ms), C.ctypes.byref(a_l), C.ctypes.byref(a_pts))
+    flops = assembly_flops(C, lib)
+    m_asm, m_rs = e0.elapsed_time(e1), e1.elapsed_time(e2)
+    tf = flops / (a_ms.value * 1e-3) / 1e12 if a_ms.value > 0 else None
+    diff = max(abs(float(o.min()) - p["sigma_min_min"]) / p["sigma_min_min"] for o, p in zip(outs, per))
+    del Ts
     return {"workload": "8 scatterers (4 star polygons, 4 Fourier curves), N=100..800, order 11, %d k each in "
                         "[1,30]; mixed rSVD sketch 12, q=2" % nk,
             "T_per_s": 1e3 * tot_T / tot_ms, "assembly_share": asm_ms_all / tot_ms, "rsvd_share": rs_ms_all / tot_ms,
-            "per_scatterer": per}
+            "per_scatterer": per,
+            "one_launch": {"T_per_s": 1e3 * tot_T / (m_asm + m_rs), "assembly_ms": m_asm, "rsvd_ms": m_rs,
+                           "assembly_launches": int(a_l.value), "assembly_fp64_tflops": tf,
+                           "assembly_frac_of_measured_fp64": (tf / peak) if (tf and peak) else None,
+                           "assembly_frac_of_nominal_fp64": (tf / nominal_fp64_tflops()) if tf else None,
+                           "sigma_min_min_max_rel_diff_vs_per_scatterer": diff}}
 
 
 def combine_ranks(tot_ms, tot_v, world):
@@ -841,7 +894,7 @@ def run_gpu(args):
     scale = assembly_at_scale(torch, C, api, geometry, lib, peak)
     tail = dense_tail_at_scale(torch, C, api, geometry, lib, peak)
     prec = precision_at_scale(torch, C, api, geometry, lib)
-    batch = batching_sample(torch, C, api, geometry, lib)
+    batch = batching_sample(torch, C, api, geometry, lib, peak=peak)
     adapt = adaptive_search(torch, so, step(so)[1])
     arnoldi, arn_mats = arnoldi_at_scale(torch, C, api, geometry, lib)
     field, field_sample = field_at_scale(torch, C, api, geometry, lib, peak)
@@ -907,7 +960,7 @@ def run_full_configs():
     from helmholtzbem_gb300 import _capi as C, api, geometry
     lib = C.lib()
     torch.cuda.set_device(0)
-    batch = batching_sample(torch, C, api, geometry, lib, nk=256)
+    batch = batching_sample(torch, C, api, geometry, lib, nk=256, peak=fp64_peak_tflops())
     prec = precision_at_scale(torch, C, api, geometry, lib, ks=tuple(float(k) for k in range(40, 48)))
     print(json.dumps({"batching_full": batch, "precision_full": prec}))
 

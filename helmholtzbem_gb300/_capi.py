@@ -22,7 +22,7 @@ EXPORTS = [
     "hbem_builder_create", "hbem_builder_destroy", "hbem_builder_info", "hbem_builder_is_adjacent",
     "hbem_assemble_dense", "hbem_assemble_dense_sub", "hbem_get_layer", "hbem_get_layer_device",
     "hbem_solop_create", "hbem_solop_destroy", "hbem_mass_matrix", "hbem_gen_sol_op",
-    "hbem_gen_sol_op_batch_device", "hbem_sv_dense_batch_device", "hbem_sv_dense_batch_noalloc",
+    "hbem_gen_sol_op_batch_device", "hbem_gen_sol_op_multi_device", "hbem_sv_dense_batch_device", "hbem_sv_dense_batch_noalloc",
     "hbem_sv_dense_batch", "hbem_sweep_sigma", "hbem_rand_sketch", "hbem_rsvd_sv_batch",
     "hbem_rsvd_sv_batch_device", "hbem_rsvd_sv_batch_device_ex", "hbem_lu_factor_batch_device", "hbem_lu_solve_batch_device",
     "hbem_cgemm_f32_batch_device", "hbem_solop_info", "hbem_sigma_rsvd_sweep", "hbem_opt_subdiv",
@@ -98,6 +98,7 @@ def load(path=LIB_PATH):
         "hbem_mass_matrix": (_i, [_vp, _dp]),
         "hbem_gen_sol_op": (_i, [_vp, _d, _d, _d, _d, _u, _dp]),
         "hbem_gen_sol_op_batch_device": (_i, [_vp, _dp, _i, _d, _d, _u, _vp]),
+        "hbem_gen_sol_op_multi_device": (_i, [_vp, _i, _ip, _dp, _dp, _d, _u, ctypes.POINTER(_vp)]),
         "hbem_sv_dense_batch_device": (_i, [_i, _i, _u, _vp, ctypes.c_longlong, ctypes.c_longlong, _dp, _dp]),
         "hbem_sv_dense_batch_noalloc": (_i, [_i, _i, _u, _vp, ctypes.c_longlong, ctypes.c_longlong, _vp, _vp, _vp]),
         "hbem_sv_dense_batch": (_i, [_i, _i, _u, _dp, _dp, _dp]),

@@ -405,6 +405,24 @@ def sweep_sigma_multi(ops, ks, c_o, c_i, d=0):
     return np.split(out, np.cumsum(counts)[:-1])
 
 
+def gen_sol_op_multi_device(ops, ks, c_o, c_i, d=0, out=None):
+    """T(k) and its first d derivatives of operator i at the wavenumbers ks[i] (inner
+    index c_i[i]) on the device, every scatterer's panel-pair quadrature in the same
+    launches: list of torch tensors [len(ks[i]), d + 1, 2N_i, 2N_i] (complex128,
+    each matrix column-major, i.e. the transposes of the row-major views)."""
+    import torch
+    counts = np.array([len(k) for k in ks], np.int32)
+    flat = np.ascontiguousarray(np.concatenate([np.asarray(k, np.float64) for k in ks]))
+    ci = np.ascontiguousarray(c_i, np.float64)
+    if out is None:
+        out = [torch.empty((len(k), d + 1, 2 * o.data.npanels, 2 * o.data.npanels), dtype=torch.complex128,
+                           device="cuda") for o, k in zip(ops, ks)]
+    ptrs = (ctypes.c_void_p * len(ops))(*[t.data_ptr() for t in out])
+    check(C.lib().hbem_gen_sol_op_multi_device(_ops(ops), len(ops), iptr(counts), dptr(flat), dptr(ci), float(c_o),
+                                               int(d), ptrs))
+    return out
+
+
 def _split_roots(roots, counts):
     return np.split(roots[:int(np.sum(counts))].copy(), np.cumsum(counts)[:-1])
 

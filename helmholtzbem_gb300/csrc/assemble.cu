@@ -362,15 +362,12 @@ __global__ void k_flags_singular(DevMesh M, const SingularTask* tasks, uint8_t* 
 
 // ------------------------------------------------------------------ local-block kernels
 
-// General pairs, one thread per pair.
+// General pair number q (strictly lower pairs, in the builder's distance order when
+// it made one) of mesh M for one job: p x p Gauss points, the pair's local blocks
+// written to locj (the job's block array).
 template <int D, bool RK, bool CURVED>
-__global__ void __launch_bounds__(128) k_general(DevMesh M, const Job* jobs, cplx* loc, long long npair) {
-    __shared__ double sx[64], sw[64];
-    for (int t = threadIdx.x; t < M.p; t += blockDim.x) { sx[t] = M.xg[t]; sw[t] = M.wg[t]; }
-    __syncthreads();
-    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    long long nlow = (long long)M.n * (M.n - 1) / 2;   // strictly lower pairs
-    if (q >= nlow) return;
+__device__ __forceinline__ void general_pair(const DevMesh& M, const KConst& K, long long q, const double* sx,
+                                             const double* sw, cplx* locj) {
     // neighbouring threads take pairs of similar panel distance, so a warp's lanes
     // mostly follow the same Hankel branch and series length
     if (M.gorder) q = M.gorder[q];
@@ -381,8 +378,6 @@ __global__ void __launch_bounds__(128) k_general(DevMesh M, const Job* jobs, cpl
     long long pid = tri_index(i, j);
     uint8_t fl = M.flags[pid];
     if (fl & 0x80) return;   // coincident / adjacent: singular kernel
-    const int job = blockIdx.y;
-    KConst K = make_kconst(jobs[job]);
     const bool use_dl = !(fl & PF_DL0_ZERO), use_dlt = !(fl & PF_DLT0_ZERO), tz = (fl & PF_TDT0_ZERO) != 0;
     const int p = M.p;
     const cplx* pti = M.gpt + i * p;
@@ -415,7 +410,21 @@ __global__ void __launch_bounds__(128) k_general(DevMesh M, const Job* jobs, cpl
     }
     const cplx t0i = tgi[0], t0j = tgj[0];
     store_local<D, CURVED>(A, K, false, false, tni[0] * tnj[0], 2. * (t0i.im * t0j.im + t0i.re * t0j.re), tz,
-                           loc + ((long long)job * npair + pid) * (D + 1) * kLocPerD);
+                           locj + pid * (D + 1) * kLocPerD);
+}
+
+// General pairs, one thread per pair.
+template <int D, bool RK, bool CURVED>
+__global__ void __launch_bounds__(128) k_general(DevMesh M, const Job* jobs, cplx* loc, long long npair) {
+    __shared__ double sx[64], sw[64];
+    for (int t = threadIdx.x; t < M.p; t += blockDim.x) { sx[t] = M.xg[t]; sw[t] = M.wg[t]; }
+    __syncthreads();
+    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    long long nlow = (long long)M.n * (M.n - 1) / 2;   // strictly lower pairs
+    if (q >= nlow) return;
+    const int job = blockIdx.y;
+    KConst K = make_kconst(jobs[job]);
+    general_pair<D, RK, CURVED>(M, K, q, sx, sw, loc + (long long)job * npair * (D + 1) * kLocPerD);
 }
 
 template <int D, bool RK, bool CURVED>
@@ -583,6 +592,49 @@ __device__ __forceinline__ void singular_accumulate(Acc<D, CURVED>& A, const KCo
     }
 }
 
+// One coincident / adjacent pair (task index ti of mesh M) for one job, reduced over
+// the CTA: its local blocks written to out.  sxc, swc: the composite nodes and
+// weights in shared memory; red: reduction space.
+template <int D, bool RK, bool CURVED>
+__device__ __forceinline__ void singular_pair(const DevMesh& M, const SingularTask& T, int ti, const KConst& K,
+                                              const double* sxc, const double* swc, double* red, cplx* out) {
+    const long long pid = tri_index(T.i, T.j);
+    const uint8_t fl = M.flags[pid];
+    const int nc = M.nc, tot = nc * nc;
+    const int nset = T.kind == PK_COINC ? 1 : 2;
+    // point data from the table when the builder made one, else computed here
+    const double* G = M.sgeo ? M.sgeo + (long long)ti * 2 * kSGeoFields * tot : nullptr;
+    Acc<D, CURVED> A;
+    A.zero();
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+        const int a = e % nc, b = e / nc;
+#pragma unroll 1
+        for (int Kset = 0; Kset < nset; ++Kset) {
+            double f[kSGeoFields];
+            if (G) {
+#pragma unroll
+                for (int q = 0; q < kSGeoFields; ++q) f[q] = __ldg(G + ((long long)Kset * kSGeoFields + q) * tot + e);
+            } else {
+                singular_fields(M, T, Kset, sxc[a], sxc[b], swc[a], swc[b], f);
+            }
+            singular_accumulate<D, RK, CURVED>(A, K, T.kind, fl, Kset, f);
+        }
+    }
+    block_reduce(A, red);
+    if (threadIdx.x == 0) {
+        // per-pair constants: tangent norms (constant on lines and arcs) and, for
+        // straight panels, the tangent product
+        SPoint P;
+        singular_point(M, T, 0, sxc[0], sxc[0], P);
+        const bool adj = T.kind == PK_ADJ;
+        const bool tz = CURVED ? false : (fl & PF_TDT0_ZERO) != 0;
+        store_local<D, CURVED>(A, K, adj && !T.swap, adj && T.swap, P.tin * P.tjn,
+                               2. * (P.ti.im * P.tj.im + P.ti.re * P.tj.re), tz, out + pid * (D + 1) * kLocPerD);
+    }
+}
+
+// (the per-pair code of singular_pair, kept inline here: the order-0 instance keeps
+// its register allocation of 128 per thread)
 template <int D, bool RK, bool CURVED>
 __global__ void __launch_bounds__(128) k_singular(DevMesh M, const SingularTask* tasks, const Job* jobs, cplx* loc,
                                                   long long npair) {
@@ -629,6 +681,74 @@ __global__ void __launch_bounds__(128) k_singular(DevMesh M, const SingularTask*
                                2. * (P.ti.im * P.tj.im + P.ti.re * P.tj.re), tz,
                                loc + ((long long)job * npair + pid) * (D + 1) * kLocPerD);
     }
+}
+
+// ------------------------------------------------------------------ many meshes in one launch
+//
+// The batching path: the jobs of several meshes (scatterers of uneven panel counts,
+// each with its wavenumbers and media) in one general-pair launch and one
+// singular-pair launch.  Each CTA finds its job by a binary search over the jobs'
+// first block numbers, copies that job's mesh view to shared memory and runs the
+// same per-pair code as the single-mesh kernels.  The meshes of one launch share
+// the panel kind (all lines or all curved) and the wavenumber kind (real or not).
+
+// index of the job whose blocks [start[j], start[j + 1]) hold block b
+__device__ __forceinline__ int job_of_block(const long long* start, int njobs, long long b) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int D, bool RK, bool CURVED>
+__global__ void __launch_bounds__(128) k_general_multi(const MultiMesh* meshes, const MultiJob* jobs,
+                                                       const long long* start, int njobs, cplx* loc) {
+    __shared__ DevMesh sM;
+    __shared__ double sx[64], sw[64];
+    __shared__ int sjob;
+    if (threadIdx.x == 0) {
+        sjob = job_of_block(start, njobs, blockIdx.x);
+        sM = meshes[jobs[sjob].mesh].M;
+    }
+    __syncthreads();
+    const int job = sjob;
+    for (int t = threadIdx.x; t < sM.p; t += blockDim.x) { sx[t] = sM.xg[t]; sw[t] = sM.wg[t]; }
+    __syncthreads();
+    const long long q = (blockIdx.x - start[job]) * (long long)blockDim.x + threadIdx.x;
+    const long long nlow = (long long)sM.n * (sM.n - 1) / 2;
+    if (q >= nlow) return;
+    const MultiJob J = jobs[job];
+    const KConst K = make_kconst(J.job);
+    general_pair<D, RK, CURVED>(sM, K, q, sx, sw, loc + J.loc);
+}
+
+template <int D, bool RK, bool CURVED>
+__global__ void __launch_bounds__(128) k_singular_multi(const MultiMesh* meshes, const MultiJob* jobs,
+                                                        const long long* start, int njobs, cplx* loc) {
+    extern __shared__ double sm[];
+    __shared__ DevMesh sM;
+    __shared__ int sjob;
+    __shared__ SingularTask sT;
+    if (threadIdx.x == 0) {
+        sjob = job_of_block(start, njobs, blockIdx.x);
+        const MultiMesh& MM = meshes[jobs[sjob].mesh];
+        sM = MM.M;
+        sT = MM.tasks[blockIdx.x - start[sjob]];
+    }
+    __syncthreads();
+    const int nc = sM.nc;
+    double* sxc = sm;
+    double* swc = sm + nc;
+    double* red = sm + 2 * nc;
+    for (int t = threadIdx.x; t < nc; t += blockDim.x) { sxc[t] = sM.xc[t]; swc[t] = sM.wc[t]; }
+    __syncthreads();
+    const MultiJob J = jobs[sjob];
+    const KConst K = make_kconst(J.job);
+    const SingularTask T = sT;
+    singular_pair<D, RK, CURVED>(sM, T, (int)(blockIdx.x - start[sjob]), K, sxc, swc, red, loc + J.loc);
 }
 
 // ------------------------------------------------------------------ gather
@@ -796,26 +916,32 @@ cudaError_t launch_hankel01(int n, const cplx* z, int complex_arg, cplx* h0, cpl
 
 // ------------------------------------------------------------------ launchers
 
+// General-pair layout of a launch: kLayoutAuto picks by size (a thread per pair
+// once pairs x jobs fill the GPU, else a warp per pair with ppw pairs per warp);
+// 0 forces a thread per pair, ppw > 0 a warp per pair with that many pairs.
+constexpr int kLayoutAuto = -1;
+
 template <int D, bool RK, bool CURVED>
 static cudaError_t launch_local_c(const DevMesh& M, const SingularTask* tasks, int ntasks, const Job* jobs, int njobs,
-                                  cplx* loc, cudaStream_t st) {
+                                  cplx* loc, cudaStream_t st, int layout, int which) {
     long long npair = (long long)M.n * (M.n + 1) / 2;
     long long nlow = (long long)M.n * (M.n - 1) / 2;
-    if (nlow > 0) {
-        if (nlow * njobs >= 152LL * 16 * 32) {
-            // enough pairs x media for a thread per pair to fill the GPU
+    if (nlow > 0 && (which & 1)) {
+        int ppw = layout;
+        if (layout == kLayoutAuto) {
+            if (nlow * njobs >= 152LL * 16 * 32) ppw = 0;   // enough pairs x media for a thread per pair
+            else ppw = (int)std::min(16LL, std::max(1LL, nlow * njobs / 8192));   // ~8k warps in the launch
+        }
+        if (ppw == 0) {
             dim3 g((unsigned)((nlow + 127) / 128), njobs);
             k_general<D, RK, CURVED><<<g, 128, 0, st>>>(M, jobs, loc, npair);
         } else {
-            // few: a warp per pair, ppw pairs per warp keeping ~8k warps in the launch
-            const long long want = std::max(1LL, nlow * njobs / 8192);
-            const int ppw = (int)std::min(16LL, want);
             const long long per_cta = 4LL * ppw;
             dim3 g((unsigned)((nlow + per_cta - 1) / per_cta), njobs);
             k_general_w<D, RK, CURVED><<<g, 128, 0, st>>>(M, jobs, loc, npair, ppw);
         }
     }
-    if (ntasks > 0) {
+    if (ntasks > 0 && (which & 2)) {
         constexpr int NV = (int)(sizeof(Acc<D, CURVED>) / sizeof(double));
         size_t smem = (2 * (size_t)M.nc + 4 * NV) * sizeof(double);
         dim3 g(ntasks, njobs);
@@ -826,9 +952,9 @@ static cudaError_t launch_local_c(const DevMesh& M, const SingularTask* tasks, i
 
 template <int D, bool RK>
 static cudaError_t launch_local_t(const DevMesh& M, const SingularTask* tasks, int ntasks, const Job* jobs, int njobs,
-                                  cplx* loc, cudaStream_t st) {
-    if (M.lines) return launch_local_c<D, RK, false>(M, tasks, ntasks, jobs, njobs, loc, st);
-    return launch_local_c<D, RK, true>(M, tasks, ntasks, jobs, njobs, loc, st);
+                                  cplx* loc, cudaStream_t st, int layout, int which) {
+    if (M.lines) return launch_local_c<D, RK, false>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which);
+    return launch_local_c<D, RK, true>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which);
 }
 
 size_t singular_geo_bytes(int nc, int ntasks) {
@@ -848,16 +974,54 @@ cudaError_t launch_flags(const DevMesh& M, const SingularTask* tasks, int ntasks
     return cudaGetLastError();
 }
 
-cudaError_t launch_local(const DevMesh& M, const SingularTask* tasks, int ntasks, const Job* jobs, int njobs,
-                         bool real_k, int d, cplx* loc, cudaStream_t st) {
-    if (real_k) {
-        if (d == 0) return launch_local_t<0, true>(M, tasks, ntasks, jobs, njobs, loc, st);
-        if (d == 1) return launch_local_t<1, true>(M, tasks, ntasks, jobs, njobs, loc, st);
-        return launch_local_t<2, true>(M, tasks, ntasks, jobs, njobs, loc, st);
+template <int D, bool RK, bool CURVED>
+static cudaError_t launch_multi_c(const MultiMesh* meshes, const MultiJob* jobs, int njobs, const long long* gstart,
+                                  long long gblocks, const long long* sstart, long long sblocks, int max_nc, cplx* loc,
+                                  cudaStream_t st) {
+    if (gblocks > 0) k_general_multi<D, RK, CURVED><<<(unsigned)gblocks, 128, 0, st>>>(meshes, jobs, gstart, njobs, loc);
+    if (sblocks > 0) {
+        constexpr int NV = (int)(sizeof(Acc<D, CURVED>) / sizeof(double));
+        const size_t smem = (2 * (size_t)max_nc + 4 * NV) * sizeof(double);
+        k_singular_multi<D, RK, CURVED><<<(unsigned)sblocks, 128, smem, st>>>(meshes, jobs, sstart, njobs, loc);
     }
-    if (d == 0) return launch_local_t<0, false>(M, tasks, ntasks, jobs, njobs, loc, st);
-    if (d == 1) return launch_local_t<1, false>(M, tasks, ntasks, jobs, njobs, loc, st);
-    return launch_local_t<2, false>(M, tasks, ntasks, jobs, njobs, loc, st);
+    return cudaGetLastError();
+}
+
+// The pair blocks of njobs jobs over several meshes in two launches (see the
+// many-mesh kernels): gstart / sstart (njobs + 1 entries, device) are the jobs'
+// first CTA numbers of the general and singular launch.
+cudaError_t launch_local_multi(const MultiMesh* meshes, const MultiJob* jobs, int njobs, const long long* gstart,
+                               long long gblocks, const long long* sstart, long long sblocks, int max_nc, bool curved,
+                               bool real_k, int d, cplx* loc, cudaStream_t st) {
+    if (gblocks > 0x7fffffffLL || sblocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+#define HB_MULTI(D_, RK_)                                                                                        \
+    return curved ? launch_multi_c<D_, RK_, true>(meshes, jobs, njobs, gstart, gblocks, sstart, sblocks, max_nc, \
+                                                  loc, st)                                                       \
+                  : launch_multi_c<D_, RK_, false>(meshes, jobs, njobs, gstart, gblocks, sstart, sblocks, max_nc, \
+                                                   loc, st)
+    if (real_k) {
+        if (d == 0) HB_MULTI(0, true);
+        if (d == 1) HB_MULTI(1, true);
+        HB_MULTI(2, true);
+    }
+    if (d == 0) HB_MULTI(0, false);
+    if (d == 1) HB_MULTI(1, false);
+    HB_MULTI(2, false);
+#undef HB_MULTI
+}
+
+// layout: kLayoutAuto or a forced general-pair layout (see launch_local_c); which:
+// bit 0 the general pairs, bit 1 the singular pairs
+cudaError_t launch_local(const DevMesh& M, const SingularTask* tasks, int ntasks, const Job* jobs, int njobs,
+                         bool real_k, int d, cplx* loc, cudaStream_t st, int layout, int which) {
+    if (real_k) {
+        if (d == 0) return launch_local_t<0, true>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which);
+        if (d == 1) return launch_local_t<1, true>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which);
+        return launch_local_t<2, true>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which);
+    }
+    if (d == 0) return launch_local_t<0, false>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which);
+    if (d == 1) return launch_local_t<1, false>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which);
+    return launch_local_t<2, false>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which);
 }
 
 cudaError_t launch_gather_T(int N, int d, const cplx* loc, const double* Mmass, int nk, int sp, cplx* T,

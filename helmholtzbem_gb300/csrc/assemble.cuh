@@ -66,6 +66,21 @@ struct Job {
     double kre, kim, c;
 };
 
+// a mesh of a many-mesh launch: its device view and singular-pair list
+struct MultiMesh {
+    DevMesh M;
+    const SingularTask* tasks;
+    int ntasks;
+};
+
+// a job of a many-mesh launch: (k, c), the mesh, and the offset (complex entries)
+// of the job's pair-block array in the launch's scratch
+struct MultiJob {
+    Job job;
+    int mesh;
+    long long loc;
+};
+
 // number of complex entries of a pair's local block set per derivative order:
 // DL(2x2) DLt(2x2) HY(2x2) SL(2x2)
 constexpr int kLocPerD = 16;

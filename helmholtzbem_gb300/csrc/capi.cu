@@ -3,7 +3,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
+#include <cstdio>
+#include <cstdlib>
+#include <map>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -21,9 +25,12 @@ size_t singular_geo_bytes(int nc, int ntasks);
 cudaError_t launch_singular_geo(const DevMesh& M, const SingularTask* tasks, int ntasks, double* geo,
                                 cudaStream_t st);
 cudaError_t launch_local(const DevMesh& M, const SingularTask* tasks, int ntasks, const Job* jobs, int njobs,
-                         bool real_k, int d, cplx* loc, cudaStream_t st);
+                         bool real_k, int d, cplx* loc, cudaStream_t st, int layout, int which);
 cudaError_t launch_gather_T(int N, int d, const cplx* loc, const double* Mmass, int nk, int sp, cplx* T,
                             cudaStream_t st);
+cudaError_t launch_local_multi(const MultiMesh* meshes, const MultiJob* jobs, int njobs, const long long* gstart,
+                               long long gblocks, const long long* sstart, long long sblocks, int max_nc, bool curved,
+                               bool real_k, int d, cplx* loc, cudaStream_t st);
 cudaError_t launch_gather_layers(int N, int d, int layers, const cplx* loc, int job, int sp, cplx* out,
                                  cudaStream_t st);
 cudaError_t launch_gather_layers_sub(int N, int d, int layers, const cplx* loc, int job, int row, int rows, int col,
@@ -233,15 +240,92 @@ double dist(cplx a, cplx b) { return std::hypot(a.re - b.re, a.im - b.im); }
 
 // panel-pair assembly launch with launch counting and, when enabled, CUDA-event
 // timing on the launching stream
+// ---- autotuner of the general-pair layout (option "autotune", default 0)
+//
+// The general pairs of a launch run a thread per pair or a warp per pair with ppw
+// pairs per warp; the built-in rule picks by the number of pairs x jobs.  With the
+// autotuner on, the first launch of each (panels, order, jobs rounded up to a power
+// of two, derivative order, real k, curved) times every layout once on the launch's
+// own data (CUDA events on its stream) and keeps the fastest; later launches of the
+// key use it.  The choices are kept for the process and, when the environment
+// variable HBEM_TUNE_CACHE names a file, read from it at the first tuned launch and
+// appended to it, so later processes start tuned.  The layouts sum the same
+// quadrature points in different orders: results agree to rounding (~1e-15).
+constexpr int kLayoutAuto = -1;
+const int kTuneLayouts[] = {0, 1, 2, 4, 8, 16};
+std::atomic<int> g_autotune{0};
+std::mutex g_tune_mu;
+std::map<std::array<int, 6>, int> g_tune;
+bool g_tune_loaded = false;
+
+std::array<int, 6> tune_key(const DevMesh& M, int njobs, int d, bool real_k) {
+    int nb = 1;
+    while (nb < njobs) nb <<= 1;
+    return {M.n, M.p, nb, d, real_k ? 1 : 0, M.lines ? 0 : 1};
+}
+
+void tune_load_locked() {
+    g_tune_loaded = true;
+    const char* f = getenv("HBEM_TUNE_CACHE");
+    if (!f || !*f) return;
+    FILE* fp = fopen(f, "r");
+    if (!fp) return;
+    std::array<int, 6> k;
+    int v;
+    while (fscanf(fp, "%d %d %d %d %d %d %d", &k[0], &k[1], &k[2], &k[3], &k[4], &k[5], &v) == 7) g_tune[k] = v;
+    fclose(fp);
+}
+
+int tuned_layout(const DevMesh& M, const SingularTask* tasks, int ntasks, const Job* jobs, int njobs, bool real_k,
+                 int d, cplx* loc, cudaStream_t st) {
+    const auto key = tune_key(M, njobs, d, real_k);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        if (!g_tune_loaded) tune_load_locked();
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) return it->second;
+    }
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) return kLayoutAuto;
+    int best = kLayoutAuto;
+    float best_ms = 0.f;
+    for (int lay : kTuneLayouts) {
+        cudaEventRecord(a, st);
+        if (launch_local(M, tasks, ntasks, jobs, njobs, real_k, d, loc, st, lay, 1) != cudaSuccess) break;
+        cudaEventRecord(b, st);
+        if (cudaEventSynchronize(b) != cudaSuccess) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        g_launches += 1;
+        if (best == kLayoutAuto || ms < best_ms) { best = lay; best_ms = ms; }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (best == kLayoutAuto) return best;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = best;
+    if (const char* f = getenv("HBEM_TUNE_CACHE")) {
+        if (*f) {
+            if (FILE* fp = fopen(f, "a")) {
+                fprintf(fp, "%d %d %d %d %d %d %d\n", key[0], key[1], key[2], key[3], key[4], key[5], best);
+                fclose(fp);
+            }
+        }
+    }
+    return best;
+}
+
 cudaError_t local_assembly(const DevMesh& M, const SingularTask* tasks, int ntasks, int ncoinc, const Job* jobs,
                            int njobs, bool real_k, int d, cplx* loc, cudaStream_t st) {
+    const int layout = (g_autotune && M.n > 1) ? tuned_layout(M, tasks, ntasks, jobs, njobs, real_k, d, loc, st)
+                                               : kLayoutAuto;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (g_timing) {
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
         cudaEventRecord(e0, st);
     }
-    cudaError_t e = launch_local(M, tasks, ntasks, jobs, njobs, real_k, d, loc, st);
+    cudaError_t e = launch_local(M, tasks, ntasks, jobs, njobs, real_k, d, loc, st, layout, 3);
     g_launches += (M.n > 1 ? 1 : 0) + (ntasks > 0 ? 1 : 0);
     if (g_timing) {
         cudaEventRecord(e1, st);
@@ -403,6 +487,10 @@ int hbem_set_option(const char* name, int value) {
         g_svd_fast = value ? 1 : 0;
         return HBEM_OK;
     }
+    if (k == "autotune") {
+        g_autotune = value ? 1 : 0;
+        return HBEM_OK;
+    }
     if (k == "svd_fast_force_redo") {
         g_svd_force_redo = value ? 1 : 0;
         return HBEM_OK;
@@ -438,6 +526,7 @@ int hbem_get_option(const char* name, int* value) {
     else if (k == "lu_tensor_cores") *value = lu_get_tensor_cores();
     else if (k == "svd_fast") *value = g_svd_fast.load();
     else if (k == "svd_fast_force_redo") *value = g_svd_force_redo.load();
+    else if (k == "autotune") *value = g_autotune.load();
     else if (k == "mlp_tensor_cores") *value = mlp_get_tensor_cores();
     else if (k == "singular_table") *value = g_singular_table;
     else if (k == "plain_warm_start") *value = g_plain_warm_start;
@@ -818,6 +907,140 @@ int hbem_gen_sol_op_batch_device(hbem_solop s, const double* k_host, int nk, dou
     return HBEM_OK;
 }
 
+// Several operators (scatterers of uneven panel counts) at their own wavenumbers: the
+// pair blocks of every (scatterer, k, medium) job in one general-pair and one
+// singular-pair launch per group of meshes of one panel kind, then each operator's
+// gather and projection, all on the first operator's stream.
+int hbem_gen_sol_op_multi_device(const hbem_solop* ops, int nops, const int* counts, const double* k_host,
+                                 const double* c_i_host, double c_o, unsigned d, void* const* T_dev) {
+    if (!ops || nops < 1 || !counts || !k_host || !c_i_host || !T_dev || d > 2)
+        return fail(HBEM_ERR_INVALID, "gen_sol_op_multi: bad argument");
+    for (int i = 0; i < nops; ++i) {
+        if (!ops[i] || counts[i] < 0 || (counts[i] > 0 && !T_dev[i]))
+            return fail(HBEM_ERR_INVALID, "gen_sol_op_multi: bad argument");
+        if (ops[i]->b->device != ops[0]->b->device)
+            return fail(HBEM_ERR_INVALID, "gen_sol_op_multi: operators on different devices");
+        if (int r = check_kc(0., c_i_host[i])) return r;
+    }
+    if (int r = check_kc(0., c_o)) return r;
+    std::vector<size_t> koff(nops + 1, 0);
+    for (int i = 0; i < nops; ++i) {
+        koff[i + 1] = koff[i] + (size_t)counts[i];
+        for (int q = 0; q < counts[i]; ++q)
+            if (!(k_host[koff[i] + q] > 0.))
+                return fail(HBEM_ERR_INVALID, "gen_sol_op_multi: wavenumbers must be real and positive");
+    }
+    hbem_builder b0 = ops[0]->b;
+    HB_CK(cudaSetDevice(b0->device));
+    cudaStream_t st = b0->st;
+    // the other operators' streams may still hold work on their buffers
+    for (int i = 1; i < nops; ++i) HB_CK(cudaStreamSynchronize(ops[i]->b->st));
+    // job table and pair-block scratch: the first operator's builder's buffers
+    static thread_local DBuf d_meshes, d_start;
+    DBuf& d_jobs = b0->d_jobs;
+    DBuf& d_loc = b0->d_loc;
+    std::vector<MultiMesh> meshes(nops);
+    int max_nc = 0;
+    for (int i = 0; i < nops; ++i) {
+        meshes[i] = MultiMesh{ops[i]->b->view(), ops[i]->b->d_tasks.as<SingularTask>(), (int)ops[i]->b->tasks.size()};
+        max_nc = std::max(max_nc, ops[i]->b->nc);
+    }
+    HB_CK(upload(d_meshes, meshes, st));
+    const size_t per_pair = (size_t)(d + 1) * kLocPerD;   // complex entries per pair and job
+    const size_t budget = ((size_t)4 << 30) / sizeof(cplx);
+    size_t kmax = 0;
+    for (int i = 0; i < nops; ++i) kmax = std::max(kmax, (size_t)counts[i]);
+    for (int curved = 0; curved < 2; ++curved) {
+        // wavenumber chunks: every operator of the group advances by `chunk` wavenumbers
+        // per launch pair, within the 4 GiB scratch bound
+        size_t per_k = 0;
+        for (int i = 0; i < nops; ++i)
+            if ((ops[i]->b->lines == 0) == (curved == 1)) per_k += 2 * (size_t)ops[i]->b->npair() * per_pair;
+        if (per_k == 0) continue;
+        const size_t chunk = std::max<size_t>(1, budget / per_k);
+        for (size_t q0 = 0; q0 < kmax; q0 += chunk) {
+            std::vector<MultiJob> jobs;
+            std::vector<long long> gstart{0}, sstart{0};
+            std::vector<size_t> first(nops, 0), nk(nops, 0);
+            long long off = 0;
+            for (int i = 0; i < nops; ++i) {
+                hbem_builder b = ops[i]->b;
+                if ((b->lines == 0) != (curved == 1) || (size_t)counts[i] <= q0) continue;
+                nk[i] = std::min(chunk, (size_t)counts[i] - q0);
+                first[i] = jobs.size();
+                const long long nlow = (long long)b->n * (b->n - 1) / 2;
+                for (size_t q = 0; q < nk[i]; ++q) {
+                    const double k = k_host[koff[i] + q0 + q];
+                    for (double c : {c_i_host[i], c_o}) {
+                        jobs.push_back(MultiJob{Job{k, 0., c}, i, off});
+                        off += (long long)(b->npair() * per_pair);
+                        gstart.push_back(gstart.back() + (nlow + 127) / 128);
+                        sstart.push_back(sstart.back() + (long long)b->tasks.size());
+                    }
+                }
+            }
+            if (jobs.empty()) continue;
+            const int njobs = (int)jobs.size();
+            std::vector<long long> starts(gstart);
+            starts.insert(starts.end(), sstart.begin(), sstart.end());
+            HB_CK(upload(d_jobs, jobs, st));
+            HB_CK(upload(d_start, starts, st));
+            HB_CK(d_loc.ensure((size_t)off * sizeof(cplx)));
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            if (g_timing) {
+                cudaEventCreate(&e0);
+                cudaEventCreate(&e1);
+                cudaEventRecord(e0, st);
+            }
+            HB_CK(launch_local_multi(d_meshes.as<MultiMesh>(), d_jobs.as<MultiJob>(), njobs, d_start.as<long long>(),
+                                     gstart.back(), d_start.as<long long>() + gstart.size(), sstart.back(), max_nc,
+                                     curved == 1, true, (int)d, d_loc.as<cplx>(), st));
+            g_launches += (gstart.back() > 0 ? 1 : 0) + (sstart.back() > 0 ? 1 : 0);
+            if (g_timing) {
+                cudaEventRecord(e1, st);
+                cudaEventSynchronize(e1);
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                {
+                    std::lock_guard<std::mutex> lk(g_stats_mu);
+                    g_asm_ms += ms;
+                }
+                g_asm_launches += 1;
+                for (int i = 0; i < nops; ++i) {
+                    if (!nk[i]) continue;
+                    const hbem_builder b = ops[i]->b;
+                    const long long nc2 = (long long)b->nc * b->nc, ntasks = (long long)b->tasks.size();
+                    const long long ncoinc = b->n, nadj = ntasks - ncoinc;
+                    const long long gen = b->npair() - ntasks;
+                    const long long nj = 2LL * (long long)nk[i];
+                    g_asm_points += nj * (ncoinc * nc2 + nadj * 2 * nc2 + gen * (long long)b->p * b->p);
+                    g_asm_split[d] += nj * gen * b->p * b->p;
+                    g_asm_split[(b->d_sgeo.p && g_singular_table ? 3 : 6) + d] += nj * (ncoinc * nc2 + nadj * 2 * nc2);
+                }
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+            }
+            for (int i = 0; i < nops; ++i) {
+                if (!nk[i]) continue;
+                hbem_solop s = ops[i];
+                const int N = s->b->n;
+                const size_t mat = 4ULL * N * N;
+                cplx* Tk = static_cast<cplx*>(T_dev[i]) + q0 * (d + 1) * mat;
+                HB_CK(launch_gather_T(N, (int)d, d_loc.as<cplx>() + jobs[first[i]].loc, s->d_M.as<double>(),
+                                      (int)nk[i], s->b->sp(), Tk, st));
+                g_launches += 1;
+                if (s->proj) {
+                    HB_CK(launch_projection(N, s->d_id.as<double>(), s->d_sb.as<double>(), s->d_lr.as<double>(), Tk,
+                                            (int)nk[i] * (int)(d + 1), st));
+                    g_launches += 2;
+                }
+            }
+        }
+    }
+    HB_CK(cudaStreamSynchronize(st));
+    return HBEM_OK;
+}
+
 // ---------------------------------------------------------------- singular values
 
 static int sv_batch(cudaStream_t st, int n, int nmat, unsigned d, const cplx* T, long long mat_stride,
@@ -1013,7 +1236,7 @@ int hbem_cgemm_f32_batch_device(int m, int n, int k, const void* A, long long ld
                                 long long ldb, long long sb, void* C, long long ldc, long long sc, int nmat,
                                 int tensor_cores) {
     if (m < 0 || n < 0 || k < 0 || nmat < 1 || nmat > 65535 || !A || !B || !C || lda < std::max(1, m) ||
-        ldb < std::max(1, k) || ldc < std::max(1, m) || (tensor_cores && k > 32))
+        ldb < std::max(1, k) || ldc < std::max(1, m))
         return fail(HBEM_ERR_INVALID, "cgemm_f32_batch: bad argument");
     HB_CK(cudaSetDevice(g_device));
     static thread_local DBuf err;

@@ -200,12 +200,14 @@ __global__ void __launch_bounds__(kLuPanelThreads) k_lu_panel_cluster(int n, int
     cl.sync();   // no CTA leaves while another may still read its shared memory
 }
 
-// grid (ceil(n/32), nmat): column block b covers columns [32 b, 32 b + 32).
+// grid (ceil(n/32), nmat): column block b covers columns [32 b, 32 b + 32).  Columns
+// from cmax on are left alone (the two-level factorisation exchanges and solves them
+// once per 128-column block, k_lu_swap_trsm_block).
 template <class E>
 __global__ void __launch_bounds__(256) k_lu_swap_trsm(int n, int k0, int nb, E* A, long long stride,
-                                                      const int* piv) {
+                                                      const int* piv, int cmax) {
     const int col0 = blockIdx.x * kLuNB;
-    if (col0 == k0) return;                            // the panel itself
+    if (col0 == k0 || col0 >= cmax) return;            // the panel itself, or deferred
     E* M = A + (long long)blockIdx.y * stride;
     const int* pv = piv + (long long)blockIdx.y * n;
     const int ncols = min(kLuNB, n - col0);
@@ -244,9 +246,76 @@ __global__ void __launch_bounds__(256) k_lu_swap_trsm(int n, int k0, int nb, E* 
     }
 }
 
-// grid (tiles over trailing rows, tiles over trailing columns, nmat)
+// Two-level factorisation, after the kb (<= 128) columns from K0 are factored: the
+// row exchanges of those columns applied, in order, to the columns right of them
+// (cbase on), and the block row solved with the kb x kb unit lower triangle,
+// U12 = L11^-1 A12.  grid (ceil((n - cbase) / 32), nmat); L11 in shared memory
+// (kb x (kb + 1)); a warp per column, lane l holding rows l, l + 32, l + 64, l + 96.
+constexpr int kLuBlock = 128;
 template <class E>
-__global__ void __launch_bounds__(256) k_lu_gemm(int n, int k0, int nb, E* A, long long stride) {
+__global__ void __launch_bounds__(256) k_lu_swap_trsm_block(int n, int K0, int kb, E* A, long long stride,
+                                                            const int* piv) {
+    extern __shared__ double blk_sm[];
+    E* L = reinterpret_cast<E*>(blk_sm);                  // [r][k], leading dimension kb + 1
+    __shared__ int sp[kLuBlock];
+    const int cbase = K0 + kb;
+    const int col0 = cbase + blockIdx.x * kLuNB;
+    E* M = A + (long long)blockIdx.y * stride;
+    const int* pv = piv + (long long)blockIdx.y * n;
+    const int ncols = min(kLuNB, n - col0);
+    for (int j = threadIdx.x; j < kb; j += blockDim.x) sp[j] = pv[K0 + j];
+    for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
+        const int r = e % kb, k = e / kb;
+        L[r * (kb + 1) + k] = M[(K0 + r) + (long long)(K0 + k) * n];
+    }
+    __syncthreads();
+    if (threadIdx.x < ncols) {
+        E* a = M + (long long)(col0 + threadIdx.x) * n;
+        for (int j = 0; j < kb; ++j) {
+            const int p = sp[j];
+            if (p != K0 + j) {
+                const E t = a[K0 + j];
+                a[K0 + j] = a[p];
+                a[p] = t;
+            }
+        }
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int cc = warp; cc < ncols; cc += (blockDim.x >> 5)) {
+        E* a = M + (long long)(col0 + cc) * n + K0;
+        E x[kLuBlock / 32];
+#pragma unroll
+        for (int s = 0; s < kLuBlock / 32; ++s) {
+            const int r = lane + 32 * s;
+            x[s] = r < kb ? a[r] : Elem<E>::zero();
+        }
+#pragma unroll
+        for (int s0 = 0; s0 < kLuBlock / 32; ++s0) {
+            for (int kk = 0; kk < 32; ++kk) {
+                const int k = 32 * s0 + kk;
+                if (k >= kb) break;
+                E xk;
+                xk.re = __shfl_sync(0xffffffffu, x[s0].re, kk);
+                xk.im = __shfl_sync(0xffffffffu, x[s0].im, kk);
+#pragma unroll
+                for (int s = 0; s < kLuBlock / 32; ++s) {
+                    const int r = lane + 32 * s;
+                    if (s >= s0 && r > k && r < kb) cfms(x[s], L[r * (kb + 1) + k], xk);
+                }
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < kLuBlock / 32; ++s) {
+            const int r = lane + 32 * s;
+            if (r < kb) a[r] = x[s];
+        }
+    }
+}
+
+// grid (tiles over trailing rows, tiles over trailing columns below cend, nmat)
+template <class E>
+__global__ void __launch_bounds__(256) k_lu_gemm(int n, int k0, int nb, E* A, long long stride, int cend) {
     extern __shared__ double lu_smem[];
     E* La = reinterpret_cast<E*>(lu_smem);                // [k][i], 32 x 64
     E* Ub = La + kLuNB * kLuTile;                         // [k][j], 32 x 64
@@ -257,7 +326,7 @@ __global__ void __launch_bounds__(256) k_lu_gemm(int n, int k0, int nb, E* A, lo
         const int i = e % kLuTile, k = e / kLuTile;
         La[k * kLuTile + i] = (k < nb && r0 + i < n) ? M[(r0 + i) + (long long)(k0 + k) * n] : Elem<E>::zero();
         const int kk = e % kLuNB, j = e / kLuNB;
-        Ub[kk * kLuTile + j] = (kk < nb && c0 + j < n) ? M[(k0 + kk) + (long long)(c0 + j) * n] : Elem<E>::zero();
+        Ub[kk * kLuTile + j] = (kk < nb && c0 + j < cend) ? M[(k0 + kk) + (long long)(c0 + j) * n] : Elem<E>::zero();
     }
     __syncthreads();
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -283,7 +352,7 @@ __global__ void __launch_bounds__(256) k_lu_gemm(int n, int k0, int nb, E* A, lo
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
         const int j = c0 + ty + 16 * b;
-        if (j >= n) continue;
+        if (j >= cend) continue;
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
             const int i = r0 + tx + 16 * a;
@@ -628,43 +697,104 @@ cudaError_t lu_factor_impl(int n, int nmat, E* A, long long stride, int* piv, in
     if (e != cudaSuccess) return e;
     long long nl = 0;
     const int ncb = (n + kLuNB - 1) / kLuNB;
-    for (int k0 = 0; k0 < n; k0 += kLuNB) {
-        const int nb = min(kLuNB, n - k0);
+    // one 32-column panel: factor, exchange and solve the columns below cmax, update
+    // the trailing columns below cend
+    auto panel_step = [&](int k0, int nb, int cmax, int cend) -> cudaError_t {
         const size_t psm = (size_t)(n - k0) * nb * sizeof(E);
         if (psm <= kLuSmemLimit) {
             k_lu_panel<E, true><<<nmat, kLuPanelThreads, psm, st>>>(n, k0, nb, A, stride, piv, info);
         } else {
             bool launched = false;
             if (g_lu_cluster_panels) {
-                e = launch_panel_cluster<E>(n, k0, nb, nmat, A, stride, piv, info, st, &launched);
-                if (e != cudaSuccess) return e;
+                cudaError_t e2 = launch_panel_cluster<E>(n, k0, nb, nmat, A, stride, piv, info, st, &launched);
+                if (e2 != cudaSuccess) return e2;
             }
             if (!launched) k_lu_panel<E, false><<<nmat, kLuPanelThreads, 0, st>>>(n, k0, nb, A, stride, piv, info);
         }
         ++nl;
         if (ncb > 1) {
-            k_lu_swap_trsm<E><<<dim3(ncb, nmat), 256, 0, st>>>(n, k0, nb, A, stride, piv);
+            k_lu_swap_trsm<E><<<dim3(ncb, nmat), 256, 0, st>>>(n, k0, nb, A, stride, piv, cmax);
             ++nl;
         }
-        const int m = n - k0 - nb;
-        if (m > 0) {
-            bool done = false;
-            if constexpr (std::is_same<E, cplxf>::value) {
-                // complex64: A22 -= L21 U12 on the tensor cores (3xTF32) once the trailing
-                // block spans at least one 128-row tile
-                if (tc_err && g_lu_tensor_cores && m >= 128) {
-                    const int t0 = k0 + nb;
-                    e = launch_cgemm_f32(m, m, nb, A + t0 + (long long)k0 * n, n, stride, A + k0 + (long long)t0 * n,
-                                         n, stride, A + t0 + (long long)t0 * n, n, stride, nmat, 1, tc_err, st);
+        const int t0 = k0 + nb;
+        if (t0 < n && cend > t0) {
+            const int rt = (n - t0 + kLuTile - 1) / kLuTile, ct = (cend - t0 + kLuTile - 1) / kLuTile;
+            k_lu_gemm<E><<<dim3(rt, ct, nmat), 256, gemm_smem, st>>>(n, k0, nb, A, stride, cend);
+            ++nl;
+        }
+        return cudaGetLastError();
+    };
+    bool two_level = false;
+    if constexpr (std::is_same<E, cplxf>::value) two_level = tc_err && g_lu_tensor_cores && n >= 2 * kLuBlock;
+    if (two_level) {
+        // complex64 with tensor cores: 128-column blocks.  Inside a block its four
+        // panels update only the block's own columns; then the block's exchanges and
+        // triangular solve reach the columns right of it once, and the trailing matrix
+        // takes one update of depth 128 on the tensor cores (3xTF32), instead of four
+        // of depth 32 -- a quarter of the trailing matrix's reads and writes.
+        if constexpr (std::is_same<E, cplxf>::value) {
+            const size_t blk_smem = (size_t)kLuBlock * (kLuBlock + 1) * sizeof(E);
+            e = cudaFuncSetAttribute(k_lu_swap_trsm_block<E>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)blk_smem);
+            if (e != cudaSuccess) return e;
+            for (int K0 = 0; K0 < n; K0 += kLuBlock) {
+                const int kb = min(kLuBlock, n - K0), cmax = K0 + kb;
+                for (int k0 = K0; k0 < cmax; k0 += kLuNB) {
+                    e = panel_step(k0, min(kLuNB, cmax - k0), cmax, cmax);
                     if (e != cudaSuccess) return e;
-                    done = true;
+                }
+                const int m = n - cmax;
+                if (m > 0) {
+                    const size_t sm = (size_t)kb * (kb + 1) * sizeof(E);
+                    k_lu_swap_trsm_block<E><<<dim3((m + kLuNB - 1) / kLuNB, nmat), 256, sm, st>>>(n, K0, kb, A, stride,
+                                                                                                   piv);
+                    ++nl;
+                    e = launch_cgemm_f32(m, m, kb, A + cmax + (long long)K0 * n, n, stride, A + K0 + (long long)cmax * n,
+                                         n, stride, A + cmax + (long long)cmax * n, n, stride, nmat, 1, tc_err, st);
+                    if (e != cudaSuccess) return e;
+                    ++nl;
                 }
             }
-            if (!done) {
-                const int tiles = (m + kLuTile - 1) / kLuTile;
-                k_lu_gemm<E><<<dim3(tiles, tiles, nmat), 256, gemm_smem, st>>>(n, k0, nb, A, stride);
+        }
+    } else {
+        for (int k0 = 0; k0 < n; k0 += kLuNB) {
+            const int nb = min(kLuNB, n - k0);
+            const size_t psm = (size_t)(n - k0) * nb * sizeof(E);
+            if (psm <= kLuSmemLimit) {
+                k_lu_panel<E, true><<<nmat, kLuPanelThreads, psm, st>>>(n, k0, nb, A, stride, piv, info);
+            } else {
+                bool launched = false;
+                if (g_lu_cluster_panels) {
+                    e = launch_panel_cluster<E>(n, k0, nb, nmat, A, stride, piv, info, st, &launched);
+                    if (e != cudaSuccess) return e;
+                }
+                if (!launched) k_lu_panel<E, false><<<nmat, kLuPanelThreads, 0, st>>>(n, k0, nb, A, stride, piv, info);
             }
             ++nl;
+            if (ncb > 1) {
+                k_lu_swap_trsm<E><<<dim3(ncb, nmat), 256, 0, st>>>(n, k0, nb, A, stride, piv, n);
+                ++nl;
+            }
+            const int m = n - k0 - nb;
+            if (m > 0) {
+                bool done = false;
+                if constexpr (std::is_same<E, cplxf>::value) {
+                    // complex64: A22 -= L21 U12 on the tensor cores (3xTF32) once the trailing
+                    // block spans at least one 128-row tile
+                    if (tc_err && g_lu_tensor_cores && m >= 128) {
+                        const int t0 = k0 + nb;
+                        e = launch_cgemm_f32(m, m, nb, A + t0 + (long long)k0 * n, n, stride, A + k0 + (long long)t0 * n,
+                                             n, stride, A + t0 + (long long)t0 * n, n, stride, nmat, 1, tc_err, st);
+                        if (e != cudaSuccess) return e;
+                        done = true;
+                    }
+                }
+                if (!done) {
+                    const int tiles = (m + kLuTile - 1) / kLuTile;
+                    k_lu_gemm<E><<<dim3(tiles, tiles, nmat), 256, gemm_smem, st>>>(n, k0, nb, A, stride, n);
+                }
+                ++nl;
+            }
         }
     }
     e = lu_perm_from_piv(n, nmat, piv, perm, st);

@@ -1,6 +1,7 @@
 // Batched complex64 update C -= A B on the 5th-generation tensor cores (tcgen05,
 // kind::tf32) with 3xTF32 split products and FP32 accumulation in tensor memory.
-// It is the trailing update of the complex-FP32 LU (csrc/lu.cu), K <= 32.
+// It is the trailing update of the complex-FP32 LU (csrc/lu.cu); K is taken in
+// chunks of 32 complex columns (the LU's blocks are 128 wide).
 //
 // Complex product as one real GEMM of a 128 x 64 complex tile:
 //   A' = [A_r | A_i]               (128 x 64 real, K-major)
@@ -27,7 +28,7 @@ namespace hbem {
 constexpr int kTcM = 128;                    // complex rows per tile = MMA M
 constexpr int kTcNc = 64;                    // complex columns per tile
 constexpr int kTcN = 2 * kTcNc;              // MMA N (real): [re | im]
-constexpr int kTcKc = 32;                    // complex K per launch (the LU panel width)
+constexpr int kTcKc = 32;                    // complex K per chunk
 constexpr int kTcK = 2 * kTcKc;              // real K: [re | im]
 constexpr int kTcThreads = 256;
 constexpr uint32_t kTcKBlockBytes = 128u * 128u;           // 128 rows x 128 bytes
@@ -95,6 +96,7 @@ __global__ void __launch_bounds__(kTcThreads) k_cgemm_tc(TcJob J) {
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_slot;
     __shared__ int s_fail;
+    __shared__ int s_last;   // last chunk whose MMAs were committed (-1: none)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int r0 = blockIdx.x * kTcM, c0 = blockIdx.y * kTcNc;
     const cplxf* A = J.A + (long long)blockIdx.z * J.sa;
@@ -108,79 +110,99 @@ __global__ void __launch_bounds__(kTcThreads) k_cgemm_tc(TcJob J) {
     }
     if (tid == 0) {
         s_fail = 0;
+        s_last = -1;
         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar)), "r"(1));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    // A' = [A_r | A_i]: row r, K index k (re) and 32 + k (im); the loads of a thread
-    // are issued together (16 per thread) before the conversions and stores
-    {
-        constexpr int per = kTcM * kTcKc / kTcThreads;
-        cplxf a[per];
+    // The K dimension in chunks of 32 complex columns: each chunk's A' and B' are split
+    // into TF32 hi / lo parts in shared memory and multiplied into the same TMEM
+    // accumulator.  The global loads of chunk c + 1 are issued into registers before
+    // the wait for chunk c's MMAs, whose operands they then overwrite.
+    constexpr int perA = kTcM * kTcKc / kTcThreads;    // 16 complex per thread
+    constexpr int perB = kTcKc * kTcNc / kTcThreads;   // 8 complex per thread
+    cplxf a[perA], b[perB];
+    auto load_chunk = [&](int kc) {
 #pragma unroll
-        for (int q = 0; q < per; ++q) {
-            const int e = tid + q * kTcThreads, r = e % kTcM, k = e / kTcM;
+        for (int q = 0; q < perA; ++q) {
+            const int e = tid + q * kTcThreads, r = e % kTcM, k = kc + e / kTcM;
             a[q] = (r0 + r < J.m && k < J.k) ? A[(r0 + r) + (long long)k * J.lda] : mkf(0.f);
         }
 #pragma unroll
-        for (int q = 0; q < per; ++q) {
+        for (int q = 0; q < perB; ++q) {
+            const int e = tid + q * kTcThreads, k = kc + e % kTcKc, j = e / kTcKc;
+            b[q] = (k < J.k && c0 + j < J.n) ? B[k + (long long)(c0 + j) * J.ldb] : mkf(0.f);
+        }
+    };
+    const int nchunk = (J.k + kTcKc - 1) / kTcKc;
+    const uint32_t mbar_addr = smem_u32(&mbar);
+    load_chunk(0);
+    for (int c = 0; c < nchunk; ++c) {
+        if (c > 0) {
+            // the MMAs of chunk c - 1 (commit number c - 1: phase parity (c - 1) & 1)
+            // must be done before their operands are overwritten; bounded wait
+            uint32_t done = 0;
+            for (long long it = 0; it < kTcSpinCap && !done && !s_fail; ++it)
+                asm volatile(
+                    "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+                    : "=r"(done)
+                    : "r"(mbar_addr), "r"((uint32_t)((c - 1) & 1))
+                    : "memory");
+            if (!done) s_fail = 1;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            __syncthreads();
+            if (s_fail) break;
+        }
+        // A' = [A_r | A_i]: row r, K index k (re) and 32 + k (im)
+#pragma unroll
+        for (int q = 0; q < perA; ++q) {
             const int e = tid + q * kTcThreads, r = e % kTcM, k = e / kTcM;
             store_split(Ahi, Alo, sw128_offset(r, k), a[q].re);
             store_split(Ahi, Alo, sw128_offset(r, kTcKc + k), a[q].im);
         }
-    }
-    // B' rows (N index): j -> (B_r ; -B_i), 64 + j -> (B_i ; B_r)
-    {
-        constexpr int per = kTcKc * kTcNc / kTcThreads;
-        cplxf b[per];
+        // B' rows (N index): j -> (B_r ; -B_i), 64 + j -> (B_i ; B_r)
 #pragma unroll
-        for (int q = 0; q < per; ++q) {
-            const int e = tid + q * kTcThreads, k = e % kTcKc, j = e / kTcKc;
-            b[q] = (k < J.k && c0 + j < J.n) ? B[k + (long long)(c0 + j) * J.ldb] : mkf(0.f);
-        }
-#pragma unroll
-        for (int q = 0; q < per; ++q) {
+        for (int q = 0; q < perB; ++q) {
             const int e = tid + q * kTcThreads, k = e % kTcKc, j = e / kTcKc;
             store_split(Bhi, Blo, sw128_offset(j, k), b[q].re);
             store_split(Bhi, Blo, sw128_offset(j, kTcKc + k), -b[q].im);
             store_split(Bhi, Blo, sw128_offset(kTcNc + j, k), b[q].im);
             store_split(Bhi, Blo, sw128_offset(kTcNc + j, kTcKc + k), b[q].re);
         }
+        // generic-proxy shared-memory writes -> visible to the tensor core (async proxy)
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (tid == 0) {
+            const uint32_t taddr = tmem_slot;
+            const uint8_t* as[3] = {Alo, Ahi, Ahi};
+            const uint8_t* bs[3] = {Bhi, Blo, Bhi};
+            for (int g = 0; g < 3; ++g)
+                for (int kk = 0; kk < kTcK / 8; ++kk) {
+                    const uint32_t koff = (uint32_t)(kk >> 2) * kTcKBlockBytes + (uint32_t)(kk & 3) * 32u;
+                    const uint64_t ad = sw128_desc(smem_u32(as[g]) + koff);
+                    const uint64_t bd = sw128_desc(smem_u32(bs[g]) + koff);
+                    const uint32_t acc = (c == 0 && g == 0 && kk == 0) ? 0u : 1u;
+                    asm volatile(
+                        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr),
+                        "l"(ad), "l"(bd), "r"(kTcIdesc), "r"(acc));
+                }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_addr)
+                         : "memory");
+            s_last = c;
+        }
+        if (c + 1 < nchunk) load_chunk((c + 1) * kTcKc);
     }
-    // generic-proxy shared-memory writes -> visible to the tensor core (async proxy)
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t taddr = tmem_slot;
-    const uint32_t mbar_addr = smem_u32(&mbar);
-
-    if (tid == 0) {
-        const uint8_t* as[3] = {Alo, Ahi, Ahi};
-        const uint8_t* bs[3] = {Bhi, Blo, Bhi};
-        int first = 1;
-        for (int g = 0; g < 3; ++g)
-            for (int kk = 0; kk < kTcK / 8; ++kk) {
-                const uint32_t koff = (uint32_t)(kk >> 2) * kTcKBlockBytes + (uint32_t)(kk & 3) * 32u;
-                const uint64_t ad = sw128_desc(smem_u32(as[g]) + koff);
-                const uint64_t bd = sw128_desc(smem_u32(bs[g]) + koff);
-                const uint32_t acc = first ? 0u : 1u;
-                first = 0;
-                asm volatile(
-                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                    "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr),
-                    "l"(ad), "l"(bd), "r"(kTcIdesc), "r"(acc));
-            }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_addr)
-                     : "memory");
-    }
-    // wait for the MMAs (phase 0), bounded
-    {
+    // wait for the last chunk's MMAs (commit number nchunk - 1), bounded
+    if (!s_fail) {
         uint32_t done = 0;
         for (long long it = 0; it < kTcSpinCap && !done; ++it)
             asm volatile(
                 "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
                 : "=r"(done)
-                : "r"(mbar_addr), "r"(0u)
+                : "r"(mbar_addr), "r"((uint32_t)((nchunk - 1) & 1))
                 : "memory");
         if (!done) s_fail = 1;
     }
@@ -224,13 +246,14 @@ __global__ void __launch_bounds__(kTcThreads) k_cgemm_tc(TcJob J) {
         }
     } else if (tid == 0) {
         atomicExch(J.err, 1);
-        // give the MMAs another bounded chance to finish before the memory is released
+        // give the last committed MMAs another bounded chance to finish before the
+        // memory is released
         uint32_t done = 0;
-        for (long long it = 0; it < kTcSpinCap && !done; ++it)
+        for (long long it = 0; it < kTcSpinCap && !done && s_last >= 0; ++it)
             asm volatile(
                 "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
                 : "=r"(done)
-                : "r"(mbar_addr), "r"(0u)
+                : "r"(mbar_addr), "r"((uint32_t)(s_last & 1))
                 : "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -264,7 +287,7 @@ cudaError_t launch_cgemm_f32(int m, int n, int k, const cplxf* A, long long lda,
     if (m == 0 || n == 0 || k == 0) return cudaSuccess;
     TcJob J{m, n, k, A, B, C, lda, ldb, ldc, sa, sb, sc, err};
     if (use_tc) {
-        if (k > kTcKc || !err) return cudaErrorInvalidValue;
+        if (!err) return cudaErrorInvalidValue;
         static bool attr = false;
         if (!attr) {
             cudaError_t e = cudaFuncSetAttribute(k_cgemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,

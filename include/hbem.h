@@ -71,6 +71,12 @@ int hbem_set_device(int device);
  *   0 computes it in the kernel for every wavenumber and medium.
  *   "plain_speculate" (default 1): speculative bisection points in the plain
  *   search's small Newton rounds (hbem_find_resonances_plain).
+ *   "autotune" (default 0): the panel-pair assembly times each layout of its general
+ *   pairs (a thread per pair, or a warp per pair with 1-16 pairs per warp) on the
+ *   first launch of every (panels, order, jobs rounded up to a power of two,
+ *   derivative order, real k, panel kind) and uses the fastest from then on; the
+ *   choices persist in the file the environment variable HBEM_TUNE_CACHE names, if
+ *   any.  Results of different layouts agree to rounding (~1e-15).
  *   "plain_warm_start" (default 1): in the plain search, the dense kernel's FP32
  *   Jacobi at a bracket end or Newton point starts from the right singular vectors
  *   of the nearest wavenumber already evaluated (same stopping rule, fewer sweeps). */
@@ -156,6 +162,17 @@ int hbem_gen_sol_op(hbem_solop s, double k_re, double k_im, double c_o, double c
 /* batched form over nk real wavenumbers; T_dev receives [nk][d + 1][2N][2N] */
 int hbem_gen_sol_op_batch_device(hbem_solop s, const double* k_host, int nk, double c_o, double c_i, unsigned d,
                                  void* T_dev);
+/* Many scatterers at once (the batching path of the reference's drivers, which loop
+ * over scatterers and sweep k with std::execution::par,
+ * examples/roots_newton_polygon_rsvd.cpp:172-177): operator i at counts[i] real
+ * wavenumbers k_host[sum_{j<i} counts[j] + q] with inner index c_i_host[i]; T(k) and
+ * its first d derivatives of operator i into T_dev[i] (layout of
+ * hbem_gen_sol_op_batch_device).  The panel-pair quadrature of every (scatterer, k,
+ * medium) runs in one general-pair and one singular-pair launch per panel kind
+ * (lines / arcs), whatever the panel counts; the work is issued on the first
+ * operator's stream and finished on return.                                       */
+int hbem_gen_sol_op_multi_device(const hbem_solop* ops, int nops, const int* counts, const double* k_host,
+                                 const double* c_i_host, double c_o, unsigned d, void* const* T_dev);
 
 /* ------------------------------------------------------------------ scatterers (host only) */
 
@@ -378,7 +395,8 @@ int hbem_arnoldi_sv_batch_device(int n, int nmat, unsigned d, int count, double 
  * ldc, batch strides sa, sb, sc in elements): the trailing update of the LU's
  * complex-FP32 factorisation (the FP32 stand-in for the trailing GEMMs of Eigen's
  * PartialPivLU at source/utilities/randsvd.cpp:104).  tensor_cores = 1: tcgen05
- * MMAs with 3xTF32 split products and FP32 accumulation (k <= 32); 0: FP32 FMA.  */
+ * MMAs with 3xTF32 split products and FP32 accumulation, K in chunks of 32 into one
+ * tensor-memory accumulator; 0: FP32 FMA.                                        */
 int hbem_cgemm_f32_batch_device(int m, int n, int k, const void* A, long long lda, long long sa, const void* B,
                                 long long ldb, long long sb, void* C, long long ldc, long long sc, int nmat,
                                 int tensor_cores);

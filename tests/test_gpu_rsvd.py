@@ -137,3 +137,25 @@ def test_rsvd_mixed_precision_matches_fp64():
         assert np.max(np.abs(got[:, 0] - ref[:, 0]) / ref[:, 0]) < 1e-10
         assert np.max(np.abs(got[:, 1] - ref[:, 1]) / np.maximum(np.abs(ref[:, 1]), 1e-2)) < 1e-8
         assert np.max(np.abs(got[:, 2] - ref[:, 2]) / np.maximum(np.abs(ref[:, 2]), 1e-1)) < 1e-7
+
+
+@pytest.mark.parametrize("n", [256, 300, 513])
+def test_rsvd_mixed_two_level_lu_block_edges(n):
+    """The complex-FP32 LU of order >= 256 runs in 128-column blocks with one depth-128
+    tensor-core update per block (whole blocks, a ragged last block, a single extra
+    column): with FP64 refinement its sigma equals the FP64 path's on the same sketch,
+    with the trailing updates on the tensor cores and in FP32 FMA alike."""
+    rng = np.random.default_rng(n)
+    mats = [[rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) + 3.0 * np.sqrt(n) * np.eye(n)]
+            for _ in range(2)]
+    R = O.rand_sketch(n, 12, seed=n)
+    ref = _rsvd_device(mats, R, 2, 0, 0, 1)[:, 0]
+    got = _rsvd_device(mats, R, 2, 0, 1, 3)[:, 0]
+    assert np.max(np.abs(got - ref) / ref) < 1e-10
+    from helmholtzbem_gb300 import _capi as C
+    C.check(C.lib().hbem_set_option(b"lu_tensor_cores", 0))
+    try:
+        fma = _rsvd_device(mats, R, 2, 0, 1, 3)[:, 0]
+    finally:
+        C.check(C.lib().hbem_set_option(b"lu_tensor_cores", 1))
+    assert np.max(np.abs(fma - ref) / ref) < 1e-10

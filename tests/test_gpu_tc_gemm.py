@@ -41,12 +41,21 @@ def test_tc_update_exact_small_integers():
     got = _update(A, B, C0, 1)[0]
     ref = C0[0] - A[0] @ B[0]
     assert np.array_equal(got, ref.astype(np.complex64))
+    # the same with K = 128 (four chunks accumulated in tensor memory)
+    A = [rng.integers(-2, 3, (m, 128)) + 1j * rng.integers(-2, 3, (m, 128))]
+    B = [rng.integers(-2, 3, (128, n)) + 1j * rng.integers(-2, 3, (128, n))]
+    got = _update(A, B, C0, 1)[0]
+    ref = C0[0] - A[0] @ B[0]
+    assert np.array_equal(got, ref.astype(np.complex64))
 
 
-@pytest.mark.parametrize("shape", [(300, 200, 32, 2), (130, 70, 17, 3), (1, 1, 1, 1), (257, 129, 32, 1)])
+@pytest.mark.parametrize("shape", [(300, 200, 32, 2), (130, 70, 17, 3), (1, 1, 1, 1), (257, 129, 32, 1),
+                                   (300, 200, 128, 2), (190, 77, 77, 1), (256, 128, 96, 1), (129, 65, 33, 2)])
 def test_tc_update_matches_fp32_and_numpy(shape):
-    """Ragged tiles, K < 32, batches: 3xTF32 products with FP32 accumulation agree
-    with the FP32 FMA kernel and with numpy to the FP32 rounding level."""
+    """Ragged tiles, K below, at and above the 32-column chunk (the LU's 128-wide
+    blocks take four chunks into the same accumulator), batches: 3xTF32 products
+    with FP32 accumulation agree with the FP32 FMA kernel and with numpy to the FP32
+    rounding level."""
     m, n, k, nmat = shape
     rng = np.random.default_rng(m + n + k)
     A = [rng.standard_normal((m, k)) + 1j * rng.standard_normal((m, k)) for _ in range(nmat)]

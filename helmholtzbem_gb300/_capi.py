@@ -25,7 +25,7 @@ EXPORTS = [
     "hbem_gen_sol_op_batch_device", "hbem_gen_sol_op_multi_device", "hbem_sv_dense_batch_device", "hbem_sv_dense_batch_noalloc",
     "hbem_sv_dense_batch", "hbem_sweep_sigma", "hbem_rand_sketch", "hbem_rsvd_sv_batch",
     "hbem_rsvd_sv_batch_device", "hbem_rsvd_sv_batch_device_ex", "hbem_lu_factor_batch_device", "hbem_lu_solve_batch_device",
-    "hbem_cgemm_f32_batch_device", "hbem_solop_info", "hbem_sigma_rsvd_sweep", "hbem_opt_subdiv",
+    "hbem_cgemm_f32_batch_device", "hbem_lu_factor_batch_device_f32", "hbem_solop_info", "hbem_sigma_rsvd_sweep", "hbem_opt_subdiv",
     "hbem_find_resonances_adaptive", "hbem_arnoldi_sv_batch", "hbem_arnoldi_sv_batch_device",
     "hbem_scatterer_read", "hbem_polygon_length", "hbem_auto_num_panels", "hbem_polygon_panels",
     "hbem_polygon_panels_graded", "hbem_choose_num_panels",
@@ -148,6 +148,7 @@ def load(path=LIB_PATH):
         "hbem_find_resonances_adaptive": (_i, [_vp, _d, _d, _d, _d, _i, _i, _d, _d, ctypes.c_ulonglong, _i, _i, _dp, _i,
                                                _ip, _ip, _ip]),
         "hbem_lu_factor_batch_device": (_i, [_i, _i, _vp, ctypes.c_longlong, _vp, _ip]),
+        "hbem_lu_factor_batch_device_f32": (_i, [_i, _i, _vp, ctypes.c_longlong, _vp, _ip]),
         "hbem_lu_solve_batch_device": (_i, [_i, _i, _i, _vp, ctypes.c_longlong, _vp, _i, _vp, ctypes.c_longlong]),
         "hbem_find_resonances_plain": (_i, [_vp, _d, _d, _i, _d, _d, _d, _dp, _i, _ip, _dp, _ip]),
         "hbem_rtsafe": (_d, [FN, FN_BOTH, _vp, _d, _d, _d, _ip, _up]),

@@ -50,6 +50,8 @@ cudaError_t rsvd_batched(int n, int nmat, int s, int q, int D, int precision, in
                          void* work, size_t work_bytes, cudaStream_t st, long long* launches);
 cudaError_t lu_factor_batched(int n, int nmat, cplx* A, long long stride, int* piv, int* perm, int* info,
                               cudaStream_t st, long long* launches);
+cudaError_t lu_factor_batched_f32(int n, int nmat, cplxf* A, long long stride, int* piv, int* perm, int* info,
+                                  cudaStream_t st, long long* launches, int* tc_err);
 cudaError_t lu_solve_batched(int n, int nmat, int trans, const cplx* LU, long long stride, const int* perm, int s,
                              cplx* X, long long xstride, cudaStream_t st);
 cudaError_t lu_perm_from_piv(int n, int nmat, const int* piv, int* perm, cudaStream_t st);
@@ -92,6 +94,34 @@ std::atomic<long long> g_launches{0};
 int g_timing = 0;
 std::mutex g_stats_mu;
 double g_asm_ms = 0.;
+// CUDA events bracketing timed assembly launches, resolved (synchronised) when the
+// statistics are read, so that timing does not stall the streams
+std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_asm_pending;
+
+// take the elapsed times of the pending event pairs into g_asm_ms (g_stats_mu held)
+void resolve_pending_locked() {
+    for (auto& pr : g_asm_pending) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(pr.second) == cudaSuccess && cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess)
+            g_asm_ms += ms;
+        cudaEventDestroy(pr.first);
+        cudaEventDestroy(pr.second);
+    }
+    g_asm_pending.clear();
+}
+
+// start / end of a timed assembly launch on stream st (no wait)
+void timing_begin(cudaEvent_t* e0, cudaStream_t st) {
+    *e0 = nullptr;
+    if (cudaEventCreate(e0) == cudaSuccess) cudaEventRecord(*e0, st);
+}
+void timing_end(cudaEvent_t e0, cudaStream_t st) {
+    cudaEvent_t e1 = nullptr;
+    if (!e0 || cudaEventCreate(&e1) != cudaSuccess) return;
+    cudaEventRecord(e1, st);
+    std::lock_guard<std::mutex> lk(g_stats_mu);
+    g_asm_pending.emplace_back(e0, e1);
+}
 std::atomic<long long> g_asm_launches{0};
 std::atomic<long long> g_asm_points{0};   // quadrature points x media processed by timed launches
 // the same split by derivative order and by kind: [d] general pairs, [3 + d] singular
@@ -107,6 +137,7 @@ inline bool svd_fast_on() { return g_svd_fast.load(std::memory_order_relaxed) &&
 int g_arnoldi_maxit = 1000;   // block iterations of hbem_arnoldi_sv_batch*
 int g_plain_speculate = 1;    // plain search: speculative bisection points in small Newton rounds
 int g_plain_warm_start = 1;   // plain search: dense-kernel Jacobi warm-started from nearby V sets
+int g_plain_async = 1;        // plain search: Newton candidates advance independently on their own streams
 int g_singular_table = 1;     // singular pairs read their k-independent point data from a table
 const size_t kSingularTableMax = (size_t)256 << 20;
 
@@ -319,23 +350,13 @@ cudaError_t local_assembly(const DevMesh& M, const SingularTask* tasks, int ntas
                            int njobs, bool real_k, int d, cplx* loc, cudaStream_t st) {
     const int layout = (g_autotune && M.n > 1) ? tuned_layout(M, tasks, ntasks, jobs, njobs, real_k, d, loc, st)
                                                : kLayoutAuto;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    if (g_timing) {
-        cudaEventCreate(&e0);
-        cudaEventCreate(&e1);
-        cudaEventRecord(e0, st);
-    }
+    cudaEvent_t e0 = nullptr;
+    const bool timed = g_timing != 0;
+    if (timed) timing_begin(&e0, st);
     cudaError_t e = launch_local(M, tasks, ntasks, jobs, njobs, real_k, d, loc, st, layout, 3);
     g_launches += (M.n > 1 ? 1 : 0) + (ntasks > 0 ? 1 : 0);
-    if (g_timing) {
-        cudaEventRecord(e1, st);
-        cudaEventSynchronize(e1);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        {
-            std::lock_guard<std::mutex> lk(g_stats_mu);
-            g_asm_ms += ms;
-        }
+    if (timed) {
+        timing_end(e0, st);
         g_asm_launches += 1;
         long long nc2 = (long long)M.nc * M.nc;
         long long nadj = ntasks - ncoinc;
@@ -343,8 +364,6 @@ cudaError_t local_assembly(const DevMesh& M, const SingularTask* tasks, int ntas
         g_asm_points += (long long)njobs * (ncoinc * nc2 + nadj * 2 * nc2 + gen * (long long)M.p * M.p);
         g_asm_split[d] += (long long)njobs * gen * M.p * M.p;
         g_asm_split[(M.sgeo ? 3 : 6) + d] += (long long)njobs * (ncoinc * nc2 + nadj * 2 * nc2);
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
     }
     return e;
 }
@@ -402,7 +421,29 @@ struct hbem_builder_s {
     }
 };
 
+// One in-flight evaluation of sigma, sigma', sigma'' at a few wavenumbers on its own
+// stream (the plain search's Newton phase runs several at once): job table, pair
+// blocks, T / T' / T'', results, and pinned host copies of the results.
+struct EvalLane {
+    cudaStream_t st = nullptr;
+    cudaEvent_t done = nullptr;
+    DBuf jobs, loc, T, out, status, slots;
+    double* h_out = nullptr;   // pinned, 3 x kLaneMaxPts
+    int* h_status = nullptr;   // pinned, kLaneMaxPts
+    int npts = 0;
+    double k[8];
+    ~EvalLane() {
+        for (DBuf* x : {&jobs, &loc, &T, &out, &status, &slots}) x->release();
+        if (h_out) cudaFreeHost(h_out);
+        if (h_status) cudaFreeHost(h_status);
+        if (done) cudaEventDestroy(done);
+        if (st) cudaStreamDestroy(st);
+    }
+};
+constexpr int kLaneMaxPts = 8;
+
 struct hbem_solop_s {
+    std::vector<EvalLane*> lanes;   // created on demand by the lane functions below
     hbem_builder b = nullptr;
     int proj = 1;
     std::vector<double> M;    // N x N column-major
@@ -411,6 +452,7 @@ struct hbem_solop_s {
     DBuf d_uv, d_d1;         // singular vectors of sigma_min kept by sweep_sigma_warm, sigma' scratch
     int uv_count = 0;        // wavenumbers whose (u, v) d_uv holds (0: none valid)
     ~hbem_solop_s() {
+        for (EvalLane* l : lanes) delete l;
         for (DBuf* x : {&d_M, &d_id, &d_sb, &d_lr, &d_T, &d_svdA, &d_svdV, &d_out, &d_status, &d_sig, &d_vpool,
                         &d_slots, &d_uv, &d_d1})
             x->release();
@@ -427,6 +469,7 @@ void hbem_stats_reset(void) {
     g_launches = 0;
     {
         std::lock_guard<std::mutex> lk(g_stats_mu);
+        resolve_pending_locked();
         g_asm_ms = 0.;
     }
     g_asm_launches = 0;
@@ -439,6 +482,7 @@ void hbem_stats_read(long long* launches, double* assembly_ms, long long* assemb
     if (launches) *launches = g_launches;
     if (assembly_ms) {
         std::lock_guard<std::mutex> lk(g_stats_mu);
+        resolve_pending_locked();
         *assembly_ms = g_asm_ms;
     }
     if (assembly_launches) *assembly_launches = g_asm_launches;
@@ -511,6 +555,10 @@ int hbem_set_option(const char* name, int value) {
         g_plain_speculate = value ? 1 : 0;
         return HBEM_OK;
     }
+    if (k == "plain_async") {
+        g_plain_async = value ? 1 : 0;
+        return HBEM_OK;
+    }
     if (k == "arnoldi_maxit") {
         if (value < 1) return fail(HBEM_ERR_INVALID, "set_option: arnoldi_maxit must be >= 1");
         g_arnoldi_maxit = value;
@@ -531,6 +579,7 @@ int hbem_get_option(const char* name, int* value) {
     else if (k == "singular_table") *value = g_singular_table;
     else if (k == "plain_warm_start") *value = g_plain_warm_start;
     else if (k == "plain_speculate") *value = g_plain_speculate;
+    else if (k == "plain_async") *value = g_plain_async;
     else if (k == "arnoldi_maxit") *value = g_arnoldi_maxit;
     else return fail(HBEM_ERR_INVALID, "get_option: unknown option " + k);
     return HBEM_OK;
@@ -847,8 +896,17 @@ int hbem_mass_matrix(hbem_solop s, double* host_out) {
 
 // T(k) (+ derivatives) for nk wavenumbers into T_dev [nk][d+1][2N][2N]; k_host may be complex
 // (interleaved) when kim_host != NULL.
+static int gen_T_batch_ws(hbem_solop s, const double* k_host, const double* kim_host, int nk, double c_o, double c_i,
+                          unsigned d, cplx* T_dev, DBuf& d_jobs, DBuf& d_loc, cudaStream_t st);
+
 static int gen_T_batch(hbem_solop s, const double* k_host, const double* kim_host, int nk, double c_o, double c_i,
                        unsigned d, cplx* T_dev) {
+    return gen_T_batch_ws(s, k_host, kim_host, nk, c_o, c_i, d, T_dev, s->b->d_jobs, s->b->d_loc, s->b->st);
+}
+
+// T(k) batch with the job table and pair-block scratch given, on stream st
+static int gen_T_batch_ws(hbem_solop s, const double* k_host, const double* kim_host, int nk, double c_o, double c_i,
+                          unsigned d, cplx* T_dev, DBuf& d_jobs, DBuf& d_loc, cudaStream_t st) {
     hbem_builder b = s->b;
     const int N = b->n;
     const long long np = b->npair();
@@ -868,16 +926,16 @@ static int gen_T_batch(hbem_solop s, const double* k_host, const double* kim_hos
             jobs.push_back(Job{kr, ki, c_i});
             jobs.push_back(Job{kr, ki, c_o});
         }
-        HB_CK(upload(b->d_jobs, jobs, b->st));
-        HB_CK(b->d_loc.ensure(per_job * 2 * kn));
-        HB_CK(local_assembly(b->view(), b->d_tasks.as<SingularTask>(), (int)b->tasks.size(), b->n, b->d_jobs.as<Job>(),
-                             2 * kn, real_k, (int)d, b->d_loc.as<cplx>(), b->st));
+        HB_CK(upload(d_jobs, jobs, st));
+        HB_CK(d_loc.ensure(per_job * 2 * kn));
+        HB_CK(local_assembly(b->view(), b->d_tasks.as<SingularTask>(), (int)b->tasks.size(), b->n, d_jobs.as<Job>(),
+                             2 * kn, real_k, (int)d, d_loc.as<cplx>(), st));
         cplx* Tk = T_dev + (size_t)k0 * (d + 1) * mat;
-        HB_CK(launch_gather_T(N, (int)d, b->d_loc.as<cplx>(), s->d_M.as<double>(), kn, b->sp(), Tk, b->st));
+        HB_CK(launch_gather_T(N, (int)d, d_loc.as<cplx>(), s->d_M.as<double>(), kn, b->sp(), Tk, st));
         g_launches += 1;
         if (s->proj) {
             HB_CK(launch_projection(N, s->d_id.as<double>(), s->d_sb.as<double>(), s->d_lr.as<double>(), Tk,
-                                    kn * (int)(d + 1), b->st));
+                                    kn * (int)(d + 1), st));
             g_launches += 2;
         }
     }
@@ -986,25 +1044,15 @@ int hbem_gen_sol_op_multi_device(const hbem_solop* ops, int nops, const int* cou
             HB_CK(upload(d_jobs, jobs, st));
             HB_CK(upload(d_start, starts, st));
             HB_CK(d_loc.ensure((size_t)off * sizeof(cplx)));
-            cudaEvent_t e0 = nullptr, e1 = nullptr;
-            if (g_timing) {
-                cudaEventCreate(&e0);
-                cudaEventCreate(&e1);
-                cudaEventRecord(e0, st);
-            }
+            cudaEvent_t e0 = nullptr;
+            const bool timed = g_timing != 0;
+            if (timed) timing_begin(&e0, st);
             HB_CK(launch_local_multi(d_meshes.as<MultiMesh>(), d_jobs.as<MultiJob>(), njobs, d_start.as<long long>(),
                                      gstart.back(), d_start.as<long long>() + gstart.size(), sstart.back(), max_nc,
                                      curved == 1, true, (int)d, d_loc.as<cplx>(), st));
             g_launches += (gstart.back() > 0 ? 1 : 0) + (sstart.back() > 0 ? 1 : 0);
-            if (g_timing) {
-                cudaEventRecord(e1, st);
-                cudaEventSynchronize(e1);
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, e0, e1);
-                {
-                    std::lock_guard<std::mutex> lk(g_stats_mu);
-                    g_asm_ms += ms;
-                }
+            if (timed) {
+                timing_end(e0, st);
                 g_asm_launches += 1;
                 for (int i = 0; i < nops; ++i) {
                     if (!nk[i]) continue;
@@ -1017,8 +1065,6 @@ int hbem_gen_sol_op_multi_device(const hbem_solop* ops, int nops, const int* cou
                     g_asm_split[d] += nj * gen * b->p * b->p;
                     g_asm_split[(b->d_sgeo.p && g_singular_table ? 3 : 6) + d] += nj * (ncoinc * nc2 + nadj * 2 * nc2);
                 }
-                cudaEventDestroy(e0);
-                cudaEventDestroy(e1);
             }
             for (int i = 0; i < nops; ++i) {
                 if (!nk[i]) continue;
@@ -1251,6 +1297,35 @@ int hbem_cgemm_f32_batch_device(int m, int n, int k, const void* A, long long ld
     return HBEM_OK;
 }
 
+int hbem_lu_factor_batch_device_f32(int n, int nmat, void* A_dev, long long stride, int* piv_dev, int* info_host) {
+    if (n < 1 || nmat < 1 || nmat > 65535 || !A_dev || !piv_dev || stride < (long long)n * n)
+        return fail(HBEM_ERR_INVALID, "lu_factor_batch_f32: bad argument");
+    if ((size_t)n * sizeof(int) > 220 * 1024) return fail(HBEM_ERR_UNSUPPORTED, "lu_factor_batch_f32: n too large");
+    HB_CK(cudaSetDevice(g_device));
+    static thread_local DBuf perm, info, tc_err;
+    HB_CK(perm.ensure((size_t)nmat * n * sizeof(int)));
+    HB_CK(info.ensure((size_t)nmat * sizeof(int)));
+    HB_CK(tc_err.ensure(sizeof(int)));
+    HB_CK(cudaMemsetAsync(tc_err.p, 0, sizeof(int), 0));
+    long long nl = 0;
+    HB_CK(lu_factor_batched_f32(n, nmat, static_cast<cplxf*>(A_dev), stride, piv_dev, perm.as<int>(), info.as<int>(),
+                                0, &nl, tc_err.as<int>()));
+    g_launches += nl;
+    std::vector<int> inf(nmat);
+    int terr = 0;
+    HB_CK(cudaMemcpy(inf.data(), info.p, (size_t)nmat * sizeof(int), cudaMemcpyDeviceToHost));
+    HB_CK(cudaMemcpy(&terr, tc_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (terr) return fail(HBEM_ERR_NOCONV, "lu_factor_batch_f32: a tensor-core completion wait timed out");
+    int first = 0;
+    for (int m = 0; m < nmat; ++m) {
+        if (info_host) info_host[m] = inf[m];
+        if (inf[m] && !first) first = m + 1;
+    }
+    if (first)
+        return fail(HBEM_ERR_SINGULAR, "lu_factor_batch_f32: zero pivot (matrix " + std::to_string(first - 1) + ")");
+    return HBEM_OK;
+}
+
 int hbem_lu_factor_batch_device(int n, int nmat, void* A_dev, long long stride, int* piv_dev, int* info_host) {
     if (n < 1 || nmat < 1 || nmat > 65535 || !A_dev || !piv_dev || stride < (long long)n * n)
         return fail(HBEM_ERR_INVALID, "lu_factor_batch: bad argument");
@@ -1463,6 +1538,103 @@ int plain_speculate_ok(hbem_solop s) {
 }
 
 int plain_warm_start_ok() { return g_plain_warm_start; }
+
+int plain_async_ok() { return g_plain_async; }
+
+// The FP32 V-set pool of the dense kernel's warm starts holds at least npool slots
+// (contents kept when it grows).  Synchronous.
+int vpool_ensure(hbem_solop s, int npool) {
+    hbem_builder b = s->b;
+    const size_t mat = 4ULL * b->n * b->n;
+    const size_t pool_bytes = (size_t)npool * mat * sizeof(cplxf);
+    if (pool_bytes <= s->d_vpool.cap) return HBEM_OK;
+    HB_CK(cudaSetDevice(b->device));
+    for (EvalLane* l : s->lanes) HB_CK(cudaStreamSynchronize(l->st));
+    DBuf grown;
+    HB_CK(grown.ensure(pool_bytes));
+    if (s->d_vpool.p) {
+        HB_CK(cudaMemcpyAsync(grown.p, s->d_vpool.p, s->d_vpool.cap, cudaMemcpyDeviceToDevice, b->st));
+        HB_CK(cudaStreamSynchronize(b->st));
+    }
+    s->d_vpool.release();
+    s->d_vpool = grown;
+    return HBEM_OK;
+}
+
+// Lanes: asynchronous sigma, sigma', sigma'' (d = 2) of up to kLaneMaxPts wavenumbers
+// through the one-CTA dense kernel with warm starts from the operator's pool (slots as
+// sweep_sigma_warm).  lane_launch enqueues the assembly, the dense kernel and the copy
+// of the results on the lane's own stream and returns; lane_wait tells whether the
+// lane has finished (blocking when `block`); lane_results gives its values, redoing
+// with the FP64-polished kernel, synchronously, any matrix the fast kernel could not
+// finish.  The dense kernel must take the operator's order (plain_speculate_ok).
+int lane_launch(hbem_solop s, int lane, const double* k_host, int npts, double c_o, double c_i, const int* wslot,
+                const int* oslot, int npool) {
+    if (!s || lane < 0 || lane >= 64 || npts < 1 || npts > kLaneMaxPts)
+        return fail(HBEM_ERR_INVALID, "lane_launch: bad argument");
+    hbem_builder b = s->b;
+    HB_CK(cudaSetDevice(b->device));
+    while ((int)s->lanes.size() <= lane) {
+        EvalLane* l = new EvalLane();
+        s->lanes.push_back(l);
+        HB_CK(cudaStreamCreateWithFlags(&l->st, cudaStreamNonBlocking));
+        HB_CK(cudaEventCreateWithFlags(&l->done, cudaEventDisableTiming));
+        HB_CK(cudaMallocHost(&l->h_out, 3 * kLaneMaxPts * sizeof(double)));
+        HB_CK(cudaMallocHost(&l->h_status, kLaneMaxPts * sizeof(int)));
+    }
+    for (int i = 0; i < npts; ++i)
+        if (wslot[i] >= npool || oslot[i] >= npool) return fail(HBEM_ERR_INVALID, "lane_launch: slot outside the pool");
+    if (int r = vpool_ensure(s, npool)) return r;
+    EvalLane& L = *s->lanes[lane];
+    const int n = 2 * b->n;
+    const size_t mat = (size_t)n * n;
+    L.npts = npts;
+    std::copy(k_host, k_host + npts, L.k);
+    std::vector<int> slots(2 * (size_t)npts);
+    std::copy(wslot, wslot + npts, slots.begin());
+    std::copy(oslot, oslot + npts, slots.begin() + npts);
+    HB_CK(upload(L.slots, slots, L.st));
+    HB_CK(L.T.ensure((size_t)npts * 3 * mat * sizeof(cplx)));
+    HB_CK(L.out.ensure(3 * kLaneMaxPts * sizeof(double)));
+    HB_CK(L.status.ensure(kLaneMaxPts * sizeof(int)));
+    if (int r = gen_T_batch_ws(s, k_host, nullptr, npts, c_o, c_i, 2, L.T.as<cplx>(), L.jobs, L.loc, L.st)) return r;
+    HB_CK(launch_svd_fast(n, npts, 2, L.T.as<cplx>(), 3LL * (long long)mat, (long long)mat, L.out.as<double>(),
+                          L.status.as<int>(), L.st, s->d_vpool.as<cplxf>(), L.slots.as<int>(), L.slots.as<int>() + npts,
+                          nullptr));
+    g_launches += 1;
+    HB_CK(cudaMemcpyAsync(L.h_out, L.out.p, 3 * (size_t)npts * sizeof(double), cudaMemcpyDeviceToHost, L.st));
+    HB_CK(cudaMemcpyAsync(L.h_status, L.status.p, (size_t)npts * sizeof(int), cudaMemcpyDeviceToHost, L.st));
+    HB_CK(cudaEventRecord(L.done, L.st));
+    return HBEM_OK;
+}
+
+int lane_wait(hbem_solop s, int lane, int block, int* finished) {
+    EvalLane& L = *s->lanes[lane];
+    cudaError_t e = block ? cudaEventSynchronize(L.done) : cudaEventQuery(L.done);
+    if (e == cudaErrorNotReady) {
+        *finished = 0;
+        return HBEM_OK;
+    }
+    HB_CK(e);
+    *finished = 1;
+    return HBEM_OK;
+}
+
+int lane_results(hbem_solop s, int lane, double c_o, double c_i, double* out_host) {
+    EvalLane& L = *s->lanes[lane];
+    bool redo = g_svd_force_redo.load(std::memory_order_relaxed) != 0;
+    for (int i = 0; i < L.npts; ++i) redo |= L.h_status[i] != 0;
+    if (!redo) {
+        std::copy(L.h_out, L.h_out + 3 * L.npts, out_host);
+        return HBEM_OK;
+    }
+    const int save = t_svd_polished_only;
+    t_svd_polished_only = 1;
+    const int r = hbem_sweep_sigma(s, L.k, L.npts, c_o, c_i, 2, out_host);
+    t_svd_polished_only = save;
+    return r;
+}
+
 
 // hbem_sweep_sigma through the one-CTA dense kernel with warm starts: a pool of npool
 // FP32 V sets (2N x 2N each) held by the operator; wavenumber i starts its FP32

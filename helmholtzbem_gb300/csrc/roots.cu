@@ -23,6 +23,11 @@
 namespace hbem {
 int plain_speculate_ok(hbem_solop s);
 int plain_warm_start_ok();
+int plain_async_ok();
+int lane_launch(hbem_solop s, int lane, const double* k_host, int npts, double c_o, double c_i, const int* wslot,
+                const int* oslot, int npool);
+int lane_wait(hbem_solop s, int lane, int block, int* finished);
+int lane_results(hbem_solop s, int lane, double c_o, double c_i, double* out_host);
 int sweep_sigma_warm(hbem_solop s, const double* k_host, int nk, double c_o, double c_i, unsigned d,
                      const int* warm_slot, const int* out_slot, int npool, double* out_host, int keep_uv = 0);
 int sigma1_from_kept(hbem_solop s, const double* k_host, const int* idx, int ne, double c_o, double c_i,
@@ -483,6 +488,109 @@ int newton_rounds(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i,
     return HBEM_OK;
 }
 
+// The same Newton phase with every candidate on its own: a candidate's next point is
+// enqueued as soon as its previous one is evaluated, on one of several streams
+// ("lanes"), so one candidate's assembly runs while another's one-CTA dense sigma
+// does, instead of all candidates waiting for the slowest of each lock-step round.
+// Each candidate takes the same Newton and bisection steps as in newton_rounds, with
+// the same warm-start slots; speculative points follow the same rule (a candidate at
+// its first point or after a bisection speculates while at most kSpecRound
+// candidates are unfinished), counted at the moment of its launch rather than per
+// round, so a point may be evaluated from another warm start than in lock step: its
+// values then agree to the dense kernel's accuracy (sigma to ~1e-15, sigma' and
+// sigma'' to ~1e-12 relative), not bit for bit.
+int newton_async(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, int& evals,
+                 const std::vector<int>& first_warm, int slot_base) {
+    const size_t nc = nt.size();
+    if (nc == 0) return HBEM_OK;
+    std::vector<std::vector<std::array<double, 3>>> cache(nc);
+    std::vector<int> cur(first_warm);
+    const int npool = slot_base + 2 * (int)nc;
+    const int nlanes = (int)std::min<size_t>(nc, 32);
+    struct Flight { int cand; int npts; bool spec[4]; double x[4]; };
+    std::vector<Flight> fl(nlanes);
+    std::vector<int> busy(nlanes, 0), in_flight(nc, 0);
+    std::vector<size_t> order;   // lanes in launch order (the oldest is waited for first)
+    auto unfinished = [&]() {
+        size_t u = 0;
+        for (size_t c = 0; c < nc; ++c) u += !nt[c].done;
+        return u;
+    };
+    double out[12];
+    for (;;) {
+        // candidates without a point in flight: consume speculative values, then launch
+        for (size_t c = 0; c < nc; ++c) {
+            if (in_flight[c]) continue;
+            while (!nt[c].done) {
+                auto it = std::find_if(cache[c].begin(), cache[c].end(),
+                                       [&](const std::array<double, 3>& e) { return e[0] == nt[c].rts; });
+                if (it == cache[c].end()) break;
+                nt[c].feed((*it)[1], (*it)[2]);
+                ++evals;
+            }
+            if (nt[c].done) continue;
+            int lane = -1;
+            for (int l = 0; l < nlanes; ++l)
+                if (!busy[l]) { lane = l; break; }
+            if (lane < 0) break;
+            Flight& F = fl[lane];
+            F.cand = (int)c;
+            F.npts = 1;
+            F.x[0] = nt[c].rts;
+            F.spec[0] = false;
+            if (unfinished() <= (size_t)kSpecRound && (nt[c].first || nt[c].bisected)) {
+                cache[c].clear();
+                double sp[2];
+                const int m = nt[c].bisect_next(sp);
+                for (int j = 0; j < m; ++j)
+                    if (sp[j] != nt[c].rts) {
+                        F.x[F.npts] = sp[j];
+                        F.spec[F.npts++] = true;
+                    }
+            }
+            const int own0 = slot_base + 2 * (int)c;
+            int ws[4], os[4];
+            for (int q = 0; q < F.npts; ++q) {
+                ws[q] = cur[c];
+                os[q] = F.spec[q] ? -1 : (cur[c] == own0 ? own0 + 1 : own0);
+            }
+            if (int r = hbem::lane_launch(s, lane, F.x, F.npts, c_o, c_i, ws, os, npool)) return r;
+            cur[c] = os[0];
+            busy[lane] = 1;
+            in_flight[c] = 1;
+            order.push_back((size_t)lane);
+        }
+        if (order.empty()) break;
+        // the first finished lane, else wait for the oldest
+        size_t pick = order.size();
+        for (size_t q = 0; q < order.size() && pick == order.size(); ++q) {
+            int fin = 0;
+            if (int r = hbem::lane_wait(s, (int)order[q], 0, &fin)) return r;
+            if (fin) pick = q;
+        }
+        if (pick == order.size()) {
+            int fin = 0;
+            if (int r = hbem::lane_wait(s, (int)order[0], 1, &fin)) return r;
+            pick = 0;
+        }
+        const int lane = (int)order[pick];
+        order.erase(order.begin() + (long)pick);
+        const Flight& F = fl[lane];
+        if (int r = hbem::lane_results(s, lane, c_o, c_i, out)) return r;
+        for (int q = 0; q < F.npts; ++q) {
+            if (F.spec[q]) {
+                cache[F.cand].push_back({F.x[q], out[3 * q + 1], out[3 * q + 2]});
+            } else {
+                nt[F.cand].feed(out[3 * q + 1], out[3 * q + 2]);
+                ++evals;
+            }
+        }
+        busy[lane] = 0;
+        in_flight[F.cand] = 0;
+    }
+    return HBEM_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -742,7 +850,9 @@ int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npo
     for (size_t c = 0; c < cands.size(); ++c) nt[c].start(cands[c].a, cands[c].a + 2 * h, cands[c].guess, tol);
     // lock-step Newton rounds: one batched sigma', sigma'' evaluation per round (with
     // speculative bisection points where the dense sigma is latency bound)
-    if (hbem::plain_speculate_ok(s)) {
+    if (hbem::plain_speculate_ok(s) && warm && hbem::plain_async_ok()) {
+        if (int r = newton_async(s, nt, c_o, c_i, evals, first_warm, npoints)) return r;
+    } else if (hbem::plain_speculate_ok(s)) {
         if (int r = newton_rounds(s, nt, c_o, c_i, evals, warm ? &first_warm : nullptr, npoints)) return r;
     } else {
         for (int round = 0; round < kMaxIt; ++round) {

@@ -77,6 +77,10 @@ int hbem_set_device(int device);
  *   derivative order, real k, panel kind) and uses the fastest from then on; the
  *   choices persist in the file the environment variable HBEM_TUNE_CACHE names, if
  *   any.  Results of different layouts agree to rounding (~1e-15).
+ *   "plain_async" (default 1): in the plain search (with warm starts), each Newton
+ *   candidate's next point is assembled and evaluated on its own stream as soon as its
+ *   previous one is done, instead of all candidates advancing in lock-step rounds;
+ *   the same Newton steps either way.
  *   "plain_warm_start" (default 1): in the plain search, the dense kernel's FP32
  *   Jacobi at a bracket end or Newton point starts from the right singular vectors
  *   of the nearest wavenumber already evaluated (same stopping rule, fewer sweeps). */
@@ -407,6 +411,12 @@ int hbem_cgemm_f32_batch_device(int m, int n, int k, const void* A, long long ld
  * row k at step k (0-based LAPACK ipiv).  info_host (may be NULL): per matrix 0 or
  * 1 + the first step with a zero pivot; any zero pivot -> HBEM_ERR_SINGULAR.     */
 int hbem_lu_factor_batch_device(int n, int nmat, void* A_dev, long long stride, int* piv_dev, int* info_host);
+/* The same in complex FP32 (the factorisation behind the mixed-precision randomized
+ * SVD): complex64 matrices; from order 256 on in 128-column blocks whose trailing
+ * updates run on the tensor cores with 3xTF32 products and FP32 accumulation
+ * (set_option "lu_tensor_cores" 0: FP32 FMA and 32-column panels).  HBEM_ERR_NOCONV
+ * if a tensor-core completion wait timed out.                                   */
+int hbem_lu_factor_batch_device_f32(int n, int nmat, void* A_dev, long long stride, int* piv_dev, int* info_host);
 /* Solve with the factors (PartialPivLU::solve, and .adjoint().solve for trans = 1):
  * X_m <- T_m^-1 X_m or T_m^-H X_m, nrhs columns at X_dev + m * xstride, leading
  * dimension n.                                                                   */

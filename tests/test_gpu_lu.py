@@ -113,3 +113,34 @@ def test_cluster_panel_matches_global_panel(n):
     for m in range(nmat):
         ref = np.linalg.solve(mats[m], b)
         assert np.linalg.norm(X.cpu().numpy()[m].T - ref) <= 1e-12 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("n", [100, 256, 300, 513])
+def test_lu_f32_reconstructs_pa_both_update_paths(n):
+    """The complex-FP32 LU (from order 256: 128-column blocks with depth-128 tensor-core
+    updates, 3xTF32) reconstructs P A to the FP32 rounding level, with |L| <= 1, and
+    its pivots are those of the FP32 FMA path with 32-column panels."""
+    nmat = 2
+    mats = _mats(n, nmat, seed=3 * n)
+    res = []
+    for tc in (1, 0):
+        check(C.lib().hbem_set_option(b"lu_tensor_cores", tc))
+        try:
+            A = torch.from_numpy(np.ascontiguousarray(np.stack([m.T for m in mats]).astype(np.complex64))).cuda()
+            piv = torch.zeros(nmat * n, dtype=torch.int32, device="cuda")
+            check(C.lib().hbem_lu_factor_batch_device_f32(n, nmat, ctypes.c_void_p(A.data_ptr()), n * n,
+                                                          ctypes.c_void_p(piv.data_ptr()), None))
+        finally:
+            check(C.lib().hbem_set_option(b"lu_tensor_cores", 1))
+        res.append((A.cpu().numpy(), piv.cpu().numpy().reshape(nmat, n)))
+    for (F, p) in res:
+        for m in range(nmat):
+            LU = F[m].T.astype(np.complex128)
+            L = np.tril(LU, -1) + np.eye(n)
+            U = np.triu(LU)
+            PA = mats[m].copy()
+            for k in range(n):
+                PA[[k, p[m, k]]] = PA[[p[m, k], k]]
+            assert np.linalg.norm(L @ U - PA) <= 2e-6 * np.linalg.norm(PA)
+            assert np.max(np.abs(L)) <= 1.0 + 1e-6
+    assert np.array_equal(res[0][1], res[1][1])

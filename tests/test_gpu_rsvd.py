@@ -146,8 +146,15 @@ def test_rsvd_mixed_two_level_lu_block_edges(n):
     column): with FP64 refinement its sigma equals the FP64 path's on the same sketch,
     with the trailing updates on the tensor cores and in FP32 FMA alike."""
     rng = np.random.default_rng(n)
-    mats = [[rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) + 3.0 * np.sqrt(n) * np.eye(n)]
-            for _ in range(2)]
+    mats = []
+    for _ in range(2):
+        # a clear smallest singular value, so that the randomized estimate has converged
+        # and only the LU's accuracy can move it
+        U, _ = np.linalg.qr(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+        V, _ = np.linalg.qr(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+        sv = np.linspace(1.0, 4.0, n)
+        sv[0] = 1e-3
+        mats.append([(U * sv) @ V.conj().T])
     R = O.rand_sketch(n, 12, seed=n)
     ref = _rsvd_device(mats, R, 2, 0, 0, 1)[:, 0]
     got = _rsvd_device(mats, R, 2, 0, 1, 3)[:, 0]

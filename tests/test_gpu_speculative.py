@@ -85,3 +85,21 @@ def test_batched_plain_search_with_speculation_matches_plain_rounds():
         assert len(a) == len(b)
         if len(a):
             assert np.max(np.abs(np.asarray(a) - np.asarray(b))) <= 1e-10
+
+
+def test_async_newton_matches_lock_step():
+    """The plain search's Newton phase with every candidate on its own stream (the
+    default) against the lock-step rounds: the same roots to 1e-10 and the same number
+    of evaluations, on the bench workload (circle N = 50, order 11, 200 points)."""
+    from helmholtzbem_gb300 import _capi as C, api, geometry
+    so = api.SolutionsOperator(api.BuilderData(geometry.circle(0.25, 50), order=11))
+    a_roots, a_grid, a_nev = so.find_resonances_plain(0.5, 10.0, 200, 1.0, 23.4, tol=1e-8)
+    C.check(C.lib().hbem_set_option(b"plain_async", 0))
+    try:
+        l_roots, l_grid, l_nev = so.find_resonances_plain(0.5, 10.0, 200, 1.0, 23.4, tol=1e-8)
+    finally:
+        C.check(C.lib().hbem_set_option(b"plain_async", 1))
+    assert a_roots.size == l_roots.size == 10
+    assert np.max(np.abs(np.sort(a_roots) - np.sort(l_roots))) <= 1e-10
+    assert a_nev == l_nev
+    np.testing.assert_array_equal(a_grid[:, 0], l_grid[:, 0])

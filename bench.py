@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--full-configs", action="store_true",
                     help="one run of the batching configuration at its full size (8 scatterers x 256 k) and "
                          "of the precision configuration at all eight wavenumbers 40..47; prints one JSON line")
+    ap.add_argument("--profile-lu", action="store_true",
+                    help="one complex-FP32 LU of order 8000 (for ncu captures of the tensor-core update)")
     ap.add_argument("--profile-field", action="store_true",
                     help="no timing: the field-at-scale scatterer lifted on a 160 x 160 grid (for ncu captures)")
     return ap.parse_args()
@@ -112,6 +114,33 @@ def run_profile_dense_tail():
         C.check(L.hbem_rsvd_sv_batch_device_ex(n, nk, 0, ctypes.c_void_p(T.data_ptr()), n * n, n * n,
                                                ctypes.c_void_p(R.data_ptr()), 12, 2, prec, 3, C.dptr(out)))
     print("profile dense tail done, sigma = %s" % out)
+
+
+def run_profile_lu():
+    """The complex-FP32 LU of one matrix of order 8000 (the precision configuration's
+    size; a random complex matrix with a dominant diagonal stands in for T(k)): 62
+    depth-128 tensor-core trailing updates, each preceded by four panel
+    factorisations and a block triangular solve."""
+    import ctypes
+    import torch
+    from helmholtzbem_gb300 import _capi as C
+    n = 8000
+    g = torch.Generator(device="cuda").manual_seed(8000)
+    A = torch.randn((n, n), dtype=torch.complex64, device="cuda", generator=g)
+    A += 3.0 * math.sqrt(n) * torch.eye(n, dtype=torch.complex64, device="cuda")
+    piv = torch.zeros(n, dtype=torch.int32, device="cuda")
+    C.check(C.lib().hbem_lu_factor_batch_device_f32(n, 1, ctypes.c_void_p(A.data_ptr()), n * n,
+                                                    ctypes.c_void_p(piv.data_ptr()), None))
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    A2 = torch.randn((n, n), dtype=torch.complex64, device="cuda", generator=g)
+    A2 += 3.0 * math.sqrt(n) * torch.eye(n, dtype=torch.complex64, device="cuda")
+    ev[0].record()
+    C.check(C.lib().hbem_lu_factor_batch_device_f32(n, 1, ctypes.c_void_p(A2.data_ptr()), n * n,
+                                                    ctypes.c_void_p(piv.data_ptr()), None))
+    ev[1].record()
+    torch.cuda.synchronize()
+    print("profile lu done: n = %d, %.2f ms" % (n, ev[0].elapsed_time(ev[1])))
 
 
 def dist_env():
@@ -436,6 +465,21 @@ def precision_at_scale(torch, C, api, geometry, lib, ks=(40.0, 41.0)):
     mixed_ms = timed(lambda: rsvd(1))
     fp64_ms = timed(lambda: rsvd(0))
     err = np.abs(out[1] - out[0]) / out[0]
+    # the complex-FP32 LU alone (tensor-core 128-column blocks, and FP32 FMA with
+    # 32-column panels for comparison), on a complex64 copy of the first T
+    lu = {}
+    T32 = torch.empty((n, n), dtype=torch.complex64, device="cuda")
+    piv = torch.zeros(n, dtype=torch.int32, device="cuda")
+    for tc in (1, 0):
+        C.check(lib.hbem_set_option(b"lu_tensor_cores", tc))
+        try:
+            T32.copy_(T[0])
+            ms = timed(lambda: C.check(lib.hbem_lu_factor_batch_device_f32(n, 1, ctypes.c_void_p(T32.data_ptr()), n * n,
+                                                                           ctypes.c_void_p(piv.data_ptr()), None)))
+        finally:
+            C.check(lib.hbem_set_option(b"lu_tensor_cores", 1))
+        lu["tensor_cores" if tc else "fp32_fma"] = {"ms": ms, "tflops": 8.0 / 3.0 * n ** 3 / (ms * 1e-3) / 1e12}
+    del T32
     # sigma_min of T itself in FP64: the Arnoldi path (block iteration on T^-1 T^-H
     # with an FP64 LU, ARPACK's residual test at 1e-12; checked against dense SVD and
     # against ARPACK in the tests) -- the dense FP64 reference at this order
@@ -453,6 +497,7 @@ def precision_at_scale(torch, C, api, geometry, lib, ks=(40.0, 41.0)):
             "sigma_min_dense_fp64": [float(x) for x in arn],
             "dense_fp64_method": "Arnoldi on T^-1 T^-H, FP64 LU, residual <= 1e-12 sigma (iterations %s)" % list(it),
             "arnoldi_ms_per_T": arn_ms / nk,
+            "lu_complex64_n8000": lu,
             "rel_err_vs_dense_fp64": {"mixed": [float(x) for x in np.abs(out[1] - arn) / arn],
                                       "fp64_rsvd": [float(x) for x in np.abs(out[0] - arn) / arn]}}
 
@@ -825,7 +870,6 @@ def run_gpu(args):
 
     lib = C.lib()
     lib.hbem_stats_reset()
-    lib.hbem_stats_enable_timing(1)
     tot_ms, tot_v, nev_tot = 0.0, 0, 0
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
@@ -839,10 +883,9 @@ def run_gpu(args):
             tot_ms += e0.elapsed_time(e1)
             tot_v += v
             nev_tot += nev
-    lib.hbem_stats_enable_timing(0)
     launches, asm_ms, asm_l, asm_pts = (C.ctypes.c_longlong(), C.ctypes.c_double(), C.ctypes.c_longlong(),
                                         C.ctypes.c_longlong())
-    lib.hbem_stats_read(C.ctypes.byref(launches), C.ctypes.byref(asm_ms), C.ctypes.byref(asm_l), C.ctypes.byref(asm_pts))
+    lib.hbem_stats_read(C.ctypes.byref(launches), None, None, None)
     ms, tot_v_all = combine_ranks(tot_ms, tot_v, world)
     value = tot_v_all / (ms * 1e-3)
 
@@ -867,7 +910,20 @@ def run_gpu(args):
     d2h = int(roots.nbytes + CFG["npoints"] * 3 * 8 + 2 * roots.size * 3 * 8)   # roots, grid, verification
 
     # roofline of the dominant kernel (panel-pair assembly, FP64 CUDA-core bound):
-    # algorithmic work of the timed launches by derivative order and point kind
+    # algorithmic work of the timed launches by derivative order and point kind, on one
+    # search of the workload with the Newton candidates in lock step, so that the timed
+    # assembly launches do not overlap (on per-candidate streams a launch's event
+    # interval would also cover other candidates' kernels)
+    C.check(lib.hbem_set_option(b"plain_async", 0))
+    try:
+        lib.hbem_stats_reset()
+        lib.hbem_stats_enable_timing(1)
+        step(so)
+        torch.cuda.synchronize()
+        lib.hbem_stats_enable_timing(0)
+        lib.hbem_stats_read(None, C.ctypes.byref(asm_ms), C.ctypes.byref(asm_l), C.ctypes.byref(asm_pts))
+    finally:
+        C.check(lib.hbem_set_option(b"plain_async", 1))
     flops = assembly_flops(C, lib)
     achieved = flops / (asm_ms.value * 1e-3) / 1e12 if asm_ms.value > 0 else 0.0
     peak = fp64_peak_tflops()
@@ -881,6 +937,7 @@ def run_gpu(args):
                 "traffic": 3.0e7, "traffic_unit": "bytes per launch",
                 "peak_source": "measured: cuBLAS DGEMM 8192^3 on this GPU (MEASURED_PEAKS.json has no FP64 entry)",
                 "kernel": "k_general + k_singular (panel-pair assembly)", "launches": asm_l.value,
+                "measured_on": "one search of the workload, Newton candidates in lock step (non-overlapping launches)",
                 "avg_launch_ms": asm_ms.value / max(1, asm_l.value),
                 # nominal FP64 peak: 2 DFMA per cycle per SM x 152 SMs at the sampled SM clock
                 "peak_nominal": nominal_fp64_tflops(), "frac_of_nominal": achieved / nominal_fp64_tflops(),
@@ -977,6 +1034,8 @@ def main():
         run_profile_case()
     elif args.profile_field:
         run_profile_field()
+    elif args.profile_lu:
+        run_profile_lu()
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -442,8 +442,32 @@ struct EvalLane {
 };
 constexpr int kLaneMaxPts = 8;
 
+// Lanes are kept per host thread and device (a search runs on one thread at a time),
+// so that operators created one after another reuse their streams, events and pinned
+// result buffers; a lane's device buffers grow to the largest batch it has served.
+struct LanePool {
+    int device = -1;
+    std::vector<EvalLane*> lanes;
+    ~LanePool() {
+        for (EvalLane* l : lanes) delete l;
+    }
+};
+thread_local std::vector<LanePool*> t_lane_pools;
+thread_local struct LanePoolsOwner {
+    ~LanePoolsOwner() {
+        for (LanePool* p : t_lane_pools) delete p;
+    }
+} t_lane_pools_owner;
+
+LanePool& lane_pool(int device) {
+    for (LanePool* p : t_lane_pools)
+        if (p->device == device) return *p;
+    t_lane_pools.push_back(new LanePool());
+    t_lane_pools.back()->device = device;
+    return *t_lane_pools.back();
+}
+
 struct hbem_solop_s {
-    std::vector<EvalLane*> lanes;   // created on demand by the lane functions below
     hbem_builder b = nullptr;
     int proj = 1;
     std::vector<double> M;    // N x N column-major
@@ -452,7 +476,6 @@ struct hbem_solop_s {
     DBuf d_uv, d_d1;         // singular vectors of sigma_min kept by sweep_sigma_warm, sigma' scratch
     int uv_count = 0;        // wavenumbers whose (u, v) d_uv holds (0: none valid)
     ~hbem_solop_s() {
-        for (EvalLane* l : lanes) delete l;
         for (DBuf* x : {&d_M, &d_id, &d_sb, &d_lr, &d_T, &d_svdA, &d_svdV, &d_out, &d_status, &d_sig, &d_vpool,
                         &d_slots, &d_uv, &d_d1})
             x->release();
@@ -1549,7 +1572,7 @@ int vpool_ensure(hbem_solop s, int npool) {
     const size_t pool_bytes = (size_t)npool * mat * sizeof(cplxf);
     if (pool_bytes <= s->d_vpool.cap) return HBEM_OK;
     HB_CK(cudaSetDevice(b->device));
-    for (EvalLane* l : s->lanes) HB_CK(cudaStreamSynchronize(l->st));
+    for (EvalLane* l : lane_pool(b->device).lanes) HB_CK(cudaStreamSynchronize(l->st));
     DBuf grown;
     HB_CK(grown.ensure(pool_bytes));
     if (s->d_vpool.p) {
@@ -1574,9 +1597,10 @@ int lane_launch(hbem_solop s, int lane, const double* k_host, int npts, double c
         return fail(HBEM_ERR_INVALID, "lane_launch: bad argument");
     hbem_builder b = s->b;
     HB_CK(cudaSetDevice(b->device));
-    while ((int)s->lanes.size() <= lane) {
+    std::vector<EvalLane*>& lanes = lane_pool(b->device).lanes;
+    while ((int)lanes.size() <= lane) {
         EvalLane* l = new EvalLane();
-        s->lanes.push_back(l);
+        lanes.push_back(l);
         HB_CK(cudaStreamCreateWithFlags(&l->st, cudaStreamNonBlocking));
         HB_CK(cudaEventCreateWithFlags(&l->done, cudaEventDisableTiming));
         HB_CK(cudaMallocHost(&l->h_out, 3 * kLaneMaxPts * sizeof(double)));
@@ -1585,7 +1609,7 @@ int lane_launch(hbem_solop s, int lane, const double* k_host, int npts, double c
     for (int i = 0; i < npts; ++i)
         if (wslot[i] >= npool || oslot[i] >= npool) return fail(HBEM_ERR_INVALID, "lane_launch: slot outside the pool");
     if (int r = vpool_ensure(s, npool)) return r;
-    EvalLane& L = *s->lanes[lane];
+    EvalLane& L = *lanes[lane];
     const int n = 2 * b->n;
     const size_t mat = (size_t)n * n;
     L.npts = npts;
@@ -1609,7 +1633,7 @@ int lane_launch(hbem_solop s, int lane, const double* k_host, int npts, double c
 }
 
 int lane_wait(hbem_solop s, int lane, int block, int* finished) {
-    EvalLane& L = *s->lanes[lane];
+    EvalLane& L = *lane_pool(s->b->device).lanes[lane];
     cudaError_t e = block ? cudaEventSynchronize(L.done) : cudaEventQuery(L.done);
     if (e == cudaErrorNotReady) {
         *finished = 0;
@@ -1621,7 +1645,7 @@ int lane_wait(hbem_solop s, int lane, int block, int* finished) {
 }
 
 int lane_results(hbem_solop s, int lane, double c_o, double c_i, double* out_host) {
-    EvalLane& L = *s->lanes[lane];
+    EvalLane& L = *lane_pool(s->b->device).lanes[lane];
     bool redo = g_svd_force_redo.load(std::memory_order_relaxed) != 0;
     for (int i = 0; i < L.npts; ++i) redo |= L.h_status[i] != 0;
     if (!redo) {

@@ -490,37 +490,76 @@ int newton_rounds(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i,
 
 // The same Newton phase with every candidate on its own: a candidate's next point is
 // enqueued as soon as its previous one is evaluated, on one of several streams
-// ("lanes"), so one candidate's assembly runs while another's one-CTA dense sigma
-// does, instead of all candidates waiting for the slowest of each lock-step round.
-// Each candidate takes the same Newton and bisection steps as in newton_rounds, with
-// the same warm-start slots; speculative points follow the same rule (a candidate at
-// its first point or after a bisection speculates while at most kSpecRound
-// candidates are unfinished), counted at the moment of its launch rather than per
-// round, so a point may be evaluated from another warm start than in lock step: its
-// values then agree to the dense kernel's accuracy (sigma to ~1e-15, sigma' and
-// sigma'' to ~1e-12 relative), not bit for bit.
+// ("lanes", one point each), so one candidate's assembly runs while another's
+// one-CTA dense sigma does, instead of all candidates waiting for the slowest of
+// each lock-step round.  Speculative bisection points go to lanes of their own, so
+// they do not delay the Newton point they accompany; while at most kSpecDeep
+// candidates are unfinished (the GPU otherwise idle) the points of the bisection
+// after next are speculated too.  Each candidate takes the same Newton and
+// bisection steps as in newton_rounds, with the same warm-start slots for its Newton
+// points; a speculative point may be evaluated from another warm start than in lock
+// step, so its values agree to the dense kernel's accuracy (sigma to ~1e-15, sigma'
+// and sigma'' to ~1e-12 relative), not bit for bit.
+constexpr int kSpecDeep = 2;
+constexpr int kLanes = 32;
+
 int newton_async(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, int& evals,
                  const std::vector<int>& first_warm, int slot_base) {
     const size_t nc = nt.size();
     if (nc == 0) return HBEM_OK;
     std::vector<std::vector<std::array<double, 3>>> cache(nc);
+    std::vector<std::vector<double>> pend(nc);   // speculative points in flight
     std::vector<int> cur(first_warm);
     const int npool = slot_base + 2 * (int)nc;
-    const int nlanes = (int)std::min<size_t>(nc, 32);
-    struct Flight { int cand; int npts; bool spec[4]; double x[4]; };
-    std::vector<Flight> fl(nlanes);
-    std::vector<int> busy(nlanes, 0), in_flight(nc, 0);
-    std::vector<size_t> order;   // lanes in launch order (the oldest is waited for first)
+    struct Flight { int cand; double x; bool spec; int rslot; };
+    std::vector<Flight> fl(kLanes);
+    std::vector<int> busy(kLanes, 0), in_flight(nc, 0);
+    std::vector<int> order;   // lanes in launch order (the oldest is waited for first)
     auto unfinished = [&]() {
         size_t u = 0;
         for (size_t c = 0; c < nc; ++c) u += !nt[c].done;
         return u;
     };
-    double out[12];
-    for (;;) {
-        // candidates without a point in flight: consume speculative values, then launch
-        for (size_t c = 0; c < nc; ++c) {
-            if (in_flight[c]) continue;
+    auto has = [](const std::vector<double>& v, double x) { return std::find(v.begin(), v.end(), x) != v.end(); };
+    auto cached = [&](size_t c, double x) {
+        return std::find_if(cache[c].begin(), cache[c].end(),
+                            [&](const std::array<double, 3>& e) { return e[0] == x; }) != cache[c].end();
+    };
+    auto free_lane = [&]() {
+        for (int l = 0; l < kLanes; ++l)
+            if (!busy[l]) return l;
+        return -1;
+    };
+    double out[3];
+    // take the results of a finished lane
+    auto finish = [&](int lane) -> int {
+        order.erase(std::find(order.begin(), order.end(), lane));
+        const Flight F = fl[lane];
+        busy[lane] = 0;
+        if (int r = hbem::lane_results(s, lane, c_o, c_i, out)) return r;
+        if (F.spec) {
+            cache[F.cand].push_back({F.x, out[1], out[2]});
+            pend[F.cand].erase(std::find(pend[F.cand].begin(), pend[F.cand].end(), F.x));
+        } else {
+            nt[F.cand].feed(out[1], out[2]);
+            ++evals;
+            in_flight[F.cand] = 0;
+        }
+        return HBEM_OK;
+    };
+    auto launch = [&](int lane, size_t c, double x, bool spec, int ws, int os) -> int {
+        if (int r = hbem::lane_launch(s, lane, &x, 1, c_o, c_i, &ws, &os, npool)) return r;
+        fl[lane] = Flight{(int)c, x, spec, ws};
+        busy[lane] = 1;
+        order.push_back(lane);
+        return HBEM_OK;
+    };
+    // launch candidate c's next point (and its speculative points) if it needs one:
+    // returns -1 when no lane is free, a status code on error, 0 otherwise
+    auto advance = [&](size_t c) -> int {
+        for (;;) {
+            if (in_flight[c]) return 0;
+            // values already at hand (speculative points evaluated earlier)
             while (!nt[c].done) {
                 auto it = std::find_if(cache[c].begin(), cache[c].end(),
                                        [&](const std::array<double, 3>& e) { return e[0] == nt[c].rts; });
@@ -528,65 +567,77 @@ int newton_async(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, 
                 nt[c].feed((*it)[1], (*it)[2]);
                 ++evals;
             }
-            if (nt[c].done) continue;
-            int lane = -1;
-            for (int l = 0; l < nlanes; ++l)
-                if (!busy[l]) { lane = l; break; }
-            if (lane < 0) break;
-            Flight& F = fl[lane];
-            F.cand = (int)c;
-            F.npts = 1;
-            F.x[0] = nt[c].rts;
-            F.spec[0] = false;
-            if (unfinished() <= (size_t)kSpecRound && (nt[c].first || nt[c].bisected)) {
-                cache[c].clear();
-                double sp[2];
-                const int m = nt[c].bisect_next(sp);
-                for (int j = 0; j < m; ++j)
-                    if (sp[j] != nt[c].rts) {
-                        F.x[F.npts] = sp[j];
-                        F.spec[F.npts++] = true;
-                    }
+            if (nt[c].done || has(pend[c], nt[c].rts)) return 0;   // done, or its point is on its way
+            const int own0 = slot_base + 2 * (int)c, wslot = cur[c], oslot = cur[c] == own0 ? own0 + 1 : own0;
+            // the slot this point's V set goes to must not be read by a speculative point
+            // still in flight (it started from the slot before)
+            bool waited = false;
+            for (size_t q = 0; q < order.size(); ++q) {
+                const int l = order[q];
+                if (fl[l].cand == (int)c && fl[l].spec && fl[l].rslot == oslot) {
+                    int fin = 0;
+                    if (int r = hbem::lane_wait(s, l, 1, &fin)) return r;
+                    if (int r = finish(l)) return r;
+                    waited = true;
+                    break;
+                }
             }
-            const int own0 = slot_base + 2 * (int)c;
-            int ws[4], os[4];
-            for (int q = 0; q < F.npts; ++q) {
-                ws[q] = cur[c];
-                os[q] = F.spec[q] ? -1 : (cur[c] == own0 ? own0 + 1 : own0);
-            }
-            if (int r = hbem::lane_launch(s, lane, F.x, F.npts, c_o, c_i, ws, os, npool)) return r;
-            cur[c] = os[0];
-            busy[lane] = 1;
+            if (waited) continue;   // look again: the wait may have brought this point's value
+            const int lane = free_lane();
+            if (lane < 0) return -1;
+            if (int r = launch(lane, c, nt[c].rts, false, wslot, oslot)) return r;
             in_flight[c] = 1;
-            order.push_back((size_t)lane);
+            cur[c] = oslot;
+            // speculative bisection points (the same rule as the lock-step rounds, plus the
+            // next level when few candidates are left)
+            const size_t left = unfinished();
+            if (left <= (size_t)kSpecRound && (nt[c].first || nt[c].bisected)) {
+                double pts[6];
+                int np = nt[c].bisect_next(pts);
+                if (left <= (size_t)kSpecDeep && !nt[c].first) {
+                    const int n1 = np;
+                    for (int j = 0; j < n1; ++j) {
+                        // the state after a bisection to pts[j] (feed()'s operations)
+                        Newton t = nt[c];
+                        if (j == 0) t.xl = t.rts;
+                        else t.xh = t.rts;
+                        t.dx = 0.5 * (t.xh - t.xl);
+                        t.rts = t.xl + t.dx;
+                        if (t.rts == pts[j]) np += t.bisect_next(pts + np);
+                    }
+                }
+                for (int j = 0; j < np; ++j) {
+                    const double x = pts[j];
+                    if (x == nt[c].rts || cached(c, x) || has(pend[c], x)) continue;
+                    const int l2 = free_lane();
+                    if (l2 < 0) break;
+                    if (int r = launch(l2, c, x, true, wslot, -1)) return r;
+                    pend[c].push_back(x);
+                }
+            }
+            return 0;
+        }
+    };
+    for (;;) {
+        for (size_t c = 0; c < nc; ++c) {
+            const int r = advance(c);
+            if (r == -1) break;
+            if (r) return r;
         }
         if (order.empty()) break;
         // the first finished lane, else wait for the oldest
-        size_t pick = order.size();
-        for (size_t q = 0; q < order.size() && pick == order.size(); ++q) {
+        int pick = -1;
+        for (size_t q = 0; q < order.size() && pick < 0; ++q) {
             int fin = 0;
-            if (int r = hbem::lane_wait(s, (int)order[q], 0, &fin)) return r;
-            if (fin) pick = q;
+            if (int r = hbem::lane_wait(s, order[q], 0, &fin)) return r;
+            if (fin) pick = order[q];
         }
-        if (pick == order.size()) {
+        if (pick < 0) {
             int fin = 0;
-            if (int r = hbem::lane_wait(s, (int)order[0], 1, &fin)) return r;
-            pick = 0;
+            pick = order[0];
+            if (int r = hbem::lane_wait(s, pick, 1, &fin)) return r;
         }
-        const int lane = (int)order[pick];
-        order.erase(order.begin() + (long)pick);
-        const Flight& F = fl[lane];
-        if (int r = hbem::lane_results(s, lane, c_o, c_i, out)) return r;
-        for (int q = 0; q < F.npts; ++q) {
-            if (F.spec[q]) {
-                cache[F.cand].push_back({F.x[q], out[3 * q + 1], out[3 * q + 2]});
-            } else {
-                nt[F.cand].feed(out[3 * q + 1], out[3 * q + 2]);
-                ++evals;
-            }
-        }
-        busy[lane] = 0;
-        in_flight[F.cand] = 0;
+        if (int r = finish(pick)) return r;
     }
     return HBEM_OK;
 }

@@ -848,18 +848,12 @@ def run_gpu(args):
     last_grid = [None]
 
     def step(solop):
-        roots, grid, nev = solop.find_resonances_plain(CFG["k_min"], CFG["k_max"], CFG["npoints"], CFG["c_o"],
-                                                       CFG["c_i"], tol=CFG["tol"])
+        # the search with every root checked: sigma' at root - tol and root + tol, each
+        # root's two points evaluated as soon as it has converged
+        roots, grid, nev, chk = solop.find_resonances_plain_verified(CFG["k_min"], CFG["k_max"], CFG["npoints"],
+                                                                     CFG["c_o"], CFG["c_i"], tol=CFG["tol"])
         last_grid[0] = grid[:, 0].copy()
-        if roots.size:
-            # verification: sigma' changes sign across [root - tol, root + tol]; both
-            # ends of every root in one batched evaluation
-            d1 = solop.sweep_sigma(np.concatenate([roots - CFG["tol"], roots + CFG["tol"]]), CFG["c_o"], CFG["c_i"],
-                                   d=1)[:, 1]
-            lo, hi = d1[:roots.size], d1[roots.size:]
-            ver = int(np.sum((lo <= 0.0) & (hi >= 0.0)))
-        else:
-            ver = 0
+        ver = int(np.sum((chk[:, 0] <= 0.0) & (chk[:, 1] >= 0.0)))
         return ver, roots, nev
 
     for _ in range(max(3, args.warmup)):
@@ -907,7 +901,7 @@ def run_gpu(args):
         e2e_ms += e0.elapsed_time(e1)
         e2e_v += v
         del s2, d2
-    d2h = int(roots.nbytes + CFG["npoints"] * 3 * 8 + 2 * roots.size * 3 * 8)   # roots, grid, verification
+    d2h = int(roots.nbytes + CFG["npoints"] * 3 * 8 + 2 * roots.size * 8)   # roots, grid, the roots' checks
 
     # roofline of the dominant kernel (panel-pair assembly, FP64 CUDA-core bound):
     # algorithmic work of the timed launches by derivative order and point kind, on one

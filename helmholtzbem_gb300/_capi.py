@@ -33,7 +33,7 @@ EXPORTS = [
     "hbem_mlp_create", "hbem_mlp_destroy", "hbem_mlp_num_params", "hbem_mlp_get_params", "hbem_mlp_set_params",
     "hbem_mlp_forward", "hbem_mlp_gradients", "hbem_mlp_train_step", "hbem_bf16_gemm_device",
     "hbem_refine_brackets", "hbem_sweep_sigma_multi", "hbem_find_resonances_plain_multi", "hbem_refine_brackets_multi",
-    "hbem_find_resonances_plain", "hbem_rtsafe", "hbem_zbrent", "hbem_brent_min",
+    "hbem_find_resonances_plain", "hbem_find_resonances_plain_verified", "hbem_rtsafe", "hbem_zbrent", "hbem_brent_min",
     "hbem_brent_rc_create", "hbem_brent_rc_step", "hbem_brent_rc_destroy", "hbem_brent_guess", "hbem_brent_gsl",
     "hbem_brent_gsl_with_values",
 ]
@@ -151,6 +151,7 @@ def load(path=LIB_PATH):
         "hbem_lu_factor_batch_device_f32": (_i, [_i, _i, _vp, ctypes.c_longlong, _vp, _ip]),
         "hbem_lu_solve_batch_device": (_i, [_i, _i, _i, _vp, ctypes.c_longlong, _vp, _i, _vp, ctypes.c_longlong]),
         "hbem_find_resonances_plain": (_i, [_vp, _d, _d, _i, _d, _d, _d, _dp, _i, _ip, _dp, _ip]),
+        "hbem_find_resonances_plain_verified": (_i, [_vp, _d, _d, _i, _d, _d, _d, _dp, _i, _ip, _dp, _ip, _dp]),
         "hbem_rtsafe": (_d, [FN, FN_BOTH, _vp, _d, _d, _d, _ip, _up]),
         "hbem_zbrent": (_d, [FN, _vp, _d, _d, _d, _ip, _up]),
         "hbem_brent_min": (_d, [FN, _vp, _d, _d, _d]),

@@ -165,6 +165,20 @@ class SolutionsOperator:
                                            int(max_shift), dptr(out), max_roots, ctypes.byref(nr), ctypes.byref(ne)))
         return out[:min(nr.value, max_roots)].copy(), ne.value
 
+    def find_resonances_plain_verified(self, k_min, k_max, npoints, c_o, c_i, tol=1e-8, max_roots=4096):
+        """The plain search with every root checked: (roots, grid, evaluations, check),
+        check[i] = sigma' at roots[i] - tol and roots[i] + tol; a root is verified when
+        check[i, 0] <= 0 <= check[i, 1]."""
+        roots = np.zeros(max_roots)
+        grid = np.zeros((npoints, 3))
+        chk = np.zeros((max_roots, 2))
+        nr, ne = ctypes.c_int(), ctypes.c_int()
+        check(C.lib().hbem_find_resonances_plain_verified(self._h, float(k_min), float(k_max), int(npoints),
+                                                          float(c_o), float(c_i), float(tol), dptr(roots), max_roots,
+                                                          ctypes.byref(nr), dptr(grid), ctypes.byref(ne), dptr(chk)))
+        m = min(nr.value, max_roots)
+        return roots[:m].copy(), grid, ne.value, chk[:m].copy()
+
     def find_resonances_plain(self, k_min, k_max, npoints, c_o, c_i, tol=1e-8, max_roots=4096):
         roots = np.zeros(max_roots)
         grid = np.zeros((npoints, 3))

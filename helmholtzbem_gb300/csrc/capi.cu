@@ -430,7 +430,7 @@ struct EvalLane {
     DBuf jobs, loc, T, out, status, slots;
     double* h_out = nullptr;   // pinned, 3 x kLaneMaxPts
     int* h_status = nullptr;   // pinned, kLaneMaxPts
-    int npts = 0;
+    int npts = 0, d = 2;
     double k[8];
     ~EvalLane() {
         for (DBuf* x : {&jobs, &loc, &T, &out, &status, &slots}) x->release();
@@ -1584,7 +1584,7 @@ int vpool_ensure(hbem_solop s, int npool) {
     return HBEM_OK;
 }
 
-// Lanes: asynchronous sigma, sigma', sigma'' (d = 2) of up to kLaneMaxPts wavenumbers
+// Lanes: asynchronous sigma and its first d derivatives (d = 1 or 2) of up to kLaneMaxPts wavenumbers
 // through the one-CTA dense kernel with warm starts from the operator's pool (slots as
 // sweep_sigma_warm).  lane_launch enqueues the assembly, the dense kernel and the copy
 // of the results on the lane's own stream and returns; lane_wait tells whether the
@@ -1592,8 +1592,8 @@ int vpool_ensure(hbem_solop s, int npool) {
 // with the FP64-polished kernel, synchronously, any matrix the fast kernel could not
 // finish.  The dense kernel must take the operator's order (plain_speculate_ok).
 int lane_launch(hbem_solop s, int lane, const double* k_host, int npts, double c_o, double c_i, const int* wslot,
-                const int* oslot, int npool) {
-    if (!s || lane < 0 || lane >= 64 || npts < 1 || npts > kLaneMaxPts)
+                const int* oslot, int npool, unsigned d) {
+    if (!s || lane < 0 || lane >= 64 || npts < 1 || npts > kLaneMaxPts || d > 2)
         return fail(HBEM_ERR_INVALID, "lane_launch: bad argument");
     hbem_builder b = s->b;
     HB_CK(cudaSetDevice(b->device));
@@ -1618,11 +1618,12 @@ int lane_launch(hbem_solop s, int lane, const double* k_host, int npts, double c
     std::copy(wslot, wslot + npts, slots.begin());
     std::copy(oslot, oslot + npts, slots.begin() + npts);
     HB_CK(upload(L.slots, slots, L.st));
-    HB_CK(L.T.ensure((size_t)npts * 3 * mat * sizeof(cplx)));
+    L.d = (int)d;
+    HB_CK(L.T.ensure((size_t)npts * (d + 1) * mat * sizeof(cplx)));
     HB_CK(L.out.ensure(3 * kLaneMaxPts * sizeof(double)));
     HB_CK(L.status.ensure(kLaneMaxPts * sizeof(int)));
-    if (int r = gen_T_batch_ws(s, k_host, nullptr, npts, c_o, c_i, 2, L.T.as<cplx>(), L.jobs, L.loc, L.st)) return r;
-    HB_CK(launch_svd_fast(n, npts, 2, L.T.as<cplx>(), 3LL * (long long)mat, (long long)mat, L.out.as<double>(),
+    if (int r = gen_T_batch_ws(s, k_host, nullptr, npts, c_o, c_i, d, L.T.as<cplx>(), L.jobs, L.loc, L.st)) return r;
+    HB_CK(launch_svd_fast(n, npts, (int)d, L.T.as<cplx>(), (long long)(d + 1) * (long long)mat, (long long)mat, L.out.as<double>(),
                           L.status.as<int>(), L.st, s->d_vpool.as<cplxf>(), L.slots.as<int>(), L.slots.as<int>() + npts,
                           nullptr));
     g_launches += 1;
@@ -1654,7 +1655,7 @@ int lane_results(hbem_solop s, int lane, double c_o, double c_i, double* out_hos
     }
     const int save = t_svd_polished_only;
     t_svd_polished_only = 1;
-    const int r = hbem_sweep_sigma(s, L.k, L.npts, c_o, c_i, 2, out_host);
+    const int r = hbem_sweep_sigma(s, L.k, L.npts, c_o, c_i, (unsigned)L.d, out_host);
     t_svd_polished_only = save;
     return r;
 }

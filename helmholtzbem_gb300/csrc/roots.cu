@@ -25,7 +25,7 @@ int plain_speculate_ok(hbem_solop s);
 int plain_warm_start_ok();
 int plain_async_ok();
 int lane_launch(hbem_solop s, int lane, const double* k_host, int npts, double c_o, double c_i, const int* wslot,
-                const int* oslot, int npool);
+                const int* oslot, int npool, unsigned d);
 int lane_wait(hbem_solop s, int lane, int block, int* finished);
 int lane_results(hbem_solop s, int lane, double c_o, double c_i, double* out_host);
 int sweep_sigma_warm(hbem_solop s, const double* k_host, int nk, double c_o, double c_i, unsigned d,
@@ -503,17 +503,24 @@ int newton_rounds(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i,
 constexpr int kSpecDeep = 2;
 constexpr int kLanes = 32;
 
+// With vder given, a candidate that converges has sigma' at root - vtol and root + vtol
+// (the check that sigma' changes sign there) evaluated on two more lanes while other
+// candidates still iterate: vder[2c], vder[2c + 1] (NaN for candidates without a root).
+constexpr int kMain = 0, kSpec = 1, kVerify = 2;
+
 int newton_async(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, int& evals,
-                 const std::vector<int>& first_warm, int slot_base) {
+                 const std::vector<int>& first_warm, int slot_base, std::vector<double>* vder = nullptr,
+                 double vtol = 0.) {
     const size_t nc = nt.size();
     if (nc == 0) return HBEM_OK;
     std::vector<std::vector<std::array<double, 3>>> cache(nc);
     std::vector<std::vector<double>> pend(nc);   // speculative points in flight
     std::vector<int> cur(first_warm);
     const int npool = slot_base + 2 * (int)nc;
-    struct Flight { int cand; double x; bool spec; int rslot; };
+    struct Flight { int cand; double x; int kind; int side; int rslot; };
     std::vector<Flight> fl(kLanes);
-    std::vector<int> busy(kLanes, 0), in_flight(nc, 0);
+    std::vector<int> busy(kLanes, 0), in_flight(nc, 0), vsent(nc, 0);
+    if (vder) vder->assign(2 * nc, NAN);
     std::vector<int> order;   // lanes in launch order (the oldest is waited for first)
     auto unfinished = [&]() {
         size_t u = 0;
@@ -537,9 +544,11 @@ int newton_async(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, 
         const Flight F = fl[lane];
         busy[lane] = 0;
         if (int r = hbem::lane_results(s, lane, c_o, c_i, out)) return r;
-        if (F.spec) {
+        if (F.kind == kSpec) {
             cache[F.cand].push_back({F.x, out[1], out[2]});
             pend[F.cand].erase(std::find(pend[F.cand].begin(), pend[F.cand].end(), F.x));
+        } else if (F.kind == kVerify) {
+            (*vder)[2 * (size_t)F.cand + F.side] = out[1];
         } else {
             nt[F.cand].feed(out[1], out[2]);
             ++evals;
@@ -547,9 +556,9 @@ int newton_async(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, 
         }
         return HBEM_OK;
     };
-    auto launch = [&](int lane, size_t c, double x, bool spec, int ws, int os) -> int {
-        if (int r = hbem::lane_launch(s, lane, &x, 1, c_o, c_i, &ws, &os, npool)) return r;
-        fl[lane] = Flight{(int)c, x, spec, ws};
+    auto launch = [&](int lane, size_t c, double x, int kind, int side, int ws, int os) -> int {
+        if (int r = hbem::lane_launch(s, lane, &x, 1, c_o, c_i, &ws, &os, npool, kind == kVerify ? 1u : 2u)) return r;
+        fl[lane] = Flight{(int)c, x, kind, side, ws};
         busy[lane] = 1;
         order.push_back(lane);
         return HBEM_OK;
@@ -567,14 +576,32 @@ int newton_async(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, 
                 nt[c].feed((*it)[1], (*it)[2]);
                 ++evals;
             }
-            if (nt[c].done || has(pend[c], nt[c].rts)) return 0;   // done, or its point is on its way
+            if (nt[c].done) {
+                // a converged candidate: its root's sign-change check beside the others' iterations
+                if (vder && !vsent[c] && nt[c].found && nt[c].rts == nt[c].rts) {
+                    const int l0 = free_lane();
+                    if (l0 < 0) return -1;
+                    if (int r = launch(l0, c, nt[c].rts - vtol, kVerify, 0, cur[c], -1)) return r;
+                    const int l1 = free_lane();
+                    if (l1 < 0) { vsent[c] = 1; return -1; }
+                    if (int r = launch(l1, c, nt[c].rts + vtol, kVerify, 1, cur[c], -1)) return r;
+                    vsent[c] = 2;
+                } else if (vder && vsent[c] == 1) {
+                    const int l1 = free_lane();
+                    if (l1 < 0) return -1;
+                    if (int r = launch(l1, c, nt[c].rts + vtol, kVerify, 1, cur[c], -1)) return r;
+                    vsent[c] = 2;
+                }
+                return 0;
+            }
+            if (has(pend[c], nt[c].rts)) return 0;   // its point is on its way
             const int own0 = slot_base + 2 * (int)c, wslot = cur[c], oslot = cur[c] == own0 ? own0 + 1 : own0;
             // the slot this point's V set goes to must not be read by a speculative point
             // still in flight (it started from the slot before)
             bool waited = false;
             for (size_t q = 0; q < order.size(); ++q) {
                 const int l = order[q];
-                if (fl[l].cand == (int)c && fl[l].spec && fl[l].rslot == oslot) {
+                if (fl[l].cand == (int)c && fl[l].kind == kSpec && fl[l].rslot == oslot) {
                     int fin = 0;
                     if (int r = hbem::lane_wait(s, l, 1, &fin)) return r;
                     if (int r = finish(l)) return r;
@@ -585,7 +612,7 @@ int newton_async(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, 
             if (waited) continue;   // look again: the wait may have brought this point's value
             const int lane = free_lane();
             if (lane < 0) return -1;
-            if (int r = launch(lane, c, nt[c].rts, false, wslot, oslot)) return r;
+            if (int r = launch(lane, c, nt[c].rts, kMain, 0, wslot, oslot)) return r;
             in_flight[c] = 1;
             cur[c] = oslot;
             // speculative bisection points (the same rule as the lock-step rounds, plus the
@@ -611,7 +638,7 @@ int newton_async(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, 
                     if (x == nt[c].rts || cached(c, x) || has(pend[c], x)) continue;
                     const int l2 = free_lane();
                     if (l2 < 0) break;
-                    if (int r = launch(l2, c, x, true, wslot, -1)) return r;
+                    if (int r = launch(l2, c, x, kSpec, 0, wslot, -1)) return r;
                     pend[c].push_back(x);
                 }
             }
@@ -817,6 +844,13 @@ double hbem_brent_min(hbem_fn f, void* user, double a, double b, double tol) {
 int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npoints, double c_o, double c_i,
                                double tol, double* roots_host, int max_roots, int* nroots, double* grid_host,
                                int* n_evals) {
+    return hbem_find_resonances_plain_verified(s, k_min, k_max, npoints, c_o, c_i, tol, roots_host, max_roots, nroots,
+                                               grid_host, n_evals, nullptr);
+}
+
+int hbem_find_resonances_plain_verified(hbem_solop s, double k_min, double k_max, int npoints, double c_o, double c_i,
+                                        double tol, double* roots_host, int max_roots, int* nroots, double* grid_host,
+                                        int* n_evals, double* check_host) {
     if (!s || npoints < 3 || !(k_max > k_min) || !nroots) return HBEM_ERR_INVALID;
     std::vector<double> ks(npoints), g(3 * (size_t)npoints);
     const double h = (k_max - k_min) / (npoints - 1);
@@ -901,8 +935,12 @@ int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npo
     for (size_t c = 0; c < cands.size(); ++c) nt[c].start(cands[c].a, cands[c].a + 2 * h, cands[c].guess, tol);
     // lock-step Newton rounds: one batched sigma', sigma'' evaluation per round (with
     // speculative bisection points where the dense sigma is latency bound)
+    std::vector<double> vder;
+    bool checked = false;
     if (hbem::plain_speculate_ok(s) && warm && hbem::plain_async_ok()) {
-        if (int r = newton_async(s, nt, c_o, c_i, evals, first_warm, npoints)) return r;
+        if (int r = newton_async(s, nt, c_o, c_i, evals, first_warm, npoints, check_host ? &vder : nullptr, tol))
+            return r;
+        checked = check_host != nullptr;
     } else if (hbem::plain_speculate_ok(s)) {
         if (int r = newton_rounds(s, nt, c_o, c_i, evals, warm ? &first_warm : nullptr, npoints)) return r;
     } else {
@@ -919,11 +957,29 @@ int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npo
         }
     }
     int cnt = 0;
-    for (auto& x : nt)
+    std::vector<double> vpts;   // sign-change check points evaluated after the search
+    for (size_t c = 0; c < nt.size(); ++c) {
+        const Newton& x = nt[c];
         if (x.done && x.found && x.rts == x.rts) {
             if (roots_host && cnt < max_roots) roots_host[cnt] = x.rts;
+            if (check_host && cnt < max_roots) {
+                if (checked) {
+                    check_host[2 * cnt] = vder[2 * c];
+                    check_host[2 * cnt + 1] = vder[2 * c + 1];
+                } else {
+                    vpts.push_back(x.rts - tol);
+                    vpts.push_back(x.rts + tol);
+                }
+            }
             ++cnt;
         }
+    }
+    if (check_host && !checked && !vpts.empty()) {
+        // sigma' at both ends of every root in one batch after the search
+        std::vector<double> o(3 * vpts.size());
+        if (int r = hbem_sweep_sigma(s, vpts.data(), (int)vpts.size(), c_o, c_i, 1, o.data())) return r;
+        for (size_t e = 0; e < vpts.size(); ++e) check_host[e] = o[3 * e + 1];
+    }
     *nroots = cnt;
     if (n_evals) *n_evals = evals;
     return HBEM_OK;

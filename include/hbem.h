@@ -456,6 +456,16 @@ int hbem_sweep_sigma(hbem_solop s, const double* k_host, int nk, double c_o, dou
 int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npoints, double c_o, double c_i,
                                double tol, double* roots_host, int max_roots, int* nroots, double* grid_host,
                                int* n_evals);
+/* The same search with every root checked (no counterpart in the reference, whose
+ * drivers report rtsafe's result as is): check_host[2i], check_host[2i + 1] receive
+ * sigma' at roots_host[i] - tol and roots_host[i] + tol, so that a root is verified
+ * when check_host[2i] <= 0 <= check_host[2i + 1].  With the Newton candidates on
+ * their own streams (option "plain_async") a candidate's two points are evaluated as
+ * soon as it converges, beside the other candidates' iterations; otherwise in one
+ * batch after the search.                                                          */
+int hbem_find_resonances_plain_verified(hbem_solop s, double k_min, double k_max, int npoints, double c_o, double c_i,
+                                        double tol, double* roots_host, int max_roots, int* nroots, double* grid_host,
+                                        int* n_evals, double* check_host);
 
 /* Adaptive resonance search (examples/find_resonances.cpp:128-250 with the sampler
  * opt_subdiv, source/utilities/find_roots.cpp:1615-1726): batches of batch_size

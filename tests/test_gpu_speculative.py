@@ -103,3 +103,26 @@ def test_async_newton_matches_lock_step():
     assert np.max(np.abs(np.sort(a_roots) - np.sort(l_roots))) <= 1e-10
     assert a_nev == l_nev
     np.testing.assert_array_equal(a_grid[:, 0], l_grid[:, 0])
+
+
+def test_verified_search_checks_every_root():
+    """hbem_find_resonances_plain_verified: the roots of the plain search, each with
+    sigma' at root -/+ tol -- evaluated beside the other candidates' iterations with
+    the candidates on their own streams, in one batch after the search in lock step --
+    equal to the separate evaluation to the dense kernel's accuracy, with the sign
+    change of every root of the bench workload."""
+    from helmholtzbem_gb300 import _capi as C, api, geometry
+    so = api.SolutionsOperator(api.BuilderData(geometry.circle(0.25, 50), order=11))
+    plain, _, nev = so.find_resonances_plain(0.5, 10.0, 200, 1.0, 23.4, tol=1e-8)
+    for async_on in (1, 0):
+        C.check(C.lib().hbem_set_option(b"plain_async", async_on))
+        try:
+            roots, _, nev2, chk = so.find_resonances_plain_verified(0.5, 10.0, 200, 1.0, 23.4, tol=1e-8)
+        finally:
+            C.check(C.lib().hbem_set_option(b"plain_async", 1))
+        assert roots.size == plain.size == 10 and nev2 == nev
+        assert np.max(np.abs(np.sort(roots) - np.sort(plain))) <= 1e-10
+        assert np.all(chk[:, 0] <= 0) and np.all(chk[:, 1] >= 0)
+        sep = np.stack([so.sweep_sigma(roots - 1e-8, 1.0, 23.4, d=1)[:, 1],
+                        so.sweep_sigma(roots + 1e-8, 1.0, 23.4, d=1)[:, 1]], axis=1)
+        assert np.max(np.abs(chk - sep)) <= 1e-10   # sigma' there is ~1e-7 .. 1e-6

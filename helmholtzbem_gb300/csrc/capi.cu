@@ -138,6 +138,8 @@ int g_arnoldi_maxit = 1000;   // block iterations of hbem_arnoldi_sv_batch*
 int g_plain_speculate = 1;    // plain search: speculative bisection points in small Newton rounds
 int g_plain_warm_start = 1;   // plain search: dense-kernel Jacobi warm-started from nearby V sets
 int g_plain_async = 1;        // plain search: Newton candidates advance independently on their own streams
+int g_plain_spec_async = 8;   // ... speculating while at most this many candidates are unfinished
+int g_plain_spec_deep = 2;    // ... two bisection levels deep while at most this many are
 int g_singular_table = 1;     // singular pairs read their k-independent point data from a table
 const size_t kSingularTableMax = (size_t)256 << 20;
 
@@ -582,6 +584,16 @@ int hbem_set_option(const char* name, int value) {
         g_plain_async = value ? 1 : 0;
         return HBEM_OK;
     }
+    if (k == "plain_spec_async") {
+        if (value < 0) return fail(HBEM_ERR_INVALID, "set_option: plain_spec_async must be >= 0");
+        g_plain_spec_async = value;
+        return HBEM_OK;
+    }
+    if (k == "plain_spec_deep") {
+        if (value < 0) return fail(HBEM_ERR_INVALID, "set_option: plain_spec_deep must be >= 0");
+        g_plain_spec_deep = value;
+        return HBEM_OK;
+    }
     if (k == "arnoldi_maxit") {
         if (value < 1) return fail(HBEM_ERR_INVALID, "set_option: arnoldi_maxit must be >= 1");
         g_arnoldi_maxit = value;
@@ -603,6 +615,8 @@ int hbem_get_option(const char* name, int* value) {
     else if (k == "plain_warm_start") *value = g_plain_warm_start;
     else if (k == "plain_speculate") *value = g_plain_speculate;
     else if (k == "plain_async") *value = g_plain_async;
+    else if (k == "plain_spec_async") *value = g_plain_spec_async;
+    else if (k == "plain_spec_deep") *value = g_plain_spec_deep;
     else if (k == "arnoldi_maxit") *value = g_arnoldi_maxit;
     else return fail(HBEM_ERR_INVALID, "get_option: unknown option " + k);
     return HBEM_OK;
@@ -1563,6 +1577,10 @@ int plain_speculate_ok(hbem_solop s) {
 int plain_warm_start_ok() { return g_plain_warm_start; }
 
 int plain_async_ok() { return g_plain_async; }
+int plain_spec_limits(int* deep) {
+    *deep = g_plain_spec_deep;
+    return g_plain_spec_async;
+}
 
 // The FP32 V-set pool of the dense kernel's warm starts holds at least npool slots
 // (contents kept when it grows).  Synchronous.

@@ -24,6 +24,7 @@ namespace hbem {
 int plain_speculate_ok(hbem_solop s);
 int plain_warm_start_ok();
 int plain_async_ok();
+int plain_spec_limits(int* deep);
 int lane_launch(hbem_solop s, int lane, const double* k_host, int npts, double c_o, double c_i, const int* wslot,
                 const int* oslot, int npool, unsigned d);
 int lane_wait(hbem_solop s, int lane, int block, int* finished);
@@ -493,9 +494,9 @@ int newton_rounds(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i,
 // ("lanes", one point each), so one candidate's assembly runs while another's
 // one-CTA dense sigma does, instead of all candidates waiting for the slowest of
 // each lock-step round.  Speculative bisection points go to lanes of their own, so
-// they do not delay the Newton point they accompany; while at most kSpecDeep
-// candidates are unfinished (the GPU otherwise idle) the points of the bisection
-// after next are speculated too.  Each candidate takes the same Newton and
+// they do not delay the Newton point they accompany; a candidate speculates while at
+// most "plain_spec_async" candidates (option, default 8) are unfinished, and while at
+// most "plain_spec_deep" (default 2) are, the points of the bisection after next too.  Each candidate takes the same Newton and
 // bisection steps as in newton_rounds, with the same warm-start slots for its Newton
 // points; a speculative point may be evaluated from another warm start than in lock
 // step, so its values agree to the dense kernel's accuracy (sigma to ~1e-15, sigma'
@@ -517,6 +518,8 @@ int newton_async(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, 
     std::vector<std::vector<double>> pend(nc);   // speculative points in flight
     std::vector<int> cur(first_warm);
     const int npool = slot_base + 2 * (int)nc;
+    int spec_deep = kSpecDeep;
+    const int spec_lim = hbem::plain_spec_limits(&spec_deep);
     struct Flight { int cand; double x; int kind; int side; int rslot; };
     std::vector<Flight> fl(kLanes);
     std::vector<int> busy(kLanes, 0), in_flight(nc, 0), vsent(nc, 0);
@@ -618,10 +621,10 @@ int newton_async(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, 
             // speculative bisection points (the same rule as the lock-step rounds, plus the
             // next level when few candidates are left)
             const size_t left = unfinished();
-            if (left <= (size_t)kSpecRound && (nt[c].first || nt[c].bisected)) {
+            if (left <= (size_t)spec_lim && (nt[c].first || nt[c].bisected)) {
                 double pts[6];
                 int np = nt[c].bisect_next(pts);
-                if (left <= (size_t)kSpecDeep && !nt[c].first) {
+                if (left <= (size_t)spec_deep && !nt[c].first) {
                     const int n1 = np;
                     for (int j = 0; j < n1; ++j) {
                         // the state after a bisection to pts[j] (feed()'s operations)

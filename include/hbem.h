@@ -81,6 +81,9 @@ int hbem_set_device(int device);
  *   candidate's next point is assembled and evaluated on its own stream as soon as its
  *   previous one is done, instead of all candidates advancing in lock-step rounds;
  *   the same Newton steps either way.
+ *   "plain_spec_async" (default 8), "plain_spec_deep" (default 2): with "plain_async",
+ *   a candidate speculates bisection points while at most plain_spec_async candidates
+ *   are unfinished, two bisection levels deep while at most plain_spec_deep are.
  *   "plain_warm_start" (default 1): in the plain search, the dense kernel's FP32
  *   Jacobi at a bracket end or Newton point starts from the right singular vectors
  *   of the nearest wavenumber already evaluated (same stopping rule, fewer sweeps). */

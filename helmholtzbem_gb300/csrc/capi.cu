@@ -426,23 +426,24 @@ struct hbem_builder_s {
 // One in-flight evaluation of sigma, sigma', sigma'' at a few wavenumbers on its own
 // stream (the plain search's Newton phase runs several at once): job table, pair
 // blocks, T / T' / T'', results, and pinned host copies of the results.
+constexpr int kLaneMaxPts = 64;
 struct EvalLane {
     cudaStream_t st = nullptr;
-    cudaEvent_t done = nullptr;
+    cudaEvent_t done = nullptr, asm_done = nullptr;   // all work / the assembly part finished
     DBuf jobs, loc, T, out, status, slots;
     double* h_out = nullptr;   // pinned, 3 x kLaneMaxPts
     int* h_status = nullptr;   // pinned, kLaneMaxPts
-    int npts = 0, d = 2;
-    double k[8];
+    int npts = 0, d = 2, mode = 0;   // mode 0: sigma (+ derivatives), 1: grid chunk, 2: bracket ends
+    double k[kLaneMaxPts];
     ~EvalLane() {
         for (DBuf* x : {&jobs, &loc, &T, &out, &status, &slots}) x->release();
         if (h_out) cudaFreeHost(h_out);
         if (h_status) cudaFreeHost(h_status);
         if (done) cudaEventDestroy(done);
+        if (asm_done) cudaEventDestroy(asm_done);
         if (st) cudaStreamDestroy(st);
     }
 };
-constexpr int kLaneMaxPts = 8;
 
 // Lanes are kept per host thread and device (a search runs on one thread at a time),
 // so that operators created one after another reuse their streams, events and pinned
@@ -1609,21 +1610,29 @@ int vpool_ensure(hbem_solop s, int npool) {
 // lane has finished (blocking when `block`); lane_results gives its values, redoing
 // with the FP64-polished kernel, synchronously, any matrix the fast kernel could not
 // finish.  The dense kernel must take the operator's order (plain_speculate_ok).
+// the lanes up to `lane` of this thread's pool for `device` exist
+static int lane_make(int device, int lane) {
+    std::vector<EvalLane*>& lanes = lane_pool(device).lanes;
+    while ((int)lanes.size() <= lane) {
+        EvalLane* l = new EvalLane();
+        lanes.push_back(l);
+        HB_CK(cudaStreamCreateWithFlags(&l->st, cudaStreamNonBlocking));
+        HB_CK(cudaEventCreateWithFlags(&l->done, cudaEventDisableTiming));
+        HB_CK(cudaEventCreateWithFlags(&l->asm_done, cudaEventDisableTiming));
+        HB_CK(cudaMallocHost(&l->h_out, 3 * kLaneMaxPts * sizeof(double)));
+        HB_CK(cudaMallocHost(&l->h_status, kLaneMaxPts * sizeof(int)));
+    }
+    return HBEM_OK;
+}
+
 int lane_launch(hbem_solop s, int lane, const double* k_host, int npts, double c_o, double c_i, const int* wslot,
                 const int* oslot, int npool, unsigned d) {
     if (!s || lane < 0 || lane >= 64 || npts < 1 || npts > kLaneMaxPts || d > 2)
         return fail(HBEM_ERR_INVALID, "lane_launch: bad argument");
     hbem_builder b = s->b;
     HB_CK(cudaSetDevice(b->device));
+    if (int r = lane_make(b->device, lane)) return r;
     std::vector<EvalLane*>& lanes = lane_pool(b->device).lanes;
-    while ((int)lanes.size() <= lane) {
-        EvalLane* l = new EvalLane();
-        lanes.push_back(l);
-        HB_CK(cudaStreamCreateWithFlags(&l->st, cudaStreamNonBlocking));
-        HB_CK(cudaEventCreateWithFlags(&l->done, cudaEventDisableTiming));
-        HB_CK(cudaMallocHost(&l->h_out, 3 * kLaneMaxPts * sizeof(double)));
-        HB_CK(cudaMallocHost(&l->h_status, kLaneMaxPts * sizeof(int)));
-    }
     for (int i = 0; i < npts; ++i)
         if (wslot[i] >= npool || oslot[i] >= npool) return fail(HBEM_ERR_INVALID, "lane_launch: slot outside the pool");
     if (int r = vpool_ensure(s, npool)) return r;
@@ -1631,6 +1640,7 @@ int lane_launch(hbem_solop s, int lane, const double* k_host, int npts, double c
     const int n = 2 * b->n;
     const size_t mat = (size_t)n * n;
     L.npts = npts;
+    L.mode = 0;
     std::copy(k_host, k_host + npts, L.k);
     std::vector<int> slots(2 * (size_t)npts);
     std::copy(wslot, wslot + npts, slots.begin());
@@ -1660,6 +1670,110 @@ int lane_wait(hbem_solop s, int lane, int block, int* finished) {
     }
     HB_CK(e);
     *finished = 1;
+    return HBEM_OK;
+}
+
+// The plain search with its grid in chunks: the pool for `npool` V sets and room for
+// the singular vectors of sigma_min at `npoints` grid points.  Synchronous.
+int pipeline_setup(hbem_solop s, int npoints, int npool) {
+    hbem_builder b = s->b;
+    HB_CK(cudaSetDevice(b->device));
+    if (int r = vpool_ensure(s, npool)) return r;
+    const int n = 2 * b->n;
+    s->uv_count = 0;
+    HB_CK(s->d_uv.ensure((size_t)npoints * 2 * n * sizeof(cplx)));
+    return HBEM_OK;
+}
+
+// the grid points have kept singular vectors (for sigma1_from_kept) up to npoints
+void pipeline_keep_uv(hbem_solop s, int npoints) { s->uv_count = npoints; }
+
+// Grid chunk on a lane: sigma at npts grid points first .. first + npts - 1 (cold
+// start), the V sets to pool slots first + q and the singular vectors of sigma_min to
+// rows first + q of the kept vectors.  The chunk's assembly starts after lane `after`'s
+// assembly (-1: none), so chunks assemble in order while a chunk's dense kernel
+// overlaps the next chunk's assembly.  lane_results then gives sigma (no redo:
+// *all_fast = 0 when the fast kernel could not finish a matrix).
+int lane_launch_grid(hbem_solop s, int lane, const double* k_host, int npts, int first, double c_o, double c_i,
+                     int npool, int after) {
+    if (!s || lane < 0 || lane >= 64 || npts < 1 || npts > kLaneMaxPts || first < 0 || first + npts > npool)
+        return fail(HBEM_ERR_INVALID, "lane_launch_grid: bad argument");
+    hbem_builder b = s->b;
+    HB_CK(cudaSetDevice(b->device));
+    if (int r = lane_make(b->device, std::max(lane, after))) return r;
+    std::vector<EvalLane*>& lanes = lane_pool(b->device).lanes;
+    EvalLane& L = *lanes[lane];
+    const int n = 2 * b->n;
+    const size_t mat = (size_t)n * n;
+    L.npts = npts;
+    L.mode = 1;
+    L.d = 0;
+    std::copy(k_host, k_host + npts, L.k);
+    std::vector<int> slots(2 * (size_t)npts);
+    for (int q = 0; q < npts; ++q) {
+        slots[q] = -1;
+        slots[npts + q] = first + q;
+    }
+    HB_CK(upload(L.slots, slots, L.st));
+    HB_CK(L.T.ensure((size_t)npts * mat * sizeof(cplx)));
+    HB_CK(L.out.ensure(3 * kLaneMaxPts * sizeof(double)));
+    HB_CK(L.status.ensure(kLaneMaxPts * sizeof(int)));
+    if (after >= 0) HB_CK(cudaStreamWaitEvent(L.st, lanes[after]->asm_done, 0));
+    if (int r = gen_T_batch_ws(s, k_host, nullptr, npts, c_o, c_i, 0, L.T.as<cplx>(), L.jobs, L.loc, L.st)) return r;
+    HB_CK(cudaEventRecord(L.asm_done, L.st));
+    HB_CK(launch_svd_fast(n, npts, 0, L.T.as<cplx>(), (long long)mat, (long long)mat, L.out.as<double>(),
+                          L.status.as<int>(), L.st, s->d_vpool.as<cplxf>(), L.slots.as<int>(), L.slots.as<int>() + npts,
+                          s->d_uv.as<cplx>() + 2LL * n * first));
+    g_launches += 1;
+    HB_CK(cudaMemcpyAsync(L.h_out, L.out.p, 3 * (size_t)npts * sizeof(double), cudaMemcpyDeviceToHost, L.st));
+    HB_CK(cudaMemcpyAsync(L.h_status, L.status.p, (size_t)npts * sizeof(int), cudaMemcpyDeviceToHost, L.st));
+    HB_CK(cudaEventRecord(L.done, L.st));
+    return HBEM_OK;
+}
+
+// Bracket ends on a lane: sigma' at two grid points from the grid's kept singular
+// vectors (sigma1_from_kept for one candidate): T' assembled at k_host[0..1], then
+// Re u^H T' v with (u, v) of grid points gidx[0..1].  lane_results gives sigma' in
+// out_host[3q + 1].
+int lane_launch_ends(hbem_solop s, int lane, const double* k_host, const int* gidx, double c_o, double c_i) {
+    if (!s || lane < 0 || lane >= 64 || !k_host || !gidx) return fail(HBEM_ERR_INVALID, "lane_launch_ends: bad argument");
+    hbem_builder b = s->b;
+    HB_CK(cudaSetDevice(b->device));
+    if (int r = lane_make(b->device, lane)) return r;
+    EvalLane& L = *lane_pool(b->device).lanes[lane];
+    const int n = 2 * b->n;
+    const size_t mat = (size_t)n * n;
+    L.npts = 2;
+    L.mode = 2;
+    L.d = 1;
+    std::copy(k_host, k_host + 2, L.k);
+    std::vector<int> id(gidx, gidx + 2);
+    HB_CK(upload(L.slots, id, L.st));
+    HB_CK(L.T.ensure(2 * 2 * mat * sizeof(cplx)));
+    HB_CK(L.out.ensure(3 * kLaneMaxPts * sizeof(double)));
+    if (int r = gen_T_batch_ws(s, k_host, nullptr, 2, c_o, c_i, 1, L.T.as<cplx>(), L.jobs, L.loc, L.st)) return r;
+    HB_CK(launch_sigma1_uv(n, 2, L.T.as<cplx>() + mat, (long long)(2 * mat), s->d_uv.as<cplx>(), L.slots.as<int>(),
+                           L.out.as<double>(), L.st));
+    g_launches += 1;
+    HB_CK(cudaMemcpyAsync(L.h_out, L.out.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, L.st));
+    HB_CK(cudaEventRecord(L.done, L.st));
+    return HBEM_OK;
+}
+
+int lane_results_grid(hbem_solop s, int lane, double* sigma_host, int* all_fast) {
+    EvalLane& L = *lane_pool(s->b->device).lanes[lane];
+    *all_fast = 1;
+    for (int i = 0; i < L.npts; ++i) {
+        sigma_host[i] = L.h_out[3 * i];
+        if (L.h_status[i] != 0) *all_fast = 0;
+    }
+    return HBEM_OK;
+}
+
+int lane_results_ends(hbem_solop s, int lane, double* d1_host) {
+    EvalLane& L = *lane_pool(s->b->device).lanes[lane];
+    d1_host[0] = L.h_out[0];
+    d1_host[1] = L.h_out[1];
     return HBEM_OK;
 }
 

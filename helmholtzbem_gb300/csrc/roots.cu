@@ -25,6 +25,13 @@ int plain_speculate_ok(hbem_solop s);
 int plain_warm_start_ok();
 int plain_async_ok();
 int plain_spec_limits(int* deep);
+int pipeline_setup(hbem_solop s, int npoints, int npool);
+void pipeline_keep_uv(hbem_solop s, int npoints);
+int lane_launch_grid(hbem_solop s, int lane, const double* k_host, int npts, int first, double c_o, double c_i,
+                     int npool, int after);
+int lane_launch_ends(hbem_solop s, int lane, const double* k_host, const int* gidx, double c_o, double c_i);
+int lane_results_grid(hbem_solop s, int lane, double* sigma_host, int* all_fast);
+int lane_results_ends(hbem_solop s, int lane, double* d1_host);
 int lane_launch(hbem_solop s, int lane, const double* k_host, int npts, double c_o, double c_i, const int* wslot,
                 const int* oslot, int npool, unsigned d);
 int lane_wait(hbem_solop s, int lane, int block, int* finished);
@@ -489,47 +496,71 @@ int newton_rounds(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i,
     return HBEM_OK;
 }
 
-// The same Newton phase with every candidate on its own: a candidate's next point is
-// enqueued as soon as its previous one is evaluated, on one of several streams
-// ("lanes", one point each), so one candidate's assembly runs while another's
-// one-CTA dense sigma does, instead of all candidates waiting for the slowest of
-// each lock-step round.  Speculative bisection points go to lanes of their own, so
-// they do not delay the Newton point they accompany; a candidate speculates while at
-// most "plain_spec_async" candidates (option, default 8) are unfinished, and while at
-// most "plain_spec_deep" (default 2) are, the points of the bisection after next too.  Each candidate takes the same Newton and
-// bisection steps as in newton_rounds, with the same warm-start slots for its Newton
-// points; a speculative point may be evaluated from another warm start than in lock
-// step, so its values agree to the dense kernel's accuracy (sigma to ~1e-15, sigma'
-// and sigma'' to ~1e-12 relative), not bit for bit.
+// The plain search as one pipeline on several streams ("lanes"): the grid in chunks
+// whose assemblies run in order while each chunk's dense sigma overlaps the next
+// chunk's assembly; a candidate's bracket ends (sigma' from the grid's kept singular
+// vectors) as soon as the grid around it is known; its Newton steps as soon as its
+// previous point is evaluated, one point per lane; and, when asked for, its root's
+// sign-change check as soon as it converges.  The FP64 assembly of one candidate runs
+// while another's one-CTA dense sigma does, and the grid's tail overlaps the first
+// candidates' work.  Values are those of the lock-step search: the same grid
+// (chunks of at least the size below, so that their general pairs take the same
+// layout as one batch), the same bracket ends, and the same Newton and bisection
+// steps with the same warm-start slots for the Newton points.  Speculative bisection
+// points run on lanes of their own once the grid is complete and at most
+// "plain_spec_async" candidates are unfinished (option; "plain_spec_deep": the
+// bisection after next too); one may be evaluated from another warm start than in
+// lock step, so its values agree to the dense kernel's accuracy (sigma' and sigma''
+// to ~1e-12 relative), not bit for bit.
 constexpr int kSpecDeep = 2;
 constexpr int kLanes = 32;
+constexpr int kMain = 0, kSpec = 1, kVerify = 2, kGrid = 3, kEnds = 4;
 
-// With vder given, a candidate that converges has sigma' at root - vtol and root + vtol
-// (the check that sigma' changes sign there) evaluated on two more lanes while other
-// candidates still iterate: vder[2c], vder[2c + 1] (NaN for candidates without a root).
-constexpr int kMain = 0, kSpec = 1, kVerify = 2;
-
-int newton_async(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, int& evals,
-                 const std::vector<int>& first_warm, int slot_base, std::vector<double>* vder = nullptr,
-                 double vtol = 0.) {
-    const size_t nc = nt.size();
-    if (nc == 0) return HBEM_OK;
-    std::vector<std::vector<std::array<double, 3>>> cache(nc);
-    std::vector<std::vector<double>> pend(nc);   // speculative points in flight
-    std::vector<int> cur(first_warm);
-    const int npool = slot_base + 2 * (int)nc;
+// Returns HBEM_ERR_UNSUPPORTED, with nothing left in flight, when the grid cannot be
+// chunked without changing its values or a grid matrix needs the polished kernel:
+// the caller then runs the lock-step search.
+int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, double c_o, double c_i, double tol,
+                    std::vector<double>& g, std::vector<Newton>& nt, std::vector<double>* vder, int& evals) {
+    const int npoints = (int)ks.size();
+    int npan = 0;
+    if (int r = hbem_solop_info(s, &npan)) return r;
+    // chunk size: general pairs x jobs of a chunk on the same side of the thread / warp
+    // layout threshold (152 x 16 x 32) as the whole grid's
+    const long long nlow = (long long)npan * (npan - 1) / 2;
+    const long long thr = 152LL * 16 * 32;
+    const bool whole_thread = nlow * 2 * npoints >= thr;
+    int csize = std::max(32, (npoints + 4) / 5);
+    if (whole_thread) csize = std::max<long long>(csize, (thr + 2 * nlow - 1) / (2 * nlow));
+    if (csize > 64) return HBEM_ERR_UNSUPPORTED;
+    const int nch = (npoints + csize - 1) / csize;
+    if (nch + 2 > kLanes) return HBEM_ERR_UNSUPPORTED;
+    if (!whole_thread) {
+        // every chunk, the smallest last one included, must stay below the threshold too
+        // (it does: fewer jobs than the whole grid)
+    } else if (nlow * 2 * (npoints - (nch - 1) * csize) < thr) {
+        return HBEM_ERR_UNSUPPORTED;
+    }
+    const int npool = 2 * npoints;   // grid slots, then two per candidate (at most npoints / 2)
+    if (int r = hbem::pipeline_setup(s, npoints, npool)) return r;
     int spec_deep = kSpecDeep;
     const int spec_lim = hbem::plain_spec_limits(&spec_deep);
+
     struct Flight { int cand; double x; int kind; int side; int rslot; };
     std::vector<Flight> fl(kLanes);
-    std::vector<int> busy(kLanes, 0), in_flight(nc, 0), vsent(nc, 0);
-    if (vder) vder->assign(2 * nc, NAN);
-    std::vector<int> order;   // lanes in launch order (the oldest is waited for first)
-    auto unfinished = [&]() {
-        size_t u = 0;
-        for (size_t c = 0; c < nc; ++c) u += !nt[c].done;
-        return u;
-    };
+    std::vector<int> busy(kLanes, 0);
+    std::vector<int> order;   // lanes in launch order
+    // candidates (grid index, state 0: bracket ends to launch, 1: ends in flight,
+    // 2: rejected, 3: Newton)
+    std::vector<int> cgrid, cstate, cur, in_flight, vsent;
+    std::vector<std::vector<std::array<double, 3>>> cache;
+    std::vector<std::vector<double>> pend;
+    nt.clear();
+    std::vector<double> vd;   // sigma' at root -/+ tol per candidate (NaN: none)
+    std::vector<int> chunk_done(nch, 0);
+    int known = 0, scanned = 0, chunks_in_order = 0;
+    bool grid_ok = true;
+    for (int i = 0; i < npoints; ++i) g[3 * i] = g[3 * i + 1] = g[3 * i + 2] = NAN;
+
     auto has = [](const std::vector<double>& v, double x) { return std::find(v.begin(), v.end(), x) != v.end(); };
     auto cached = [&](size_t c, double x) {
         return std::find_if(cache[c].begin(), cache[c].end(),
@@ -540,18 +571,70 @@ int newton_async(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, 
             if (!busy[l]) return l;
         return -1;
     };
-    double out[3];
-    // take the results of a finished lane
+    auto unfinished = [&]() {
+        if (chunks_in_order < nch) return (size_t)1 << 30;   // candidates still to come
+        size_t u = 0;
+        for (size_t c = 0; c < cstate.size(); ++c) u += cstate[c] < 2 || (cstate[c] == 3 && !nt[c].done);
+        return u;
+    };
+    double out[3 * 64];
     auto finish = [&](int lane) -> int {
         order.erase(std::find(order.begin(), order.end(), lane));
         const Flight F = fl[lane];
         busy[lane] = 0;
+        if (F.kind == kGrid) {
+            int fast = 1;
+            if (int r = hbem::lane_results_grid(s, lane, out, &fast)) return r;
+            const int first = F.cand * csize, cnt = std::min(csize, npoints - first);
+            for (int q = 0; q < cnt; ++q) g[3 * (first + q)] = out[q];
+            if (!fast) grid_ok = false;
+            chunk_done[F.cand] = 1;
+            while (chunks_in_order < nch && chunk_done[chunks_in_order]) ++chunks_in_order;
+            known = std::min(npoints, chunks_in_order * csize);
+            // 3-point local minima (roots_newton_polygon_rsvd.cpp:185-194) of the known grid
+            for (; scanned + 2 < known; ++scanned) {
+                const int i = scanned;
+                const double L = g[3 * i], C = g[3 * (i + 1)], R = g[3 * (i + 2)];
+                if (L - C > 0. && R - C > 0.) {
+                    cgrid.push_back(i);
+                    cstate.push_back(0);
+                    cur.push_back(-1);
+                    in_flight.push_back(0);
+                    vsent.push_back(0);
+                    cache.emplace_back();
+                    pend.emplace_back();
+                    nt.emplace_back();
+                    vd.push_back(NAN);
+                    vd.push_back(NAN);
+                }
+            }
+            return HBEM_OK;
+        }
+        if (F.kind == kEnds) {
+            double d[2];
+            if (int r = hbem::lane_results_ends(s, lane, d)) return r;
+            const size_t c = (size_t)F.cand;
+            const int i = cgrid[c];
+            g[3 * i + 1] = d[0];
+            g[3 * (i + 2) + 1] = d[1];
+            evals += 2;
+            // validation sigma'(left) < 0 < sigma'(right), quartic guess (:209-245)
+            if (!(d[0] < 0. && d[1] > 0.)) {
+                cstate[c] = 2;
+                return HBEM_OK;
+            }
+            const double guess = quartic_guess(ks[i], h, g[3 * i], g[3 * (i + 1)], g[3 * (i + 2)], d[0], d[1], tol);
+            cur[c] = guess - ks[i] < 0.5 * h ? i : (guess - ks[i] < 1.5 * h ? i + 1 : i + 2);
+            nt[c].start(ks[i], ks[i] + 2 * h, guess, tol);
+            cstate[c] = 3;
+            return HBEM_OK;
+        }
         if (int r = hbem::lane_results(s, lane, c_o, c_i, out)) return r;
         if (F.kind == kSpec) {
             cache[F.cand].push_back({F.x, out[1], out[2]});
             pend[F.cand].erase(std::find(pend[F.cand].begin(), pend[F.cand].end(), F.x));
         } else if (F.kind == kVerify) {
-            (*vder)[2 * (size_t)F.cand + F.side] = out[1];
+            vd[2 * (size_t)F.cand + F.side] = out[1];
         } else {
             nt[F.cand].feed(out[1], out[2]);
             ++evals;
@@ -566,10 +649,24 @@ int newton_async(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, 
         order.push_back(lane);
         return HBEM_OK;
     };
-    // launch candidate c's next point (and its speculative points) if it needs one:
-    // returns -1 when no lane is free, a status code on error, 0 otherwise
+    // candidate c's next launch, if it needs one: -1 when no lane is free, a status code
+    // on error, 0 otherwise
     auto advance = [&](size_t c) -> int {
         for (;;) {
+            if (cstate[c] == 2 || cstate[c] == 1) return 0;
+            if (cstate[c] == 0) {
+                const int lane = free_lane();
+                if (lane < 0) return -1;
+                const int i = cgrid[c];
+                const double e2[2] = {ks[i], ks[i + 2]};
+                const int gi[2] = {i, i + 2};
+                if (int r = hbem::lane_launch_ends(s, lane, e2, gi, c_o, c_i)) return r;
+                fl[lane] = Flight{(int)c, 0., kEnds, 0, -1};
+                busy[lane] = 1;
+                order.push_back(lane);
+                cstate[c] = 1;
+                return 0;
+            }
             if (in_flight[c]) return 0;
             // values already at hand (speculative points evaluated earlier)
             while (!nt[c].done) {
@@ -580,25 +677,19 @@ int newton_async(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, 
                 ++evals;
             }
             if (nt[c].done) {
-                // a converged candidate: its root's sign-change check beside the others' iterations
-                if (vder && !vsent[c] && nt[c].found && nt[c].rts == nt[c].rts) {
-                    const int l0 = free_lane();
-                    if (l0 < 0) return -1;
-                    if (int r = launch(l0, c, nt[c].rts - vtol, kVerify, 0, cur[c], -1)) return r;
-                    const int l1 = free_lane();
-                    if (l1 < 0) { vsent[c] = 1; return -1; }
-                    if (int r = launch(l1, c, nt[c].rts + vtol, kVerify, 1, cur[c], -1)) return r;
-                    vsent[c] = 2;
-                } else if (vder && vsent[c] == 1) {
-                    const int l1 = free_lane();
-                    if (l1 < 0) return -1;
-                    if (int r = launch(l1, c, nt[c].rts + vtol, kVerify, 1, cur[c], -1)) return r;
-                    vsent[c] = 2;
+                // a converged candidate: its root's sign-change check beside the others' work
+                if (vder && vsent[c] < 2 && nt[c].found && nt[c].rts == nt[c].rts) {
+                    const int l = free_lane();
+                    if (l < 0) return -1;
+                    const int side = vsent[c];
+                    if (int r = launch(l, c, nt[c].rts + (side ? tol : -tol), kVerify, side, cur[c], -1)) return r;
+                    ++vsent[c];
+                    continue;
                 }
                 return 0;
             }
             if (has(pend[c], nt[c].rts)) return 0;   // its point is on its way
-            const int own0 = slot_base + 2 * (int)c, wslot = cur[c], oslot = cur[c] == own0 ? own0 + 1 : own0;
+            const int own0 = npoints + 2 * (int)c, wslot = cur[c], oslot = cur[c] == own0 ? own0 + 1 : own0;
             // the slot this point's V set goes to must not be read by a speculative point
             // still in flight (it started from the slot before)
             bool waited = false;
@@ -618,8 +709,7 @@ int newton_async(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, 
             if (int r = launch(lane, c, nt[c].rts, kMain, 0, wslot, oslot)) return r;
             in_flight[c] = 1;
             cur[c] = oslot;
-            // speculative bisection points (the same rule as the lock-step rounds, plus the
-            // next level when few candidates are left)
+            // speculative bisection points (plus the next level when few candidates are left)
             const size_t left = unfinished();
             if (left <= (size_t)spec_lim && (nt[c].first || nt[c].bisected)) {
                 double pts[6];
@@ -648,11 +738,35 @@ int newton_async(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, 
             return 0;
         }
     };
+    auto drain = [&]() {
+        for (int l : order) {
+            int fin = 0;
+            hbem::lane_wait(s, l, 1, &fin);
+        }
+    };
+    // the grid chunks, assembled in order on lanes 0 .. nch - 1
+    for (int j = 0; j < nch; ++j) {
+        const int first = j * csize, cnt = std::min(csize, npoints - first);
+        if (int r = hbem::lane_launch_grid(s, j, ks.data() + first, cnt, first, c_o, c_i, npool, j - 1)) {
+            drain();
+            return r;
+        }
+        fl[j] = Flight{j, 0., kGrid, 0, -1};
+        busy[j] = 1;
+        order.push_back(j);
+    }
     for (;;) {
-        for (size_t c = 0; c < nc; ++c) {
+        if (!grid_ok) {   // a grid matrix the fast kernel could not finish: the lock-step path redoes it
+            drain();
+            return HBEM_ERR_UNSUPPORTED;
+        }
+        for (size_t c = 0; c < cstate.size(); ++c) {
             const int r = advance(c);
             if (r == -1) break;
-            if (r) return r;
+            if (r) {
+                drain();
+                return r;
+            }
         }
         if (order.empty()) break;
         // the first finished lane, else wait for the oldest
@@ -667,8 +781,13 @@ int newton_async(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i, 
             pick = order[0];
             if (int r = hbem::lane_wait(s, pick, 1, &fin)) return r;
         }
-        if (int r = finish(pick)) return r;
+        if (int r = finish(pick)) {
+            drain();
+            return r;
+        }
     }
+    if (vder) *vder = vd;
+    hbem::pipeline_keep_uv(s, npoints);
     return HBEM_OK;
 }
 
@@ -859,106 +978,120 @@ int hbem_find_resonances_plain_verified(hbem_solop s, double k_min, double k_max
     const double h = (k_max - k_min) / (npoints - 1);
     for (int i = 0; i < npoints; ++i) ks[i] = k_min + i * h;
     int evals = npoints;
-    // where sigma comes from the one-CTA dense kernel, every evaluation leaves its FP32
-    // V set in a pool slot (grid point i: slot i) and later evaluations near it start
-    // their Jacobi sweeps there
-    bool warm = hbem::plain_speculate_ok(s) && hbem::plain_warm_start_ok();
-    std::vector<int> wslot, oslot;
-    // sigma on the grid (randomized_svd::sv / direct::sv at roots_newton_polygon_rsvd.cpp:172-177)
-    if (warm) {
-        wslot.assign(npoints, -1);
-        oslot.resize(npoints);
-        for (int i = 0; i < npoints; ++i) oslot[i] = i;
-        const int r = hbem::sweep_sigma_warm(s, ks.data(), npoints, c_o, c_i, 0, wslot.data(), oslot.data(), npoints,
-                                             g.data(), 1);
-        if (r == HBEM_ERR_UNSUPPORTED) warm = false;
-        else if (r) return r;
-    }
-    if (!warm)
-        if (int r = hbem_sweep_sigma(s, ks.data(), npoints, c_o, c_i, 0, g.data())) return r;
-    for (int i = 0; i < npoints; ++i) g[3 * i + 1] = g[3 * i + 2] = NAN;
-    // 3-point local minima (:185-194)
-    std::vector<int> cidx;
-    for (int i = 0; i + 2 < npoints; ++i) {
-        const double L = g[3 * i], C = g[3 * (i + 1)], R = g[3 * (i + 2)];
-        if (L - C > 0. && R - C > 0.) cidx.push_back(i);
-    }
-    // sigma' at both bracket ends of every candidate in one batch (sv_der, :204-208)
-    std::vector<double> ends(2 * cidx.size()), der(6 * cidx.size());
-    for (size_t c = 0; c < cidx.size(); ++c) {
-        ends[2 * c] = ks[cidx[c]];
-        ends[2 * c + 1] = ks[cidx[c] + 2];
-    }
-    if (!ends.empty()) {
-        // the bracket ends are grid points: sigma' from the grid's own singular vectors
-        // (sv_der there would redo the same SVD), else their V sets start the Jacobi
-        std::vector<int> gidx(ends.size());
-        for (size_t c = 0; c < cidx.size(); ++c) {
-            gidx[2 * c] = cidx[c];
-            gidx[2 * c + 1] = cidx[c] + 2;
-        }
-        std::vector<double> d1v(ends.size());
-        const int kept = warm ? hbem::sigma1_from_kept(s, ends.data(), gidx.data(), (int)ends.size(), c_o, c_i,
-                                                       d1v.data())
-                              : (int)HBEM_ERR_UNSUPPORTED;
-        if (kept == HBEM_OK) {
-            for (size_t e = 0; e < ends.size(); ++e) {
-                der[3 * e] = g[3 * (size_t)gidx[e]];
-                der[3 * e + 1] = d1v[e];
-                der[3 * e + 2] = 0.;
-            }
-        } else if (kept != HBEM_ERR_UNSUPPORTED) {
-            return kept;
-        } else if (warm) {
-            oslot.assign(ends.size(), -1);
-            if (int r = hbem::sweep_sigma_warm(s, ends.data(), (int)ends.size(), c_o, c_i, 1, gidx.data(),
-                                               oslot.data(), npoints, der.data()))
-                return r;
-        } else if (int r = hbem_sweep_sigma(s, ends.data(), (int)ends.size(), c_o, c_i, 1, der.data())) {
-            return r;
-        }
-        evals += (int)ends.size();
-    }
-    // validation sigma'(left) < 0 < sigma'(right), quartic Hermite model + Brent (:209-245)
-    struct Cand { double a, guess; };
-    std::vector<Cand> cands;
-    std::vector<int> first_warm;   // grid point beside the guess (its V set starts the first Newton point)
-    for (size_t c = 0; c < cidx.size(); ++c) {
-        const int i = cidx[c];
-        const double d1 = der[3 * (2 * c) + 1], d2 = der[3 * (2 * c + 1) + 1];
-        g[3 * i + 1] = d1;
-        g[3 * (i + 2) + 1] = d2;
-        if (!(d1 < 0. && d2 > 0.)) continue;
-        cands.push_back(Cand{ks[i], quartic_guess(ks[i], h, g[3 * i], g[3 * (i + 1)], g[3 * (i + 2)], d1, d2, tol)});
-        const double gs = cands.back().guess;
-        first_warm.push_back(gs - ks[i] < 0.5 * h ? i : (gs - ks[i] < 1.5 * h ? i + 1 : i + 2));
-    }
-    if (grid_host) std::copy(g.begin(), g.end(), grid_host);
-    std::vector<Newton> nt(cands.size());
-    for (size_t c = 0; c < cands.size(); ++c) nt[c].start(cands[c].a, cands[c].a + 2 * h, cands[c].guess, tol);
-    // lock-step Newton rounds: one batched sigma', sigma'' evaluation per round (with
-    // speculative bisection points where the dense sigma is latency bound)
+    std::vector<Newton> nt;
     std::vector<double> vder;
-    bool checked = false;
-    if (hbem::plain_speculate_ok(s) && warm && hbem::plain_async_ok()) {
-        if (int r = newton_async(s, nt, c_o, c_i, evals, first_warm, npoints, check_host ? &vder : nullptr, tol))
+    bool checked = false, piped = false;
+    // the whole search as one pipeline of streams (option "plain_async") where the
+    // one-CTA dense kernel takes the order; else grid, bracket ends and lock-step
+    // Newton rounds one after another
+    if (hbem::plain_speculate_ok(s) && hbem::plain_warm_start_ok() && hbem::plain_async_ok()) {
+        const int r = plain_pipelined(s, ks, h, c_o, c_i, tol, g, nt, check_host ? &vder : nullptr, evals);
+        if (r == HBEM_OK) {
+            piped = true;
+            checked = check_host != nullptr;
+        } else if (r != HBEM_ERR_UNSUPPORTED) {
             return r;
-        checked = check_host != nullptr;
-    } else if (hbem::plain_speculate_ok(s)) {
-        if (int r = newton_rounds(s, nt, c_o, c_i, evals, warm ? &first_warm : nullptr, npoints)) return r;
-    } else {
-        for (int round = 0; round < kMaxIt; ++round) {
-            std::vector<double> xs;
-            std::vector<size_t> who;
-            for (size_t c = 0; c < nt.size(); ++c)
-                if (!nt[c].done) { xs.push_back(nt[c].rts); who.push_back(c); }
-            if (xs.empty()) break;
-            std::vector<double> out(3 * xs.size());
-            if (int r = hbem_sweep_sigma(s, xs.data(), (int)xs.size(), c_o, c_i, 2, out.data())) return r;
-            evals += (int)xs.size();
-            for (size_t q = 0; q < who.size(); ++q) nt[who[q]].feed(out[3 * q + 1], out[3 * q + 2]);
+        } else {
+            evals = npoints;
         }
     }
+    if (!piped) {
+        // where sigma comes from the one-CTA dense kernel, every evaluation leaves its FP32
+        // V set in a pool slot (grid point i: slot i) and later evaluations near it start
+        // their Jacobi sweeps there
+        bool warm = hbem::plain_speculate_ok(s) && hbem::plain_warm_start_ok();
+        std::vector<int> wslot, oslot;
+        // sigma on the grid (randomized_svd::sv / direct::sv at roots_newton_polygon_rsvd.cpp:172-177)
+        if (warm) {
+            wslot.assign(npoints, -1);
+            oslot.resize(npoints);
+            for (int i = 0; i < npoints; ++i) oslot[i] = i;
+            const int r = hbem::sweep_sigma_warm(s, ks.data(), npoints, c_o, c_i, 0, wslot.data(), oslot.data(),
+                                                 npoints, g.data(), 1);
+            if (r == HBEM_ERR_UNSUPPORTED) warm = false;
+            else if (r) return r;
+        }
+        if (!warm)
+            if (int r = hbem_sweep_sigma(s, ks.data(), npoints, c_o, c_i, 0, g.data())) return r;
+        for (int i = 0; i < npoints; ++i) g[3 * i + 1] = g[3 * i + 2] = NAN;
+        // 3-point local minima (:185-194)
+        std::vector<int> cidx;
+        for (int i = 0; i + 2 < npoints; ++i) {
+            const double L = g[3 * i], C = g[3 * (i + 1)], R = g[3 * (i + 2)];
+            if (L - C > 0. && R - C > 0.) cidx.push_back(i);
+        }
+        // sigma' at both bracket ends of every candidate in one batch (sv_der, :204-208)
+        std::vector<double> ends(2 * cidx.size()), der(6 * cidx.size());
+        for (size_t c = 0; c < cidx.size(); ++c) {
+            ends[2 * c] = ks[cidx[c]];
+            ends[2 * c + 1] = ks[cidx[c] + 2];
+        }
+        if (!ends.empty()) {
+            // the bracket ends are grid points: sigma' from the grid's own singular vectors
+            // (sv_der there would redo the same SVD), else their V sets start the Jacobi
+            std::vector<int> gidx(ends.size());
+            for (size_t c = 0; c < cidx.size(); ++c) {
+                gidx[2 * c] = cidx[c];
+                gidx[2 * c + 1] = cidx[c] + 2;
+            }
+            std::vector<double> d1v(ends.size());
+            const int kept = warm ? hbem::sigma1_from_kept(s, ends.data(), gidx.data(), (int)ends.size(), c_o, c_i,
+                                                           d1v.data())
+                                  : (int)HBEM_ERR_UNSUPPORTED;
+            if (kept == HBEM_OK) {
+                for (size_t e = 0; e < ends.size(); ++e) {
+                    der[3 * e] = g[3 * (size_t)gidx[e]];
+                    der[3 * e + 1] = d1v[e];
+                    der[3 * e + 2] = 0.;
+                }
+            } else if (kept != HBEM_ERR_UNSUPPORTED) {
+                return kept;
+            } else if (warm) {
+                oslot.assign(ends.size(), -1);
+                if (int r = hbem::sweep_sigma_warm(s, ends.data(), (int)ends.size(), c_o, c_i, 1, gidx.data(),
+                                                   oslot.data(), npoints, der.data()))
+                    return r;
+            } else if (int r = hbem_sweep_sigma(s, ends.data(), (int)ends.size(), c_o, c_i, 1, der.data())) {
+                return r;
+            }
+            evals += (int)ends.size();
+        }
+        // validation sigma'(left) < 0 < sigma'(right), quartic Hermite model + Brent (:209-245)
+        struct Cand { double a, guess; };
+        std::vector<Cand> cands;
+        std::vector<int> first_warm;   // grid point beside the guess (its V set starts the first Newton point)
+        for (size_t c = 0; c < cidx.size(); ++c) {
+            const int i = cidx[c];
+            const double d1 = der[3 * (2 * c) + 1], d2 = der[3 * (2 * c + 1) + 1];
+            g[3 * i + 1] = d1;
+            g[3 * (i + 2) + 1] = d2;
+            if (!(d1 < 0. && d2 > 0.)) continue;
+            cands.push_back(
+                Cand{ks[i], quartic_guess(ks[i], h, g[3 * i], g[3 * (i + 1)], g[3 * (i + 2)], d1, d2, tol)});
+            const double gs = cands.back().guess;
+            first_warm.push_back(gs - ks[i] < 0.5 * h ? i : (gs - ks[i] < 1.5 * h ? i + 1 : i + 2));
+        }
+        nt.assign(cands.size(), Newton());
+        for (size_t c = 0; c < cands.size(); ++c) nt[c].start(cands[c].a, cands[c].a + 2 * h, cands[c].guess, tol);
+        // lock-step Newton rounds: one batched sigma', sigma'' evaluation per round (with
+        // speculative bisection points where the dense sigma is latency bound)
+        if (hbem::plain_speculate_ok(s)) {
+            if (int r = newton_rounds(s, nt, c_o, c_i, evals, warm ? &first_warm : nullptr, npoints)) return r;
+        } else {
+            for (int round = 0; round < kMaxIt; ++round) {
+                std::vector<double> xs;
+                std::vector<size_t> who;
+                for (size_t c = 0; c < nt.size(); ++c)
+                    if (!nt[c].done) { xs.push_back(nt[c].rts); who.push_back(c); }
+                if (xs.empty()) break;
+                std::vector<double> out(3 * xs.size());
+                if (int r = hbem_sweep_sigma(s, xs.data(), (int)xs.size(), c_o, c_i, 2, out.data())) return r;
+                evals += (int)xs.size();
+                for (size_t q = 0; q < who.size(); ++q) nt[who[q]].feed(out[3 * q + 1], out[3 * q + 2]);
+            }
+        }
+    }   // !piped
+    if (grid_host) std::copy(g.begin(), g.end(), grid_host);
     int cnt = 0;
     std::vector<double> vpts;   // sign-change check points evaluated after the search
     for (size_t c = 0; c < nt.size(); ++c) {

@@ -77,10 +77,10 @@ int hbem_set_device(int device);
  *   derivative order, real k, panel kind) and uses the fastest from then on; the
  *   choices persist in the file the environment variable HBEM_TUNE_CACHE names, if
  *   any.  Results of different layouts agree to rounding (~1e-15).
- *   "plain_async" (default 1): in the plain search (with warm starts), each Newton
- *   candidate's next point is assembled and evaluated on its own stream as soon as its
- *   previous one is done, instead of all candidates advancing in lock-step rounds;
- *   the same Newton steps either way.
+ *   "plain_async" (default 1): the plain search (with warm starts) as one pipeline of
+ *   streams: grid chunks overlapping, each candidate's bracket ends and Newton points
+ *   as soon as their inputs are known, instead of one batch per phase and lock-step
+ *   Newton rounds; the same Newton steps either way.
  *   "plain_spec_async" (default 8), "plain_spec_deep" (default 2): with "plain_async",
  *   a candidate speculates bisection points while at most plain_spec_async candidates
  *   are unfinished, two bisection levels deep while at most plain_spec_deep are.
@@ -443,19 +443,24 @@ int hbem_sweep_sigma(hbem_solop s, const double* k_host, int nk, double c_o, dou
 /* Plain resonance search on [k_min, k_max] with npoints grid points
  * (examples/roots_newton_polygon_rsvd.cpp:172-265 with the dense sigma of
  * examples/roots_newton_circle.cpp): sigma on the grid; 3-point local minima;
- * sigma' at both bracket ends (one batch), validation sigma'(left) < 0 <
- * sigma'(right); quartic Hermite model minimised by Brent; rtsafe on sigma' with
- * sigma'' to tolerance tol, all candidates' Newton steps in one batch per round.
+ * sigma' at both bracket ends, validation sigma'(left) < 0 < sigma'(right); quartic
+ * Hermite model minimised by Brent; rtsafe on sigma' with sigma'' to tolerance tol.
+ * Where the one-CTA dense kernel takes the order, the search runs as one pipeline
+ * on several streams (option "plain_async", default 1): the grid in chunks whose
+ * dense sigma overlaps the next chunk's assembly, each candidate's bracket ends as
+ * soon as the grid around it is known, and its Newton points one after another,
+ * independently of the other candidates; otherwise each phase is one batch, the
+ * Newton steps of all candidates in one batch per round.  The values are the same.
  * roots_host receives up to max_roots roots, *nroots their count; grid_host
  * (npoints x 3, may be NULL) sigma at every grid point and sigma' at the bracket
  * ends (NaN where not evaluated); *n_evals the number of T(k) evaluated.
- * Where the one-CTA dense sigma kernel takes the order (2N <= 100), in Newton
- * rounds with at most 8 active candidates a candidate at its first point or just
- * after a bisection step also has the one or two points a further bisection step of
- * rtsafe could move to evaluated (option "plain_speculate", default 1); when that
- * step follows, its point needs no round of its own.  Every candidate is fed the
- * same values as without speculation, so the roots are the same; *n_evals counts
- * the evaluations the search used (unused speculative points excluded).          */
+ * Where the one-CTA dense sigma kernel takes the order (2N <= 100), while few
+ * candidates are left a candidate at its first point or just after a bisection step
+ * also has the points a further bisection step of rtsafe could move to evaluated
+ * (option "plain_speculate", default 1); when that step follows, its point needs no
+ * evaluation of its own.  Every candidate takes the same steps as without
+ * speculation, so the roots are the same; *n_evals counts the evaluations the
+ * search used (unused speculative points excluded).                               */
 int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npoints, double c_o, double c_i,
                                double tol, double* roots_host, int max_roots, int* nroots, double* grid_host,
                                int* n_evals);

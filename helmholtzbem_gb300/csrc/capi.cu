@@ -138,7 +138,7 @@ int g_arnoldi_maxit = 1000;   // block iterations of hbem_arnoldi_sv_batch*
 int g_plain_speculate = 1;    // plain search: speculative bisection points in small Newton rounds
 int g_plain_warm_start = 1;   // plain search: dense-kernel Jacobi warm-started from nearby V sets
 int g_plain_async = 1;        // plain search: Newton candidates advance independently on their own streams
-int g_plain_spec_async = 8;   // ... speculating while at most this many candidates are unfinished
+int g_plain_spec_async = 2;   // ... speculating while at most this many candidates are unfinished
 int g_plain_spec_deep = 2;    // ... two bisection levels deep while at most this many are
 int g_singular_table = 1;     // singular pairs read their k-independent point data from a table
 const size_t kSingularTableMax = (size_t)256 << 20;
@@ -1610,13 +1610,20 @@ int vpool_ensure(hbem_solop s, int npool) {
 // lane has finished (blocking when `block`); lane_results gives its values, redoing
 // with the FP64-polished kernel, synchronously, any matrix the fast kernel could not
 // finish.  The dense kernel must take the operator's order (plain_speculate_ok).
-// the lanes up to `lane` of this thread's pool for `device` exist
+// the lanes up to `lane` of this thread's pool for `device` exist.  Lanes below
+// kBulkLanes (the plain search's grid chunks) run at the lowest stream priority, the
+// others (its candidates' evaluations, on the critical path) at the highest, so that a
+// candidate's blocks are scheduled ahead of the grid's remaining ones.
+constexpr int kBulkLanes = 8;
 static int lane_make(int device, int lane) {
     std::vector<EvalLane*>& lanes = lane_pool(device).lanes;
+    int least = 0, greatest = 0;
+    HB_CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
     while ((int)lanes.size() <= lane) {
         EvalLane* l = new EvalLane();
         lanes.push_back(l);
-        HB_CK(cudaStreamCreateWithFlags(&l->st, cudaStreamNonBlocking));
+        const int prio = (int)lanes.size() - 1 < kBulkLanes ? least : greatest;
+        HB_CK(cudaStreamCreateWithPriority(&l->st, cudaStreamNonBlocking, prio));
         HB_CK(cudaEventCreateWithFlags(&l->done, cudaEventDisableTiming));
         HB_CK(cudaEventCreateWithFlags(&l->asm_done, cudaEventDisableTiming));
         HB_CK(cudaMallocHost(&l->h_out, 3 * kLaneMaxPts * sizeof(double)));

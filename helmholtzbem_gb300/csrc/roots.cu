@@ -16,6 +16,7 @@
 #include <cmath>
 #include <limits>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/hbem.h"
@@ -506,14 +507,17 @@ int newton_rounds(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i,
 // candidates' work.  Values are those of the lock-step search: the same grid
 // (chunks of at least the size below, so that their general pairs take the same
 // layout as one batch), the same bracket ends, and the same Newton and bisection
-// steps with the same warm-start slots for the Newton points.  Speculative bisection
-// points run on lanes of their own once the grid is complete and at most
-// "plain_spec_async" candidates are unfinished (option; "plain_spec_deep": the
-// bisection after next too); one may be evaluated from another warm start than in
-// lock step, so its values agree to the dense kernel's accuracy (sigma' and sigma''
-// to ~1e-12 relative), not bit for bit.
+// steps with the same warm-start slots for the Newton points.  Grid chunks run on
+// low-priority streams, candidates' evaluations on high-priority ones, and the host
+// polls every lane so that each result is taken as soon as it is there.  Speculative
+// bisection points run on lanes of their own once the grid is complete and at most
+// "plain_spec_async" candidates (option, default 2) are unfinished
+// ("plain_spec_deep": the bisection after next too); one may be evaluated from
+// another warm start than in lock step, so its values agree to the dense kernel's
+// accuracy (sigma' and sigma'' to ~1e-12 relative), not bit for bit.
 constexpr int kSpecDeep = 2;
-constexpr int kLanes = 32;
+constexpr int kLanes = 40;
+constexpr int kCandLane = 8;   // the first lane of candidates' evaluations (the grid's below)
 constexpr int kMain = 0, kSpec = 1, kVerify = 2, kGrid = 3, kEnds = 4;
 
 // Returns HBEM_ERR_UNSUPPORTED, with nothing left in flight, when the grid cannot be
@@ -533,7 +537,7 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
     if (whole_thread) csize = std::max<long long>(csize, (thr + 2 * nlow - 1) / (2 * nlow));
     if (csize > 64) return HBEM_ERR_UNSUPPORTED;
     const int nch = (npoints + csize - 1) / csize;
-    if (nch + 2 > kLanes) return HBEM_ERR_UNSUPPORTED;
+    if (nch > kCandLane) return HBEM_ERR_UNSUPPORTED;
     if (!whole_thread) {
         // every chunk, the smallest last one included, must stay below the threshold too
         // (it does: fewer jobs than the whole grid)
@@ -566,8 +570,10 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
         return std::find_if(cache[c].begin(), cache[c].end(),
                             [&](const std::array<double, 3>& e) { return e[0] == x; }) != cache[c].end();
     };
+    // candidates' evaluations on lanes kCandLane .. (high stream priority), grid chunks
+    // on lanes 0 .. nch - 1 (low priority)
     auto free_lane = [&]() {
-        for (int l = 0; l < kLanes; ++l)
+        for (int l = kCandLane; l < kLanes; ++l)
             if (!busy[l]) return l;
         return -1;
     };
@@ -769,17 +775,19 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
             }
         }
         if (order.empty()) break;
-        // the first finished lane, else wait for the oldest
+        // the first lane to finish, whichever it is: poll them all (blocking on one lane
+        // would hold up the results of lanes that finish before it)
         int pick = -1;
-        for (size_t q = 0; q < order.size() && pick < 0; ++q) {
-            int fin = 0;
-            if (int r = hbem::lane_wait(s, order[q], 0, &fin)) return r;
-            if (fin) pick = order[q];
-        }
-        if (pick < 0) {
-            int fin = 0;
-            pick = order[0];
-            if (int r = hbem::lane_wait(s, pick, 1, &fin)) return r;
+        for (long long spin = 0; pick < 0; ++spin) {
+            for (size_t q = 0; q < order.size() && pick < 0; ++q) {
+                int fin = 0;
+                if (int r = hbem::lane_wait(s, order[q], 0, &fin)) {
+                    drain();
+                    return r;
+                }
+                if (fin) pick = order[q];
+            }
+            if (pick < 0 && spin > 64) std::this_thread::yield();
         }
         if (int r = finish(pick)) {
             drain();

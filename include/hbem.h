@@ -81,7 +81,7 @@ int hbem_set_device(int device);
  *   streams: grid chunks overlapping, each candidate's bracket ends and Newton points
  *   as soon as their inputs are known, instead of one batch per phase and lock-step
  *   Newton rounds; the same Newton steps either way.
- *   "plain_spec_async" (default 8), "plain_spec_deep" (default 2): with "plain_async",
+ *   "plain_spec_async" (default 2), "plain_spec_deep" (default 2): with "plain_async",
  *   a candidate speculates bisection points while at most plain_spec_async candidates
  *   are unfinished, two bisection levels deep while at most plain_spec_deep are.
  *   "plain_warm_start" (default 1): in the plain search, the dense kernel's FP32

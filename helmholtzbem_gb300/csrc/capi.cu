@@ -60,6 +60,8 @@ void lu_set_cluster_panels(int on);
 void lu_set_tensor_cores(int on);
 void mlp_set_tensor_cores(int on);
 int lu_get_cluster_panels();
+void svd_set_pair_max(int m);
+int svd_get_pair_max();
 int lu_get_tensor_cores();
 int mlp_get_tensor_cores();
 cudaError_t launch_cgemm_f32(int m, int n, int k, const cplxf* A, long long lda, long long sa, const cplxf* B,
@@ -557,6 +559,11 @@ int hbem_set_option(const char* name, int value) {
         g_svd_fast = value ? 1 : 0;
         return HBEM_OK;
     }
+    if (k == "svd_pair_max") {
+        if (value < 0) return fail(HBEM_ERR_INVALID, "set_option: svd_pair_max must be >= 0");
+        svd_set_pair_max(value);
+        return HBEM_OK;
+    }
     if (k == "autotune") {
         g_autotune = value ? 1 : 0;
         return HBEM_OK;
@@ -609,6 +616,7 @@ int hbem_get_option(const char* name, int* value) {
     if (k == "lu_cluster_panels") *value = lu_get_cluster_panels();
     else if (k == "lu_tensor_cores") *value = lu_get_tensor_cores();
     else if (k == "svd_fast") *value = g_svd_fast.load();
+    else if (k == "svd_pair_max") *value = svd_get_pair_max();
     else if (k == "svd_fast_force_redo") *value = g_svd_force_redo.load();
     else if (k == "autotune") *value = g_autotune.load();
     else if (k == "mlp_tensor_cores") *value = mlp_get_tensor_cores();

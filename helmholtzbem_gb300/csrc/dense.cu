@@ -12,10 +12,16 @@
 // perturbation of W.  Partners numerically degenerate with sigma
 // (|sigma_j - sigma| <= 1e-9 sigma) are left out of the first sum: a
 // perturbation that keeps the degeneracy does not couple them.
+#include <atomic>
+
+#include <cooperative_groups.h>
+
 #include "hbem_device.cuh"
 #include "smem_linalg.cuh"
 
 namespace hbem {
+
+namespace cg = cooperative_groups;
 
 constexpr int kSvdThreads = 512;
 constexpr int kSvdMaxSweeps = 40;
@@ -451,6 +457,8 @@ cudaError_t launch_svd_mixed(int n, int nmat, int D, int which, const cplx* T, l
 constexpr int kFastKmax = 12;
 constexpr int kFastInvIter = 4;
 constexpr int kFastNeumannMax = 200;   // preconditioned CG iteration cap
+// launches of at most this many matrices run the paired (two-CTA cluster) form
+static std::atomic<int> g_svd_pair_max{16};
 
 struct SvdFastJob {
     int n, nmat, D;
@@ -587,10 +595,23 @@ static __device__ void rows_times(cplx* B, int n, int kb, const cplx* M) {
     __syncthreads();
 }
 
+// PAIR: a cluster of two CTAs per matrix (blocks 2m, 2m + 1), for launches of a few
+// matrices where the latency of one matrix matters.  CTA 0 runs stage 1 (FP32 Jacobi,
+// near block) while CTA 1 factors T in FP64; CTA 0 then copies the factors out of CTA
+// 1's shared memory and the two split the columns of the inverse iterations and of
+// Y = T X between them, exchanging columns through distributed shared memory; CTA 1
+// finishes alone.  Every column sees the single-CTA kernel's arithmetic in the same
+// order, so both forms give bit-identical results.
+template <bool PAIR>
 __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
     extern __shared__ double smraw[];
     char* sb = reinterpret_cast<char*>(smraw);
-    const int n = J.n, mat = blockIdx.x;
+    const int n = J.n, mat = PAIR ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
+    int rank = 0;   // PAIR: 0 = the Jacobi CTA, 1 = the LU CTA
+    if constexpr (PAIR) {
+        rank = (int)cg::this_cluster().block_rank();
+        cg::this_cluster().sync();   // both CTAs are running before either touches the other's memory
+    }
     const FastSmem L = fast_layout(n);
     cplx* T64 = reinterpret_cast<cplx*>(sb + L.r0);
     cpf* A32 = reinterpret_cast<cpf*>(sb + L.r0);
@@ -615,8 +636,9 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
     const cplx* T0 = J.T + (long long)mat * J.mat_stride;
     double* out = J.out + 3LL * mat;
 
-    // 1. FP32 Jacobi, from the pool's V set of a nearby wavenumber when given
     const long long nn = (long long)n * n;
+    if (!PAIR || rank == 0) {
+    // 1. FP32 Jacobi, from the pool's V set of a nearby wavenumber when given
     const int wslot = (J.vpool && J.warm_slot) ? J.warm_slot[mat] : -1;
     const int oslot = (J.vpool && J.out_slot) ? J.out_slot[mat] : -1;
     jacobi_fp32(T0, n, A32, V32, &s_rot, wslot >= 0 ? J.vpool + wslot * nn : nullptr, reinterpret_cast<cpf*>(X));
@@ -655,7 +677,6 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
     if (threadIdx.x == 0) {
         const int kb = min(n, kFastKmax);
         s_kb = kb;
-        s_sing = 0;
         // Block inverse iterations: the start block's components outside the kb
         // smallest singular directions shrink by (sigma_1 / sigma_kb+1)^2 per iteration.
         // Four iterations at a ratio of 1/3 (a factor 3^-8) are the least reduction the
@@ -680,44 +701,95 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_fast(SvdFastJob J) {
         s_iters = iters;
     }
     __syncthreads();
+    {
+        const int kb = s_kb;
+        for (int e = threadIdx.x; e < n * kb; e += blockDim.x) {
+            const cpf v = V32[idx[e / n] * n + e % n];
+            X[e] = mk((double)v.re, (double)v.im);
+        }
+        __syncthreads();
+        if constexpr (PAIR) {   // the start block and its two counts to CTA 1
+            cg::cluster_group cl = cg::this_cluster();
+            cplx* Xr = cl.map_shared_rank(X, 1);
+            for (int e = threadIdx.x; e < n * kb; e += blockDim.x) Xr[e] = X[e];
+            if (threadIdx.x == 0) {
+                *cl.map_shared_rank(&s_kb, 1) = kb;
+                *cl.map_shared_rank(&s_iters, 1) = s_iters;
+            }
+        }
+    }
+    }   // stage 1
+    if (!PAIR || rank == 1) {
+        // FP64 LU of T (in the single-CTA form over the FP32 work space)
+        if (threadIdx.x == 0) s_sing = 0;
+        for (int e = threadIdx.x; e < n * n; e += blockDim.x) T64[e] = T0[e];
+        __syncthreads();
+        lu_smem(T64, n, piv, &s_sing, sbuf);
+        perm_from_piv(piv, n, perm);
+        // U's diagonal replaced by its reciprocals: the solves below multiply
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            const cplx d = T64[k + (long long)k * n];
+            T64[k + (long long)k * n] = norm2(d) > 0. ? cdiv(mk(1.), d) : mk(0.);
+        }
+        __syncthreads();
+    }
+    if constexpr (PAIR) {
+        cg::cluster_group cl = cg::this_cluster();
+        cl.sync();   // CTA 1 holds the start block; CTA 0 is done with its FP32 work space
+        if (rank == 0) {   // the factors and the permutation from CTA 1
+            const cplx* Tr = cl.map_shared_rank(T64, 1);
+            for (long long e = threadIdx.x; e < nn; e += blockDim.x) T64[e] = Tr[e];
+            const int* pr = cl.map_shared_rank(perm, 1);
+            for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = pr[i];
+            __syncthreads();
+        }
+    }
     const int kb = s_kb;
-    for (int e = threadIdx.x; e < n * kb; e += blockDim.x) {
-        const cpf v = V32[idx[e / n] * n + e % n];
-        X[e] = mk((double)v.re, (double)v.im);
-    }
-    __syncthreads();
-    // FP64 LU of T over the FP32 work space
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) T64[e] = T0[e];
-    __syncthreads();
-    lu_smem(T64, n, piv, &s_sing, sbuf);
-    perm_from_piv(piv, n, perm);
-    // U's diagonal replaced by its reciprocals: the solves below multiply
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        const cplx d = T64[k + (long long)k * n];
-        T64[k + (long long)k * n] = norm2(d) > 0. ? cdiv(mk(1.), d) : mk(0.);
-    }
-    __syncthreads();
     qr_cgs2(X, n, kb, coef, red);
+    // the columns this CTA iterates on: all of them, or its half in the paired form
+    int col0 = 0, cnt = kb;
+    if constexpr (PAIR) {
+        const int h = (kb + 1) / 2;
+        col0 = rank ? h : 0;
+        cnt = rank ? kb - h : h;
+    }
+    cplx* Xc = X + (long long)col0 * n;
     const int inv_iters = s_iters;
     for (int it = 0; it < inv_iters; ++it) {   // Y is free until the Rayleigh-Ritz step
-        solve_lu_h_blk(T64, perm, n, X, kb, sbuf, Y, true);
-        solve_lu_blk(T64, perm, n, X, kb, sbuf, Y, true);
+        solve_lu_h_blk(T64, perm, n, Xc, cnt, sbuf, Y, true);
+        solve_lu_blk(T64, perm, n, Xc, cnt, sbuf, Y, true);
+        if constexpr (PAIR) {   // each CTA's columns to the other, then both orthonormalise all
+            cg::cluster_group cl = cg::this_cluster();
+            cl.sync();   // the other CTA has finished reading its block (the last QR)
+            cplx* Xr = cl.map_shared_rank(Xc, rank ^ 1);
+            for (int e = threadIdx.x; e < n * cnt; e += blockDim.x) Xr[e] = Xc[e];
+            cl.sync();
+        }
         qr_cgs2(X, n, kb, coef, red);
     }
     // Rayleigh-Ritz: Y = T X = Q_Y Rf, Rf W = Q_R Sigma.  One thread per entry of Y:
     // consecutive threads take consecutive rows (coalesced reads of T's columns from
-    // global memory), X's entries are shared-memory broadcasts.
-    for (int e = threadIdx.x; e < n * kb; e += blockDim.x) {
-        const int r = e % n, j = e / n;
-        const cplx* xj = X + (long long)j * n;
-        cplx a0 = mk(0.), a1 = mk(0.);
-        int c = 0;
-        for (; c + 1 < n; c += 2) {
-            cfma(a0, T0[r + (long long)c * n], xj[c]);
-            cfma(a1, T0[r + (long long)(c + 1) * n], xj[c + 1]);
+    // global memory), X's entries are shared-memory broadcasts.  Paired: CTA 0 writes
+    // its columns straight into CTA 1's Y and leaves.
+    {
+        cplx* Yd = Y;
+        if constexpr (PAIR) Yd = cg::this_cluster().map_shared_rank(Y, 1);
+        for (int e = threadIdx.x; e < n * cnt; e += blockDim.x) {
+            const int r = e % n, j = col0 + e / n;
+            const cplx* xj = X + (long long)j * n;
+            cplx a0 = mk(0.), a1 = mk(0.);
+            int c = 0;
+            for (; c + 1 < n; c += 2) {
+                cfma(a0, T0[r + (long long)c * n], xj[c]);
+                cfma(a1, T0[r + (long long)(c + 1) * n], xj[c + 1]);
+            }
+            if (c < n) cfma(a0, T0[r + (long long)c * n], xj[c]);
+            Yd[r + (long long)j * n] = a0 + a1;
         }
-        if (c < n) cfma(a0, T0[r + (long long)c * n], xj[c]);
-        Y[e] = a0 + a1;
+    }
+    if constexpr (PAIR) {
+        cg::this_cluster().sync();
+        if (rank == 0) return;
     }
     __syncthreads();
     qr_cgs2(Y, n, kb, coef, red, Rf);
@@ -916,12 +988,32 @@ cudaError_t launch_svd_fast(int n, int nmat, int D, const cplx* T, long long mat
                             const int* out_slot, cplx* uv) {
     const size_t limit = 220 * 1024, smem = svd_fast_smem_bytes(n);
     if (smem > limit || n < 2) return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(k_svd_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit);
-    if (e != cudaSuccess) return e;
     SvdFastJob J{n, nmat, D, T, mat_stride, der_stride, out, status, vpool, warm_slot, out_slot, uv};
-    k_svd_fast<<<nmat, kSvdThreads, smem, st>>>(J);
-    return cudaGetLastError();
+    if (nmat > g_svd_pair_max.load(std::memory_order_relaxed)) {
+        cudaError_t e = cudaFuncSetAttribute(k_svd_fast<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit);
+        if (e != cudaSuccess) return e;
+        k_svd_fast<false><<<nmat, kSvdThreads, smem, st>>>(J);
+        return cudaGetLastError();
+    }
+    cudaError_t e = cudaFuncSetAttribute(k_svd_fast<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2 * nmat);
+    cfg.blockDim = dim3(kSvdThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_svd_fast<true>, J);
 }
+
+void svd_set_pair_max(int m) { g_svd_pair_max = m < 0 ? 0 : m; }
+int svd_get_pair_max() { return g_svd_pair_max.load(); }
 
 // ---------------------------------------------------------------- allocation-free variant
 //

@@ -29,6 +29,9 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# 32 hardware work queues for the search's many streams (the package sets the same
+# default on import; here it must precede torch's CUDA initialisation)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 CFG = dict(radius=0.25, N=50, c_i=23.4, c_o=1.0, order=11, k_min=0.5, k_max=10.0, npoints=200, tol=1e-8)
 WORKLOAD = ("plain sweep: circle r=0.25, N=50 arc panels, c_i=23.4, c_o=1, Gauss order 11, P1/P1 "

@@ -487,6 +487,15 @@ struct hbem_solop_s {
     }
 };
 
+// The plain search keeps up to ~40 streams busy at once.  With CUDA's default of 8
+// hardware work queues per device, streams share queues and a stream's launches wait
+// behind another stream's (a grid chunk's event wait, a long kernel) that they do not
+// depend on.  At load time, before a CUDA context exists, ask for the maximum of 32
+// queues unless the process has chosen a number already.
+__attribute__((constructor)) static void hbem_default_connections() {
+    setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
+}
+
 extern "C" {
 
 int hbem_version(void) { return 100; }

@@ -459,6 +459,11 @@ constexpr int kFastInvIter = 4;
 constexpr int kFastNeumannMax = 200;   // preconditioned CG iteration cap
 // launches of at most this many matrices run the paired (two-CTA cluster) form
 static std::atomic<int> g_svd_pair_max{16};
+// per host thread: set while long-running launches of other streams keep the GPU full.
+// A cluster needs two SMs of one GPC free at once, and the block scheduler fills SMs
+// that free one at a time with the other streams' blocks, whatever their priority, so
+// a cluster launch waits until those launches have drained; one-CTA launches do not.
+thread_local int t_svd_pair_hold = 0;
 
 struct SvdFastJob {
     int n, nmat, D;
@@ -989,7 +994,7 @@ cudaError_t launch_svd_fast(int n, int nmat, int D, const cplx* T, long long mat
     const size_t limit = 220 * 1024, smem = svd_fast_smem_bytes(n);
     if (smem > limit || n < 2) return cudaErrorInvalidValue;
     SvdFastJob J{n, nmat, D, T, mat_stride, der_stride, out, status, vpool, warm_slot, out_slot, uv};
-    if (nmat > g_svd_pair_max.load(std::memory_order_relaxed)) {
+    if (t_svd_pair_hold || nmat > g_svd_pair_max.load(std::memory_order_relaxed)) {
         cudaError_t e = cudaFuncSetAttribute(k_svd_fast<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit);
         if (e != cudaSuccess) return e;
         k_svd_fast<false><<<nmat, kSvdThreads, smem, st>>>(J);
@@ -1014,6 +1019,7 @@ cudaError_t launch_svd_fast(int n, int nmat, int D, const cplx* T, long long mat
 
 void svd_set_pair_max(int m) { g_svd_pair_max = m < 0 ? 0 : m; }
 int svd_get_pair_max() { return g_svd_pair_max.load(); }
+void svd_pair_hold(int on) { t_svd_pair_hold = on ? 1 : 0; }
 
 // ---------------------------------------------------------------- allocation-free variant
 //

@@ -26,6 +26,7 @@ int plain_speculate_ok(hbem_solop s);
 int plain_warm_start_ok();
 int plain_async_ok();
 int plain_spec_limits(int* deep);
+void svd_pair_hold(int on);
 int pipeline_setup(hbem_solop s, int npoints, int npool);
 void pipeline_keep_uv(hbem_solop s, int npoints);
 int lane_launch_grid(hbem_solop s, int lane, const double* k_host, int npts, int first, double c_o, double c_i,
@@ -498,8 +499,8 @@ int newton_rounds(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i,
 }
 
 // The plain search as one pipeline on several streams ("lanes"): the grid in chunks
-// whose assemblies run in order while each chunk's dense sigma overlaps the next
-// chunk's assembly; a candidate's bracket ends (sigma' from the grid's kept singular
+// whose assemblies run one after another (from the top of the range down) while each
+// chunk's dense sigma overlaps the next chunk's assembly; a candidate's bracket ends (sigma' from the grid's kept singular
 // vectors) as soon as the grid around it is known; its Newton steps as soon as its
 // previous point is evaluated, one point per lane; and, when asked for, its root's
 // sign-change check as soon as it converges.  The FP64 assembly of one candidate runs
@@ -560,8 +561,8 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
     std::vector<std::vector<double>> pend;
     nt.clear();
     std::vector<double> vd;   // sigma' at root -/+ tol per candidate (NaN: none)
-    std::vector<int> chunk_done(nch, 0);
-    int known = 0, scanned = 0, chunks_in_order = 0;
+    std::vector<char> gknown(npoints, 0), scanned(npoints, 0);
+    int chunks_done = 0;
     bool grid_ok = true;
     for (int i = 0; i < npoints; ++i) g[3 * i] = g[3 * i + 1] = g[3 * i + 2] = NAN;
 
@@ -578,7 +579,7 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
         return -1;
     };
     auto unfinished = [&]() {
-        if (chunks_in_order < nch) return (size_t)1 << 30;   // candidates still to come
+        if (chunks_done < nch) return (size_t)1 << 30;   // candidates still to come
         size_t u = 0;
         for (size_t c = 0; c < cstate.size(); ++c) u += cstate[c] < 2 || (cstate[c] == 3 && !nt[c].done);
         return u;
@@ -594,12 +595,13 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
             const int first = F.cand * csize, cnt = std::min(csize, npoints - first);
             for (int q = 0; q < cnt; ++q) g[3 * (first + q)] = out[q];
             if (!fast) grid_ok = false;
-            chunk_done[F.cand] = 1;
-            while (chunks_in_order < nch && chunk_done[chunks_in_order]) ++chunks_in_order;
-            known = std::min(npoints, chunks_in_order * csize);
-            // 3-point local minima (roots_newton_polygon_rsvd.cpp:185-194) of the known grid
-            for (; scanned + 2 < known; ++scanned) {
-                const int i = scanned;
+            ++chunks_done;
+            for (int q = 0; q < cnt; ++q) gknown[first + q] = 1;
+            // 3-point local minima (roots_newton_polygon_rsvd.cpp:185-194) of the grid
+            // triples this chunk completes (candidates are put in grid order at the end)
+            for (int i = std::max(0, first - 2); i <= std::min(npoints - 3, first + cnt - 1); ++i) {
+                if (scanned[i] || !gknown[i] || !gknown[i + 1] || !gknown[i + 2]) continue;
+                scanned[i] = 1;
                 const double L = g[3 * i], C = g[3 * (i + 1)], R = g[3 * (i + 2)];
                 if (L - C > 0. && R - C > 0.) {
                     cgrid.push_back(i);
@@ -649,6 +651,11 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
         return HBEM_OK;
     };
     auto launch = [&](int lane, size_t c, double x, int kind, int side, int ws, int os) -> int {
+        // one-CTA dense sigma while grid chunks still fill the GPU (a two-CTA cluster
+        // would wait for them to drain), the paired form afterwards
+        bool grid_left = false;
+        for (int j = 0; j < nch; ++j) grid_left = grid_left || (busy[j] && fl[j].kind == kGrid);
+        hbem::svd_pair_hold(grid_left ? 1 : 0);
         if (int r = hbem::lane_launch(s, lane, &x, 1, c_o, c_i, &ws, &os, npool, kind == kVerify ? 1u : 2u)) return r;
         fl[lane] = Flight{(int)c, x, kind, side, ws};
         busy[lane] = 1;
@@ -750,10 +757,13 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
             hbem::lane_wait(s, l, 1, &fin);
         }
     };
-    // the grid chunks, assembled in order on lanes 0 .. nch - 1
-    for (int j = 0; j < nch; ++j) {
+    // the grid chunks (chunk j on lane j), assembled one after another from the top of
+    // the range down: the sharpest minima, whose Newton runs take the most steps (long
+    // bisection runs), tend to lie at the higher wavenumbers, so their runs start first
+    for (int q = 0; q < nch; ++q) {
+        const int j = nch - 1 - q;
         const int first = j * csize, cnt = std::min(csize, npoints - first);
-        if (int r = hbem::lane_launch_grid(s, j, ks.data() + first, cnt, first, c_o, c_i, npool, j - 1)) {
+        if (int r = hbem::lane_launch_grid(s, j, ks.data() + first, cnt, first, c_o, c_i, npool, q ? j + 1 : -1)) {
             drain();
             return r;
         }
@@ -794,6 +804,19 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
             return r;
         }
     }
+    // candidates in grid order, the order the lock-step search finds them in
+    std::vector<size_t> by_k(cgrid.size());
+    for (size_t c = 0; c < by_k.size(); ++c) by_k[c] = c;
+    std::sort(by_k.begin(), by_k.end(), [&](size_t a, size_t b) { return cgrid[a] < cgrid[b]; });
+    std::vector<Newton> nt_k;
+    std::vector<double> vd_k;
+    for (size_t c : by_k) {
+        nt_k.push_back(nt[c]);
+        vd_k.push_back(vd[2 * c]);
+        vd_k.push_back(vd[2 * c + 1]);
+    }
+    nt.swap(nt_k);
+    vd.swap(vd_k);
     if (vder) *vder = vd;
     hbem::pipeline_keep_uv(s, npoints);
     return HBEM_OK;
@@ -994,6 +1017,7 @@ int hbem_find_resonances_plain_verified(hbem_solop s, double k_min, double k_max
     // Newton rounds one after another
     if (hbem::plain_speculate_ok(s) && hbem::plain_warm_start_ok() && hbem::plain_async_ok()) {
         const int r = plain_pipelined(s, ks, h, c_o, c_i, tol, g, nt, check_host ? &vder : nullptr, evals);
+        hbem::svd_pair_hold(0);
         if (r == HBEM_OK) {
             piped = true;
             checked = check_host != nullptr;

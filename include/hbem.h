@@ -63,6 +63,10 @@ int hbem_set_device(int device);
  *   fallback is per call and per host thread and leaves this switch unchanged.
  *   "svd_fast_force_redo" (default 0): 1 sends every fast-kernel result through that
  *   fallback as well (more work, same results), so tests can exercise it.
+ *   "svd_pair_max" (default 16, >= 0): launches of the fast kernel with at most this
+ *   many matrices run each matrix on a cluster of two CTAs (FP32 Jacobi beside the
+ *   FP64 LU, inverse iterations split by columns): lower latency per matrix, results
+ *   bit-identical to the one-CTA form; 0 never pairs.
  *   "arnoldi_maxit" (default 1000, >= 1): iteration cap of hbem_arnoldi_sv_batch*.
  *   "mlp_tensor_cores" (default 1): the MLP's BF16 products on tcgen05; 0 uses FP32 FMA.
  *   "singular_table" (default 1): coincident / adjacent panel pairs read the

@@ -174,46 +174,50 @@ __device__ __forceinline__ cplx entry_yx(const cplx (&m)[4], int a, bool ry, int
 //   ttp    : |tau_i||tau_j| (constant per pair: lines and circular arcs)
 //   tdt    : 2 tau_i.tau_j for straight panels (constant per pair); ignored when CURVED
 //   tz     : the tangent product vanishes for the pair -> no k^2 term in W
+// The entries of shape-function pair (a, b) of every layer and derivative order.
+template <int D, bool CURVED>
+__device__ __forceinline__ void store_local_ab(const Acc<D, CURVED>& A, const KConst& K, bool rx, bool ry, double ttp,
+                                               double tdt, bool tz, cplx* dst, int a, int b) {
+    const cplx kc = K.c * K.k;
+    const int e = 2 * a + b;
+    const double dd = (a == b) ? 1. : -1.;   // b'_a b'_b for P1 (+1, -1)
+    cplx T[D + 1], S[D + 1];
+#pragma unroll
+    for (int t = 0; t <= D; ++t) {
+        S[t] = A.s[t][0];
+        if (tz) T[t] = mk(0.);
+        else if (CURVED) T[t] = entry_xy(A.w[CURVED ? t : 0], a, rx, b, ry);
+        else T[t] = tdt * entry_xy(A.s[t], a, rx, b, ry);
+    }
+#pragma unroll
+    for (int t = 0; t <= D; ++t) {
+        cplx dl = entry_xy(A.dl[t], a, rx, b, ry);
+        cplx dlt = entry_yx(A.dlt[t], a, ry, b, rx);
+        cplx sl = ttp * entry_xy(A.s[t], a, rx, b, ry);
+        cplx hy = dd * S[t] - K.k2ch * T[t];
+        if (t == 1) hy += K.ks * T[0];
+        if (t == 2) hy -= K.ks_two * T[1] - T[0];
+        if (t == 1) {
+            dl = dl * kc; dlt = dlt * kc;
+            hy = -K.sqrtc * hy; sl = -K.sqrtc * sl;
+        } else if (t == 2) {
+            dl = K.c * dl; dlt = K.c * dlt;
+            hy = -K.c * hy; sl = -K.c * sl;   // single layer: c * (-q)
+        }
+        dst[t * kLocPerD + 0 + e] = dl;
+        dst[t * kLocPerD + 4 + e] = dlt;
+        dst[t * kLocPerD + 8 + e] = hy;
+        dst[t * kLocPerD + 12 + e] = sl;
+    }
+}
+
 template <int D, bool CURVED>
 __device__ __forceinline__ void store_local(const Acc<D, CURVED>& A, const KConst& K, bool rx, bool ry, double ttp,
                                             double tdt, bool tz, cplx* dst) {
-    const cplx kc = K.c * K.k;
 #pragma unroll
-    for (int a = 0; a < 2; ++a) {
+    for (int a = 0; a < 2; ++a)
 #pragma unroll
-        for (int b = 0; b < 2; ++b) {
-            const int e = 2 * a + b;
-            const double dd = (a == b) ? 1. : -1.;   // b'_a b'_b for P1 (+1, -1)
-            cplx T[D + 1], S[D + 1];
-#pragma unroll
-            for (int t = 0; t <= D; ++t) {
-                S[t] = A.s[t][0];
-                if (tz) T[t] = mk(0.);
-                else if (CURVED) T[t] = entry_xy(A.w[CURVED ? t : 0], a, rx, b, ry);
-                else T[t] = tdt * entry_xy(A.s[t], a, rx, b, ry);
-            }
-#pragma unroll
-            for (int t = 0; t <= D; ++t) {
-                cplx dl = entry_xy(A.dl[t], a, rx, b, ry);
-                cplx dlt = entry_yx(A.dlt[t], a, ry, b, rx);
-                cplx sl = ttp * entry_xy(A.s[t], a, rx, b, ry);
-                cplx hy = dd * S[t] - K.k2ch * T[t];
-                if (t == 1) hy += K.ks * T[0];
-                if (t == 2) hy -= K.ks_two * T[1] - T[0];
-                if (t == 1) {
-                    dl = dl * kc; dlt = dlt * kc;
-                    hy = -K.sqrtc * hy; sl = -K.sqrtc * sl;
-                } else if (t == 2) {
-                    dl = K.c * dl; dlt = K.c * dlt;
-                    hy = -K.c * hy; sl = -K.c * sl;   // single layer: c * (-q)
-                }
-                dst[t * kLocPerD + 0 + e] = dl;
-                dst[t * kLocPerD + 4 + e] = dlt;
-                dst[t * kLocPerD + 8 + e] = hy;
-                dst[t * kLocPerD + 12 + e] = sl;
-            }
-        }
-    }
+        for (int b = 0; b < 2; ++b) store_local_ab<D, CURVED>(A, K, rx, ry, ttp, tdt, tz, dst, a, b);
 }
 
 __device__ __forceinline__ bool close100eps(cplx a, cplx b) { return hypot(a.re - b.re, a.im - b.im) < 100. * kEps; }
@@ -683,6 +687,100 @@ __global__ void __launch_bounds__(128) k_singular(DevMesh M, const SingularTask*
     }
 }
 
+// ------------------------------------------------------------------ launches of few jobs
+//
+// A launch of a few wavenumbers (one Newton point of the plain search: 2 media) has
+// fewer singular CTAs than 4 per SM, and an adjacent pair's CTA (two point sets) takes
+// twice a coincident pair's time, so k_singular ends in a tail on part of the GPU.
+// Here each (pair, job) is split into CTAs of 1/q of a point set each: q parts for a
+// coincident pair, 2q for an adjacent one (blocks 2q t .. 2q t + 2q - 1 of pair t,
+// the upper q of a coincident pair empty), so that every CTA has the same work.  Their block sums go to `part`
+// ([job][pair x 2q][NV] doubles) and k_singular_join adds them in part order and forms
+// the pair blocks.
+
+template <int D, bool RK, bool CURVED>
+__global__ void __launch_bounds__(128) k_singular_part(DevMesh M, const SingularTask* tasks, const Job* jobs, int q,
+                                                       double* part) {
+    extern __shared__ double sm[];
+    double* sxc = sm;
+    double* swc = sm + M.nc;
+    double* red = sm + 2 * M.nc;
+    for (int t = threadIdx.x; t < M.nc; t += blockDim.x) { sxc[t] = M.xc[t]; swc[t] = M.wc[t]; }
+    __syncthreads();
+    const int task = blockIdx.x / (2 * q), sub = blockIdx.x - task * 2 * q;
+    const SingularTask T = tasks[task];
+    const int nset = T.kind == PK_COINC ? 1 : 2;
+    if (sub >= nset * q) return;   // whole CTA, before any barrier
+    const int job = blockIdx.y;
+    KConst K = make_kconst(jobs[job]);
+    const uint8_t fl = M.flags[tri_index(T.i, T.j)];
+    const int nc = M.nc, tot = nc * nc;
+    const long long W = (long long)nset * tot;
+    const long long w0 = W * sub / (nset * q), w1 = W * (sub + 1) / (nset * q);
+    const double* G = M.sgeo ? M.sgeo + (long long)task * 2 * kSGeoFields * tot : nullptr;
+    Acc<D, CURVED> A;
+    A.zero();
+    for (long long w = w0 + threadIdx.x; w < w1; w += blockDim.x) {
+        const int Kset = (int)(w / tot), e = (int)(w - (long long)Kset * tot);
+        double f[kSGeoFields];
+        if (G) {
+#pragma unroll
+            for (int q = 0; q < kSGeoFields; ++q) f[q] = __ldg(G + ((long long)Kset * kSGeoFields + q) * tot + e);
+        } else {
+            const int a = e % nc, b = e / nc;
+            singular_fields(M, T, Kset, sxc[a], sxc[b], swc[a], swc[b], f);
+        }
+        singular_accumulate<D, RK, CURVED>(A, K, T.kind, fl, Kset, f);
+    }
+    block_reduce(A, red);
+    constexpr int NV = (int)(sizeof(Acc<D, CURVED>) / sizeof(double));
+    if (threadIdx.x == 0) {
+        const double* av = reinterpret_cast<const double*>(&A);
+        double* dst = part + ((long long)job * gridDim.x + blockIdx.x) * NV;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) dst[v] = av[v];
+    }
+}
+
+// one warp per (pair, job): its lanes add the pair's partial sums (each lane some of
+// the moments, the parts in order), then four lanes form the blocks of one
+// shape-function pair each
+template <int D, bool CURVED>
+__global__ void __launch_bounds__(128) k_singular_join(DevMesh M, const SingularTask* tasks, const Job* jobs,
+                                                       int ntasks, int q, const double* part, cplx* loc,
+                                                       long long npair) {
+    constexpr int NV = (int)(sizeof(Acc<D, CURVED>) / sizeof(double));
+    __shared__ double sacc[4][NV];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int task = blockIdx.x * 4 + warp;
+    if (task >= ntasks) return;   // whole warp
+    const int job = blockIdx.y;
+    const SingularTask T = tasks[task];
+    const int nparts = (T.kind == PK_COINC ? 1 : 2) * q;
+    const double* src = part + ((long long)job * ntasks + task) * 2 * q * NV;
+    for (int v = lane; v < NV; v += 32) {
+        double x = 0.;
+        for (int u = 0; u < nparts; ++u) x += src[(long long)u * NV + v];
+        sacc[warp][v] = x;
+    }
+    __syncwarp();
+    if (lane >= 4) return;
+    Acc<D, CURVED> A;
+    double* av = reinterpret_cast<double*>(&A);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) av[v] = sacc[warp][v];
+    const KConst K = make_kconst(jobs[job]);
+    const long long pid = tri_index(T.i, T.j);
+    const uint8_t fl = M.flags[pid];
+    SPoint P;
+    singular_point(M, T, 0, M.xc[0], M.xc[0], P);
+    const bool adj = T.kind == PK_ADJ;
+    const bool tz = CURVED ? false : (fl & PF_TDT0_ZERO) != 0;
+    store_local_ab<D, CURVED>(A, K, adj && !T.swap, adj && T.swap, P.tin * P.tjn,
+                              2. * (P.ti.im * P.tj.im + P.ti.re * P.tj.re), tz,
+                              loc + ((long long)job * npair + pid) * (D + 1) * kLocPerD, lane >> 1, lane & 1);
+}
+
 // ------------------------------------------------------------------ many meshes in one launch
 //
 // The batching path: the jobs of several meshes (scatterers of uneven panel counts,
@@ -921,11 +1019,36 @@ cudaError_t launch_hankel01(int n, const cplx* z, int complex_arg, cplx* h0, cpl
 // 0 forces a thread per pair, ppw > 0 a warp per pair with that many pairs.
 constexpr int kLayoutAuto = -1;
 
+// Parts per point set (q) of the split singular launch: about four CTAs per SM (152
+// SMs) counting an adjacent pair's two sets, at most 8; 0 when the launch has that
+// many CTAs without splitting.
+int singular_parts(int ntasks, int njobs) {
+    const long long ctas = (long long)ntasks * njobs, want = 4LL * 152;
+    if (ntasks <= 0 || njobs <= 0 || ctas >= want) return 0;
+    return (int)std::min<long long>(8, (want + 2 * ctas - 1) / (2 * ctas));
+}
+
+size_t singular_part_bytes(int ntasks, int njobs, int d, bool curved) {
+    const int nparts = 2 * singular_parts(ntasks, njobs);
+    size_t nv = 0;
+    if (d == 0) nv = curved ? sizeof(Acc<0, true>) : sizeof(Acc<0, false>);
+    else if (d == 1) nv = curved ? sizeof(Acc<1, true>) : sizeof(Acc<1, false>);
+    else nv = curved ? sizeof(Acc<2, true>) : sizeof(Acc<2, false>);
+    return (size_t)nparts * ntasks * njobs * nv;
+}
+
+// part: scratch of singular_part_bytes for the split singular launch of few jobs, or
+// null (one CTA per pair and job)
 template <int D, bool RK, bool CURVED>
 static cudaError_t launch_local_c(const DevMesh& M, const SingularTask* tasks, int ntasks, const Job* jobs, int njobs,
-                                  cplx* loc, cudaStream_t st, int layout, int which) {
+                                  cplx* loc, cudaStream_t st, int layout, int which, double* part) {
     long long npair = (long long)M.n * (M.n + 1) / 2;
     long long nlow = (long long)M.n * (M.n - 1) / 2;
+    constexpr int NV = (int)(sizeof(Acc<D, CURVED>) / sizeof(double));
+    const size_t ssmem = (2 * (size_t)M.nc + 4 * NV) * sizeof(double);
+    const int q = (part && (which & 2)) ? singular_parts(ntasks, njobs) : 0;
+    if (q > 0)
+        k_singular_part<D, RK, CURVED><<<dim3(ntasks * 2 * q, njobs), 128, ssmem, st>>>(M, tasks, jobs, q, part);
     if (nlow > 0 && (which & 1)) {
         int ppw = layout;
         if (layout == kLayoutAuto) {
@@ -941,20 +1064,21 @@ static cudaError_t launch_local_c(const DevMesh& M, const SingularTask* tasks, i
             k_general_w<D, RK, CURVED><<<g, 128, 0, st>>>(M, jobs, loc, npair, ppw);
         }
     }
-    if (ntasks > 0 && (which & 2)) {
-        constexpr int NV = (int)(sizeof(Acc<D, CURVED>) / sizeof(double));
-        size_t smem = (2 * (size_t)M.nc + 4 * NV) * sizeof(double);
+    if (q > 0) {
+        k_singular_join<D, CURVED><<<dim3((ntasks + 3) / 4, njobs), 128, 0, st>>>(M, tasks, jobs, ntasks, q, part, loc,
+                                                                                   npair);
+    } else if (ntasks > 0 && (which & 2)) {
         dim3 g(ntasks, njobs);
-        k_singular<D, RK, CURVED><<<g, 128, smem, st>>>(M, tasks, jobs, loc, npair);
+        k_singular<D, RK, CURVED><<<g, 128, ssmem, st>>>(M, tasks, jobs, loc, npair);
     }
     return cudaGetLastError();
 }
 
 template <int D, bool RK>
 static cudaError_t launch_local_t(const DevMesh& M, const SingularTask* tasks, int ntasks, const Job* jobs, int njobs,
-                                  cplx* loc, cudaStream_t st, int layout, int which) {
-    if (M.lines) return launch_local_c<D, RK, false>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which);
-    return launch_local_c<D, RK, true>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which);
+                                  cplx* loc, cudaStream_t st, int layout, int which, double* part) {
+    if (M.lines) return launch_local_c<D, RK, false>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which, part);
+    return launch_local_c<D, RK, true>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which, part);
 }
 
 size_t singular_geo_bytes(int nc, int ntasks) {
@@ -1011,17 +1135,17 @@ cudaError_t launch_local_multi(const MultiMesh* meshes, const MultiJob* jobs, in
 }
 
 // layout: kLayoutAuto or a forced general-pair layout (see launch_local_c); which:
-// bit 0 the general pairs, bit 1 the singular pairs
+// bit 0 the general pairs, bit 1 the singular pairs; part: see launch_local_c
 cudaError_t launch_local(const DevMesh& M, const SingularTask* tasks, int ntasks, const Job* jobs, int njobs,
-                         bool real_k, int d, cplx* loc, cudaStream_t st, int layout, int which) {
+                         bool real_k, int d, cplx* loc, cudaStream_t st, int layout, int which, double* part) {
     if (real_k) {
-        if (d == 0) return launch_local_t<0, true>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which);
-        if (d == 1) return launch_local_t<1, true>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which);
-        return launch_local_t<2, true>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which);
+        if (d == 0) return launch_local_t<0, true>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which, part);
+        if (d == 1) return launch_local_t<1, true>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which, part);
+        return launch_local_t<2, true>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which, part);
     }
-    if (d == 0) return launch_local_t<0, false>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which);
-    if (d == 1) return launch_local_t<1, false>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which);
-    return launch_local_t<2, false>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which);
+    if (d == 0) return launch_local_t<0, false>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which, part);
+    if (d == 1) return launch_local_t<1, false>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which, part);
+    return launch_local_t<2, false>(M, tasks, ntasks, jobs, njobs, loc, st, layout, which, part);
 }
 
 cudaError_t launch_gather_T(int N, int d, const cplx* loc, const double* Mmass, int nk, int sp, cplx* T,

@@ -25,7 +25,9 @@ size_t singular_geo_bytes(int nc, int ntasks);
 cudaError_t launch_singular_geo(const DevMesh& M, const SingularTask* tasks, int ntasks, double* geo,
                                 cudaStream_t st);
 cudaError_t launch_local(const DevMesh& M, const SingularTask* tasks, int ntasks, const Job* jobs, int njobs,
-                         bool real_k, int d, cplx* loc, cudaStream_t st, int layout, int which);
+                         bool real_k, int d, cplx* loc, cudaStream_t st, int layout, int which, double* part);
+int singular_parts(int ntasks, int njobs);
+size_t singular_part_bytes(int ntasks, int njobs, int d, bool curved);
 cudaError_t launch_gather_T(int N, int d, const cplx* loc, const double* Mmass, int nk, int sp, cplx* T,
                             cudaStream_t st);
 cudaError_t launch_local_multi(const MultiMesh* meshes, const MultiJob* jobs, int njobs, const long long* gstart,
@@ -138,6 +140,8 @@ std::atomic<int> g_svd_force_redo{0};   // test hook: every fast-kernel result g
 inline bool svd_fast_on() { return g_svd_fast.load(std::memory_order_relaxed) && !t_svd_polished_only; }
 int g_arnoldi_maxit = 1000;   // block iterations of hbem_arnoldi_sv_batch*
 int g_plain_speculate = 1;    // plain search: speculative bisection points in small Newton rounds
+int g_singular_split = 1;     // launches of few jobs: singular pairs split over several CTAs each
+thread_local int t_split_hold = 0;   // per host thread: no split while other streams keep the GPU full
 int g_plain_warm_start = 1;   // plain search: dense-kernel Jacobi warm-started from nearby V sets
 int g_plain_async = 1;        // plain search: Newton candidates advance independently on their own streams
 int g_plain_spec_async = 2;   // ... speculating while at most this many candidates are unfinished
@@ -326,7 +330,7 @@ int tuned_layout(const DevMesh& M, const SingularTask* tasks, int ntasks, const 
     float best_ms = 0.f;
     for (int lay : kTuneLayouts) {
         cudaEventRecord(a, st);
-        if (launch_local(M, tasks, ntasks, jobs, njobs, real_k, d, loc, st, lay, 1) != cudaSuccess) break;
+        if (launch_local(M, tasks, ntasks, jobs, njobs, real_k, d, loc, st, lay, 1, nullptr) != cudaSuccess) break;
         cudaEventRecord(b, st);
         if (cudaEventSynchronize(b) != cudaSuccess) break;
         float ms = 0.f;
@@ -350,15 +354,17 @@ int tuned_layout(const DevMesh& M, const SingularTask* tasks, int ntasks, const 
     return best;
 }
 
+// part: scratch of singular_part_bytes for the split singular launch of few jobs (or
+// null: one CTA per pair and job)
 cudaError_t local_assembly(const DevMesh& M, const SingularTask* tasks, int ntasks, int ncoinc, const Job* jobs,
-                           int njobs, bool real_k, int d, cplx* loc, cudaStream_t st) {
+                           int njobs, bool real_k, int d, cplx* loc, cudaStream_t st, double* part = nullptr) {
     const int layout = (g_autotune && M.n > 1) ? tuned_layout(M, tasks, ntasks, jobs, njobs, real_k, d, loc, st)
                                                : kLayoutAuto;
     cudaEvent_t e0 = nullptr;
     const bool timed = g_timing != 0;
     if (timed) timing_begin(&e0, st);
-    cudaError_t e = launch_local(M, tasks, ntasks, jobs, njobs, real_k, d, loc, st, layout, 3);
-    g_launches += (M.n > 1 ? 1 : 0) + (ntasks > 0 ? 1 : 0);
+    cudaError_t e = launch_local(M, tasks, ntasks, jobs, njobs, real_k, d, loc, st, layout, 3, part);
+    g_launches += (M.n > 1 ? 1 : 0) + (ntasks > 0 ? 1 : 0) + (part && singular_parts(ntasks, njobs) > 0 ? 1 : 0);
     if (timed) {
         timing_end(e0, st);
         g_asm_launches += 1;
@@ -593,6 +599,10 @@ int hbem_set_option(const char* name, int value) {
         g_plain_warm_start = value ? 1 : 0;
         return HBEM_OK;
     }
+    if (k == "singular_split") {
+        g_singular_split = value ? 1 : 0;
+        return HBEM_OK;
+    }
     if (k == "plain_speculate") {
         g_plain_speculate = value ? 1 : 0;
         return HBEM_OK;
@@ -631,6 +641,7 @@ int hbem_get_option(const char* name, int* value) {
     else if (k == "mlp_tensor_cores") *value = mlp_get_tensor_cores();
     else if (k == "singular_table") *value = g_singular_table;
     else if (k == "plain_warm_start") *value = g_plain_warm_start;
+    else if (k == "singular_split") *value = g_singular_split;
     else if (k == "plain_speculate") *value = g_plain_speculate;
     else if (k == "plain_async") *value = g_plain_async;
     else if (k == "plain_spec_async") *value = g_plain_spec_async;
@@ -982,9 +993,14 @@ static int gen_T_batch_ws(hbem_solop s, const double* k_host, const double* kim_
             jobs.push_back(Job{kr, ki, c_o});
         }
         HB_CK(upload(d_jobs, jobs, st));
-        HB_CK(d_loc.ensure(per_job * 2 * kn));
+        // the pair blocks, then the partial sums of a split singular launch
+        const size_t part_bytes =
+            (g_singular_split && !t_split_hold) ? singular_part_bytes((int)b->tasks.size(), 2 * kn, (int)d, !b->lines)
+                                                : 0;
+        HB_CK(d_loc.ensure(per_job * 2 * kn + part_bytes));
+        double* part = part_bytes ? reinterpret_cast<double*>(d_loc.as<char>() + per_job * 2 * kn) : nullptr;
         HB_CK(local_assembly(b->view(), b->d_tasks.as<SingularTask>(), (int)b->tasks.size(), b->n, d_jobs.as<Job>(),
-                             2 * kn, real_k, (int)d, d_loc.as<cplx>(), st));
+                             2 * kn, real_k, (int)d, d_loc.as<cplx>(), st, part));
         cplx* Tk = T_dev + (size_t)k0 * (d + 1) * mat;
         HB_CK(launch_gather_T(N, (int)d, d_loc.as<cplx>(), s->d_M.as<double>(), kn, b->sp(), Tk, st));
         g_launches += 1;
@@ -1684,6 +1700,8 @@ int lane_launch(hbem_solop s, int lane, const double* k_host, int npts, double c
     HB_CK(cudaEventRecord(L.done, L.st));
     return HBEM_OK;
 }
+
+void singular_split_hold(int on) { t_split_hold = on ? 1 : 0; }
 
 int lane_wait(hbem_solop s, int lane, int block, int* finished) {
     EvalLane& L = *lane_pool(s->b->device).lanes[lane];

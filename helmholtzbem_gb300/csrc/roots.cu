@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <array>
 #include <cstdint>
+#include <cstdlib>
 #include <functional>
 #include <cmath>
 #include <limits>
@@ -27,6 +28,7 @@ int plain_warm_start_ok();
 int plain_async_ok();
 int plain_spec_limits(int* deep);
 void svd_pair_hold(int on);
+void singular_split_hold(int on);
 int pipeline_setup(hbem_solop s, int npoints, int npool);
 void pipeline_keep_uv(hbem_solop s, int npoints);
 int lane_launch_grid(hbem_solop s, int lane, const double* k_host, int npts, int first, double c_o, double c_i,
@@ -1016,8 +1018,12 @@ int hbem_find_resonances_plain_verified(hbem_solop s, double k_min, double k_max
     // one-CTA dense kernel takes the order; else grid, bracket ends and lock-step
     // Newton rounds one after another
     if (hbem::plain_speculate_ok(s) && hbem::plain_warm_start_ok() && hbem::plain_async_ok()) {
+        // its launches share the GPU with each other: the split singular launch of few
+        // jobs (lower latency alone, more launches and CTAs) measured no faster there
+        hbem::singular_split_hold(1);
         const int r = plain_pipelined(s, ks, h, c_o, c_i, tol, g, nt, check_host ? &vder : nullptr, evals);
         hbem::svd_pair_hold(0);
+        hbem::singular_split_hold(0);
         if (r == HBEM_OK) {
             piped = true;
             checked = check_host != nullptr;

@@ -73,6 +73,11 @@ int hbem_set_device(int device);
  *   k-independent data of their composite quadrature points (distance, tangent and
  *   normal products, weights) from a table the builder makes once (up to 256 MB);
  *   0 computes it in the kernel for every wavenumber and medium.
+ *   "singular_split" (default 1): assembly launches of few wavenumbers (coincident /
+ *   adjacent pairs x media below four CTAs per SM) split every such pair over several
+ *   CTAs of equal work and add the parts in a second launch: lower latency for one
+ *   T(k); sums in another order (results agree to ~1e-15).  The pipelined plain search
+ *   does not split (its launches share the GPU).
  *   "plain_speculate" (default 1): speculative bisection points in the plain
  *   search's small Newton rounds (hbem_find_resonances_plain).
  *   "autotune" (default 0): the panel-pair assembly times each layout of its general

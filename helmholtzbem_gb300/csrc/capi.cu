@@ -1644,10 +1644,13 @@ int vpool_ensure(hbem_solop s, int npool) {
 // with the FP64-polished kernel, synchronously, any matrix the fast kernel could not
 // finish.  The dense kernel must take the operator's order (plain_speculate_ok).
 // the lanes up to `lane` of this thread's pool for `device` exist.  Lanes below
-// kBulkLanes (the plain search's grid chunks) run at the lowest stream priority, the
-// others (its candidates' evaluations, on the critical path) at the highest, so that a
-// candidate's blocks are scheduled ahead of the grid's remaining ones.
+// kBulkLanes (the plain search's grid chunks) run at the lowest stream priority, lanes
+// kBulkLanes .. kUrgentLanes - 1 (candidates deep into their Newton runs, the search's
+// critical path) at the highest, the others (its other candidates' evaluations) one
+// level above the lowest, so that a candidate's blocks are scheduled ahead of the
+// grid's remaining ones and the longest runs' ahead of all.
 constexpr int kBulkLanes = 8;
+constexpr int kUrgentLanes = 16;
 static int lane_make(int device, int lane) {
     std::vector<EvalLane*>& lanes = lane_pool(device).lanes;
     int least = 0, greatest = 0;
@@ -1655,7 +1658,9 @@ static int lane_make(int device, int lane) {
     while ((int)lanes.size() <= lane) {
         EvalLane* l = new EvalLane();
         lanes.push_back(l);
-        const int prio = (int)lanes.size() - 1 < kBulkLanes ? least : greatest;
+        const int idx = (int)lanes.size() - 1;
+        const int mid = greatest < least - 1 ? least - 1 : greatest;
+        const int prio = idx < kBulkLanes ? least : (idx < kUrgentLanes ? greatest : mid);
         HB_CK(cudaStreamCreateWithPriority(&l->st, cudaStreamNonBlocking, prio));
         HB_CK(cudaEventCreateWithFlags(&l->done, cudaEventDisableTiming));
         HB_CK(cudaEventCreateWithFlags(&l->asm_done, cudaEventDisableTiming));

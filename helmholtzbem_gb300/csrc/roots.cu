@@ -521,6 +521,7 @@ int newton_rounds(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i,
 constexpr int kSpecDeep = 2;
 constexpr int kLanes = 40;
 constexpr int kCandLane = 8;   // the first lane of candidates' evaluations (the grid's below)
+constexpr int kUrgentEnd = 16; // lanes kCandLane .. kUrgentEnd - 1: highest stream priority
 constexpr int kMain = 0, kSpec = 1, kVerify = 2, kGrid = 3, kEnds = 4;
 
 // Returns HBEM_ERR_UNSUPPORTED, with nothing left in flight, when the grid cannot be
@@ -573,13 +574,19 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
         return std::find_if(cache[c].begin(), cache[c].end(),
                             [&](const std::array<double, 3>& e) { return e[0] == x; }) != cache[c].end();
     };
-    // candidates' evaluations on lanes kCandLane .. (high stream priority), grid chunks
-    // on lanes 0 .. nch - 1 (low priority)
-    auto free_lane = [&]() {
-        for (int l = kCandLane; l < kLanes; ++l)
+    // candidates' evaluations on lanes kCandLane .. (higher stream priority than the grid
+    // chunks on lanes 0 .. nch - 1): a free lane of the highest priority for a candidate
+    // deep into its Newton run (the runs with bisection steps, the longest, set the
+    // search's end), else one of the next
+    auto free_lane = [&](bool urgent = false) {
+        const int first = urgent ? kCandLane : kUrgentEnd, nl = kLanes - kCandLane;
+        for (int q = 0; q < nl; ++q) {
+            const int l = kCandLane + (first - kCandLane + q) % nl;
             if (!busy[l]) return l;
+        }
         return -1;
     };
+    auto urgent = [&](size_t c) { return cstate[c] == 3 && nt[c].it >= 3; };
     auto unfinished = [&]() {
         if (chunks_done < nch) return (size_t)1 << 30;   // candidates still to come
         size_t u = 0;
@@ -694,7 +701,7 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
             if (nt[c].done) {
                 // a converged candidate: its root's sign-change check beside the others' work
                 if (vder && vsent[c] < 2 && nt[c].found && nt[c].rts == nt[c].rts) {
-                    const int l = free_lane();
+                    const int l = free_lane(urgent(c));
                     if (l < 0) return -1;
                     const int side = vsent[c];
                     if (int r = launch(l, c, nt[c].rts + (side ? tol : -tol), kVerify, side, cur[c], -1)) return r;
@@ -719,7 +726,7 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
                 }
             }
             if (waited) continue;   // look again: the wait may have brought this point's value
-            const int lane = free_lane();
+            const int lane = free_lane(urgent(c));
             if (lane < 0) return -1;
             if (int r = launch(lane, c, nt[c].rts, kMain, 0, wslot, oslot)) return r;
             in_flight[c] = 1;
@@ -744,7 +751,7 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
                 for (int j = 0; j < np; ++j) {
                     const double x = pts[j];
                     if (x == nt[c].rts || cached(c, x) || has(pend[c], x)) continue;
-                    const int l2 = free_lane();
+                    const int l2 = free_lane(urgent(c));
                     if (l2 < 0) break;
                     if (int r = launch(l2, c, x, kSpec, 0, wslot, -1)) return r;
                     pend[c].push_back(x);

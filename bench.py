@@ -89,12 +89,13 @@ def run_profile_case():
 
 
 def run_profile_search():
-    """One plain search of the workload (grid, bracket-end sigma', Newton rounds)."""
+    """One step of the workload: the plain search with every root checked (grid, bracket-end
+    sigma', Newton runs and the roots' sign-change checks, as the timed step)."""
     from helmholtzbem_gb300 import api, geometry
     data = api.BuilderData(geometry.circle(CFG["radius"], CFG["N"]), order=CFG["order"])
     so = api.SolutionsOperator(data)
-    roots, grid, nev = so.find_resonances_plain(CFG["k_min"], CFG["k_max"], CFG["npoints"], CFG["c_o"], CFG["c_i"],
-                                                tol=CFG["tol"])
+    roots, grid, nev, chk = so.find_resonances_plain_verified(CFG["k_min"], CFG["k_max"], CFG["npoints"], CFG["c_o"],
+                                                              CFG["c_i"], tol=CFG["tol"])
     print("profile search done: %d roots, %d T(k) evaluations" % (roots.size, nev))
 
 

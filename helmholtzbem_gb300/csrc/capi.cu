@@ -39,6 +39,7 @@ cudaError_t launch_gather_layers_sub(int N, int d, int layers, const cplx* loc, 
                                      int cols, int sp, cplx* out, cudaStream_t st);
 cudaError_t launch_projection(int N, const double* id, const double* sb, const double* lr, cplx* T, int nmat,
                               cudaStream_t st);
+cudaError_t launch_taylor_pair(long long mat, const cplx* src, double h0, double h1, cplx* dst, cudaStream_t st);
 cudaError_t launch_svd(int n, int nmat, int D, int which, const cplx* T, long long mat_stride, long long der_stride,
                        cplx* gA, cplx* gV, double* out, double* sig_all, int* status, cudaStream_t st);
 cudaError_t launch_svd_mixed(int n, int nmat, int D, int which, const cplx* T, long long mat_stride,
@@ -439,12 +440,13 @@ struct EvalLane {
     cudaStream_t st = nullptr;
     cudaEvent_t done = nullptr, asm_done = nullptr;   // all work / the assembly part finished
     DBuf jobs, loc, T, out, status, slots;
+    DBuf T2;                   // T, T' at a root's two check points (lane_launch_verify)
     double* h_out = nullptr;   // pinned, 3 x kLaneMaxPts
     int* h_status = nullptr;   // pinned, kLaneMaxPts
     int npts = 0, d = 2, mode = 0;   // mode 0: sigma (+ derivatives), 1: grid chunk, 2: bracket ends
     double k[kLaneMaxPts];
     ~EvalLane() {
-        for (DBuf* x : {&jobs, &loc, &T, &out, &status, &slots}) x->release();
+        for (DBuf* x : {&jobs, &loc, &T, &out, &status, &slots, &T2}) x->release();
         if (h_out) cudaFreeHost(h_out);
         if (h_status) cudaFreeHost(h_status);
         if (done) cudaEventDestroy(done);
@@ -1707,6 +1709,46 @@ int lane_launch(hbem_solop s, int lane, const double* k_host, int npts, double c
 }
 
 void singular_split_hold(int on) { t_split_hold = on ? 1 : 0; }
+
+// A root's sign-change check on the lane that has just evaluated the root's last Newton
+// point (one point with T, T', T'' in the lane's buffer): T and T' at the two check
+// points k_host[0..1] from that point's three matrices by their Taylor polynomials
+// (launch_taylor_pair; the check points lie within 1e-6 of it), then sigma' there by the
+// dense kernel with warm slots wslot[0..1], all on the lane's own stream, behind the
+// evaluation.  lane_results then gives sigma' at the two points in out[1], out[4] (a
+// redo assembles them).  HBEM_ERR_UNSUPPORTED when the lane holds no such point: the
+// caller then assembles the check points.
+int lane_launch_verify(hbem_solop s, int lane, const double* k_host, const int* wslot, int npool) {
+    if (!s || lane < 0 || lane >= 64 || !k_host || !wslot) return fail(HBEM_ERR_INVALID, "lane_launch_verify: bad argument");
+    hbem_builder b = s->b;
+    std::vector<EvalLane*>& lanes = lane_pool(b->device).lanes;
+    if (lane >= (int)lanes.size()) return fail(HBEM_ERR_INVALID, "lane_launch_verify: no such lane");
+    EvalLane& L = *lanes[lane];
+    if (L.mode != 0 || L.d != 2 || L.npts != 1) return HBEM_ERR_UNSUPPORTED;
+    const double x = L.k[0], h0 = k_host[0] - x, h1 = k_host[1] - x;
+    if (!(std::fabs(h0) <= 1e-6 && std::fabs(h1) <= 1e-6)) return HBEM_ERR_UNSUPPORTED;
+    for (int q = 0; q < 2; ++q)
+        if (wslot[q] >= npool) return fail(HBEM_ERR_INVALID, "lane_launch_verify: slot outside the pool");
+    HB_CK(cudaSetDevice(b->device));
+    const int n = 2 * b->n;
+    const size_t mat = (size_t)n * n;
+    L.npts = 2;
+    L.d = 1;
+    L.k[0] = k_host[0];
+    L.k[1] = k_host[1];
+    std::vector<int> slots = {wslot[0], wslot[1], -1, -1};
+    HB_CK(upload(L.slots, slots, L.st));
+    HB_CK(L.T2.ensure(4 * mat * sizeof(cplx)));
+    HB_CK(launch_taylor_pair((long long)mat, L.T.as<cplx>(), h0, h1, L.T2.as<cplx>(), L.st));
+    HB_CK(launch_svd_fast(n, 2, 1, L.T2.as<cplx>(), 2LL * (long long)mat, (long long)mat, L.out.as<double>(),
+                          L.status.as<int>(), L.st, s->d_vpool.as<cplxf>(), L.slots.as<int>(), L.slots.as<int>() + 2,
+                          nullptr));
+    g_launches += 2;
+    HB_CK(cudaMemcpyAsync(L.h_out, L.out.p, 6 * sizeof(double), cudaMemcpyDeviceToHost, L.st));
+    HB_CK(cudaMemcpyAsync(L.h_status, L.status.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, L.st));
+    HB_CK(cudaEventRecord(L.done, L.st));
+    return HBEM_OK;
+}
 
 int lane_wait(hbem_solop s, int lane, int block, int* finished) {
     EvalLane& L = *lane_pool(s->b->device).lanes[lane];

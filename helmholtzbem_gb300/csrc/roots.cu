@@ -40,6 +40,7 @@ int lane_launch(hbem_solop s, int lane, const double* k_host, int npts, double c
                 const int* oslot, int npool, unsigned d);
 int lane_wait(hbem_solop s, int lane, int block, int* finished);
 int lane_results(hbem_solop s, int lane, double c_o, double c_i, double* out_host);
+int lane_launch_verify(hbem_solop s, int lane, const double* k_host, const int* wslot, int npool);
 int sweep_sigma_warm(hbem_solop s, const double* k_host, int nk, double c_o, double c_i, unsigned d,
                      const int* warm_slot, const int* out_slot, int npool, double* out_host, int keep_uv = 0);
 int sigma1_from_kept(hbem_solop s, const double* k_host, const int* idx, int ne, double c_o, double c_i,
@@ -522,7 +523,7 @@ constexpr int kSpecDeep = 2;
 constexpr int kLanes = 40;
 constexpr int kCandLane = 8;   // the first lane of candidates' evaluations (the grid's below)
 constexpr int kUrgentEnd = 16; // lanes kCandLane .. kUrgentEnd - 1: highest stream priority
-constexpr int kMain = 0, kSpec = 1, kVerify = 2, kGrid = 3, kEnds = 4;
+constexpr int kMain = 0, kSpec = 1, kVerify = 2, kGrid = 3, kEnds = 4, kVerify2 = 5;
 
 // Returns HBEM_ERR_UNSUPPORTED, with nothing left in flight, when the grid cannot be
 // chunked without changing its values or a grid matrix needs the polished kernel:
@@ -594,6 +595,11 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
         return u;
     };
     double out[3 * 64];
+    auto grid_left = [&]() {
+        for (int j = 0; j < nch; ++j)
+            if (busy[j] && fl[j].kind == kGrid) return true;
+        return false;
+    };
     auto finish = [&](int lane) -> int {
         order.erase(std::find(order.begin(), order.end(), lane));
         const Flight F = fl[lane];
@@ -652,19 +658,37 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
             pend[F.cand].erase(std::find(pend[F.cand].begin(), pend[F.cand].end(), F.x));
         } else if (F.kind == kVerify) {
             vd[2 * (size_t)F.cand + F.side] = out[1];
+        } else if (F.kind == kVerify2) {
+            vd[2 * (size_t)F.cand] = out[1];
+            vd[2 * (size_t)F.cand + 1] = out[4];
         } else {
-            nt[F.cand].feed(out[1], out[2]);
+            const size_t c = (size_t)F.cand;
+            nt[c].feed(out[1], out[2]);
             ++evals;
-            in_flight[F.cand] = 0;
+            in_flight[c] = 0;
+            // a root that has just converged: its sign-change check at once, on this lane,
+            // from this point's T, T', T'' (the check points lie within 2 tol of it)
+            if (vder && vsent[c] == 0 && nt[c].done && nt[c].found && nt[c].rts == nt[c].rts) {
+                const double xv[2] = {nt[c].rts - tol, nt[c].rts + tol};
+                const int ws[2] = {cur[c], cur[c]};
+                hbem::svd_pair_hold(grid_left() ? 1 : 0);
+                const int r = hbem::lane_launch_verify(s, lane, xv, ws, npool);
+                if (r == HBEM_OK) {
+                    fl[lane] = Flight{(int)c, nt[c].rts, kVerify2, 0, cur[c]};
+                    busy[lane] = 1;
+                    order.push_back(lane);
+                    vsent[c] = 2;
+                } else if (r != HBEM_ERR_UNSUPPORTED) {
+                    return r;
+                }
+            }
         }
         return HBEM_OK;
     };
     auto launch = [&](int lane, size_t c, double x, int kind, int side, int ws, int os) -> int {
         // one-CTA dense sigma while grid chunks still fill the GPU (a two-CTA cluster
         // would wait for them to drain), the paired form afterwards
-        bool grid_left = false;
-        for (int j = 0; j < nch; ++j) grid_left = grid_left || (busy[j] && fl[j].kind == kGrid);
-        hbem::svd_pair_hold(grid_left ? 1 : 0);
+        hbem::svd_pair_hold(grid_left() ? 1 : 0);
         if (int r = hbem::lane_launch(s, lane, &x, 1, c_o, c_i, &ws, &os, npool, kind == kVerify ? 1u : 2u)) return r;
         fl[lane] = Flight{(int)c, x, kind, side, ws};
         busy[lane] = 1;

@@ -70,4 +70,27 @@ cudaError_t launch_projection(int N, const double* id, const double* sb, const d
     return cudaGetLastError();
 }
 
+// T and T' at x_q = x_src + h[q] (q = 0, 1) from T, T', T'' at x_src (src: three
+// n x n matrices one after another) by their Taylor polynomials,
+//   T(x_q) = T + h T' + h^2/2 T'',  T'(x_q) = T' + h T'',
+// into dst = [q][T, T'].  For |h| of a few times 1e-8 the neglected terms (h^3 T''' / 6,
+// h^2 T''' / 2) are below FP64 rounding of T and T'.
+__global__ void k_taylor_pair(long long mat, const cplx* src, double h0, double h1, cplx* dst) {
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= mat) return;
+    const cplx t0 = src[e], t1 = src[mat + e], t2 = src[2 * mat + e];
+    const double hq[2] = {h0, h1};
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const double h = hq[q];
+        dst[2 * q * mat + e] = t0 + h * (t1 + (0.5 * h) * t2);
+        dst[(2 * q + 1) * mat + e] = t1 + h * t2;
+    }
+}
+
+cudaError_t launch_taylor_pair(long long mat, const cplx* src, double h0, double h1, cplx* dst, cudaStream_t st) {
+    k_taylor_pair<<<(unsigned)((mat + 255) / 256), 256, 0, st>>>(mat, src, h0, h1, dst);
+    return cudaGetLastError();
+}
+
 }  // namespace hbem

@@ -478,8 +478,10 @@ int hbem_find_resonances_plain(hbem_solop s, double k_min, double k_max, int npo
  * sigma' at roots_host[i] - tol and roots_host[i] + tol, so that a root is verified
  * when check_host[2i] <= 0 <= check_host[2i + 1].  With the Newton candidates on
  * their own streams (option "plain_async") a candidate's two points are evaluated as
- * soon as it converges, beside the other candidates' iterations; otherwise in one
- * batch after the search.                                                          */
+ * soon as it converges, beside the other candidates' iterations, with T and T' there
+ * taken from the last Newton point's T, T', T'' by their Taylor polynomials (the
+ * points lie within 2 tol of it, so the terms left out are below FP64 rounding;
+ * no assembly); otherwise the points are assembled, in one batch after the search.  */
 int hbem_find_resonances_plain_verified(hbem_solop s, double k_min, double k_max, int npoints, double c_o, double c_i,
                                         double tol, double* roots_host, int max_roots, int* nroots, double* grid_host,
                                         int* n_evals, double* check_host);

@@ -39,7 +39,8 @@ cudaError_t launch_gather_layers_sub(int N, int d, int layers, const cplx* loc, 
                                      int cols, int sp, cplx* out, cudaStream_t st);
 cudaError_t launch_projection(int N, const double* id, const double* sb, const double* lr, cplx* T, int nmat,
                               cudaStream_t st);
-cudaError_t launch_taylor_pair(long long mat, const cplx* src, double h0, double h1, cplx* dst, cudaStream_t st);
+cudaError_t launch_taylor_near(long long mat, const cplx* src, int nq, double h0, double h1, int d, cplx* dst,
+                               cudaStream_t st);
 cudaError_t launch_svd(int n, int nmat, int D, int which, const cplx* T, long long mat_stride, long long der_stride,
                        cplx* gA, cplx* gV, double* out, double* sig_all, int* status, cudaStream_t st);
 cudaError_t launch_svd_mixed(int n, int nmat, int D, int which, const cplx* T, long long mat_stride,
@@ -440,7 +441,8 @@ struct EvalLane {
     cudaStream_t st = nullptr;
     cudaEvent_t done = nullptr, asm_done = nullptr;   // all work / the assembly part finished
     DBuf jobs, loc, T, out, status, slots;
-    DBuf T2;                   // T, T' at a root's two check points (lane_launch_verify)
+    DBuf T2;                   // matrices from lane_launch_near's Taylor polynomials
+    bool near_cur = false;     // the lane's last point's T, T', T'' are in T2 (else in T)
     double* h_out = nullptr;   // pinned, 3 x kLaneMaxPts
     int* h_status = nullptr;   // pinned, kLaneMaxPts
     int npts = 0, d = 2, mode = 0;   // mode 0: sigma (+ derivatives), 1: grid chunk, 2: bracket ends
@@ -1688,6 +1690,7 @@ int lane_launch(hbem_solop s, int lane, const double* k_host, int npts, double c
     const size_t mat = (size_t)n * n;
     L.npts = npts;
     L.mode = 0;
+    L.near_cur = false;
     std::copy(k_host, k_host + npts, L.k);
     std::vector<int> slots(2 * (size_t)npts);
     std::copy(wslot, wslot + npts, slots.begin());
@@ -1710,42 +1713,58 @@ int lane_launch(hbem_solop s, int lane, const double* k_host, int npts, double c
 
 void singular_split_hold(int on) { t_split_hold = on ? 1 : 0; }
 
-// A root's sign-change check on the lane that has just evaluated the root's last Newton
-// point (one point with T, T', T'' in the lane's buffer): T and T' at the two check
-// points k_host[0..1] from that point's three matrices by their Taylor polynomials
-// (launch_taylor_pair; the check points lie within 1e-6 of it), then sigma' there by the
-// dense kernel with warm slots wslot[0..1], all on the lane's own stream, behind the
-// evaluation.  lane_results then gives sigma' at the two points in out[1], out[4] (a
-// redo assembles them).  HBEM_ERR_UNSUPPORTED when the lane holds no such point: the
-// caller then assembles the check points.
-int lane_launch_verify(hbem_solop s, int lane, const double* k_host, const int* wslot, int npool) {
-    if (!s || lane < 0 || lane >= 64 || !k_host || !wslot) return fail(HBEM_ERR_INVALID, "lane_launch_verify: bad argument");
+// Points near the lane's last one without assembly: the lane has just evaluated one
+// point with T, T', T'' (lane_launch with d = 2, or an earlier call of this one with
+// d = 2); T, T' (and T'' for d = 2) at the npts (1 or 2) points k_host come from that
+// point's three matrices by their Taylor polynomials (launch_taylor_near; each point
+// within 1e-6 of it), then the dense kernel with warm slots wslot / oslot, all on the
+// lane's own stream, behind the evaluation.  Uses: a root's two sign-change check
+// points (d = 1) and a Newton step of at most 1e-6 (d = 2).  lane_results then gives
+// the values as for lane_launch (a redo assembles the points).  HBEM_ERR_UNSUPPORTED
+// when the lane holds no such point: the caller then assembles.
+int lane_launch_near(hbem_solop s, int lane, const double* k_host, int npts, unsigned d, const int* wslot,
+                     const int* oslot, int npool) {
+    if (!s || lane < 0 || lane >= 64 || !k_host || !wslot || !oslot || npts < 1 || npts > 2 || d < 1 || d > 2)
+        return fail(HBEM_ERR_INVALID, "lane_launch_near: bad argument");
     hbem_builder b = s->b;
     std::vector<EvalLane*>& lanes = lane_pool(b->device).lanes;
-    if (lane >= (int)lanes.size()) return fail(HBEM_ERR_INVALID, "lane_launch_verify: no such lane");
+    if (lane >= (int)lanes.size()) return fail(HBEM_ERR_INVALID, "lane_launch_near: no such lane");
     EvalLane& L = *lanes[lane];
     if (L.mode != 0 || L.d != 2 || L.npts != 1) return HBEM_ERR_UNSUPPORTED;
-    const double x = L.k[0], h0 = k_host[0] - x, h1 = k_host[1] - x;
-    if (!(std::fabs(h0) <= 1e-6 && std::fabs(h1) <= 1e-6)) return HBEM_ERR_UNSUPPORTED;
-    for (int q = 0; q < 2; ++q)
-        if (wslot[q] >= npool) return fail(HBEM_ERR_INVALID, "lane_launch_verify: slot outside the pool");
+    const double x = L.k[0];
+    double h[2] = {0., 0.};
+    for (int q = 0; q < npts; ++q) {
+        h[q] = k_host[q] - x;
+        if (!(std::fabs(h[q]) <= 1e-6)) return HBEM_ERR_UNSUPPORTED;
+        if (wslot[q] >= npool || oslot[q] >= npool) return fail(HBEM_ERR_INVALID, "lane_launch_near: slot outside the pool");
+    }
     HB_CK(cudaSetDevice(b->device));
     const int n = 2 * b->n;
     const size_t mat = (size_t)n * n;
-    L.npts = 2;
-    L.d = 1;
-    L.k[0] = k_host[0];
-    L.k[1] = k_host[1];
-    std::vector<int> slots = {wslot[0], wslot[1], -1, -1};
+    // the source point's matrices stay where they are; the new ones go to the other buffer
+    DBuf& src = L.near_cur ? L.T2 : L.T;
+    DBuf& dst = L.near_cur ? L.T : L.T2;
+    if (dst.cap < (size_t)npts * (d + 1) * mat * sizeof(cplx)) {
+        // growing a buffer drops its contents: only the destination may grow
+        HB_CK(dst.ensure((size_t)npts * (d + 1) * mat * sizeof(cplx)));
+    }
+    L.npts = npts;
+    L.d = (int)d;
+    std::vector<int> slots(2 * (size_t)npts);
+    for (int q = 0; q < npts; ++q) {
+        L.k[q] = k_host[q];
+        slots[q] = wslot[q];
+        slots[npts + q] = oslot[q];
+    }
     HB_CK(upload(L.slots, slots, L.st));
-    HB_CK(L.T2.ensure(4 * mat * sizeof(cplx)));
-    HB_CK(launch_taylor_pair((long long)mat, L.T.as<cplx>(), h0, h1, L.T2.as<cplx>(), L.st));
-    HB_CK(launch_svd_fast(n, 2, 1, L.T2.as<cplx>(), 2LL * (long long)mat, (long long)mat, L.out.as<double>(),
-                          L.status.as<int>(), L.st, s->d_vpool.as<cplxf>(), L.slots.as<int>(), L.slots.as<int>() + 2,
-                          nullptr));
+    HB_CK(launch_taylor_near((long long)mat, src.as<cplx>(), npts, h[0], h[1], (int)d, dst.as<cplx>(), L.st));
+    HB_CK(launch_svd_fast(n, npts, (int)d, dst.as<cplx>(), (long long)(d + 1) * (long long)mat, (long long)mat,
+                          L.out.as<double>(), L.status.as<int>(), L.st, s->d_vpool.as<cplxf>(), L.slots.as<int>(),
+                          L.slots.as<int>() + npts, nullptr));
+    L.near_cur = !L.near_cur;
     g_launches += 2;
-    HB_CK(cudaMemcpyAsync(L.h_out, L.out.p, 6 * sizeof(double), cudaMemcpyDeviceToHost, L.st));
-    HB_CK(cudaMemcpyAsync(L.h_status, L.status.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, L.st));
+    HB_CK(cudaMemcpyAsync(L.h_out, L.out.p, 3 * (size_t)npts * sizeof(double), cudaMemcpyDeviceToHost, L.st));
+    HB_CK(cudaMemcpyAsync(L.h_status, L.status.p, (size_t)npts * sizeof(int), cudaMemcpyDeviceToHost, L.st));
     HB_CK(cudaEventRecord(L.done, L.st));
     return HBEM_OK;
 }

@@ -40,7 +40,8 @@ int lane_launch(hbem_solop s, int lane, const double* k_host, int npts, double c
                 const int* oslot, int npool, unsigned d);
 int lane_wait(hbem_solop s, int lane, int block, int* finished);
 int lane_results(hbem_solop s, int lane, double c_o, double c_i, double* out_host);
-int lane_launch_verify(hbem_solop s, int lane, const double* k_host, const int* wslot, int npool);
+int lane_launch_near(hbem_solop s, int lane, const double* k_host, int npts, unsigned d, const int* wslot,
+                     const int* oslot, int npool);
 int sweep_sigma_warm(hbem_solop s, const double* k_host, int nk, double c_o, double c_i, unsigned d,
                      const int* warm_slot, const int* out_slot, int npool, double* out_host, int keep_uv = 0);
 int sigma1_from_kept(hbem_solop s, const double* k_host, const int* idx, int ne, double c_o, double c_i,
@@ -561,6 +562,11 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
     // candidates (grid index, state 0: bracket ends to launch, 1: ends in flight,
     // 2: rejected, 3: Newton)
     std::vector<int> cgrid, cstate, cur, in_flight, vsent;
+    // the lane of each candidate's last Newton point, that lane's launch count then and
+    // the point: while the lane has had no launch since, it still holds T, T', T''
+    std::vector<int> last_lane, last_gen;
+    std::vector<double> last_x;
+    std::vector<long long> lane_gen(kLanes, 0);
     std::vector<std::vector<std::array<double, 3>>> cache;
     std::vector<std::vector<double>> pend;
     nt.clear();
@@ -579,13 +585,24 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
     // chunks on lanes 0 .. nch - 1): a free lane of the highest priority for a candidate
     // deep into its Newton run (the runs with bisection steps, the longest, set the
     // search's end), else one of the next
+    // busy[l]: 0 free, 1 in flight, 2 held for candidate fl[l].cand (the lane keeps that
+    // candidate's last Newton point's T, T', T'' for its next step, lane_launch_near)
     auto free_lane = [&](bool urgent = false) {
         const int first = urgent ? kCandLane : kUrgentEnd, nl = kLanes - kCandLane;
         for (int q = 0; q < nl; ++q) {
             const int l = kCandLane + (first - kCandLane + q) % nl;
             if (!busy[l]) return l;
         }
+        for (int l = kCandLane; l < kLanes; ++l)   // none free: give up a held lane
+            if (busy[l] == 2) {
+                busy[l] = 0;
+                return l;
+            }
         return -1;
+    };
+    auto release = [&](size_t c) {
+        const int ll = last_lane[c];
+        if (ll >= 0 && busy[ll] == 2 && fl[ll].cand == (int)c) busy[ll] = 0;
     };
     auto urgent = [&](size_t c) { return cstate[c] == 3 && nt[c].it >= 3; };
     auto unfinished = [&]() {
@@ -622,6 +639,9 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
                     cgrid.push_back(i);
                     cstate.push_back(0);
                     cur.push_back(-1);
+                    last_lane.push_back(-1);
+                    last_gen.push_back(0);
+                    last_x.push_back(NAN);
                     in_flight.push_back(0);
                     vsent.push_back(0);
                     cache.emplace_back();
@@ -666,15 +686,19 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
             nt[c].feed(out[1], out[2]);
             ++evals;
             in_flight[c] = 0;
+            last_lane[c] = lane;
+            last_gen[c] = (int)lane_gen[lane];
+            last_x[c] = F.x;
             // a root that has just converged: its sign-change check at once, on this lane,
             // from this point's T, T', T'' (the check points lie within 2 tol of it)
             if (vder && vsent[c] == 0 && nt[c].done && nt[c].found && nt[c].rts == nt[c].rts) {
                 const double xv[2] = {nt[c].rts - tol, nt[c].rts + tol};
-                const int ws[2] = {cur[c], cur[c]};
+                const int ws[2] = {cur[c], cur[c]}, os[2] = {-1, -1};
                 hbem::svd_pair_hold(grid_left() ? 1 : 0);
-                const int r = hbem::lane_launch_verify(s, lane, xv, ws, npool);
+                const int r = hbem::lane_launch_near(s, lane, xv, 2, 1u, ws, os, npool);
                 if (r == HBEM_OK) {
                     fl[lane] = Flight{(int)c, nt[c].rts, kVerify2, 0, cur[c]};
+                    ++lane_gen[lane];
                     busy[lane] = 1;
                     order.push_back(lane);
                     vsent[c] = 2;
@@ -682,6 +706,8 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
                     return r;
                 }
             }
+            // a Newton step of at most 1e-6 next: keep this lane's matrices for it
+            if (!busy[lane] && !nt[c].done && std::fabs(nt[c].dx) <= 1e-6) busy[lane] = 2;
         }
         return HBEM_OK;
     };
@@ -691,6 +717,7 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
         hbem::svd_pair_hold(grid_left() ? 1 : 0);
         if (int r = hbem::lane_launch(s, lane, &x, 1, c_o, c_i, &ws, &os, npool, kind == kVerify ? 1u : 2u)) return r;
         fl[lane] = Flight{(int)c, x, kind, side, ws};
+        ++lane_gen[lane];
         busy[lane] = 1;
         order.push_back(lane);
         return HBEM_OK;
@@ -708,6 +735,7 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
                 const int gi[2] = {i, i + 2};
                 if (int r = hbem::lane_launch_ends(s, lane, e2, gi, c_o, c_i)) return r;
                 fl[lane] = Flight{(int)c, 0., kEnds, 0, -1};
+                ++lane_gen[lane];
                 busy[lane] = 1;
                 order.push_back(lane);
                 cstate[c] = 1;
@@ -723,6 +751,7 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
                 ++evals;
             }
             if (nt[c].done) {
+                release(c);
                 // a converged candidate: its root's sign-change check beside the others' work
                 if (vder && vsent[c] < 2 && nt[c].found && nt[c].rts == nt[c].rts) {
                     const int l = free_lane(urgent(c));
@@ -734,7 +763,10 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
                 }
                 return 0;
             }
-            if (has(pend[c], nt[c].rts)) return 0;   // its point is on its way
+            if (has(pend[c], nt[c].rts)) {   // its point is on its way
+                release(c);
+                return 0;
+            }
             const int own0 = npoints + 2 * (int)c, wslot = cur[c], oslot = cur[c] == own0 ? own0 + 1 : own0;
             // the slot this point's V set goes to must not be read by a speculative point
             // still in flight (it started from the slot before)
@@ -750,9 +782,31 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
                 }
             }
             if (waited) continue;   // look again: the wait may have brought this point's value
-            const int lane = free_lane(urgent(c));
-            if (lane < 0) return -1;
-            if (int r = launch(lane, c, nt[c].rts, kMain, 0, wslot, oslot)) return r;
+            // a Newton step of at most 1e-6 from the point just evaluated: that point's T,
+            // T', T'' by their Taylor polynomials on the lane that holds them (no assembly)
+            int lane = -1;
+            const int ll = last_lane[c];
+            const bool held = ll >= 0 && busy[ll] == 2 && fl[ll].cand == (int)c;
+            release(c);
+            if (held && lane_gen[ll] == last_gen[c] && std::fabs(nt[c].rts - last_x[c]) <= 1e-6) {
+                const double x = nt[c].rts;
+                hbem::svd_pair_hold(grid_left() ? 1 : 0);
+                const int r = hbem::lane_launch_near(s, ll, &x, 1, 2u, &wslot, &oslot, npool);
+                if (r == HBEM_OK) {
+                    fl[ll] = Flight{(int)c, x, kMain, 0, wslot};
+                    ++lane_gen[ll];
+                    busy[ll] = 1;
+                    order.push_back(ll);
+                    lane = ll;
+                } else if (r != HBEM_ERR_UNSUPPORTED) {
+                    return r;
+                }
+            }
+            if (lane < 0) {
+                lane = free_lane(urgent(c));
+                if (lane < 0) return -1;
+                if (int r = launch(lane, c, nt[c].rts, kMain, 0, wslot, oslot)) return r;
+            }
             in_flight[c] = 1;
             cur[c] = oslot;
             // speculative bisection points (plus the next level when few candidates are left)
@@ -801,6 +855,7 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
             return r;
         }
         fl[j] = Flight{j, 0., kGrid, 0, -1};
+        ++lane_gen[j];
         busy[j] = 1;
         order.push_back(j);
     }

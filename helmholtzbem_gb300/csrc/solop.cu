@@ -70,26 +70,30 @@ cudaError_t launch_projection(int N, const double* id, const double* sb, const d
     return cudaGetLastError();
 }
 
-// T and T' at x_q = x_src + h[q] (q = 0, 1) from T, T', T'' at x_src (src: three
-// n x n matrices one after another) by their Taylor polynomials,
-//   T(x_q) = T + h T' + h^2/2 T'',  T'(x_q) = T' + h T'',
-// into dst = [q][T, T'].  For |h| of a few times 1e-8 the neglected terms (h^3 T''' / 6,
-// h^2 T''' / 2) are below FP64 rounding of T and T'.
-__global__ void k_taylor_pair(long long mat, const cplx* src, double h0, double h1, cplx* dst) {
+// T, T' (and T'' when d = 2) at x_q = x_src + h_q (q < nq <= 2) from T, T', T'' at
+// x_src (src: three n x n matrices one after another) by their Taylor polynomials,
+//   T(x_q) = T + h T' + h^2/2 T'',  T'(x_q) = T' + h T'',  T''(x_q) = T'',
+// into dst = [q][0 .. d].  The terms left out are h^3/6 T''', h^2/2 T''' and h T''':
+// for |h| <= 1e-6 (T''' of the order of (sqrt(c) r)^2 T' for panel distances r) they
+// are below 1e-11 of T' and T, and T'' (which only sets a Newton step's length) is
+// good to ~1e-5.
+__global__ void k_taylor_near(long long mat, const cplx* src, int nq, double h0, double h1, int d, cplx* dst) {
     const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (e >= mat) return;
     const cplx t0 = src[e], t1 = src[mat + e], t2 = src[2 * mat + e];
-    const double hq[2] = {h0, h1};
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        const double h = hq[q];
-        dst[2 * q * mat + e] = t0 + h * (t1 + (0.5 * h) * t2);
-        dst[(2 * q + 1) * mat + e] = t1 + h * t2;
+    for (int q = 0; q < nq; ++q) {
+        const double h = q ? h1 : h0;
+        cplx* o = dst + (long long)q * (d + 1) * mat;
+        o[e] = t0 + h * (t1 + (0.5 * h) * t2);
+        o[mat + e] = t1 + h * t2;
+        if (d == 2) o[2 * mat + e] = t2;
     }
 }
 
-cudaError_t launch_taylor_pair(long long mat, const cplx* src, double h0, double h1, cplx* dst, cudaStream_t st) {
-    k_taylor_pair<<<(unsigned)((mat + 255) / 256), 256, 0, st>>>(mat, src, h0, h1, dst);
+cudaError_t launch_taylor_near(long long mat, const cplx* src, int nq, double h0, double h1, int d, cplx* dst,
+                               cudaStream_t st) {
+    if (nq < 1 || nq > 2 || d < 1 || d > 2) return cudaErrorInvalidValue;
+    k_taylor_near<<<(unsigned)((mat + 255) / 256), 256, 0, st>>>(mat, src, nq, h0, h1, d, dst);
     return cudaGetLastError();
 }
 

@@ -12,7 +12,6 @@
 #include <algorithm>
 #include <array>
 #include <cstdint>
-#include <cstdlib>
 #include <functional>
 #include <cmath>
 #include <limits>
@@ -504,16 +503,20 @@ int newton_rounds(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i,
 
 // The plain search as one pipeline on several streams ("lanes"): the grid in chunks
 // whose assemblies run one after another (from the top of the range down) while each
-// chunk's dense sigma overlaps the next chunk's assembly; a candidate's bracket ends (sigma' from the grid's kept singular
-// vectors) as soon as the grid around it is known; its Newton steps as soon as its
-// previous point is evaluated, one point per lane; and, when asked for, its root's
-// sign-change check as soon as it converges.  The FP64 assembly of one candidate runs
-// while another's one-CTA dense sigma does, and the grid's tail overlaps the first
-// candidates' work.  Values are those of the lock-step search: the same grid
-// (chunks of at least the size below, so that their general pairs take the same
-// layout as one batch), the same bracket ends, and the same Newton and bisection
-// steps with the same warm-start slots for the Newton points.  Grid chunks run on
-// low-priority streams, candidates' evaluations on high-priority ones, and the host
+// chunk's dense sigma overlaps the next chunk's assembly; a candidate's bracket ends
+// (sigma' from the grid's kept singular vectors) as soon as the grid around it is
+// known; its Newton steps as soon as its previous point is evaluated, one point per
+// lane; and, when asked for, its root's sign-change check as soon as it converges.
+// The FP64 assembly of one candidate runs while another's dense sigma does, and the
+// grid's tail overlaps the first candidates' work.  Values are those of the lock-step
+// search -- the same grid (chunks of at least the size below, so that their general
+// pairs take the same layout as one batch), the same bracket ends, and the same Newton
+// and bisection steps with the same warm-start slots for the Newton points -- except
+// for points within 1e-6 of the point a candidate has just evaluated (a Newton step
+// that small, the root's two check points): they take that point's T, T', T'' by
+// Taylor polynomials (lane_launch_near), so their sigma' agrees with an assembled
+// one to ~1e-11 rather than bit for bit.  Grid chunks run on the lowest-priority
+// streams, candidates' evaluations above them (the long runs highest), and the host
 // polls every lane so that each result is taken as soon as it is there.  Speculative
 // bisection points run on lanes of their own once the grid is complete and at most
 // "plain_spec_async" candidates (option, default 2) are unfinished
@@ -564,7 +567,8 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
     std::vector<int> cgrid, cstate, cur, in_flight, vsent;
     // the lane of each candidate's last Newton point, that lane's launch count then and
     // the point: while the lane has had no launch since, it still holds T, T', T''
-    std::vector<int> last_lane, last_gen;
+    std::vector<int> last_lane;
+    std::vector<long long> last_gen;
     std::vector<double> last_x;
     std::vector<long long> lane_gen(kLanes, 0);
     std::vector<std::vector<std::array<double, 3>>> cache;
@@ -687,7 +691,7 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
             ++evals;
             in_flight[c] = 0;
             last_lane[c] = lane;
-            last_gen[c] = (int)lane_gen[lane];
+            last_gen[c] = lane_gen[lane];
             last_x[c] = F.x;
             // a root that has just converged: its sign-change check at once, on this lane,
             // from this point's T, T', T'' (the check points lie within 2 tol of it)

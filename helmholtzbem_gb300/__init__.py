@@ -6,7 +6,7 @@ direct::sv / find_roots interface in ``helmholtzbem_gb300.api``.
 """
 import os
 
-# Up to ~40 streams run at once in the plain search; with CUDA's default of 8 hardware
+# Up to 24 streams run at once in the plain search; with CUDA's default of 8 hardware
 # work queues, launches of one stream wait behind unrelated launches of another that
 # shares its queue.  The setting only takes effect if no CUDA context exists yet
 # (import this package before anything initialises CUDA); a value already set wins.

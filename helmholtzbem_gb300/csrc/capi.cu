@@ -497,7 +497,7 @@ struct hbem_solop_s {
     }
 };
 
-// The plain search keeps up to ~40 streams busy at once.  With CUDA's default of 8
+// The plain search keeps up to 24 streams busy at once.  With CUDA's default of 8
 // hardware work queues per device, streams share queues and a stream's launches wait
 // behind another stream's (a grid chunk's event wait, a long kernel) that they do not
 // depend on.  At load time, before a CUDA context exists, ask for the maximum of 32

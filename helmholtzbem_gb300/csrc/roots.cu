@@ -524,7 +524,10 @@ int newton_rounds(hbem_solop s, std::vector<Newton>& nt, double c_o, double c_i,
 // another warm start than in lock step, so its values agree to the dense kernel's
 // accuracy (sigma' and sigma'' to ~1e-12 relative), not bit for bit.
 constexpr int kSpecDeep = 2;
-constexpr int kLanes = 40;
+// lanes (streams) of the search: with the builder's and the runtime's own streams they
+// stay within the 32 hardware work queues, so that no two lanes share one (a lane's
+// launch that waits for its own stream's previous one would hold up the other's)
+constexpr int kLanes = 24;
 constexpr int kCandLane = 8;   // the first lane of candidates' evaluations (the grid's below)
 constexpr int kUrgentEnd = 16; // lanes kCandLane .. kUrgentEnd - 1: highest stream priority
 constexpr int kMain = 0, kSpec = 1, kVerify = 2, kGrid = 3, kEnds = 4, kVerify2 = 5;

@@ -37,3 +37,21 @@ def test_fixture_grid_and_roots_are_the_oracles():
     mins = [i for i in range(sig.size - 2) if sig[i] > sig[i + 1] < sig[i + 2]]
     for r in gold["roots"]:
         assert any(cfg["k_min"] + i * h <= r <= cfg["k_min"] + (i + 2) * h for i in mins)
+
+
+def test_polygon_fixture_grid_and_roots_are_the_oracles():
+    with open(os.path.join(HERE, "golden", "plain_search_star12_N48.json")) as f:
+        gold = json.load(f)
+    cfg = gold["config"]
+    kinds = np.array(gold["panel_kinds"], dtype=np.int32)
+    par = np.array(gold["panel_params"], dtype=np.float64).reshape(len(kinds), -1)
+    oso = O.SolutionsOperator(O.Builder(kinds, par, cfg["order"]))
+    h = (cfg["k_max"] - cfg["k_min"]) / (cfg["npoints"] - 1)
+    for i in (0, 101, 199):
+        s = O.sv_derivs(oso.gen_sol_op(cfg["k_min"] + i * h, cfg["c_o"], cfg["c_i"])[0])[0]
+        assert abs(s - gold["grid_sigma"][i]) <= 1e-11 * s
+    assert len(gold["roots"]) == 33 and all(gold["verified"])
+    r = gold["roots"][17]
+    lo = O.sv_derivs(*oso.gen_sol_op(r - cfg["tol"], cfg["c_o"], cfg["c_i"], d=1))[1]
+    hi = O.sv_derivs(*oso.gen_sol_op(r + cfg["tol"], cfg["c_o"], cfg["c_i"], d=1))[1]
+    assert lo <= 0.0 <= hi

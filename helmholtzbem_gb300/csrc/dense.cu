@@ -439,8 +439,8 @@ cudaError_t launch_svd_mixed(int n, int nmat, int D, int which, const cplx* T, l
 // sigma_min, sigma', sigma'' of one matrix per CTA with O(n^3) work only in FP32
 // (the Jacobi sweeps) and in one FP64 LU; everything else in FP64 is O(n^2 k):
 //  1. FP32 one-sided Jacobi: all singular triplets to the FP32 noise level.
-//  2. The near block: the right vectors of the k = min(n, 12) smallest FP32 singular
-//     values.  FP64 LU of T in shared memory; four block inverse iterations
+//  2. The near block: the right vectors of the k = min(n, 8) smallest FP32 singular
+//     values.  FP64 LU of T in shared memory; one to four block inverse iterations
 //     X <- qr(T^-1 T^-H X); Rayleigh-Ritz: T X = Q_Y R, SVD of the k x k factor R
 //     gives FP64 Ritz triplets (sigma_j, u_j, v_j).
 //  3. sigma = smallest Ritz value, sigma' = Re u^H T' v.
@@ -454,7 +454,12 @@ cudaError_t launch_svd_mixed(int n, int nmat, int D, int which, const cplx* T, l
 // A CG that does not converge sets status 4 and a singular LU status 5; the host
 // then recomputes the batch with the FP64-polished Jacobi kernel.
 
-constexpr int kFastKmax = 12;
+// Near-block width: 8 holds the target with a few degenerate pairs (the circle's
+// sigma come in pairs) and needs as many inverse iterations as 12 near the minima
+// the searches evaluate, at two thirds of the FP64 solve and Rayleigh-Ritz work
+// (measured: 142.8 -> 138.0 ms per bench step; 139.7 ms with 10).  At least 8: the
+// block's storage doubles as the Jacobi warm start's row buffer (16 warps x n).
+constexpr int kFastKmax = 8;
 constexpr int kFastInvIter = 4;
 constexpr int kFastNeumannMax = 200;   // preconditioned CG iteration cap
 // launches of at most this many matrices run the paired (two-CTA cluster) form

@@ -600,11 +600,15 @@ int plain_pipelined(hbem_solop s, const std::vector<double>& ks, double h, doubl
             const int l = kCandLane + (first - kCandLane + q) % nl;
             if (!busy[l]) return l;
         }
-        for (int l = kCandLane; l < kLanes; ++l)   // none free: give up a held lane
-            if (busy[l] == 2) {
-                busy[l] = 0;
-                return l;
-            }
+        // none free: wait for a lane in flight; with none in flight, give up a held lane
+        // (only then, so that while lanes suffice the Taylor steps, and with them the
+        // values, do not depend on timing)
+        if (order.empty())
+            for (int l = kCandLane; l < kLanes; ++l)
+                if (busy[l] == 2) {
+                    busy[l] = 0;
+                    return l;
+                }
         return -1;
     };
     auto release = [&](size_t c) {

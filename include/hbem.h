@@ -459,7 +459,10 @@ int hbem_sweep_sigma(hbem_solop s, const double* k_host, int nk, double c_o, dou
  * dense sigma overlaps the next chunk's assembly, each candidate's bracket ends as
  * soon as the grid around it is known, and its Newton points one after another,
  * independently of the other candidates; otherwise each phase is one batch, the
- * Newton steps of all candidates in one batch per round.  The values are the same.
+ * Newton steps of all candidates in one batch per round.  The values are the same,
+ * except that in the pipeline a Newton step of at most 1e-6 takes T, T', T'' from the
+ * point just evaluated by their Taylor polynomials instead of assembling them (sigma'
+ * there agrees with the assembled value to ~1e-11, the roots to ~1e-12).
  * roots_host receives up to max_roots roots, *nroots their count; grid_host
  * (npoints x 3, may be NULL) sigma at every grid point and sigma' at the bracket
  * ends (NaN where not evaluated); *n_evals the number of T(k) evaluated.

@@ -131,7 +131,8 @@ def test_every_documented_option_is_accepted():
     src = open(os.path.join(ROOT, "include", "hbem.h")).read()
     block = src[src.index("Process-wide switches"):src.index("int hbem_set_option")]
     documented = re.findall(r'"(\w+)" \(default (\d+)', block)
-    assert {"svd_fast", "singular_table", "plain_speculate", "plain_warm_start"} <= {n for n, _ in documented}
+    assert {"svd_fast", "singular_table", "plain_speculate", "plain_warm_start", "svd_pair_max",
+            "singular_split", "plain_async"} <= {n for n, _ in documented}
     import ctypes
     v = ctypes.c_int(-1)
     for name, default in documented:
